@@ -1,0 +1,138 @@
+/*
+ * quadblas_gpu.h — C ABI of libquadblas_gpu.so, a GB300 (sm_103a) GPU
+ * implementation of QuadBLAS's IEEE binary128 BLAS hot path.
+ *
+ * Binary128 arguments are `void *` pointers to 16-byte IEEE binary128
+ * values (Sleef_quad, __float128, AArch64 long double), little-endian,
+ * 16-byte aligned for the device-pointer entry points.
+ *
+ * Part 1 keeps the reference's C interface signatures
+ * (include/quadblas/interface/c_interface.hpp of QuadBLAS 1.0.0) so that
+ * existing callers link unchanged.  Part 2 adds binary128 scalars/results,
+ * 64-bit sizes and status returns; part 3 adds device-pointer entry points
+ * ordered on a caller-given CUDA stream.
+ *
+ * Semantics shared by all entry points:
+ *  - dot, gemv and gemm sums are the exact sum of the exact products,
+ *    rounded to binary128 once (round to nearest, ties to even) — except
+ *    in the rare case where the exact sum is within about
+ *    n * 2^-190 * max|a_i b_i| of a rounding boundary, or where the
+ *    Ozaki method is selected for qgemm (then the accuracy is set by the
+ *    slice count).  The reference instead
+ *    rounds after every FMA; both are within k * 2^-113 * sum|a_i b_i|
+ *    of each other.
+ *  - gemv/gemm then apply the reference epilogue y = fma(alpha, sum, beta*y)
+ *    with one rounding, bit-identical to SLEEF's Sleef_fmaq1_u05.
+ *  - axpy is y_i = fma(alpha, x_i, y_i), bit-identical to the reference.
+ *  - Increments must be positive.  Column-major ('C'/'c') and transposed
+ *    ('T','t','C','c') operands are supported by qgemv (as in the
+ *    reference) and by qgemm (the reference ignores transa/transb and
+ *    mis-indexes column-major C above 64; this library implements the
+ *    intended semantics of the reference's test loops).
+ *  - Status codes are the QBLAS_* values below.
+ */
+#ifndef QUADBLAS_GPU_H
+#define QUADBLAS_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  QBLAS_OK = 0,
+  QBLAS_ERR_INVALID_VALUE = 1,
+  QBLAS_ERR_CUDA = 2,
+  QBLAS_ERR_NO_MEMORY = 3,
+  QBLAS_ERR_NOT_SUPPORTED = 4,
+  QBLAS_ERR_NO_DEVICE = 5,
+  QBLAS_ERR_MISALIGNED = 6
+};
+
+enum { QBLAS_METHOD_AUTO = 0, QBLAS_METHOD_SOFTFLOAT = 1, QBLAS_METHOD_OZAKI = 2 };
+
+/* ---- Part 1: reference-compatible entry points (host pointers) --------- */
+
+/* Replaces quadblas_qdot, c_interface.hpp:21.  Returns the binary128 dot
+ * rounded to double (as the reference does). */
+double quadblas_qdot(int n, void *x, int incx, void *y, int incy);
+
+/* Replaces quadblas_qnrm2, c_interface.hpp:34: sqrt(dot(x, x)). */
+double quadblas_qnrm2(int n, void *x, int incx);
+
+/* Replaces quadblas_qaxpy, c_interface.hpp:47: y = alpha*x + y. */
+void quadblas_qaxpy(int n, double alpha, void *x, int incx, void *y, int incy);
+
+/* Replaces quadblas_qgemv, c_interface.hpp:64: y = alpha*op(A)*x + beta*y;
+ * layout 'C'/'c' = column-major, else row-major; trans in T/t/C/c swaps
+ * m and n and flips the layout (c_interface.hpp:79-85). */
+void quadblas_qgemv(char layout, char trans, int m, int n, double alpha, void *A, int lda,
+                    void *x, int incx, double beta, void *y, int incy);
+
+/* Replaces quadblas_qgemm, c_interface.hpp:95: C = alpha*op(A)*op(B) + beta*C. */
+void quadblas_qgemm(char layout, char transa, char transb, int m, int n, int k, double alpha,
+                    void *A, int lda, void *B, int ldb, double beta, void *C, int ldc);
+
+/* Replaces quadblas_set_num_threads / get_num_threads, c_interface.hpp:122,128.
+ * Kept for ABI compatibility: the value is recorded and reported, the GPU
+ * path has no host thread pool. */
+void quadblas_set_num_threads(int num_threads);
+int quadblas_get_num_threads(void);
+
+/* Replaces quadblas_get_version, c_interface.hpp:134. */
+const char *quadblas_get_version(void);
+
+/* Replaces quadblas_is_aligned, c_interface.hpp:140 (32-byte test). */
+int quadblas_is_aligned(const void *ptr);
+
+/* ---- Part 2: binary128 scalars and results, host pointers ------------- */
+/* Same operations as part 1 (QuadBLAS::dot/axpy/gemv/gemm,
+ * algorithms/level1.hpp:80,190, level2.hpp:85, level3.hpp:215, which the
+ * C++ classes of interface/cpp_classes.hpp:66-153 call with binary128
+ * scalars); alpha, beta and result point to binary128 values. */
+int quadblas_qdot_q(int64_t n, const void *x, int64_t incx, const void *y, int64_t incy,
+                    void *result);
+int quadblas_qnrm2_q(int64_t n, const void *x, int64_t incx, void *result);
+int quadblas_qaxpy_q(int64_t n, const void *alpha, const void *x, int64_t incx, void *y,
+                     int64_t incy);
+int quadblas_qgemv_q(char layout, char trans, int64_t m, int64_t n, const void *alpha,
+                     const void *A, int64_t lda, const void *x, int64_t incx, const void *beta,
+                     void *y, int64_t incy);
+int quadblas_qgemm_q(char layout, char transa, char transb, int64_t m, int64_t n, int64_t k,
+                     const void *alpha, const void *A, int64_t lda, const void *B, int64_t ldb,
+                     const void *beta, void *C, int64_t ldc);
+
+/* ---- Part 3: device pointers, ordered on `stream` (a cudaStream_t; NULL
+ * is the legacy default stream).  alpha/beta are HOST pointers to
+ * binary128 values; d_result is a device pointer.  The calls return after
+ * enqueueing the work.  Same operations as part 2; no reference
+ * counterpart (the reference is CPU-only). */
+int quadblas_qdot_dev(int64_t n, const void *dx, int64_t incx, const void *dy, int64_t incy,
+                      void *d_result, void *stream);
+int quadblas_qnrm2_dev(int64_t n, const void *dx, int64_t incx, void *d_result, void *stream);
+int quadblas_qaxpy_dev(int64_t n, const void *alpha, const void *dx, int64_t incx, void *dy,
+                       int64_t incy, void *stream);
+int quadblas_qgemv_dev(char layout, char trans, int64_t m, int64_t n, const void *alpha,
+                       const void *dA, int64_t lda, const void *dx, int64_t incx,
+                       const void *beta, void *dy, int64_t incy, void *stream);
+int quadblas_qgemm_dev(char layout, char transa, char transb, int64_t m, int64_t n, int64_t k,
+                       const void *alpha, const void *dA, int64_t lda, const void *dB,
+                       int64_t ldb, const void *beta, void *dC, int64_t ldc, void *stream);
+
+/* ---- Configuration and errors (no reference counterpart) -------------- */
+/* qgemm method: QBLAS_METHOD_AUTO, _SOFTFLOAT or _OZAKI. */
+int quadblas_set_method(int method);
+int quadblas_get_method(void);
+/* Ozaki slice count (0 = automatic, else 2..32). */
+int quadblas_set_ozaki_slices(int slices);
+int quadblas_get_ozaki_slices(void);
+/* Status of the calling thread's last call (part 1 calls record it too). */
+int quadblas_last_error(void);
+const char *quadblas_error_string(int code);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* QUADBLAS_GPU_H */

@@ -1,0 +1,137 @@
+"""Python front end of the C ABI, mirroring the reference's C interface
+(include/quadblas/interface/c_interface.hpp) argument for argument.
+
+Host functions take numpy ``(n, 2)`` uint64 binary128 arrays (see
+``quad.py``) and update outputs in place, like the C calls.  Device
+functions take CUDA tensors whose storage holds binary128 values (any
+dtype; 16 bytes per element, e.g. int64 of shape (n, 2)) and an optional
+CUDA stream (defaults to torch's current stream)."""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import quad
+from ._lib import check, load
+
+
+def _p(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _q1(v) -> np.ndarray:
+    if isinstance(v, (float, int)):
+        return quad.scalar(float(v))
+    return quad.as_quad(v)
+
+
+def _c(ch: str) -> bytes:
+    return ch.encode()[:1]
+
+
+# ---- reference-compatible (double scalars, host pointers) ---------------
+def qdot(n, x, incx, y, incy) -> float:
+    return load().quadblas_qdot(n, _p(x), incx, _p(y), incy)
+
+
+def qnrm2(n, x, incx) -> float:
+    return load().quadblas_qnrm2(n, _p(x), incx)
+
+
+def qaxpy(n, alpha: float, x, incx, y, incy) -> None:
+    load().quadblas_qaxpy(n, alpha, _p(x), incx, _p(y), incy)
+
+
+def qgemv(layout, trans, m, n, alpha: float, A, lda, x, incx, beta: float, y, incy) -> None:
+    load().quadblas_qgemv(_c(layout), _c(trans), m, n, alpha, _p(A), lda, _p(x), incx, beta, _p(y), incy)
+
+
+def qgemm(layout, transa, transb, m, n, k, alpha: float, A, lda, B, ldb, beta: float, C, ldc) -> None:
+    load().quadblas_qgemm(_c(layout), _c(transa), _c(transb), m, n, k, alpha, _p(A), lda, _p(B), ldb,
+                          beta, _p(C), ldc)
+
+
+# ---- binary128 results and scalars (host pointers) ----------------------
+def dot(x, y, n=None, incx=1, incy=1) -> np.ndarray:
+    x, y = quad.as_quad(x), quad.as_quad(y)
+    if n is None:
+        n = len(x) // incx
+    out = quad.empty(1)
+    check(load().quadblas_qdot_q(n, _p(x), incx, _p(y), incy, _p(out)))
+    return out
+
+
+def nrm2(x, n=None, incx=1) -> np.ndarray:
+    x = quad.as_quad(x)
+    if n is None:
+        n = len(x) // incx
+    out = quad.empty(1)
+    check(load().quadblas_qnrm2_q(n, _p(x), incx, _p(out)))
+    return out
+
+
+def axpy(alpha, x, y, n=None, incx=1, incy=1) -> None:
+    x, y, a = quad.as_quad(x), quad.as_quad(y), _q1(alpha)
+    if n is None:
+        n = len(x) // incx
+    check(load().quadblas_qaxpy_q(n, _p(a), _p(x), incx, _p(y), incy))
+
+
+def gemv(layout, trans, m, n, alpha, A, lda, x, incx, beta, y, incy) -> None:
+    a, b = _q1(alpha), _q1(beta)
+    check(load().quadblas_qgemv_q(_c(layout), _c(trans), m, n, _p(a), _p(A), lda, _p(x), incx, _p(b),
+                                  _p(y), incy))
+
+
+def gemm(layout, transa, transb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc) -> None:
+    a, b = _q1(alpha), _q1(beta)
+    check(load().quadblas_qgemm_q(_c(layout), _c(transa), _c(transb), m, n, k, _p(a), _p(A), lda, _p(B),
+                                  ldb, _p(b), _p(C), ldc))
+
+
+# ---- device pointers ------------------------------------------------------
+def _stream(stream):
+    if stream is None:
+        import torch
+        return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    if isinstance(stream, int):
+        return ctypes.c_void_p(stream)
+    return ctypes.c_void_p(stream.cuda_stream)
+
+
+def _dp(t):
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def dot_dev(n, dx, incx, dy, incy, dres, stream=None) -> None:
+    check(load().quadblas_qdot_dev(n, _dp(dx), incx, _dp(dy), incy, _dp(dres), _stream(stream)))
+
+
+def nrm2_dev(n, dx, incx, dres, stream=None) -> None:
+    check(load().quadblas_qnrm2_dev(n, _dp(dx), incx, _dp(dres), _stream(stream)))
+
+
+def axpy_dev(n, alpha, dx, incx, dy, incy, stream=None) -> None:
+    a = _q1(alpha)
+    check(load().quadblas_qaxpy_dev(n, _p(a), _dp(dx), incx, _dp(dy), incy, _stream(stream)))
+
+
+def gemv_dev(layout, trans, m, n, alpha, dA, lda, dx, incx, beta, dy, incy, stream=None) -> None:
+    a, b = _q1(alpha), _q1(beta)
+    check(load().quadblas_qgemv_dev(_c(layout), _c(trans), m, n, _p(a), _dp(dA), lda, _dp(dx), incx,
+                                    _p(b), _dp(dy), incy, _stream(stream)))
+
+
+def gemm_dev(layout, transa, transb, m, n, k, alpha, dA, lda, dB, ldb, beta, dC, ldc, stream=None) -> None:
+    a, b = _q1(alpha), _q1(beta)
+    check(load().quadblas_qgemm_dev(_c(layout), _c(transa), _c(transb), m, n, k, _p(a), _dp(dA), lda,
+                                    _dp(dB), ldb, _p(b), _dp(dC), ldc, _stream(stream)))
+
+
+def set_method(method: int) -> None:
+    check(load().quadblas_set_method(method))
+
+
+def set_ozaki_slices(s: int) -> None:
+    check(load().quadblas_set_ozaki_slices(s))

@@ -1,0 +1,546 @@
+// C ABI of libquadblas_gpu.so (declared in include/quadblas_gpu.h).
+//
+// The nine reference entry points keep the exact signatures of
+// include/quadblas/interface/c_interface.hpp:21-144 (host Sleef_quad
+// pointers, double scalars, void/double returns).  Each one stages its
+// operands into device buffers owned by this library, runs the kernels on
+// an internal stream of the current device and copies the result back
+// before returning, so it is a drop-in for the reference's synchronous CPU
+// call.  Extensions:
+//   *_q   : host pointers, binary128 scalars and results, int64 sizes,
+//           status return;
+//   *_dev : device pointers on a caller-given CUDA stream (no host sync).
+// There is no CPU fallback: with no usable GPU every call fails with
+// QBLAS_ERR_NO_DEVICE (reference-compatible calls then return 0 / leave
+// outputs unchanged and record the error for quadblas_last_error()).
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string.h>
+
+#include <algorithm>
+#include <atomic>
+#include <mutex>
+#include <thread>
+
+#include "kernels.h"
+
+using qb::q128;
+
+namespace {
+
+thread_local int g_last_error = 0;
+std::atomic<int> g_num_threads{0};
+std::atomic<int> g_method{0};   // 0 auto, 1 soft-float, 2 Ozaki
+std::atomic<int> g_slices{0};   // 0 = automatic
+
+int fail(int code) {
+  g_last_error = code;
+  return code;
+}
+
+int cuda_status(cudaError_t e) {
+  if (e == cudaSuccess) return qb::kOk;
+  if (e == cudaErrorMemoryAllocation) return qb::kErrNoMemory;
+  if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return qb::kErrNoDevice;
+  return qb::kErrCuda;
+}
+
+q128 q_from_double(double d) {
+  uint64_t b;
+  memcpy(&b, &d, 8);
+  return qb::q_from_double_bits(b);
+}
+
+double q_to_double(q128 q) {
+  uint64_t b = qb::q_to_double_bits(q);
+  double d;
+  memcpy(&d, &b, 8);
+  return d;
+}
+
+q128 q_load(const void* p) {
+  q128 v;
+  memcpy(&v, p, 16);
+  return v;
+}
+
+// ---- per-device state for the host-pointer entry points -------------------
+enum Slot { kSlotA, kSlotB, kSlotC, kSlotScratch, kSlotResult, kNumSlots };
+
+struct DevState {
+  std::mutex mu;
+  cudaStream_t stream = nullptr;
+  void* buf[kNumSlots] = {nullptr};
+  size_t cap[kNumSlots] = {0};
+  bool pool_ready = false;
+};
+
+constexpr int kMaxDevices = 64;
+DevState g_dev[kMaxDevices];
+
+int current_device(int& dev) {
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_status(e);
+  if (dev < 0 || dev >= kMaxDevices) return qb::kErrNoDevice;
+  return qb::kOk;
+}
+
+// Keeps memory freed by cudaFreeAsync cached in the device's default pool so
+// per-call scratch does not return to the driver between calls.
+void ensure_pool(DevState& st, int dev) {
+  if (st.pool_ready) return;
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+    uint64_t thr = UINT64_MAX;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+  }
+  st.pool_ready = true;
+}
+
+int ensure_slot(DevState& st, Slot s, size_t bytes) {
+  if (bytes == 0) bytes = 16;
+  if (st.cap[s] >= bytes) return qb::kOk;
+  if (st.buf[s]) {
+    cudaStreamSynchronize(st.stream);
+    cudaFree(st.buf[s]);
+    st.buf[s] = nullptr;
+    st.cap[s] = 0;
+  }
+  size_t want = bytes + bytes / 8;
+  cudaError_t e = cudaMalloc(&st.buf[s], want);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    st.buf[s] = nullptr;
+    return cuda_status(e);
+  }
+  st.cap[s] = want;
+  return qb::kOk;
+}
+
+// Locks the current device's state and makes sure its stream exists.
+struct HostCall {
+  DevState* st = nullptr;
+  std::unique_lock<std::mutex> lock;
+  int status = qb::kOk;
+  HostCall() {
+    int dev;
+    status = current_device(dev);
+    if (status) return;
+    st = &g_dev[dev];
+    lock = std::unique_lock<std::mutex>(st->mu);
+    ensure_pool(*st, dev);
+    if (!st->stream) {
+      cudaError_t e = cudaStreamCreateWithFlags(&st->stream, cudaStreamNonBlocking);
+      if (e != cudaSuccess) {
+        cudaGetLastError();
+        status = cuda_status(e);
+      }
+    }
+  }
+};
+
+int64_t extent(int64_t rows, int64_t cols, int64_t srow, int64_t scol) {
+  if (rows <= 0 || cols <= 0) return 0;
+  return (rows - 1) * srow + (cols - 1) * scol + 1;
+}
+
+bool aligned16(const void* p) { return ((uintptr_t)p & 15u) == 0; }
+
+int h2d(void* dst, const void* src, int64_t elems, cudaStream_t s) {
+  if (elems <= 0) return qb::kOk;
+  return cuda_status(cudaMemcpyAsync(dst, src, (size_t)elems * 16, cudaMemcpyHostToDevice, s));
+}
+int d2h(void* dst, const void* src, int64_t elems, cudaStream_t s) {
+  if (elems <= 0) return qb::kOk;
+  return cuda_status(cudaMemcpyAsync(dst, src, (size_t)elems * 16, cudaMemcpyDeviceToHost, s));
+}
+
+bool is_trans(char t) { return t == 'T' || t == 't' || t == 'C' || t == 'c'; }
+bool is_col(char layout) { return layout == 'C' || layout == 'c'; }
+
+// ---- argument resolution (shared by host and device entry points) --------
+struct GemvPlan {
+  int64_t m, n;  // op(A) is m x n after the reference's trans handling
+  qb::MatView A;
+  int64_t a_rows, a_cols;  // storage extent in (row, col) of the view
+};
+
+// Reference semantics (c_interface.hpp:76-85): trans swaps m and n and
+// flips the layout; then row-major reads A[i*lda + j], column-major
+// A[j*lda + i] (level2.hpp:33-44, :72-79).
+int plan_gemv(char layout, char trans, int64_t m, int64_t n, int64_t lda, GemvPlan& p) {
+  if (m < 0 || n < 0) return qb::kErrInvalidValue;
+  bool col = is_col(layout);
+  if (is_trans(trans)) {
+    std::swap(m, n);
+    col = !col;
+  }
+  p.m = m;
+  p.n = n;
+  if (!col) {
+    if (lda < std::max<int64_t>(1, n)) return qb::kErrInvalidValue;
+    p.A.si = lda;
+    p.A.sj = 1;
+  } else {
+    if (lda < std::max<int64_t>(1, m)) return qb::kErrInvalidValue;
+    p.A.si = 1;
+    p.A.sj = lda;
+  }
+  p.A.p = nullptr;
+  return qb::kOk;
+}
+
+struct GemmPlan {
+  qb::GemmArgs g;
+  int64_t extA, extB, extC;
+};
+
+int plan_gemm(char layout, char transa, char transb, int64_t m, int64_t n, int64_t k, int64_t lda,
+              int64_t ldb, int64_t ldc, GemmPlan& p) {
+  if (m < 0 || n < 0 || k < 0) return qb::kErrInvalidValue;
+  bool col = is_col(layout), ta = is_trans(transa), tb = is_trans(transb);
+  qb::GemmArgs& g = p.g;
+  g.m = m;
+  g.n = n;
+  g.k = k;
+  // op(A) is m x k, op(B) is k x n, C is m x n.
+  // Stored A has (ar x ac) = ta ? (k x m) : (m x k); likewise B.
+  int64_t ar = ta ? k : m, ac = ta ? m : k;
+  int64_t br = tb ? n : k, bc = tb ? k : n;
+  if (!col) {
+    if (lda < std::max<int64_t>(1, ac) || ldb < std::max<int64_t>(1, bc) ||
+        ldc < std::max<int64_t>(1, n))
+      return qb::kErrInvalidValue;
+    // stored element (r, c) at r*ld + c
+    g.sai = ta ? 1 : lda;
+    g.sal = ta ? lda : 1;
+    g.sbl = tb ? 1 : ldb;
+    g.sbj = tb ? ldb : 1;
+    g.sci = ldc;
+    g.scj = 1;
+  } else {
+    if (lda < std::max<int64_t>(1, ar) || ldb < std::max<int64_t>(1, br) ||
+        ldc < std::max<int64_t>(1, m))
+      return qb::kErrInvalidValue;
+    // stored element (r, c) at c*ld + r
+    g.sai = ta ? lda : 1;
+    g.sal = ta ? 1 : lda;
+    g.sbl = tb ? ldb : 1;
+    g.sbj = tb ? 1 : ldb;
+    g.sci = 1;
+    g.scj = ldc;
+  }
+  p.extA = extent(m, k, g.sai, g.sal);
+  p.extB = extent(k, n, g.sbl, g.sbj);
+  p.extC = extent(m, n, g.sci, g.scj);
+  return qb::kOk;
+}
+
+// ---- device-pointer implementations -----------------------------------
+int dev_dot(int64_t n, const void* dx, int64_t incx, const void* dy, int64_t incy, void* dres,
+            int take_sqrt, cudaStream_t s, void* scratch_or_null) {
+  if (n < 0 || (n > 0 && (incx <= 0 || incy <= 0))) return qb::kErrInvalidValue;
+  if (!aligned16(dx) || !aligned16(dy) || !aligned16(dres)) return qb::kErrMisaligned;
+  size_t sb = qb::dot_scratch_bytes(n);
+  void* scratch = scratch_or_null;
+  if (!scratch && n > 0) {
+    cudaError_t e = cudaMallocAsync(&scratch, sb, s);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return cuda_status(e);
+    }
+  }
+  cudaError_t e = qb::launch_dot(n, (const q128*)dx, incx, (const q128*)dy, incy, (q128*)dres,
+                                 take_sqrt, scratch, s);
+  if (!scratch_or_null && scratch) cudaFreeAsync(scratch, s);
+  return cuda_status(e);
+}
+
+int dev_gemv(const GemvPlan& p0, const void* alpha, const void* dA, const void* dx, int64_t incx,
+             const void* beta, void* dy, int64_t incy, cudaStream_t s, void* scratch_or_null) {
+  GemvPlan p = p0;
+  if (p.m > 0 && p.n > 0 && (incx <= 0 || incy <= 0)) return qb::kErrInvalidValue;
+  if (!aligned16(dA) || !aligned16(dx) || !aligned16(dy)) return qb::kErrMisaligned;
+  p.A.p = (const q128*)dA;
+  size_t sb = qb::gemv_scratch_bytes(p.m, p.n, p.A);
+  void* scratch = scratch_or_null;
+  if (!scratch && sb) {
+    cudaError_t e = cudaMallocAsync(&scratch, sb, s);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return cuda_status(e);
+    }
+  }
+  cudaError_t e = qb::launch_gemv(p.m, p.n, q_load(alpha), p.A, (const q128*)dx, incx, q_load(beta),
+                                  (q128*)dy, incy, scratch, s);
+  if (!scratch_or_null && scratch) cudaFreeAsync(scratch, s);
+  return cuda_status(e);
+}
+
+int dev_gemm(GemmPlan p, const void* alpha, const void* dA, const void* dB, const void* beta,
+             void* dC, cudaStream_t s) {
+  if (!aligned16(dA) || !aligned16(dB) || !aligned16(dC)) return qb::kErrMisaligned;
+  p.g.A = (const q128*)dA;
+  p.g.B = (const q128*)dB;
+  p.g.C = (q128*)dC;
+  p.g.alpha = q_load(alpha);
+  p.g.beta = q_load(beta);
+  return cuda_status(qb::launch_gemm_softfloat(p.g, s));
+}
+
+// ---- host-pointer implementations --------------------------------------
+int host_dot(int64_t n, const void* x, int64_t incx, const void* y, int64_t incy, void* result,
+             int take_sqrt) {
+  if (n < 0 || (n > 0 && (incx <= 0 || incy <= 0))) return qb::kErrInvalidValue;
+  if (!result || (n > 0 && (!x || !y))) return qb::kErrInvalidValue;
+  HostCall hc;
+  if (hc.status) return hc.status;
+  DevState& st = *hc.st;
+  int64_t ex = extent(n, 1, incx, 1), ey = extent(n, 1, incy, 1);
+  int rc;
+  if ((rc = ensure_slot(st, kSlotA, ex * 16)) || (rc = ensure_slot(st, kSlotB, ey * 16)) ||
+      (rc = ensure_slot(st, kSlotResult, 16)) ||
+      (rc = ensure_slot(st, kSlotScratch, qb::dot_scratch_bytes(n))))
+    return rc;
+  if ((rc = h2d(st.buf[kSlotA], x, ex, st.stream)) || (rc = h2d(st.buf[kSlotB], y, ey, st.stream)))
+    return rc;
+  rc = dev_dot(n, st.buf[kSlotA], incx, st.buf[kSlotB], incy, st.buf[kSlotResult], take_sqrt,
+               st.stream, st.buf[kSlotScratch]);
+  if (rc) return rc;
+  if ((rc = d2h(result, st.buf[kSlotResult], 1, st.stream))) return rc;
+  return cuda_status(cudaStreamSynchronize(st.stream));
+}
+
+int host_axpy(int64_t n, const void* alpha, const void* x, int64_t incx, void* y, int64_t incy) {
+  if (n <= 0) return qb::kOk;  // c_interface.hpp:49
+  if (incx <= 0 || incy <= 0 || !x || !y || !alpha) return qb::kErrInvalidValue;
+  HostCall hc;
+  if (hc.status) return hc.status;
+  DevState& st = *hc.st;
+  int64_t ex = extent(n, 1, incx, 1), ey = extent(n, 1, incy, 1);
+  int rc;
+  if ((rc = ensure_slot(st, kSlotA, ex * 16)) || (rc = ensure_slot(st, kSlotC, ey * 16))) return rc;
+  if ((rc = h2d(st.buf[kSlotA], x, ex, st.stream)) || (rc = h2d(st.buf[kSlotC], y, ey, st.stream)))
+    return rc;
+  rc = cuda_status(qb::launch_axpy(n, q_load(alpha), (const q128*)st.buf[kSlotA], incx,
+                                   (q128*)st.buf[kSlotC], incy, st.stream));
+  if (rc) return rc;
+  if ((rc = d2h(y, st.buf[kSlotC], ey, st.stream))) return rc;
+  return cuda_status(cudaStreamSynchronize(st.stream));
+}
+
+int host_gemv(char layout, char trans, int64_t m, int64_t n, const void* alpha, const void* A,
+              int64_t lda, const void* x, int64_t incx, const void* beta, void* y, int64_t incy) {
+  GemvPlan p;
+  int rc = plan_gemv(layout, trans, m, n, lda, p);
+  if (rc) return rc;
+  if (p.m == 0 || p.n == 0) return qb::kOk;  // level2.hpp:21,61
+  if (incx <= 0 || incy <= 0 || !A || !x || !y || !alpha || !beta) return qb::kErrInvalidValue;
+  HostCall hc;
+  if (hc.status) return hc.status;
+  DevState& st = *hc.st;
+  int64_t eA = extent(p.m, p.n, p.A.si, p.A.sj), ex = extent(p.n, 1, incx, 1),
+          ey = extent(p.m, 1, incy, 1);
+  if ((rc = ensure_slot(st, kSlotA, eA * 16)) || (rc = ensure_slot(st, kSlotB, ex * 16)) ||
+      (rc = ensure_slot(st, kSlotC, ey * 16)))
+    return rc;
+  qb::MatView probe = p.A;
+  size_t sb = qb::gemv_scratch_bytes(p.m, p.n, probe);
+  if ((rc = ensure_slot(st, kSlotScratch, sb))) return rc;
+  if ((rc = h2d(st.buf[kSlotA], A, eA, st.stream)) || (rc = h2d(st.buf[kSlotB], x, ex, st.stream)) ||
+      (rc = h2d(st.buf[kSlotC], y, ey, st.stream)))
+    return rc;
+  rc = dev_gemv(p, alpha, st.buf[kSlotA], st.buf[kSlotB], incx, beta, st.buf[kSlotC], incy, st.stream,
+                st.buf[kSlotScratch]);
+  if (rc) return rc;
+  if ((rc = d2h(y, st.buf[kSlotC], ey, st.stream))) return rc;
+  return cuda_status(cudaStreamSynchronize(st.stream));
+}
+
+int host_gemm(char layout, char transa, char transb, int64_t m, int64_t n, int64_t k,
+              const void* alpha, const void* A, int64_t lda, const void* B, int64_t ldb,
+              const void* beta, void* C, int64_t ldc) {
+  GemmPlan p;
+  int rc = plan_gemm(layout, transa, transb, m, n, k, lda, ldb, ldc, p);
+  if (rc) return rc;
+  if (m == 0 || n == 0 || k == 0) return qb::kOk;  // level3.hpp:221
+  if (!A || !B || !C || !alpha || !beta) return qb::kErrInvalidValue;
+  HostCall hc;
+  if (hc.status) return hc.status;
+  DevState& st = *hc.st;
+  if ((rc = ensure_slot(st, kSlotA, p.extA * 16)) || (rc = ensure_slot(st, kSlotB, p.extB * 16)) ||
+      (rc = ensure_slot(st, kSlotC, p.extC * 16)))
+    return rc;
+  if ((rc = h2d(st.buf[kSlotA], A, p.extA, st.stream)) ||
+      (rc = h2d(st.buf[kSlotB], B, p.extB, st.stream)) ||
+      (rc = h2d(st.buf[kSlotC], C, p.extC, st.stream)))
+    return rc;
+  rc = dev_gemm(p, alpha, st.buf[kSlotA], st.buf[kSlotB], beta, st.buf[kSlotC], st.stream);
+  if (rc) return rc;
+  if ((rc = d2h(C, st.buf[kSlotC], p.extC, st.stream))) return rc;
+  return cuda_status(cudaStreamSynchronize(st.stream));
+}
+
+}  // namespace
+
+#define QBLAS_EXPORT extern "C" __attribute__((visibility("default")))
+
+// ===========================================================================
+// Reference-compatible entry points (c_interface.hpp:21-144)
+// ===========================================================================
+QBLAS_EXPORT double quadblas_qdot(int n, void* x, int incx, void* y, int incy) {
+  q128 r = qb::q_zero(0);
+  int rc = host_dot(n, x, incx, y, incy, &r, 0);
+  if (rc) {
+    fail(rc);
+    return 0.0;
+  }
+  g_last_error = 0;
+  return q_to_double(r);
+}
+
+QBLAS_EXPORT double quadblas_qnrm2(int n, void* x, int incx) {
+  q128 r = qb::q_zero(0);
+  int rc = host_dot(n, x, incx, x, incx, &r, 1);
+  if (rc) {
+    fail(rc);
+    return 0.0;
+  }
+  g_last_error = 0;
+  return q_to_double(r);
+}
+
+QBLAS_EXPORT void quadblas_qaxpy(int n, double alpha, void* x, int incx, void* y, int incy) {
+  q128 a = q_from_double(alpha);
+  int rc = host_axpy(n, &a, x, incx, y, incy);
+  g_last_error = rc;
+}
+
+QBLAS_EXPORT void quadblas_qgemv(char layout, char trans, int m, int n, double alpha, void* A,
+                                 int lda, void* x, int incx, double beta, void* y, int incy) {
+  q128 a = q_from_double(alpha), b = q_from_double(beta);
+  g_last_error = host_gemv(layout, trans, m, n, &a, A, lda, x, incx, &b, y, incy);
+}
+
+QBLAS_EXPORT void quadblas_qgemm(char layout, char transa, char transb, int m, int n, int k,
+                                 double alpha, void* A, int lda, void* B, int ldb, double beta,
+                                 void* C, int ldc) {
+  q128 a = q_from_double(alpha), b = q_from_double(beta);
+  g_last_error = host_gemm(layout, transa, transb, m, n, k, &a, A, lda, B, ldb, &b, C, ldc);
+}
+
+QBLAS_EXPORT void quadblas_set_num_threads(int num_threads) {
+  g_num_threads.store(num_threads > 0 ? num_threads : 0);
+}
+
+QBLAS_EXPORT int quadblas_get_num_threads(void) {
+  int v = g_num_threads.load();
+  if (v > 0) return v;
+  unsigned hc = std::thread::hardware_concurrency();
+  return hc ? (int)hc : 1;
+}
+
+QBLAS_EXPORT const char* quadblas_get_version(void) {
+  return "QuadBLAS 1.0.0 - qblas-gb300 binary128 BLAS for sm_103a";
+}
+
+QBLAS_EXPORT int quadblas_is_aligned(const void* ptr) {
+  return ((uintptr_t)ptr % 32u) == 0;  // core/constants.hpp:18 (ALIGNMENT = 32)
+}
+
+// ===========================================================================
+// Extensions: binary128 scalars/results on host pointers
+// ===========================================================================
+QBLAS_EXPORT int quadblas_qdot_q(int64_t n, const void* x, int64_t incx, const void* y,
+                                 int64_t incy, void* result) {
+  return fail(host_dot(n, x, incx, y, incy, result, 0));
+}
+QBLAS_EXPORT int quadblas_qnrm2_q(int64_t n, const void* x, int64_t incx, void* result) {
+  return fail(host_dot(n, x, incx, x, incx, result, 1));
+}
+QBLAS_EXPORT int quadblas_qaxpy_q(int64_t n, const void* alpha, const void* x, int64_t incx,
+                                  void* y, int64_t incy) {
+  return fail(host_axpy(n, alpha, x, incx, y, incy));
+}
+QBLAS_EXPORT int quadblas_qgemv_q(char layout, char trans, int64_t m, int64_t n, const void* alpha,
+                                  const void* A, int64_t lda, const void* x, int64_t incx,
+                                  const void* beta, void* y, int64_t incy) {
+  return fail(host_gemv(layout, trans, m, n, alpha, A, lda, x, incx, beta, y, incy));
+}
+QBLAS_EXPORT int quadblas_qgemm_q(char layout, char transa, char transb, int64_t m, int64_t n,
+                                  int64_t k, const void* alpha, const void* A, int64_t lda,
+                                  const void* B, int64_t ldb, const void* beta, void* C,
+                                  int64_t ldc) {
+  return fail(host_gemm(layout, transa, transb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc));
+}
+
+// ===========================================================================
+// Extensions: device pointers, stream-ordered (stream is a cudaStream_t)
+// ===========================================================================
+QBLAS_EXPORT int quadblas_qdot_dev(int64_t n, const void* dx, int64_t incx, const void* dy,
+                                   int64_t incy, void* d_result, void* stream) {
+  return fail(dev_dot(n, dx, incx, dy, incy, d_result, 0, (cudaStream_t)stream, nullptr));
+}
+QBLAS_EXPORT int quadblas_qnrm2_dev(int64_t n, const void* dx, int64_t incx, void* d_result,
+                                    void* stream) {
+  return fail(dev_dot(n, dx, incx, dx, incx, d_result, 1, (cudaStream_t)stream, nullptr));
+}
+QBLAS_EXPORT int quadblas_qaxpy_dev(int64_t n, const void* alpha, const void* dx, int64_t incx,
+                                    void* dy, int64_t incy, void* stream) {
+  if (n <= 0) return fail(qb::kOk);
+  if (incx <= 0 || incy <= 0 || !alpha) return fail(qb::kErrInvalidValue);
+  if (!aligned16(dx) || !aligned16(dy)) return fail(qb::kErrMisaligned);
+  return fail(cuda_status(qb::launch_axpy(n, q_load(alpha), (const q128*)dx, incx, (q128*)dy, incy,
+                                          (cudaStream_t)stream)));
+}
+QBLAS_EXPORT int quadblas_qgemv_dev(char layout, char trans, int64_t m, int64_t n,
+                                    const void* alpha, const void* dA, int64_t lda, const void* dx,
+                                    int64_t incx, const void* beta, void* dy, int64_t incy,
+                                    void* stream) {
+  GemvPlan p;
+  int rc = plan_gemv(layout, trans, m, n, lda, p);
+  if (rc) return fail(rc);
+  if (p.m == 0 || p.n == 0) return fail(qb::kOk);
+  if (!alpha || !beta) return fail(qb::kErrInvalidValue);
+  return fail(dev_gemv(p, alpha, dA, dx, incx, beta, dy, incy, (cudaStream_t)stream, nullptr));
+}
+QBLAS_EXPORT int quadblas_qgemm_dev(char layout, char transa, char transb, int64_t m, int64_t n,
+                                    int64_t k, const void* alpha, const void* dA, int64_t lda,
+                                    const void* dB, int64_t ldb, const void* beta, void* dC,
+                                    int64_t ldc, void* stream) {
+  GemmPlan p;
+  int rc = plan_gemm(layout, transa, transb, m, n, k, lda, ldb, ldc, p);
+  if (rc) return fail(rc);
+  if (m == 0 || n == 0 || k == 0) return fail(qb::kOk);
+  if (!alpha || !beta) return fail(qb::kErrInvalidValue);
+  return fail(dev_gemm(p, alpha, dA, dB, beta, dC, (cudaStream_t)stream));
+}
+
+// ===========================================================================
+// Configuration and errors
+// ===========================================================================
+QBLAS_EXPORT int quadblas_set_method(int method) {
+  if (method < 0 || method > 2) return fail(qb::kErrInvalidValue);
+  g_method.store(method);
+  return fail(qb::kOk);
+}
+QBLAS_EXPORT int quadblas_get_method(void) { return g_method.load(); }
+QBLAS_EXPORT int quadblas_set_ozaki_slices(int slices) {
+  if (slices < 0 || slices > 32) return fail(qb::kErrInvalidValue);
+  g_slices.store(slices);
+  return fail(qb::kOk);
+}
+QBLAS_EXPORT int quadblas_get_ozaki_slices(void) { return g_slices.load(); }
+QBLAS_EXPORT int quadblas_last_error(void) { return g_last_error; }
+QBLAS_EXPORT const char* quadblas_error_string(int code) {
+  switch (code) {
+    case qb::kOk: return "success";
+    case qb::kErrInvalidValue: return "invalid argument";
+    case qb::kErrCuda: return "CUDA error";
+    case qb::kErrNoMemory: return "out of device memory";
+    case qb::kErrNotSupported: return "not supported";
+    case qb::kErrNoDevice: return "no usable CUDA device";
+    case qb::kErrMisaligned: return "device pointer not 16-byte aligned";
+    default: return "unknown error";
+  }
+}

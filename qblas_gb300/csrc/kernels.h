@@ -1,0 +1,64 @@
+// Internal interface between the C ABI layer (capi.cpp) and the CUDA
+// kernels.  All pointers are device pointers; all strides are in elements
+// (16-byte binary128 values) and positive.  Every launcher is stream-ordered
+// and allocates nothing: scratch memory, when a kernel needs it, is passed
+// in by the caller and its size is given by the matching *_scratch_bytes().
+#pragma once
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include "softquad.cuh"
+
+namespace qb {
+
+// Error codes of the C ABI (mirrored in include/quadblas_gpu.h).
+enum Status : int {
+  kOk = 0,
+  kErrInvalidValue = 1,
+  kErrCuda = 2,
+  kErrNoMemory = 3,
+  kErrNotSupported = 4,
+  kErrNoDevice = 5,
+  kErrMisaligned = 6,
+};
+
+// op(A) is an m x n matrix with element (i, j) at A[i*si + j*sj].
+struct MatView {
+  const q128* p;
+  int64_t si, sj;
+};
+
+// ---- level 1 -----------------------------------------------------------
+// out[0] = round(sum_i x_i*y_i)  (sqrt of it when take_sqrt != 0)
+size_t dot_scratch_bytes(int64_t n);
+cudaError_t launch_dot(int64_t n, const q128* x, int64_t incx, const q128* y, int64_t incy,
+                       q128* out, int take_sqrt, void* scratch, cudaStream_t s);
+// y_i = fma(alpha, x_i, y_i)
+cudaError_t launch_axpy(int64_t n, q128 alpha, const q128* x, int64_t incx, q128* y, int64_t incy,
+                        cudaStream_t s);
+
+// ---- level 2 -----------------------------------------------------------
+// y_i = fma(alpha, round(sum_j op(A)(i,j) x_j), beta * y_i), i < m
+size_t gemv_scratch_bytes(int64_t m, int64_t n, MatView A);
+cudaError_t launch_gemv(int64_t m, int64_t n, q128 alpha, MatView A, const q128* x, int64_t incx,
+                        q128 beta, q128* y, int64_t incy, void* scratch, cudaStream_t s);
+
+// ---- level 3 -----------------------------------------------------------
+struct GemmArgs {
+  int64_t m, n, k;
+  const q128* A;
+  int64_t sai, sal;  // op(A)(i, l) = A[i*sai + l*sal]
+  const q128* B;
+  int64_t sbl, sbj;  // op(B)(l, j) = B[l*sbl + j*sbj]
+  q128* C;
+  int64_t sci, scj;  // C(i, j) = C[i*sci + j*scj]
+  q128 alpha, beta;
+};
+// C = fma(alpha, round(sum_l op(A)(i,l) op(B)(l,j)), beta * C), soft-float
+cudaError_t launch_gemm_softfloat(const GemmArgs& g, cudaStream_t s);
+
+// Multiprocessor count of the current device (cached).
+int device_sm_count();
+
+}  // namespace qb

@@ -1,0 +1,126 @@
+// Level-3 soft-float kernel: qgemm, C = alpha * op(A) op(B) + beta * C.
+//
+// Replaces QuadBLAS::gemm / gemm_simple / the blocked macro and micro
+// kernels (include/quadblas/algorithms/level3.hpp:17-336).  Each C(i,j) is
+// the correctly rounded exact sum_l op(A)(i,l) op(B)(l,j) (wide accumulator,
+// one rounding) followed by the reference epilogue
+// C = fma(alpha, sum, beta * C) (level3.hpp:40,107,210).  The reference
+// rounds once per k-panel of 126; this kernel rounds once in total, which is
+// more accurate and within the k * u_q * sum|a b| reduction bound.
+//
+// Integer-pipe bound.  A CTA owns a 32 x 32 tile of C; its 256 threads each
+// own a 2 x 2 block.  A and B k-slices of 16 are loaded once per CTA,
+// unpacked (sign, exponent, significand shifted to bit 127) and staged in
+// shared memory as structure-of-arrays, so the inner loop is the 128x128-bit
+// product and the aligned add into the accumulator.
+#include "kernels.h"
+#include "reduce.cuh"
+
+namespace qb {
+
+constexpr int kTM = 32, kTN = 32, kTK = 16;
+constexpr int kGemmThreads = 256;
+
+struct SoftTile {
+  uint32_t m0[kTK][kTM], m1[kTK][kTM], m2[kTK][kTM], m3[kTK][kTM];
+  int32_t e[kTK][kTM];
+  uint32_t sc[kTK][kTM];  // sign | class << 1
+};
+
+__device__ __forceinline__ void tile_put(SoftTile& t, int kk, int idx, q128 v) {
+  qop o = qop_unpack(v);
+  t.m0[kk][idx] = o.m0;
+  t.m1[kk][idx] = o.m1;
+  t.m2[kk][idx] = o.m2;
+  t.m3[kk][idx] = o.m3;
+  t.e[kk][idx] = o.e;
+  t.sc[kk][idx] = o.s | (o.cls << 1);
+}
+
+__device__ __forceinline__ qop tile_get(const SoftTile& t, int kk, int idx) {
+  qop o;
+  o.m0 = t.m0[kk][idx];
+  o.m1 = t.m1[kk][idx];
+  o.m2 = t.m2[kk][idx];
+  o.m3 = t.m3[kk][idx];
+  o.e = t.e[kk][idx];
+  uint32_t sc = t.sc[kk][idx];
+  o.s = sc & 1u;
+  o.cls = sc >> 1;
+  return o;
+}
+
+__global__ void __launch_bounds__(kGemmThreads)
+    qgemm_soft_kernel(int64_t m, int64_t n, int64_t k, const q128* __restrict__ A, int64_t sai,
+                      int64_t sal, const q128* __restrict__ B, int64_t sbl, int64_t sbj,
+                      q128* __restrict__ C, int64_t sci, int64_t scj, q128 alpha, q128 beta) {
+  __shared__ SoftTile sA, sB;
+  const int tid = threadIdx.x;
+  const int tx = tid & 15, ty = tid >> 4;
+  const int64_t i0 = (int64_t)blockIdx.y * kTM, j0 = (int64_t)blockIdx.x * kTN;
+  const q128 zero = q_zero(0);
+
+  wacc c00, c01, c10, c11;
+  wacc_init(c00);
+  wacc_init(c01);
+  wacc_init(c10);
+  wacc_init(c11);
+
+  for (int64_t l0 = 0; l0 < k; l0 += kTK) {
+    // Stage op(A)[i0:i0+32, l0:l0+16]: element e -> (row e/16, kk e%16)
+    // and op(B)[l0:l0+16, j0:j0+32]: element e -> (kk e/32, col e%32).
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+      int e = tid + r * kGemmThreads;
+      int ar = e >> 4, ak = e & 15;
+      int64_t gi = i0 + ar, gl = l0 + ak;
+      q128 av = (gi < m && gl < k) ? ld_cached(A + gi * sai + gl * sal) : zero;
+      int bk = e >> 5, bc = e & 31;
+      int64_t bl = l0 + bk, gj = j0 + bc;
+      q128 bv = (bl < k && gj < n) ? ld_cached(B + bl * sbl + gj * sbj) : zero;
+      tile_put(sA, ak, ar, av);
+      tile_put(sB, bk, bc, bv);
+    }
+    __syncthreads();
+#pragma unroll 2
+    for (int kk = 0; kk < kTK; ++kk) {
+      qop a0 = tile_get(sA, kk, 2 * ty), a1 = tile_get(sA, kk, 2 * ty + 1);
+      qop b0 = tile_get(sB, kk, 2 * tx), b1 = tile_get(sB, kk, 2 * tx + 1);
+      wacc_add_product(c00, a0, b0);
+      wacc_add_product(c01, a0, b1);
+      wacc_add_product(c10, a1, b0);
+      wacc_add_product(c11, a1, b1);
+    }
+    __syncthreads();
+  }
+
+  const int64_t ia = i0 + 2 * ty, ja = j0 + 2 * tx;
+  if (ia < m && ja < n) {
+    q128* p = C + ia * sci + ja * scj;
+    *p = q_fma(alpha, wacc_round(c00), q_mul(beta, *p));
+  }
+  if (ia < m && ja + 1 < n) {
+    q128* p = C + ia * sci + (ja + 1) * scj;
+    *p = q_fma(alpha, wacc_round(c01), q_mul(beta, *p));
+  }
+  if (ia + 1 < m && ja < n) {
+    q128* p = C + (ia + 1) * sci + ja * scj;
+    *p = q_fma(alpha, wacc_round(c10), q_mul(beta, *p));
+  }
+  if (ia + 1 < m && ja + 1 < n) {
+    q128* p = C + (ia + 1) * sci + (ja + 1) * scj;
+    *p = q_fma(alpha, wacc_round(c11), q_mul(beta, *p));
+  }
+}
+
+cudaError_t launch_gemm_softfloat(const GemmArgs& g, cudaStream_t s) {
+  if (g.m <= 0 || g.n <= 0 || g.k <= 0) return cudaSuccess;
+  int64_t gx = (g.n + kTN - 1) / kTN, gy = (g.m + kTM - 1) / kTM;
+  if (gy > 65535) return cudaErrorInvalidConfiguration;
+  dim3 grid((unsigned)gx, (unsigned)gy);
+  qgemm_soft_kernel<<<grid, kGemmThreads, 0, s>>>(g.m, g.n, g.k, g.A, g.sai, g.sal, g.B, g.sbl, g.sbj,
+                                                  g.C, g.sci, g.scj, g.alpha, g.beta);
+  return cudaGetLastError();
+}
+
+}  // namespace qb

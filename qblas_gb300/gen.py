@@ -1,0 +1,91 @@
+"""Seeded synthetic binary128 inputs for each benchmark workload.
+
+All generators return ``(n, 2)`` uint64 binary128 arrays (see ``quad.py``)
+and are fully determined by the numpy ``Generator`` they are given.
+
+Workloads (sizes and value distributions):
+  * full-mantissa uniform   : a binary64 drawn uniform in [-1, 1) widened to
+    binary128, with the 60 significand bits below the binary64 precision
+    filled randomly (a random low-order tail below 2^-53 relative), so every
+    value has a full 113-bit significand.  Used for the 512^3 soft-float
+    qgemm and the batched workload.
+  * wide-exponent           : +-u * 2^e, u uniform in [1, 2) with all 112
+    fraction bits random, e a uniform integer in [emin, emax] (qdot n=2^26
+    and qgemv 8192^2 use [-60, 60]).
+  * cancelling dot pairs    : wide-exponent vectors in which half of the
+    terms come in pairs whose products cancel to within 2^-80 relative.
+  * spread uniform          : u * 2^e with u uniform in [-1, 1) at full
+    113-bit significand and e a uniform integer in [emin, emax] (the 4096^3
+    Ozaki qgemm uses [-20, 20]).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from .quad import BIAS, U64, empty, from_double
+
+_M48 = U64((1 << 48) - 1)
+_M60 = U64((1 << 60) - 1)
+
+
+def rng_for(seed: int) -> np.random.Generator:
+    return np.random.Generator(np.random.PCG64(seed))
+
+
+def _rand_u64(rng: np.random.Generator, n: int) -> np.ndarray:
+    return rng.integers(0, np.iinfo(np.uint64).max, size=n, dtype=np.uint64, endpoint=True)
+
+
+def uniform_full(rng: np.random.Generator, n: int) -> np.ndarray:
+    """Binary64 uniform in [-1, 1) plus a random 60-bit tail below 2^-53."""
+    d = rng.uniform(-1.0, 1.0, size=int(n))
+    q = from_double(d)
+    nz = d != 0
+    q[:, 0] = np.where(nz, q[:, 0] | (_rand_u64(rng, d.size) & _M60), q[:, 0])
+    return q
+
+
+def wide_exponent(rng: np.random.Generator, n: int, emin: int = -60, emax: int = 60) -> np.ndarray:
+    """+-u * 2^e, u in [1, 2) with 112 random fraction bits, e uniform in [emin, emax]."""
+    n = int(n)
+    q = empty(n)
+    sign = rng.integers(0, 2, size=n, dtype=np.uint64)
+    e = rng.integers(emin, emax, size=n, endpoint=True).astype(np.int64)
+    bexp = (e + BIAS).astype(np.uint64)
+    q[:, 1] = (sign << U64(63)) | (bexp << U64(48)) | (_rand_u64(rng, n) & _M48)
+    q[:, 0] = _rand_u64(rng, n)
+    return q
+
+
+def cancelling_dot(rng: np.random.Generator, n: int, emin: int = -60, emax: int = 60):
+    """x, y for a dot product in which half of the terms form n/4 pairs whose
+    products cancel to within 2^-80 relative (x_b = -x_a perturbed in its
+    low 32 significand bits, y_b = y_a), like 1e20 + 1 - 1e20 at scale."""
+    x = wide_exponent(rng, n, emin, emax)
+    y = wide_exponent(rng, n, emin, emax)
+    npairs = n // 4
+    if npairs:
+        idx = rng.permutation(n)[: 2 * npairs].reshape(npairs, 2)
+        a, b = idx[:, 0], idx[:, 1]
+        x[b, 1] = x[a, 1] ^ U64(1 << 63)
+        x[b, 0] = (x[a, 0] & ~U64(0xFFFFFFFF)) | (_rand_u64(rng, npairs) & U64(0xFFFFFFFF))
+        y[b] = y[a]
+    return x, y
+
+
+def spread_uniform(rng: np.random.Generator, n: int, emin: int = -20, emax: int = 20) -> np.ndarray:
+    """u * 2^e with u uniform in [-1, 1) (full 113-bit significand) and e
+    uniform in [emin, emax]."""
+    q = uniform_full(rng, n)
+    e = rng.integers(emin, emax, size=int(n), endpoint=True).astype(np.int64)
+    bexp = ((q[:, 1] >> U64(48)) & U64(0x7FFF)).astype(np.int64)
+    nz = bexp != 0
+    nb = np.where(nz, bexp + e, 0).astype(np.uint64)
+    q[:, 1] = (q[:, 1] & ~U64(0x7FFF << 48)) | (nb << U64(48))
+    return q
+
+
+def log_uniform_int(rng: np.random.Generator, lo: int, hi: int, n: int) -> np.ndarray:
+    """Integers log-uniform in [lo, hi]."""
+    v = np.exp(rng.uniform(np.log(lo), np.log(hi + 1), size=int(n)))
+    return np.clip(np.floor(v).astype(np.int64), lo, hi)

@@ -1,0 +1,51 @@
+// Test harness: the device soft-float core (qblas_gb300/csrc/softquad.cuh)
+// compiled as plain host C++, so its bit patterns can be compared with the
+// host binary128 library on a machine without a GPU.
+#include <stdint.h>
+
+#include "../qblas_gb300/csrc/softquad.cuh"
+#include "../qblas_gb300/csrc/wacc.cuh"
+
+using qb::q128;
+
+extern "C" {
+void sq_fma_n(int64_t n, const q128* a, const q128* b, const q128* c, q128* out) {
+  for (int64_t i = 0; i < n; ++i) out[i] = qb::q_fma(a[i], b[i], c[i]);
+}
+void sq_mul_n(int64_t n, const q128* a, const q128* b, q128* out) {
+  for (int64_t i = 0; i < n; ++i) out[i] = qb::q_mul(a[i], b[i]);
+}
+void sq_add_n(int64_t n, const q128* a, const q128* b, q128* out) {
+  for (int64_t i = 0; i < n; ++i) out[i] = qb::q_add(a[i], b[i]);
+}
+void sq_sub_n(int64_t n, const q128* a, const q128* b, q128* out) {
+  for (int64_t i = 0; i < n; ++i) out[i] = qb::q_sub(a[i], b[i]);
+}
+void sq_sqrt_n(int64_t n, const q128* a, q128* out) {
+  for (int64_t i = 0; i < n; ++i) out[i] = qb::q_sqrt(a[i]);
+}
+void sq_from_double_n(int64_t n, const uint64_t* d, q128* out) {
+  for (int64_t i = 0; i < n; ++i) out[i] = qb::q_from_double_bits(d[i]);
+}
+void sq_to_double_n(int64_t n, const q128* a, uint64_t* out) {
+  for (int64_t i = 0; i < n; ++i) out[i] = qb::q_to_double_bits(a[i]);
+}
+// Dot product through the wide accumulator: the n terms are cut into
+// `nsplit` contiguous chunks, each accumulated separately, then merged in
+// order (the structure of the device reduction).
+void sq_wacc_dot(int64_t n, const q128* x, int64_t incx, const q128* y, int64_t incy, int64_t nsplit,
+                 q128* out) {
+  qb::wacc tot;
+  qb::wacc_init(tot);
+  if (nsplit < 1) nsplit = 1;
+  int64_t chunk = (n + nsplit - 1) / nsplit;
+  for (int64_t s = 0; s < nsplit; ++s) {
+    qb::wacc a;
+    qb::wacc_init(a);
+    for (int64_t i = s * chunk; i < n && i < (s + 1) * chunk; ++i)
+      qb::wacc_add_product(a, qb::qop_unpack(x[i * incx]), qb::qop_unpack(y[i * incy]));
+    qb::wacc_merge(tot, a);
+  }
+  *out = qb::wacc_round(tot);
+}
+}
