@@ -21,12 +21,12 @@ def epilogue(O, alpha, R, beta, yold):
     return O.fma(rep(alpha, n), R, O.mul(rep(beta, n), yold))
 
 
-def epilogue_bound(O, alpha, absum, beta, yold, kfac):
-    """kfac * 2^-113 * (|alpha| * sum|a b| + |beta y|) as a binary128 array,
-    with kfac folded into the returned 'absum' for oracle.bound_violations."""
+def epilogue_bound(O, alpha, absum, beta, yold):
+    """|alpha| * sum|a b| + |beta y| per output, the magnitude that the
+    reduction bound k * 2^-113 * (...) is taken of (oracle.bound_violations
+    applies the factor k * 2^-113)."""
     n = len(absum)
-    t = O.fma(rep(qabs(alpha), n), absum, qabs(O.mul(rep(beta, n), yold)))
-    return t
+    return O.fma(rep(qabs(alpha), n), absum, qabs(O.mul(rep(beta, n), yold)))
 
 
 def strided(a: np.ndarray, inc: int) -> np.ndarray:
