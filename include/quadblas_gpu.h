@@ -120,6 +120,25 @@ int quadblas_qgemm_dev(char layout, char transa, char transb, int64_t m, int64_t
                        const void *alpha, const void *dA, int64_t lda, const void *dB,
                        int64_t ldb, const void *beta, void *dC, int64_t ldc, void *stream);
 
+/* Capacity of quadblas_qdot_dev_noalloc's static scratch, in partial
+ * accumulators of 40 bytes (40 KiB). */
+#define QBLAS_NOALLOC_MAX_PARTIALS 1024
+
+/* No counterpart in the reference.  Same operation and result as
+ * quadblas_qdot_dev, for callers that cannot allocate device memory —
+ * programs whose device memory belongs to their own allocator or a fixed
+ * memory plan, and latency-sensitive loops that cannot call into the CUDA
+ * allocator — so it allocates nothing: its scratch is a static 40 KiB array
+ * that the library keeps on every GPU it is loaded on, until exit.  Any n
+ * fits on GPUs with up to 256 SMs; a problem that would need more than
+ * QBLAS_NOALLOC_MAX_PARTIALS partial accumulators returns
+ * QBLAS_ERR_INVALID_VALUE.  The first call on a device looks up the array's
+ * address (make that call before any stream capture).  All calls share the
+ * array: calls that overlap on the GPU race.  The status is reported by the
+ * return value only (quadblas_last_error is not updated). */
+int quadblas_qdot_dev_noalloc(int64_t n, const void *dx, int64_t incx, const void *dy,
+                              int64_t incy, void *d_result, void *stream);
+
 /* ---- Configuration and errors (no reference counterpart) -------------- */
 /* qgemm method: QBLAS_METHOD_AUTO, _SOFTFLOAT or _OZAKI. */
 int quadblas_set_method(int method);

@@ -40,6 +40,7 @@ _SIGS = {
     "quadblas_qaxpy_dev": (ci, [i64, vp, vp, i64, vp, i64, vp]),
     "quadblas_qgemv_dev": (ci, [cc, cc, i64, i64, vp, vp, i64, vp, i64, vp, vp, i64, vp]),
     "quadblas_qgemm_dev": (ci, [cc, cc, cc, i64, i64, i64, vp, vp, i64, vp, i64, vp, vp, i64, vp]),
+    "quadblas_qdot_dev_noalloc": (ci, [i64, vp, i64, vp, i64, vp, vp]),
     # configuration
     "quadblas_set_method": (ci, [ci]),
     "quadblas_get_method": (ci, []),
