@@ -276,6 +276,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="qgemm4096", choices=["qgemm4096", "qgemm512", "qgemv8192", "qdot26"])
+    ap.add_argument("--method", default="softfloat", choices=["softfloat", "ozaki"])
+    ap.add_argument("--slices", type=int, default=0)
     ap.add_argument("--no-secondary", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
@@ -292,9 +294,11 @@ def main():
         import torch.distributed as td
         td.init_process_group("nccl")
         dist = td
-    from qblas_gb300 import _lib
+    from qblas_gb300 import _lib, api
     _lib.load()
     pk, pk_src = peaks()
+    api.set_method(2 if args.method == "ozaki" else 1)
+    api.set_ozaki_slices(args.slices)
 
     wl = args.workload
     if wl.startswith("qgemm"):
@@ -316,7 +320,7 @@ def main():
         cfg = {"workload": f"qgemm m=n=k={size} row-major NN alpha=1 beta=0, entries u*2^e "
                            f"(u uniform [-1,1) full 113-bit significand, e uniform [-20,20])" if size == 4096 else
                            f"qgemm m=n=k={size} row-major NN alpha=1 beta=0, full-mantissa uniform [-1,1)",
-               "method": "softfloat", "l2": "inputs larger than L2 (no flush)" if size == 4096 else
+               "method": args.method, "l2": "inputs larger than L2 (no flush)" if size == 4096 else
                "inputs fit in L2; one launch per step", "parallelism": f"replicas x{world}"}
         dtype = "u32 (soft-float integer limbs)"
     elif wl == "qgemv8192":

@@ -143,7 +143,7 @@ int quadblas_qdot_dev_noalloc(int64_t n, const void *dx, int64_t incx, const voi
 /* qgemm method: QBLAS_METHOD_AUTO, _SOFTFLOAT or _OZAKI. */
 int quadblas_set_method(int method);
 int quadblas_get_method(void);
-/* Ozaki slice count (0 = automatic, else 2..32). */
+/* Ozaki digit (slice) count per operand: 0 = default (20), else 2..22. */
 int quadblas_set_ozaki_slices(int slices);
 int quadblas_get_ozaki_slices(void);
 /* Status of the calling thread's last call (part 1 calls record it too). */

@@ -15,6 +15,7 @@
 // outputs unchanged and record the error for quadblas_last_error()).
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <algorithm>
@@ -277,15 +278,59 @@ int dev_gemv(const GemvPlan& p0, const void* alpha, const void* dA, const void* 
   return cuda_status(e);
 }
 
+// qgemm method: quadblas_set_method(), else the QBLAS_METHOD environment
+// variable ("softfloat" / "ozaki"), else automatic (soft-float, which is
+// correctly rounded; Ozaki accuracy depends on the digit count).
+int gemm_method() {
+  int m = g_method.load();
+  if (m != 0) return m;
+  static int env = -1;
+  if (env < 0) {
+    const char* v = getenv("QBLAS_METHOD");
+    env = 1;
+    if (v && (strcmp(v, "ozaki") == 0 || strcmp(v, "2") == 0)) env = 2;
+  }
+  return env;
+}
+
+int gemm_digits() {
+  int s = g_slices.load();
+  if (s > 0) return s;
+  static int env = -1;
+  if (env < 0) {
+    const char* v = getenv("QBLAS_SLICES");
+    env = v ? atoi(v) : 0;
+    if (env < 2 || env > 22) env = 0;
+  }
+  return env ? env : qb::ozaki_default_digits();
+}
+
+size_t gemm_scratch_bytes(const GemmPlan& p) {
+  if (gemm_method() != 2) return 0;
+  return qb::ozaki_scratch_bytes(p.g.m, p.g.n, p.g.k, gemm_digits());
+}
+
 int dev_gemm(GemmPlan p, const void* alpha, const void* dA, const void* dB, const void* beta,
-             void* dC, cudaStream_t s) {
+             void* dC, cudaStream_t s, void* scratch_or_null) {
   if (!aligned16(dA) || !aligned16(dB) || !aligned16(dC)) return qb::kErrMisaligned;
   p.g.A = (const q128*)dA;
   p.g.B = (const q128*)dB;
   p.g.C = (q128*)dC;
   p.g.alpha = q_load(alpha);
   p.g.beta = q_load(beta);
-  return cuda_status(qb::launch_gemm_softfloat(p.g, s));
+  if (gemm_method() != 2) return cuda_status(qb::launch_gemm_softfloat(p.g, s));
+  size_t sb = gemm_scratch_bytes(p);
+  void* scratch = scratch_or_null;
+  if (!scratch) {
+    cudaError_t e = cudaMallocAsync(&scratch, sb, s);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return cuda_status(e);
+    }
+  }
+  cudaError_t e = qb::launch_gemm_ozaki(p.g, gemm_digits(), scratch, s);
+  if (!scratch_or_null) cudaFreeAsync(scratch, s);
+  return cuda_status(e);
 }
 
 // ---- host-pointer implementations --------------------------------------
@@ -369,13 +414,15 @@ int host_gemm(char layout, char transa, char transb, int64_t m, int64_t n, int64
   if (hc.status) return hc.status;
   DevState& st = *hc.st;
   if ((rc = ensure_slot(st, kSlotA, p.extA * 16)) || (rc = ensure_slot(st, kSlotB, p.extB * 16)) ||
-      (rc = ensure_slot(st, kSlotC, p.extC * 16)))
+      (rc = ensure_slot(st, kSlotC, p.extC * 16)) ||
+      (rc = ensure_slot(st, kSlotScratch, gemm_scratch_bytes(p))))
     return rc;
   if ((rc = h2d(st.buf[kSlotA], A, p.extA, st.stream)) ||
       (rc = h2d(st.buf[kSlotB], B, p.extB, st.stream)) ||
       (rc = h2d(st.buf[kSlotC], C, p.extC, st.stream)))
     return rc;
-  rc = dev_gemm(p, alpha, st.buf[kSlotA], st.buf[kSlotB], beta, st.buf[kSlotC], st.stream);
+  rc = dev_gemm(p, alpha, st.buf[kSlotA], st.buf[kSlotB], beta, st.buf[kSlotC], st.stream,
+                st.buf[kSlotScratch]);
   if (rc) return rc;
   if ((rc = d2h(C, st.buf[kSlotC], p.extC, st.stream))) return rc;
   return cuda_status(cudaStreamSynchronize(st.stream));
@@ -513,7 +560,7 @@ QBLAS_EXPORT int quadblas_qgemm_dev(char layout, char transa, char transb, int64
   if (rc) return fail(rc);
   if (m == 0 || n == 0 || k == 0) return fail(qb::kOk);
   if (!alpha || !beta) return fail(qb::kErrInvalidValue);
-  return fail(dev_gemm(p, alpha, dA, dB, beta, dC, (cudaStream_t)stream));
+  return fail(dev_gemm(p, alpha, dA, dB, beta, dC, (cudaStream_t)stream, nullptr));
 }
 
 // ===========================================================================
@@ -526,7 +573,7 @@ QBLAS_EXPORT int quadblas_set_method(int method) {
 }
 QBLAS_EXPORT int quadblas_get_method(void) { return g_method.load(); }
 QBLAS_EXPORT int quadblas_set_ozaki_slices(int slices) {
-  if (slices < 0 || slices > 32) return fail(qb::kErrInvalidValue);
+  if (slices < 0 || slices == 1 || slices > 22) return fail(qb::kErrInvalidValue);
   g_slices.store(slices);
   return fail(qb::kOk);
 }

@@ -58,7 +58,18 @@ struct GemmArgs {
 // C = fma(alpha, round(sum_l op(A)(i,l) op(B)(l,j)), beta * C), soft-float
 cudaError_t launch_gemm_softfloat(const GemmArgs& g, cudaStream_t s);
 
+// C = fma(alpha, round(sum), beta * C) with the sum from the Ozaki digit
+// split on the tensor cores (`digits` balanced 7-bit digits per operand).
+int ozaki_default_digits();
+size_t ozaki_scratch_bytes(int64_t m, int64_t n, int64_t k, int digits);
+size_t ozaki_error_flag_offset(int64_t m, int64_t n, int64_t k, int digits);
+cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, void* scratch, cudaStream_t s);
+
 // Multiprocessor count of the current device (cached).
 int device_sm_count();
+
+// Blocks of `kernel` (with `threads` threads and `smem` dynamic shared
+// memory) that fit on one multiprocessor of the current device.
+int resident_blocks_per_sm(const void* kernel, int threads, size_t smem);
 
 }  // namespace qb

@@ -30,17 +30,19 @@ int device_sm_count() {
   return cached[dev];
 }
 
-static int64_t dot_blocks(int64_t n) {
-  int64_t per_block = (int64_t)kDotThreads * 4;  // at least 4 terms per thread
-  int64_t want = (n + per_block - 1) / per_block;
-  int64_t cap = (int64_t)device_sm_count() * kDotBlocksPerSm;
-  if (want < 1) want = 1;
-  return want < cap ? want : cap;
+int resident_blocks_per_sm(const void* kernel, int threads, size_t smem) {
+  int nb = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, threads, smem) != cudaSuccess ||
+      nb < 1) {
+    cudaGetLastError();
+    nb = 1;
+  }
+  return nb;
 }
 
-size_t dot_scratch_bytes(int64_t n) { return (size_t)dot_blocks(n) * sizeof(wacc); }
 
-__global__ void __launch_bounds__(kDotThreads)
+
+__global__ void __launch_bounds__(kDotThreads, 4)
     qdot_partial_kernel(int64_t n, const q128* __restrict__ x, int64_t incx,
                         const q128* __restrict__ y, int64_t incy, wacc* __restrict__ partials) {
   __shared__ wacc sm[kDotThreads / 32];
@@ -81,6 +83,26 @@ __global__ void __launch_bounds__(kDotThreads)
     *out = r;
   }
 }
+
+// One wave of resident blocks (no tail wave), fewer for short vectors.
+static int64_t dot_blocks(int64_t n) {
+  static int cached[64] = {0};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  int per_sm = kDotBlocksPerSm;
+  if (dev >= 0 && dev < 64) {
+    if (!cached[dev])
+      cached[dev] = resident_blocks_per_sm((const void*)qdot_partial_kernel, kDotThreads, 0);
+    per_sm = cached[dev] < kDotBlocksPerSm ? cached[dev] : kDotBlocksPerSm;
+  }
+  int64_t per_block = (int64_t)kDotThreads * 4;  // at least 4 terms per thread
+  int64_t want = (n + per_block - 1) / per_block;
+  int64_t cap = (int64_t)device_sm_count() * per_sm;
+  if (want < 1) want = 1;
+  return want < cap ? want : cap;
+}
+
+size_t dot_scratch_bytes(int64_t n) { return (size_t)dot_blocks(n) * sizeof(wacc); }
 
 __global__ void qzero_kernel(q128* out, int take_sqrt) {
   (void)take_sqrt;

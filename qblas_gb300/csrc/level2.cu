@@ -7,10 +7,14 @@
 // y_i = fma(alpha, sum, beta * y_i) (level2.hpp:48; test_quadblas.cpp:172),
 // so given the rounded sum the epilogue is bit-identical to the reference.
 //
+// x is unpacked once per call into scratch (significand at bit 127,
+// exponent, sign and class), since every element of x is used m times.
 // Two memory layouts of op(A):
-//  * rows contiguous (row-major, or column-major with trans): one warp per
-//    row; lanes read consecutive 16-byte elements of the row (512 B per
-//    warp per step) and x through the read-only cache.
+//  * rows contiguous (row-major, or column-major with trans): a row is
+//    shared by 1, 2, 4 or 8 warps of a 256-thread block (more warps for
+//    longer rows); lanes read consecutive 16-byte elements (512 B per warp
+//    per step) and the warps' accumulators are merged in shared memory in a
+//    fixed order.  One block per 8/wpr rows keeps the grid fine-grained.
 //  * columns contiguous (column-major, or row-major with trans): one thread
 //    per row, so a warp reads 32 consecutive elements of a column; the
 //    columns are split into chunks over blockIdx.y to fill the GPU, each
@@ -21,53 +25,86 @@
 
 namespace qb {
 
-constexpr int kRowWarps = 8;  // warps per block of the row kernel
-
 __device__ __forceinline__ q128 gemv_epilogue(q128 alpha, q128 sum, q128 beta, q128 yv) {
   return q_fma(alpha, sum, q_mul(beta, yv));
 }
 
-__global__ void __launch_bounds__(kRowWarps * 32)
-    qgemv_rows_kernel(int64_t m, int64_t n, const q128* __restrict__ A, int64_t lda,
-                      const q128* __restrict__ x, int64_t incx, q128 alpha, q128 beta,
-                      q128* __restrict__ y, int64_t incy) {
-  const int lane = threadIdx.x & 31;
-  const int64_t warp0 = (int64_t)blockIdx.x * kRowWarps + (threadIdx.x >> 5);
-  const int64_t nwarps = (int64_t)gridDim.x * kRowWarps;
-  for (int64_t row = warp0; row < m; row += nwarps) {
-    const q128* Ar = A + row * lda;
-    wacc acc;
-    wacc_init(acc);
-    int64_t j = lane;
-    for (; j + 96 < n; j += 128) {
-      q128 a0 = ld_stream(Ar + j), a1 = ld_stream(Ar + j + 32);
-      q128 a2 = ld_stream(Ar + j + 64), a3 = ld_stream(Ar + j + 96);
-      q128 x0 = ld_cached(x + j * incx), x1 = ld_cached(x + (j + 32) * incx);
-      q128 x2 = ld_cached(x + (j + 64) * incx), x3 = ld_cached(x + (j + 96) * incx);
-      wacc_add_product(acc, qop_unpack(a0), qop_unpack(x0));
-      wacc_add_product(acc, qop_unpack(a1), qop_unpack(x1));
-      wacc_add_product(acc, qop_unpack(a2), qop_unpack(x2));
-      wacc_add_product(acc, qop_unpack(a3), qop_unpack(x3));
-    }
-    for (; j < n; j += 32)
-      wacc_add_product(acc, qop_unpack(ld_stream(Ar + j)), qop_unpack(ld_cached(x + j * incx)));
-    wacc_warp_reduce(acc);
-    if (lane == 0) {
-      q128* yp = y + row * incy;
-      *yp = gemv_epilogue(alpha, wacc_round(acc), beta, *yp);
-    }
+// ---- x unpacked once -------------------------------------------------------
+__global__ void qop_unpack_kernel(int64_t n, const q128* __restrict__ x, int64_t incx,
+                                  uint4* __restrict__ xm, int2* __restrict__ xe) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    qop o = qop_unpack(ld_cached(x + i * incx));
+    xm[i] = make_uint4(o.m0, o.m1, o.m2, o.m3);
+    xe[i] = make_int2(o.e, (int)(o.s | (o.cls << 1)));
   }
 }
 
+__device__ __forceinline__ qop qop_fetch(const uint4* __restrict__ xm, const int2* __restrict__ xe,
+                                         int64_t i) {
+  uint4 m = __ldg(xm + i);
+  int2 e = __ldg(xe + i);
+  qop o;
+  o.m0 = m.x;
+  o.m1 = m.y;
+  o.m2 = m.z;
+  o.m3 = m.w;
+  o.e = e.x;
+  o.s = (uint32_t)e.y & 1u;
+  o.cls = (uint32_t)e.y >> 1;
+  return o;
+}
+
+// ---- rows contiguous ------------------------------------------------------
+constexpr int kRowThreads = 256;
+
+__global__ void __launch_bounds__(kRowThreads, 4)
+    qgemv_rows_kernel(int64_t m, int64_t n, const q128* __restrict__ A, int64_t lda,
+                      const uint4* __restrict__ xm, const int2* __restrict__ xe, int wpr_log2,
+                      q128 alpha, q128 beta, q128* __restrict__ y, int64_t incy) {
+  __shared__ wacc sm[kRowThreads / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int wpr = 1 << wpr_log2;
+  const int sub = warp & (wpr - 1);
+  const int64_t row = (int64_t)blockIdx.x * ((kRowThreads / 32) >> wpr_log2) + (warp >> wpr_log2);
+  wacc acc;
+  wacc_init(acc);
+  if (row < m) {
+    const q128* Ar = A + row * lda;
+    const int64_t step = 32 * (int64_t)wpr;
+    int64_t j = (int64_t)sub * 32 + lane;
+    for (; j + 3 * step < n; j += 4 * step) {
+      q128 a0 = ld_stream(Ar + j), a1 = ld_stream(Ar + j + step);
+      q128 a2 = ld_stream(Ar + j + 2 * step), a3 = ld_stream(Ar + j + 3 * step);
+      wacc_add_product(acc, qop_unpack(a0), qop_fetch(xm, xe, j));
+      wacc_add_product(acc, qop_unpack(a1), qop_fetch(xm, xe, j + step));
+      wacc_add_product(acc, qop_unpack(a2), qop_fetch(xm, xe, j + 2 * step));
+      wacc_add_product(acc, qop_unpack(a3), qop_fetch(xm, xe, j + 3 * step));
+    }
+    for (; j < n; j += step) wacc_add_product(acc, qop_unpack(ld_stream(Ar + j)), qop_fetch(xm, xe, j));
+  }
+  wacc_warp_reduce(acc);
+  if (lane == 0) sm[warp] = acc;
+  __syncthreads();
+  if (lane == 0 && sub == 0 && row < m) {
+    wacc a = sm[warp];
+    for (int k = 1; k < wpr; ++k) wacc_merge(a, sm[warp + k]);
+    q128* yp = y + row * incy;
+    *yp = gemv_epilogue(alpha, wacc_round(a), beta, *yp);
+  }
+}
+
+// ---- columns contiguous ---------------------------------------------------
 constexpr int kColThreads = 128;
 
 // Partial sums over columns [chunk*jc, min(n, (chunk+1)*jc)) for rows
-// i = blockIdx.x*128 + threadIdx.x.  With nchunks == 1 the epilogue is
-// applied directly; otherwise partials[chunk * m + i] is written.
+// i = blockIdx.x*128 + threadIdx.x.  With one chunk the epilogue is applied
+// directly; otherwise partials[chunk * m + i] is written.
 __global__ void __launch_bounds__(kColThreads)
     qgemv_cols_kernel(int64_t m, int64_t n, const q128* __restrict__ A, int64_t lda,
-                      const q128* __restrict__ x, int64_t incx, int64_t jc, q128 alpha, q128 beta,
-                      q128* __restrict__ y, int64_t incy, wacc* __restrict__ partials) {
+                      const uint4* __restrict__ xm, const int2* __restrict__ xe, int64_t jc,
+                      q128 alpha, q128 beta, q128* __restrict__ y, int64_t incy,
+                      wacc* __restrict__ partials) {
   const int64_t i = (int64_t)blockIdx.x * kColThreads + threadIdx.x;
   const int64_t chunk = blockIdx.y;
   int64_t j0 = chunk * jc, j1 = j0 + jc;
@@ -79,15 +116,12 @@ __global__ void __launch_bounds__(kColThreads)
   for (; j + 3 < j1; j += 4) {
     q128 a0 = ld_stream(A + j * lda + i), a1 = ld_stream(A + (j + 1) * lda + i);
     q128 a2 = ld_stream(A + (j + 2) * lda + i), a3 = ld_stream(A + (j + 3) * lda + i);
-    q128 x0 = ld_cached(x + j * incx), x1 = ld_cached(x + (j + 1) * incx);
-    q128 x2 = ld_cached(x + (j + 2) * incx), x3 = ld_cached(x + (j + 3) * incx);
-    wacc_add_product(acc, qop_unpack(a0), qop_unpack(x0));
-    wacc_add_product(acc, qop_unpack(a1), qop_unpack(x1));
-    wacc_add_product(acc, qop_unpack(a2), qop_unpack(x2));
-    wacc_add_product(acc, qop_unpack(a3), qop_unpack(x3));
+    wacc_add_product(acc, qop_unpack(a0), qop_fetch(xm, xe, j));
+    wacc_add_product(acc, qop_unpack(a1), qop_fetch(xm, xe, j + 1));
+    wacc_add_product(acc, qop_unpack(a2), qop_fetch(xm, xe, j + 2));
+    wacc_add_product(acc, qop_unpack(a3), qop_fetch(xm, xe, j + 3));
   }
-  for (; j < j1; ++j)
-    wacc_add_product(acc, qop_unpack(ld_stream(A + j * lda + i)), qop_unpack(ld_cached(x + j * incx)));
+  for (; j < j1; ++j) wacc_add_product(acc, qop_unpack(ld_stream(A + j * lda + i)), qop_fetch(xm, xe, j));
   if (gridDim.y == 1) {
     q128* yp = y + i * incy;
     *yp = gemv_epilogue(alpha, wacc_round(acc), beta, *yp);
@@ -118,33 +152,54 @@ static int64_t col_chunks(int64_t m, int64_t n) {
   return c;
 }
 
+static size_t round256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+// Scratch: [x significands: 16n][x exponents: 8n] (+ column partials)
 size_t gemv_scratch_bytes(int64_t m, int64_t n, MatView A) {
-  if (A.sj == 1 || m <= 0 || n <= 0) return 0;
+  if (m <= 0 || n <= 0) return 0;
+  size_t xs = round256((size_t)n * 16) + round256((size_t)n * 8);
+  if (A.sj == 1) return xs;
   int64_t c = col_chunks(m, n);
-  return c > 1 ? (size_t)c * (size_t)m * sizeof(wacc) : 0;
+  return xs + (c > 1 ? (size_t)c * (size_t)m * sizeof(wacc) : 0);
+}
+
+// Warps per row: enough lanes that each has at least 64 terms.
+static int rows_wpr_log2(int64_t n) {
+  int l = 0;
+  while (l < 3 && n >= (int64_t)(32 << (l + 1)) * 64) ++l;
+  return l;
 }
 
 cudaError_t launch_gemv(int64_t m, int64_t n, q128 alpha, MatView A, const q128* x, int64_t incx,
                         q128 beta, q128* y, int64_t incy, void* scratch, cudaStream_t s) {
   if (m <= 0) return cudaSuccess;
-  if (n <= 0) {
-    // The reference returns without touching y when n == 0 (level2.hpp:21,61).
-    return cudaSuccess;
+  if (n <= 0) return cudaSuccess;  // the reference leaves y untouched (level2.hpp:21,61)
+  char* base = static_cast<char*>(scratch);
+  uint4* xm = reinterpret_cast<uint4*>(base);
+  int2* xe = reinterpret_cast<int2*>(base + round256((size_t)n * 16));
+  {
+    int64_t nb = (n + 255) / 256;
+    int64_t cap = (int64_t)device_sm_count() * 4;
+    qop_unpack_kernel<<<(unsigned)(nb < cap ? nb : cap), 256, 0, s>>>(n, x, incx, xm, xe);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
   }
   if (A.sj == 1) {
-    int64_t want = (m + kRowWarps - 1) / kRowWarps;
-    int64_t cap = (int64_t)device_sm_count() * 8;
-    int64_t nb = want < cap ? want : cap;
-    qgemv_rows_kernel<<<(unsigned)nb, kRowWarps * 32, 0, s>>>(m, n, A.p, A.si, x, incx, alpha, beta,
-                                                              y, incy);
+    int l = rows_wpr_log2(n);
+    int64_t rows_per_block = (kRowThreads / 32) >> l;
+    int64_t nb = (m + rows_per_block - 1) / rows_per_block;
+    if (nb > 0x7fffffff) return cudaErrorInvalidConfiguration;
+    qgemv_rows_kernel<<<(unsigned)nb, kRowThreads, 0, s>>>(m, n, A.p, A.si, xm, xe, l, alpha, beta,
+                                                           y, incy);
     return cudaGetLastError();
   }
   int64_t c = col_chunks(m, n);
   int64_t jc = (n + c - 1) / c;
   c = (n + jc - 1) / jc;
   dim3 grid((unsigned)((m + kColThreads - 1) / kColThreads), (unsigned)c);
-  wacc* partials = static_cast<wacc*>(scratch);
-  qgemv_cols_kernel<<<grid, kColThreads, 0, s>>>(m, n, A.p, A.sj, x, incx, jc, alpha, beta, y, incy,
+  size_t xs = round256((size_t)n * 16) + round256((size_t)n * 8);
+  wacc* partials = reinterpret_cast<wacc*>(base + xs);
+  qgemv_cols_kernel<<<grid, kColThreads, 0, s>>>(m, n, A.p, A.sj, xm, xe, jc, alpha, beta, y, incy,
                                                  partials);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess || c == 1) return e;

@@ -1,0 +1,650 @@
+// Ozaki-split qgemm on the 5th-generation tensor cores (tcgen05, sm_103a).
+//
+// Replaces the reference's soft-float GEMM loops
+// (include/quadblas/algorithms/level3.hpp:17-336) by an error-free integer
+// splitting (ozaki.cuh): each row of op(A) and column of op(B) is cut into s
+// signed 7-bit digits stored as bf16, every digit pair (t, u) is an exact
+// bf16 x bf16 -> fp32 GEMM on tcgen05.mma kind::f16 (sums <= 2^24 stay
+// exact; k is processed in chunks of 4096), the pairs of one diagonal
+// g = t + u are summed exactly in int32, and a fold kernel combines the
+// diagonals into a 192-bit integer per output that is rounded once to
+// binary128 and passed through the reference epilogue
+// C = fma(alpha, sum, beta * C) (level3.hpp:107).
+//
+// tcgen05 kind::i8 does not exist on sm_103a, so integer digits travel as
+// bf16 (|d| <= 64 is exact) with fp32 accumulation in tensor memory.
+//
+// Kernels:
+//   ozaki_scale_kernel  : S_i = max_l (exponent(x_il) + 1) per row of a
+//                         strided view (A, or B^T), plus NaN/inf flags
+//   ozaki_split_kernel  : digits of every element, written digit-major and
+//                         K-major: D[t][row][l] (bf16), zero padded
+//   ozaki_mma_kernel    : persistent, warp-specialised: warp 0 issues TMA
+//                         loads (128B-swizzled 64-wide K slices of A_t and
+//                         B_u) into a 4-stage shared-memory ring, warp 1
+//                         issues tcgen05.mma (M=128, N=256, K=16) into one
+//                         of two 256-column fp32 accumulators in tensor
+//                         memory, warps 2..9 read the accumulators with
+//                         tcgen05.ld, convert to int32 and sum a diagonal
+//                         in registers, then store C_g[row][col] (int32).
+//                         Every mbarrier wait is bounded (1 s); on timeout
+//                         the kernel records an error, drains its own
+//                         copies and MMAs, frees tensor memory and exits.
+//   ozaki_fold_kernel   : Horner fold of C_0..C_G (and k passes) per output,
+//                         one rounding, reference epilogue; rows/columns that
+//                         hold NaN or inf are computed by a direct wide-
+//                         accumulator dot instead, so specials keep IEEE
+//                         semantics.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "kernels.h"
+#include "ozaki.cuh"
+#include "reduce.cuh"
+
+namespace qb {
+
+// ---------------------------------------------------------------------------
+// Scaling and splitting
+// ---------------------------------------------------------------------------
+// One thread per (row, chunk of 64 columns) of the view X(r, c) = p[r*sr + c*sc].
+__global__ void ozaki_scale_kernel(int64_t rows, int64_t cols, const q128* __restrict__ p,
+                                   int64_t sr, int64_t sc, int* __restrict__ S,
+                                   uint32_t* __restrict__ flags) {
+  const int64_t nchunk = (cols + 63) / 64;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < rows * nchunk; w += stride) {
+    int64_t r, ch;
+    if (sr == 1) {  // rows contiguous in memory: consecutive threads take consecutive rows
+      r = w % rows;
+      ch = w / rows;
+    } else {
+      r = w / nchunk;
+      ch = w % nchunk;
+    }
+    int64_t c0 = ch * 64, c1 = c0 + 64 < cols ? c0 + 64 : cols;
+    int mx = kOzakiScaleEmpty;
+    uint32_t fl = 0;
+    for (int64_t c = c0; c < c1; ++c) {
+      q128 v = ld_cached(p + r * sr + c * sc);
+      int e = ozaki_exp_plus1(v);
+      mx = e > mx ? e : mx;
+      fl |= ozaki_special_flags(v);
+    }
+    if (mx != kOzakiScaleEmpty) atomicMax(S + r, mx);
+    if (fl) atomicOr(flags + r, fl);
+  }
+}
+
+__global__ void ozaki_fill_kernel(int64_t n, int* __restrict__ S, uint32_t* __restrict__ flags) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    S[i] = kOzakiScaleEmpty;
+    flags[i] = 0u;
+  }
+}
+
+// Digits of the (rows_pad x cols_pad) zero-padded view into
+// D[t * rows_pad * cols_pad + r * cols_pad + c] (bf16).  Block (32, 8):
+// x along columns (coalesced digit stores), y along rows.
+__global__ void __launch_bounds__(256)
+    ozaki_split_kernel(int64_t rows, int64_t cols, int64_t rows_pad, int64_t cols_pad,
+                       const q128* __restrict__ p, int64_t sr, int64_t sc,
+                       const int* __restrict__ S, int s, __nv_bfloat16* __restrict__ D) {
+  const int64_t c = (int64_t)blockIdx.x * 32 + threadIdx.x;
+  const int64_t r = (int64_t)blockIdx.y * 8 + threadIdx.y;
+  if (c >= cols_pad || r >= rows_pad) return;
+  int dg[kOzakiMaxDigits];
+  if (r < rows && c < cols) {
+    ozaki_digits(ld_cached(p + r * sr + c * sc), S[r], s, dg);
+  } else {
+#pragma unroll
+    for (int t = 0; t < kOzakiMaxDigits; ++t) dg[t] = 0;
+  }
+  const int64_t plane = rows_pad * cols_pad;
+  __nv_bfloat16* out = D + r * cols_pad + c;
+#pragma unroll
+  for (int t = 0; t < kOzakiMaxDigits; ++t)
+    if (t < s) out[t * plane] = __int2bfloat16_rn(dg[t]);
+}
+
+// ---------------------------------------------------------------------------
+// tcgen05 digit GEMM
+// ---------------------------------------------------------------------------
+constexpr int kBM = 128, kBN = 256, kBK = 64;  // tile; kBK bf16 = 128 bytes per row
+constexpr int kStages = 4;
+constexpr int kStageA = kBM * kBK * 2;          // 16 KiB
+constexpr int kStageB = kBN * kBK * 2;          // 32 KiB
+constexpr int kStageBytes = kStageA + kStageB;  // 48 KiB
+constexpr int kMmaThreads = 320;                // 10 warps
+constexpr int kEpiWarps = 8;
+constexpr int kTmemCols = 512;                  // two 256-column fp32 accumulators
+constexpr int kExactChunkKB = 4096 / kBK;       // k-blocks summed exactly in fp32
+constexpr size_t kMmaSmem = (size_t)kStages * kStageBytes + 1024 + 256;
+constexpr unsigned long long kWaitLimitNs = 1000000000ull;  // 1 s per wait
+
+struct OzakiMmaParams {
+  int tiles_m, tiles_n;
+  int G;         // highest diagonal (s - 1)
+  int m_pad, n_pad;
+  int kb_begin, kb_end;  // k-blocks of this pass
+  int32_t* C;            // [G+1][m_pad][n_pad]
+  int* err;              // set to nonzero on a timeout
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ unsigned long long global_timer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait for the phase with the given parity to complete.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+  if (mbar_try(bar, parity)) return true;
+  unsigned long long t0 = global_timer();
+  while (true) {
+    if (mbar_try(bar, parity)) return true;
+    if (global_timer() - t0 > kWaitLimitNs) return false;
+  }
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, uint32_t bar,
+                                            int c0, int c1) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%3, %4}], [%2];" ::"r"(dst),
+      "l"((unsigned long long)map), "r"(bar), "r"(c0), "r"(c1)
+      : "memory");
+}
+
+// Shared-memory matrix descriptor: K-major, 128-byte swizzle, rows of 128
+// bytes, 8-row groups 1024 bytes apart (SBO), descriptor version 1.
+__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t addr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((addr & 0x3FFFFu) >> 4);        // start address
+  d |= (uint64_t)1 << 16;                          // leading byte offset (unused for swizzled K-major)
+  d |= (uint64_t)(1024 >> 4) << 32;                // stride byte offset
+  d |= (uint64_t)1 << 46;                          // version
+  d |= (uint64_t)2 << 61;                          // 128-byte swizzle
+  return d;
+}
+
+// Instruction descriptor: kind::f16, A = B = bf16, D = f32, K-major A and B,
+// N = 256, M = 128.
+constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kBN >> 3) << 17) |
+                            ((uint32_t)(kBM >> 4) << 24);
+
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t accum) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
+      "l"(a), "l"(b), "r"(kIdesc), "r"(accum)
+      : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+      : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+      "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+      "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
+        "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
+        "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+__global__ void __launch_bounds__(kMmaThreads, 1)
+    ozaki_mma_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                     OzakiMmaParams P) {
+  extern __shared__ uint8_t smem_raw[];
+  const uint32_t raw = smem_u32(smem_raw);
+  const uint32_t base = (raw + 1023u) & ~1023u;  // 128B swizzle needs 1024-byte alignment
+  uint8_t* gbase = smem_raw + (base - raw);
+  // barriers and the tensor-memory address live after the stages
+  const uint32_t bar0 = base + kStages * kStageBytes;
+  auto full_bar = [&](int s) { return bar0 + 8u * s; };
+  auto empty_bar = [&](int s) { return bar0 + 8u * (kStages + s); };
+  auto tfull_bar = [&](int b) { return bar0 + 8u * (2 * kStages + b); };
+  auto tempty_bar = [&](int b) { return bar0 + 8u * (2 * kStages + 2 + b); };
+  const uint32_t drain_bar = bar0 + 8u * (2 * kStages + 4);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(gbase + kStages * kStageBytes + 8 * (2 * kStages + 5));
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kStages; ++s) {
+      mbar_init(full_bar(s), 1);
+      mbar_init(empty_bar(s), 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(tfull_bar(b), 1);
+      mbar_init(tempty_bar(b), kEpiWarps);
+    }
+    mbar_init(drain_bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(tmem_slot)),
+                 "r"(kTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+
+  const int tiles = P.tiles_m * P.tiles_n;
+  const int units = (P.G + 1) * tiles;
+  const int nkb = P.kb_end - P.kb_begin;
+  const int nchunks = (nkb + kExactChunkKB - 1) / kExactChunkKB;
+  bool ok = true;
+
+  if (warp == 0) {
+    // ---------------- TMA producer ----------------
+    if (lane == 0) {
+      uint32_t it = 0;
+      for (int unit = blockIdx.x; unit < units && ok; unit += gridDim.x) {
+        const int g = P.G - unit / tiles, tile = unit % tiles;
+        const int tm = tile / P.tiles_n, tn = tile % P.tiles_n;
+        for (int t = 0; t <= g && ok; ++t) {
+          const int u = g - t;
+          for (int kb = P.kb_begin; kb < P.kb_end && ok; ++kb, ++it) {
+            const int s = it % kStages;
+            const uint32_t round = it / kStages;
+            if (!mbar_wait(empty_bar(s), (round & 1u) ^ 1u)) {
+              ok = false;
+              break;
+            }
+            mbar_expect_tx(full_bar(s), kStageBytes);
+            const uint32_t sa = base + s * kStageBytes, sb = sa + kStageA;
+            tma_load_2d(sa, &tmA, full_bar(s), kb * kBK, t * P.m_pad + tm * kBM);
+            tma_load_2d(sb, &tmB, full_bar(s), kb * kBK, u * P.n_pad + tn * kBN);
+          }
+        }
+      }
+      if (!ok) {
+        atomicExch(P.err, 1);
+        // drain the copies still in flight: the last kStages issued fills
+        for (uint32_t j = (it > kStages ? it - kStages : 0); j < it; ++j)
+          mbar_wait(full_bar(j % kStages), (j / kStages) & 1u);
+      }
+    }
+  } else if (warp == 1) {
+    // ---------------- MMA issuer ----------------
+    if (lane == 0) {
+      uint32_t it = 0, acc_it = 0;
+      bool issued_any = false;
+      for (int unit = blockIdx.x; unit < units && ok; unit += gridDim.x) {
+        const int g = P.G - unit / tiles;
+        for (int t = 0; t <= g && ok; ++t) {
+          for (int ch = 0; ch < nchunks && ok; ++ch) {
+            const int kb0 = P.kb_begin + ch * kExactChunkKB;
+            const int kb1 = kb0 + kExactChunkKB < P.kb_end ? kb0 + kExactChunkKB : P.kb_end;
+            const int buf = acc_it & 1;
+            const uint32_t round = acc_it >> 1;
+            if (!mbar_wait(tempty_bar(buf), (round & 1u) ^ 1u)) {
+              ok = false;
+              break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t dcol = tmem + (uint32_t)(buf * kBN);
+            for (int kb = kb0; kb < kb1; ++kb, ++it) {
+              const int s = it % kStages;
+              if (!mbar_wait(full_bar(s), (it / kStages) & 1u)) {
+                ok = false;
+                break;
+              }
+              asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+              const uint32_t sa = base + s * kStageBytes, sb = sa + kStageA;
+              const uint64_t da = smem_desc_sw128(sa), db = smem_desc_sw128(sb);
+#pragma unroll
+              for (int k = 0; k < kBK / 16; ++k) {
+                // +32 bytes per K=16 step inside the 128-byte swizzled row
+                mma_bf16(dcol, da + (uint64_t)(2 * k), db + (uint64_t)(2 * k),
+                         (kb > kb0 || k > 0) ? 1u : 0u);
+              }
+              issued_any = true;
+              mma_commit(empty_bar(s));
+            }
+            if (!ok) break;
+            mma_commit(tfull_bar(buf));
+            ++acc_it;
+          }
+        }
+      }
+      if (!ok) {
+        atomicExch(P.err, 1);
+        if (issued_any) {
+          mma_commit(drain_bar);
+          mbar_wait(drain_bar, 0);
+        }
+      }
+    }
+  } else {
+    // ---------------- epilogue: 8 warps ----------------
+    const int e = warp - 2;
+    const int quad = warp & 3;           // tensor-memory lane quadrant of this warp
+    const int half = e >> 2;             // column half: [0,128) or [128,256)
+    const int row_in_tile = quad * 32 + lane;
+    int32_t acc[kBN / 2];
+#pragma unroll
+    for (int i = 0; i < kBN / 2; ++i) acc[i] = 0;
+    uint32_t acc_it = 0;
+    for (int unit = blockIdx.x; unit < units && ok; unit += gridDim.x) {
+      const int g = P.G - unit / tiles, tile = unit % tiles;
+      const int tm = tile / P.tiles_n, tn = tile % P.tiles_n;
+      for (int t = 0; t <= g && ok; ++t) {
+        for (int ch = 0; ch < nchunks && ok; ++ch) {
+          const int buf = acc_it & 1;
+          if (!mbar_wait(tfull_bar(buf), (acc_it >> 1) & 1u)) {
+            ok = false;
+            break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          const uint32_t taddr =
+              tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(buf * kBN + half * (kBN / 2));
+#pragma unroll
+          for (int c = 0; c < kBN / 2; c += 32) {
+            uint32_t r[32];
+            tmem_ld32(taddr + (uint32_t)c, r);
+#pragma unroll
+            for (int i = 0; i < 32; ++i) acc[c + i] += __float2int_rn(__uint_as_float(r[i]));
+          }
+          asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+          __syncwarp();
+          if (lane == 0) mbar_arrive(tempty_bar(buf));
+          ++acc_it;
+        }
+      }
+      if (!ok) break;
+      // store diagonal g of this tile: row (tm*128 + row_in_tile), 128 columns
+      int32_t* dst = P.C + ((size_t)g * P.m_pad + (size_t)tm * kBM + row_in_tile) * P.n_pad +
+                     (size_t)tn * kBN + half * (kBN / 2);
+#pragma unroll
+      for (int i = 0; i < kBN / 2; i += 4) {
+        *reinterpret_cast<int4*>(dst + i) = make_int4(acc[i], acc[i + 1], acc[i + 2], acc[i + 3]);
+        acc[i] = acc[i + 1] = acc[i + 2] = acc[i + 3] = 0;
+      }
+    }
+    if (!ok && lane == 0) atomicExch(P.err, 1);
+  }
+
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (warp == 1) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols)
+                 : "memory");
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Fold
+// ---------------------------------------------------------------------------
+struct OzakiFoldParams {
+  int64_t m, n, k;
+  int G, npass;
+  int64_t m_pad, n_pad;
+  const int32_t* C;      // [npass][G+1][m_pad][n_pad]
+  const int* S;          // row scales of op(A)
+  const int* F;          // column scales of op(B)
+  const uint32_t* fa;    // row special flags
+  const uint32_t* fb;    // column special flags
+  const q128* A;
+  int64_t sai, sal;
+  const q128* B;
+  int64_t sbl, sbj;
+  q128* Cout;
+  int64_t sci, scj;
+  q128 alpha, beta;
+  const int* err;
+};
+
+__global__ void __launch_bounds__(256) ozaki_fold_kernel(OzakiFoldParams P) {
+  const int64_t j = (int64_t)blockIdx.x * 32 + threadIdx.x;
+  const int64_t i = (int64_t)blockIdx.y * 8 + threadIdx.y;
+  if (i >= P.m || j >= P.n) return;
+  q128 sum;
+  if (*P.err) {
+    sum = q_nan();
+  } else if (P.fa[i] | P.fb[j]) {
+    // a NaN or infinity in row i or column j: direct wide-accumulator dot
+    wacc acc;
+    wacc_init(acc);
+    for (int64_t l = 0; l < P.k; ++l)
+      wacc_add_product(acc, qop_unpack(ld_cached(P.A + i * P.sai + l * P.sal)),
+                       qop_unpack(ld_cached(P.B + l * P.sbl + j * P.sbj)));
+    sum = wacc_round(acc);
+  } else {
+    fold192 f;
+    fold_init(f);
+    const size_t plane = (size_t)P.m_pad * P.n_pad;
+    const size_t off = (size_t)i * P.n_pad + j;
+    // Horner over diagonals, most significant first; k passes add up
+    for (int g = 0; g <= P.G; ++g) {
+      int64_t v = 0;
+      for (int p = 0; p < P.npass; ++p) v += P.C[((size_t)p * (P.G + 1) + g) * plane + off];
+      fold_step(f, v);
+    }
+    sum = fold_round(f, ozaki_fold_exp(P.S[i], P.F[j], P.G));
+  }
+  q128* cp = P.Cout + i * P.sci + j * P.scj;
+  *cp = q_fma(P.alpha, sum, q_mul(P.beta, *cp));
+}
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                  const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                  const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_fn() {
+  static EncodeTiledFn fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (EncodeTiledFn)p;
+    else
+      cudaGetLastError();
+  }
+  return fn;
+}
+
+// 2-D bf16 tensor map over D[rows][cols] with a (64 x box_rows) box, 128B swizzle.
+static bool make_map(CUtensorMap* map, const void* D, int64_t rows, int64_t cols, int box_rows) {
+  EncodeTiledFn fn = encode_fn();
+  if (!fn) return false;
+  cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)cols * 2};
+  cuuint32_t box[2] = {(cuuint32_t)kBK, (cuuint32_t)box_rows};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(D), dims, strides, box,
+                  estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
+static int64_t rup(int64_t v, int64_t a) { return (v + a - 1) / a * a; }
+static size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+// k-blocks per pass: diagonals hold at most s pairs, each pair adds at most
+// ceil(kb / 64) exact chunks of |sum| <= 2^24, and the int32 sum must stay
+// below 2^31.
+static int pass_kblocks(int s) {
+  int chunks = (int)(((1ll << 31) - 1) / ((int64_t)s << 24));  // exact chunks per pass
+  if (chunks < 1) chunks = 1;
+  return chunks * kExactChunkKB;
+}
+
+struct OzakiLayout {
+  int64_t m_pad, n_pad, k_pad;
+  int s, G, npass;
+  size_t off_S, off_F, off_fa, off_fb, off_err, off_DA, off_DB, off_C, total;
+};
+
+static OzakiLayout ozaki_layout(int64_t m, int64_t n, int64_t k, int s) {
+  OzakiLayout L;
+  L.s = s;
+  L.G = s - 1;
+  L.m_pad = rup(m, kBM);
+  L.n_pad = rup(n, kBN);
+  L.k_pad = rup(k, kBK);
+  int64_t kbp = pass_kblocks(s);
+  L.npass = (int)((L.k_pad / kBK + kbp - 1) / kbp);
+  size_t o = 0;
+  L.off_S = o;  o += align256((size_t)m * 4);
+  L.off_F = o;  o += align256((size_t)n * 4);
+  L.off_fa = o; o += align256((size_t)m * 4);
+  L.off_fb = o; o += align256((size_t)n * 4);
+  L.off_err = o; o += 256;
+  L.off_DA = o; o += align256((size_t)s * L.m_pad * L.k_pad * 2);
+  L.off_DB = o; o += align256((size_t)s * L.n_pad * L.k_pad * 2);
+  L.off_C = o;  o += align256((size_t)L.npass * (L.G + 1) * L.m_pad * L.n_pad * 4);
+  L.total = o;
+  return L;
+}
+
+int ozaki_default_digits() { return 20; }
+
+size_t ozaki_scratch_bytes(int64_t m, int64_t n, int64_t k, int digits) {
+  if (m <= 0 || n <= 0 || k <= 0) return 0;
+  return ozaki_layout(m, n, k, digits).total;
+}
+
+cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, void* scratch, cudaStream_t st) {
+  if (g.m <= 0 || g.n <= 0 || g.k <= 0) return cudaSuccess;
+  if (digits < 2 || digits > kOzakiMaxDigits) return cudaErrorInvalidValue;
+  OzakiLayout L = ozaki_layout(g.m, g.n, g.k, digits);
+  char* base = static_cast<char*>(scratch);
+  int* S = reinterpret_cast<int*>(base + L.off_S);
+  int* F = reinterpret_cast<int*>(base + L.off_F);
+  uint32_t* fa = reinterpret_cast<uint32_t*>(base + L.off_fa);
+  uint32_t* fb = reinterpret_cast<uint32_t*>(base + L.off_fb);
+  int* err = reinterpret_cast<int*>(base + L.off_err);
+  __nv_bfloat16* DA = reinterpret_cast<__nv_bfloat16*>(base + L.off_DA);
+  __nv_bfloat16* DB = reinterpret_cast<__nv_bfloat16*>(base + L.off_DB);
+  int32_t* Cg = reinterpret_cast<int32_t*>(base + L.off_C);
+  cudaError_t e;
+  const int sms = device_sm_count();
+
+  // 1. scales and flags: rows of op(A); rows of op(B)^T (= columns of op(B))
+  ozaki_fill_kernel<<<(unsigned)((g.m + 255) / 256), 256, 0, st>>>(g.m, S, fa);
+  ozaki_fill_kernel<<<(unsigned)((g.n + 255) / 256), 256, 0, st>>>(g.n, F, fb);
+  if ((e = cudaMemsetAsync(err, 0, 4, st)) != cudaSuccess) return e;
+  {
+    int64_t wa = g.m * ((g.k + 63) / 64), wb = g.n * ((g.k + 63) / 64);
+    unsigned ba = (unsigned)std::min<int64_t>((wa + 255) / 256, (int64_t)sms * 8);
+    unsigned bb = (unsigned)std::min<int64_t>((wb + 255) / 256, (int64_t)sms * 8);
+    ozaki_scale_kernel<<<ba, 256, 0, st>>>(g.m, g.k, g.A, g.sai, g.sal, S, fa);
+    ozaki_scale_kernel<<<bb, 256, 0, st>>>(g.n, g.k, g.B, g.sbj, g.sbl, F, fb);
+  }
+  // 2. digits
+  {
+    dim3 blk(32, 8);
+    dim3 ga((unsigned)(L.k_pad / 32), (unsigned)(L.m_pad / 8));
+    dim3 gb((unsigned)(L.k_pad / 32), (unsigned)(L.n_pad / 8));
+    ozaki_split_kernel<<<ga, blk, 0, st>>>(g.m, g.k, L.m_pad, L.k_pad, g.A, g.sai, g.sal, S, L.s, DA);
+    ozaki_split_kernel<<<gb, blk, 0, st>>>(g.n, g.k, L.n_pad, L.k_pad, g.B, g.sbj, g.sbl, F, L.s, DB);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  }
+  // 3. digit products on the tensor cores, one launch per k pass
+  CUtensorMap tmA, tmB;
+  if (!make_map(&tmA, DA, (int64_t)L.s * L.m_pad, L.k_pad, kBM) ||
+      !make_map(&tmB, DB, (int64_t)L.s * L.n_pad, L.k_pad, kBN))
+    return cudaErrorInvalidValue;
+  static bool attr_set[64] = {false};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev >= 0 && dev < 64 && !attr_set[dev]) {
+    if ((e = cudaFuncSetAttribute(ozaki_mma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)kMmaSmem)) != cudaSuccess)
+      return e;
+    attr_set[dev] = true;
+  }
+  const int tiles_m = (int)(L.m_pad / kBM), tiles_n = (int)(L.n_pad / kBN);
+  const int units = (L.G + 1) * tiles_m * tiles_n;
+  const int kb_total = (int)(L.k_pad / kBK), kbp = pass_kblocks(L.s);
+  for (int p = 0; p < L.npass; ++p) {
+    OzakiMmaParams P;
+    P.tiles_m = tiles_m;
+    P.tiles_n = tiles_n;
+    P.G = L.G;
+    P.m_pad = (int)L.m_pad;
+    P.n_pad = (int)L.n_pad;
+    P.kb_begin = p * kbp;
+    P.kb_end = std::min(kb_total, (p + 1) * kbp);
+    P.C = Cg + (size_t)p * (L.G + 1) * L.m_pad * L.n_pad;
+    P.err = err;
+    ozaki_mma_kernel<<<(unsigned)std::min(units, sms), kMmaThreads, kMmaSmem, st>>>(tmA, tmB, P);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  }
+  // 4. fold + epilogue
+  OzakiFoldParams F2;
+  F2.m = g.m; F2.n = g.n; F2.k = g.k;
+  F2.G = L.G; F2.npass = L.npass;
+  F2.m_pad = L.m_pad; F2.n_pad = L.n_pad;
+  F2.C = Cg; F2.S = S; F2.F = F; F2.fa = fa; F2.fb = fb;
+  F2.A = g.A; F2.sai = g.sai; F2.sal = g.sal;
+  F2.B = g.B; F2.sbl = g.sbl; F2.sbj = g.sbj;
+  F2.Cout = g.C; F2.sci = g.sci; F2.scj = g.scj;
+  F2.alpha = g.alpha; F2.beta = g.beta;
+  F2.err = err;
+  if ((g.m + 7) / 8 > 65535) return cudaErrorInvalidConfiguration;
+  dim3 fblk(32, 8), fgrid((unsigned)((g.n + 31) / 32), (unsigned)((g.m + 7) / 8));
+  ozaki_fold_kernel<<<fgrid, fblk, 0, st>>>(F2);
+  return cudaGetLastError();
+}
+
+size_t ozaki_error_flag_offset(int64_t m, int64_t n, int64_t k, int digits) {
+  return ozaki_layout(m, n, k, digits).off_err;
+}
+
+}  // namespace qb

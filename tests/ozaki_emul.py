@@ -1,0 +1,48 @@
+"""CPU emulation of the Ozaki qgemm pipeline for the parity tests.
+
+The digit split and the fold are the device code itself (ozaki.cuh) built
+for the host (tests/softquad_host.cpp); the digit products are exact
+numpy int64 matrix products.  Given the same inputs and digit count, the GPU
+path must reproduce this emulation bit for bit: the tensor-core products
+are exact integers, so any difference is a defect."""
+import ctypes
+
+import numpy as np
+
+P = lambda a: a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
+c64 = ctypes.c_int64
+
+
+def split(sq, X, rows, cols, sr, sc, s):
+    S = np.zeros(rows, dtype=np.int32)
+    D = np.zeros((s, rows, cols), dtype=np.int32)
+    sq.sq_ozaki_split(c64(rows), c64(cols), P(np.ascontiguousarray(X)), c64(sr), c64(sc), ctypes.c_int(s),
+                      P(S), P(D))
+    return S, D
+
+
+def diagonals(DA, DB):
+    """C_g = sum_{t+u=g, g<=s-1} DA_t @ DB_u^T (int64, exact)."""
+    s = DA.shape[0]
+    A64, B64 = DA.astype(np.int64), DB.astype(np.int64)
+    C = np.zeros((s, DA.shape[1], DB.shape[1]), dtype=np.int64)
+    for g in range(s):
+        for t in range(g + 1):
+            C[g] += A64[t] @ B64[g - t].T
+    return C
+
+
+def fold(sq, C, S, F):
+    G = C.shape[0] - 1
+    m, n = C.shape[1], C.shape[2]
+    out = np.zeros((m * n, 2), dtype=np.uint64)
+    sq.sq_ozaki_fold(c64(m), c64(n), ctypes.c_int(G), P(np.ascontiguousarray(C)), P(S), P(F), P(out))
+    return out
+
+
+def gemm_sum(sq, m, n, k, A, sai, sal, B, sbl, sbj, s):
+    """round(sum_l op(A)(i,l) op(B)(l,j)) as the Ozaki path computes it,
+    row-major (m*n, 2)."""
+    SA, DA = split(sq, A, m, k, sai, sal, s)
+    SB, DB = split(sq, B, n, k, sbj, sbl, s)  # op(B)^T rows = columns of op(B)
+    return fold(sq, diagonals(DA, DB), SA, SB)
