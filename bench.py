@@ -1,15 +1,22 @@
 """Benchmark of the binary128 hot path on GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload qgemm4096|qgemm512|qgemv8192|qdot26]
+                    [--workload qgemm4096|qgemm2048|qgemm512|qgemv8192|qdot26]
+                    [--method ozaki|softfloat] [--slices S]
 
-Default workload: qgemm m = n = k = 4096, row-major 'N','N', alpha = 1,
-beta = 0, entries u * 2^e (u uniform in [-1, 1) with full 113-bit
-significand, e uniform in [-20, 20]); the metric is binary128 GFLOP/s
-(2mnk per second).  One step is one qgemm with inputs resident in HBM.
-The qgemv 8192^2 and qdot 2^26 HBM workloads are measured beside it
-("secondary").  Each rank runs its own problem (weak scaling; the paths
-need no collective), rank 0 prints one JSON line.
+Default: qgemm m = n = k = 4096, row-major 'N','N', alpha = 1, beta = 0,
+entries u * 2^e (u uniform in [-1, 1) with a full 113-bit significand, e a
+uniform integer in [-20, 20]), Ozaki method with 20 digits per operand;
+metric binary128 GFLOP/s (2mnk per second).  One step is one qgemm with the
+inputs resident in HBM (A and B are 256 MB each, larger than L2, so no
+flush is needed).  Beside it ("secondary"): the soft-float qgemm of the
+same problem (the speed-up the Ozaki path is judged by), a digit-count
+sweep with the ulp distance of each result from the correctly rounded
+soft-float result, qgemv 8192^2 and qdot 2^26 (HBM rooflines) and the
+512^3 soft-float qgemm.
+
+Each rank runs its own problem (weak scaling; the path needs no
+collective); rank 0 prints one JSON line.
 
 --impl reference times the reference's CPU algorithm (the oracle's
 restatement of QuadBLAS's blocked gemm, OpenMP over all host cores) on a
@@ -18,6 +25,7 @@ bounded sample of the same workload.
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
 import os
 import statistics
@@ -33,16 +41,15 @@ sys.path.insert(0, ROOT)
 from qblas_gb300 import gen as G  # noqa: E402
 from qblas_gb300 import quad as Q  # noqa: E402
 
-L2_BYTES = 129 * 2**20
 FALLBACK = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}
+SWEEP = (8, 12, 16, 18, 19, 20, 21, 22)
 
 
 def peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
         with open(path) as f:
-            d = json.load(f)
-        return d, "measured"
+            return json.load(f), "measured"
     except (OSError, ValueError):
         return dict(FALLBACK), "fallback"
 
@@ -58,6 +65,7 @@ class ClockSampler:
     def __init__(self, device_index: int):
         self.dev = device_index
         self.proc = None
+        self.lines = []
 
     def __enter__(self):
         try:
@@ -70,7 +78,6 @@ class ClockSampler:
         return self
 
     def __exit__(self, *a):
-        self.lines = []
         if self.proc is not None:
             time.sleep(0.25)
             self.proc.terminate()
@@ -82,9 +89,7 @@ class ClockSampler:
             self.lines = [ln for ln in out.splitlines() if ln.strip()]
 
     def summary(self):
-        if not getattr(self, "lines", None):
-            return None
-        sm, mx, reasons = [], 0.0, set()
+        sm, mx, power, reasons = [], 0.0, [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for ln in self.lines:
             f = [s.strip() for s in ln.split(",")]
@@ -93,6 +98,7 @@ class ClockSampler:
             try:
                 sm.append(float(f[1]))
                 mx = max(mx, float(f[2]))
+                power.append(float(f[3]))
             except ValueError:
                 continue
             for nm, v in zip(names, f[5:9]):
@@ -102,17 +108,22 @@ class ClockSampler:
             return None
         load = [s for s in sm if s > 0.5 * max(sm)]
         return {"sm_mhz": statistics.median(load or sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
-                "samples": len(sm)}
+                "power_w_max": max(power) if power else None, "samples": len(sm)}
 
 
 # ---------------------------------------------------------------------------
-# workloads (ours)
+# helpers
 # ---------------------------------------------------------------------------
 def dev_tensor(torch, a: np.ndarray):
     return torch.from_numpy(np.ascontiguousarray(a).view(np.int64)).cuda()
 
 
+def to_host(t) -> np.ndarray:
+    return np.ascontiguousarray(t.cpu().numpy()).view(np.uint64)
+
+
 def time_steps(torch, fn, steps, warmup, dist=None):
+    """CUDA-event time (ms) of `steps` calls on the current stream, max over ranks."""
     for _ in range(warmup):
         fn()
     torch.cuda.synchronize()
@@ -133,6 +144,19 @@ def time_steps(torch, fn, steps, warmup, dist=None):
         ms = float(t.item())
         dist.barrier()
     return ms
+
+
+def ulp_distance(a: np.ndarray, b: np.ndarray) -> np.ndarray:
+    """|a - b| in binary128 ulps (distance in the ordered bit patterns)."""
+    def key(q):
+        out = []
+        for lo, hi in q:
+            v = (int(hi) << 64) | int(lo)
+            mag = v & ((1 << 127) - 1)
+            out.append(-mag if v >> 127 else mag)
+        return out
+    ka, kb = key(a), key(b)
+    return np.array([abs(x - y) for x, y in zip(ka, kb)], dtype=np.float64)
 
 
 class Qgemm:
@@ -156,10 +180,9 @@ class Qgemm:
         self.api.gemm_dev("R", "N", "N", self.m, self.n, self.k, self.alpha, self.dA, self.k, self.dB, self.n,
                           self.beta, self.dC, self.n)
 
-    def launches_per_step(self):
-        return 1
-
     def e2e(self, steps):
+        """Public host-pointer API (quadblas_qgemm_q): H2D of A, B, C and D2H of C
+        from pinned host memory inside the timed region."""
         torch, api = self.torch, self.api
         pin = lambda a: torch.from_numpy(a.view(np.int64)).pin_memory().numpy().view(np.uint64)  # noqa: E731
         hA, hB, hC = pin(self.A), pin(self.B), pin(self.C)
@@ -169,15 +192,13 @@ class Qgemm:
             api.gemm("R", "N", "N", self.m, self.n, self.k, self.alpha, hA, self.k, hB, self.n, self.beta, hC,
                      self.n)
         dt = time.perf_counter() - t0
-        h2d = (self.A.size + self.B.size + self.C.size) * 8
-        d2h = self.C.size * 8
-        return dt / steps, h2d, d2h
+        return dt / steps, (self.A.size + self.B.size + self.C.size) * 8, self.C.size * 8
 
 
 class Qgemv:
     def __init__(self, torch, m, n, seed):
         from qblas_gb300 import api
-        self.torch, self.api, self.m, self.n = torch, api, m, n
+        self.api, self.m, self.n = api, m, n
         rng = G.rng_for(seed)
         self.dA = dev_tensor(torch, G.wide_exponent(rng, m * n))
         self.dx = dev_tensor(torch, G.wide_exponent(rng, n))
@@ -194,7 +215,7 @@ class Qgemv:
 class Qdot:
     def __init__(self, torch, n, seed):
         from qblas_gb300 import api
-        self.torch, self.api, self.n = torch, api, n
+        self.api, self.n = api, n
         x, y = G.cancelling_dot(G.rng_for(seed), n)
         self.dx, self.dy = dev_tensor(torch, x), dev_tensor(torch, y)
         self.dr = torch.zeros((1, 2), dtype=torch.int64, device="cuda")
@@ -211,6 +232,13 @@ def hbm_roofline(pk, src, nbytes, ms_per_launch):
     peak = float(pk.get("hbm_gbs", FALLBACK["hbm_gbs"]))
     return {"bound": "hbm", "achieved": round(gbs, 1), "peak": peak, "unit": "GB/s", "frac": round(gbs / peak, 4),
             "traffic": None, "peak_source": src}
+
+
+def profile_read(lib):
+    out = (ctypes.c_double * 4)()
+    calls = ctypes.c_int(0)
+    lib.quadblas_profile_read(out, ctypes.byref(calls))
+    return list(out), calls.value
 
 
 # ---------------------------------------------------------------------------
@@ -232,38 +260,34 @@ def cpu_gemm_sample(target_s=12.0):
         O.ref_gemm(0, mm, nn, k, Q.scalar(1.0), A, k, B, nn, Q.scalar(0.0), C, nn, lib_order=1, nthreads=cores)
         return time.perf_counter() - t0
 
-    mm = nn = 16
-    t = run(mm, nn)
-    rate = (mm * nn) / max(t, 1e-6)
-    side = int(np.sqrt(rate * target_s))
-    side = max(16, min(side, 1024))
+    t = run(16, 16)
+    rate = 256 / max(t, 1e-6)
+    side = max(16, min(int(np.sqrt(rate * target_s)), 1024))
     t = run(side, side)
-    gflops = 2.0 * side * side * k / t / 1e9
-    return {"value": gflops, "unit": "GFLOP/s", "cores": cores, "kind": "port",
-            "sample": f"qgemm {side}x{side}x{k} (reference blocked order, kc=126) in {t:.1f} s, "
-                      f"OpenMP {cores} threads"}
+    return {"value": 2.0 * side * side * k / t / 1e9, "unit": "GFLOP/s", "cores": cores, "kind": "port",
+            "sample": f"qgemm {side}x{side}x{k} slice of the 4096^3 workload (reference blocked order, "
+                      f"kc=126, OpenMP {cores} threads) in {t:.1f} s"}
 
 
 def run_reference(args):
-    rank = int(os.environ.get("RANK", "0"))
-    if rank != 0:
+    if int(os.environ.get("RANK", "0")) != 0:
         return 0
-    base = None
-    times = []
-    for _ in range(max(args.warmup, 0) and 1):
-        cpu_gemm_sample(target_s=3.0)
-    for _ in range(args.steps):
+    if args.warmup > 0:
+        cpu_gemm_sample(target_s=2.0)
+    vals, base = [], None
+    for _ in range(max(args.steps, 1)):
         base = cpu_gemm_sample(target_s=8.0)
-        times.append(base["value"])
-    v = statistics.median(times)
-    line = {"metric": "qgemm binary128 GFLOP/s (4096^3 workload)", "value": round(v, 6), "unit": "GFLOP/s",
-            "impl": "reference", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "binary128 (host long double / __float128 FMA)", "data": "synthetic",
-            "config": {"workload": "qgemm m=n=k=4096 row-major NN alpha=1 beta=0 (sampled m x n slice, full k)"},
-            "cpu_baseline": {"value": round(v, 6), "unit": "GFLOP/s", "cores": base["cores"], "kind": "port",
+        vals.append(base["value"])
+    v = round(statistics.median(vals), 6)
+    line = {"metric": "qgemm binary128 GFLOP/s (4096^3)", "value": v, "unit": "GFLOP/s", "impl": "reference",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": None,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "binary128 (host long double / __float128 FMA)", "data": "synthetic (seeded)",
+            "config": {"workload": "qgemm m=n=k=4096 row-major NN alpha=1 beta=0, u*2^e entries "
+                                   "(sampled m x n slice, full k)"},
+            "cpu_baseline": {"value": v, "unit": "GFLOP/s", "cores": base["cores"], "kind": "port",
                              "sample": base["sample"]},
-            "e2e": {"value": round(v, 6), "unit": "GFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "e2e": {"value": v, "unit": "GFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
 
@@ -275,8 +299,8 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="qgemm4096", choices=["qgemm4096", "qgemm512", "qgemv8192", "qdot26"])
-    ap.add_argument("--method", default="softfloat", choices=["softfloat", "ozaki"])
+    ap.add_argument("--workload", default="qgemm4096", choices=["qgemm4096", "qgemm2048", "qgemm512", "qgemv8192", "qdot26"])
+    ap.add_argument("--method", default="ozaki", choices=["softfloat", "ozaki"])
     ap.add_argument("--slices", type=int, default=0)
     ap.add_argument("--no-secondary", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
@@ -295,34 +319,102 @@ def main():
         td.init_process_group("nccl")
         dist = td
     from qblas_gb300 import _lib, api
-    _lib.load()
+    lib = _lib.load()
     pk, pk_src = peaks()
-    api.set_method(2 if args.method == "ozaki" else 1)
+    method = 2 if args.method == "ozaki" else 1
+    api.set_method(method)
     api.set_ozaki_slices(args.slices)
+    slices = args.slices or 20
 
+    line = {}
+    secondary = {}
     wl = args.workload
     if wl.startswith("qgemm"):
-        size = 4096 if wl == "qgemm4096" else 512
-        W = Qgemm(torch, size, size, size, seed=0xC0FFEE + 2 + rank, spread=(size == 4096))
+        size = int(wl[5:])
+        W = Qgemm(torch, size, size, size, seed=0xC0FFEE + 2 + rank, spread=(size >= 2048))
+        lib.quadblas_profile_enable(1 if method == 2 else 0)
+        profile_read(lib)
         with ClockSampler(local) as clk:
             ms = time_steps(torch, W.step, args.steps, args.warmup, dist)
+        lib.quadblas_profile_enable(0)
         ms_step = ms / args.steps
         value = world * W.flops() / (ms_step * 1e-3) / 1e9
+        if method == 2:
+            ph, calls = profile_read(lib)  # warm-up and timed calls, recorded on the launching stream
+            tot_calls = max(calls, 1)
+            mma_ms = ph[1] / tot_calls
+            tflops = (ph[3] / tot_calls) / (mma_ms * 1e-3) / 1e12
+            peak = float(pk.get("bf16_tflops_sustained", FALLBACK["bf16_tflops_sustained"]))
+            roof = {"bound": "tensor", "achieved": round(tflops, 1), "peak": peak, "unit": "TFLOP/s",
+                    "frac": round(tflops / peak, 4), "traffic": None, "peak_source": pk_src + " (sustained bf16)",
+                    "kernel": "ozaki_mma_kernel", "kernel_ms": round(mma_ms, 4),
+                    "algorithmic": "2*m*n*k*pairs bf16 flops, pairs = s(s+1)/2",
+                    "phases_ms": {"scale_split": round(ph[0] / tot_calls, 4), "digit_products": round(mma_ms, 4),
+                                  "fold": round(ph[2] / tot_calls, 4)}}
+            launches = (7 + 1) * args.steps
+            dtype = "bf16 digit products (fp32 accumulate, int32/192-bit fold)"
+        else:
+            roof = {"bound": "int", "achieved": round(W.flops() / (ms_step * 1e-3) / 1e9, 3), "peak": None,
+                    "unit": "quad GFLOP/s", "frac": None, "traffic": None,
+                    "note": "soft-float kernel is integer-pipe bound"}
+            launches = args.steps
+            dtype = "u32 (soft-float integer limbs)"
         metric, unit = f"qgemm binary128 GFLOP/s ({size}^3)", "GFLOP/s"
-        launches = W.launches_per_step() * args.steps
-        # soft-float qgemm: one kernel per step, so the step time is the kernel time
-        roof = {"bound": "int", "achieved": round(W.flops() / (ms_step * 1e-3) / 1e9, 3),
-                "peak": None, "unit": "quad GFLOP/s", "frac": None, "traffic": None,
-                "note": "soft-float kernel is integer-pipe bound; no tensor/HBM roofline applies"}
         e2e_s, h2d, d2h = W.e2e(max(1, min(args.steps, 3)))
         e2e = {"value": round(W.flops() / e2e_s / 1e9, 3), "unit": unit, "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": int(d2h)}
-        cfg = {"workload": f"qgemm m=n=k={size} row-major NN alpha=1 beta=0, entries u*2^e "
-                           f"(u uniform [-1,1) full 113-bit significand, e uniform [-20,20])" if size == 4096 else
-                           f"qgemm m=n=k={size} row-major NN alpha=1 beta=0, full-mantissa uniform [-1,1)",
-               "method": args.method, "l2": "inputs larger than L2 (no flush)" if size == 4096 else
-               "inputs fit in L2; one launch per step", "parallelism": f"replicas x{world}"}
-        dtype = "u32 (soft-float integer limbs)"
+        cfg = {"workload": (f"qgemm m=n=k={size} row-major NN alpha=1 beta=0, entries u*2^e (u uniform [-1,1) "
+                            "full 113-bit significand, e uniform [-20,20])") if size >= 2048 else
+               f"qgemm m=n=k={size} row-major NN alpha=1 beta=0, full-mantissa uniform [-1,1)",
+               "method": args.method, "digits_per_operand": slices if method == 2 else None,
+               "l2": "inputs larger than L2 (no flush)" if size >= 2048 else "inputs fit in L2",
+               "parallelism": f"replicas x{world}"}
+
+        if not args.no_secondary and size == 4096 and method == 2:
+            # soft-float qgemm of the same problem: speed-up and the correctly rounded reference result
+            C_oz = to_host(W.dC)
+            api.set_method(1)
+            ms_sf = time_steps(torch, W.step, 1, 1, dist)
+            C_sf = to_host(W.dC)
+            sf_gflops = W.flops() / (ms_sf * 1e-3) / 1e9
+            secondary["softfloat_qgemm4096"] = {"value": round(sf_gflops, 3), "unit": "GFLOP/s",
+                                                "ms_per_step": round(ms_sf, 3),
+                                                "ozaki_speedup": round(value / world / sf_gflops, 2)}
+            rng = np.random.default_rng(5)
+            idx = rng.integers(0, size * size, 4096)
+            d = ulp_distance(C_oz[idx], C_sf[idx])
+            secondary["ozaki_ulp_vs_correctly_rounded"] = {"max": float(d.max()), "exact_frac": float((d == 0).mean()),
+                                                           "samples": len(idx)}
+            api.set_method(2)
+            sweep = []
+            for s in SWEEP:
+                api.set_ozaki_slices(s)
+                ms_s = time_steps(torch, W.step, 2, 1, dist) / 2
+                ds = ulp_distance(to_host(W.dC)[idx], C_sf[idx])
+                sweep.append({"digits": s, "pairs": s * (s + 1) // 2, "ms": round(ms_s, 3),
+                              "gflops": round(W.flops() / (ms_s * 1e-3) / 1e9, 1),
+                              "speedup_vs_softfloat": round(ms_sf / ms_s, 2),
+                              "max_ulp": float(ds.max()), "exact_frac": float((ds == 0).mean())})
+            api.set_ozaki_slices(args.slices)
+            secondary["digit_sweep"] = sweep
+        if not args.no_secondary and size == 4096:
+            del W
+            torch.cuda.empty_cache()
+            for name, mk in [("qgemv8192", lambda: Qgemv(torch, 8192, 8192, 11 + rank)),
+                             ("qdot26", lambda: Qdot(torch, 1 << 26, 13 + rank))]:
+                S = mk()
+                ms2 = time_steps(torch, S.step, args.steps, 3, dist) / args.steps
+                secondary[name] = {"value": round(S.bytes() / (ms2 * 1e-3) / 1e9, 1), "unit": "GB/s",
+                                   "ms_per_step": round(ms2, 4),
+                                   "roofline": hbm_roofline(pk, pk_src, S.bytes(), ms2)}
+                del S
+                torch.cuda.empty_cache()
+            api.set_method(1)
+            S = Qgemm(torch, 512, 512, 512, seed=0xC0FFEE, spread=False)
+            ms2 = time_steps(torch, S.step, 20, 3, dist) / 20
+            secondary["qgemm512_softfloat"] = {"value": round(S.flops() / (ms2 * 1e-3) / 1e9, 3),
+                                               "unit": "GFLOP/s", "ms_per_step": round(ms2, 4)}
+            api.set_method(method)
     elif wl == "qgemv8192":
         W = Qgemv(torch, 8192, 8192, seed=11 + rank)
         with ClockSampler(local) as clk:
@@ -330,9 +422,11 @@ def main():
         ms_step = ms / args.steps
         value = world * W.bytes() / (ms_step * 1e-3) / 1e9
         metric, unit = "qgemv binary128 GB/s (8192^2 row-major)", "GB/s"
-        launches = args.steps
+        launches = 2 * args.steps
         roof = hbm_roofline(pk, pk_src, W.bytes(), ms_step)
-        e2e, cfg, dtype = None, {"workload": "qgemv 8192x8192 row-major alpha=1 beta=0 wide-exponent"}, "u32"
+        e2e, dtype = None, "u32 (soft-float integer limbs)"
+        cfg = {"workload": "qgemv 8192x8192 row-major alpha=1 beta=0, wide-exponent values",
+               "l2": "inputs larger than L2 (no flush)"}
     else:
         W = Qdot(torch, 1 << 26, seed=13 + rank)
         with ClockSampler(local) as clk:
@@ -342,27 +436,12 @@ def main():
         metric, unit = "qdot binary128 GB/s (n=2^26)", "GB/s"
         launches = 2 * args.steps
         roof = hbm_roofline(pk, pk_src, W.bytes(), ms_step)
-        e2e, cfg, dtype = None, {"workload": "qdot n=2^26 wide-exponent with cancelling pairs"}, "u32"
-
-    secondary = {}
-    if not args.no_secondary and wl == "qgemm4096":
-        del W
-        torch.cuda.empty_cache()
-        for name, mk, unitb in [("qgemv8192", lambda: Qgemv(torch, 8192, 8192, 11 + rank), "GB/s"),
-                                ("qdot26", lambda: Qdot(torch, 1 << 26, 13 + rank), "GB/s")]:
-            S = mk()
-            ms2 = time_steps(torch, S.step, args.steps, 3, dist) / args.steps
-            secondary[name] = {"value": round(S.bytes() / (ms2 * 1e-3) / 1e9, 1), "unit": unitb,
-                               "ms_per_step": round(ms2, 4), "roofline": hbm_roofline(pk, pk_src, S.bytes(), ms2)}
-            del S
-            torch.cuda.empty_cache()
-        S = Qgemm(torch, 512, 512, 512, seed=0xC0FFEE, spread=False)
-        ms2 = time_steps(torch, S.step, 20, 3, dist) / 20
-        secondary["qgemm512_softfloat"] = {"value": round(S.flops() / (ms2 * 1e-3) / 1e9, 3), "unit": "GFLOP/s",
-                                           "ms_per_step": round(ms2, 4)}
+        e2e, dtype = None, "u32 (soft-float integer limbs)"
+        cfg = {"workload": "qdot n=2^26 wide-exponent values with cancelling pairs",
+               "l2": "inputs larger than L2 (no flush)"}
 
     cpu = None
-    if rank == 0 and not args.no_cpu and wl.startswith("qgemm"):
+    if rank == 0 and not args.no_cpu and wl == "qgemm4096":
         cpu = cpu_gemm_sample()
         cpu["value"] = round(cpu["value"], 6)
 

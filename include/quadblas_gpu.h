@@ -146,6 +146,13 @@ int quadblas_get_method(void);
 /* Ozaki digit (slice) count per operand: 0 = default (20), else 2..22. */
 int quadblas_set_ozaki_slices(int slices);
 int quadblas_get_ozaki_slices(void);
+/* Phase timing of Ozaki qgemm calls (no reference counterpart): when
+ * enabled, each call records CUDA events on its stream; read returns the
+ * summed times in ms since the last read — out4[0] scaling and digit split,
+ * out4[1] digit products on the tensor cores, out4[2] fold and epilogue —
+ * and out4[3] the tensor flops of those calls (2*m*n*k*pairs). */
+int quadblas_profile_enable(int on);
+int quadblas_profile_read(double *out4, int *calls);
 /* Status of the calling thread's last call (part 1 calls record it too). */
 int quadblas_last_error(void);
 const char *quadblas_error_string(int code);

@@ -578,6 +578,14 @@ QBLAS_EXPORT int quadblas_set_ozaki_slices(int slices) {
   return fail(qb::kOk);
 }
 QBLAS_EXPORT int quadblas_get_ozaki_slices(void) { return g_slices.load(); }
+QBLAS_EXPORT int quadblas_profile_enable(int on) {
+  qb::ozaki_profile_enable(on != 0);
+  return qb::kOk;
+}
+QBLAS_EXPORT int quadblas_profile_read(double* out4, int* calls) {
+  if (!out4 || !calls) return fail(qb::kErrInvalidValue);
+  return qb::ozaki_profile_read(out4, calls);
+}
 QBLAS_EXPORT int quadblas_last_error(void) { return g_last_error; }
 QBLAS_EXPORT const char* quadblas_error_string(int code) {
   switch (code) {

@@ -64,6 +64,9 @@ int ozaki_default_digits();
 size_t ozaki_scratch_bytes(int64_t m, int64_t n, int64_t k, int digits);
 size_t ozaki_error_flag_offset(int64_t m, int64_t n, int64_t k, int digits);
 cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, void* scratch, cudaStream_t s);
+// Phase timing of Ozaki calls with CUDA events (off by default).
+void ozaki_profile_enable(bool on);
+int ozaki_profile_read(double* out4, int* calls);
 
 // Multiprocessor count of the current device (cached).
 int device_sm_count();

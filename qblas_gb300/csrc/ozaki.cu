@@ -40,6 +40,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <mutex>
+#include <vector>
 
 #include "kernels.h"
 #include "ozaki.cuh"
@@ -554,6 +556,59 @@ static OzakiLayout ozaki_layout(int64_t m, int64_t n, int64_t k, int s) {
 
 int ozaki_default_digits() { return 20; }
 
+// ---- optional phase timing (CUDA events on the launching stream) ----------
+namespace {
+struct PhaseEvents {
+  cudaEvent_t ev[4];  // start, after split, after digit products, after fold
+  int64_t mma_flop_units;  // 2*m*n*k*pairs / 2^20, for the tensor roofline
+};
+std::mutex g_prof_mu;
+bool g_prof_on = false;
+std::vector<PhaseEvents> g_prof_pending;
+double g_prof_sum[3] = {0, 0, 0};
+double g_prof_flop = 0;
+int g_prof_calls = 0;
+
+void prof_record(PhaseEvents* pe, int i, cudaStream_t st) {
+  if (pe) cudaEventRecord(pe->ev[i], st);
+}
+}  // namespace
+
+void ozaki_profile_enable(bool on) {
+  std::lock_guard<std::mutex> l(g_prof_mu);
+  g_prof_on = on;
+}
+
+// Sums of the phase times (ms) of the calls recorded since the last read:
+// out[0] scale + split, out[1] digit products (tensor cores), out[2] fold;
+// out[3] the algorithmic tensor flops of those calls (2*m*n*k*pairs).
+int ozaki_profile_read(double* out, int* calls) {
+  std::lock_guard<std::mutex> l(g_prof_mu);
+  for (PhaseEvents& pe : g_prof_pending) {
+    cudaEventSynchronize(pe.ev[3]);
+    float a = 0, b = 0, c = 0;
+    cudaEventElapsedTime(&a, pe.ev[0], pe.ev[1]);
+    cudaEventElapsedTime(&b, pe.ev[1], pe.ev[2]);
+    cudaEventElapsedTime(&c, pe.ev[2], pe.ev[3]);
+    g_prof_sum[0] += a;
+    g_prof_sum[1] += b;
+    g_prof_sum[2] += c;
+    g_prof_flop += (double)pe.mma_flop_units * 1048576.0;
+    ++g_prof_calls;
+    for (int i = 0; i < 4; ++i) cudaEventDestroy(pe.ev[i]);
+  }
+  g_prof_pending.clear();
+  out[0] = g_prof_sum[0];
+  out[1] = g_prof_sum[1];
+  out[2] = g_prof_sum[2];
+  out[3] = g_prof_flop;
+  *calls = g_prof_calls;
+  g_prof_sum[0] = g_prof_sum[1] = g_prof_sum[2] = 0;
+  g_prof_flop = 0;
+  g_prof_calls = 0;
+  return 0;
+}
+
 size_t ozaki_scratch_bytes(int64_t m, int64_t n, int64_t k, int digits) {
   if (m <= 0 || n <= 0 || k <= 0) return 0;
   return ozaki_layout(m, n, k, digits).total;
@@ -574,6 +629,19 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, void* scratch, cuda
   int32_t* Cg = reinterpret_cast<int32_t*>(base + L.off_C);
   cudaError_t e;
   const int sms = device_sm_count();
+  PhaseEvents pev;
+  PhaseEvents* pe = nullptr;
+  {
+    std::lock_guard<std::mutex> l(g_prof_mu);
+    if (g_prof_on) {
+      bool okev = true;
+      for (int i = 0; i < 4; ++i) okev = okev && cudaEventCreate(&pev.ev[i]) == cudaSuccess;
+      if (okev) pe = &pev;
+      int64_t pairs = (int64_t)L.s * (L.s + 1) / 2;
+      pev.mma_flop_units = (int64_t)((2.0 * g.m * g.n * g.k * pairs) / 1048576.0);
+    }
+  }
+  prof_record(pe, 0, st);
 
   // 1. scales and flags: rows of op(A); rows of op(B)^T (= columns of op(B))
   ozaki_fill_kernel<<<(unsigned)((g.m + 255) / 256), 256, 0, st>>>(g.m, S, fa);
@@ -595,6 +663,7 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, void* scratch, cuda
     ozaki_split_kernel<<<gb, blk, 0, st>>>(g.n, g.k, L.n_pad, L.k_pad, g.B, g.sbj, g.sbl, F, L.s, DB);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
   }
+  prof_record(pe, 1, st);
   // 3. digit products on the tensor cores, one launch per k pass
   CUtensorMap tmA, tmB;
   if (!make_map(&tmA, DA, (int64_t)L.s * L.m_pad, L.k_pad, kBM) ||
@@ -626,6 +695,7 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, void* scratch, cuda
     ozaki_mma_kernel<<<(unsigned)std::min(units, sms), kMmaThreads, kMmaSmem, st>>>(tmA, tmB, P);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
   }
+  prof_record(pe, 2, st);
   // 4. fold + epilogue
   OzakiFoldParams F2;
   F2.m = g.m; F2.n = g.n; F2.k = g.k;
@@ -640,7 +710,13 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, void* scratch, cuda
   if ((g.m + 7) / 8 > 65535) return cudaErrorInvalidConfiguration;
   dim3 fblk(32, 8), fgrid((unsigned)((g.n + 31) / 32), (unsigned)((g.m + 7) / 8));
   ozaki_fold_kernel<<<fgrid, fblk, 0, st>>>(F2);
-  return cudaGetLastError();
+  e = cudaGetLastError();
+  prof_record(pe, 3, st);
+  if (pe) {
+    std::lock_guard<std::mutex> l(g_prof_mu);
+    g_prof_pending.push_back(pev);
+  }
+  return e;
 }
 
 size_t ozaki_error_flag_offset(int64_t m, int64_t n, int64_t k, int digits) {
