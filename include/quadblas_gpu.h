@@ -143,9 +143,13 @@ int quadblas_qdot_dev_noalloc(int64_t n, const void *dx, int64_t incx, const voi
 /* qgemm method: QBLAS_METHOD_AUTO, _SOFTFLOAT or _OZAKI. */
 int quadblas_set_method(int method);
 int quadblas_get_method(void);
-/* Ozaki digit (slice) count per operand: 0 = default (20), else 2..22. */
+/* Ozaki digit (slice) count per operand: 0 = default (18 for 8-bit digits,
+ * 20 for 7-bit), else 2..20 (8-bit) or 2..22 (7-bit). */
 int quadblas_set_ozaki_slices(int slices);
 int quadblas_get_ozaki_slices(void);
+/* Ozaki digit width: 0 = default (8), 7 or 8 bits per balanced digit. */
+int quadblas_set_ozaki_digit_bits(int bits);
+int quadblas_get_ozaki_digit_bits(void);
 /* Phase timing of Ozaki qgemm calls (no reference counterpart): when
  * enabled, each call records CUDA events on its stream; read returns the
  * summed times in ms since the last read — out4[0] scaling and digit split,

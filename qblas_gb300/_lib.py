@@ -46,6 +46,8 @@ _SIGS = {
     "quadblas_get_method": (ci, []),
     "quadblas_set_ozaki_slices": (ci, [ci]),
     "quadblas_get_ozaki_slices": (ci, []),
+    "quadblas_set_ozaki_digit_bits": (ci, [ci]),
+    "quadblas_get_ozaki_digit_bits": (ci, []),
     "quadblas_profile_enable": (ci, [ci]),
     "quadblas_profile_read": (ci, [vp, vp]),
     "quadblas_last_error": (ci, []),

@@ -135,3 +135,7 @@ def set_method(method: int) -> None:
 
 def set_ozaki_slices(s: int) -> None:
     check(load().quadblas_set_ozaki_slices(s))
+
+
+def set_ozaki_digit_bits(b: int) -> None:
+    check(load().quadblas_set_ozaki_digit_bits(b))

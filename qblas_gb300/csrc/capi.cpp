@@ -33,6 +33,7 @@ thread_local int g_last_error = 0;
 std::atomic<int> g_num_threads{0};
 std::atomic<int> g_method{0};   // 0 auto, 1 soft-float, 2 Ozaki
 std::atomic<int> g_slices{0};   // 0 = automatic
+std::atomic<int> g_digit_bits{0};  // 0 = automatic (8)
 
 int fail(int code) {
   g_last_error = code;
@@ -293,21 +294,28 @@ int gemm_method() {
   return env;
 }
 
+int gemm_digit_bits() {
+  int b = g_digit_bits.load();
+  return b ? b : qb::ozaki_default_digit_bits();
+}
+
 int gemm_digits() {
+  int b = gemm_digit_bits();
+  int smax = b == 7 ? 22 : 20;
   int s = g_slices.load();
-  if (s > 0) return s;
+  if (s > 0) return std::min(s, smax);
   static int env = -1;
   if (env < 0) {
     const char* v = getenv("QBLAS_SLICES");
     env = v ? atoi(v) : 0;
     if (env < 2 || env > 22) env = 0;
   }
-  return env ? env : qb::ozaki_default_digits();
+  return env ? std::min(env, smax) : qb::ozaki_default_digits(b);
 }
 
 size_t gemm_scratch_bytes(const GemmPlan& p) {
   if (gemm_method() != 2) return 0;
-  return qb::ozaki_scratch_bytes(p.g.m, p.g.n, p.g.k, gemm_digits());
+  return qb::ozaki_scratch_bytes(p.g.m, p.g.n, p.g.k, gemm_digits(), gemm_digit_bits());
 }
 
 int dev_gemm(GemmPlan p, const void* alpha, const void* dA, const void* dB, const void* beta,
@@ -328,7 +336,7 @@ int dev_gemm(GemmPlan p, const void* alpha, const void* dA, const void* dB, cons
       return cuda_status(e);
     }
   }
-  cudaError_t e = qb::launch_gemm_ozaki(p.g, gemm_digits(), scratch, s);
+  cudaError_t e = qb::launch_gemm_ozaki(p.g, gemm_digits(), gemm_digit_bits(), scratch, s);
   if (!scratch_or_null) cudaFreeAsync(scratch, s);
   return cuda_status(e);
 }
@@ -578,6 +586,12 @@ QBLAS_EXPORT int quadblas_set_ozaki_slices(int slices) {
   return fail(qb::kOk);
 }
 QBLAS_EXPORT int quadblas_get_ozaki_slices(void) { return g_slices.load(); }
+QBLAS_EXPORT int quadblas_set_ozaki_digit_bits(int bits) {
+  if (bits != 0 && bits != 7 && bits != 8) return fail(qb::kErrInvalidValue);
+  g_digit_bits.store(bits);
+  return fail(qb::kOk);
+}
+QBLAS_EXPORT int quadblas_get_ozaki_digit_bits(void) { return g_digit_bits.load(); }
 QBLAS_EXPORT int quadblas_profile_enable(int on) {
   qb::ozaki_profile_enable(on != 0);
   return qb::kOk;

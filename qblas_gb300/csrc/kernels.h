@@ -59,11 +59,14 @@ struct GemmArgs {
 cudaError_t launch_gemm_softfloat(const GemmArgs& g, cudaStream_t s);
 
 // C = fma(alpha, round(sum), beta * C) with the sum from the Ozaki digit
-// split on the tensor cores (`digits` balanced 7-bit digits per operand).
-int ozaki_default_digits();
-size_t ozaki_scratch_bytes(int64_t m, int64_t n, int64_t k, int digits);
-size_t ozaki_error_flag_offset(int64_t m, int64_t n, int64_t k, int digits);
-cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, void* scratch, cudaStream_t s);
+// split on the tensor cores (`digits` balanced digits of `bits` = 7 or 8
+// bits per operand).
+int ozaki_default_digit_bits();
+int ozaki_default_digits(int bits);
+size_t ozaki_scratch_bytes(int64_t m, int64_t n, int64_t k, int digits, int bits);
+size_t ozaki_error_flag_offset(int64_t m, int64_t n, int64_t k, int digits, int bits);
+cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scratch,
+                              cudaStream_t s);
 // Phase timing of Ozaki calls with CUDA events (off by default).
 void ozaki_profile_enable(bool on);
 int ozaki_profile_read(double* out4, int* calls);

@@ -26,7 +26,7 @@
 namespace qb {
 
 __device__ __forceinline__ q128 gemv_epilogue(q128 alpha, q128 sum, q128 beta, q128 yv) {
-  return q_fma(alpha, sum, q_mul(beta, yv));
+  return q_epilogue(alpha, sum, beta, yv);
 }
 
 // ---- x unpacked once -------------------------------------------------------

@@ -97,19 +97,19 @@ __global__ void __launch_bounds__(kGemmThreads)
   const int64_t ia = i0 + 2 * ty, ja = j0 + 2 * tx;
   if (ia < m && ja < n) {
     q128* p = C + ia * sci + ja * scj;
-    *p = q_fma(alpha, wacc_round(c00), q_mul(beta, *p));
+    *p = q_epilogue(alpha, wacc_round(c00), beta, *p);
   }
   if (ia < m && ja + 1 < n) {
     q128* p = C + ia * sci + (ja + 1) * scj;
-    *p = q_fma(alpha, wacc_round(c01), q_mul(beta, *p));
+    *p = q_epilogue(alpha, wacc_round(c01), beta, *p);
   }
   if (ia + 1 < m && ja < n) {
     q128* p = C + (ia + 1) * sci + ja * scj;
-    *p = q_fma(alpha, wacc_round(c10), q_mul(beta, *p));
+    *p = q_epilogue(alpha, wacc_round(c10), beta, *p);
   }
   if (ia + 1 < m && ja + 1 < n) {
     q128* p = C + (ia + 1) * sci + (ja + 1) * scj;
-    *p = q_fma(alpha, wacc_round(c11), q_mul(beta, *p));
+    *p = q_epilogue(alpha, wacc_round(c11), beta, *p);
   }
 }
 

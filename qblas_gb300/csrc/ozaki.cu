@@ -3,16 +3,17 @@
 // Replaces the reference's soft-float GEMM loops
 // (include/quadblas/algorithms/level3.hpp:17-336) by an error-free integer
 // splitting (ozaki.cuh): each row of op(A) and column of op(B) is cut into s
-// signed 7-bit digits stored as bf16, every digit pair (t, u) is an exact
-// bf16 x bf16 -> fp32 GEMM on tcgen05.mma kind::f16 (sums <= 2^24 stay
-// exact; k is processed in chunks of 4096), the pairs of one diagonal
+// signed 8-bit (or 7-bit) digits stored as bf16, every digit pair (t, u) is
+// an exact bf16 x bf16 -> fp32 GEMM on tcgen05.mma kind::f16 (sums <= 2^24
+// stay exact; k is processed in chunks of 1024 (4096 for 7-bit digits)),
+// the pairs of one diagonal
 // g = t + u are summed exactly in int32, and a fold kernel combines the
 // diagonals into a 192-bit integer per output that is rounded once to
 // binary128 and passed through the reference epilogue
 // C = fma(alpha, sum, beta * C) (level3.hpp:107).
 //
 // tcgen05 kind::i8 does not exist on sm_103a, so integer digits travel as
-// bf16 (|d| <= 64 is exact) with fp32 accumulation in tensor memory.
+// bf16 (|d| <= 128 is exact) with fp32 accumulation in tensor memory.
 //
 // Kernels:
 //   ozaki_scale_kernel  : S_i = max_l (exponent(x_il) + 1) per row of a
@@ -91,26 +92,24 @@ __global__ void ozaki_fill_kernel(int64_t n, int* __restrict__ S, uint32_t* __re
 
 // Digits of the (rows_pad x cols_pad) zero-padded view into
 // D[t * rows_pad * cols_pad + r * cols_pad + c] (bf16).  Block (32, 8):
-// x along columns (coalesced digit stores), y along rows.
+// x along columns (coalesced digit stores), y along rows; each digit is
+// stored as soon as it is extracted.
 __global__ void __launch_bounds__(256)
     ozaki_split_kernel(int64_t rows, int64_t cols, int64_t rows_pad, int64_t cols_pad,
                        const q128* __restrict__ p, int64_t sr, int64_t sc,
-                       const int* __restrict__ S, int s, __nv_bfloat16* __restrict__ D) {
+                       const int* __restrict__ S, int s, int b, __nv_bfloat16* __restrict__ D) {
   const int64_t c = (int64_t)blockIdx.x * 32 + threadIdx.x;
   const int64_t r = (int64_t)blockIdx.y * 8 + threadIdx.y;
   if (c >= cols_pad || r >= rows_pad) return;
-  int dg[kOzakiMaxDigits];
-  if (r < rows && c < cols) {
-    ozaki_digits(ld_cached(p + r * sr + c * sc), S[r], s, dg);
-  } else {
-#pragma unroll
-    for (int t = 0; t < kOzakiMaxDigits; ++t) dg[t] = 0;
-  }
   const int64_t plane = rows_pad * cols_pad;
   __nv_bfloat16* out = D + r * cols_pad + c;
-#pragma unroll
-  for (int t = 0; t < kOzakiMaxDigits; ++t)
-    if (t < s) out[t * plane] = __int2bfloat16_rn(dg[t]);
+  q128 v = q_zero(0);
+  int Sr = kOzakiScaleEmpty;
+  if (r < rows && c < cols) {
+    v = ld_cached(p + r * sr + c * sc);
+    Sr = S[r];
+  }
+  ozaki_digits_emit(v, Sr, s, b, [&](int t, int d) { out[t * plane] = __int2bfloat16_rn(d); });
 }
 
 // ---------------------------------------------------------------------------
@@ -124,7 +123,6 @@ constexpr int kStageBytes = kStageA + kStageB;  // 48 KiB
 constexpr int kMmaThreads = 320;                // 10 warps
 constexpr int kEpiWarps = 8;
 constexpr int kTmemCols = 512;                  // two 256-column fp32 accumulators
-constexpr int kExactChunkKB = 4096 / kBK;       // k-blocks summed exactly in fp32
 constexpr size_t kMmaSmem = (size_t)kStages * kStageBytes + 1024 + 256;
 constexpr unsigned long long kWaitLimitNs = 1000000000ull;  // 1 s per wait
 
@@ -133,6 +131,7 @@ struct OzakiMmaParams {
   int G;         // highest diagonal (s - 1)
   int m_pad, n_pad;
   int kb_begin, kb_end;  // k-blocks of this pass
+  int chunk_kb;          // k-blocks summed exactly in fp32 before a readout
   int32_t* C;            // [G+1][m_pad][n_pad]
   int* err;              // set to nonzero on a timeout
 };
@@ -281,7 +280,7 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
   const int tiles = P.tiles_m * P.tiles_n;
   const int units = (P.G + 1) * tiles;
   const int nkb = P.kb_end - P.kb_begin;
-  const int nchunks = (nkb + kExactChunkKB - 1) / kExactChunkKB;
+  const int nchunks = (nkb + P.chunk_kb - 1) / P.chunk_kb;
   bool ok = true;
 
   if (warp == 0) {
@@ -323,8 +322,8 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
         const int g = P.G - unit / tiles;
         for (int t = 0; t <= g && ok; ++t) {
           for (int ch = 0; ch < nchunks && ok; ++ch) {
-            const int kb0 = P.kb_begin + ch * kExactChunkKB;
-            const int kb1 = kb0 + kExactChunkKB < P.kb_end ? kb0 + kExactChunkKB : P.kb_end;
+            const int kb0 = P.kb_begin + ch * P.chunk_kb;
+            const int kb1 = kb0 + P.chunk_kb < P.kb_end ? kb0 + P.chunk_kb : P.kb_end;
             const int buf = acc_it & 1;
             const uint32_t round = acc_it >> 1;
             if (!mbar_wait(tempty_bar(buf), (round & 1u) ^ 1u)) {
@@ -428,7 +427,7 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
 // ---------------------------------------------------------------------------
 struct OzakiFoldParams {
   int64_t m, n, k;
-  int G, npass;
+  int G, npass, b;
   int64_t m_pad, n_pad;
   const int32_t* C;      // [npass][G+1][m_pad][n_pad]
   const int* S;          // row scales of op(A)
@@ -469,12 +468,12 @@ __global__ void __launch_bounds__(256) ozaki_fold_kernel(OzakiFoldParams P) {
     for (int g = 0; g <= P.G; ++g) {
       int64_t v = 0;
       for (int p = 0; p < P.npass; ++p) v += P.C[((size_t)p * (P.G + 1) + g) * plane + off];
-      fold_step(f, v);
+      fold_step(f, v, P.b);
     }
-    sum = fold_round(f, ozaki_fold_exp(P.S[i], P.F[j], P.G));
+    sum = fold_round(f, ozaki_fold_exp(P.S[i], P.F[j], P.G, P.b));
   }
   q128* cp = P.Cout + i * P.sci + j * P.scj;
-  *cp = q_fma(P.alpha, sum, q_mul(P.beta, *cp));
+  *cp = q_epilogue(P.alpha, sum, P.beta, *cp);
 }
 
 // ---------------------------------------------------------------------------
@@ -517,29 +516,31 @@ static bool make_map(CUtensorMap* map, const void* D, int64_t rows, int64_t cols
 static int64_t rup(int64_t v, int64_t a) { return (v + a - 1) / a * a; }
 static size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
 
-// k-blocks per pass: diagonals hold at most s pairs, each pair adds at most
-// ceil(kb / 64) exact chunks of |sum| <= 2^24, and the int32 sum must stay
-// below 2^31.
-static int pass_kblocks(int s) {
+// k-blocks per pass: a diagonal holds at most s pairs, each pair adds one
+// exact chunk sum of magnitude <= 2^24 per chunk, and the int32 diagonal sum
+// must stay below 2^31.
+static int chunk_kblocks(int b) { return ozaki_exact_chunk(b) / kBK; }
+static int pass_kblocks(int s, int b) {
   int chunks = (int)(((1ll << 31) - 1) / ((int64_t)s << 24));  // exact chunks per pass
   if (chunks < 1) chunks = 1;
-  return chunks * kExactChunkKB;
+  return chunks * chunk_kblocks(b);
 }
 
 struct OzakiLayout {
   int64_t m_pad, n_pad, k_pad;
-  int s, G, npass;
+  int s, b, G, npass;
   size_t off_S, off_F, off_fa, off_fb, off_err, off_DA, off_DB, off_C, total;
 };
 
-static OzakiLayout ozaki_layout(int64_t m, int64_t n, int64_t k, int s) {
+static OzakiLayout ozaki_layout(int64_t m, int64_t n, int64_t k, int s, int b) {
   OzakiLayout L;
   L.s = s;
+  L.b = b;
   L.G = s - 1;
   L.m_pad = rup(m, kBM);
   L.n_pad = rup(n, kBN);
   L.k_pad = rup(k, kBK);
-  int64_t kbp = pass_kblocks(s);
+  int64_t kbp = pass_kblocks(s, b);
   L.npass = (int)((L.k_pad / kBK + kbp - 1) / kbp);
   size_t o = 0;
   L.off_S = o;  o += align256((size_t)m * 4);
@@ -554,7 +555,8 @@ static OzakiLayout ozaki_layout(int64_t m, int64_t n, int64_t k, int s) {
   return L;
 }
 
-int ozaki_default_digits() { return 20; }
+int ozaki_default_digits(int b) { return b == 7 ? 20 : 18; }
+int ozaki_default_digit_bits() { return 8; }
 
 // ---- optional phase timing (CUDA events on the launching stream) ----------
 namespace {
@@ -609,15 +611,16 @@ int ozaki_profile_read(double* out, int* calls) {
   return 0;
 }
 
-size_t ozaki_scratch_bytes(int64_t m, int64_t n, int64_t k, int digits) {
+size_t ozaki_scratch_bytes(int64_t m, int64_t n, int64_t k, int digits, int bits) {
   if (m <= 0 || n <= 0 || k <= 0) return 0;
-  return ozaki_layout(m, n, k, digits).total;
+  return ozaki_layout(m, n, k, digits, bits).total;
 }
 
-cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, void* scratch, cudaStream_t st) {
+cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scratch, cudaStream_t st) {
   if (g.m <= 0 || g.n <= 0 || g.k <= 0) return cudaSuccess;
-  if (digits < 2 || digits > kOzakiMaxDigits) return cudaErrorInvalidValue;
-  OzakiLayout L = ozaki_layout(g.m, g.n, g.k, digits);
+  if ((bits != 7 && bits != 8) || digits < 2 || digits > ozaki_max_digits(bits))
+    return cudaErrorInvalidValue;
+  OzakiLayout L = ozaki_layout(g.m, g.n, g.k, digits, bits);
   char* base = static_cast<char*>(scratch);
   int* S = reinterpret_cast<int*>(base + L.off_S);
   int* F = reinterpret_cast<int*>(base + L.off_F);
@@ -659,8 +662,8 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, void* scratch, cuda
     dim3 blk(32, 8);
     dim3 ga((unsigned)(L.k_pad / 32), (unsigned)(L.m_pad / 8));
     dim3 gb((unsigned)(L.k_pad / 32), (unsigned)(L.n_pad / 8));
-    ozaki_split_kernel<<<ga, blk, 0, st>>>(g.m, g.k, L.m_pad, L.k_pad, g.A, g.sai, g.sal, S, L.s, DA);
-    ozaki_split_kernel<<<gb, blk, 0, st>>>(g.n, g.k, L.n_pad, L.k_pad, g.B, g.sbj, g.sbl, F, L.s, DB);
+    ozaki_split_kernel<<<ga, blk, 0, st>>>(g.m, g.k, L.m_pad, L.k_pad, g.A, g.sai, g.sal, S, L.s, L.b, DA);
+    ozaki_split_kernel<<<gb, blk, 0, st>>>(g.n, g.k, L.n_pad, L.k_pad, g.B, g.sbj, g.sbl, F, L.s, L.b, DB);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
   }
   prof_record(pe, 1, st);
@@ -680,7 +683,7 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, void* scratch, cuda
   }
   const int tiles_m = (int)(L.m_pad / kBM), tiles_n = (int)(L.n_pad / kBN);
   const int units = (L.G + 1) * tiles_m * tiles_n;
-  const int kb_total = (int)(L.k_pad / kBK), kbp = pass_kblocks(L.s);
+  const int kb_total = (int)(L.k_pad / kBK), kbp = pass_kblocks(L.s, L.b);
   for (int p = 0; p < L.npass; ++p) {
     OzakiMmaParams P;
     P.tiles_m = tiles_m;
@@ -690,6 +693,7 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, void* scratch, cuda
     P.n_pad = (int)L.n_pad;
     P.kb_begin = p * kbp;
     P.kb_end = std::min(kb_total, (p + 1) * kbp);
+    P.chunk_kb = chunk_kblocks(L.b);
     P.C = Cg + (size_t)p * (L.G + 1) * L.m_pad * L.n_pad;
     P.err = err;
     ozaki_mma_kernel<<<(unsigned)std::min(units, sms), kMmaThreads, kMmaSmem, st>>>(tmA, tmB, P);
@@ -699,7 +703,7 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, void* scratch, cuda
   // 4. fold + epilogue
   OzakiFoldParams F2;
   F2.m = g.m; F2.n = g.n; F2.k = g.k;
-  F2.G = L.G; F2.npass = L.npass;
+  F2.G = L.G; F2.npass = L.npass; F2.b = L.b;
   F2.m_pad = L.m_pad; F2.n_pad = L.n_pad;
   F2.C = Cg; F2.S = S; F2.F = F; F2.fa = fa; F2.fb = fb;
   F2.A = g.A; F2.sai = g.sai; F2.sal = g.sal;
@@ -719,8 +723,8 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, void* scratch, cuda
   return e;
 }
 
-size_t ozaki_error_flag_offset(int64_t m, int64_t n, int64_t k, int digits) {
-  return ozaki_layout(m, n, k, digits).off_err;
+size_t ozaki_error_flag_offset(int64_t m, int64_t n, int64_t k, int digits, int bits) {
+  return ozaki_layout(m, n, k, digits, bits).off_err;
 }
 
 }  // namespace qb

@@ -521,4 +521,13 @@ QB_HD q128 q_sqrt(q128 a) {
   return round_pack(0, R, !exact, k2 / 2);
 }
 
+// The reference epilogue y = fma(alpha, sum, beta * y) (level2.hpp:48,
+// level3.hpp:107).  fma(1, s, t) is s + t with one rounding, so alpha == 1
+// takes the cheaper addition; the result bits are identical.
+QB_HD q128 q_epilogue(q128 alpha, q128 sum, q128 beta, q128 y) {
+  q128 t = q_mul(beta, y);
+  if (alpha.hi == 0x3FFF000000000000ull && alpha.lo == 0) return q_add(sum, t);
+  return q_fma(alpha, sum, t);
+}
+
 }  // namespace qb

@@ -13,11 +13,11 @@ P = lambda a: a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
 c64 = ctypes.c_int64
 
 
-def split(sq, X, rows, cols, sr, sc, s):
+def split(sq, X, rows, cols, sr, sc, s, b=8):
     S = np.zeros(rows, dtype=np.int32)
     D = np.zeros((s, rows, cols), dtype=np.int32)
     sq.sq_ozaki_split(c64(rows), c64(cols), P(np.ascontiguousarray(X)), c64(sr), c64(sc), ctypes.c_int(s),
-                      P(S), P(D))
+                      ctypes.c_int(b), P(S), P(D))
     return S, D
 
 
@@ -32,17 +32,18 @@ def diagonals(DA, DB):
     return C
 
 
-def fold(sq, C, S, F):
+def fold(sq, C, S, F, b=8):
     G = C.shape[0] - 1
     m, n = C.shape[1], C.shape[2]
     out = np.zeros((m * n, 2), dtype=np.uint64)
-    sq.sq_ozaki_fold(c64(m), c64(n), ctypes.c_int(G), P(np.ascontiguousarray(C)), P(S), P(F), P(out))
+    sq.sq_ozaki_fold(c64(m), c64(n), ctypes.c_int(G), ctypes.c_int(b), P(np.ascontiguousarray(C)), P(S), P(F),
+                     P(out))
     return out
 
 
-def gemm_sum(sq, m, n, k, A, sai, sal, B, sbl, sbj, s):
-    """round(sum_l op(A)(i,l) op(B)(l,j)) as the Ozaki path computes it,
-    row-major (m*n, 2)."""
-    SA, DA = split(sq, A, m, k, sai, sal, s)
-    SB, DB = split(sq, B, n, k, sbj, sbl, s)  # op(B)^T rows = columns of op(B)
-    return fold(sq, diagonals(DA, DB), SA, SB)
+def gemm_sum(sq, m, n, k, A, sai, sal, B, sbl, sbj, s, b=8):
+    """round(sum_l op(A)(i,l) op(B)(l,j)) as the Ozaki path computes it with
+    s digits of b bits, row-major (m*n, 2)."""
+    SA, DA = split(sq, A, m, k, sai, sal, s, b)
+    SB, DB = split(sq, B, n, k, sbj, sbl, s, b)  # op(B)^T rows = columns of op(B)
+    return fold(sq, diagonals(DA, DB), SA, SB, b)

@@ -52,7 +52,7 @@ void sq_wacc_dot(int64_t n, const q128* x, int64_t incx, const q128* y, int64_t 
 // Ozaki split of a rows x cols view X(r, c) = X[r*sr + c*sc]: row scales
 // S[r] and digits D[t][r][c] (int32), the device kernels' arithmetic.
 void sq_ozaki_split(int64_t rows, int64_t cols, const q128* X, int64_t sr, int64_t sc, int s,
-                    int32_t* S, int32_t* D) {
+                    int b, int32_t* S, int32_t* D) {
   for (int64_t r = 0; r < rows; ++r) {
     int mx = qb::kOzakiScaleEmpty;
     for (int64_t c = 0; c < cols; ++c) {
@@ -62,20 +62,20 @@ void sq_ozaki_split(int64_t rows, int64_t cols, const q128* X, int64_t sr, int64
     S[r] = mx;
     for (int64_t c = 0; c < cols; ++c) {
       int dg[qb::kOzakiMaxDigits];
-      qb::ozaki_digits(X[r * sr + c * sc], mx, s, dg);
+      qb::ozaki_digits(X[r * sr + c * sc], mx, s, b, dg);
       for (int t = 0; t < s; ++t) D[((int64_t)t * rows + r) * cols + c] = dg[t];
     }
   }
 }
 // Fold of diagonals C[g][i][j] (int64, g <= G) with scales S[i], F[j].
-void sq_ozaki_fold(int64_t m, int64_t n, int G, const int64_t* C, const int32_t* S, const int32_t* F,
-                   q128* out) {
+void sq_ozaki_fold(int64_t m, int64_t n, int G, int b, const int64_t* C, const int32_t* S,
+                   const int32_t* F, q128* out) {
   for (int64_t i = 0; i < m; ++i)
     for (int64_t j = 0; j < n; ++j) {
       qb::fold192 f;
       qb::fold_init(f);
-      for (int g = 0; g <= G; ++g) qb::fold_step(f, C[((int64_t)g * m + i) * n + j]);
-      out[i * n + j] = qb::fold_round(f, qb::ozaki_fold_exp(S[i], F[j], G));
+      for (int g = 0; g <= G; ++g) qb::fold_step(f, C[((int64_t)g * m + i) * n + j], b);
+      out[i * n + j] = qb::fold_round(f, qb::ozaki_fold_exp(S[i], F[j], G, b));
     }
 }
 }

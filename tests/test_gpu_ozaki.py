@@ -4,10 +4,9 @@
   the digit split and fold of ozaki.cuh built for the host, digit products
   as exact numpy int64 GEMMs): the tensor-core products are exact integers,
   so any difference is a defect of the GPU path.
-* Accuracy against the exact oracle: with 20 digits per operand the result
-  is within 1 ulp (u_q = 2^-113) of the exact sum on spread-exponent data
-  (e uniform in [-20, 20]); with s digits it is within the representation
-  bound of the split.
+* Accuracy against the exact oracle: with 17 digits of 8 bits (or 20 of 7
+  bits) per operand the result is within 1 ulp (u_q = 2^-113) of the exact
+  sum on spread-exponent data (e uniform in [-20, 20]).
 * NaN / infinity rows and columns follow the exact-oracle semantics.
 """
 import ctypes
@@ -31,6 +30,7 @@ def ozaki(qlib):
     yield qlib
     api.set_method(0)
     api.set_ozaki_slices(0)
+    api.set_ozaki_digit_bits(0)
 
 
 def strides(layout, ta, tb, lda, ldb, ldc):
@@ -46,7 +46,7 @@ def strides(layout, ta, tb, lda, ldb, ldc):
     return sa, sb, sc
 
 
-def run_case(O, sq, rng, layout, transa, transb, m, n, k, s, gen, al_d, be_d):
+def run_case(O, sq, rng, layout, transa, transb, m, n, k, s, gen, al_d, be_d, b=8):
     col = layout == "C"
     ta, tb = transa == "T", transb == "T"
     ar, ac = (k, m) if ta else (m, k)
@@ -59,10 +59,11 @@ def run_case(O, sq, rng, layout, transa, transb, m, n, k, s, gen, al_d, be_d):
     C = G.uniform_full(rng, (n if col else m) * ldc)
     alpha, beta = Q.scalar(al_d), Q.scalar(be_d)
     api.set_ozaki_slices(s)
+    api.set_ozaki_digit_bits(b)
     got = C.copy()
     api.gemm(layout, transa, transb, m, n, k, alpha, A, lda, B, ldb, beta, got, ldc)
     (sai, sal), (sbl, sbj), (sci, scj) = strides(layout, ta, tb, lda, ldb, ldc)
-    sums = E.gemm_sum(sq, m, n, k, A, sai, sal, B, sbl, sbj, s)
+    sums = E.gemm_sum(sq, m, n, k, A, sai, sal, B, sbl, sbj, s, b)
     rows, cols = np.meshgrid(np.arange(m), np.arange(n), indexing="ij")
     idx = rows.ravel() * sci + cols.ravel() * scj
     exp = epilogue(O, alpha, sums, beta, C[idx])
@@ -76,21 +77,22 @@ def test_ozaki_one_tile_bit_exact(ozaki, O, sq):
     assert Q.same_bits(got[idx], exp).all()
 
 
-@pytest.mark.parametrize("s", [2, 7, 20])
-def test_ozaki_bit_exact_vs_emulation(ozaki, O, sq, s):
-    rng = G.rng_for(10 + s)
+@pytest.mark.parametrize("s,b", [(2, 8), (7, 8), (18, 8), (20, 8), (7, 7), (20, 7)])
+def test_ozaki_bit_exact_vs_emulation(ozaki, O, sq, s, b):
+    rng = G.rng_for(10 + s + 100 * b)
     cases = [("R", "N", "N", 1, 1, 1), ("R", "N", "N", 5, 7, 9), ("R", "T", "N", 130, 257, 70),
              ("C", "N", "N", 200, 100, 300), ("C", "T", "T", 33, 290, 129), ("R", "N", "T", 129, 255, 65)]
     for layout, ta, tb, m, n, k in cases:
-        got, idx, exp, _ = run_case(O, sq, rng, layout, ta, tb, m, n, k, s, G.spread_uniform, 2.5, -1.5)
-        assert Q.same_bits(got[idx], exp).all(), (layout, ta, tb, m, n, k, s)
+        got, idx, exp, _ = run_case(O, sq, rng, layout, ta, tb, m, n, k, s, G.spread_uniform, 2.5, -1.5, b)
+        assert Q.same_bits(got[idx], exp).all(), (layout, ta, tb, m, n, k, s, b)
 
 
-def test_ozaki_two_exact_chunks(ozaki, O, sq):
-    """k > 4096: two fp32-exact chunks summed in int32 per diagonal."""
-    rng = G.rng_for(2)
-    got, idx, exp, _ = run_case(O, sq, rng, "R", "N", "N", 128, 256, 4096 + 64 + 5, 6, G.spread_uniform,
-                                1.0, 0.0)
+@pytest.mark.parametrize("b,k", [(7, 4096 + 64 + 5), (8, 3 * 1024 + 64 + 5)])
+def test_ozaki_several_exact_chunks(ozaki, O, sq, b, k):
+    """k above the fp32-exact chunk (4096 for 7-bit, 1024 for 8-bit digits):
+    chunk sums are read out of tensor memory and added in int32."""
+    rng = G.rng_for(2 + b)
+    got, idx, exp, _ = run_case(O, sq, rng, "R", "N", "N", 128, 256, k, 6, G.spread_uniform, 1.0, 0.0, b)
     assert Q.same_bits(got[idx], exp).all()
 
 
@@ -103,24 +105,28 @@ def test_ozaki_mixed_magnitudes(ozaki, O, sq):
         q[: n // 7] = 0
         return q
 
-    got, idx, exp, _ = run_case(O, sq, rng, "R", "N", "N", 67, 301, 45, 20, gen, 1.0, 0.0)
-    assert Q.same_bits(got[idx], exp).all()
+    for b, s in ((8, 18), (7, 20)):
+        got, idx, exp, _ = run_case(O, sq, rng, "R", "N", "N", 67, 301, 45, s, gen, 1.0, 0.0, b)
+        assert Q.same_bits(got[idx], exp).all(), b
 
 
-def test_ozaki_accuracy_512_spread(ozaki, O, torch_cuda):
-    """512^3 on e-uniform-[-20, 20] data: with 20 digits every sampled entry
-    is within 1 ulp of the exact sum."""
+@pytest.mark.parametrize("size,s,b", [(512, 18, 8), (512, 20, 7), (4096, 17, 8)])
+def test_ozaki_accuracy_spread(ozaki, O, torch_cuda, size, s, b):
+    """size^3 on e-uniform-[-20, 20] data (the 4096^3 benchmark workload at
+    its digit count): every sampled entry is within 1 ulp of the exact sum."""
     torch = torch_cuda
-    m = n = k = 512
+    m = n = k = size
     rng = G.rng_for(0xC0FFEE + 2)
     A, B = G.spread_uniform(rng, m * k), G.spread_uniform(rng, k * n)
     C = Q.from_double(np.zeros(m * n))
     dA, dB, dC = to_dev(torch, A), to_dev(torch, B), to_dev(torch, C)
-    api.set_ozaki_slices(20)
+    api.set_ozaki_slices(s)
+    api.set_ozaki_digit_bits(b)
     api.gemm_dev("R", "N", "N", m, n, k, Q.scalar(1.0), dA, k, dB, n, Q.scalar(0.0), dC, n)
     torch.cuda.synchronize()
     got = to_host(dC)
-    rows, cols = rng.integers(0, m, 20000), rng.integers(0, n, 20000)
+    nsamp = 20000 if size <= 512 else 6000
+    rows, cols = rng.integers(0, m, nsamp), rng.integers(0, n, nsamp)
     R, r, _ = O.exact_gemm(k, A, k, 1, B, n, 1, rows, cols, nthreads=16)
     err = O.ulp_err(got[rows * n + cols], R, r)
     assert err.max() <= 1.0, err.max()
@@ -134,7 +140,6 @@ def test_ozaki_special_values(ozaki, O):
     A[5 * k + 1] = [0, 0x7FFF000000000000]   # +inf in row 5
     B[4 * n + 7] = [0, 0xFFFF000000000000]   # -inf in column 7
     C = Q.from_double(np.zeros(m * n))
-    api.set_ozaki_slices(20)
     got = C.copy()
     api.gemm("R", "N", "N", m, n, k, Q.scalar(1.0), A, k, B, n, Q.scalar(0.0), got, n)
     rows, cols = np.meshgrid(np.arange(m), np.arange(n), indexing="ij")
@@ -153,8 +158,7 @@ def test_ozaki_reference_c_interface(ozaki, O, sq):
     rng = G.rng_for(5)
     m, n, k = 40, 50, 60
     A, B, C = G.spread_uniform(rng, m * k), G.spread_uniform(rng, k * n), G.uniform_full(rng, m * n)
-    api.set_ozaki_slices(20)
     got = C.copy()
-    api.qgemm("R", "N", "N", m, n, k, 2.0, A, k, B, n, 0.5, got, n)
-    sums = E.gemm_sum(sq, m, n, k, A, k, 1, B, n, 1, 20)
+    api.qgemm("R", "N", "N", m, n, k, 2.0, A, k, B, n, 0.5, got, n)  # library defaults: 18 digits of 8 bits
+    sums = E.gemm_sum(sq, m, n, k, A, k, 1, B, n, 1, 18, 8)
     assert Q.same_bits(got, epilogue(O, Q.scalar(2.0), sums, Q.scalar(0.5), C)).all()
