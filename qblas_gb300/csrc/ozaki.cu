@@ -94,10 +94,11 @@ __global__ void ozaki_fill_kernel(int64_t n, int* __restrict__ S, uint32_t* __re
 // D[t * rows_pad * cols_pad + r * cols_pad + c] (bf16).  Block (32, 8):
 // x along columns (coalesced digit stores), y along rows; each digit is
 // stored as soon as it is extracted.
+template <int B>
 __global__ void __launch_bounds__(256)
     ozaki_split_kernel(int64_t rows, int64_t cols, int64_t rows_pad, int64_t cols_pad,
                        const q128* __restrict__ p, int64_t sr, int64_t sc,
-                       const int* __restrict__ S, int s, int b, __nv_bfloat16* __restrict__ D) {
+                       const int* __restrict__ S, int s, __nv_bfloat16* __restrict__ D) {
   const int64_t c = (int64_t)blockIdx.x * 32 + threadIdx.x;
   const int64_t r = (int64_t)blockIdx.y * 8 + threadIdx.y;
   if (c >= cols_pad || r >= rows_pad) return;
@@ -109,7 +110,7 @@ __global__ void __launch_bounds__(256)
     v = ld_cached(p + r * sr + c * sc);
     Sr = S[r];
   }
-  ozaki_digits_emit(v, Sr, s, b, [&](int t, int d) { out[t * plane] = __int2bfloat16_rn(d); });
+  ozaki_digits_emit<B>(v, Sr, s, [&](int t, int d) { out[t * plane] = __int2bfloat16_rn(d); });
 }
 
 // ---------------------------------------------------------------------------
@@ -444,6 +445,7 @@ struct OzakiFoldParams {
   const int* err;
 };
 
+template <int B>
 __global__ void __launch_bounds__(256) ozaki_fold_kernel(OzakiFoldParams P) {
   const int64_t j = (int64_t)blockIdx.x * 32 + threadIdx.x;
   const int64_t i = (int64_t)blockIdx.y * 8 + threadIdx.y;
@@ -468,9 +470,9 @@ __global__ void __launch_bounds__(256) ozaki_fold_kernel(OzakiFoldParams P) {
     for (int g = 0; g <= P.G; ++g) {
       int64_t v = 0;
       for (int p = 0; p < P.npass; ++p) v += P.C[((size_t)p * (P.G + 1) + g) * plane + off];
-      fold_step(f, v, P.b);
+      fold_step_t<B>(f, v);
     }
-    sum = fold_round(f, ozaki_fold_exp(P.S[i], P.F[j], P.G, P.b));
+    sum = fold_round(f, ozaki_fold_exp(P.S[i], P.F[j], P.G, B));
   }
   q128* cp = P.Cout + i * P.sci + j * P.scj;
   *cp = q_epilogue(P.alpha, sum, P.beta, *cp);
@@ -662,8 +664,13 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scr
     dim3 blk(32, 8);
     dim3 ga((unsigned)(L.k_pad / 32), (unsigned)(L.m_pad / 8));
     dim3 gb((unsigned)(L.k_pad / 32), (unsigned)(L.n_pad / 8));
-    ozaki_split_kernel<<<ga, blk, 0, st>>>(g.m, g.k, L.m_pad, L.k_pad, g.A, g.sai, g.sal, S, L.s, L.b, DA);
-    ozaki_split_kernel<<<gb, blk, 0, st>>>(g.n, g.k, L.n_pad, L.k_pad, g.B, g.sbj, g.sbl, F, L.s, L.b, DB);
+    if (L.b == 7) {
+      ozaki_split_kernel<7><<<ga, blk, 0, st>>>(g.m, g.k, L.m_pad, L.k_pad, g.A, g.sai, g.sal, S, L.s, DA);
+      ozaki_split_kernel<7><<<gb, blk, 0, st>>>(g.n, g.k, L.n_pad, L.k_pad, g.B, g.sbj, g.sbl, F, L.s, DB);
+    } else {
+      ozaki_split_kernel<8><<<ga, blk, 0, st>>>(g.m, g.k, L.m_pad, L.k_pad, g.A, g.sai, g.sal, S, L.s, DA);
+      ozaki_split_kernel<8><<<gb, blk, 0, st>>>(g.n, g.k, L.n_pad, L.k_pad, g.B, g.sbj, g.sbl, F, L.s, DB);
+    }
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
   }
   prof_record(pe, 1, st);
@@ -713,7 +720,10 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scr
   F2.err = err;
   if ((g.m + 7) / 8 > 65535) return cudaErrorInvalidConfiguration;
   dim3 fblk(32, 8), fgrid((unsigned)((g.n + 31) / 32), (unsigned)((g.m + 7) / 8));
-  ozaki_fold_kernel<<<fgrid, fblk, 0, st>>>(F2);
+  if (L.b == 7)
+    ozaki_fold_kernel<7><<<fgrid, fblk, 0, st>>>(F2);
+  else
+    ozaki_fold_kernel<8><<<fgrid, fblk, 0, st>>>(F2);
   e = cudaGetLastError();
   prof_record(pe, 3, st);
   if (pe) {

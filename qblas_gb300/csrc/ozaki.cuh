@@ -58,12 +58,29 @@ QB_HD uint32_t ozaki_special_flags(q128 a) {
   return q_sign(a) ? 4u : 2u;
 }
 
-// The s balanced base-2^b digits of a for scale S, passed to emit(t, d_t)
+// Bit field [p, p + B) of the 192-bit value (v2:v1:v0); p and B are
+// compile-time constants after unrolling, so the shifts are constant.
+template <int B>
+QB_HD uint32_t ozaki_field(uint64_t v0, uint64_t v1, uint64_t v2, int p) {
+  const uint64_t mask = (1ull << B) - 1;
+  const int limb = p >> 6, off = p & 63;
+  uint64_t lo = limb == 0 ? v0 : limb == 1 ? v1 : v2;
+  uint64_t x = lo >> off;
+  if (off + B > 64 && limb < 2) x |= (limb == 0 ? v1 : v2) << (64 - off);
+  return (uint32_t)(x & mask);
+}
+
+// The s balanced base-2^B digits of a for scale S, passed to emit(t, d_t)
 // from the least significant (t = s-1) to the most significant (t = 0).
-// Requires 1 <= s <= ozaki_max_digits(b); V is held in three 64-bit limbs
-// (b*s - 1 <= 175 bits).
-template <typename Emit>
-QB_HD void ozaki_digits_emit(q128 a, int S, int s, int b, Emit emit) {
+// V = trunc(|a| * 2^(B*s - 1 - S)) < 2^(B*s - 1) is cut into its raw B-bit
+// fields r_j (j = 0 least significant); a carry c (0 or 1) turns them into
+// balanced digits: d_j = r_j + c - 2^B and c = 1 when r_j + c >= 2^(B-1),
+// otherwise d_j = r_j + c and c = 0; the top digit takes r_{s-1} + c
+// unchanged, which stays in [0, 2^(B-1)].  The signs follow a.
+// Requires 1 <= s <= ozaki_max_digits(B).
+template <int B, typename Emit>
+QB_HD void ozaki_digits_emit(q128 a, int S, int s, Emit emit) {
+  constexpr int kMax = B == 7 ? 22 : 20;
   int be = q_bexp(a);
   if (be == kExpField || q_iszero(a) || S == kOzakiScaleEmpty) {
     for (int t = s - 1; t >= 0; --t) emit(t, 0);
@@ -73,8 +90,8 @@ QB_HD void ozaki_digits_emit(q128 a, int S, int s, int b, Emit emit) {
   uint64_t mh, ml;
   int E;
   q_unpack_norm(a, mh, ml, E);
-  // V = trunc(m * 2^(E + b*s - 113 - S)); the shift is at most b*s - 114.
-  int sh = E + b * s - 113 - S;
+  // V = trunc(m * 2^(E + B*s - 113 - S)); the shift is at most B*s - 114.
+  int sh = E + B * s - 113 - S;
   uint64_t v0, v1, v2;
   if (sh >= 0) {
     u256 t = u256_shl(u256_make(0, 0, mh, ml), sh);
@@ -88,41 +105,26 @@ QB_HD void ozaki_digits_emit(q128 a, int S, int s, int b, Emit emit) {
     v1 = t.w1;
     v2 = 0;
   }
-  // balanced digits from the least significant end: d in [-2^(b-1), 2^(b-1) - 1],
-  // top digit in [-2^(b-1), 2^(b-1)]
-  const uint64_t mask = (1ull << b) - 1, half = 1ull << (b - 1);
-  for (int t = s - 1; t >= 1; --t) {
-    int d = (int)(v0 & mask);
-    if ((uint64_t)d >= half) d -= (int)(1 << b);
-    // V = (V - d) / 2^b (V stays non-negative)
-    if (d >= 0) {
-      uint64_t n0 = v0 - (uint64_t)d;
-      uint64_t br = n0 > v0;
-      v0 = n0;
-      uint64_t n1 = v1 - br;
-      br = br && v1 == 0;
-      v1 = n1;
-      v2 -= br;
-    } else {
-      uint64_t n0 = v0 + (uint64_t)(-d);
-      uint64_t c = n0 < v0;
-      v0 = n0;
-      v1 += c;
-      c = c && v1 == 0;
-      v2 += c;
+  int carry = 0;
+#pragma unroll
+  for (int j = 0; j < kMax; ++j) {
+    if (j < s) {
+      int d = (int)ozaki_field<B>(v0, v1, v2, B * j) + carry;
+      if (j < s - 1) {
+        carry = d >= (1 << (B - 1));
+        d -= carry << B;
+      }
+      emit(s - 1 - j, neg ? -d : d);
     }
-    v0 = (v0 >> b) | (v1 << (64 - b));
-    v1 = (v1 >> b) | (v2 << (64 - b));
-    v2 >>= b;
-    emit(t, neg ? -d : d);
   }
-  // |V| < 2^(b*s-1) keeps the top digit in [0, 2^(b-1)]
-  emit(0, neg ? -(int)v0 : (int)v0);
 }
 
-// The digits into an array: digits[t] for t < s.
+// The digits into an array: digits[t] for t < s (b = 7 or 8).
 QB_HD void ozaki_digits(q128 a, int S, int s, int b, int* digits) {
-  ozaki_digits_emit(a, S, s, b, [&](int t, int d) { digits[t] = d; });
+  if (b == 7)
+    ozaki_digits_emit<7>(a, S, s, [&](int t, int d) { digits[t] = d; });
+  else
+    ozaki_digits_emit<8>(a, S, s, [&](int t, int d) { digits[t] = d; });
 }
 
 // 192-bit two's complement accumulator for the fold (Horner in base 2^b).
@@ -132,8 +134,10 @@ struct fold192 {
 
 QB_HD void fold_init(fold192& f) { f.w0 = f.w1 = f.w2 = 0; }
 
-// f = f * 2^b + v
-QB_HD void fold_step(fold192& f, int64_t v, int b) {
+// f = f * 2^B + v
+template <int B>
+QB_HD void fold_step_t(fold192& f, int64_t v) {
+  const int b = B;
   f.w2 = (f.w2 << b) | (f.w1 >> (64 - b));
   f.w1 = (f.w1 << b) | (f.w0 >> (64 - b));
   f.w0 = f.w0 << b;
@@ -148,6 +152,13 @@ QB_HD void fold_step(fold192& f, int64_t v, int b) {
   c1 += n1 < t1;
   f.w1 = n1;
   f.w2 = f.w2 + ext + c1;
+}
+
+QB_HD void fold_step(fold192& f, int64_t v, int b) {
+  if (b == 7)
+    fold_step_t<7>(f, v);
+  else
+    fold_step_t<8>(f, v);
 }
 
 // value = f * 2^e rounded to binary128
