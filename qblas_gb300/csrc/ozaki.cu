@@ -447,9 +447,12 @@ struct OzakiFoldParams {
 
 template <int B>
 __global__ void __launch_bounds__(256) ozaki_fold_kernel(OzakiFoldParams P) {
+  constexpr int kMaxG = (B == 7 ? 22 : 20);
   const int64_t j = (int64_t)blockIdx.x * 32 + threadIdx.x;
   const int64_t i = (int64_t)blockIdx.y * 8 + threadIdx.y;
   if (i >= P.m || j >= P.n) return;
+  q128* cp = P.Cout + i * P.sci + j * P.scj;
+  const q128 cold = *cp;
   q128 sum;
   if (*P.err) {
     sum = q_nan();
@@ -462,20 +465,32 @@ __global__ void __launch_bounds__(256) ozaki_fold_kernel(OzakiFoldParams P) {
                        qop_unpack(ld_cached(P.B + l * P.sbl + j * P.sbj)));
     sum = wacc_round(acc);
   } else {
+    const size_t plane = (size_t)P.m_pad * P.n_pad;
+    const int32_t* src = P.C + (size_t)i * P.n_pad + j;
+    int32_t v[kMaxG];
+    // all diagonal loads first (independent), then the Horner fold
+#pragma unroll
+    for (int g = 0; g < kMaxG; ++g) v[g] = g <= P.G ? __ldcs(src + g * plane) : 0;
     fold192 f;
     fold_init(f);
-    const size_t plane = (size_t)P.m_pad * P.n_pad;
-    const size_t off = (size_t)i * P.n_pad + j;
-    // Horner over diagonals, most significant first; k passes add up
-    for (int g = 0; g <= P.G; ++g) {
-      int64_t v = 0;
-      for (int p = 0; p < P.npass; ++p) v += P.C[((size_t)p * (P.G + 1) + g) * plane + off];
-      fold_step_t<B>(f, v);
+    if (P.npass == 1) {
+#pragma unroll
+      for (int g = 0; g < kMaxG; ++g)
+        if (g <= P.G) fold_step_t<B>(f, v[g]);
+    } else {
+      const size_t pass = (size_t)(P.G + 1) * plane;
+#pragma unroll
+      for (int g = 0; g < kMaxG; ++g) {
+        if (g <= P.G) {
+          int64_t t = v[g];
+          for (int p = 1; p < P.npass; ++p) t += __ldcs(src + p * pass + g * plane);
+          fold_step_t<B>(f, t);
+        }
+      }
     }
     sum = fold_round(f, ozaki_fold_exp(P.S[i], P.F[j], P.G, B));
   }
-  q128* cp = P.Cout + i * P.sci + j * P.scj;
-  *cp = q_epilogue(P.alpha, sum, P.beta, *cp);
+  *cp = q_epilogue(P.alpha, sum, P.beta, cold);
 }
 
 // ---------------------------------------------------------------------------
