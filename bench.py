@@ -236,6 +236,107 @@ def hbm_roofline(pk, src, nbytes, ms_per_launch):
             "traffic": None, "peak_source": src}
 
 
+def batched_config4(torch, api, rank, reps=3):
+    """10,000 qgemm (m, n, k log-uniform in [8, 256]), 10,000 qgemv (m, n in
+    [16, 2048]) and 10,000 qdot (n in [64, 65536]) with full-mantissa uniform
+    values, row-major 'N', alpha = 1, beta = 0: one persistent launch (CUDA
+    graph replay) against the same problems launched one call at a time."""
+    rng = G.rng_for(4000 + rank)
+    gm = G.log_uniform_int(rng, 8, 256, 3 * 10000).reshape(3, 10000)
+    gv = G.log_uniform_int(rng, 16, 2048, 2 * 10000).reshape(2, 10000)
+    dn = G.log_uniform_int(rng, 64, 65536, 10000)
+    sizes = []
+    for i in range(10000):
+        m, n, k = int(gm[0, i]), int(gm[1, i]), int(gm[2, i])
+        sizes.append((0, m, n, k, m * k, k * n, m * n))
+    for i in range(10000):
+        m, n = int(gv[0, i]), int(gv[1, i])
+        sizes.append((1, m, n, 0, m * n, n, m))
+    for i in range(10000):
+        n = int(dn[i])
+        sizes.append((2, 0, n, 0, n, n, 1))
+    total = sum(a + b + c for _, _, _, _, a, b, c in sizes)
+    buf = G.uniform_full_device(torch, total, seed=4100 + rank)
+    base = buf.data_ptr()
+    probs = np.zeros(len(sizes), dtype=api.PROBLEM_DTYPE)
+    one, zero = Q.scalar(1.0)[0], Q.scalar(0.0)[0]
+    off = 0
+    flops = 0.0
+    for p, (op, m, n, k, sa, sb, sc) in zip(probs, sizes):
+        p["op"], p["layout"], p["transa"], p["transb"] = op, b"R", b"N", b"N"
+        p["m"], p["n"], p["k"] = m, n, k
+        p["alpha"], p["beta"] = one, zero
+        p["A"], p["B"], p["C"] = base + 16 * off, base + 16 * (off + sa), base + 16 * (off + sa + sb)
+        if op == 0:
+            p["lda"], p["ldb"], p["ldc"] = k, n, n
+            flops += 2.0 * m * n * k
+        elif op == 1:
+            p["lda"], p["ldb"], p["ldc"] = n, 1, 1
+            flops += 2.0 * m * n
+        else:
+            p["lda"], p["ldb"], p["ldc"] = 1, 1, 1
+            flops += 2.0 * n
+        off += sa + sb + sc
+    t0 = time.perf_counter()
+    plan = api.BatchPlan(probs)
+    plan_s = time.perf_counter() - t0
+    info = plan.info()
+    st = torch.cuda.Stream()
+    st.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(st):
+        plan.execute(stream=st)
+        torch.cuda.synchronize()
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph, stream=st):
+            plan.execute(stream=st)
+    torch.cuda.synchronize()
+    graph.replay()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        graph.replay()
+    e1.record()
+    torch.cuda.synchronize()
+    ms_batched = e0.elapsed_time(e1) / reps
+    # the same problems, one library call each, on the current stream
+    lib = api.load()
+    cs = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    a_p, b_p = one.ctypes.data_as(ctypes.c_void_p), zero.ctypes.data_as(ctypes.c_void_p)
+    A_, B_, C_ = (ctypes.c_void_p(int(v)) for v in (0, 0, 0))
+
+    def one_by_one():
+        for p in probs:
+            op = int(p["op"])
+            A_, B_, C_ = ctypes.c_void_p(int(p["A"])), ctypes.c_void_p(int(p["B"])), ctypes.c_void_p(int(p["C"]))
+            if op == 0:
+                lib.quadblas_qgemm_dev(b"R", b"N", b"N", int(p["m"]), int(p["n"]), int(p["k"]), a_p, A_,
+                                       int(p["lda"]), B_, int(p["ldb"]), b_p, C_, int(p["ldc"]), cs)
+            elif op == 1:
+                lib.quadblas_qgemv_dev(b"R", b"N", int(p["m"]), int(p["n"]), a_p, A_, int(p["lda"]), B_, 1, b_p,
+                                       C_, 1, cs)
+            else:
+                lib.quadblas_qdot_dev(int(p["n"]), A_, 1, B_, 1, C_, cs)
+
+    one_by_one()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e0.record()
+    one_by_one()
+    e1.record()
+    torch.cuda.synchronize()
+    wall_single = time.perf_counter() - t0
+    ms_single = max(e0.elapsed_time(e1), wall_single * 1e3)
+    plan.close()
+    del buf
+    torch.cuda.empty_cache()
+    return {"problems": len(sizes), "gflops": round(flops / (ms_batched * 1e-3) / 1e9, 2),
+            "ms_batched_graph_replay": round(ms_batched, 3), "ms_one_call_per_problem": round(ms_single, 3),
+            "speedup_vs_one_by_one": round(ms_single / ms_batched, 2), "plan_ms": round(plan_s * 1e3, 1),
+            "work_items": info["items"], "grain": info["grain"], "launches_per_batch": 1,
+            "method": "soft-float wide accumulator for every problem", "quad_flops": flops}
+
+
 def profile_read(lib):
     out = (ctypes.c_double * 4)()
     calls = ctypes.c_int(0)
@@ -419,6 +520,7 @@ def main():
                 del S
                 torch.cuda.empty_cache()
             api.set_method(1)
+            secondary["batched_config4"] = batched_config4(torch, api, rank)
             S = Qgemm(torch, 512, 512, 512, seed=0xC0FFEE, spread=False)
             ms2 = time_steps(torch, S.step, 20, 3, dist) / 20
             secondary["qgemm512_softfloat"] = {"value": round(S.flops() / (ms2 * 1e-3) / 1e9, 3),

@@ -139,6 +139,46 @@ int quadblas_qgemm_dev(char layout, char transa, char transb, int64_t m, int64_t
 int quadblas_qdot_dev_noalloc(int64_t n, const void *dx, int64_t incx, const void *dy,
                               int64_t incy, void *d_result, void *stream);
 
+/* ---- Part 4: batched problems in one persistent launch (no reference
+ * counterpart; each problem has the semantics of the single call).
+ *   QBLAS_OP_GEMM: C = alpha*op(A)*op(B) + beta*C as quadblas_qgemm_dev
+ *                  (layout, transa, transb, m, n, k, A/lda, B/ldb, C/ldc);
+ *   QBLAS_OP_GEMV: y = alpha*op(A)*x + beta*y as quadblas_qgemv_dev with
+ *                  trans = transa, A/lda, x = B (incx = ldb), y = C (incy = ldc);
+ *   QBLAS_OP_DOT : *C = sum_i x_i y_i with x = A (incx = lda), y = B
+ *                  (incy = ldb), n elements.
+ * All pointers are device pointers (16-byte aligned); alpha and beta hold
+ * binary128 values (low word first).  quadblas_batch_plan cuts the problems
+ * into equal-cost work items (granularity from the autotuner) and uploads
+ * them; quadblas_batch_execute runs the whole batch on `stream` with one
+ * memset and one persistent kernel and allocates nothing, so it can be
+ * recorded in a CUDA graph and replayed; concurrent executions of one plan
+ * must not overlap.  quadblas_batch_autotune times a calibration batch at
+ * several granularities and caches the best per device (in memory and in
+ * $QBLAS_AUTOTUNE_CACHE, default $HOME/.cache/qblas_gb300_autotune.txt). */
+enum { QBLAS_OP_GEMM = 0, QBLAS_OP_GEMV = 1, QBLAS_OP_DOT = 2 };
+
+typedef struct {
+  int32_t op;
+  char layout, transa, transb, reserved;
+  int64_t m, n, k;
+  uint64_t alpha[2], beta[2];
+  const void *A;
+  int64_t lda;
+  const void *B;
+  int64_t ldb;
+  void *C;
+  int64_t ldc;
+} qblas_problem;
+
+int quadblas_batch_plan(const qblas_problem *problems, int64_t count, void **plan);
+int quadblas_batch_execute(void *plan, void *stream);
+int quadblas_batch_destroy(void *plan);
+/* info4: work items, granularity (products per item), blocks, split groups */
+int quadblas_batch_info(void *plan, int64_t *info4);
+int quadblas_batch_autotune(int64_t *grain_out);
+int quadblas_batch_set_grain(int64_t grain);
+
 /* ---- Configuration and errors (no reference counterpart) -------------- */
 /* qgemm method: QBLAS_METHOD_AUTO, _SOFTFLOAT or _OZAKI. */
 int quadblas_set_method(int method);

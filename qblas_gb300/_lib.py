@@ -41,6 +41,13 @@ _SIGS = {
     "quadblas_qgemv_dev": (ci, [cc, cc, i64, i64, vp, vp, i64, vp, i64, vp, vp, i64, vp]),
     "quadblas_qgemm_dev": (ci, [cc, cc, cc, i64, i64, i64, vp, vp, i64, vp, i64, vp, vp, i64, vp]),
     "quadblas_qdot_dev_noalloc": (ci, [i64, vp, i64, vp, i64, vp, vp]),
+    # batched
+    "quadblas_batch_plan": (ci, [vp, i64, vp]),
+    "quadblas_batch_execute": (ci, [vp, vp]),
+    "quadblas_batch_destroy": (ci, [vp]),
+    "quadblas_batch_info": (ci, [vp, vp]),
+    "quadblas_batch_autotune": (ci, [vp]),
+    "quadblas_batch_set_grain": (ci, [i64]),
     # configuration
     "quadblas_set_method": (ci, [ci]),
     "quadblas_get_method": (ci, []),

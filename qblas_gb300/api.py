@@ -139,3 +139,54 @@ def set_ozaki_slices(s: int) -> None:
 
 def set_ozaki_digit_bits(b: int) -> None:
     check(load().quadblas_set_ozaki_digit_bits(b))
+
+
+# ---- batched problems (one persistent launch) -------------------------------
+OP_GEMM, OP_GEMV, OP_DOT = 0, 1, 2
+
+PROBLEM_DTYPE = np.dtype([("op", "<i4"), ("layout", "S1"), ("transa", "S1"), ("transb", "S1"),
+                          ("reserved", "S1"), ("m", "<i8"), ("n", "<i8"), ("k", "<i8"),
+                          ("alpha", "<u8", (2,)), ("beta", "<u8", (2,)), ("A", "<u8"), ("lda", "<i8"),
+                          ("B", "<u8"), ("ldb", "<i8"), ("C", "<u8"), ("ldc", "<i8")], align=True)
+assert PROBLEM_DTYPE.itemsize == 112
+
+
+class BatchPlan:
+    """A planned batch (quadblas_batch_plan); execute() replays it on a stream."""
+
+    def __init__(self, problems: np.ndarray):
+        problems = np.ascontiguousarray(problems, dtype=PROBLEM_DTYPE)
+        self._problems = problems
+        h = ctypes.c_void_p()
+        check(load().quadblas_batch_plan(problems.ctypes.data_as(ctypes.c_void_p), len(problems),
+                                         ctypes.byref(h)))
+        self.handle = h
+
+    def execute(self, stream=None) -> None:
+        check(load().quadblas_batch_execute(self.handle, _stream(stream)))
+
+    def info(self) -> dict:
+        out = (ctypes.c_int64 * 4)()
+        check(load().quadblas_batch_info(self.handle, out))
+        return {"items": out[0], "grain": out[1], "blocks": out[2], "split_groups": out[3]}
+
+    def close(self) -> None:
+        if self.handle:
+            load().quadblas_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def batch_autotune() -> int:
+    g = ctypes.c_int64(0)
+    check(load().quadblas_batch_autotune(ctypes.byref(g)))
+    return g.value
+
+
+def batch_set_grain(grain: int) -> None:
+    check(load().quadblas_batch_set_grain(grain))

@@ -1,0 +1,763 @@
+// Batched binary128 BLAS: thousands of uneven qgemm / qgemv / qdot problems
+// in one persistent launch.  No counterpart in the reference (which has one
+// synchronous CPU call per problem); each problem has the semantics of the
+// corresponding single call (level1.hpp:80, level2.hpp:85, level3.hpp:215
+// with the epilogues of level2.hpp:48 / level3.hpp:107).
+//
+// Plan (host): every problem is cut into work items of roughly equal cost
+// (cost = number of products): qgemm into 32 x 32 C tiles, split along k
+// when a tile's k-loop is long; qgemv into groups of 8 rows, split along
+// the columns for long rows; qdot into chunks.  Items are sorted by
+// decreasing cost (longest-processing-time first).  The item granularity is
+// chosen by an autotuner that times a calibration batch once per device
+// (cached in memory and in a file).
+//
+// Execute: a counter reset and one persistent kernel with (SM count x
+// resident blocks) blocks; each block takes the next item from an atomic
+// queue.  Items of a split group write their partial wide accumulators to
+// scratch; the block that completes a group (atomic arrival count) merges
+// the partials in index order and applies the epilogue, so results do not
+// depend on scheduling.  No block ever waits for another, so nothing can
+// spin.  Execute allocates nothing and issues one memset and one kernel,
+// so it can be recorded in a CUDA graph.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "kernels.h"
+#include "quadblas_gpu.h"
+#include "reduce.cuh"
+
+namespace qb {
+
+constexpr int kBThreads = 256;
+constexpr int kBTile = 32;   // gemm tile edge
+constexpr int kBTK = 16;     // gemm k slice staged in shared memory
+constexpr int kBRows = 8;    // gemv rows per item (one warp each)
+
+enum : int32_t { kOpGemm = 0, kOpGemv = 1, kOpDot = 2 };
+
+struct BProb {
+  int32_t op;
+  int32_t nparts;  // items that reduce into each output group (1 = no split)
+  int64_t m, n, k;
+  q128 alpha, beta;
+  const q128* A;
+  int64_t sai, sal;  // gemm op(A)(i,l); gemv op(A)(i,j); dot: x stride in sal
+  const q128* B;
+  int64_t sbl, sbj;  // gemm op(B)(l,j); gemv: x stride in sbl; dot: y stride in sbl
+  q128* C;
+  int64_t sci, scj;  // gemm C(i,j); gemv: y stride in sci; dot: result
+  int64_t part_base;   // first partial-accumulator slot of this problem
+  int64_t group_base;  // first arrival counter of this problem
+};
+
+struct BItem {
+  int32_t prob;
+  int32_t part;   // index within the split group
+  int64_t i0, j0; // gemm tile origin / gemv first row / unused
+  int64_t l0, l1; // k range (gemm), column range (gemv), element range (dot)
+  int64_t group;  // output group within the problem (tile / row block / 0)
+};
+
+// ---------------------------------------------------------------------------
+// device
+// ---------------------------------------------------------------------------
+struct BTile {
+  uint32_t m0[kBTK][kBTile], m1[kBTK][kBTile], m2[kBTK][kBTile], m3[kBTK][kBTile];
+  int32_t e[kBTK][kBTile];
+  uint32_t sc[kBTK][kBTile];
+};
+
+struct BShared {
+  BTile a, b;
+  wacc red[kBThreads / 32];
+  int item;
+  int last;
+};
+
+__device__ __forceinline__ void btile_put(BTile& t, int kk, int idx, q128 v) {
+  qop o = qop_unpack(v);
+  t.m0[kk][idx] = o.m0;
+  t.m1[kk][idx] = o.m1;
+  t.m2[kk][idx] = o.m2;
+  t.m3[kk][idx] = o.m3;
+  t.e[kk][idx] = o.e;
+  t.sc[kk][idx] = o.s | (o.cls << 1);
+}
+
+__device__ __forceinline__ qop btile_get(const BTile& t, int kk, int idx) {
+  qop o;
+  o.m0 = t.m0[kk][idx];
+  o.m1 = t.m1[kk][idx];
+  o.m2 = t.m2[kk][idx];
+  o.m3 = t.m3[kk][idx];
+  o.e = t.e[kk][idx];
+  uint32_t sc = t.sc[kk][idx];
+  o.s = sc & 1u;
+  o.cls = sc >> 1;
+  return o;
+}
+
+__device__ __forceinline__ wacc wacc_ldcg(const wacc* p) {
+  const uint32_t* q = reinterpret_cast<const uint32_t*>(p);
+  wacc a;
+  a.w0 = __ldcg(q + 0);
+  a.w1 = __ldcg(q + 1);
+  a.w2 = __ldcg(q + 2);
+  a.w3 = __ldcg(q + 3);
+  a.w4 = __ldcg(q + 4);
+  a.w5 = __ldcg(q + 5);
+  a.w6 = __ldcg(q + 6);
+  a.w7 = __ldcg(q + 7);
+  a.e = (int32_t)__ldcg(q + 8);
+  a.flags = __ldcg(q + 9);
+  return a;
+}
+
+// Marks one item of a split group done; true in every thread of the block
+// that completed the group.  Partials written before the call are visible
+// to that block afterwards.
+__device__ __forceinline__ bool group_arrive(BShared& sh, int* counter, int nparts) {
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int prev = atomicAdd(counter, 1);
+    sh.last = prev == nparts - 1;
+    if (sh.last) *counter = 0;  // ready for the next execution
+  }
+  __syncthreads();
+  bool last = sh.last != 0;
+  if (last) __threadfence();
+  return last;
+}
+
+__device__ void run_gemm_item(BShared& sh, const BProb& P, const BItem& it, wacc* partials,
+                              int* counters) {
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  const q128 zero = q_zero(0);
+  wacc c[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) wacc_init(c[q]);
+  for (int64_t l0 = it.l0; l0 < it.l1; l0 += kBTK) {
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+      int e = tid + r * kBThreads;
+      int ar = e >> 4, ak = e & 15;
+      int64_t gi = it.i0 + ar, gl = l0 + ak;
+      q128 av = (gi < P.m && gl < it.l1) ? ld_cached(P.A + gi * P.sai + gl * P.sal) : zero;
+      int bk = e >> 5, bc = e & 31;
+      int64_t bl = l0 + bk, gj = it.j0 + bc;
+      q128 bv = (bl < it.l1 && gj < P.n) ? ld_cached(P.B + bl * P.sbl + gj * P.sbj) : zero;
+      btile_put(sh.a, ak, ar, av);
+      btile_put(sh.b, bk, bc, bv);
+    }
+    __syncthreads();
+#pragma unroll 2
+    for (int kk = 0; kk < kBTK; ++kk) {
+      qop a0 = btile_get(sh.a, kk, 2 * ty), a1 = btile_get(sh.a, kk, 2 * ty + 1);
+      qop b0 = btile_get(sh.b, kk, 2 * tx), b1 = btile_get(sh.b, kk, 2 * tx + 1);
+      wacc_add_product(c[0], a0, b0);
+      wacc_add_product(c[1], a0, b1);
+      wacc_add_product(c[2], a1, b0);
+      wacc_add_product(c[3], a1, b1);
+    }
+    __syncthreads();
+  }
+  if (P.nparts > 1) {
+    // partial slot layout: [group][part][thread][4]
+    wacc* mine = partials + P.part_base + ((it.group * P.nparts + it.part) * kBThreads + tid) * 4;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) mine[q] = c[q];
+    if (!group_arrive(sh, counters + P.group_base + it.group, P.nparts)) return;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) wacc_init(c[q]);
+    for (int p = 0; p < P.nparts; ++p) {
+      const wacc* src = partials + P.part_base + ((it.group * P.nparts + p) * kBThreads + tid) * 4;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) wacc_merge(c[q], wacc_ldcg(src + q));
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    int64_t i = it.i0 + 2 * ty + (q >> 1), j = it.j0 + 2 * tx + (q & 1);
+    if (i < P.m && j < P.n) {
+      q128* p = P.C + i * P.sci + j * P.scj;
+      *p = q_epilogue(P.alpha, wacc_round(c[q]), P.beta, *p);
+    }
+  }
+}
+
+__device__ void run_gemv_item(BShared& sh, const BProb& P, const BItem& it, wacc* partials,
+                              int* counters) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t row = it.i0 + warp;
+  wacc acc;
+  wacc_init(acc);
+  if (row < P.m) {
+    const q128* Ar = P.A + row * P.sai;
+    for (int64_t j = it.l0 + lane; j < it.l1; j += 32)
+      wacc_add_product(acc, qop_unpack(ld_cached(Ar + j * P.sal)), qop_unpack(ld_cached(P.B + j * P.sbl)));
+  }
+  wacc_warp_reduce(acc);
+  if (P.nparts > 1) {
+    wacc* slot = partials + P.part_base + (it.group * P.nparts + it.part) * kBRows + warp;
+    if (lane == 0) *slot = acc;
+    if (!group_arrive(sh, counters + P.group_base + it.group, P.nparts)) return;
+    if (lane == 0) {
+      wacc_init(acc);
+      for (int p = 0; p < P.nparts; ++p)
+        wacc_merge(acc, wacc_ldcg(partials + P.part_base + (it.group * P.nparts + p) * kBRows + warp));
+    }
+  }
+  if (lane == 0 && row < P.m) {
+    q128* yp = P.C + row * P.sci;
+    *yp = q_epilogue(P.alpha, wacc_round(acc), P.beta, *yp);
+  }
+}
+
+__device__ void run_dot_item(BShared& sh, const BProb& P, const BItem& it, wacc* partials,
+                             int* counters) {
+  wacc acc;
+  wacc_init(acc);
+  for (int64_t i = it.l0 + threadIdx.x; i < it.l1; i += kBThreads)
+    wacc_add_product(acc, qop_unpack(ld_cached(P.A + i * P.sal)), qop_unpack(ld_cached(P.B + i * P.sbl)));
+  wacc_block_reduce(acc, sh.red);
+  if (P.nparts > 1) {
+    if (threadIdx.x == 0) partials[P.part_base + it.part] = acc;
+    if (!group_arrive(sh, counters + P.group_base, P.nparts)) return;
+    if (threadIdx.x == 0) {
+      wacc_init(acc);
+      for (int p = 0; p < P.nparts; ++p) wacc_merge(acc, wacc_ldcg(partials + P.part_base + p));
+    }
+  }
+  if (threadIdx.x == 0) *P.C = wacc_round(acc);
+}
+
+__global__ void __launch_bounds__(kBThreads)
+    batched_persistent_kernel(const BProb* __restrict__ probs, const BItem* __restrict__ items,
+                              int64_t nitems, int* queue, int* counters, wacc* partials) {
+  __shared__ BShared sh;
+  while (true) {
+    if (threadIdx.x == 0) sh.item = atomicAdd(queue, 1);
+    __syncthreads();
+    const int64_t idx = sh.item;
+    __syncthreads();
+    if (idx >= nitems) break;
+    const BItem it = items[idx];
+    const BProb P = probs[it.prob];
+    if (P.op == kOpGemm)
+      run_gemm_item(sh, P, it, partials, counters);
+    else if (P.op == kOpGemv)
+      run_gemv_item(sh, P, it, partials, counters);
+    else
+      run_dot_item(sh, P, it, partials, counters);
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// host: plan, execute, autotune
+// ---------------------------------------------------------------------------
+struct BatchPlan {
+  int device = -1;
+  int64_t nitems = 0, nprobs = 0, ngroups = 0, nparts = 0;
+  int64_t grain = 0;
+  BProb* d_probs = nullptr;
+  BItem* d_items = nullptr;
+  int* d_counters = nullptr;  // [0] = queue head, [1..] group counters
+  wacc* d_partials = nullptr;
+  int blocks = 0;
+};
+
+static bool is_trans(char t) { return t == 'T' || t == 't' || t == 'C' || t == 'c'; }
+static bool is_col(char l) { return l == 'C' || l == 'c'; }
+
+static int resolve(const qblas_problem& q, BProb& P) {
+  memset(&P, 0, sizeof(P));
+  memcpy(&P.alpha, q.alpha, 16);
+  memcpy(&P.beta, q.beta, 16);
+  P.A = (const q128*)q.A;
+  P.B = (const q128*)q.B;
+  P.C = (q128*)q.C;
+  if (!q.C) return kErrInvalidValue;
+  if (q.op == QBLAS_OP_GEMM) {
+    if (q.m < 0 || q.n < 0 || q.k < 0) return kErrInvalidValue;
+    bool col = is_col(q.layout), ta = is_trans(q.transa), tb = is_trans(q.transb);
+    int64_t ar = ta ? q.k : q.m, ac = ta ? q.m : q.k, br = tb ? q.n : q.k, bc = tb ? q.k : q.n;
+    if (!col) {
+      if (q.lda < std::max<int64_t>(1, ac) || q.ldb < std::max<int64_t>(1, bc) ||
+          q.ldc < std::max<int64_t>(1, q.n))
+        return kErrInvalidValue;
+      P.sai = ta ? 1 : q.lda;
+      P.sal = ta ? q.lda : 1;
+      P.sbl = tb ? 1 : q.ldb;
+      P.sbj = tb ? q.ldb : 1;
+      P.sci = q.ldc;
+      P.scj = 1;
+    } else {
+      if (q.lda < std::max<int64_t>(1, ar) || q.ldb < std::max<int64_t>(1, br) ||
+          q.ldc < std::max<int64_t>(1, q.m))
+        return kErrInvalidValue;
+      P.sai = ta ? q.lda : 1;
+      P.sal = ta ? 1 : q.lda;
+      P.sbl = tb ? q.ldb : 1;
+      P.sbj = tb ? 1 : q.ldb;
+      P.sci = 1;
+      P.scj = q.ldc;
+    }
+    P.op = kOpGemm;
+    P.m = q.m;
+    P.n = q.n;
+    P.k = q.k;
+  } else if (q.op == QBLAS_OP_GEMV) {
+    int64_t m = q.m, n = q.n;
+    bool col = is_col(q.layout);
+    if (m < 0 || n < 0) return kErrInvalidValue;
+    if (is_trans(q.transa)) {
+      std::swap(m, n);
+      col = !col;
+    }
+    if (!col) {
+      if (q.lda < std::max<int64_t>(1, n)) return kErrInvalidValue;
+      P.sai = q.lda;
+      P.sal = 1;
+    } else {
+      if (q.lda < std::max<int64_t>(1, m)) return kErrInvalidValue;
+      P.sai = 1;
+      P.sal = q.lda;
+    }
+    if ((m > 0 && n > 0) && (q.ldb <= 0 || q.ldc <= 0)) return kErrInvalidValue;
+    P.op = kOpGemv;
+    P.m = m;
+    P.n = n;
+    P.sbl = q.ldb;  // incx
+    P.sci = q.ldc;  // incy
+  } else if (q.op == QBLAS_OP_DOT) {
+    if (q.n < 0 || (q.n > 0 && (q.lda <= 0 || q.ldb <= 0))) return kErrInvalidValue;
+    P.op = kOpDot;
+    P.n = q.n;
+    P.sal = q.lda;  // incx
+    P.sbl = q.ldb;  // incy
+  } else {
+    return kErrInvalidValue;
+  }
+  return kOk;
+}
+
+static int64_t cdiv(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+// Items of all problems for a granularity `grain` (products per item).
+static int build_items(std::vector<BProb>& probs, int64_t grain, std::vector<BItem>& items,
+                       std::vector<int64_t>& cost, int64_t& ngroups, int64_t& nparts_total) {
+  items.clear();
+  cost.clear();
+  ngroups = 0;
+  nparts_total = 0;
+  for (size_t pi = 0; pi < probs.size(); ++pi) {
+    BProb& P = probs[pi];
+    P.group_base = 1 + ngroups;  // counter 0 is the queue head
+    P.part_base = nparts_total;
+    P.nparts = 1;
+    if (P.op == kOpGemm) {
+      if (P.m == 0 || P.n == 0 || P.k == 0) continue;  // level3.hpp:221
+      int64_t tm = cdiv(P.m, kBTile), tn = cdiv(P.n, kBTile);
+      int64_t kslices = cdiv(P.k, kBTK);
+      int64_t per = (int64_t)kBTile * kBTile * P.k;
+      int64_t parts = std::min<int64_t>(std::max<int64_t>(1, cdiv(per, grain)), kslices);
+      int64_t kper = cdiv(kslices, parts) * kBTK;
+      parts = cdiv(P.k, kper);
+      P.nparts = (int32_t)parts;
+      for (int64_t a = 0; a < tm; ++a)
+        for (int64_t b = 0; b < tn; ++b)
+          for (int64_t p = 0; p < parts; ++p) {
+            BItem it;
+            it.prob = (int32_t)pi;
+            it.part = (int32_t)p;
+            it.i0 = a * kBTile;
+            it.j0 = b * kBTile;
+            it.l0 = p * kper;
+            it.l1 = std::min(P.k, (p + 1) * kper);
+            it.group = a * tn + b;
+            items.push_back(it);
+            cost.push_back((int64_t)kBTile * kBTile * (it.l1 - it.l0));
+          }
+      if (parts > 1) {
+        ngroups += tm * tn;
+        nparts_total += tm * tn * parts * kBThreads * 4;
+      }
+    } else if (P.op == kOpGemv) {
+      if (P.m == 0 || P.n == 0) continue;  // level2.hpp:21,61
+      int64_t rb = cdiv(P.m, kBRows);
+      int64_t per = (int64_t)kBRows * P.n;
+      int64_t parts = std::min<int64_t>(std::max<int64_t>(1, cdiv(per, grain)), cdiv(P.n, 256));
+      int64_t cper = cdiv(P.n, parts);
+      parts = cdiv(P.n, cper);
+      P.nparts = (int32_t)parts;
+      for (int64_t a = 0; a < rb; ++a)
+        for (int64_t p = 0; p < parts; ++p) {
+          BItem it;
+          it.prob = (int32_t)pi;
+          it.part = (int32_t)p;
+          it.i0 = a * kBRows;
+          it.j0 = 0;
+          it.l0 = p * cper;
+          it.l1 = std::min(P.n, (p + 1) * cper);
+          it.group = a;
+          items.push_back(it);
+          cost.push_back((int64_t)kBRows * (it.l1 - it.l0));
+        }
+      if (parts > 1) {
+        ngroups += rb;
+        nparts_total += rb * parts * kBRows;
+      }
+    } else {
+      int64_t parts = std::max<int64_t>(1, cdiv(P.n, grain));
+      if (P.n == 0) parts = 1;
+      int64_t cper = std::max<int64_t>(1, cdiv(P.n, parts));
+      parts = P.n == 0 ? 1 : cdiv(P.n, cper);
+      P.nparts = (int32_t)parts;
+      for (int64_t p = 0; p < parts; ++p) {
+        BItem it;
+        it.prob = (int32_t)pi;
+        it.part = (int32_t)p;
+        it.i0 = it.j0 = 0;
+        it.l0 = p * cper;
+        it.l1 = std::min(P.n, (p + 1) * cper);
+        it.group = 0;
+        items.push_back(it);
+        cost.push_back(2 * (it.l1 - it.l0) + 256);
+      }
+      if (parts > 1) {
+        ngroups += 1;
+        nparts_total += parts;
+      }
+    }
+  }
+  // longest processing time first (stable, so equal costs keep problem order)
+  std::vector<int64_t> order(items.size());
+  for (size_t i = 0; i < order.size(); ++i) order[i] = (int64_t)i;
+  std::stable_sort(order.begin(), order.end(), [&](int64_t a, int64_t b) { return cost[a] > cost[b]; });
+  std::vector<BItem> sorted(items.size());
+  for (size_t i = 0; i < order.size(); ++i) sorted[i] = items[order[i]];
+  items.swap(sorted);
+  return kOk;
+}
+
+static int plan_free(BatchPlan* p) {
+  if (!p) return kOk;
+  cudaFree(p->d_probs);
+  cudaFree(p->d_items);
+  cudaFree(p->d_counters);
+  cudaFree(p->d_partials);
+  delete p;
+  return kOk;
+}
+
+static int cuda_rc(cudaError_t e) {
+  if (e == cudaSuccess) return kOk;
+  cudaGetLastError();
+  if (e == cudaErrorMemoryAllocation) return kErrNoMemory;
+  if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return kErrNoDevice;
+  return kErrCuda;
+}
+
+static int plan_build(const qblas_problem* problems, int64_t count, int64_t grain, BatchPlan** out) {
+  *out = nullptr;
+  if (count < 0 || (count > 0 && !problems)) return kErrInvalidValue;
+  std::vector<BProb> probs((size_t)count);
+  for (int64_t i = 0; i < count; ++i) {
+    int rc = resolve(problems[i], probs[i]);
+    if (rc) return rc;
+  }
+  std::vector<BItem> items;
+  std::vector<int64_t> cost;
+  int64_t ngroups = 0, nparts = 0;
+  build_items(probs, grain, items, cost, ngroups, nparts);
+  BatchPlan* p = new BatchPlan();
+  cudaGetDevice(&p->device);
+  p->nitems = (int64_t)items.size();
+  p->nprobs = count;
+  p->ngroups = ngroups;
+  p->nparts = nparts;
+  p->grain = grain;
+  int rc = kOk;
+  if ((rc = cuda_rc(cudaMalloc(&p->d_probs, sizeof(BProb) * std::max<int64_t>(1, count)))) ||
+      (rc = cuda_rc(cudaMalloc(&p->d_items, sizeof(BItem) * std::max<int64_t>(1, p->nitems)))) ||
+      (rc = cuda_rc(cudaMalloc(&p->d_counters, sizeof(int) * (1 + ngroups)))) ||
+      (rc = cuda_rc(cudaMalloc(&p->d_partials, sizeof(wacc) * std::max<int64_t>(1, nparts))))) {
+    plan_free(p);
+    return rc;
+  }
+  if (count > 0 &&
+      (rc = cuda_rc(cudaMemcpy(p->d_probs, probs.data(), sizeof(BProb) * count, cudaMemcpyHostToDevice)))) {
+    plan_free(p);
+    return rc;
+  }
+  if (p->nitems > 0 && (rc = cuda_rc(cudaMemcpy(p->d_items, items.data(), sizeof(BItem) * p->nitems,
+                                                 cudaMemcpyHostToDevice)))) {
+    plan_free(p);
+    return rc;
+  }
+  if ((rc = cuda_rc(cudaMemset(p->d_counters, 0, sizeof(int) * (1 + ngroups))))) {
+    plan_free(p);
+    return rc;
+  }
+  int per_sm = resident_blocks_per_sm((const void*)batched_persistent_kernel, kBThreads, 0);
+  p->blocks = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)device_sm_count() * per_sm, p->nitems));
+  *out = p;
+  return kOk;
+}
+
+static int plan_execute(BatchPlan* p, cudaStream_t s) {
+  if (!p) return kErrInvalidValue;
+  if (p->nitems == 0) return kOk;
+  cudaError_t e = cudaMemsetAsync(p->d_counters, 0, sizeof(int) * (1 + p->ngroups), s);
+  if (e != cudaSuccess) return cuda_rc(e);
+  batched_persistent_kernel<<<p->blocks, kBThreads, 0, s>>>(p->d_probs, p->d_items, p->nitems, p->d_counters,
+                                                            p->d_counters, p->d_partials);
+  return cuda_rc(cudaGetLastError());
+}
+
+// ---- autotuner ------------------------------------------------------------
+// Granularity (products per work item) candidates; the tuner times a fixed
+// calibration batch (shapes like the batched benchmark, sizes scaled down,
+// data generated on the device) at each and keeps the fastest.  The result
+// is cached per device in memory and in the file $QBLAS_AUTOTUNE_CACHE
+// (default $HOME/.cache/qblas_gb300_autotune.txt) as "<device name> <grain>".
+static const int64_t kGrains[] = {1 << 14, 1 << 15, 1 << 16, 1 << 17, 1 << 18};
+static const int64_t kDefaultGrain = 1 << 16;
+static std::mutex g_tune_mu;
+static int64_t g_grain[64] = {0};
+
+static std::string cache_path() {
+  const char* e = getenv("QBLAS_AUTOTUNE_CACHE");
+  if (e && *e) return e;
+  const char* h = getenv("HOME");
+  return std::string(h ? h : "/tmp") + "/.cache/qblas_gb300_autotune.txt";
+}
+
+static std::string device_key(int dev) {
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, dev) != cudaSuccess) return "unknown";
+  std::string k = prop.name;
+  for (char& c : k)
+    if (c == ' ') c = '_';
+  return k + "_sm" + std::to_string(prop.multiProcessorCount);
+}
+
+static int64_t cached_grain(int dev) {
+  std::lock_guard<std::mutex> l(g_tune_mu);
+  if (dev < 0 || dev >= 64) return kDefaultGrain;
+  if (g_grain[dev]) return g_grain[dev];
+  FILE* f = fopen(cache_path().c_str(), "r");
+  if (f) {
+    char name[256];
+    long long g;
+    std::string key = device_key(dev);
+    while (fscanf(f, "%255s %lld", name, &g) == 2)
+      if (key == name && g > 0) g_grain[dev] = g;
+    fclose(f);
+  }
+  return g_grain[dev] ? g_grain[dev] : kDefaultGrain;
+}
+
+__global__ void fill_bits_kernel(uint64_t* p, int64_t n, uint64_t seed) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  // splitmix64 bits; element i is a binary128 with a random significand and
+  // an exponent near 1 (|x| in [1, 2)), sign from the hash
+  uint64_t z = seed + (uint64_t)i * 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  z ^= z >> 31;
+  if (i & 1)
+    p[i] = (z & 0x8000FFFFFFFFFFFFull) | (0x3FFFull << 48);
+  else
+    p[i] = z;
+}
+
+static int run_autotune(int dev, int64_t* best_out) {
+  // calibration batch: 600 gemm (8..128), 600 gemv (16..1024), 600 dot (64..16384)
+  const int nper = 600;
+  uint64_t st = 0x2545F4914F6CDD1Dull;
+  auto rnd = [&]() {
+    st ^= st << 13;
+    st ^= st >> 7;
+    st ^= st << 17;
+    return st;
+  };
+  auto logu = [&](double lo, double hi) {
+    double u = (double)(rnd() >> 11) * (1.0 / 9007199254740992.0);
+    double v = exp(log(lo) + u * (log(hi + 1) - log(lo)));
+    int64_t r = (int64_t)v;
+    return std::min<int64_t>(std::max<int64_t>(r, (int64_t)lo), (int64_t)hi);
+  };
+  std::vector<qblas_problem> probs;
+  int64_t total = 0;
+  struct Sz {
+    int op;
+    int64_t m, n, k;
+  };
+  std::vector<Sz> sz;
+  for (int i = 0; i < nper; ++i) {
+    Sz a{QBLAS_OP_GEMM, logu(8, 128), logu(8, 128), logu(8, 128)};
+    Sz b{QBLAS_OP_GEMV, logu(16, 1024), logu(16, 1024), 0};
+    Sz c{QBLAS_OP_DOT, 0, logu(64, 16384), 0};
+    sz.push_back(a);
+    sz.push_back(b);
+    sz.push_back(c);
+  }
+  for (const Sz& z : sz) {
+    if (z.op == QBLAS_OP_GEMM) total += z.m * z.k + z.k * z.n + z.m * z.n;
+    if (z.op == QBLAS_OP_GEMV) total += z.m * z.n + z.n + z.m;
+    if (z.op == QBLAS_OP_DOT) total += 2 * z.n + 1;
+  }
+  uint64_t* buf = nullptr;
+  if (cudaMalloc(&buf, (size_t)total * 16) != cudaSuccess) {
+    cudaGetLastError();
+    return kErrNoMemory;
+  }
+  fill_bits_kernel<<<(unsigned)((2 * total + 255) / 256), 256>>>(buf, 2 * total, 12345);
+  int64_t off = 0;
+  uint64_t one[2] = {0, 0x3FFF000000000000ull}, zero[2] = {0, 0};
+  for (const Sz& z : sz) {
+    qblas_problem q;
+    memset(&q, 0, sizeof(q));
+    q.op = z.op;
+    q.layout = 'R';
+    q.transa = q.transb = 'N';
+    memcpy(q.alpha, one, 16);
+    memcpy(q.beta, zero, 16);
+    q128* b = (q128*)buf + off;
+    if (z.op == QBLAS_OP_GEMM) {
+      q.m = z.m; q.n = z.n; q.k = z.k;
+      q.A = b; q.lda = z.k;
+      q.B = b + z.m * z.k; q.ldb = z.n;
+      q.C = b + z.m * z.k + z.k * z.n; q.ldc = z.n;
+      off += z.m * z.k + z.k * z.n + z.m * z.n;
+    } else if (z.op == QBLAS_OP_GEMV) {
+      q.m = z.m; q.n = z.n;
+      q.A = b; q.lda = z.n;
+      q.B = b + z.m * z.n; q.ldb = 1;
+      q.C = b + z.m * z.n + z.n; q.ldc = 1;
+      off += z.m * z.n + z.n + z.m;
+    } else {
+      q.n = z.n;
+      q.A = b; q.lda = 1;
+      q.B = b + z.n; q.ldb = 1;
+      q.C = b + 2 * z.n;
+      off += 2 * z.n + 1;
+    }
+    probs.push_back(q);
+  }
+  cudaStream_t s;
+  cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float best_ms = 1e30f;
+  int64_t best = kDefaultGrain;
+  for (int64_t g : kGrains) {
+    BatchPlan* p = nullptr;
+    if (plan_build(probs.data(), (int64_t)probs.size(), g, &p) != kOk) continue;
+    plan_execute(p, s);  // warm-up
+    cudaEventRecord(e0, s);
+    for (int r = 0; r < 3; ++r) plan_execute(p, s);
+    cudaEventRecord(e1, s);
+    cudaEventSynchronize(e1);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms < best_ms) {
+      best_ms = ms;
+      best = g;
+    }
+    plan_free(p);
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaStreamDestroy(s);
+  cudaFree(buf);
+  *best_out = best;
+  {
+    std::lock_guard<std::mutex> l(g_tune_mu);
+    g_grain[dev] = best;
+  }
+  std::string path = cache_path();
+  std::string dir = path.substr(0, path.find_last_of('/'));
+  std::string cmd = "mkdir -p '" + dir + "' 2>/dev/null";
+  if (system(cmd.c_str()) == 0) {
+    FILE* f = fopen(path.c_str(), "a");
+    if (f) {
+      fprintf(f, "%s %lld\n", device_key(dev).c_str(), (long long)best);
+      fclose(f);
+    }
+  }
+  return kOk;
+}
+
+}  // namespace qb
+
+#define QBLAS_EXPORT extern "C" __attribute__((visibility("default")))
+
+QBLAS_EXPORT int quadblas_batch_plan(const qblas_problem* problems, int64_t count, void** plan) {
+  if (!plan) return QBLAS_ERR_INVALID_VALUE;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    return QBLAS_ERR_NO_DEVICE;
+  }
+  qb::BatchPlan* p = nullptr;
+  int rc = qb::plan_build(problems, count, qb::cached_grain(dev), &p);
+  *plan = p;
+  return rc;
+}
+
+QBLAS_EXPORT int quadblas_batch_execute(void* plan, void* stream) {
+  return qb::plan_execute(static_cast<qb::BatchPlan*>(plan), static_cast<cudaStream_t>(stream));
+}
+
+QBLAS_EXPORT int quadblas_batch_destroy(void* plan) {
+  return qb::plan_free(static_cast<qb::BatchPlan*>(plan));
+}
+
+QBLAS_EXPORT int quadblas_batch_info(void* plan, int64_t* info4) {
+  qb::BatchPlan* p = static_cast<qb::BatchPlan*>(plan);
+  if (!p || !info4) return QBLAS_ERR_INVALID_VALUE;
+  info4[0] = p->nitems;
+  info4[1] = p->grain;
+  info4[2] = p->blocks;
+  info4[3] = p->ngroups;
+  return QBLAS_OK;
+}
+
+QBLAS_EXPORT int quadblas_batch_autotune(int64_t* grain_out) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    return QBLAS_ERR_NO_DEVICE;
+  }
+  int64_t g = 0;
+  int rc = qb::run_autotune(dev, &g);
+  if (grain_out) *grain_out = g;
+  return rc;
+}
+
+QBLAS_EXPORT int quadblas_batch_set_grain(int64_t grain) {
+  int dev = 0;
+  if (grain < 256 || cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+    cudaGetLastError();
+    return QBLAS_ERR_INVALID_VALUE;
+  }
+  std::lock_guard<std::mutex> l(qb::g_tune_mu);
+  qb::g_grain[dev] = grain;
+  return QBLAS_OK;
+}

@@ -89,3 +89,29 @@ def log_uniform_int(rng: np.random.Generator, lo: int, hi: int, n: int) -> np.nd
     """Integers log-uniform in [lo, hi]."""
     v = np.exp(rng.uniform(np.log(lo), np.log(hi + 1), size=int(n)))
     return np.clip(np.floor(v).astype(np.int64), lo, hi)
+
+
+def uniform_full_device(torch, n: int, seed: int, chunk: int = 1 << 26):
+    """uniform_full() generated on the GPU with torch (for multi-GB inputs):
+    a binary64 uniform in [-1, 1) widened to binary128 plus a random 60-bit
+    tail below 2^-53 relative.  Returns an int64 tensor of shape (n, 2)
+    (low word, high word) on the current CUDA device."""
+    dev = torch.device("cuda")
+    out = torch.empty((int(n), 2), dtype=torch.int64, device=dev)
+    g = torch.Generator(device=dev)
+    g.manual_seed(int(seed))
+    m52 = (1 << 52) - 1
+    for s in range(0, int(n), chunk):
+        e = min(int(n), s + chunk)
+        d = torch.rand(e - s, dtype=torch.float64, device=dev, generator=g) * 2.0 - 1.0
+        bits = d.view(torch.int64)
+        sign = (bits >> 63) & 1
+        ex = (bits >> 52) & 0x7FF
+        frac = bits & m52
+        hi = (sign << 63) | ((ex - 1023 + 16383) << 48) | (frac >> 4)
+        tail = torch.randint(0, 1 << 60, (e - s,), dtype=torch.int64, device=dev, generator=g)
+        lo = ((frac & 0xF) << 60) | tail
+        zero = d == 0
+        out[s:e, 0] = torch.where(zero, torch.zeros_like(lo), lo)
+        out[s:e, 1] = torch.where(zero, sign << 63, hi)
+    return out
