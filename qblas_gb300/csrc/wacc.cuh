@@ -33,41 +33,55 @@ struct qop {
 
 enum : uint32_t { kClsFinite = 0, kClsZero = 1, kClsInf = 2, kClsNan = 3 };
 
-// Unpack a binary128 value.  The common case (normal numbers) is a few
-// integer instructions; zero, subnormal, infinity and NaN take a branch.
+QB_HD uint32_t fshl32(uint32_t lo, uint32_t hi, uint32_t s) {  // ((hi:lo) << s) >> 32, 0 < s < 32
+#if defined(__CUDA_ARCH__)
+  return __funnelshift_l(lo, hi, s);
+#else
+  return (hi << s) | (lo >> (32 - s));
+#endif
+}
+
+// Unpack a binary128 value.  Normal numbers take a few 32-bit funnel
+// shifts; zero, subnormal, infinity and NaN take a branch.
 QB_HD qop qop_unpack(q128 a) {
   qop r;
-  uint32_t be = (uint32_t)(a.hi >> 48) & 0x7fff;
-  r.s = (uint32_t)(a.hi >> 63);
-  uint64_t mh = a.hi & kMantHiMask, ml = a.lo;
-  int E;
-  if (be - 1u < 0x7ffeu) {  // normal
-    mh |= kHiddenBit;
-    E = (int)be - kBias;
+  const uint32_t w0 = (uint32_t)a.lo, w1 = (uint32_t)(a.lo >> 32);
+  const uint32_t w2 = (uint32_t)a.hi, w3 = (uint32_t)(a.hi >> 32);
+  const uint32_t be = (w3 >> 16) & 0x7fffu;
+  r.s = w3 >> 31;
+  if (be - 1u < 0x7ffeu) {  // normal: significand (hidden bit | 112 bits) << 15
+    const uint32_t s3 = (w3 & 0xFFFFu) | 0x10000u;
+    r.m3 = fshl32(w2, s3, 15);
+    r.m2 = fshl32(w1, w2, 15);
+    r.m1 = fshl32(w0, w1, 15);
+    r.m0 = w0 << 15;
+    r.e = (int)be - kBias - 127;
     r.cls = kClsFinite;
-  } else if (be == 0) {
+    return r;
+  }
+  uint64_t mh = a.hi & kMantHiMask, ml = a.lo;
+  if (be == 0) {
     if ((mh | ml) == 0) {
       r.cls = kClsZero;
       r.m0 = r.m1 = r.m2 = r.m3 = 0;
       r.e = 0;
       return r;
     }
+    int E;
     q_unpack_norm(a, mh, ml, E);
+    uint64_t th = (mh << 15) | (ml >> 49);
+    uint64_t tl = ml << 15;
+    r.m0 = (uint32_t)tl;
+    r.m1 = (uint32_t)(tl >> 32);
+    r.m2 = (uint32_t)th;
+    r.m3 = (uint32_t)(th >> 32);
+    r.e = E - 127;
     r.cls = kClsFinite;
-  } else {
-    r.cls = ((mh | ml) != 0) ? kClsNan : kClsInf;
-    r.m0 = r.m1 = r.m2 = r.m3 = 0;
-    r.e = 0;
     return r;
   }
-  // (mh:ml) has its leading one at bit 112; shift left by 15.
-  uint64_t th = (mh << 15) | (ml >> 49);
-  uint64_t tl = ml << 15;
-  r.m0 = (uint32_t)tl;
-  r.m1 = (uint32_t)(tl >> 32);
-  r.m2 = (uint32_t)th;
-  r.m3 = (uint32_t)(th >> 32);
-  r.e = E - 127;
+  r.cls = ((mh | ml) != 0) ? kClsNan : kClsInf;
+  r.m0 = r.m1 = r.m2 = r.m3 = 0;
+  r.e = 0;
   return r;
 }
 
@@ -237,6 +251,9 @@ QB_HD uint32_t special_product_flags(const qop& a, const qop& b) {
   return 0u;
 }
 
+// (x & m) | (y & ~m): one 3-input logic instruction.
+QB_HD uint32_t sel32(uint32_t m, uint32_t x, uint32_t y) { return (x & m) | (y & ~m); }
+
 // acc += a * b
 QB_HD void wacc_add_product(wacc& acc, const qop& a, const qop& b) {
   if ((a.cls | b.cls) != kClsFinite) {
@@ -247,34 +264,24 @@ QB_HD void wacc_add_product(wacc& acc, const qop& a, const qop& b) {
   mul128x128_top224(a, b, p1, p2, p3, p4, p5, p6, p7);
   int pe = a.e + b.e + 32;  // exponent of p1's bit 0
   int r = acc.e - pe;       // right shift that aligns the product to the frame
-  if (r < 0) {              // product above the frame top: move the frame up
+  if (r < 0) {              // product above the frame top: move the frame up (rare)
     wacc_ashr(acc, -r);
     acc.e = pe;
     r = 0;
   }
-  uint32_t q0, q1, q2, q3, q4, q5, q6;
-  if (r >= 224) return;  // entirely below the frame
-  uint32_t b5 = (uint32_t)r & 31u;
-  q0 = fshr32(p1, p2, b5);
-  q1 = fshr32(p2, p3, b5);
-  q2 = fshr32(p3, p4, b5);
-  q3 = fshr32(p4, p5, b5);
-  q4 = fshr32(p5, p6, b5);
-  q5 = fshr32(p6, p7, b5);
-  q6 = fshr32(p7, 0u, b5);
-  int w = r >> 5;
-  if (w & 4) {
-    q0 = q4; q1 = q5; q2 = q6;
-    q3 = q4 = q5 = q6 = 0;
-  }
-  if (w & 2) {
-    q0 = q2; q1 = q3; q2 = q4; q3 = q5; q4 = q6;
-    q5 = q6 = 0;
-  }
-  if (w & 1) {
-    q0 = q1; q1 = q2; q2 = q3; q3 = q4; q4 = q5; q5 = q6;
-    q6 = 0;
-  }
+  r = r < 224 ? r : 224;    // 224: the whole product falls below the frame
+  const uint32_t b5 = (uint32_t)r & 31u, w = (uint32_t)r >> 5;
+  uint32_t q0 = fshr32(p1, p2, b5), q1 = fshr32(p2, p3, b5), q2 = fshr32(p3, p4, b5),
+           q3 = fshr32(p4, p5, b5), q4 = fshr32(p5, p6, b5), q5 = fshr32(p6, p7, b5),
+           q6 = fshr32(p7, 0u, b5);
+  // word shift by w (0..7) without branches: stages of 4, 2 and 1 words
+  const uint32_t m4 = 0u - ((w >> 2) & 1u), m2 = 0u - ((w >> 1) & 1u), m1 = 0u - (w & 1u);
+  q0 = sel32(m4, q4, q0); q1 = sel32(m4, q5, q1); q2 = sel32(m4, q6, q2);
+  q3 &= ~m4; q4 &= ~m4; q5 &= ~m4; q6 &= ~m4;
+  q0 = sel32(m2, q2, q0); q1 = sel32(m2, q3, q1); q2 = sel32(m2, q4, q2);
+  q3 = sel32(m2, q5, q3); q4 = sel32(m2, q6, q4); q5 &= ~m2; q6 &= ~m2;
+  q0 = sel32(m1, q1, q0); q1 = sel32(m1, q2, q1); q2 = sel32(m1, q3, q2);
+  q3 = sel32(m1, q4, q3); q4 = sel32(m1, q5, q4); q5 = sel32(m1, q6, q5); q6 &= ~m1;
   wacc_add_signed(acc, q0, q1, q2, q3, q4, q5, q6, 0u, a.s ^ b.s);
 }
 
