@@ -251,9 +251,6 @@ QB_HD uint32_t special_product_flags(const qop& a, const qop& b) {
   return 0u;
 }
 
-// (x & m) | (y & ~m): one 3-input logic instruction.
-QB_HD uint32_t sel32(uint32_t m, uint32_t x, uint32_t y) { return (x & m) | (y & ~m); }
-
 // acc += a * b
 QB_HD void wacc_add_product(wacc& acc, const qop& a, const qop& b) {
   if ((a.cls | b.cls) != kClsFinite) {
@@ -264,24 +261,34 @@ QB_HD void wacc_add_product(wacc& acc, const qop& a, const qop& b) {
   mul128x128_top224(a, b, p1, p2, p3, p4, p5, p6, p7);
   int pe = a.e + b.e + 32;  // exponent of p1's bit 0
   int r = acc.e - pe;       // right shift that aligns the product to the frame
-  if (r < 0) {              // product above the frame top: move the frame up (rare)
+  if (r < 0) {              // product above the frame top: move the frame up
     wacc_ashr(acc, -r);
     acc.e = pe;
     r = 0;
   }
-  r = r < 224 ? r : 224;    // 224: the whole product falls below the frame
-  const uint32_t b5 = (uint32_t)r & 31u, w = (uint32_t)r >> 5;
-  uint32_t q0 = fshr32(p1, p2, b5), q1 = fshr32(p2, p3, b5), q2 = fshr32(p3, p4, b5),
-           q3 = fshr32(p4, p5, b5), q4 = fshr32(p5, p6, b5), q5 = fshr32(p6, p7, b5),
-           q6 = fshr32(p7, 0u, b5);
-  // word shift by w (0..7) without branches: stages of 4, 2 and 1 words
-  const uint32_t m4 = 0u - ((w >> 2) & 1u), m2 = 0u - ((w >> 1) & 1u), m1 = 0u - (w & 1u);
-  q0 = sel32(m4, q4, q0); q1 = sel32(m4, q5, q1); q2 = sel32(m4, q6, q2);
-  q3 &= ~m4; q4 &= ~m4; q5 &= ~m4; q6 &= ~m4;
-  q0 = sel32(m2, q2, q0); q1 = sel32(m2, q3, q1); q2 = sel32(m2, q4, q2);
-  q3 = sel32(m2, q5, q3); q4 = sel32(m2, q6, q4); q5 &= ~m2; q6 &= ~m2;
-  q0 = sel32(m1, q1, q0); q1 = sel32(m1, q2, q1); q2 = sel32(m1, q3, q2);
-  q3 = sel32(m1, q4, q3); q4 = sel32(m1, q5, q4); q5 = sel32(m1, q6, q5); q6 &= ~m1;
+  uint32_t q0, q1, q2, q3, q4, q5, q6;
+  if (r >= 224) return;  // entirely below the frame
+  uint32_t b5 = (uint32_t)r & 31u;
+  q0 = fshr32(p1, p2, b5);
+  q1 = fshr32(p2, p3, b5);
+  q2 = fshr32(p3, p4, b5);
+  q3 = fshr32(p4, p5, b5);
+  q4 = fshr32(p5, p6, b5);
+  q5 = fshr32(p6, p7, b5);
+  q6 = fshr32(p7, 0u, b5);
+  int w = r >> 5;
+  if (w & 4) {
+    q0 = q4; q1 = q5; q2 = q6;
+    q3 = q4 = q5 = q6 = 0;
+  }
+  if (w & 2) {
+    q0 = q2; q1 = q3; q2 = q4; q3 = q5; q4 = q6;
+    q5 = q6 = 0;
+  }
+  if (w & 1) {
+    q0 = q1; q1 = q2; q2 = q3; q3 = q4; q4 = q5; q5 = q6;
+    q6 = 0;
+  }
   wacc_add_signed(acc, q0, q1, q2, q3, q4, q5, q6, 0u, a.s ^ b.s);
 }
 
