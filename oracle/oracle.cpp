@@ -302,6 +302,10 @@ struct LongAcc {
     nadds = 0;
     nan = pinf = ninf = false;
   }
+  // Carry-propagates the digits into [0, 2^32), except that a negative
+  // total keeps its sign in a negative top digit: value =
+  // sum_{i<hi} D_i 2^(32 i) + D_hi 2^(32 hi) with D_hi in [-2^32, 0).
+  // Idempotent: repeated calls do not grow the digit range.
   void normalize() {
     if (hi < lo) return;
     int64_t carry = 0;
@@ -310,17 +314,20 @@ struct LongAcc {
       D[i] = v & 0xffffffffLL;
       carry = v >> 32;  // arithmetic
     }
-    int i = hi + 1;
     while (carry != 0 && carry != -1) {
-      int64_t v = D[i] + carry;
-      D[i] = v & 0xffffffffLL;
+      ++hi;
+      int64_t v = D[hi] + carry;
+      D[hi] = v & 0xffffffffLL;
       carry = v >> 32;
-      hi = i;
-      ++i;
     }
-    if (carry == -1) {  // negative total: keep the borrow in one top digit
-      D[hi + 1] += -1;
-      hi = hi + 1;
+    if (carry == -1) {
+      // value = digits - 2^(32(hi+1)): drop all-ones sign-extension digits,
+      // then fold the borrow into the top digit
+      while (hi > lo && D[hi] == 0xffffffffLL) {
+        D[hi] = 0;
+        --hi;
+      }
+      D[hi] -= (1LL << 32);
     }
     nadds = 0;
   }
@@ -408,16 +415,17 @@ struct LongAcc {
     normalize();
     if (hi < lo) return 0;
     bool neg = D[hi] < 0;
-    // magnitude digits
-    int n = hi - lo + 1;
-    std::vector<uint32_t> mag(n);
+    // magnitude digits (one spare digit above hi for the negation)
+    int n = hi - lo + 2;
+    std::vector<uint32_t> mag(n, 0u);
     if (!neg) {
-      for (int i = 0; i < n; ++i) mag[i] = (uint32_t)D[lo + i];
+      for (int i = 0; i + 1 < n; ++i) mag[i] = (uint32_t)D[lo + i];
     } else {
-      // two's complement negate over digits lo..hi (D[hi] holds the -1 borrow)
+      // two's complement negation of digits lo..hi, sign-extended by one digit
       uint64_t carry = 1;
       for (int i = 0; i < n; ++i) {
-        uint64_t v = (uint64_t)(uint32_t)(~(uint32_t)D[lo + i]) + carry;
+        uint32_t d = i + 1 < n ? (uint32_t)D[lo + i] : 0xffffffffu;
+        uint64_t v = (uint64_t)(uint32_t)(~d) + carry;
         mag[i] = (uint32_t)v;
         carry = v >> 32;
       }
@@ -550,6 +558,72 @@ void oq_ulp_err(int64_t n, const oq* got, const oq* R, const oq* r, double* out)
     double v = (double)u;
     out[i] = v;
   }
+}
+
+// ---------------------------------------------------------------------------
+// 3. Ill-conditioned dot products of prescribed condition
+// ---------------------------------------------------------------------------
+// GenDot of Ogita, Rump and Oishi ("Accurate sum and dot product", SIAM J.
+// Sci. Comput. 26(6), 2005, Algorithm 6.1), restated for binary128: the
+// first half of x, y has random signs, random significands and exponents
+// spread over [0, b/2] (b = log2(cond)), including both ends; in the second
+// half the exponents fall linearly from b/2 to 0 and each y_i is chosen so
+// that x_i*y_i nearly cancels the running exact sum, which the exact long
+// accumulator provides (the paper uses a twice-working-precision dot).  The
+// pairs are then permuted at random.  Deterministic for a given seed.
+static inline uint64_t gd_next(uint64_t& s) {
+  uint64_t z = (s += 0x9E3779B97F4A7C15ull);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+// uniform in [-1, 1) with 106 random significand bits
+static inline oq gd_unit(uint64_t& s) {
+  const uint64_t hi = gd_next(s) >> 11;  // two statements: a fixed draw order
+  const uint64_t lo = gd_next(s) >> 11;
+  oq u = (oq)hi * q_ldexp((oq)1, -53) + (oq)lo * q_ldexp((oq)1, -106);
+  return 2 * u - 1;
+}
+
+void oq_gendot(int64_t n, double cond, uint64_t seed, oq* x, oq* y) {
+  uint64_t s = seed;
+  LongAcc* acc = new LongAcc();
+  const double b = log2(cond);
+  const int64_t n2 = (n + 1) / 2;
+  for (int64_t i = 0; i < n2; ++i) {
+    int ex = (int)llround((double)(gd_next(s) >> 11) * 0x1p-53 * b / 2);
+    int ey = (int)llround((double)(gd_next(s) >> 11) * 0x1p-53 * b / 2);
+    if (i == 0) ex = ey = (int)llround(b / 2) + 1;
+    if (i == n2 - 1) ex = ey = 0;
+    x[i] = q_ldexp(gd_unit(s), ex);
+    y[i] = q_ldexp(gd_unit(s), ey);
+    acc->add_product(x[i], y[i]);
+  }
+  for (int64_t i = n2; i < n; ++i) {
+    double frac = (n - 1 > n2) ? (double)(n - 1 - i) / (double)(n - 1 - n2) : 0.0;
+    int e = (int)llround(b / 2 * frac);
+    x[i] = q_ldexp(gd_unit(s), e);
+    oq S = acc->round();
+    y[i] = (q_ldexp(gd_unit(s), e) - S) / x[i];
+    acc->add_product(x[i], y[i]);
+  }
+  for (int64_t i = n - 1; i > 0; --i) {
+    int64_t j = (int64_t)(gd_next(s) % (uint64_t)(i + 1));
+    oq t = x[i];
+    x[i] = x[j];
+    x[j] = t;
+    t = y[i];
+    y[i] = y[j];
+    y[j] = t;
+  }
+  delete acc;
+}
+
+// Condition number 2 * sum|x_i y_i| / |sum x_i y_i| of a dot product (double).
+double oq_dot_condition(int64_t n, const oq* x, int64_t incx, const oq* y, int64_t incy) {
+  oq R, r, ab;
+  oq_exact_dot(n, x, incx, y, incy, &R, &r, &ab);
+  return (double)(2 * ab / q_fabs(R));
 }
 
 // Counts entries with |got - ref| > kfac * 2^-113 * absum (the reduction

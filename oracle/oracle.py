@@ -187,6 +187,23 @@ def exact_gemm(k, A, sai, sal, B, sbl, sbj, rows, cols, nthreads=8):
     return R, r, ab
 
 
+def gendot(n, cond, seed):
+    """x, y of length n whose dot product has condition number about `cond`
+    (Ogita-Rump-Oishi GenDot, restated for binary128)."""
+    x, y = qs(n), qs(n)
+    lib().oq_gendot(c_i64(n), ctypes.c_double(cond), ctypes.c_uint64(seed), P(x), P(y))
+    return x, y
+
+
+def dot_condition(x, y, n=None, incx=1, incy=1):
+    x, y = q(x), q(y)
+    if n is None:
+        n = len(x) // incx
+    f = lib().oq_dot_condition
+    f.restype = ctypes.c_double
+    return f(c_i64(n), P(x), c_i64(incx), P(y), c_i64(incy))
+
+
 def ulp_err(got, R, r):
     got, R, r = q(got), q(R), q(r)
     out = np.zeros(len(got), dtype=np.float64)

@@ -166,3 +166,27 @@ def test_exact_accumulator_order_invariant(O):
     xn[:, 1] ^= np.uint64(1 << 63)
     R3, _, _ = O.exact_dot(np.concatenate([x, xn]), np.concatenate([y, y]))
     assert Q.same_bits(R3, Q.scalar(0.0)).all()
+
+
+def test_exact_accumulator_negative_totals(O):
+    # a negative running total survives many intermediate roundings (GenDot
+    # rounds the accumulator once per generated pair)
+    rng = G.rng_for(13)
+    x, y = G.cancelling_dot(rng, 4000, -100, 100)
+    R, r, _ = O.exact_dot(x, y)
+    xn = x.copy()
+    xn[:, 1] ^= np.uint64(1 << 63)
+    Rn, rn, _ = O.exact_dot(xn, y)
+    for a, b in ((Rn, R), (rn, r)):
+        neg = b.copy()
+        neg[:, 1] ^= np.uint64(1 << 63)
+        assert Q.same_bits(a, neg).all()
+
+
+@pytest.mark.parametrize("cond", [1e10, 1e20, 1e30, 1e40])
+def test_gendot_condition(O, cond):
+    x, y = O.gendot(4096, cond, 7)
+    c = O.dot_condition(x, y)
+    assert cond / 10 <= c <= cond * 1e3, c
+    x2, y2 = O.gendot(4096, cond, 7)
+    assert Q.same_bits(x, x2).all() and Q.same_bits(y, y2).all()
