@@ -124,6 +124,24 @@ def to_host(t) -> np.ndarray:
     return np.ascontiguousarray(t.cpu().numpy()).view(np.uint64)
 
 
+def max_over_ranks(dist, x: float) -> float:
+    """The largest x over all ranks (x itself without a process group).  The
+    reduction runs on the GPU under NCCL and on the CPU under gloo."""
+    if dist is None:
+        return float(x)
+    import torch
+    dev = "cpu" if dist.get_backend() == "gloo" else "cuda"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_rank: float, world: int, seconds: float) -> float:
+    """Units per second of the whole job: every rank processes units_per_rank
+    (weak scaling) and the job takes the slowest rank's time."""
+    return world * units_per_rank / seconds
+
+
 def time_steps(torch, fn, steps, warmup, dist=None):
     """CUDA-event time (ms) of `steps` calls on the current stream, max over ranks."""
     for _ in range(warmup):
@@ -139,11 +157,8 @@ def time_steps(torch, fn, steps, warmup, dist=None):
         fn()
     e1.record(st)
     torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1)
+    ms = max_over_ranks(dist, e0.elapsed_time(e1))
     if dist is not None:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
         dist.barrier()
     return ms
 
@@ -277,6 +292,10 @@ def batched_config4(torch, api, rank, reps=3):
             p["lda"], p["ldb"], p["ldc"] = 1, 1, 1
             flops += 2.0 * n
         off += sa + sb + sc
+    # the work-item granularity comes from the autotuner (cached per GPU model)
+    t0 = time.perf_counter()
+    grain = api.batch_autotune()
+    tune_s = time.perf_counter() - t0
     t0 = time.perf_counter()
     plan = api.BatchPlan(probs)
     plan_s = time.perf_counter() - t0
@@ -333,7 +352,8 @@ def batched_config4(torch, api, rank, reps=3):
     return {"problems": len(sizes), "gflops": round(flops / (ms_batched * 1e-3) / 1e9, 2),
             "ms_batched_graph_replay": round(ms_batched, 3), "ms_one_call_per_problem": round(ms_single, 3),
             "speedup_vs_one_by_one": round(ms_single / ms_batched, 2), "plan_ms": round(plan_s * 1e3, 1),
-            "work_items": info["items"], "grain": info["grain"], "launches_per_batch": 1,
+            "work_items": info["items"], "grain": info["grain"], "autotuned_grain": grain,
+            "autotune_ms": round(tune_s * 1e3, 1), "launches_per_batch": 1,
             "method": "soft-float wide accumulator for every problem", "quad_flops": flops}
 
 
@@ -442,7 +462,7 @@ def main():
             ms = time_steps(torch, W.step, args.steps, args.warmup, dist)
         lib.quadblas_profile_enable(0)
         ms_step = ms / args.steps
-        value = world * W.flops() / (ms_step * 1e-3) / 1e9
+        value = whole_job_rate(W.flops(), world, ms_step * 1e-3) / 1e9
         if method == 2:
             ph, calls = profile_read(lib)  # warm-up and timed calls, recorded on the launching stream
             tot_calls = max(calls, 1)
@@ -465,7 +485,11 @@ def main():
             dtype = "u32 (soft-float integer limbs)"
         metric, unit = f"qgemm binary128 GFLOP/s ({size}^3)", "GFLOP/s"
         e2e_s, h2d, d2h = W.e2e(max(1, min(args.steps, 3)))
-        e2e = {"value": round(W.flops() / e2e_s / 1e9, 3), "unit": unit, "h2d_bytes_per_step": int(h2d),
+        if dist is not None:
+            dist.barrier()
+        e2e_s = max_over_ranks(dist, e2e_s)
+        e2e = {"value": round(whole_job_rate(W.flops(), world, e2e_s) / 1e9, 3), "unit": unit,
+               "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": int(d2h)}
         cfg = {"workload": (f"qgemm m=n=k={size} row-major NN alpha=1 beta=0, entries u*2^e (u uniform [-1,1) "
                             "full 113-bit significand, e uniform [-20,20])") if size >= 2048 else
@@ -531,7 +555,7 @@ def main():
         with ClockSampler(local) as clk:
             ms = time_steps(torch, W.step, args.steps, args.warmup, dist)
         ms_step = ms / args.steps
-        value = world * W.bytes() / (ms_step * 1e-3) / 1e9
+        value = whole_job_rate(W.bytes(), world, ms_step * 1e-3) / 1e9
         metric, unit = "qgemv binary128 GB/s (8192^2 row-major)", "GB/s"
         launches = 2 * args.steps
         roof = hbm_roofline(pk, pk_src, W.bytes(), ms_step)
@@ -543,7 +567,7 @@ def main():
         with ClockSampler(local) as clk:
             ms = time_steps(torch, W.step, args.steps, args.warmup, dist)
         ms_step = ms / args.steps
-        value = world * W.bytes() / (ms_step * 1e-3) / 1e9
+        value = whole_job_rate(W.bytes(), world, ms_step * 1e-3) / 1e9
         metric, unit = "qdot binary128 GB/s (n=2^26)", "GB/s"
         launches = 2 * args.steps
         roof = hbm_roofline(pk, pk_src, W.bytes(), ms_step)

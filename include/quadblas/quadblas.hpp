@@ -168,7 +168,7 @@ template <Layout layout>
 class Matrix {
  public:
   Matrix(size_t rows, size_t cols) : rows_(rows), cols_(cols), ld_(cols), owns_(true) {
-    data_ = aligned_alloc<Sleef_quad>(rows * cols ? rows * cols : 1);
+    data_ = aligned_alloc<Sleef_quad>(rows * cols != 0 ? rows * cols : 1);
     if (!data_) throw std::bad_alloc();
     memset(static_cast<void*>(data_), 0, sizeof(Sleef_quad) * rows * cols);
   }

@@ -619,6 +619,14 @@ void oq_gendot(int64_t n, double cond, uint64_t seed, oq* x, oq* y) {
   delete acc;
 }
 
+// `count` independent GenDot pairs: pair p (condition conds[p], seed
+// seeds[p]) is written to X + p*n and Y + p*n.
+void oq_gendot_batch(int64_t count, int64_t n, const double* conds, const uint64_t* seeds, oq* X,
+                     oq* Y, int nthreads) {
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads > 0 ? nthreads : 1)
+  for (int64_t p = 0; p < count; ++p) oq_gendot(n, conds[p], seeds[p], X + p * n, Y + p * n);
+}
+
 // Condition number 2 * sum|x_i y_i| / |sum x_i y_i| of a dot product (double).
 double oq_dot_condition(int64_t n, const oq* x, int64_t incx, const oq* y, int64_t incy) {
   oq R, r, ab;

@@ -195,6 +195,18 @@ def gendot(n, cond, seed):
     return x, y
 
 
+def gendot_batch(n, conds, seeds, nthreads=None):
+    """len(conds) GenDot pairs of length n as (count*n, 2) arrays X, Y: pair p
+    occupies rows p*n .. p*n+n-1, with condition about conds[p]."""
+    conds = np.ascontiguousarray(conds, dtype=np.float64)
+    seeds = np.ascontiguousarray(seeds, dtype=np.uint64)
+    cnt = conds.size
+    X, Y = qs(cnt * n), qs(cnt * n)
+    nt = nthreads or os.cpu_count() or 1
+    lib().oq_gendot_batch(c_i64(cnt), c_i64(n), P(conds), P(seeds), P(X), P(Y), ctypes.c_int(nt))
+    return X, Y
+
+
 def dot_condition(x, y, n=None, incx=1, incy=1):
     x, y = q(x), q(y)
     if n is None:

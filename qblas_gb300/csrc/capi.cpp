@@ -299,9 +299,12 @@ int gemm_digit_bits() {
   return b ? b : qb::ozaki_default_digit_bits();
 }
 
-int gemm_digits() {
+// Digit count for inner dimension k: the configured count (set_ozaki_slices,
+// else QBLAS_SLICES, else the default), capped where the 192-bit fold could
+// overflow for this k.
+int gemm_digits(int64_t k) {
   int b = gemm_digit_bits();
-  int smax = b == 7 ? 22 : 20;
+  int smax = qb::ozaki_digit_cap(b, k);
   int s = g_slices.load();
   if (s > 0) return std::min(s, smax);
   static int env = -1;
@@ -310,12 +313,12 @@ int gemm_digits() {
     env = v ? atoi(v) : 0;
     if (env < 2 || env > 22) env = 0;
   }
-  return env ? std::min(env, smax) : qb::ozaki_default_digits(b);
+  return std::min(env ? env : qb::ozaki_default_digits(b), smax);
 }
 
 size_t gemm_scratch_bytes(const GemmPlan& p) {
   if (gemm_method() != 2) return 0;
-  return qb::ozaki_scratch_bytes(p.g.m, p.g.n, p.g.k, gemm_digits(), gemm_digit_bits());
+  return qb::ozaki_scratch_bytes(p.g.m, p.g.n, p.g.k, gemm_digits(p.g.k), gemm_digit_bits());
 }
 
 int dev_gemm(GemmPlan p, const void* alpha, const void* dA, const void* dB, const void* beta,
@@ -336,7 +339,7 @@ int dev_gemm(GemmPlan p, const void* alpha, const void* dA, const void* dB, cons
       return cuda_status(e);
     }
   }
-  cudaError_t e = qb::launch_gemm_ozaki(p.g, gemm_digits(), gemm_digit_bits(), scratch, s);
+  cudaError_t e = qb::launch_gemm_ozaki(p.g, gemm_digits(p.g.k), gemm_digit_bits(), scratch, s);
   if (!scratch_or_null) cudaFreeAsync(scratch, s);
   return cuda_status(e);
 }

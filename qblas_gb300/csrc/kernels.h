@@ -63,6 +63,8 @@ cudaError_t launch_gemm_softfloat(const GemmArgs& g, cudaStream_t s);
 // bits per operand).
 int ozaki_default_digit_bits();
 int ozaki_default_digits(int bits);
+// Largest digit count whose 192-bit fold cannot overflow for inner dimension k.
+int ozaki_digit_cap(int bits, int64_t k);
 size_t ozaki_scratch_bytes(int64_t m, int64_t n, int64_t k, int digits, int bits);
 size_t ozaki_error_flag_offset(int64_t m, int64_t n, int64_t k, int digits, int bits);
 cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scratch,

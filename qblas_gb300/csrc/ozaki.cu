@@ -574,6 +574,7 @@ static OzakiLayout ozaki_layout(int64_t m, int64_t n, int64_t k, int s, int b) {
 
 int ozaki_default_digits(int b) { return b == 7 ? 20 : 18; }
 int ozaki_default_digit_bits() { return 8; }
+int ozaki_digit_cap(int bits, int64_t k) { return ozaki_max_digits_for_k(bits, k); }
 
 // ---- optional phase timing (CUDA events on the launching stream) ----------
 namespace {
@@ -635,7 +636,7 @@ size_t ozaki_scratch_bytes(int64_t m, int64_t n, int64_t k, int digits, int bits
 
 cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scratch, cudaStream_t st) {
   if (g.m <= 0 || g.n <= 0 || g.k <= 0) return cudaSuccess;
-  if ((bits != 7 && bits != 8) || digits < 2 || digits > ozaki_max_digits(bits))
+  if ((bits != 7 && bits != 8) || digits < 2 || digits > ozaki_max_digits_for_k(bits, g.k))
     return cudaErrorInvalidValue;
   OzakiLayout L = ozaki_layout(g.m, g.n, g.k, digits, bits);
   char* base = static_cast<char*>(scratch);

@@ -32,6 +32,19 @@ constexpr int kOzakiMaxDigits = 22;  // V < 2^(b*s - 1) <= 2^175 (192-bit split)
 // 31 (int32 diagonal) + b*(s-1) + 1 (sign) <= 191.
 QB_HD int ozaki_max_digits(int b) { return b == 7 ? 22 : 20; }
 
+// Largest digit count for inner dimension k.  The fold value is
+// sum_g C_g 2^(b(G-g)) with |C_g| <= (g+1) k 2^(2(b-1)), so
+// |value| < 2 k 2^(2(b-1)) 2^(b(s-1)) (the geometric tail adds < 2^-6);
+// it fits a 192-bit two's complement number when
+// ceil(log2 k) + 2(b-1) + b(s-1) + 2 <= 191.
+QB_HD int ozaki_max_digits_for_k(int b, int64_t k) {
+  int lk = 0;
+  while (lk < 63 && ((int64_t)1 << lk) < k) ++lk;
+  int s = (191 - 2 - 2 * (b - 1) - lk) / b + 1;
+  int cap = ozaki_max_digits(b);
+  return s < cap ? s : cap;
+}
+
 // k-chunk (in elements) over which a digit product sums exactly in fp32:
 // k * (2^(b-1))^2 <= 2^24.
 QB_HD int ozaki_exact_chunk(int b) { return 1 << (24 - 2 * (b - 1)); }

@@ -292,8 +292,10 @@ QB_HD void wacc_add_product(wacc& acc, const qop& a, const qop& b) {
   wacc_add_signed(acc, q0, q1, q2, q3, q4, q5, q6, 0u, a.s ^ b.s);
 }
 
-// a += b (b unchanged).  The frame moves one bit above the larger operand's
-// so that the sum cannot overflow; bits shifted out are dropped.
+// a += b (b unchanged).  The smaller-exponent operand is aligned to the larger one's frame.  The
+// frame moves up one bit only when an operand could make the sum overflow
+// (|W| >= 2^254, seen as the top two bits differing), so a chain of merges
+// drops no low-order bits unless the magnitude really grows.
 QB_HD void wacc_merge(wacc& a, const wacc& b) {
   a.flags |= b.flags;
   wacc t = b;
@@ -303,11 +305,13 @@ QB_HD void wacc_merge(wacc& a, const wacc& b) {
     a.flags = u.flags;
     t = u;
   }
-  int e_new = a.e + 1;
-  wacc_ashr(a, 1);
-  int k = e_new - t.e;
-  wacc_ashr(t, k);
-  a.e = e_new;
+  wacc_ashr(t, a.e - t.e);
+  const uint32_t big = ((a.w7 ^ (a.w7 << 1)) | (t.w7 ^ (t.w7 << 1))) >> 31;
+  if (big) {
+    wacc_ashr(a, 1);
+    wacc_ashr(t, 1);
+    a.e += 1;
+  }
   wacc_add_signed(a, t.w0, t.w1, t.w2, t.w3, t.w4, t.w5, t.w6, t.w7, 0u);
 }
 
