@@ -72,6 +72,10 @@ enum Slot { kSlotA, kSlotB, kSlotC, kSlotScratch, kSlotResult, kNumSlots };
 struct DevState {
   std::mutex mu;
   cudaStream_t stream = nullptr;
+  // host-pointer qgemm (Ozaki): side streams for the copies of B and C and
+  // the events that order them against the main stream
+  cudaStream_t side[2] = {nullptr, nullptr};
+  cudaEvent_t ev[2] = {nullptr, nullptr};
   void* buf[kNumSlots] = {nullptr};
   size_t cap[kNumSlots] = {0};
   bool pool_ready = false;
@@ -140,6 +144,30 @@ struct HostCall {
     }
   }
 };
+
+int ensure_side_streams(DevState& st) {
+  for (int i = 0; i < 2; ++i) {
+    if (!st.side[i]) {
+      cudaError_t e = cudaStreamCreateWithFlags(&st.side[i], cudaStreamNonBlocking);
+      if (e != cudaSuccess) {
+        cudaGetLastError();
+        st.side[i] = nullptr;
+        return cuda_status(e);
+      }
+    }
+  }
+  for (int i = 0; i < 2; ++i) {
+    if (!st.ev[i]) {
+      cudaError_t e = cudaEventCreateWithFlags(&st.ev[i], cudaEventDisableTiming);
+      if (e != cudaSuccess) {
+        cudaGetLastError();
+        st.ev[i] = nullptr;
+        return cuda_status(e);
+      }
+    }
+  }
+  return qb::kOk;
+}
 
 int64_t extent(int64_t rows, int64_t cols, int64_t srow, int64_t scol) {
   if (rows <= 0 || cols <= 0) return 0;
@@ -322,7 +350,8 @@ size_t gemm_scratch_bytes(const GemmPlan& p) {
 }
 
 int dev_gemm(GemmPlan p, const void* alpha, const void* dA, const void* dB, const void* beta,
-             void* dC, cudaStream_t s, void* scratch_or_null) {
+             void* dC, cudaStream_t s, void* scratch_or_null,
+             const qb::OzakiOverlap* overlap = nullptr) {
   if (!aligned16(dA) || !aligned16(dB) || !aligned16(dC)) return qb::kErrMisaligned;
   p.g.A = (const q128*)dA;
   p.g.B = (const q128*)dB;
@@ -339,7 +368,7 @@ int dev_gemm(GemmPlan p, const void* alpha, const void* dA, const void* dB, cons
       return cuda_status(e);
     }
   }
-  cudaError_t e = qb::launch_gemm_ozaki(p.g, gemm_digits(p.g.k), gemm_digit_bits(), scratch, s);
+  cudaError_t e = qb::launch_gemm_ozaki(p.g, gemm_digits(p.g.k), gemm_digit_bits(), scratch, s, overlap);
   if (!scratch_or_null) cudaFreeAsync(scratch, s);
   return cuda_status(e);
 }
@@ -413,6 +442,33 @@ int host_gemv(char layout, char trans, int64_t m, int64_t n, const void* alpha, 
   return cuda_status(cudaStreamSynchronize(st.stream));
 }
 
+// Copies rows [i0, i1) of the staged C back to the caller once the fold of
+// that band (enqueued on the main stream) is done, on side[1].
+struct BandCopy {
+  DevState* st;
+  void* host_C;
+  GemmPlan p;
+  int64_t copied_rows;
+  static int done(void* ctx, int64_t i0, int64_t i1) {
+    BandCopy* b = static_cast<BandCopy*>(ctx);
+    DevState& s = *b->st;
+    const int64_t sci = b->p.g.sci, n = b->p.g.n;
+    const int64_t off = i0 * sci, cnt = (i1 - 1 - i0) * sci + n;
+    cudaError_t e = cudaEventRecord(s.ev[1], s.stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s.side[1], s.ev[1], 0);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(static_cast<char*>(b->host_C) + off * 16,
+                          static_cast<const char*>(s.buf[kSlotC]) + off * 16, (size_t)cnt * 16,
+                          cudaMemcpyDeviceToHost, s.side[1]);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return 1;
+    }
+    b->copied_rows += i1 - i0;
+    return 0;
+  }
+};
+
 int host_gemm(char layout, char transa, char transb, int64_t m, int64_t n, int64_t k,
               const void* alpha, const void* A, int64_t lda, const void* B, int64_t ldb,
               const void* beta, void* C, int64_t ldc) {
@@ -428,13 +484,44 @@ int host_gemm(char layout, char transa, char transb, int64_t m, int64_t n, int64
       (rc = ensure_slot(st, kSlotC, p.extC * 16)) ||
       (rc = ensure_slot(st, kSlotScratch, gemm_scratch_bytes(p))))
     return rc;
-  if ((rc = h2d(st.buf[kSlotA], A, p.extA, st.stream)) ||
-      (rc = h2d(st.buf[kSlotB], B, p.extB, st.stream)) ||
-      (rc = h2d(st.buf[kSlotC], C, p.extC, st.stream)))
+  if (gemm_method() == 2) {
+    // Ozaki: B is copied and cut into digits on a side stream and C is copied
+    // on another while A is copied and cut on the main stream; the digit
+    // products wait for B's digits and the fold for C.
+    if ((rc = ensure_side_streams(st))) return rc;
+    // rows of C are copied back band by band on side[1] while later bands fold
+    BandCopy bc{&st, C, p, qb::kOk};
+    qb::OzakiOverlap ov{st.side[0], st.ev[0], st.ev[1], &BandCopy::done, &bc};
+    if ((rc = h2d(st.buf[kSlotA], A, p.extA, st.stream)) ||
+        (rc = h2d(st.buf[kSlotB], B, p.extB, st.side[0])) ||
+        (rc = h2d(st.buf[kSlotC], C, p.extC, st.side[1])))
+      return rc;
+    if ((rc = cuda_status(cudaEventRecord(st.ev[1], st.side[1])))) return rc;
+    rc = dev_gemm(p, alpha, st.buf[kSlotA], st.buf[kSlotB], beta, st.buf[kSlotC], st.stream,
+                  st.buf[kSlotScratch], &ov);
+    if (!rc && bc.copied_rows > 0) {
+      // the bands covered C; wait for their copies
+      if (bc.copied_rows != p.g.m) rc = qb::kErrCuda;
+      int rc2 = cuda_status(cudaStreamSynchronize(st.side[1]));
+      int rc3 = cuda_status(cudaStreamSynchronize(st.stream));
+      return rc ? rc : (rc2 ? rc2 : rc3);
+    }
+  } else {
+    if ((rc = h2d(st.buf[kSlotA], A, p.extA, st.stream)) ||
+        (rc = h2d(st.buf[kSlotB], B, p.extB, st.stream)) ||
+        (rc = h2d(st.buf[kSlotC], C, p.extC, st.stream)))
+      return rc;
+    rc = dev_gemm(p, alpha, st.buf[kSlotA], st.buf[kSlotB], beta, st.buf[kSlotC], st.stream,
+                  st.buf[kSlotScratch]);
+  }
+  if (rc) {
+    // leave no copy in flight into the staging buffers on any stream
+    cudaStreamSynchronize(st.stream);
+    if (st.side[0]) cudaStreamSynchronize(st.side[0]);
+    if (st.side[1]) cudaStreamSynchronize(st.side[1]);
+    cudaGetLastError();
     return rc;
-  rc = dev_gemm(p, alpha, st.buf[kSlotA], st.buf[kSlotB], beta, st.buf[kSlotC], st.stream,
-                st.buf[kSlotScratch]);
-  if (rc) return rc;
+  }
   if ((rc = d2h(C, st.buf[kSlotC], p.extC, st.stream))) return rc;
   return cuda_status(cudaStreamSynchronize(st.stream));
 }

@@ -67,8 +67,25 @@ int ozaki_default_digits(int bits);
 int ozaki_digit_cap(int bits, int64_t k);
 size_t ozaki_scratch_bytes(int64_t m, int64_t n, int64_t k, int digits, int bits);
 size_t ozaki_error_flag_offset(int64_t m, int64_t n, int64_t k, int digits, int bits);
+// Optional overlap for callers that copy op(B) and C to the device
+// themselves: the op(B) side (its scales and digits) runs on `b_stream`,
+// in stream order after the copy of B that the caller put there, while op(A)
+// is cut on the main stream; the digit products wait for the op(B) side
+// (`b_done`, recorded here) and the fold waits for `c_ready` (the caller's
+// copy of C).
+// When `band_done` is set and C's rows are contiguous, the fold runs in row
+// bands and band_done(band_ctx, i0, i1) is called after each band's fold is
+// enqueued (rows [i0, i1) of C are then final in stream order), so that the
+// caller can copy a band out while the next one is folded.
+struct OzakiOverlap {
+  cudaStream_t b_stream;
+  cudaEvent_t b_done;
+  cudaEvent_t c_ready;
+  int (*band_done)(void* ctx, int64_t i0, int64_t i1);
+  void* band_ctx;
+};
 cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scratch,
-                              cudaStream_t s);
+                              cudaStream_t s, const OzakiOverlap* overlap = nullptr);
 // Phase timing of Ozaki calls with CUDA events (off by default).
 void ozaki_profile_enable(bool on);
 int ozaki_profile_read(double* out4, int* calls);

@@ -634,7 +634,8 @@ size_t ozaki_scratch_bytes(int64_t m, int64_t n, int64_t k, int digits, int bits
   return ozaki_layout(m, n, k, digits, bits).total;
 }
 
-cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scratch, cudaStream_t st) {
+cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scratch, cudaStream_t st,
+                              const OzakiOverlap* ov) {
   if (g.m <= 0 || g.n <= 0 || g.k <= 0) return cudaSuccess;
   if ((bits != 7 && bits != 8) || digits < 2 || digits > ozaki_max_digits_for_k(bits, g.k))
     return cudaErrorInvalidValue;
@@ -664,16 +665,18 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scr
   }
   prof_record(pe, 0, st);
 
-  // 1. scales and flags: rows of op(A); rows of op(B)^T (= columns of op(B))
+  // 1. scales and flags: rows of op(A); rows of op(B)^T (= columns of op(B)).
+  // The op(B) side runs on sb (the caller's stream for B when overlapping).
+  cudaStream_t sb = ov ? ov->b_stream : st;
   ozaki_fill_kernel<<<(unsigned)((g.m + 255) / 256), 256, 0, st>>>(g.m, S, fa);
-  ozaki_fill_kernel<<<(unsigned)((g.n + 255) / 256), 256, 0, st>>>(g.n, F, fb);
+  ozaki_fill_kernel<<<(unsigned)((g.n + 255) / 256), 256, 0, sb>>>(g.n, F, fb);
   if ((e = cudaMemsetAsync(err, 0, 4, st)) != cudaSuccess) return e;
   {
     int64_t wa = g.m * ((g.k + 63) / 64), wb = g.n * ((g.k + 63) / 64);
     unsigned ba = (unsigned)std::min<int64_t>((wa + 255) / 256, (int64_t)sms * 8);
     unsigned bb = (unsigned)std::min<int64_t>((wb + 255) / 256, (int64_t)sms * 8);
     ozaki_scale_kernel<<<ba, 256, 0, st>>>(g.m, g.k, g.A, g.sai, g.sal, S, fa);
-    ozaki_scale_kernel<<<bb, 256, 0, st>>>(g.n, g.k, g.B, g.sbj, g.sbl, F, fb);
+    ozaki_scale_kernel<<<bb, 256, 0, sb>>>(g.n, g.k, g.B, g.sbj, g.sbl, F, fb);
   }
   // 2. digits
   {
@@ -682,12 +685,16 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scr
     dim3 gb((unsigned)(L.k_pad / 32), (unsigned)(L.n_pad / 8));
     if (L.b == 7) {
       ozaki_split_kernel<7><<<ga, blk, 0, st>>>(g.m, g.k, L.m_pad, L.k_pad, g.A, g.sai, g.sal, S, L.s, DA);
-      ozaki_split_kernel<7><<<gb, blk, 0, st>>>(g.n, g.k, L.n_pad, L.k_pad, g.B, g.sbj, g.sbl, F, L.s, DB);
+      ozaki_split_kernel<7><<<gb, blk, 0, sb>>>(g.n, g.k, L.n_pad, L.k_pad, g.B, g.sbj, g.sbl, F, L.s, DB);
     } else {
       ozaki_split_kernel<8><<<ga, blk, 0, st>>>(g.m, g.k, L.m_pad, L.k_pad, g.A, g.sai, g.sal, S, L.s, DA);
-      ozaki_split_kernel<8><<<gb, blk, 0, st>>>(g.n, g.k, L.n_pad, L.k_pad, g.B, g.sbj, g.sbl, F, L.s, DB);
+      ozaki_split_kernel<8><<<gb, blk, 0, sb>>>(g.n, g.k, L.n_pad, L.k_pad, g.B, g.sbj, g.sbl, F, L.s, DB);
     }
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if (ov) {
+      if ((e = cudaEventRecord(ov->b_done, sb)) != cudaSuccess) return e;
+      if ((e = cudaStreamWaitEvent(st, ov->b_done, 0)) != cudaSuccess) return e;
+    }
   }
   prof_record(pe, 1, st);
   // 3. digit products on the tensor cores, one launch per k pass
@@ -735,12 +742,29 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scr
   F2.alpha = g.alpha; F2.beta = g.beta;
   F2.err = err;
   if ((g.m + 7) / 8 > 65535) return cudaErrorInvalidConfiguration;
-  dim3 fblk(32, 8), fgrid((unsigned)((g.n + 31) / 32), (unsigned)((g.m + 7) / 8));
-  if (L.b == 7)
-    ozaki_fold_kernel<7><<<fgrid, fblk, 0, st>>>(F2);
-  else
-    ozaki_fold_kernel<8><<<fgrid, fblk, 0, st>>>(F2);
-  e = cudaGetLastError();
+  if (ov && (e = cudaStreamWaitEvent(st, ov->c_ready, 0)) != cudaSuccess) return e;
+  // row bands (multiples of 8 rows) when the caller copies C out band by band
+  const bool banded = ov && ov->band_done && g.scj == 1 && g.sci >= g.n && g.m >= 64;
+  const int64_t nbands = banded ? 4 : 1;
+  const int64_t band_rows = ((g.m + nbands - 1) / nbands + 7) / 8 * 8;
+  for (int64_t i0 = 0; i0 < g.m; i0 += band_rows) {
+    const int64_t i1 = std::min(g.m, i0 + band_rows);
+    OzakiFoldParams Fb = F2;
+    Fb.m = i1 - i0;
+    Fb.C = Cg + (size_t)i0 * L.n_pad;  // the diagonal planes keep their m_pad x n_pad shape
+    Fb.S = S + i0;
+    Fb.fa = fa + i0;
+    Fb.A = g.A + i0 * g.sai;
+    Fb.Cout = g.C + i0 * g.sci;
+    dim3 fblk(32, 8), fgrid((unsigned)((g.n + 31) / 32), (unsigned)((Fb.m + 7) / 8));
+    if (L.b == 7)
+      ozaki_fold_kernel<7><<<fgrid, fblk, 0, st>>>(Fb);
+    else
+      ozaki_fold_kernel<8><<<fgrid, fblk, 0, st>>>(Fb);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if (banded && ov->band_done(ov->band_ctx, i0, i1) != 0) return cudaErrorUnknown;
+  }
+  e = cudaSuccess;
   prof_record(pe, 3, st);
   if (pe) {
     std::lock_guard<std::mutex> l(g_prof_mu);
