@@ -43,7 +43,8 @@ from qblas_gb300 import gen as G  # noqa: E402
 from qblas_gb300 import quad as Q  # noqa: E402
 
 FALLBACK = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}
-SWEEP = ((8, 12), (8, 14), (8, 15), (8, 16), (8, 17), (8, 18), (8, 19), (8, 20), (7, 19), (7, 20))
+SWEEP = ((8, 8), (8, 10), (8, 12), (8, 13), (8, 14), (8, 15), (8, 16), (8, 17), (8, 18), (8, 19), (8, 20),
+         (7, 19), (7, 20))
 HEADLINE_DIGITS, HEADLINE_BITS = 17, 8  # <= 1 ulp on this workload (tests/test_gpu_ozaki.py)
 
 
@@ -174,6 +175,14 @@ def ulp_distance(a: np.ndarray, b: np.ndarray) -> np.ndarray:
         return out
     ka, kb = key(a), key(b)
     return np.array([abs(x - y) for x, y in zip(ka, kb)], dtype=np.float64)
+
+
+def relative_error(a: np.ndarray, ref: np.ndarray) -> np.ndarray:
+    """|a - ref| / |ref| for binary128 values, from the ulp distance and the
+    significand of ref (ulp(ref) / |ref| = 2^-112 / 1.f)."""
+    d = ulp_distance(a, ref)
+    f = 1.0 + (ref[:, 1] & np.uint64((1 << 48) - 1)).astype(np.float64) / float(1 << 48)
+    return d * 2.0 ** -112 / f
 
 
 class Qgemm:
@@ -513,6 +522,8 @@ def main():
             idx = rng.integers(0, size * size, 4096)
             d = ulp_distance(C_oz[idx], C_sf[idx])
             secondary["ozaki_ulp_from_correctly_rounded"] = {"max": float(d.max()),
+                                                             "max_rel": float(relative_error(C_oz[idx],
+                                                                                             C_sf[idx]).max()),
                                                              "exact_frac": float((d == 0).mean()),
                                                              "samples": len(idx),
                                                              "reference": "soft-float GPU qgemm (correctly rounded)"}
@@ -522,11 +533,13 @@ def main():
                 api.set_ozaki_slices(s)
                 api.set_ozaki_digit_bits(b)
                 ms_s = time_steps(torch, W.step, 2, 1, dist) / 2
-                ds = ulp_distance(to_host(W.dC)[idx], C_sf[idx])
+                Cs = to_host(W.dC)[idx]
+                ds = ulp_distance(Cs, C_sf[idx])
                 sweep.append({"digit_bits": b, "digits": s, "pairs": s * (s + 1) // 2, "ms": round(ms_s, 3),
                               "gflops": round(W.flops() / (ms_s * 1e-3) / 1e9, 1),
                               "speedup_vs_softfloat": round(ms_sf / ms_s, 2),
                               "max_ulp_from_correctly_rounded": float(ds.max()),
+                              "max_rel": float(relative_error(Cs, C_sf[idx]).max()),
                               "exact_frac": float((ds == 0).mean())})
             api.set_ozaki_slices(slices)
             api.set_ozaki_digit_bits(HEADLINE_BITS)
