@@ -121,14 +121,14 @@ int quadblas_qgemm_dev(char layout, char transa, char transb, int64_t m, int64_t
                        int64_t ldb, const void *beta, void *dC, int64_t ldc, void *stream);
 
 /* Capacity of quadblas_qdot_dev_noalloc's static scratch, in partial
- * accumulators of 40 bytes (40 KiB). */
+ * accumulators of 40 bytes (40 KiB, plus 16 KiB for the exact pass). */
 #define QBLAS_NOALLOC_MAX_PARTIALS 1024
 
 /* No counterpart in the reference.  Same operation and result as
  * quadblas_qdot_dev, for callers that cannot allocate device memory —
  * programs whose device memory belongs to their own allocator or a fixed
  * memory plan, and latency-sensitive loops that cannot call into the CUDA
- * allocator — so it allocates nothing: its scratch is a static 40 KiB array
+ * allocator — so it allocates nothing: its scratch is a static 56 KiB array
  * that the library keeps on every GPU it is loaded on, until exit.  Any n
  * fits on GPUs with up to 256 SMs; a problem that would need more than
  * QBLAS_NOALLOC_MAX_PARTIALS partial accumulators returns

@@ -18,8 +18,12 @@
 // scratch; the block that completes a group (atomic arrival count) merges
 // the partials in index order and applies the epilogue, so results do not
 // depend on scheduling.  No block ever waits for another, so nothing can
-// spin.  Execute allocates nothing and issues one memset and one kernel,
-// so it can be recorded in a CUDA graph.
+// spin.  Every final rounding is certified (exact.cuh); the outputs that are
+// not (sums cancelling below what the wide accumulator's frame holds) are
+// recomputed exactly by the block that finalized them (Kulisch accumulator
+// in the shared memory of the operand tiles).  Execute allocates nothing
+// and issues one memset and one kernel, so it can be recorded in a CUDA
+// graph.
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
@@ -32,6 +36,7 @@
 #include <string>
 #include <vector>
 
+#include "exact.cuh"
 #include "kernels.h"
 #include "quadblas_gpu.h"
 #include "reduce.cuh"
@@ -78,10 +83,17 @@ struct BTile {
 };
 
 struct BShared {
-  BTile a, b;
+  union {
+    struct {
+      BTile a, b;
+    } t;
+    KulischBlock K;  // exact recomputation after an item's accumulation
+  } u;
   wacc red[kBThreads / 32];
   int item;
   int last;
+  int nlist;
+  short list[kBTile * kBTile];  // uncertified outputs of the current item
 };
 
 __device__ __forceinline__ void btile_put(BTile& t, int kk, int idx, q128 v) {
@@ -157,14 +169,14 @@ __device__ void run_gemm_item(BShared& sh, const BProb& P, const BItem& it, wacc
       int bk = e >> 5, bc = e & 31;
       int64_t bl = l0 + bk, gj = it.j0 + bc;
       q128 bv = (bl < it.l1 && gj < P.n) ? ld_cached(P.B + bl * P.sbl + gj * P.sbj) : zero;
-      btile_put(sh.a, ak, ar, av);
-      btile_put(sh.b, bk, bc, bv);
+      btile_put(sh.u.t.a, ak, ar, av);
+      btile_put(sh.u.t.b, bk, bc, bv);
     }
     __syncthreads();
 #pragma unroll 2
     for (int kk = 0; kk < kBTK; ++kk) {
-      qop a0 = btile_get(sh.a, kk, 2 * ty), a1 = btile_get(sh.a, kk, 2 * ty + 1);
-      qop b0 = btile_get(sh.b, kk, 2 * tx), b1 = btile_get(sh.b, kk, 2 * tx + 1);
+      qop a0 = btile_get(sh.u.t.a, kk, 2 * ty), a1 = btile_get(sh.u.t.a, kk, 2 * ty + 1);
+      qop b0 = btile_get(sh.u.t.b, kk, 2 * tx), b1 = btile_get(sh.u.t.b, kk, 2 * tx + 1);
       wacc_add_product(c[0], a0, b0);
       wacc_add_product(c[1], a0, b1);
       wacc_add_product(c[2], a1, b0);
@@ -186,12 +198,27 @@ __device__ void run_gemm_item(BShared& sh, const BProb& P, const BItem& it, wacc
       for (int q = 0; q < 4; ++q) wacc_merge(c[q], wacc_ldcg(src + q));
     }
   }
+  const uint64_t err = 2 * (uint64_t)P.k + 3 * (uint64_t)P.nparts + 2;
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
     int64_t i = it.i0 + 2 * ty + (q >> 1), j = it.j0 + 2 * tx + (q & 1);
     if (i < P.m && j < P.n) {
       q128* p = P.C + i * P.sci + j * P.scj;
-      *p = q_epilogue(P.alpha, wacc_round(c[q]), P.beta, *p);
+      q128 r;
+      if (wacc_round_certified(c[q], err, r))
+        *p = q_epilogue(P.alpha, r, P.beta, *p);
+      else
+        sh.list[atomicAdd(&sh.nlist, 1)] = (short)((2 * ty + (q >> 1)) * kBTile + 2 * tx + (q & 1));
+    }
+  }
+  __syncthreads();
+  const int cnt = sh.nlist;
+  for (int t = 0; t < cnt; ++t) {
+    const int64_t i = it.i0 + sh.list[t] / kBTile, j = it.j0 + sh.list[t] % kBTile;
+    q128 r = block_exact_dot(sh.u.K, P.k, P.A + i * P.sai, P.sal, P.B + j * P.sbj, P.sbl);
+    if (threadIdx.x == 0) {
+      q128* p = P.C + i * P.sci + j * P.scj;
+      *p = q_epilogue(P.alpha, r, P.beta, *p);
     }
   }
 }
@@ -220,7 +247,21 @@ __device__ void run_gemv_item(BShared& sh, const BProb& P, const BItem& it, wacc
   }
   if (lane == 0 && row < P.m) {
     q128* yp = P.C + row * P.sci;
-    *yp = q_epilogue(P.alpha, wacc_round(acc), P.beta, *yp);
+    q128 r;
+    if (wacc_round_certified(acc, 2 * (uint64_t)P.n + 3 * (33 * (uint64_t)P.nparts + 2), r))
+      *yp = q_epilogue(P.alpha, r, P.beta, *yp);
+    else
+      sh.list[atomicAdd(&sh.nlist, 1)] = (short)warp;
+  }
+  __syncthreads();
+  const int cnt = sh.nlist;
+  for (int t = 0; t < cnt; ++t) {
+    const int64_t i = it.i0 + sh.list[t];
+    q128 r = block_exact_dot(sh.u.K, P.n, P.A + i * P.sai, P.sal, P.B, P.sbl);
+    if (threadIdx.x == 0) {
+      q128* yp = P.C + i * P.sci;
+      *yp = q_epilogue(P.alpha, r, P.beta, *yp);
+    }
   }
 }
 
@@ -239,15 +280,28 @@ __device__ void run_dot_item(BShared& sh, const BProb& P, const BItem& it, wacc*
       for (int p = 0; p < P.nparts; ++p) wacc_merge(acc, wacc_ldcg(partials + P.part_base + p));
     }
   }
-  if (threadIdx.x == 0) *P.C = wacc_round(acc);
+  if (threadIdx.x == 0) {
+    q128 r;
+    const bool ok = wacc_round_certified(acc, 2 * (uint64_t)P.n + 3 * (257 * (uint64_t)P.nparts + 2), r);
+    if (ok) *P.C = r;
+    sh.nlist = ok ? 0 : 1;
+  }
+  __syncthreads();
+  if (sh.nlist) {
+    q128 r = block_exact_dot(sh.u.K, P.n, P.A, P.sal, P.B, P.sbl);
+    if (threadIdx.x == 0) *P.C = r;
+  }
 }
 
-__global__ void __launch_bounds__(kBThreads)
+__global__ void __launch_bounds__(kBThreads, 2)
     batched_persistent_kernel(const BProb* __restrict__ probs, const BItem* __restrict__ items,
                               int64_t nitems, int* queue, int* counters, wacc* partials) {
   __shared__ BShared sh;
   while (true) {
-    if (threadIdx.x == 0) sh.item = atomicAdd(queue, 1);
+    if (threadIdx.x == 0) {
+      sh.item = atomicAdd(queue, 1);
+      sh.nlist = 0;
+    }
     __syncthreads();
     const int64_t idx = sh.item;
     __syncthreads();

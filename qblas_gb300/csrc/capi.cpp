@@ -344,13 +344,13 @@ int gemm_digits(int64_t k) {
   return std::min(env ? env : qb::ozaki_default_digits(b), smax);
 }
 
-size_t gemm_scratch_bytes(const GemmPlan& p) {
-  if (gemm_method() != 2) return 0;
+size_t gemm_scratch_bytes(const GemmPlan& p, int method) {
+  if (method != 2) return 0;
   return qb::ozaki_scratch_bytes(p.g.m, p.g.n, p.g.k, gemm_digits(p.g.k), gemm_digit_bits());
 }
 
-int dev_gemm(GemmPlan p, const void* alpha, const void* dA, const void* dB, const void* beta,
-             void* dC, cudaStream_t s, void* scratch_or_null,
+int dev_gemm(GemmPlan p, int method, const void* alpha, const void* dA, const void* dB,
+             const void* beta, void* dC, cudaStream_t s, void* scratch_or_null,
              const qb::OzakiOverlap* overlap = nullptr) {
   if (!aligned16(dA) || !aligned16(dB) || !aligned16(dC)) return qb::kErrMisaligned;
   p.g.A = (const q128*)dA;
@@ -358,8 +358,8 @@ int dev_gemm(GemmPlan p, const void* alpha, const void* dA, const void* dB, cons
   p.g.C = (q128*)dC;
   p.g.alpha = q_load(alpha);
   p.g.beta = q_load(beta);
-  if (gemm_method() != 2) return cuda_status(qb::launch_gemm_softfloat(p.g, s));
-  size_t sb = gemm_scratch_bytes(p);
+  if (method != 2) return cuda_status(qb::launch_gemm_softfloat(p.g, s));
+  size_t sb = gemm_scratch_bytes(p, method);
   void* scratch = scratch_or_null;
   if (!scratch) {
     cudaError_t e = cudaMallocAsync(&scratch, sb, s);
@@ -480,11 +480,12 @@ int host_gemm(char layout, char transa, char transb, int64_t m, int64_t n, int64
   HostCall hc;
   if (hc.status) return hc.status;
   DevState& st = *hc.st;
+  const int method = gemm_method();
   if ((rc = ensure_slot(st, kSlotA, p.extA * 16)) || (rc = ensure_slot(st, kSlotB, p.extB * 16)) ||
       (rc = ensure_slot(st, kSlotC, p.extC * 16)) ||
-      (rc = ensure_slot(st, kSlotScratch, gemm_scratch_bytes(p))))
+      (rc = ensure_slot(st, kSlotScratch, gemm_scratch_bytes(p, method))))
     return rc;
-  if (gemm_method() == 2) {
+  if (method == 2) {
     // Ozaki: B is copied and cut into digits on a side stream and C is copied
     // on another while A is copied and cut on the main stream; the digit
     // products wait for B's digits and the fold for C.
@@ -497,7 +498,7 @@ int host_gemm(char layout, char transa, char transb, int64_t m, int64_t n, int64
         (rc = h2d(st.buf[kSlotC], C, p.extC, st.side[1])))
       return rc;
     if ((rc = cuda_status(cudaEventRecord(st.ev[1], st.side[1])))) return rc;
-    rc = dev_gemm(p, alpha, st.buf[kSlotA], st.buf[kSlotB], beta, st.buf[kSlotC], st.stream,
+    rc = dev_gemm(p, method, alpha, st.buf[kSlotA], st.buf[kSlotB], beta, st.buf[kSlotC], st.stream,
                   st.buf[kSlotScratch], &ov);
     if (!rc && bc.copied_rows > 0) {
       // the bands covered C; wait for their copies
@@ -511,7 +512,7 @@ int host_gemm(char layout, char transa, char transb, int64_t m, int64_t n, int64
         (rc = h2d(st.buf[kSlotB], B, p.extB, st.stream)) ||
         (rc = h2d(st.buf[kSlotC], C, p.extC, st.stream)))
       return rc;
-    rc = dev_gemm(p, alpha, st.buf[kSlotA], st.buf[kSlotB], beta, st.buf[kSlotC], st.stream,
+    rc = dev_gemm(p, method, alpha, st.buf[kSlotA], st.buf[kSlotB], beta, st.buf[kSlotC], st.stream,
                   st.buf[kSlotScratch]);
   }
   if (rc) {
@@ -658,7 +659,7 @@ QBLAS_EXPORT int quadblas_qgemm_dev(char layout, char transa, char transb, int64
   if (rc) return fail(rc);
   if (m == 0 || n == 0 || k == 0) return fail(qb::kOk);
   if (!alpha || !beta) return fail(qb::kErrInvalidValue);
-  return fail(dev_gemm(p, alpha, dA, dB, beta, dC, (cudaStream_t)stream, nullptr));
+  return fail(dev_gemm(p, gemm_method(), alpha, dA, dB, beta, dC, (cudaStream_t)stream, nullptr));
 }
 
 // ===========================================================================

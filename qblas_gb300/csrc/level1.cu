@@ -8,7 +8,10 @@
 // 16-byte loads, every thread keeps one wide accumulator (wacc.cuh), the
 // block merges its threads' accumulators (warp shuffles + shared memory),
 // and a second single-block kernel merges the per-block partials in a
-// fixed order and rounds once.
+// fixed order and rounds once.  That rounding is certified (exact.cuh); if
+// the sum cancels below what the 256-bit frame holds, a third kernel
+// recomputes it exactly (Kulisch accumulator) — it returns at once otherwise.
+#include "exact.cuh"
 #include "kernels.h"
 #include "reduce.cuh"
 
@@ -68,20 +71,38 @@ __global__ void __launch_bounds__(kDotThreads, 4)
   if (threadIdx.x == 0) partials[blockIdx.x] = acc;
 }
 
-// Merges `count` partials and writes the rounded value (or its square root).
+// Merges `count` partials; writes the rounded value (or its square root)
+// when the rounding is certified for the error budget `err`, otherwise
+// arms and resets the exact pass in G.
 __global__ void __launch_bounds__(kDotThreads)
     wacc_finalize_kernel(const wacc* __restrict__ partials, int64_t count, q128* __restrict__ out,
-                         int take_sqrt) {
+                         int take_sqrt, uint64_t err, ExactGlobal* __restrict__ G) {
   __shared__ wacc sm[kDotThreads / 32];
+  __shared__ int need;
   wacc acc;
   wacc_init(acc);
   for (int64_t j = threadIdx.x; j < count; j += blockDim.x) wacc_merge(acc, partials[j]);
   wacc_block_reduce(acc, sm);
   if (threadIdx.x == 0) {
-    q128 r = wacc_round(acc);
-    if (take_sqrt) r = q_sqrt(r);
-    *out = r;
+    q128 r;
+    const bool ok = wacc_round_certified(acc, err, r);
+    if (ok) *out = take_sqrt ? q_sqrt(r) : r;
+    need = ok ? 0 : 1;
+    G->need = need;
   }
+  __syncthreads();
+  if (need) exact_global_reset(G);
+}
+
+// The exact pass: every block adds its share of the products to a
+// Kulisch accumulator; the last block rounds (and takes the square root).
+__global__ void __launch_bounds__(kDotThreads)
+    qdot_exact_kernel(int64_t n, const q128* __restrict__ x, int64_t incx, const q128* __restrict__ y,
+                      int64_t incy, ExactGlobal* __restrict__ G, q128* __restrict__ out, int take_sqrt) {
+  __shared__ KulischBlock K;
+  if (!*reinterpret_cast<volatile int*>(&G->need)) return;
+  q128 r;
+  if (grid_exact_dot(K, G, n, x, incx, y, incy, &r) && threadIdx.x == 0) *out = take_sqrt ? q_sqrt(r) : r;
 }
 
 // One wave of resident blocks (no tail wave), fewer for short vectors.
@@ -102,7 +123,12 @@ static int64_t dot_blocks(int64_t n) {
   return want < cap ? want : cap;
 }
 
-size_t dot_scratch_bytes(int64_t n) { return (size_t)dot_blocks(n) * sizeof(wacc); }
+static size_t dot_partials_bytes(int64_t n) {
+  return ((size_t)dot_blocks(n) * sizeof(wacc) + 255) / 256 * 256;
+}
+
+// Block partials, then the exact pass's state.
+size_t dot_scratch_bytes(int64_t n) { return dot_partials_bytes(n) + sizeof(ExactGlobal); }
 
 __global__ void qzero_kernel(q128* out, int take_sqrt) {
   (void)take_sqrt;
@@ -117,10 +143,19 @@ cudaError_t launch_dot(int64_t n, const q128* x, int64_t incx, const q128* y, in
   }
   int64_t nb = dot_blocks(n);
   wacc* partials = static_cast<wacc*>(scratch);
+  ExactGlobal* G = reinterpret_cast<ExactGlobal*>(static_cast<char*>(scratch) + dot_partials_bytes(n));
   qdot_partial_kernel<<<(unsigned)nb, kDotThreads, 0, s>>>(n, x, incx, y, incy, partials);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  wacc_finalize_kernel<<<1, kDotThreads, 0, s>>>(partials, nb, out, take_sqrt);
+  // truncation budget: 2 units per product, 3 per merge (every thread's
+  // accumulator, the block partials and the final block's merges)
+  const uint64_t err = 2 * (uint64_t)n + 3 * ((uint64_t)nb * kDotThreads + (uint64_t)nb + 2 * kDotThreads + 64);
+  wacc_finalize_kernel<<<1, kDotThreads, 0, s>>>(partials, nb, out, take_sqrt, err, G);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  int64_t gx = (n + 4 * kDotThreads - 1) / (4 * kDotThreads);
+  const int64_t gmax = 2 * (int64_t)device_sm_count();
+  if (gx > gmax) gx = gmax;
+  qdot_exact_kernel<<<(unsigned)gx, kDotThreads, 0, s>>>(n, x, incx, y, incy, G, out, take_sqrt);
   return cudaGetLastError();
 }
 

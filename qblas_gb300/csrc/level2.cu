@@ -20,10 +20,33 @@
 //    columns are split into chunks over blockIdx.y to fill the GPU, each
 //    (row, chunk) leaves a partial accumulator in scratch, and a second
 //    kernel merges the chunks of each row in order and applies the epilogue.
+#include <stddef.h>
+
+#include "exact.cuh"
 #include "kernels.h"
 #include "reduce.cuh"
 
 namespace qb {
+
+// Every row's rounding is certified (exact.cuh).  Rows that cannot be
+// (sums cancelling below the wide accumulator's frame) are left untouched
+// and listed in scratch; qgemv_exact_kernel recomputes them exactly and
+// returns at once when the list is empty.  (The fast kernels keep no exact
+// accumulator in shared memory: the unpacked x is meant to stay in L1.)
+struct RowList {
+  unsigned count;
+  unsigned pad[63];
+  int64_t row[1];  // m entries
+};
+
+__device__ __forceinline__ void gemv_finish_row(q128 alpha, const wacc& acc, uint64_t err, q128 beta,
+                                                q128* yp, int64_t row, RowList* L) {
+  q128 r;
+  if (wacc_round_certified(acc, err, r))
+    *yp = q_epilogue(alpha, r, beta, *yp);
+  else
+    L->row[atomicAdd(&L->count, 1u)] = row;
+}
 
 __device__ __forceinline__ q128 gemv_epilogue(q128 alpha, q128 sum, q128 beta, q128 yv) {
   return q_epilogue(alpha, sum, beta, yv);
@@ -31,8 +54,9 @@ __device__ __forceinline__ q128 gemv_epilogue(q128 alpha, q128 sum, q128 beta, q
 
 // ---- x unpacked once -------------------------------------------------------
 __global__ void qop_unpack_kernel(int64_t n, const q128* __restrict__ x, int64_t incx,
-                                  uint4* __restrict__ xm, int2* __restrict__ xe) {
+                                  uint4* __restrict__ xm, int2* __restrict__ xe, RowList* __restrict__ L) {
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  if (blockIdx.x == 0 && threadIdx.x == 0) L->count = 0;  // this call's list starts empty
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
     qop o = qop_unpack(ld_cached(x + i * incx));
     xm[i] = make_uint4(o.m0, o.m1, o.m2, o.m3);
@@ -61,7 +85,7 @@ constexpr int kRowThreads = 256;
 __global__ void __launch_bounds__(kRowThreads, 4)
     qgemv_rows_kernel(int64_t m, int64_t n, const q128* __restrict__ A, int64_t lda,
                       const uint4* __restrict__ xm, const int2* __restrict__ xe, int wpr_log2,
-                      q128 alpha, q128 beta, q128* __restrict__ y, int64_t incy) {
+                      q128 alpha, q128 beta, q128* __restrict__ y, int64_t incy, RowList* __restrict__ L) {
   __shared__ wacc sm[kRowThreads / 32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int wpr = 1 << wpr_log2;
@@ -89,8 +113,9 @@ __global__ void __launch_bounds__(kRowThreads, 4)
   if (lane == 0 && sub == 0 && row < m) {
     wacc a = sm[warp];
     for (int k = 1; k < wpr; ++k) wacc_merge(a, sm[warp + k]);
-    q128* yp = y + row * incy;
-    *yp = gemv_epilogue(alpha, wacc_round(a), beta, *yp);
+    // budget: 2 per product, 3 per merge (31 per warp and wpr - 1 between warps)
+    const uint64_t err = 2 * (uint64_t)n + 3 * (32 * (uint64_t)wpr + 8);
+    gemv_finish_row(alpha, a, err, beta, y + row * incy, row, L);
   }
 }
 
@@ -104,7 +129,7 @@ __global__ void __launch_bounds__(kColThreads)
     qgemv_cols_kernel(int64_t m, int64_t n, const q128* __restrict__ A, int64_t lda,
                       const uint4* __restrict__ xm, const int2* __restrict__ xe, int64_t jc,
                       q128 alpha, q128 beta, q128* __restrict__ y, int64_t incy,
-                      wacc* __restrict__ partials) {
+                      wacc* __restrict__ partials, RowList* __restrict__ L) {
   const int64_t i = (int64_t)blockIdx.x * kColThreads + threadIdx.x;
   const int64_t chunk = blockIdx.y;
   int64_t j0 = chunk * jc, j1 = j0 + jc;
@@ -122,24 +147,38 @@ __global__ void __launch_bounds__(kColThreads)
     wacc_add_product(acc, qop_unpack(a3), qop_fetch(xm, xe, j + 3));
   }
   for (; j < j1; ++j) wacc_add_product(acc, qop_unpack(ld_stream(A + j * lda + i)), qop_fetch(xm, xe, j));
-  if (gridDim.y == 1) {
-    q128* yp = y + i * incy;
-    *yp = gemv_epilogue(alpha, wacc_round(acc), beta, *yp);
-  } else {
+  if (gridDim.y == 1)
+    gemv_finish_row(alpha, acc, 2 * (uint64_t)n + 3, beta, y + i * incy, i, L);
+  else
     partials[chunk * m + i] = acc;
-  }
 }
 
 __global__ void __launch_bounds__(kColThreads)
-    qgemv_cols_finish_kernel(int64_t m, int64_t nchunks, const wacc* __restrict__ partials,
-                             q128 alpha, q128 beta, q128* __restrict__ y, int64_t incy) {
+    qgemv_cols_finish_kernel(int64_t m, int64_t n, int64_t nchunks, const wacc* __restrict__ partials,
+                             q128 alpha, q128 beta, q128* __restrict__ y, int64_t incy,
+                             RowList* __restrict__ L) {
   const int64_t i = (int64_t)blockIdx.x * kColThreads + threadIdx.x;
   if (i >= m) return;
   wacc acc;
   wacc_init(acc);
   for (int64_t c = 0; c < nchunks; ++c) wacc_merge(acc, partials[c * m + i]);
-  q128* yp = y + i * incy;
-  *yp = gemv_epilogue(alpha, wacc_round(acc), beta, *yp);
+  gemv_finish_row(alpha, acc, 2 * (uint64_t)n + 3 * ((uint64_t)nchunks + 2), beta, y + i * incy, i, L);
+}
+
+// Exact recomputation of the listed rows, one block per row.
+__global__ void __launch_bounds__(256)
+    qgemv_exact_kernel(const RowList* __restrict__ L, int64_t n, MatView A, const q128* __restrict__ x,
+                       int64_t incx, q128 alpha, q128 beta, q128* __restrict__ y, int64_t incy) {
+  __shared__ KulischBlock K;
+  const unsigned cnt = *reinterpret_cast<const volatile unsigned*>(&L->count);
+  for (unsigned t = blockIdx.x; t < cnt; t += gridDim.x) {
+    const int64_t i = L->row[t];
+    q128 r = block_exact_dot(K, n, A.p + i * A.si, A.sj, x, incx);
+    if (threadIdx.x == 0) {
+      q128* yp = y + i * incy;
+      *yp = q_epilogue(alpha, r, beta, *yp);
+    }
+  }
 }
 
 static int64_t col_chunks(int64_t m, int64_t n) {
@@ -154,10 +193,12 @@ static int64_t col_chunks(int64_t m, int64_t n) {
 
 static size_t round256(size_t b) { return (b + 255) & ~(size_t)255; }
 
-// Scratch: [x significands: 16n][x exponents: 8n] (+ column partials)
+static size_t rowlist_bytes(int64_t m) { return round256(offsetof(RowList, row) + (size_t)m * 8); }
+
+// Scratch: [x significands: 16n][x exponents: 8n][uncertified rows] (+ column partials)
 size_t gemv_scratch_bytes(int64_t m, int64_t n, MatView A) {
   if (m <= 0 || n <= 0) return 0;
-  size_t xs = round256((size_t)n * 16) + round256((size_t)n * 8);
+  size_t xs = round256((size_t)n * 16) + round256((size_t)n * 8) + rowlist_bytes(m);
   if (A.sj == 1) return xs;
   int64_t c = col_chunks(m, n);
   return xs + (c > 1 ? (size_t)c * (size_t)m * sizeof(wacc) : 0);
@@ -177,34 +218,41 @@ cudaError_t launch_gemv(int64_t m, int64_t n, q128 alpha, MatView A, const q128*
   char* base = static_cast<char*>(scratch);
   uint4* xm = reinterpret_cast<uint4*>(base);
   int2* xe = reinterpret_cast<int2*>(base + round256((size_t)n * 16));
+  RowList* L = reinterpret_cast<RowList*>(base + round256((size_t)n * 16) + round256((size_t)n * 8));
   {
     int64_t nb = (n + 255) / 256;
     int64_t cap = (int64_t)device_sm_count() * 4;
-    qop_unpack_kernel<<<(unsigned)(nb < cap ? nb : cap), 256, 0, s>>>(n, x, incx, xm, xe);
+    qop_unpack_kernel<<<(unsigned)(nb < cap ? nb : cap), 256, 0, s>>>(n, x, incx, xm, xe, L);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
+  const unsigned exact_grid = (unsigned)device_sm_count();
+  cudaError_t e;
   if (A.sj == 1) {
     int l = rows_wpr_log2(n);
     int64_t rows_per_block = (kRowThreads / 32) >> l;
     int64_t nb = (m + rows_per_block - 1) / rows_per_block;
     if (nb > 0x7fffffff) return cudaErrorInvalidConfiguration;
     qgemv_rows_kernel<<<(unsigned)nb, kRowThreads, 0, s>>>(m, n, A.p, A.si, xm, xe, l, alpha, beta,
-                                                           y, incy);
-    return cudaGetLastError();
+                                                           y, incy, L);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  } else {
+    int64_t c = col_chunks(m, n);
+    int64_t jc = (n + c - 1) / c;
+    c = (n + jc - 1) / jc;
+    dim3 grid((unsigned)((m + kColThreads - 1) / kColThreads), (unsigned)c);
+    size_t xs = round256((size_t)n * 16) + round256((size_t)n * 8) + rowlist_bytes(m);
+    wacc* partials = reinterpret_cast<wacc*>(base + xs);
+    qgemv_cols_kernel<<<grid, kColThreads, 0, s>>>(m, n, A.p, A.sj, xm, xe, jc, alpha, beta, y, incy,
+                                                   partials, L);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if (c > 1) {
+      qgemv_cols_finish_kernel<<<(unsigned)((m + kColThreads - 1) / kColThreads), kColThreads, 0, s>>>(
+          m, n, c, partials, alpha, beta, y, incy, L);
+      if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
   }
-  int64_t c = col_chunks(m, n);
-  int64_t jc = (n + c - 1) / c;
-  c = (n + jc - 1) / jc;
-  dim3 grid((unsigned)((m + kColThreads - 1) / kColThreads), (unsigned)c);
-  size_t xs = round256((size_t)n * 16) + round256((size_t)n * 8);
-  wacc* partials = reinterpret_cast<wacc*>(base + xs);
-  qgemv_cols_kernel<<<grid, kColThreads, 0, s>>>(m, n, A.p, A.sj, xm, xe, jc, alpha, beta, y, incy,
-                                                 partials);
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess || c == 1) return e;
-  qgemv_cols_finish_kernel<<<(unsigned)((m + kColThreads - 1) / kColThreads), kColThreads, 0, s>>>(
-      m, c, partials, alpha, beta, y, incy);
+  qgemv_exact_kernel<<<exact_grid, 256, 0, s>>>(L, n, A, x, incx, alpha, beta, y, incy);
   return cudaGetLastError();
 }
 

@@ -13,6 +13,12 @@
 // unpacked (sign, exponent, significand shifted to bit 127) and staged in
 // shared memory as structure-of-arrays, so the inner loop is the 128x128-bit
 // product and the aligned add into the accumulator.
+//
+// Each rounding is certified (exact.cuh).  The few outputs whose sums
+// cancel below what the 256-bit frame holds are listed in shared memory and
+// recomputed exactly by the whole CTA after its tile (Kulisch accumulator in
+// the shared memory that held the operand slices), so a call is one launch.
+#include "exact.cuh"
 #include "kernels.h"
 #include "reduce.cuh"
 
@@ -54,7 +60,18 @@ __global__ void __launch_bounds__(kGemmThreads)
     qgemm_soft_kernel(int64_t m, int64_t n, int64_t k, const q128* __restrict__ A, int64_t sai,
                       int64_t sal, const q128* __restrict__ B, int64_t sbl, int64_t sbj,
                       q128* __restrict__ C, int64_t sci, int64_t scj, q128 alpha, q128 beta) {
-  __shared__ SoftTile sA, sB;
+  // operand slices during the k-loop; the exact accumulator afterwards
+  __shared__ union {
+    struct {
+      SoftTile a, b;
+    } t;
+    KulischBlock K;
+  } sh;
+  __shared__ int nlist;
+  __shared__ short list[kTM * kTN];
+  SoftTile& sA = sh.t.a;
+  SoftTile& sB = sh.t.b;
+  if (threadIdx.x == 0) nlist = 0;
   const int tid = threadIdx.x;
   const int tx = tid & 15, ty = tid >> 4;
   const int64_t i0 = (int64_t)blockIdx.y * kTM, j0 = (int64_t)blockIdx.x * kTN;
@@ -95,21 +112,30 @@ __global__ void __launch_bounds__(kGemmThreads)
   }
 
   const int64_t ia = i0 + 2 * ty, ja = j0 + 2 * tx;
-  if (ia < m && ja < n) {
-    q128* p = C + ia * sci + ja * scj;
-    *p = q_epilogue(alpha, wacc_round(c00), beta, *p);
+  const uint64_t err = 2 * (uint64_t)k + 2;  // 2 units per product, no merges
+  const wacc* cs[4] = {&c00, &c01, &c10, &c11};
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int64_t i = ia + (q >> 1), j = ja + (q & 1);
+    if (i < m && j < n) {
+      q128 r;
+      if (wacc_round_certified(*cs[q], err, r)) {
+        q128* p = C + i * sci + j * scj;
+        *p = q_epilogue(alpha, r, beta, *p);
+      } else {
+        list[atomicAdd(&nlist, 1)] = (short)((2 * ty + (q >> 1)) * kTN + 2 * tx + (q & 1));
+      }
+    }
   }
-  if (ia < m && ja + 1 < n) {
-    q128* p = C + ia * sci + (ja + 1) * scj;
-    *p = q_epilogue(alpha, wacc_round(c01), beta, *p);
-  }
-  if (ia + 1 < m && ja < n) {
-    q128* p = C + (ia + 1) * sci + ja * scj;
-    *p = q_epilogue(alpha, wacc_round(c10), beta, *p);
-  }
-  if (ia + 1 < m && ja + 1 < n) {
-    q128* p = C + (ia + 1) * sci + (ja + 1) * scj;
-    *p = q_epilogue(alpha, wacc_round(c11), beta, *p);
+  __syncthreads();
+  const int cnt = nlist;
+  for (int t = 0; t < cnt; ++t) {
+    const int64_t i = i0 + list[t] / kTN, j = j0 + list[t] % kTN;
+    q128 r = block_exact_dot(sh.K, k, A + i * sai, sal, B + j * sbj, sbl);
+    if (threadIdx.x == 0) {
+      q128* p = C + i * sci + j * scj;
+      *p = q_epilogue(alpha, r, beta, *p);
+    }
   }
 }
 

@@ -7,20 +7,22 @@
 // memory to their own allocator or memory plan up front (so a cudaMalloc from
 // a library would fail or fragment their pool), and latency-sensitive loops
 // that cannot afford a trip into the CUDA allocator or the device-wide
-// synchronisation that cudaFree implies.  This entry point runs the same two
+// synchronisation that cudaFree implies.  This entry point runs the same
 // qdot kernels, with the same grid, but its scratch is the file-scope array
 // below, so it allocates nothing.
 //
 // The array holds kNoallocPartials = QBLAS_NOALLOC_MAX_PARTIALS accumulators
-// (40 bytes each, 40 KiB in total); every GPU on which the library's module
-// is loaded keeps it until the process exits.  A call needs one accumulator
+// (40 bytes each, 40 KiB) followed by the state of the exact pass (16 KiB of
+// Kulisch digits); every GPU on which the library's module is loaded keeps it
+// until the process exits.  A call needs one accumulator
 // per block, min(ceil(n / 1024), 4 x SM count): any n fits on GPUs with up to
 // 256 SMs (GB300 has 152); on a larger GPU an n whose block count would exceed
 // the array is rejected with QBLAS_ERR_INVALID_VALUE before anything runs.
 //
 // All calls share the one array and it keeps the last call's contents.
 // Nothing in it has to start at zero: every block overwrites its own entry
-// before the second kernel reads it.  Calls whose kernels overlap on the GPU
+// before the second kernel reads it, and the second kernel resets the exact
+// pass's state whenever it arms that pass.  Calls whose kernels overlap on the GPU
 // (the same device, different streams without ordering between them) race on
 // the array and may return wrong results; order them on one stream or with
 // events.
@@ -35,11 +37,14 @@
 
 #include "kernels.h"
 #include "quadblas_gpu.h"
+#include "exact.cuh"
 #include "wacc.cuh"
 
 constexpr int kNoallocPartials = QBLAS_NOALLOC_MAX_PARTIALS;
+constexpr size_t kNoallocBytes =
+    ((size_t)kNoallocPartials * sizeof(qb::wacc) + 255) / 256 * 256 + sizeof(qb::ExactGlobal);
 
-static __device__ __align__(256) qb::wacc g_qdot_noalloc_partials[kNoallocPartials];
+static __device__ __align__(256) unsigned char g_qdot_noalloc_partials[kNoallocBytes];
 
 namespace {
 

@@ -6,6 +6,7 @@
 #include "../qblas_gb300/csrc/softquad.cuh"
 #include "../qblas_gb300/csrc/wacc.cuh"
 #include "../qblas_gb300/csrc/ozaki.cuh"
+#include "../qblas_gb300/csrc/exact.cuh"
 
 using qb::q128;
 
@@ -48,6 +49,40 @@ void sq_wacc_dot(int64_t n, const q128* x, int64_t incx, const q128* y, int64_t 
     qb::wacc_merge(tot, a);
   }
   *out = qb::wacc_round(tot);
+}
+// The wide-accumulator dot as above plus its rounding certificate for the
+// error budget of n products and nsplit merges (2n + 3 nsplit units).
+void sq_wacc_dot_certified(int64_t n, const q128* x, const q128* y, int64_t nsplit, q128* out,
+                           int32_t* certified) {
+  qb::wacc tot;
+  qb::wacc_init(tot);
+  if (nsplit < 1) nsplit = 1;
+  int64_t chunk = (n + nsplit - 1) / nsplit;
+  for (int64_t s = 0; s < nsplit; ++s) {
+    qb::wacc a;
+    qb::wacc_init(a);
+    for (int64_t i = s * chunk; i < n && i < (s + 1) * chunk; ++i)
+      qb::wacc_add_product(a, qb::qop_unpack(x[i]), qb::qop_unpack(y[i]));
+    qb::wacc_merge(tot, a);
+  }
+  *certified = qb::wacc_round_certified(tot, 2 * (uint64_t)n + 3 * (uint64_t)nsplit + 3, *out) ? 1 : 0;
+}
+// Exact dot through the Kulisch accumulator (the device fallback's arithmetic).
+void sq_kulisch_dot(int64_t n, const q128* x, int64_t incx, const q128* y, int64_t incy, q128* out) {
+  static int64_t d[qb::kKDigits];
+  for (int i = 0; i < qb::kKDigits; ++i) d[i] = 0;
+  int lo = qb::kKDigits, hi = -1;
+  uint32_t flags = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    qb::qop a = qb::qop_unpack(x[i * incx]), b = qb::qop_unpack(y[i * incy]);
+    if ((a.cls | b.cls) != qb::kClsFinite)
+      flags |= qb::special_product_flags(a, b);
+    else
+      qb::kulisch_add_product(d, a, b, lo, hi);
+  }
+  if (lo > hi) lo = hi = 0;
+  int64_t carry = qb::kulisch_normalize(d, lo, hi);
+  *out = qb::kulisch_round(d, lo, hi, carry, flags);
 }
 // Ozaki split of a rows x cols view X(r, c) = X[r*sr + c*sc]: row scales
 // S[r] and digits D[t][r][c] (int32), the device kernels' arithmetic.

@@ -9,9 +9,10 @@ prescribed condition, Ogita-Rump-Oishi), against the exact oracle.
   and 22 digits of 7 bits.
 
 Bounds asserted (u_q = 2^-113, ulps of the exact result):
-  * soft-float: correctly rounded (<= 0.5 ulp) up to condition 1e25, where
-    the 256-bit accumulator frame still holds the result's 113 bits below
-    the largest product; at every condition within k * u_q * sum|a_i b_i|.
+  * soft-float: correctly rounded (<= 0.5 ulp) at every condition (the
+    wide accumulator's rounding is certified, and sums that cancel below
+    its 256-bit frame are recomputed exactly), hence also within
+    k * u_q * sum|a_i b_i|.
   * Ozaki with s digits of b bits: |error| <= k (s + 3) 2^(Sa + Sb - b s)
     + 1 ulp, where 2^Sa, 2^Sb bound the row of A and the column of B (the
     split keeps each element to 2^(S - b s + 1) and drops the digit pairs
@@ -78,8 +79,7 @@ def test_qdot_gendot(qlib, O):
             ulps.append(u[0])
             rels.append(rl[0])
             assert O.bound_violations(got, R, ab, K) == 0, (cond, seed)
-            if cond <= 1e25:
-                assert u[0] <= 0.5, (cond, seed, u[0])
+            assert u[0] <= 0.5, (cond, seed, u[0])
         REPORT[f"qdot k=8192 cond={cond:.0e} softfloat"] = summary(np.array(ulps), np.array(rels))
 
 
@@ -121,8 +121,7 @@ def test_qgemm_gendot_softfloat(qlib, O, gendot_matrices):
     got = run_gemm(M)
     ulp = record(O, M, "softfloat", got)
     assert O.bound_violations(got, M["R"], M["ab"], K) == 0
-    ok = M["conds"][M["rows"]] <= 1e25
-    assert ulp[ok & ~M["off"]].max() <= 0.5
+    assert ulp.max() <= 0.5
 
 
 @pytest.mark.parametrize("s,b", [(17, 8), (20, 8), (22, 7)])
