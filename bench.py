@@ -253,11 +253,27 @@ class Qdot:
         self.api.dot_dev(self.n, self.dx, 1, self.dy, 1, self.dr)
 
 
-def hbm_roofline(pk, src, nbytes, ms_per_launch):
+# DRAM bytes (read + write) per launch of the dominant kernel, from one ncu
+# capture of the same workload (profiles/ holds the summaries and commands).
+NCU_TRAFFIC = {
+    "qgemm4096": (29.31e9 + 1.18e9, "profiles/ozaki_mma_kernel_4096_traffic.md"),
+    "qdot26": (2.147608e9 + 4.091e6, "profiles/qdot_partial_kernel_n2p26.md"),
+    "qgemv8192": (1.074185e9 + 9.166e6, "profiles/qgemv_rows_kernel_8192.md"),
+}
+
+
+def traffic(workload):
+    """(DRAM bytes per launch of the dominant kernel, the profile it comes from)."""
+    t = NCU_TRAFFIC.get(workload)
+    return (t[0], t[1]) if t else (None, None)
+
+
+def hbm_roofline(pk, src, nbytes, ms_per_launch, workload=None):
     gbs = nbytes / (ms_per_launch * 1e-3) / 1e9
     peak = float(pk.get("hbm_gbs", FALLBACK["hbm_gbs"]))
+    tb, ts = traffic(workload)
     return {"bound": "hbm", "achieved": round(gbs, 1), "peak": peak, "unit": "GB/s", "frac": round(gbs / peak, 4),
-            "traffic": None, "peak_source": src}
+            "traffic": tb, "traffic_source": ts, "algorithmic_bytes": nbytes, "peak_source": src}
 
 
 def batched_config4(torch, api, rank, reps=3):
@@ -479,7 +495,8 @@ def main():
             tflops = (ph[3] / tot_calls) / (mma_ms * 1e-3) / 1e12
             peak = float(pk.get("bf16_tflops_sustained", FALLBACK["bf16_tflops_sustained"]))
             roof = {"bound": "tensor", "achieved": round(tflops, 1), "peak": peak, "unit": "TFLOP/s",
-                    "frac": round(tflops / peak, 4), "traffic": None, "peak_source": pk_src + " (sustained bf16)",
+                    "frac": round(tflops / peak, 4), "traffic": traffic(wl)[0],
+                    "traffic_source": traffic(wl)[1], "peak_source": pk_src + " (sustained bf16)",
                     "kernel": "ozaki_mma_kernel", "kernel_ms": round(mma_ms, 4),
                     "algorithmic": "2*m*n*k*pairs bf16 flops, pairs = s(s+1)/2 digit products",
                     "phases_ms": {"scale_split": round(ph[0] / tot_calls, 4), "digit_products": round(mma_ms, 4),
@@ -553,7 +570,7 @@ def main():
                 ms2 = time_steps(torch, S.step, args.steps, 3, dist) / args.steps
                 secondary[name] = {"value": round(S.bytes() / (ms2 * 1e-3) / 1e9, 1), "unit": "GB/s",
                                    "ms_per_step": round(ms2, 4),
-                                   "roofline": hbm_roofline(pk, pk_src, S.bytes(), ms2)}
+                                   "roofline": hbm_roofline(pk, pk_src, S.bytes(), ms2, name)}
                 del S
                 torch.cuda.empty_cache()
             api.set_method(1)
@@ -570,8 +587,8 @@ def main():
         ms_step = ms / args.steps
         value = whole_job_rate(W.bytes(), world, ms_step * 1e-3) / 1e9
         metric, unit = "qgemv binary128 GB/s (8192^2 row-major)", "GB/s"
-        launches = 2 * args.steps
-        roof = hbm_roofline(pk, pk_src, W.bytes(), ms_step)
+        launches = 3 * args.steps  # partial/row kernel, finalize or unpack, exact pass (returns at once)
+        roof = hbm_roofline(pk, pk_src, W.bytes(), ms_step, wl)
         e2e, dtype = None, "u32 (soft-float integer limbs)"
         cfg = {"workload": "qgemv 8192x8192 row-major alpha=1 beta=0, wide-exponent values",
                "l2": "inputs larger than L2 (no flush)"}
@@ -582,8 +599,8 @@ def main():
         ms_step = ms / args.steps
         value = whole_job_rate(W.bytes(), world, ms_step * 1e-3) / 1e9
         metric, unit = "qdot binary128 GB/s (n=2^26)", "GB/s"
-        launches = 2 * args.steps
-        roof = hbm_roofline(pk, pk_src, W.bytes(), ms_step)
+        launches = 3 * args.steps  # partial/row kernel, finalize or unpack, exact pass (returns at once)
+        roof = hbm_roofline(pk, pk_src, W.bytes(), ms_step, wl)
         e2e, dtype = None, "u32 (soft-float integer limbs)"
         cfg = {"workload": "qdot n=2^26 wide-exponent values with cancelling pairs",
                "l2": "inputs larger than L2 (no flush)"}

@@ -237,6 +237,33 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
+// The (tile, diagonal) units of one CTA, in order.  Tiles come in full
+// waves of gridDim.x: CTA c takes tile w * gridDim.x + c and runs all its
+// diagonals, highest first, so every CTA of a wave issues the same sequence
+// of (diagonal, pair, k block) loads at the same time and the digit panels
+// they share (A_t of a tile row, B_u of a tile column) are read from DRAM
+// once per wave rather than once per CTA.  The tiles left over after the
+// full waves are spread as (tile, diagonal) units, highest diagonal first.
+__device__ __forceinline__ int cta_unit_count(const OzakiMmaParams& P) {
+  const int tiles = P.tiles_m * P.tiles_n, G1 = P.G + 1;
+  const int waves = tiles / (int)gridDim.x, rem = tiles - waves * (int)gridDim.x;
+  const int tail = rem * G1 - (int)blockIdx.x;
+  return waves * G1 + (tail > 0 ? (tail + (int)gridDim.x - 1) / (int)gridDim.x : 0);
+}
+
+__device__ __forceinline__ void cta_unit(const OzakiMmaParams& P, int j, int& tile, int& g) {
+  const int tiles = P.tiles_m * P.tiles_n, G1 = P.G + 1;
+  const int waves = tiles / (int)gridDim.x, rem = tiles - waves * (int)gridDim.x;
+  if (j < waves * G1) {
+    tile = (j / G1) * (int)gridDim.x + (int)blockIdx.x;
+    g = P.G - j % G1;
+  } else {
+    const int v = (int)blockIdx.x + (j - waves * G1) * (int)gridDim.x;
+    g = P.G - v / rem;
+    tile = waves * (int)gridDim.x + v % rem;
+  }
+}
+
 __global__ void __launch_bounds__(kMmaThreads, 1)
     ozaki_mma_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                      OzakiMmaParams P) {
@@ -278,8 +305,7 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmem_slot;
 
-  const int tiles = P.tiles_m * P.tiles_n;
-  const int units = (P.G + 1) * tiles;
+  const int nun = cta_unit_count(P);
   const int nkb = P.kb_end - P.kb_begin;
   const int nchunks = (nkb + P.chunk_kb - 1) / P.chunk_kb;
   bool ok = true;
@@ -288,8 +314,9 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
     // ---------------- TMA producer ----------------
     if (lane == 0) {
       uint32_t it = 0;
-      for (int unit = blockIdx.x; unit < units && ok; unit += gridDim.x) {
-        const int g = P.G - unit / tiles, tile = unit % tiles;
+      for (int j = 0; j < nun && ok; ++j) {
+        int tile, g;
+        cta_unit(P, j, tile, g);
         const int tm = tile / P.tiles_n, tn = tile % P.tiles_n;
         for (int t = 0; t <= g && ok; ++t) {
           const int u = g - t;
@@ -319,8 +346,9 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
     if (lane == 0) {
       uint32_t it = 0, acc_it = 0;
       bool issued_any = false;
-      for (int unit = blockIdx.x; unit < units && ok; unit += gridDim.x) {
-        const int g = P.G - unit / tiles;
+      for (int j = 0; j < nun && ok; ++j) {
+        int tile, g;
+        cta_unit(P, j, tile, g);
         for (int t = 0; t <= g && ok; ++t) {
           for (int ch = 0; ch < nchunks && ok; ++ch) {
             const int kb0 = P.kb_begin + ch * P.chunk_kb;
@@ -375,8 +403,9 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
 #pragma unroll
     for (int i = 0; i < kBN / 2; ++i) acc[i] = 0;
     uint32_t acc_it = 0;
-    for (int unit = blockIdx.x; unit < units && ok; unit += gridDim.x) {
-      const int g = P.G - unit / tiles, tile = unit % tiles;
+    for (int j = 0; j < nun && ok; ++j) {
+      int tile, g;
+      cta_unit(P, j, tile, g);
       const int tm = tile / P.tiles_n, tn = tile % P.tiles_n;
       for (int t = 0; t <= g && ok; ++t) {
         for (int ch = 0; ch < nchunks && ok; ++ch) {
