@@ -94,23 +94,28 @@ __global__ void ozaki_fill_kernel(int64_t n, int* __restrict__ S, uint32_t* __re
 // D[t * rows_pad * cols_pad + r * cols_pad + c] (bf16).  Block (32, 8):
 // x along columns (coalesced digit stores), y along rows; each digit is
 // stored as soon as it is extracted.
+// Two neighbouring columns (c, c+1) of a row per thread: one packed
+// bf16x2 store per digit (cols_pad is a multiple of 64, so c is even).
 template <int B>
 __global__ void __launch_bounds__(256)
     ozaki_split_kernel(int64_t rows, int64_t cols, int64_t rows_pad, int64_t cols_pad,
                        const q128* __restrict__ p, int64_t sr, int64_t sc,
                        const int* __restrict__ S, int s, __nv_bfloat16* __restrict__ D) {
-  const int64_t c = (int64_t)blockIdx.x * 32 + threadIdx.x;
+  const int64_t c = ((int64_t)blockIdx.x * 32 + threadIdx.x) * 2;
   const int64_t r = (int64_t)blockIdx.y * 8 + threadIdx.y;
   if (c >= cols_pad || r >= rows_pad) return;
-  const int64_t plane = rows_pad * cols_pad;
-  __nv_bfloat16* out = D + r * cols_pad + c;
-  q128 v = q_zero(0);
+  const int64_t plane2 = rows_pad * cols_pad / 2;
+  __nv_bfloat162* out = reinterpret_cast<__nv_bfloat162*>(D + r * cols_pad + c);
+  q128 v0 = q_zero(0), v1 = q_zero(0);
   int Sr = kOzakiScaleEmpty;
-  if (r < rows && c < cols) {
-    v = ld_cached(p + r * sr + c * sc);
+  if (r < rows) {
     Sr = S[r];
+    if (c < cols) v0 = ld_cached(p + r * sr + c * sc);
+    if (c + 1 < cols) v1 = ld_cached(p + r * sr + (c + 1) * sc);
   }
-  ozaki_digits_emit<B>(v, Sr, s, [&](int t, int d) { out[t * plane] = __int2bfloat16_rn(d); });
+  ozaki_digits_emit2<B>(v0, v1, Sr, s, [&](int t, int d0, int d1) {
+    out[t * plane2] = __floats2bfloat162_rn((float)d0, (float)d1);
+  });
 }
 
 // ---------------------------------------------------------------------------
@@ -475,24 +480,17 @@ struct OzakiFoldParams {
 };
 
 template <int B>
-__global__ void __launch_bounds__(256) ozaki_fold_kernel(OzakiFoldParams P) {
+__global__ void __launch_bounds__(256, 3) ozaki_fold_kernel(OzakiFoldParams P) {
   constexpr int kMaxG = (B == 7 ? 22 : 20);
   const int64_t j = (int64_t)blockIdx.x * 32 + threadIdx.x;
   const int64_t i = (int64_t)blockIdx.y * 8 + threadIdx.y;
   if (i >= P.m || j >= P.n) return;
+  if (P.fa[i] | P.fb[j]) return;  // a NaN or infinity in row i or column j: ozaki_special_kernel
   q128* cp = P.Cout + i * P.sci + j * P.scj;
   const q128 cold = *cp;
   q128 sum;
   if (*P.err) {
     sum = q_nan();
-  } else if (P.fa[i] | P.fb[j]) {
-    // a NaN or infinity in row i or column j: direct wide-accumulator dot
-    wacc acc;
-    wacc_init(acc);
-    for (int64_t l = 0; l < P.k; ++l)
-      wacc_add_product(acc, qop_unpack(ld_cached(P.A + i * P.sai + l * P.sal)),
-                       qop_unpack(ld_cached(P.B + l * P.sbl + j * P.sbj)));
-    sum = wacc_round(acc);
   } else {
     const size_t plane = (size_t)P.m_pad * P.n_pad;
     const int32_t* src = P.C + (size_t)i * P.n_pad + j;
@@ -520,6 +518,24 @@ __global__ void __launch_bounds__(256) ozaki_fold_kernel(OzakiFoldParams P) {
     sum = fold_round(f, ozaki_fold_exp(P.S[i], P.F[j], P.G, B));
   }
   *cp = q_epilogue(P.alpha, sum, P.beta, cold);
+}
+
+// Outputs in a row of op(A) or a column of op(B) that holds a NaN or an
+// infinity: a direct wide-accumulator dot, so IEEE special-value semantics
+// are kept (every such sum contains a special product, so it is exact).
+// Threads of other outputs return at once.
+__global__ void __launch_bounds__(256) ozaki_special_kernel(OzakiFoldParams P) {
+  const int64_t j = (int64_t)blockIdx.x * 32 + threadIdx.x;
+  const int64_t i = (int64_t)blockIdx.y * 8 + threadIdx.y;
+  if (i >= P.m || j >= P.n) return;
+  if (!(P.fa[i] | P.fb[j])) return;
+  q128* cp = P.Cout + i * P.sci + j * P.scj;
+  wacc acc;
+  wacc_init(acc);
+  for (int64_t l = 0; l < P.k; ++l)
+    wacc_add_product(acc, qop_unpack(ld_cached(P.A + i * P.sai + l * P.sal)),
+                     qop_unpack(ld_cached(P.B + l * P.sbl + j * P.sbj)));
+  *cp = q_epilogue(P.alpha, wacc_round(acc), P.beta, *cp);
 }
 
 // ---------------------------------------------------------------------------
@@ -710,8 +726,8 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scr
   // 2. digits
   {
     dim3 blk(32, 8);
-    dim3 ga((unsigned)(L.k_pad / 32), (unsigned)(L.m_pad / 8));
-    dim3 gb((unsigned)(L.k_pad / 32), (unsigned)(L.n_pad / 8));
+    dim3 ga((unsigned)(L.k_pad / 64), (unsigned)(L.m_pad / 8));
+    dim3 gb((unsigned)(L.k_pad / 64), (unsigned)(L.n_pad / 8));
     if (L.b == 7) {
       ozaki_split_kernel<7><<<ga, blk, 0, st>>>(g.m, g.k, L.m_pad, L.k_pad, g.A, g.sai, g.sal, S, L.s, DA);
       ozaki_split_kernel<7><<<gb, blk, 0, sb>>>(g.n, g.k, L.n_pad, L.k_pad, g.B, g.sbj, g.sbl, F, L.s, DB);
@@ -790,6 +806,8 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scr
       ozaki_fold_kernel<7><<<fgrid, fblk, 0, st>>>(Fb);
     else
       ozaki_fold_kernel<8><<<fgrid, fblk, 0, st>>>(Fb);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    ozaki_special_kernel<<<fgrid, fblk, 0, st>>>(Fb);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     if (banded && ov->band_done(ov->band_ctx, i0, i1) != 0) return cudaErrorUnknown;
   }

@@ -83,6 +83,43 @@ QB_HD uint32_t ozaki_field(uint64_t v0, uint64_t v1, uint64_t v2, int p) {
   return (uint32_t)(x & mask);
 }
 
+// V = trunc(|a| * 2^(B*s - 1 - S)) as three 64-bit words and the sign of a;
+// V = 0 for zero, NaN, infinity and an empty scale.
+template <int B>
+QB_HD void ozaki_scaled(q128 a, int S, int s, uint64_t& v0, uint64_t& v1, uint64_t& v2, bool& neg) {
+  v0 = v1 = v2 = 0;
+  neg = q_sign(a) != 0;
+  if (q_bexp(a) == kExpField || q_iszero(a) || S == kOzakiScaleEmpty) return;
+  uint64_t mh, ml;
+  int E;
+  q_unpack_norm(a, mh, ml, E);
+  // V = trunc(m * 2^(E + B*s - 113 - S)); the shift is at most B*s - 114.
+  int sh = E + B * s - 113 - S;
+  if (sh >= 0) {
+    u256 t = u256_shl(u256_make(0, 0, mh, ml), sh);
+    v0 = t.w0;
+    v1 = t.w1;
+    v2 = t.w2;
+  } else {
+    bool st;
+    u256 t = u256_shr_sticky(u256_make(0, 0, mh, ml), -sh, st);
+    v0 = t.w0;
+    v1 = t.w1;
+  }
+}
+
+// Digit j (0 = least significant) of V from its raw field and the running
+// carry; the top digit (j = s - 1) keeps r + carry.
+template <int B>
+QB_HD int ozaki_digit_step(uint64_t v0, uint64_t v1, uint64_t v2, int j, int s, int& carry) {
+  int d = (int)ozaki_field<B>(v0, v1, v2, B * j) + carry;
+  if (j < s - 1) {
+    carry = d >= (1 << (B - 1));
+    d -= carry << B;
+  }
+  return d;
+}
+
 // The s balanced base-2^B digits of a for scale S, passed to emit(t, d_t)
 // from the least significant (t = s-1) to the most significant (t = 0).
 // V = trunc(|a| * 2^(B*s - 1 - S)) < 2^(B*s - 1) is cut into its raw B-bit
@@ -94,40 +131,35 @@ QB_HD uint32_t ozaki_field(uint64_t v0, uint64_t v1, uint64_t v2, int p) {
 template <int B, typename Emit>
 QB_HD void ozaki_digits_emit(q128 a, int S, int s, Emit emit) {
   constexpr int kMax = B == 7 ? 22 : 20;
-  int be = q_bexp(a);
-  if (be == kExpField || q_iszero(a) || S == kOzakiScaleEmpty) {
-    for (int t = s - 1; t >= 0; --t) emit(t, 0);
-    return;
-  }
-  const bool neg = q_sign(a) != 0;
-  uint64_t mh, ml;
-  int E;
-  q_unpack_norm(a, mh, ml, E);
-  // V = trunc(m * 2^(E + B*s - 113 - S)); the shift is at most B*s - 114.
-  int sh = E + B * s - 113 - S;
   uint64_t v0, v1, v2;
-  if (sh >= 0) {
-    u256 t = u256_shl(u256_make(0, 0, mh, ml), sh);
-    v0 = t.w0;
-    v1 = t.w1;
-    v2 = t.w2;
-  } else {
-    bool st;
-    u256 t = u256_shr_sticky(u256_make(0, 0, mh, ml), -sh, st);
-    v0 = t.w0;
-    v1 = t.w1;
-    v2 = 0;
-  }
+  bool neg;
+  ozaki_scaled<B>(a, S, s, v0, v1, v2, neg);
   int carry = 0;
 #pragma unroll
   for (int j = 0; j < kMax; ++j) {
     if (j < s) {
-      int d = (int)ozaki_field<B>(v0, v1, v2, B * j) + carry;
-      if (j < s - 1) {
-        carry = d >= (1 << (B - 1));
-        d -= carry << B;
-      }
+      int d = ozaki_digit_step<B>(v0, v1, v2, j, s, carry);
       emit(s - 1 - j, neg ? -d : d);
+    }
+  }
+}
+
+// The same for two values with one scale (two neighbours in a row):
+// emit(t, d_t(a), d_t(b)).
+template <int B, typename Emit2>
+QB_HD void ozaki_digits_emit2(q128 a, q128 b, int S, int s, Emit2 emit) {
+  constexpr int kMax = B == 7 ? 22 : 20;
+  uint64_t a0, a1, a2, b0, b1, b2;
+  bool na, nb;
+  ozaki_scaled<B>(a, S, s, a0, a1, a2, na);
+  ozaki_scaled<B>(b, S, s, b0, b1, b2, nb);
+  int ca = 0, cb = 0;
+#pragma unroll
+  for (int j = 0; j < kMax; ++j) {
+    if (j < s) {
+      int da = ozaki_digit_step<B>(a0, a1, a2, j, s, ca);
+      int db = ozaki_digit_step<B>(b0, b1, b2, j, s, cb);
+      emit(s - 1 - j, na ? -da : da, nb ? -db : db);
     }
   }
 }
