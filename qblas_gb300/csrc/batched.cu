@@ -230,9 +230,21 @@ __device__ void run_gemv_item(BShared& sh, const BProb& P, const BItem& it, wacc
   wacc acc;
   wacc_init(acc);
   if (row < P.m) {
+    // four loads in flight per lane (A read once, x shared by the rows)
     const q128* Ar = P.A + row * P.sai;
-    for (int64_t j = it.l0 + lane; j < it.l1; j += 32)
-      wacc_add_product(acc, qop_unpack(ld_cached(Ar + j * P.sal)), qop_unpack(ld_cached(P.B + j * P.sbl)));
+    int64_t j = it.l0 + lane;
+    for (; j + 96 < it.l1; j += 128) {
+      q128 a0 = ld_stream(Ar + j * P.sal), a1 = ld_stream(Ar + (j + 32) * P.sal);
+      q128 a2 = ld_stream(Ar + (j + 64) * P.sal), a3 = ld_stream(Ar + (j + 96) * P.sal);
+      q128 x0 = ld_cached(P.B + j * P.sbl), x1 = ld_cached(P.B + (j + 32) * P.sbl);
+      q128 x2 = ld_cached(P.B + (j + 64) * P.sbl), x3 = ld_cached(P.B + (j + 96) * P.sbl);
+      wacc_add_product(acc, qop_unpack(a0), qop_unpack(x0));
+      wacc_add_product(acc, qop_unpack(a1), qop_unpack(x1));
+      wacc_add_product(acc, qop_unpack(a2), qop_unpack(x2));
+      wacc_add_product(acc, qop_unpack(a3), qop_unpack(x3));
+    }
+    for (; j < it.l1; j += 32)
+      wacc_add_product(acc, qop_unpack(ld_stream(Ar + j * P.sal)), qop_unpack(ld_cached(P.B + j * P.sbl)));
   }
   wacc_warp_reduce(acc);
   if (P.nparts > 1) {
@@ -269,7 +281,18 @@ __device__ void run_dot_item(BShared& sh, const BProb& P, const BItem& it, wacc*
                              int* counters) {
   wacc acc;
   wacc_init(acc);
-  for (int64_t i = it.l0 + threadIdx.x; i < it.l1; i += kBThreads)
+  int64_t i = it.l0 + threadIdx.x;
+  for (; i + 3 * kBThreads < it.l1; i += 4 * kBThreads) {
+    q128 x0 = ld_stream(P.A + i * P.sal), x1 = ld_stream(P.A + (i + kBThreads) * P.sal);
+    q128 x2 = ld_stream(P.A + (i + 2 * kBThreads) * P.sal), x3 = ld_stream(P.A + (i + 3 * kBThreads) * P.sal);
+    q128 y0 = ld_stream(P.B + i * P.sbl), y1 = ld_stream(P.B + (i + kBThreads) * P.sbl);
+    q128 y2 = ld_stream(P.B + (i + 2 * kBThreads) * P.sbl), y3 = ld_stream(P.B + (i + 3 * kBThreads) * P.sbl);
+    wacc_add_product(acc, qop_unpack(x0), qop_unpack(y0));
+    wacc_add_product(acc, qop_unpack(x1), qop_unpack(y1));
+    wacc_add_product(acc, qop_unpack(x2), qop_unpack(y2));
+    wacc_add_product(acc, qop_unpack(x3), qop_unpack(y3));
+  }
+  for (; i < it.l1; i += kBThreads)
     wacc_add_product(acc, qop_unpack(ld_cached(P.A + i * P.sal)), qop_unpack(ld_cached(P.B + i * P.sbl)));
   wacc_block_reduce(acc, sh.red);
   if (P.nparts > 1) {
