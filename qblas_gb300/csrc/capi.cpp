@@ -68,14 +68,17 @@ q128 q_load(const void* p) {
 
 // ---- per-device state for the host-pointer entry points -------------------
 enum Slot { kSlotA, kSlotB, kSlotC, kSlotScratch, kSlotResult, kNumSlots };
+enum Side { kSideB, kSideC, kSideACopy, kSideA, kNumSides };
+enum Event { kEvBDone, kEvCReady, kEvBCopied, kEvACopied, kEvADone, kEvFoldBand, kNumEvents };
 
 struct DevState {
   std::mutex mu;
   cudaStream_t stream = nullptr;
-  // host-pointer qgemm (Ozaki): side streams for the copies of B and C and
-  // the events that order them against the main stream
-  cudaStream_t side[2] = {nullptr, nullptr};
-  cudaEvent_t ev[2] = {nullptr, nullptr};
+  // host-pointer qgemm (Ozaki): side streams (kSideB: copy and digits of B;
+  // kSideC: copies of C in and out; kSideACopy: copies of A's row bands;
+  // kSideA: digits of A) and the events that order them
+  cudaStream_t side[kNumSides] = {nullptr, nullptr, nullptr, nullptr};
+  cudaEvent_t ev[kNumEvents] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   void* buf[kNumSlots] = {nullptr};
   size_t cap[kNumSlots] = {0};
   bool pool_ready = false;
@@ -146,7 +149,7 @@ struct HostCall {
 };
 
 int ensure_side_streams(DevState& st) {
-  for (int i = 0; i < 2; ++i) {
+  for (int i = 0; i < kNumSides; ++i) {
     if (!st.side[i]) {
       cudaError_t e = cudaStreamCreateWithFlags(&st.side[i], cudaStreamNonBlocking);
       if (e != cudaSuccess) {
@@ -156,7 +159,7 @@ int ensure_side_streams(DevState& st) {
       }
     }
   }
-  for (int i = 0; i < 2; ++i) {
+  for (int i = 0; i < kNumEvents; ++i) {
     if (!st.ev[i]) {
       cudaError_t e = cudaEventCreateWithFlags(&st.ev[i], cudaEventDisableTiming);
       if (e != cudaSuccess) {
@@ -454,17 +457,61 @@ struct BandCopy {
     DevState& s = *b->st;
     const int64_t sci = b->p.g.sci, n = b->p.g.n;
     const int64_t off = i0 * sci, cnt = (i1 - 1 - i0) * sci + n;
-    cudaError_t e = cudaEventRecord(s.ev[1], s.stream);
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(s.side[1], s.ev[1], 0);
+    cudaError_t e = cudaEventRecord(s.ev[kEvFoldBand], s.stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s.side[kSideC], s.ev[kEvFoldBand], 0);
     if (e == cudaSuccess)
       e = cudaMemcpyAsync(static_cast<char*>(b->host_C) + off * 16,
                           static_cast<const char*>(s.buf[kSlotC]) + off * 16, (size_t)cnt * 16,
-                          cudaMemcpyDeviceToHost, s.side[1]);
+                          cudaMemcpyDeviceToHost, s.side[kSideC]);
     if (e != cudaSuccess) {
       cudaGetLastError();
       return 1;
     }
     b->copied_rows += i1 - i0;
+    return 0;
+  }
+};
+
+// Copies rows [r0, r1) of op(A) into the staged A on kSideACopy, after the
+// copy of B (which the first digit products need whole), and makes stream s
+// wait for them; the copy of C is queued behind the last band.  When op(A)'s
+// rows are not contiguous, the first band copies all of A.
+struct ARowCopy {
+  DevState* st;
+  const void* host_A;
+  const void* host_C;
+  GemmPlan p;
+  static int rows(void* ctx, int64_t r0, int64_t r1, cudaStream_t s) {
+    ARowCopy* a = static_cast<ARowCopy*>(ctx);
+    DevState& d = *a->st;
+    const qb::GemmArgs& g = a->p.g;
+    cudaStream_t cs = d.side[kSideACopy];
+    cudaError_t e = cudaSuccess;
+    if (r0 == 0) e = cudaStreamWaitEvent(cs, d.ev[kEvBCopied], 0);
+    int64_t off = 0, cnt = 0;
+    if (g.sal == 1 && g.sai >= g.k) {
+      off = r0 * g.sai;
+      cnt = (r1 - 1 - r0) * g.sai + g.k;
+    } else if (r0 == 0) {
+      cnt = a->p.extA;
+    }
+    if (e == cudaSuccess && cnt > 0)
+      e = cudaMemcpyAsync(static_cast<char*>(d.buf[kSlotA]) + off * 16,
+                          static_cast<const char*>(a->host_A) + off * 16, (size_t)cnt * 16,
+                          cudaMemcpyHostToDevice, cs);
+    if (e == cudaSuccess) e = cudaEventRecord(d.ev[kEvACopied], cs);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s, d.ev[kEvACopied], 0);
+    if (e == cudaSuccess && r1 == g.m) {
+      cudaStream_t cc = d.side[kSideC];
+      e = cudaStreamWaitEvent(cc, d.ev[kEvACopied], 0);
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(d.buf[kSlotC], a->host_C, (size_t)a->p.extC * 16, cudaMemcpyHostToDevice, cc);
+      if (e == cudaSuccess) e = cudaEventRecord(d.ev[kEvCReady], cc);
+    }
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return 1;
+    }
     return 0;
   }
 };
@@ -486,24 +533,25 @@ int host_gemm(char layout, char transa, char transb, int64_t m, int64_t n, int64
       (rc = ensure_slot(st, kSlotScratch, gemm_scratch_bytes(p, method))))
     return rc;
   if (method == 2) {
-    // Ozaki: B is copied and cut into digits on a side stream and C is copied
-    // on another while A is copied and cut on the main stream; the digit
-    // products wait for B's digits and the fold for C.
+    // Ozaki, with the host link kept busy in the order the GPU needs the
+    // data: B first (copied and cut into digits on kSideB), then A in row
+    // bands (each band cut on kSideA as it lands, and the digit products of
+    // the tiles that need it start at once), then C (needed by the fold);
+    // C comes back band by band on kSideC while later bands fold.
     if ((rc = ensure_side_streams(st))) return rc;
-    // rows of C are copied back band by band on side[1] while later bands fold
     BandCopy bc{&st, C, p, qb::kOk};
-    qb::OzakiOverlap ov{st.side[0], st.ev[0], st.ev[1], &BandCopy::done, &bc};
-    if ((rc = h2d(st.buf[kSlotA], A, p.extA, st.stream)) ||
-        (rc = h2d(st.buf[kSlotB], B, p.extB, st.side[0])) ||
-        (rc = h2d(st.buf[kSlotC], C, p.extC, st.side[1])))
+    ARowCopy ac{&st, A, C, p};
+    qb::OzakiOverlap ov{st.side[kSideB], st.ev[kEvBDone], st.ev[kEvCReady], &BandCopy::done, &bc,
+                        &ARowCopy::rows, &ac, st.side[kSideA], st.ev[kEvADone]};
+    if ((rc = h2d(st.buf[kSlotB], B, p.extB, st.side[kSideB])) ||
+        (rc = cuda_status(cudaEventRecord(st.ev[kEvBCopied], st.side[kSideB]))))
       return rc;
-    if ((rc = cuda_status(cudaEventRecord(st.ev[1], st.side[1])))) return rc;
     rc = dev_gemm(p, method, alpha, st.buf[kSlotA], st.buf[kSlotB], beta, st.buf[kSlotC], st.stream,
                   st.buf[kSlotScratch], &ov);
     if (!rc && bc.copied_rows > 0) {
       // the bands covered C; wait for their copies
       if (bc.copied_rows != p.g.m) rc = qb::kErrCuda;
-      int rc2 = cuda_status(cudaStreamSynchronize(st.side[1]));
+      int rc2 = cuda_status(cudaStreamSynchronize(st.side[kSideC]));
       int rc3 = cuda_status(cudaStreamSynchronize(st.stream));
       return rc ? rc : (rc2 ? rc2 : rc3);
     }
@@ -518,8 +566,8 @@ int host_gemm(char layout, char transa, char transb, int64_t m, int64_t n, int64
   if (rc) {
     // leave no copy in flight into the staging buffers on any stream
     cudaStreamSynchronize(st.stream);
-    if (st.side[0]) cudaStreamSynchronize(st.side[0]);
-    if (st.side[1]) cudaStreamSynchronize(st.side[1]);
+    for (int i = 0; i < kNumSides; ++i)
+      if (st.side[i]) cudaStreamSynchronize(st.side[i]);
     cudaGetLastError();
     return rc;
   }

@@ -77,12 +77,22 @@ size_t ozaki_error_flag_offset(int64_t m, int64_t n, int64_t k, int digits, int 
 // bands and band_done(band_ctx, i0, i1) is called after each band's fold is
 // enqueued (rows [i0, i1) of C are then final in stream order), so that the
 // caller can copy a band out while the next one is folded.
+//
+// When `a_rows` is set, op(A) is cut into digits band by band on `a_stream`:
+// a_rows(a_ctx, r0, r1, a_stream) is called before each band and must make
+// a_stream wait until rows [r0, r1) of op(A) are on the device (so that the
+// caller can copy A in row bands); the digit products of the tiles that
+// need a band start as soon as it is cut (`a_done` is recorded for that).
 struct OzakiOverlap {
   cudaStream_t b_stream;
   cudaEvent_t b_done;
   cudaEvent_t c_ready;
   int (*band_done)(void* ctx, int64_t i0, int64_t i1);
   void* band_ctx;
+  int (*a_rows)(void* ctx, int64_t r0, int64_t r1, cudaStream_t s);
+  void* a_ctx;
+  cudaStream_t a_stream;
+  cudaEvent_t a_done;
 };
 cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scratch,
                               cudaStream_t s, const OzakiOverlap* overlap = nullptr);

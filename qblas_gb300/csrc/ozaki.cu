@@ -96,15 +96,17 @@ __global__ void ozaki_fill_kernel(int64_t n, int* __restrict__ S, uint32_t* __re
 // stored as soon as it is extracted.
 // Two neighbouring columns (c, c+1) of a row per thread: one packed
 // bf16x2 store per digit (cols_pad is a multiple of 64, so c is even).
+// Digit t of row r goes to D[t * plane + r * cols_pad + c]; rows in
+// [rows, rows_pad) get zero digits.
 template <int B>
 __global__ void __launch_bounds__(256)
-    ozaki_split_kernel(int64_t rows, int64_t cols, int64_t rows_pad, int64_t cols_pad,
+    ozaki_split_kernel(int64_t rows, int64_t cols, int64_t rows_pad, int64_t cols_pad, int64_t plane,
                        const q128* __restrict__ p, int64_t sr, int64_t sc,
                        const int* __restrict__ S, int s, __nv_bfloat16* __restrict__ D) {
   const int64_t c = ((int64_t)blockIdx.x * 32 + threadIdx.x) * 2;
   const int64_t r = (int64_t)blockIdx.y * 8 + threadIdx.y;
   if (c >= cols_pad || r >= rows_pad) return;
-  const int64_t plane2 = rows_pad * cols_pad / 2;
+  const int64_t plane2 = plane / 2;
   __nv_bfloat162* out = reinterpret_cast<__nv_bfloat162*>(D + r * cols_pad + c);
   q128 v0 = q_zero(0), v1 = q_zero(0);
   int Sr = kOzakiScaleEmpty;
@@ -134,7 +136,8 @@ constexpr unsigned long long kWaitLimitNs = 1000000000ull;  // 1 s per wait
 
 struct OzakiMmaParams {
   int tiles_m, tiles_n;
-  int G;         // highest diagonal (s - 1)
+  int tile_begin, tile_end;  // tiles of this launch (tile = tm * tiles_n + tn)
+  int G;                     // highest diagonal (s - 1)
   int m_pad, n_pad;
   int kb_begin, kb_end;  // k-blocks of this pass
   int chunk_kb;          // k-blocks summed exactly in fp32 before a readout
@@ -250,22 +253,22 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
 // once per wave rather than once per CTA.  The tiles left over after the
 // full waves are spread as (tile, diagonal) units, highest diagonal first.
 __device__ __forceinline__ int cta_unit_count(const OzakiMmaParams& P) {
-  const int tiles = P.tiles_m * P.tiles_n, G1 = P.G + 1;
+  const int tiles = P.tile_end - P.tile_begin, G1 = P.G + 1;
   const int waves = tiles / (int)gridDim.x, rem = tiles - waves * (int)gridDim.x;
   const int tail = rem * G1 - (int)blockIdx.x;
   return waves * G1 + (tail > 0 ? (tail + (int)gridDim.x - 1) / (int)gridDim.x : 0);
 }
 
 __device__ __forceinline__ void cta_unit(const OzakiMmaParams& P, int j, int& tile, int& g) {
-  const int tiles = P.tiles_m * P.tiles_n, G1 = P.G + 1;
+  const int tiles = P.tile_end - P.tile_begin, G1 = P.G + 1;
   const int waves = tiles / (int)gridDim.x, rem = tiles - waves * (int)gridDim.x;
   if (j < waves * G1) {
-    tile = (j / G1) * (int)gridDim.x + (int)blockIdx.x;
+    tile = P.tile_begin + (j / G1) * (int)gridDim.x + (int)blockIdx.x;
     g = P.G - j % G1;
   } else {
     const int v = (int)blockIdx.x + (j - waves * G1) * (int)gridDim.x;
     g = P.G - v / rem;
-    tile = waves * (int)gridDim.x + v % rem;
+    tile = P.tile_begin + waves * (int)gridDim.x + v % rem;
   }
 }
 
@@ -710,39 +713,60 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scr
   }
   prof_record(pe, 0, st);
 
-  // 1. scales and flags: rows of op(A); rows of op(B)^T (= columns of op(B)).
-  // The op(B) side runs on sb (the caller's stream for B when overlapping).
+  // 1. op(B) (its rows are the columns of op(B)): scales, flags and digits on
+  // sb (the caller's stream for B when overlapping); the digit products wait
+  // for it.
   cudaStream_t sb = ov ? ov->b_stream : st;
-  ozaki_fill_kernel<<<(unsigned)((g.m + 255) / 256), 256, 0, st>>>(g.m, S, fa);
+  const bool banded = ov && ov->a_rows;
+  cudaStream_t sa = banded ? ov->a_stream : st;  // op(A): scales and digits, band by band
+  ozaki_fill_kernel<<<(unsigned)((g.m + 255) / 256), 256, 0, sa>>>(g.m, S, fa);
   ozaki_fill_kernel<<<(unsigned)((g.n + 255) / 256), 256, 0, sb>>>(g.n, F, fb);
   if ((e = cudaMemsetAsync(err, 0, 4, st)) != cudaSuccess) return e;
+  const dim3 blk(32, 8);
+  const int64_t plane_a = L.m_pad * L.k_pad, plane_b = L.n_pad * L.k_pad;
   {
-    int64_t wa = g.m * ((g.k + 63) / 64), wb = g.n * ((g.k + 63) / 64);
-    unsigned ba = (unsigned)std::min<int64_t>((wa + 255) / 256, (int64_t)sms * 8);
+    int64_t wb = g.n * ((g.k + 63) / 64);
     unsigned bb = (unsigned)std::min<int64_t>((wb + 255) / 256, (int64_t)sms * 8);
-    ozaki_scale_kernel<<<ba, 256, 0, st>>>(g.m, g.k, g.A, g.sai, g.sal, S, fa);
     ozaki_scale_kernel<<<bb, 256, 0, sb>>>(g.n, g.k, g.B, g.sbj, g.sbl, F, fb);
-  }
-  // 2. digits
-  {
-    dim3 blk(32, 8);
-    dim3 ga((unsigned)(L.k_pad / 64), (unsigned)(L.m_pad / 8));
     dim3 gb((unsigned)(L.k_pad / 64), (unsigned)(L.n_pad / 8));
-    if (L.b == 7) {
-      ozaki_split_kernel<7><<<ga, blk, 0, st>>>(g.m, g.k, L.m_pad, L.k_pad, g.A, g.sai, g.sal, S, L.s, DA);
-      ozaki_split_kernel<7><<<gb, blk, 0, sb>>>(g.n, g.k, L.n_pad, L.k_pad, g.B, g.sbj, g.sbl, F, L.s, DB);
-    } else {
-      ozaki_split_kernel<8><<<ga, blk, 0, st>>>(g.m, g.k, L.m_pad, L.k_pad, g.A, g.sai, g.sal, S, L.s, DA);
-      ozaki_split_kernel<8><<<gb, blk, 0, sb>>>(g.n, g.k, L.n_pad, L.k_pad, g.B, g.sbj, g.sbl, F, L.s, DB);
-    }
+    if (L.b == 7)
+      ozaki_split_kernel<7><<<gb, blk, 0, sb>>>(g.n, g.k, L.n_pad, L.k_pad, plane_b, g.B, g.sbj, g.sbl, F, L.s, DB);
+    else
+      ozaki_split_kernel<8><<<gb, blk, 0, sb>>>(g.n, g.k, L.n_pad, L.k_pad, plane_b, g.B, g.sbj, g.sbl, F, L.s, DB);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     if (ov) {
       if ((e = cudaEventRecord(ov->b_done, sb)) != cudaSuccess) return e;
       if ((e = cudaStreamWaitEvent(st, ov->b_done, 0)) != cudaSuccess) return e;
     }
   }
-  prof_record(pe, 1, st);
-  // 3. digit products on the tensor cores, one launch per k pass
+  // rows [r0, r1) of op(A) (r0, r1 multiples of the 128-row tile, r1 <= m_pad):
+  // scales, flags and digits on sa; the main stream then waits for them
+  auto cut_a = [&](int64_t r0, int64_t r1) -> cudaError_t {
+    const int64_t rows = std::min(r1, g.m) - r0;
+    cudaError_t ee;
+    if (banded && ov->a_rows(ov->a_ctx, r0, r0 + rows, sa) != 0) return cudaErrorUnknown;
+    int64_t wa = rows * ((g.k + 63) / 64);
+    unsigned ba = (unsigned)std::max<int64_t>(1, std::min<int64_t>((wa + 255) / 256, (int64_t)sms * 8));
+    if (rows > 0) ozaki_scale_kernel<<<ba, 256, 0, sa>>>(rows, g.k, g.A + r0 * g.sai, g.sai, g.sal, S + r0, fa + r0);
+    dim3 ga((unsigned)(L.k_pad / 64), (unsigned)((r1 - r0) / 8));
+    const q128* Ab = g.A + r0 * g.sai;
+    if (L.b == 7)
+      ozaki_split_kernel<7><<<ga, blk, 0, sa>>>(rows, g.k, r1 - r0, L.k_pad, plane_a, Ab, g.sai, g.sal, S + r0,
+                                                L.s, DA + r0 * L.k_pad);
+    else
+      ozaki_split_kernel<8><<<ga, blk, 0, sa>>>(rows, g.k, r1 - r0, L.k_pad, plane_a, Ab, g.sai, g.sal, S + r0,
+                                                L.s, DA + r0 * L.k_pad);
+    if ((ee = cudaGetLastError()) != cudaSuccess) return ee;
+    if (banded) {
+      if ((ee = cudaEventRecord(ov->a_done, sa)) != cudaSuccess) return ee;
+      if ((ee = cudaStreamWaitEvent(st, ov->a_done, 0)) != cudaSuccess) return ee;
+    }
+    return cudaSuccess;
+  };
+  // 2. digit products on the tensor cores: one launch per (tile band, k pass).
+  // Without a caller delivering op(A) by rows there is one band; with one,
+  // the bands are whole waves of tiles (one tile per SM), at most 8, and
+  // each band's digit products start as soon as its rows of op(A) are cut.
   CUtensorMap tmA, tmB;
   if (!make_map(&tmA, DA, (int64_t)L.s * L.m_pad, L.k_pad, kBM) ||
       !make_map(&tmB, DB, (int64_t)L.s * L.n_pad, L.k_pad, kBN))
@@ -757,25 +781,16 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scr
     attr_set[dev] = true;
   }
   const int tiles_m = (int)(L.m_pad / kBM), tiles_n = (int)(L.n_pad / kBN);
-  const int units = (L.G + 1) * tiles_m * tiles_n;
+  const int tiles = tiles_m * tiles_n;
   const int kb_total = (int)(L.k_pad / kBK), kbp = pass_kblocks(L.s, L.b);
-  for (int p = 0; p < L.npass; ++p) {
-    OzakiMmaParams P;
-    P.tiles_m = tiles_m;
-    P.tiles_n = tiles_n;
-    P.G = L.G;
-    P.m_pad = (int)L.m_pad;
-    P.n_pad = (int)L.n_pad;
-    P.kb_begin = p * kbp;
-    P.kb_end = std::min(kb_total, (p + 1) * kbp);
-    P.chunk_kb = chunk_kblocks(L.b);
-    P.C = Cg + (size_t)p * (L.G + 1) * L.m_pad * L.n_pad;
-    P.err = err;
-    ozaki_mma_kernel<<<(unsigned)std::min(units, sms), kMmaThreads, kMmaSmem, st>>>(tmA, tmB, P);
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  int band_tiles = tiles;
+  if (banded) {
+    const int waves = (tiles + sms - 1) / sms;
+    band_tiles = ((waves + 7) / 8) * sms;
   }
-  prof_record(pe, 2, st);
-  // 4. fold + epilogue
+  // 3. fold + epilogue of rows [i0, i1) (the diagonal planes keep their
+  // m_pad x n_pad shape); with a caller copying C out band by band, each
+  // band is handed over as soon as it is folded
   OzakiFoldParams F2;
   F2.m = g.m; F2.n = g.n; F2.k = g.k;
   F2.G = L.G; F2.npass = L.npass; F2.b = L.b;
@@ -787,16 +802,17 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scr
   F2.alpha = g.alpha; F2.beta = g.beta;
   F2.err = err;
   if ((g.m + 7) / 8 > 65535) return cudaErrorInvalidConfiguration;
-  if (ov && (e = cudaStreamWaitEvent(st, ov->c_ready, 0)) != cudaSuccess) return e;
-  // row bands (multiples of 8 rows) when the caller copies C out band by band
-  const bool banded = ov && ov->band_done && g.scj == 1 && g.sci >= g.n && g.m >= 64;
-  const int64_t nbands = banded ? 4 : 1;
-  const int64_t band_rows = ((g.m + nbands - 1) / nbands + 7) / 8 * 8;
-  for (int64_t i0 = 0; i0 < g.m; i0 += band_rows) {
-    const int64_t i1 = std::min(g.m, i0 + band_rows);
+  const bool fold_banded = ov && ov->band_done && g.scj == 1 && g.sci >= g.n && g.m >= 64;
+  bool c_waited = false;
+  auto fold_rows = [&](int64_t i0, int64_t i1) -> cudaError_t {
+    cudaError_t ee;
+    if (ov && !c_waited) {
+      if ((ee = cudaStreamWaitEvent(st, ov->c_ready, 0)) != cudaSuccess) return ee;
+      c_waited = true;
+    }
     OzakiFoldParams Fb = F2;
     Fb.m = i1 - i0;
-    Fb.C = Cg + (size_t)i0 * L.n_pad;  // the diagonal planes keep their m_pad x n_pad shape
+    Fb.C = Cg + (size_t)i0 * L.n_pad;
     Fb.S = S + i0;
     Fb.fa = fa + i0;
     Fb.A = g.A + i0 * g.sai;
@@ -806,10 +822,58 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scr
       ozaki_fold_kernel<7><<<fgrid, fblk, 0, st>>>(Fb);
     else
       ozaki_fold_kernel<8><<<fgrid, fblk, 0, st>>>(Fb);
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if ((ee = cudaGetLastError()) != cudaSuccess) return ee;
     ozaki_special_kernel<<<fgrid, fblk, 0, st>>>(Fb);
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    if (banded && ov->band_done(ov->band_ctx, i0, i1) != 0) return cudaErrorUnknown;
+    if ((ee = cudaGetLastError()) != cudaSuccess) return ee;
+    if (fold_banded && ov->band_done(ov->band_ctx, i0, i1) != 0) return cudaErrorUnknown;
+    return cudaSuccess;
+  };
+
+  int64_t rows_cut = 0, rows_folded = 0;
+  for (int t0 = 0; t0 < tiles; t0 += band_tiles) {
+    const int t1 = std::min(tiles, t0 + band_tiles);
+    const int64_t rows_needed = std::min<int64_t>(L.m_pad, (int64_t)((t1 - 1) / tiles_n + 1) * kBM);
+    if (rows_needed > rows_cut) {
+      if ((e = cut_a(rows_cut, rows_needed)) != cudaSuccess) return e;
+      rows_cut = rows_needed;
+    }
+    if (t0 == 0) prof_record(pe, 1, st);
+    const int units = (L.G + 1) * (t1 - t0);
+    for (int p = 0; p < L.npass; ++p) {
+      OzakiMmaParams P;
+      P.tiles_m = tiles_m;
+      P.tiles_n = tiles_n;
+      P.tile_begin = t0;
+      P.tile_end = t1;
+      P.G = L.G;
+      P.m_pad = (int)L.m_pad;
+      P.n_pad = (int)L.n_pad;
+      P.kb_begin = p * kbp;
+      P.kb_end = std::min(kb_total, (p + 1) * kbp);
+      P.chunk_kb = chunk_kblocks(L.b);
+      P.C = Cg + (size_t)p * (L.G + 1) * L.m_pad * L.n_pad;
+      P.err = err;
+      ozaki_mma_kernel<<<(unsigned)std::min(units, sms), kMmaThreads, kMmaSmem, st>>>(tmA, tmB, P);
+      if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
+    // rows whose tiles are all done can be folded while later bands multiply
+    if (banded && fold_banded && t1 < tiles) {
+      const int64_t rows_done = std::min<int64_t>(g.m, (int64_t)(t1 / tiles_n) * kBM);
+      if (rows_done > rows_folded) {
+        if ((e = fold_rows(rows_folded, rows_done)) != cudaSuccess) return e;
+        rows_folded = rows_done;
+      }
+    }
+  }
+  prof_record(pe, 2, st);
+  // the remaining rows (all of them without banding), in up to 4 bands when
+  // the caller copies C out band by band
+  {
+    const int64_t left = g.m - rows_folded;
+    const int64_t nb = fold_banded ? 4 : 1;
+    const int64_t band_rows = ((left + nb - 1) / nb + 7) / 8 * 8;
+    for (int64_t i0 = rows_folded; i0 < g.m; i0 += band_rows)
+      if ((e = fold_rows(i0, std::min(g.m, i0 + band_rows))) != cudaSuccess) return e;
   }
   e = cudaSuccess;
   prof_record(pe, 3, st);
