@@ -44,8 +44,8 @@ from qblas_gb300 import quad as Q  # noqa: E402
 
 FALLBACK = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}
 SWEEP = ((8, 8), (8, 10), (8, 12), (8, 13), (8, 14), (8, 15), (8, 16), (8, 17), (8, 18), (8, 19), (8, 20),
-         (7, 19), (7, 20))
-HEADLINE_DIGITS, HEADLINE_BITS = 17, 8  # <= 1 ulp on this workload (tests/test_gpu_ozaki.py)
+         (7, 19), (7, 20), (9, 13), (9, 14), (9, 15), (9, 16))
+HEADLINE_DIGITS, HEADLINE_BITS = 15, 9  # <= 1 ulp on this workload (tests/test_gpu_ozaki.py)
 
 
 def peaks():
@@ -450,6 +450,7 @@ def main():
     ap.add_argument("--workload", default="qgemm4096", choices=["qgemm4096", "qgemm2048", "qgemm512", "qgemv8192", "qdot26"])
     ap.add_argument("--method", default="ozaki", choices=["softfloat", "ozaki"])
     ap.add_argument("--slices", type=int, default=0)
+    ap.add_argument("--bits", type=int, default=0, help="digit width for the Ozaki method (7, 8 or 9)")
     ap.add_argument("--no-secondary", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
@@ -472,8 +473,9 @@ def main():
     method = 2 if args.method == "ozaki" else 1
     api.set_method(method)
     slices = args.slices or HEADLINE_DIGITS
+    bits = args.bits or HEADLINE_BITS
     api.set_ozaki_slices(slices)
-    api.set_ozaki_digit_bits(HEADLINE_BITS)
+    api.set_ozaki_digit_bits(bits)
 
     line = {}
     secondary = {}
@@ -521,7 +523,7 @@ def main():
                             "full 113-bit significand, e uniform [-20,20])") if size >= 2048 else
                f"qgemm m=n=k={size} row-major NN alpha=1 beta=0, full-mantissa uniform [-1,1)",
                "method": args.method, "digits_per_operand": slices if method == 2 else None,
-               "digit_bits": HEADLINE_BITS if method == 2 else None,
+               "digit_bits": bits if method == 2 else None,
                "l2": "inputs larger than L2 (no flush)" if size >= 2048 else "inputs fit in L2",
                "parallelism": f"replicas x{world}"}
 
@@ -559,7 +561,7 @@ def main():
                               "max_rel": float(relative_error(Cs, C_sf[idx]).max()),
                               "exact_frac": float((ds == 0).mean())})
             api.set_ozaki_slices(slices)
-            api.set_ozaki_digit_bits(HEADLINE_BITS)
+            api.set_ozaki_digit_bits(bits)
             secondary["digit_sweep"] = sweep
         if not args.no_secondary and size == 4096:
             del W

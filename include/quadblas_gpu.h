@@ -187,7 +187,9 @@ int quadblas_get_method(void);
  * 20 for 7-bit), else 2..20 (8-bit) or 2..22 (7-bit). */
 int quadblas_set_ozaki_slices(int slices);
 int quadblas_get_ozaki_slices(void);
-/* Ozaki digit width: 0 = default (8), 7 or 8 bits per balanced digit. */
+/* Ozaki digit width: 0 = default (9), 7 or 8 bits per balanced digit (bf16
+ * digit products) or 9 (fp16 digit products: fewer digit pairs for the same
+ * bits, more k passes). */
 int quadblas_set_ozaki_digit_bits(int bits);
 int quadblas_get_ozaki_digit_bits(void);
 /* Phase timing of Ozaki qgemm calls (no reference counterpart): when

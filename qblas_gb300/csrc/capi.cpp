@@ -726,7 +726,7 @@ QBLAS_EXPORT int quadblas_set_ozaki_slices(int slices) {
 }
 QBLAS_EXPORT int quadblas_get_ozaki_slices(void) { return g_slices.load(); }
 QBLAS_EXPORT int quadblas_set_ozaki_digit_bits(int bits) {
-  if (bits != 0 && bits != 7 && bits != 8) return fail(qb::kErrInvalidValue);
+  if (bits != 0 && (bits < 7 || bits > 9)) return fail(qb::kErrInvalidValue);
   g_digit_bits.store(bits);
   return fail(qb::kOk);
 }

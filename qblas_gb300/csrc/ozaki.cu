@@ -98,16 +98,28 @@ __global__ void ozaki_fill_kernel(int64_t n, int* __restrict__ S, uint32_t* __re
 // bf16x2 store per digit (cols_pad is a multiple of 64, so c is even).
 // Digit t of row r goes to D[t * plane + r * cols_pad + c]; rows in
 // [rows, rows_pad) get zero digits.
+// Digits are stored as bf16 (b = 7, 8) or fp16 (b = 9), two per 32-bit word.
+template <int B>
+__device__ __forceinline__ uint32_t pack_digits(int d0, int d1) {
+  if (B == 9) {
+    __half2 h = __floats2half2_rn((float)d0, (float)d1);
+    return *reinterpret_cast<uint32_t*>(&h);
+  } else {
+    __nv_bfloat162 h = __floats2bfloat162_rn((float)d0, (float)d1);
+    return *reinterpret_cast<uint32_t*>(&h);
+  }
+}
+
 template <int B>
 __global__ void __launch_bounds__(256)
     ozaki_split_kernel(int64_t rows, int64_t cols, int64_t rows_pad, int64_t cols_pad, int64_t plane,
                        const q128* __restrict__ p, int64_t sr, int64_t sc,
-                       const int* __restrict__ S, int s, __nv_bfloat16* __restrict__ D) {
+                       const int* __restrict__ S, int s, uint16_t* __restrict__ D) {
   const int64_t c = ((int64_t)blockIdx.x * 32 + threadIdx.x) * 2;
   const int64_t r = (int64_t)blockIdx.y * 8 + threadIdx.y;
   if (c >= cols_pad || r >= rows_pad) return;
   const int64_t plane2 = plane / 2;
-  __nv_bfloat162* out = reinterpret_cast<__nv_bfloat162*>(D + r * cols_pad + c);
+  uint32_t* out = reinterpret_cast<uint32_t*>(D + r * cols_pad + c);
   q128 v0 = q_zero(0), v1 = q_zero(0);
   int Sr = kOzakiScaleEmpty;
   if (r < rows) {
@@ -115,9 +127,7 @@ __global__ void __launch_bounds__(256)
     if (c < cols) v0 = ld_cached(p + r * sr + c * sc);
     if (c + 1 < cols) v1 = ld_cached(p + r * sr + (c + 1) * sc);
   }
-  ozaki_digits_emit2<B>(v0, v1, Sr, s, [&](int t, int d0, int d1) {
-    out[t * plane2] = __floats2bfloat162_rn((float)d0, (float)d1);
-  });
+  ozaki_digits_emit2<B>(v0, v1, Sr, s, [&](int t, int d0, int d1) { out[t * plane2] = pack_digits<B>(d0, d1); });
 }
 
 // ---------------------------------------------------------------------------
@@ -137,6 +147,7 @@ constexpr unsigned long long kWaitLimitNs = 1000000000ull;  // 1 s per wait
 struct OzakiMmaParams {
   int tiles_m, tiles_n;
   int tile_begin, tile_end;  // tiles of this launch (tile = tm * tiles_n + tn)
+  uint32_t idesc;            // instruction descriptor (bf16 or fp16 digits)
   int G;                     // highest diagonal (s - 1)
   int m_pad, n_pad;
   int kb_begin, kb_end;  // k-blocks of this pass
@@ -211,17 +222,19 @@ __device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t addr) {
   return d;
 }
 
-// Instruction descriptor: kind::f16, A = B = bf16, D = f32, K-major A and B,
-// N = 256, M = 128.
-constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kBN >> 3) << 17) |
-                            ((uint32_t)(kBM >> 4) << 24);
+// Instruction descriptors: kind::f16, D = f32, K-major A and B, N = 256,
+// M = 128; A and B both bf16 (bits 7-9 and 10-12 = 1) or both fp16 (= 0).
+constexpr uint32_t kIdescShape = (1u << 4) | ((uint32_t)(kBN >> 3) << 17) | ((uint32_t)(kBM >> 4) << 24);
+constexpr uint32_t kIdescBf16 = kIdescShape | (1u << 7) | (1u << 10);
+constexpr uint32_t kIdescF16 = kIdescShape;
 
-__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t accum) {
+__device__ __forceinline__ void mma_f16kind(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc,
+                                            uint32_t accum) {
   asm volatile(
       "{\n\t.reg .pred p;\n\t"
       "setp.ne.b32 p, %4, 0;\n\t"
       "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
-      "l"(a), "l"(b), "r"(kIdesc), "r"(accum)
+      "l"(a), "l"(b), "r"(idesc), "r"(accum)
       : "memory");
 }
 
@@ -381,8 +394,8 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
 #pragma unroll
               for (int k = 0; k < kBK / 16; ++k) {
                 // +32 bytes per K=16 step inside the 128-byte swizzled row
-                mma_bf16(dcol, da + (uint64_t)(2 * k), db + (uint64_t)(2 * k),
-                         (kb > kb0 || k > 0) ? 1u : 0u);
+                mma_f16kind(dcol, da + (uint64_t)(2 * k), db + (uint64_t)(2 * k), P.idesc,
+                            (kb > kb0 || k > 0) ? 1u : 0u);
               }
               issued_any = true;
               mma_commit(empty_bar(s));
@@ -482,45 +495,51 @@ struct OzakiFoldParams {
   const int* err;
 };
 
+// Each thread folds four neighbouring columns j0..j0+3 of one row: one
+// 16-byte load per diagonal plane (and k pass) feeds four Horner states, so
+// a warp reads 512 contiguous bytes per plane; then one rounding and the
+// reference epilogue per output.  (n_pad is a multiple of 256, so the four
+// columns are always inside the planes; columns >= n are not written.)
 template <int B>
 __global__ void __launch_bounds__(256, 3) ozaki_fold_kernel(OzakiFoldParams P) {
-  constexpr int kMaxG = (B == 7 ? 22 : 20);
-  const int64_t j = (int64_t)blockIdx.x * 32 + threadIdx.x;
+  const int64_t j0 = ((int64_t)blockIdx.x * 32 + threadIdx.x) * 4;
   const int64_t i = (int64_t)blockIdx.y * 8 + threadIdx.y;
-  if (i >= P.m || j >= P.n) return;
-  if (P.fa[i] | P.fb[j]) return;  // a NaN or infinity in row i or column j: ozaki_special_kernel
-  q128* cp = P.Cout + i * P.sci + j * P.scj;
-  const q128 cold = *cp;
-  q128 sum;
-  if (*P.err) {
-    sum = q_nan();
-  } else {
-    const size_t plane = (size_t)P.m_pad * P.n_pad;
-    const int32_t* src = P.C + (size_t)i * P.n_pad + j;
-    int32_t v[kMaxG];
-    // all diagonal loads first (independent), then the Horner fold
+  if (i >= P.m || j0 >= P.n) return;
+  const size_t plane4 = (size_t)P.m_pad * P.n_pad / 4;
+  const size_t pass4 = (size_t)(P.G + 1) * plane4;
+  const int4* src = reinterpret_cast<const int4*>(P.C + (size_t)i * P.n_pad + j0);
+  fold192 f[4];
 #pragma unroll
-    for (int g = 0; g < kMaxG; ++g) v[g] = g <= P.G ? __ldcs(src + g * plane) : 0;
-    fold192 f;
-    fold_init(f);
-    if (P.npass == 1) {
-#pragma unroll
-      for (int g = 0; g < kMaxG; ++g)
-        if (g <= P.G) fold_step_t<B>(f, v[g]);
-    } else {
-      const size_t pass = (size_t)(P.G + 1) * plane;
-#pragma unroll
-      for (int g = 0; g < kMaxG; ++g) {
-        if (g <= P.G) {
-          int64_t t = v[g];
-          for (int p = 1; p < P.npass; ++p) t += __ldcs(src + p * pass + g * plane);
-          fold_step_t<B>(f, t);
-        }
-      }
+  for (int c = 0; c < 4; ++c) fold_init(f[c]);
+#pragma unroll 4
+  for (int g = 0; g <= P.G; ++g) {
+    const int4 v = __ldcs(src + g * plane4);
+    int64_t t0 = v.x, t1 = v.y, t2 = v.z, t3 = v.w;
+    for (int p = 1; p < P.npass; ++p) {
+      const int4 w = __ldcs(src + p * pass4 + g * plane4);
+      t0 += w.x;
+      t1 += w.y;
+      t2 += w.z;
+      t3 += w.w;
     }
-    sum = fold_round(f, ozaki_fold_exp(P.S[i], P.F[j], P.G, B));
+    fold_step_t<B>(f[0], t0);
+    fold_step_t<B>(f[1], t1);
+    fold_step_t<B>(f[2], t2);
+    fold_step_t<B>(f[3], t3);
   }
-  *cp = q_epilogue(P.alpha, sum, P.beta, cold);
+  const bool failed = *P.err != 0;
+  const int Si = P.S[i];
+  const uint32_t fai = P.fa[i];
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    const int64_t j = j0 + c;
+    if (j < P.n && !(fai | P.fb[j])) {  // NaN / inf rows and columns: ozaki_special_kernel
+      q128* cp = P.Cout + i * P.sci + j * P.scj;
+      const q128 cold = *cp;
+      const q128 sum = failed ? q_nan() : fold_round(f[c], ozaki_fold_exp(Si, P.F[j], P.G, B));
+      *cp = q_epilogue(P.alpha, sum, P.beta, cold);
+    }
+  }
 }
 
 // Outputs in a row of op(A) or a column of op(B) that holds a NaN or an
@@ -564,15 +583,17 @@ static EncodeTiledFn encode_fn() {
   return fn;
 }
 
-// 2-D bf16 tensor map over D[rows][cols] with a (64 x box_rows) box, 128B swizzle.
-static bool make_map(CUtensorMap* map, const void* D, int64_t rows, int64_t cols, int box_rows) {
+// 2-D tensor map (bf16, or fp16 for 9-bit digits) over D[rows][cols] with a
+// (64 x box_rows) box, 128B swizzle.
+static bool make_map(CUtensorMap* map, const void* D, int64_t rows, int64_t cols, int box_rows, bool f16) {
   EncodeTiledFn fn = encode_fn();
   if (!fn) return false;
   cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
   cuuint64_t strides[1] = {(cuuint64_t)cols * 2};
   cuuint32_t box[2] = {(cuuint32_t)kBK, (cuuint32_t)box_rows};
   cuuint32_t estr[2] = {1, 1};
-  CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(D), dims, strides, box,
+  CUresult r = fn(map, f16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2,
+                  const_cast<void*>(D), dims, strides, box,
                   estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return r == CUDA_SUCCESS;
@@ -620,8 +641,8 @@ static OzakiLayout ozaki_layout(int64_t m, int64_t n, int64_t k, int s, int b) {
   return L;
 }
 
-int ozaki_default_digits(int b) { return b == 7 ? 20 : 18; }
-int ozaki_default_digit_bits() { return 8; }
+int ozaki_default_digits(int b) { return b == 7 ? 20 : (b == 8 ? 18 : 16); }
+int ozaki_default_digit_bits() { return 9; }
 int ozaki_digit_cap(int bits, int64_t k) { return ozaki_max_digits_for_k(bits, k); }
 
 // ---- optional phase timing (CUDA events on the launching stream) ----------
@@ -682,10 +703,32 @@ size_t ozaki_scratch_bytes(int64_t m, int64_t n, int64_t k, int digits, int bits
   return ozaki_layout(m, n, k, digits, bits).total;
 }
 
+// Launches for the digit width b (7, 8 or 9).
+static void launch_split(int b, dim3 grid, dim3 blk, cudaStream_t st, int64_t rows, int64_t cols,
+                         int64_t rows_pad, int64_t cols_pad, int64_t plane, const q128* p, int64_t sr,
+                         int64_t sc, const int* S, int s, uint16_t* D) {
+  if (b == 7)
+    ozaki_split_kernel<7><<<grid, blk, 0, st>>>(rows, cols, rows_pad, cols_pad, plane, p, sr, sc, S, s, D);
+  else if (b == 8)
+    ozaki_split_kernel<8><<<grid, blk, 0, st>>>(rows, cols, rows_pad, cols_pad, plane, p, sr, sc, S, s, D);
+  else
+    ozaki_split_kernel<9><<<grid, blk, 0, st>>>(rows, cols, rows_pad, cols_pad, plane, p, sr, sc, S, s, D);
+}
+
+static void launch_fold(int b, cudaStream_t st, const OzakiFoldParams& F) {
+  dim3 blk(32, 8), grid((unsigned)((F.n + 127) / 128), (unsigned)((F.m + 7) / 8));
+  if (b == 7)
+    ozaki_fold_kernel<7><<<grid, blk, 0, st>>>(F);
+  else if (b == 8)
+    ozaki_fold_kernel<8><<<grid, blk, 0, st>>>(F);
+  else
+    ozaki_fold_kernel<9><<<grid, blk, 0, st>>>(F);
+}
+
 cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scratch, cudaStream_t st,
                               const OzakiOverlap* ov) {
   if (g.m <= 0 || g.n <= 0 || g.k <= 0) return cudaSuccess;
-  if ((bits != 7 && bits != 8) || digits < 2 || digits > ozaki_max_digits_for_k(bits, g.k))
+  if ((bits < 7 || bits > 9) || digits < 2 || digits > ozaki_max_digits_for_k(bits, g.k))
     return cudaErrorInvalidValue;
   OzakiLayout L = ozaki_layout(g.m, g.n, g.k, digits, bits);
   char* base = static_cast<char*>(scratch);
@@ -694,8 +737,8 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scr
   uint32_t* fa = reinterpret_cast<uint32_t*>(base + L.off_fa);
   uint32_t* fb = reinterpret_cast<uint32_t*>(base + L.off_fb);
   int* err = reinterpret_cast<int*>(base + L.off_err);
-  __nv_bfloat16* DA = reinterpret_cast<__nv_bfloat16*>(base + L.off_DA);
-  __nv_bfloat16* DB = reinterpret_cast<__nv_bfloat16*>(base + L.off_DB);
+  uint16_t* DA = reinterpret_cast<uint16_t*>(base + L.off_DA);
+  uint16_t* DB = reinterpret_cast<uint16_t*>(base + L.off_DB);
   int32_t* Cg = reinterpret_cast<int32_t*>(base + L.off_C);
   cudaError_t e;
   const int sms = device_sm_count();
@@ -729,10 +772,7 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scr
     unsigned bb = (unsigned)std::min<int64_t>((wb + 255) / 256, (int64_t)sms * 8);
     ozaki_scale_kernel<<<bb, 256, 0, sb>>>(g.n, g.k, g.B, g.sbj, g.sbl, F, fb);
     dim3 gb((unsigned)(L.k_pad / 64), (unsigned)(L.n_pad / 8));
-    if (L.b == 7)
-      ozaki_split_kernel<7><<<gb, blk, 0, sb>>>(g.n, g.k, L.n_pad, L.k_pad, plane_b, g.B, g.sbj, g.sbl, F, L.s, DB);
-    else
-      ozaki_split_kernel<8><<<gb, blk, 0, sb>>>(g.n, g.k, L.n_pad, L.k_pad, plane_b, g.B, g.sbj, g.sbl, F, L.s, DB);
+    launch_split(L.b, gb, blk, sb, g.n, g.k, L.n_pad, L.k_pad, plane_b, g.B, g.sbj, g.sbl, F, L.s, DB);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     if (ov) {
       if ((e = cudaEventRecord(ov->b_done, sb)) != cudaSuccess) return e;
@@ -750,12 +790,8 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scr
     if (rows > 0) ozaki_scale_kernel<<<ba, 256, 0, sa>>>(rows, g.k, g.A + r0 * g.sai, g.sai, g.sal, S + r0, fa + r0);
     dim3 ga((unsigned)(L.k_pad / 64), (unsigned)((r1 - r0) / 8));
     const q128* Ab = g.A + r0 * g.sai;
-    if (L.b == 7)
-      ozaki_split_kernel<7><<<ga, blk, 0, sa>>>(rows, g.k, r1 - r0, L.k_pad, plane_a, Ab, g.sai, g.sal, S + r0,
-                                                L.s, DA + r0 * L.k_pad);
-    else
-      ozaki_split_kernel<8><<<ga, blk, 0, sa>>>(rows, g.k, r1 - r0, L.k_pad, plane_a, Ab, g.sai, g.sal, S + r0,
-                                                L.s, DA + r0 * L.k_pad);
+    launch_split(L.b, ga, blk, sa, rows, g.k, r1 - r0, L.k_pad, plane_a, Ab, g.sai, g.sal, S + r0, L.s,
+                 DA + r0 * L.k_pad);
     if ((ee = cudaGetLastError()) != cudaSuccess) return ee;
     if (banded) {
       if ((ee = cudaEventRecord(ov->a_done, sa)) != cudaSuccess) return ee;
@@ -768,8 +804,8 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scr
   // the bands are whole waves of tiles (one tile per SM), at most 8, and
   // each band's digit products start as soon as its rows of op(A) are cut.
   CUtensorMap tmA, tmB;
-  if (!make_map(&tmA, DA, (int64_t)L.s * L.m_pad, L.k_pad, kBM) ||
-      !make_map(&tmB, DB, (int64_t)L.s * L.n_pad, L.k_pad, kBN))
+  if (!make_map(&tmA, DA, (int64_t)L.s * L.m_pad, L.k_pad, kBM, L.b == 9) ||
+      !make_map(&tmB, DB, (int64_t)L.s * L.n_pad, L.k_pad, kBN, L.b == 9))
     return cudaErrorInvalidValue;
   static bool attr_set[64] = {false};
   int dev = 0;
@@ -817,11 +853,8 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scr
     Fb.fa = fa + i0;
     Fb.A = g.A + i0 * g.sai;
     Fb.Cout = g.C + i0 * g.sci;
+    launch_fold(L.b, st, Fb);
     dim3 fblk(32, 8), fgrid((unsigned)((g.n + 31) / 32), (unsigned)((Fb.m + 7) / 8));
-    if (L.b == 7)
-      ozaki_fold_kernel<7><<<fgrid, fblk, 0, st>>>(Fb);
-    else
-      ozaki_fold_kernel<8><<<fgrid, fblk, 0, st>>>(Fb);
     if ((ee = cudaGetLastError()) != cudaSuccess) return ee;
     ozaki_special_kernel<<<fgrid, fblk, 0, st>>>(Fb);
     if ((ee = cudaGetLastError()) != cudaSuccess) return ee;
@@ -845,6 +878,7 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scr
       P.tiles_n = tiles_n;
       P.tile_begin = t0;
       P.tile_end = t1;
+      P.idesc = L.b == 9 ? kIdescF16 : kIdescBf16;
       P.G = L.G;
       P.m_pad = (int)L.m_pad;
       P.n_pad = (int)L.n_pad;

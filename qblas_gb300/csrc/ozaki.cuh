@@ -24,13 +24,19 @@
 
 namespace qb {
 
-// Digit width b: 7 (|d| <= 64, fp32-exact over k-chunks of 4096) or 8
-// (|d| <= 128, exact over k-chunks of 1024); both are exact in bf16.
+// Digit width b: 7 (|d| <= 64, fp32-exact over k-chunks of 4096), 8
+// (|d| <= 128, chunks of 1024), both exact in bf16; or 9 (|d| <= 256,
+// chunks of 256), exact in fp16 (11-bit significand), whose 9-bit digits
+// need fewer digit pairs for the same bits.
 constexpr int kOzakiMaxDigits = 22;  // V < 2^(b*s - 1) <= 2^175 (192-bit split)
 
 // Largest digit count whose fold stays inside 192 bits:
 // 31 (int32 diagonal) + b*(s-1) + 1 (sign) <= 191.
-QB_HD int ozaki_max_digits(int b) { return b == 7 ? 22 : 20; }
+template <int B>
+struct OzakiMaxDigits {
+  static constexpr int value = B == 7 ? 22 : (B == 8 ? 20 : 18);
+};
+QB_HD int ozaki_max_digits(int b) { return b == 7 ? 22 : (b == 8 ? 20 : 18); }
 
 // Largest digit count for inner dimension k.  The fold value is
 // sum_g C_g 2^(b(G-g)) with |C_g| <= (g+1) k 2^(2(b-1)), so
@@ -130,7 +136,7 @@ QB_HD int ozaki_digit_step(uint64_t v0, uint64_t v1, uint64_t v2, int j, int s, 
 // Requires 1 <= s <= ozaki_max_digits(B).
 template <int B, typename Emit>
 QB_HD void ozaki_digits_emit(q128 a, int S, int s, Emit emit) {
-  constexpr int kMax = B == 7 ? 22 : 20;
+  constexpr int kMax = OzakiMaxDigits<B>::value;
   uint64_t v0, v1, v2;
   bool neg;
   ozaki_scaled<B>(a, S, s, v0, v1, v2, neg);
@@ -148,7 +154,7 @@ QB_HD void ozaki_digits_emit(q128 a, int S, int s, Emit emit) {
 // emit(t, d_t(a), d_t(b)).
 template <int B, typename Emit2>
 QB_HD void ozaki_digits_emit2(q128 a, q128 b, int S, int s, Emit2 emit) {
-  constexpr int kMax = B == 7 ? 22 : 20;
+  constexpr int kMax = OzakiMaxDigits<B>::value;
   uint64_t a0, a1, a2, b0, b1, b2;
   bool na, nb;
   ozaki_scaled<B>(a, S, s, a0, a1, a2, na);
@@ -164,12 +170,14 @@ QB_HD void ozaki_digits_emit2(q128 a, q128 b, int S, int s, Emit2 emit) {
   }
 }
 
-// The digits into an array: digits[t] for t < s (b = 7 or 8).
+// The digits into an array: digits[t] for t < s (b = 7, 8 or 9).
 QB_HD void ozaki_digits(q128 a, int S, int s, int b, int* digits) {
   if (b == 7)
     ozaki_digits_emit<7>(a, S, s, [&](int t, int d) { digits[t] = d; });
-  else
+  else if (b == 8)
     ozaki_digits_emit<8>(a, S, s, [&](int t, int d) { digits[t] = d; });
+  else
+    ozaki_digits_emit<9>(a, S, s, [&](int t, int d) { digits[t] = d; });
 }
 
 // 192-bit two's complement accumulator for the fold (Horner in base 2^b).
@@ -202,8 +210,10 @@ QB_HD void fold_step_t(fold192& f, int64_t v) {
 QB_HD void fold_step(fold192& f, int64_t v, int b) {
   if (b == 7)
     fold_step_t<7>(f, v);
-  else
+  else if (b == 8)
     fold_step_t<8>(f, v);
+  else
+    fold_step_t<9>(f, v);
 }
 
 // value = f * 2^e rounded to binary128

@@ -77,7 +77,7 @@ def test_ozaki_one_tile_bit_exact(ozaki, O, sq):
     assert Q.same_bits(got[idx], exp).all()
 
 
-@pytest.mark.parametrize("s,b", [(2, 8), (7, 8), (18, 8), (20, 8), (7, 7), (20, 7)])
+@pytest.mark.parametrize("s,b", [(2, 8), (7, 8), (18, 8), (20, 8), (7, 7), (20, 7), (2, 9), (15, 9), (18, 9)])
 def test_ozaki_bit_exact_vs_emulation(ozaki, O, sq, s, b):
     rng = G.rng_for(10 + s + 100 * b)
     cases = [("R", "N", "N", 1, 1, 1), ("R", "N", "N", 5, 7, 9), ("R", "T", "N", 130, 257, 70),
@@ -87,10 +87,10 @@ def test_ozaki_bit_exact_vs_emulation(ozaki, O, sq, s, b):
         assert Q.same_bits(got[idx], exp).all(), (layout, ta, tb, m, n, k, s, b)
 
 
-@pytest.mark.parametrize("b,k", [(7, 4096 + 64 + 5), (8, 3 * 1024 + 64 + 5)])
+@pytest.mark.parametrize("b,k", [(7, 4096 + 64 + 5), (8, 3 * 1024 + 64 + 5), (9, 5 * 256 + 64 + 5)])
 def test_ozaki_several_exact_chunks(ozaki, O, sq, b, k):
-    """k above the fp32-exact chunk (4096 for 7-bit, 1024 for 8-bit digits):
-    chunk sums are read out of tensor memory and added in int32."""
+    """k above the fp32-exact chunk (4096 for 7-bit, 1024 for 8-bit, 256 for
+    9-bit digits): chunk sums are read out of tensor memory and added in int32."""
     rng = G.rng_for(2 + b)
     got, idx, exp, _ = run_case(O, sq, rng, "R", "N", "N", 128, 256, k, 6, G.spread_uniform, 1.0, 0.0, b)
     assert Q.same_bits(got[idx], exp).all()
@@ -105,12 +105,12 @@ def test_ozaki_mixed_magnitudes(ozaki, O, sq):
         q[: n // 7] = 0
         return q
 
-    for b, s in ((8, 18), (7, 20)):
+    for b, s in ((8, 18), (7, 20), (9, 16)):
         got, idx, exp, _ = run_case(O, sq, rng, "R", "N", "N", 67, 301, 45, s, gen, 1.0, 0.0, b)
         assert Q.same_bits(got[idx], exp).all(), b
 
 
-@pytest.mark.parametrize("size,s,b", [(512, 18, 8), (512, 20, 7), (4096, 17, 8)])
+@pytest.mark.parametrize("size,s,b", [(512, 18, 8), (512, 20, 7), (4096, 17, 8), (4096, 15, 9)])
 def test_ozaki_accuracy_spread(ozaki, O, torch_cuda, size, s, b):
     """size^3 on e-uniform-[-20, 20] data (the 4096^3 benchmark workload at
     its digit count): every sampled entry is within 1 ulp of the exact sum."""
@@ -159,6 +159,6 @@ def test_ozaki_reference_c_interface(ozaki, O, sq):
     m, n, k = 40, 50, 60
     A, B, C = G.spread_uniform(rng, m * k), G.spread_uniform(rng, k * n), G.uniform_full(rng, m * n)
     got = C.copy()
-    api.qgemm("R", "N", "N", m, n, k, 2.0, A, k, B, n, 0.5, got, n)  # library defaults: 18 digits of 8 bits
-    sums = E.gemm_sum(sq, m, n, k, A, k, 1, B, n, 1, 18, 8)
+    api.qgemm("R", "N", "N", m, n, k, 2.0, A, k, B, n, 0.5, got, n)  # library defaults: 16 digits of 9 bits
+    sums = E.gemm_sum(sq, m, n, k, A, k, 1, B, n, 1, 16, 9)
     assert Q.same_bits(got, epilogue(O, Q.scalar(2.0), sums, Q.scalar(0.5), C)).all()

@@ -41,7 +41,8 @@ def digits_py(w, S, s, b):
     return [-x for x in d] if neg else d
 
 
-@pytest.mark.parametrize("b,s", [(7, 2), (7, 13), (7, 20), (7, 22), (8, 2), (8, 11), (8, 17), (8, 20)])
+@pytest.mark.parametrize("b,s", [(7, 2), (7, 13), (7, 20), (7, 22), (8, 2), (8, 11), (8, 17), (8, 20),
+                                 (9, 2), (9, 15), (9, 18)])
 def test_digits_match_integer_restatement(sq, b, s):
     rng = G.rng_for(100 * b + s)
     X = np.concatenate([G.spread_uniform(rng, 160), V.finite(rng, 40, -16382, -16300), V.subnormal(rng, 40),
@@ -58,7 +59,7 @@ def test_digits_match_integer_restatement(sq, b, s):
             assert abs(x - rec) < Fraction(2) ** (int(S[r]) - b * s + 1)
 
 
-@pytest.mark.parametrize("b", [7, 8])
+@pytest.mark.parametrize("b", [7, 8, 9])
 def test_fold_matches_integer_restatement(sq, b):
     rng = np.random.default_rng(b)
     s, m, n = 17, 5, 6
