@@ -125,6 +125,17 @@ def to_host(t) -> np.ndarray:
     return np.ascontiguousarray(t.cpu().numpy()).view(np.uint64)
 
 
+def ozaki_launches(k, s, b):
+    """Kernels per device-pointer Ozaki qgemm call: fill, scale and split for
+    each operand, one digit-product launch per k pass, fold, special values.
+    A k pass holds as many fp32-exact k-chunks as an int32 diagonal sum of s
+    pairs of chunk sums (each < 2^24) allows."""
+    chunk_kb = (1 << (24 - 2 * (b - 1))) // 64
+    kbp = max(1, (2 ** 31 - 1) // (s << 24)) * chunk_kb
+    npass = -(-(-(-k // 64)) // kbp)
+    return 6 + npass + 2
+
+
 def max_over_ranks(dist, x: float) -> float:
     """The largest x over all ranks (x itself without a process group).  The
     reduction runs on the GPU under NCCL and on the CPU under gloo."""
@@ -256,7 +267,7 @@ class Qdot:
 # DRAM bytes (read + write) per launch of the dominant kernel, from one ncu
 # capture of the same workload (profiles/ holds the summaries and commands).
 NCU_TRAFFIC = {
-    "qgemm4096": (29.31e9 + 1.18e9, "profiles/ozaki_mma_kernel_4096_traffic.md"),
+    "qgemm4096": (2 * (9.84e9 + 1.01e9), "profiles/ozaki_mma_kernel_4096_traffic.md"),  # 15 x 9 bit, 2 passes
     "qdot26": (2.147608e9 + 4.091e6, "profiles/qdot_partial_kernel_n2p26.md"),
     "qgemv8192": (1.074185e9 + 9.166e6, "profiles/qgemv_rows_kernel_8192.md"),
 }
@@ -503,7 +514,7 @@ def main():
                     "algorithmic": "2*m*n*k*pairs bf16 flops, pairs = s(s+1)/2 digit products",
                     "phases_ms": {"scale_split": round(ph[0] / tot_calls, 4), "digit_products": round(mma_ms, 4),
                                   "fold": round(ph[2] / tot_calls, 4)}}
-            launches = (7 + 1) * args.steps
+            launches = ozaki_launches(size, slices, bits) * args.steps
             dtype = "bf16 digit products (fp32 accumulate, int32/192-bit fold)"
         else:
             roof = {"bound": "int", "achieved": round(W.flops() / (ms_step * 1e-3) / 1e9, 3), "peak": None,
