@@ -96,6 +96,17 @@ def test_ozaki_several_exact_chunks(ozaki, O, sq, b, k):
     assert Q.same_bits(got[idx], exp).all()
 
 
+@pytest.mark.parametrize("s,b,k", [(15, 9, 2048 + 300), (18, 9, 1792 + 77), (17, 8, 7168 + 129), (20, 7, 6 * 4096 + 65)])
+def test_ozaki_several_k_passes(ozaki, O, sq, s, b, k):
+    """k above one pass (the int32 diagonal sums hold (2^31 - 1) / (s 2^24)
+    exact chunks): each pass writes its own diagonal planes and the fold adds
+    them; bit-exact with the emulation."""
+    rng = G.rng_for(20 + s + b)
+    for layout, ta, tb, m, n in (("R", "N", "N", 24, 40), ("C", "T", "N", 17, 33)):
+        got, idx, exp, _ = run_case(O, sq, rng, layout, ta, tb, m, n, k, s, G.spread_uniform, 1.0, 0.5, b)
+        assert Q.same_bits(got[idx], exp).all(), (layout, s, b, k)
+
+
 def test_ozaki_mixed_magnitudes(ozaki, O, sq):
     """Zero rows, subnormal and huge entries go through the same split."""
     rng = G.rng_for(3)
