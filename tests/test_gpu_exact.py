@@ -115,6 +115,36 @@ def test_qgemm_softfloat_any_condition(qlib, O):
     assert Q.same_bits(got, epilogue(O, alpha, R, beta, C0)).all()
 
 
+@pytest.mark.parametrize("layout,ta,tb", [("C", "N", "N"), ("R", "T", "T"), ("C", "T", "N")])
+def test_qgemm_softfloat_any_condition_layouts(qlib, O, layout, ta, tb):
+    """The in-tile exact recomputation with every stride pattern of op(A), op(B), C."""
+    m = n = 24
+    k = 1536
+    X, Y = O.gendot_batch(k, [1e45, 1e55, 1e20] * (m // 3), np.arange(m, dtype=np.uint64) + 300)
+    Xr = X.reshape(m, k, 2)                       # op(A)(i, :) = x^(i)
+    Yr = Y.reshape(n, k, 2)                       # op(B)(:, j) = y^(j)
+    col = layout == "C"
+    # store op(A) (m x k) and op(B) (k x n) in the requested layout and transposition
+    opA = Xr
+    opB = np.ascontiguousarray(Yr.transpose(1, 0, 2))
+    stA = opA.transpose(1, 0, 2) if ta == "T" else opA   # the stored matrix before layout
+    stB = opB.transpose(1, 0, 2) if tb == "T" else opB
+    if col:
+        stA, stB = stA.transpose(1, 0, 2), stB.transpose(1, 0, 2)
+    A = np.ascontiguousarray(stA).reshape(-1, 2)
+    B = np.ascontiguousarray(stB).reshape(-1, 2)
+    lda, ldb = stA.shape[1], stB.shape[1]
+    C0 = G.uniform_full(G.rng_for(97), m * n)
+    got = C0.copy()
+    api.set_method(0)
+    api.gemm(layout, ta, tb, m, n, k, Q.scalar(1.0), A, lda, B, ldb, Q.scalar(0.25), got, n if not col else m)
+    rows, cols = np.meshgrid(np.arange(m), np.arange(n), indexing="ij")
+    R, _, _ = O.exact_gemm(k, Xr.reshape(-1, 2), k, 1, np.ascontiguousarray(opB).reshape(-1, 2), n, 1,
+                           rows.ravel(), cols.ravel())
+    idx = rows.ravel() * n + cols.ravel() if not col else cols.ravel() * m + rows.ravel()
+    assert Q.same_bits(got[idx], epilogue(O, Q.scalar(1.0), R, Q.scalar(0.25), C0[idx])).all()
+
+
 def test_batched_any_condition(qlib, O, torch_cuda):
     torch = torch_cuda
     ar = Arena(torch)

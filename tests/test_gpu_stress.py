@@ -5,8 +5,8 @@ prescribed condition, Ogita-Rump-Oishi), against the exact oracle.
 * qgemm, m = n = 2048, k = 8192: row i of A and column i of B form a GenDot
   pair whose condition cycles through the four values, so the diagonal
   C(i, i) carries the prescribed condition; 2048 off-diagonal entries are
-  checked as well.  Soft-float, then Ozaki with 17 and 20 digits of 8 bits
-  and 22 digits of 7 bits.
+  checked as well.  Soft-float, then Ozaki with 15 digits of 9 bits, 17 and
+  20 of 8 bits and 22 of 7 bits.
 
 Bounds asserted (u_q = 2^-113, ulps of the exact result):
   * soft-float: correctly rounded (<= 0.5 ulp) at every condition (the
@@ -124,7 +124,7 @@ def test_qgemm_gendot_softfloat(qlib, O, gendot_matrices):
     assert ulp.max() <= 0.5
 
 
-@pytest.mark.parametrize("s,b", [(17, 8), (20, 8), (22, 7)])
+@pytest.mark.parametrize("s,b", [(15, 9), (17, 8), (20, 8), (22, 7)])
 def test_qgemm_gendot_ozaki(qlib, O, gendot_matrices, s, b):
     M = gendot_matrices
     api.set_method(2)
