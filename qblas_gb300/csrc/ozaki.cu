@@ -3,23 +3,24 @@
 // Replaces the reference's soft-float GEMM loops
 // (include/quadblas/algorithms/level3.hpp:17-336) by an error-free integer
 // splitting (ozaki.cuh): each row of op(A) and column of op(B) is cut into s
-// signed 8-bit (or 7-bit) digits stored as bf16, every digit pair (t, u) is
-// an exact bf16 x bf16 -> fp32 GEMM on tcgen05.mma kind::f16 (sums <= 2^24
-// stay exact; k is processed in chunks of 1024 (4096 for 7-bit digits)),
-// the pairs of one diagonal
-// g = t + u are summed exactly in int32, and a fold kernel combines the
-// diagonals into a 192-bit integer per output that is rounded once to
-// binary128 and passed through the reference epilogue
-// C = fma(alpha, sum, beta * C) (level3.hpp:107).
+// balanced digits of b bits (b = 9: stored as fp16; b = 8 or 7: as bf16),
+// every digit pair (t, u) with t + u < s is an exact 16-bit-float ->
+// fp32 GEMM on tcgen05.mma kind::f16 (integer sums below 2^24 stay exact,
+// so k is read out of tensor memory in chunks of 256, 1024 or 4096), the
+// pairs of one diagonal g = t + u are summed exactly in int32 (in k passes
+// when a pass would overflow), and a fold kernel combines the diagonals into
+// a 192-bit integer per output that is rounded once to binary128 and passed
+// through the reference epilogue C = fma(alpha, sum, beta * C)
+// (level3.hpp:107).
 //
 // tcgen05 kind::i8 does not exist on sm_103a, so integer digits travel as
-// bf16 (|d| <= 128 is exact) with fp32 accumulation in tensor memory.
+// 16-bit floats: bf16 holds every integer up to 256 exactly, fp16 up to 2048.
 //
 // Kernels:
 //   ozaki_scale_kernel  : S_i = max_l (exponent(x_il) + 1) per row of a
 //                         strided view (A, or B^T), plus NaN/inf flags
 //   ozaki_split_kernel  : digits of every element, written digit-major and
-//                         K-major: D[t][row][l] (bf16), zero padded
+//                         K-major: D[t][row][l], zero padded
 //   ozaki_mma_kernel    : persistent, warp-specialised: warp 0 issues TMA
 //                         loads (128B-swizzled 64-wide K slices of A_t and
 //                         B_u) into a 4-stage shared-memory ring, warp 1
@@ -32,10 +33,10 @@
 //                         the kernel records an error, drains its own
 //                         copies and MMAs, frees tensor memory and exits.
 //   ozaki_fold_kernel   : Horner fold of C_0..C_G (and k passes) per output,
-//                         one rounding, reference epilogue; rows/columns that
-//                         hold NaN or inf are computed by a direct wide-
-//                         accumulator dot instead, so specials keep IEEE
-//                         semantics.
+//                         one rounding, reference epilogue
+//   ozaki_special_kernel: outputs whose row or column holds NaN or inf, by a
+//                         direct wide-accumulator dot, so specials keep IEEE
+//                         semantics
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -90,14 +91,13 @@ __global__ void ozaki_fill_kernel(int64_t n, int* __restrict__ S, uint32_t* __re
   }
 }
 
-// Digits of the (rows_pad x cols_pad) zero-padded view into
-// D[t * rows_pad * cols_pad + r * cols_pad + c] (bf16).  Block (32, 8):
-// x along columns (coalesced digit stores), y along rows; each digit is
+// Digits of the (rows_pad x cols_pad) zero-padded view: digit t of element
+// (r, c) goes to D[t * plane + r * cols_pad + c]; rows in [rows, rows_pad)
+// and columns in [cols, cols_pad) get zero digits.  Block (32, 8): x along
+// columns (coalesced digit stores), y along rows.  A thread cuts two
+// neighbouring columns (c, c+1) of a row and stores each digit pair as one
+// 32-bit word (cols_pad is a multiple of 64, so c is even); each digit is
 // stored as soon as it is extracted.
-// Two neighbouring columns (c, c+1) of a row per thread: one packed
-// bf16x2 store per digit (cols_pad is a multiple of 64, so c is even).
-// Digit t of row r goes to D[t * plane + r * cols_pad + c]; rows in
-// [rows, rows_pad) get zero digits.
 // Digits are stored as bf16 (b = 7, 8) or fp16 (b = 9), two per 32-bit word.
 template <int B>
 __device__ __forceinline__ uint32_t pack_digits(int d0, int d1) {
@@ -133,7 +133,7 @@ __global__ void __launch_bounds__(256)
 // ---------------------------------------------------------------------------
 // tcgen05 digit GEMM
 // ---------------------------------------------------------------------------
-constexpr int kBM = 128, kBN = 256, kBK = 64;  // tile; kBK bf16 = 128 bytes per row
+constexpr int kBM = 128, kBN = 256, kBK = 64;  // tile; kBK 16-bit digits = 128 bytes per row
 constexpr int kStages = 4;
 constexpr int kStageA = kBM * kBK * 2;          // 16 KiB
 constexpr int kStageB = kBN * kBK * 2;          // 32 KiB
