@@ -199,6 +199,14 @@ int quadblas_get_ozaki_digit_bits(void);
  * and out4[3] the tensor flops of those calls (2*m*n*k*pairs). */
 int quadblas_profile_enable(int on);
 int quadblas_profile_read(double *out4, int *calls);
+/* Frees the staging buffers that host-pointer calls keep on the current
+ * device (they are allocated again, grown to need, by the next call). */
+int quadblas_release_buffers(void);
+/* Testing aid for callers' failure handling: the next `count` device
+ * allocations the library attempts fail as if the device were out of memory
+ * (the call returns QBLAS_ERR_NO_MEMORY and leaves its outputs untouched);
+ * 0 clears it.  Nothing is allocated for a failed attempt. */
+int quadblas_debug_fail_allocations(int count);
 /* Status of the calling thread's last call (part 1 calls record it too). */
 int quadblas_last_error(void);
 const char *quadblas_error_string(int code);

@@ -57,6 +57,8 @@ _SIGS = {
     "quadblas_get_ozaki_digit_bits": (ci, []),
     "quadblas_profile_enable": (ci, [ci]),
     "quadblas_profile_read": (ci, [vp, vp]),
+    "quadblas_release_buffers": (ci, []),
+    "quadblas_debug_fail_allocations": (ci, [ci]),
     "quadblas_last_error": (ci, []),
     "quadblas_error_string": (ctypes.c_char_p, [ci]),
 }

@@ -141,6 +141,14 @@ def set_ozaki_digit_bits(b: int) -> None:
     check(load().quadblas_set_ozaki_digit_bits(b))
 
 
+def release_buffers() -> None:
+    check(load().quadblas_release_buffers())
+
+
+def debug_fail_allocations(count: int) -> None:
+    check(load().quadblas_debug_fail_allocations(count))
+
+
 # ---- batched problems (one persistent launch) -------------------------------
 OP_GEMM, OP_GEMV, OP_DOT = 0, 1, 2
 

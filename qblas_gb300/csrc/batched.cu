@@ -567,10 +567,10 @@ static int plan_build(const qblas_problem* problems, int64_t count, int64_t grai
   p->nparts = nparts;
   p->grain = grain;
   int rc = kOk;
-  if ((rc = cuda_rc(cudaMalloc(&p->d_probs, sizeof(BProb) * std::max<int64_t>(1, count)))) ||
-      (rc = cuda_rc(cudaMalloc(&p->d_items, sizeof(BItem) * std::max<int64_t>(1, p->nitems)))) ||
-      (rc = cuda_rc(cudaMalloc(&p->d_counters, sizeof(int) * (1 + ngroups)))) ||
-      (rc = cuda_rc(cudaMalloc(&p->d_partials, sizeof(wacc) * std::max<int64_t>(1, nparts))))) {
+  if ((rc = cuda_rc(dev_malloc((void**)&p->d_probs, sizeof(BProb) * std::max<int64_t>(1, count)))) ||
+      (rc = cuda_rc(dev_malloc((void**)&p->d_items, sizeof(BItem) * std::max<int64_t>(1, p->nitems)))) ||
+      (rc = cuda_rc(dev_malloc((void**)&p->d_counters, sizeof(int) * (1 + ngroups)))) ||
+      (rc = cuda_rc(dev_malloc((void**)&p->d_partials, sizeof(wacc) * std::max<int64_t>(1, nparts))))) {
     plan_free(p);
     return rc;
   }
@@ -699,7 +699,7 @@ static int run_autotune(int dev, int64_t* best_out) {
     if (z.op == QBLAS_OP_DOT) total += 2 * z.n + 1;
   }
   uint64_t* buf = nullptr;
-  if (cudaMalloc(&buf, (size_t)total * 16) != cudaSuccess) {
+  if (dev_malloc((void**)&buf, (size_t)total * 16) != cudaSuccess) {
     cudaGetLastError();
     return kErrNoMemory;
   }

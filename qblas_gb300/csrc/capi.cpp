@@ -40,6 +40,15 @@ int fail(int code) {
   return code;
 }
 
+std::atomic<int> g_fail_allocs{0};  // injected allocation failures still to happen
+
+bool take_injected_failure() {
+  int v = g_fail_allocs.load();
+  while (v > 0)
+    if (g_fail_allocs.compare_exchange_weak(v, v - 1)) return true;
+  return false;
+}
+
 int cuda_status(cudaError_t e) {
   if (e == cudaSuccess) return qb::kOk;
   if (e == cudaErrorMemoryAllocation) return qb::kErrNoMemory;
@@ -116,7 +125,7 @@ int ensure_slot(DevState& st, Slot s, size_t bytes) {
     st.cap[s] = 0;
   }
   size_t want = bytes + bytes / 8;
-  cudaError_t e = cudaMalloc(&st.buf[s], want);
+  cudaError_t e = qb::dev_malloc(&st.buf[s], want);
   if (e != cudaSuccess) {
     cudaGetLastError();
     st.buf[s] = nullptr;
@@ -277,7 +286,7 @@ int dev_dot(int64_t n, const void* dx, int64_t incx, const void* dy, int64_t inc
   size_t sb = qb::dot_scratch_bytes(n);
   void* scratch = scratch_or_null;
   if (!scratch && n > 0) {
-    cudaError_t e = cudaMallocAsync(&scratch, sb, s);
+    cudaError_t e = qb::dev_malloc_async(&scratch, sb, s);
     if (e != cudaSuccess) {
       cudaGetLastError();
       return cuda_status(e);
@@ -298,7 +307,7 @@ int dev_gemv(const GemvPlan& p0, const void* alpha, const void* dA, const void* 
   size_t sb = qb::gemv_scratch_bytes(p.m, p.n, p.A);
   void* scratch = scratch_or_null;
   if (!scratch && sb) {
-    cudaError_t e = cudaMallocAsync(&scratch, sb, s);
+    cudaError_t e = qb::dev_malloc_async(&scratch, sb, s);
     if (e != cudaSuccess) {
       cudaGetLastError();
       return cuda_status(e);
@@ -365,7 +374,7 @@ int dev_gemm(GemmPlan p, int method, const void* alpha, const void* dA, const vo
   size_t sb = gemm_scratch_bytes(p, method);
   void* scratch = scratch_or_null;
   if (!scratch) {
-    cudaError_t e = cudaMallocAsync(&scratch, sb, s);
+    cudaError_t e = qb::dev_malloc_async(&scratch, sb, s);
     if (e != cudaSuccess) {
       cudaGetLastError();
       return cuda_status(e);
@@ -577,6 +586,23 @@ int host_gemm(char layout, char transa, char transb, int64_t m, int64_t n, int64
 
 }  // namespace
 
+namespace qb {
+cudaError_t dev_malloc(void** p, size_t bytes) {
+  if (take_injected_failure()) {
+    *p = nullptr;
+    return cudaErrorMemoryAllocation;
+  }
+  return cudaMalloc(p, bytes);
+}
+cudaError_t dev_malloc_async(void** p, size_t bytes, cudaStream_t s) {
+  if (take_injected_failure()) {
+    *p = nullptr;
+    return cudaErrorMemoryAllocation;
+  }
+  return cudaMallocAsync(p, bytes, s);
+}
+}  // namespace qb
+
 #define QBLAS_EXPORT extern "C" __attribute__((visibility("default")))
 
 // ===========================================================================
@@ -719,6 +745,30 @@ QBLAS_EXPORT int quadblas_set_method(int method) {
   return fail(qb::kOk);
 }
 QBLAS_EXPORT int quadblas_get_method(void) { return g_method.load(); }
+QBLAS_EXPORT int quadblas_release_buffers(void) {
+  int dev = 0;
+  int rc = current_device(dev);
+  if (rc) return fail(rc);
+  DevState& st = g_dev[dev];
+  std::lock_guard<std::mutex> l(st.mu);
+  if (st.stream) cudaStreamSynchronize(st.stream);
+  for (int i = 0; i < kNumSides; ++i)
+    if (st.side[i]) cudaStreamSynchronize(st.side[i]);
+  for (int i = 0; i < kNumSlots; ++i) {
+    if (st.buf[i]) cudaFree(st.buf[i]);
+    st.buf[i] = nullptr;
+    st.cap[i] = 0;
+  }
+  cudaGetLastError();
+  return fail(qb::kOk);
+}
+
+QBLAS_EXPORT int quadblas_debug_fail_allocations(int count) {
+  if (count < 0) return fail(qb::kErrInvalidValue);
+  g_fail_allocs.store(count);
+  return fail(qb::kOk);
+}
+
 QBLAS_EXPORT int quadblas_set_ozaki_slices(int slices) {
   if (slices < 0 || slices == 1 || slices > 22) return fail(qb::kErrInvalidValue);
   g_slices.store(slices);

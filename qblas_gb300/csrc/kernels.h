@@ -101,6 +101,11 @@ void ozaki_profile_enable(bool on);
 int ozaki_profile_read(double* out4, int* calls);
 
 // Multiprocessor count of the current device (cached).
+// Every device allocation of the library goes through these: they fail
+// with cudaErrorMemoryAllocation, allocating nothing, while an injected
+// failure count (quadblas_debug_fail_allocations) is pending.
+cudaError_t dev_malloc(void** p, size_t bytes);
+cudaError_t dev_malloc_async(void** p, size_t bytes, cudaStream_t s);
 int device_sm_count();
 
 // Blocks of `kernel` (with `threads` threads and `smem` dynamic shared
