@@ -515,7 +515,8 @@ def main():
                     "phases_ms": {"scale_split": round(ph[0] / tot_calls, 4), "digit_products": round(mma_ms, 4),
                                   "fold": round(ph[2] / tot_calls, 4)}}
             launches = ozaki_launches(size, slices, bits) * args.steps
-            dtype = "bf16 digit products (fp32 accumulate, int32/192-bit fold)"
+            dtype = (f"{'fp16' if bits == 9 else 'bf16'} digit products of {bits}-bit digits "
+                     "(fp32 accumulate, int32/192-bit fold)")
         else:
             roof = {"bound": "int", "achieved": round(W.flops() / (ms_step * 1e-3) / 1e9, 3), "peak": None,
                     "unit": "quad GFLOP/s", "frac": None, "traffic": None,
