@@ -601,7 +601,7 @@ def main():
         ms_step = ms / args.steps
         value = whole_job_rate(W.bytes(), world, ms_step * 1e-3) / 1e9
         metric, unit = "qgemv binary128 GB/s (8192^2 row-major)", "GB/s"
-        launches = 3 * args.steps  # partial/row kernel, finalize or unpack, exact pass (returns at once)
+        launches = 4 * args.steps  # x unpack, thread-per-row kernel, chunk merge, exact pass (returns at once)
         roof = hbm_roofline(pk, pk_src, W.bytes(), ms_step, wl)
         e2e, dtype = None, "u32 (soft-float integer limbs)"
         cfg = {"workload": "qgemv 8192x8192 row-major alpha=1 beta=0, wide-exponent values",
@@ -613,7 +613,7 @@ def main():
         ms_step = ms / args.steps
         value = whole_job_rate(W.bytes(), world, ms_step * 1e-3) / 1e9
         metric, unit = "qdot binary128 GB/s (n=2^26)", "GB/s"
-        launches = 3 * args.steps  # partial/row kernel, finalize or unpack, exact pass (returns at once)
+        launches = 3 * args.steps  # partial kernel, finalize, exact pass (returns at once)
         roof = hbm_roofline(pk, pk_src, W.bytes(), ms_step, wl)
         e2e, dtype = None, "u32 (soft-float integer limbs)"
         cfg = {"workload": "qdot n=2^26 wide-exponent values with cancelling pairs",

@@ -10,16 +10,18 @@
 // x is unpacked once per call into scratch (significand at bit 127,
 // exponent, sign and class), since every element of x is used m times.
 // Two memory layouts of op(A):
-//  * rows contiguous (row-major, or column-major with trans): a row is
-//    shared by 1, 2, 4 or 8 warps of a 256-thread block (more warps for
+//  * rows contiguous (row-major, or column-major with trans) and m < 4096:
+//    a row is shared by 1, 2, 4 or 8 warps of a 256-thread block (more warps for
 //    longer rows); lanes read consecutive 16-byte elements (512 B per warp
 //    per step) and the warps' accumulators are merged in shared memory in a
 //    fixed order.  One block per 8/wpr rows keeps the grid fine-grained.
-//  * columns contiguous (column-major, or row-major with trans): one thread
-//    per row, so a warp reads 32 consecutive elements of a column; the
-//    columns are split into chunks over blockIdx.y to fill the GPU, each
-//    (row, chunk) leaves a partial accumulator in scratch, and a second
-//    kernel merges the chunks of each row in order and applies the epilogue.
+//  * one thread per row (columns contiguous, i.e. column-major or row-major
+//    with trans, where a warp reads 32 consecutive elements of a column; and
+//    rows contiguous with m >= 4096, where each lane reads its row through
+//    L1): all lanes share each x_j; the columns are split into chunks over
+//    blockIdx.y to fill the GPU, each (row, chunk) leaves a partial
+//    accumulator in scratch, and a second kernel merges the chunks of each
+//    row in order and applies the epilogue.
 #include <stddef.h>
 
 #include "exact.cuh"
@@ -119,14 +121,20 @@ __global__ void __launch_bounds__(kRowThreads, 4)
   }
 }
 
-// ---- columns contiguous ---------------------------------------------------
+// ---- one thread per row --------------------------------------------------
 constexpr int kColThreads = 128;
 
 // Partial sums over columns [chunk*jc, min(n, (chunk+1)*jc)) for rows
-// i = blockIdx.x*128 + threadIdx.x.  With one chunk the epilogue is applied
-// directly; otherwise partials[chunk * m + i] is written.
+// i = blockIdx.x*128 + threadIdx.x: all lanes of a warp read the same x_j
+// (a broadcast) and keep one accumulator each, with no reduction across
+// lanes.  kRowMajor: op(A)(i, j) = A[i*ld + j], each lane reads its own row
+// through L1 (one 128-byte line serves eight consecutive columns);
+// otherwise A[j*ld + i], where a warp's loads are coalesced and read once.
+// With one chunk the epilogue is applied directly; otherwise
+// partials[chunk * m + i] is written.
+template <bool kRowMajor>
 __global__ void __launch_bounds__(kColThreads)
-    qgemv_cols_kernel(int64_t m, int64_t n, const q128* __restrict__ A, int64_t lda,
+    qgemv_lane_kernel(int64_t m, int64_t n, const q128* __restrict__ A, int64_t ld,
                       const uint4* __restrict__ xm, const int2* __restrict__ xe, int64_t jc,
                       q128 alpha, q128 beta, q128* __restrict__ y, int64_t incy,
                       wacc* __restrict__ partials, RowList* __restrict__ L) {
@@ -135,18 +143,18 @@ __global__ void __launch_bounds__(kColThreads)
   int64_t j0 = chunk * jc, j1 = j0 + jc;
   if (j1 > n) j1 = n;
   if (i >= m) return;
+  auto ldA = [&](int64_t j) { return kRowMajor ? ld_cached(A + i * ld + j) : ld_stream(A + j * ld + i); };
   wacc acc;
   wacc_init(acc);
   int64_t j = j0;
   for (; j + 3 < j1; j += 4) {
-    q128 a0 = ld_stream(A + j * lda + i), a1 = ld_stream(A + (j + 1) * lda + i);
-    q128 a2 = ld_stream(A + (j + 2) * lda + i), a3 = ld_stream(A + (j + 3) * lda + i);
+    q128 a0 = ldA(j), a1 = ldA(j + 1), a2 = ldA(j + 2), a3 = ldA(j + 3);
     wacc_add_product(acc, qop_unpack(a0), qop_fetch(xm, xe, j));
     wacc_add_product(acc, qop_unpack(a1), qop_fetch(xm, xe, j + 1));
     wacc_add_product(acc, qop_unpack(a2), qop_fetch(xm, xe, j + 2));
     wacc_add_product(acc, qop_unpack(a3), qop_fetch(xm, xe, j + 3));
   }
-  for (; j < j1; ++j) wacc_add_product(acc, qop_unpack(ld_stream(A + j * lda + i)), qop_fetch(xm, xe, j));
+  for (; j < j1; ++j) wacc_add_product(acc, qop_unpack(ldA(j)), qop_fetch(xm, xe, j));
   if (gridDim.y == 1)
     gemv_finish_row(alpha, acc, 2 * (uint64_t)n + 3, beta, y + i * incy, i, L);
   else
@@ -181,10 +189,20 @@ __global__ void __launch_bounds__(256)
   }
 }
 
-static int64_t col_chunks(int64_t m, int64_t n) {
-  int64_t target_threads = (int64_t)device_sm_count() * 1536;
+// Row-major op(A) with at least this many rows uses the thread-per-row
+// kernel (measured at 8192 x 8192: 2370 GB/s against 2170 for warps per
+// row; with few long rows the column chunks' merges cost more than they save).
+constexpr int64_t kLaneRowsMin = 4096;
+
+static bool use_lanes(int64_t m, const MatView& A) { return A.sj != 1 || m >= kLaneRowsMin; }
+
+// Column chunks of the thread-per-row kernel: enough (row, chunk) threads
+// to fill the GPU (two per resident thread slot for long row-major runs),
+// at least 64 columns each.
+static int64_t col_chunks(int64_t m, int64_t n, bool row_major) {
+  int64_t target_threads = (int64_t)device_sm_count() * (row_major && m >= 8192 ? 3072 : 1536);
   int64_t c = (target_threads + m - 1) / (m > 0 ? m : 1);
-  int64_t maxc = (n + 63) / 64;  // at least 64 columns per chunk
+  int64_t maxc = (n + 63) / 64;
   if (c > maxc) c = maxc;
   if (c > 65535) c = 65535;
   if (c < 1) c = 1;
@@ -199,8 +217,8 @@ static size_t rowlist_bytes(int64_t m) { return round256(offsetof(RowList, row) 
 size_t gemv_scratch_bytes(int64_t m, int64_t n, MatView A) {
   if (m <= 0 || n <= 0) return 0;
   size_t xs = round256((size_t)n * 16) + round256((size_t)n * 8) + rowlist_bytes(m);
-  if (A.sj == 1) return xs;
-  int64_t c = col_chunks(m, n);
+  if (!use_lanes(m, A)) return xs;
+  int64_t c = col_chunks(m, n, A.sj == 1);
   return xs + (c > 1 ? (size_t)c * (size_t)m * sizeof(wacc) : 0);
 }
 
@@ -228,7 +246,7 @@ cudaError_t launch_gemv(int64_t m, int64_t n, q128 alpha, MatView A, const q128*
   }
   const unsigned exact_grid = (unsigned)device_sm_count();
   cudaError_t e;
-  if (A.sj == 1) {
+  if (!use_lanes(m, A)) {
     int l = rows_wpr_log2(n);
     int64_t rows_per_block = (kRowThreads / 32) >> l;
     int64_t nb = (m + rows_per_block - 1) / rows_per_block;
@@ -237,14 +255,19 @@ cudaError_t launch_gemv(int64_t m, int64_t n, q128 alpha, MatView A, const q128*
                                                            y, incy, L);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
   } else {
-    int64_t c = col_chunks(m, n);
+    const bool row_major = A.sj == 1;
+    int64_t c = col_chunks(m, n, row_major);
     int64_t jc = (n + c - 1) / c;
     c = (n + jc - 1) / jc;
     dim3 grid((unsigned)((m + kColThreads - 1) / kColThreads), (unsigned)c);
     size_t xs = round256((size_t)n * 16) + round256((size_t)n * 8) + rowlist_bytes(m);
     wacc* partials = reinterpret_cast<wacc*>(base + xs);
-    qgemv_cols_kernel<<<grid, kColThreads, 0, s>>>(m, n, A.p, A.sj, xm, xe, jc, alpha, beta, y, incy,
-                                                   partials, L);
+    if (row_major)
+      qgemv_lane_kernel<true><<<grid, kColThreads, 0, s>>>(m, n, A.p, A.si, xm, xe, jc, alpha, beta, y, incy,
+                                                           partials, L);
+    else
+      qgemv_lane_kernel<false><<<grid, kColThreads, 0, s>>>(m, n, A.p, A.sj, xm, xe, jc, alpha, beta, y,
+                                                            incy, partials, L);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     if (c > 1) {
       qgemv_cols_finish_kernel<<<(unsigned)((m + kColThreads - 1) / kColThreads), kColThreads, 0, s>>>(

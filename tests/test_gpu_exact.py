@@ -73,9 +73,9 @@ def test_qnrm2_wide_range(qlib, O):
     assert Q.same_bits(api.nrm2(x), O.sqrt(R)).all()
 
 
-@pytest.mark.parametrize("layout", ["R", "C"])
-def test_qgemv_any_condition(qlib, O, layout):
-    n, m = 4096, 40
+@pytest.mark.parametrize("layout,m", [("R", 40), ("C", 40), ("R", 4200)])
+def test_qgemv_any_condition(qlib, O, layout, m):
+    n = 4096
     x, y = O.gendot(n, 1e45, 8)
     rng = G.rng_for(93)
     rows = []
