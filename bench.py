@@ -269,7 +269,7 @@ class Qdot:
 NCU_TRAFFIC = {
     "qgemm4096": (2 * (9.84e9 + 1.01e9), "profiles/ozaki_mma_kernel_4096_traffic.md"),  # 15 x 9 bit, 2 passes
     "qdot26": (2.147608e9 + 4.091e6, "profiles/qdot_partial_kernel_n2p26.md"),
-    "qgemv8192": (1.074185e9 + 9.166e6, "profiles/qgemv_rows_kernel_8192.md"),
+    "qgemv8192": (1.074079e9 + 1.8140e7, "profiles/qgemv_lane_kernel_8192.md"),
 }
 
 
