@@ -207,6 +207,13 @@ int quadblas_release_buffers(void);
  * (the call returns QBLAS_ERR_NO_MEMORY and leaves its outputs untouched);
  * 0 clears it.  Nothing is allocated for a failed attempt. */
 int quadblas_debug_fail_allocations(int count);
+/* Testing aid for the certified rounding of qgemv: while on, every qgemv
+ * records (in stream order) how many rows its exact pass recomputed because
+ * their rounding could not be certified; quadblas_debug_exact_rows returns
+ * the count of the last call once its stream has completed (-1 if never
+ * enabled). */
+int quadblas_debug_count_exact_rows(int on);
+long long quadblas_debug_exact_rows(void);
 /* Status of the calling thread's last call (part 1 calls record it too). */
 int quadblas_last_error(void);
 const char *quadblas_error_string(int code);

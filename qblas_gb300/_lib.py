@@ -59,6 +59,8 @@ _SIGS = {
     "quadblas_profile_read": (ci, [vp, vp]),
     "quadblas_release_buffers": (ci, []),
     "quadblas_debug_fail_allocations": (ci, [ci]),
+    "quadblas_debug_count_exact_rows": (ci, [ci]),
+    "quadblas_debug_exact_rows": (ctypes.c_longlong, []),
     "quadblas_last_error": (ci, []),
     "quadblas_error_string": (ctypes.c_char_p, [ci]),
 }

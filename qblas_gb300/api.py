@@ -149,6 +149,15 @@ def debug_fail_allocations(count: int) -> None:
     check(load().quadblas_debug_fail_allocations(count))
 
 
+def debug_count_exact_rows(on: bool) -> None:
+    check(load().quadblas_debug_count_exact_rows(1 if on else 0))
+
+
+def debug_exact_rows() -> int:
+    """Rows the last qgemv recomputed exactly (after its stream completed)."""
+    return int(load().quadblas_debug_exact_rows())
+
+
 # ---- batched problems (one persistent launch) -------------------------------
 OP_GEMM, OP_GEMV, OP_DOT = 0, 1, 2
 

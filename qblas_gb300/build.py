@@ -15,7 +15,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libquadblas_gpu.so")
 
-SOURCES = ["level1.cu", "level2.cu", "level3.cu", "ozaki.cu", "batched.cu", "noalloc.cu", "capi.cpp"]
+SOURCES = ["level1.cu", "level2.cu", "level3.cu", "ozaki.cu", "ozgemv.cu", "batched.cu", "noalloc.cu", "capi.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-fvisibility=hidden",
           "-I", CSRC, "-I", os.path.join(ROOT, "include")]

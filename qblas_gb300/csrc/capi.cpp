@@ -298,13 +298,18 @@ int dev_dot(int64_t n, const void* dx, int64_t incx, const void* dy, int64_t inc
   return cuda_status(e);
 }
 
+// qgemv method: quadblas_set_method() (1 soft-float, 2 Ozaki), else the
+// library's choice by size; every method returns the correctly rounded sums.
+int gemv_method() { return g_method.load(); }
+
 int dev_gemv(const GemvPlan& p0, const void* alpha, const void* dA, const void* dx, int64_t incx,
              const void* beta, void* dy, int64_t incy, cudaStream_t s, void* scratch_or_null) {
   GemvPlan p = p0;
   if (p.m > 0 && p.n > 0 && (incx <= 0 || incy <= 0)) return qb::kErrInvalidValue;
   if (!aligned16(dA) || !aligned16(dx) || !aligned16(dy)) return qb::kErrMisaligned;
   p.A.p = (const q128*)dA;
-  size_t sb = qb::gemv_scratch_bytes(p.m, p.n, p.A);
+  const int method = gemv_method();
+  size_t sb = qb::gemv_scratch_bytes(p.m, p.n, p.A, method);
   void* scratch = scratch_or_null;
   if (!scratch && sb) {
     cudaError_t e = qb::dev_malloc_async(&scratch, sb, s);
@@ -314,7 +319,7 @@ int dev_gemv(const GemvPlan& p0, const void* alpha, const void* dA, const void* 
     }
   }
   cudaError_t e = qb::launch_gemv(p.m, p.n, q_load(alpha), p.A, (const q128*)dx, incx, q_load(beta),
-                                  (q128*)dy, incy, scratch, s);
+                                  (q128*)dy, incy, scratch, s, method);
   if (!scratch_or_null && scratch) cudaFreeAsync(scratch, s);
   return cuda_status(e);
 }
@@ -442,7 +447,7 @@ int host_gemv(char layout, char trans, int64_t m, int64_t n, const void* alpha, 
       (rc = ensure_slot(st, kSlotC, ey * 16)))
     return rc;
   qb::MatView probe = p.A;
-  size_t sb = qb::gemv_scratch_bytes(p.m, p.n, probe);
+  size_t sb = qb::gemv_scratch_bytes(p.m, p.n, probe, gemv_method());
   if ((rc = ensure_slot(st, kSlotScratch, sb))) return rc;
   if ((rc = h2d(st.buf[kSlotA], A, eA, st.stream)) || (rc = h2d(st.buf[kSlotB], x, ex, st.stream)) ||
       (rc = h2d(st.buf[kSlotC], y, ey, st.stream)))
@@ -767,6 +772,26 @@ QBLAS_EXPORT int quadblas_debug_fail_allocations(int count) {
   if (count < 0) return fail(qb::kErrInvalidValue);
   g_fail_allocs.store(count);
   return fail(qb::kOk);
+}
+
+static unsigned* g_exact_rows_host = nullptr;
+
+QBLAS_EXPORT int quadblas_debug_count_exact_rows(int on) {
+  if (on && !g_exact_rows_host) {
+    void* p = nullptr;
+    if (cudaMallocHost(&p, sizeof(unsigned)) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(qb::kErrNoMemory);
+    }
+    g_exact_rows_host = static_cast<unsigned*>(p);
+    *g_exact_rows_host = 0;
+  }
+  qb::gemv_count_exact_rows(on ? g_exact_rows_host : nullptr);
+  return fail(qb::kOk);
+}
+
+QBLAS_EXPORT long long quadblas_debug_exact_rows(void) {
+  return g_exact_rows_host ? (long long)*reinterpret_cast<volatile unsigned*>(g_exact_rows_host) : -1;
 }
 
 QBLAS_EXPORT int quadblas_set_ozaki_slices(int slices) {

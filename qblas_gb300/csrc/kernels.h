@@ -39,10 +39,15 @@ cudaError_t launch_axpy(int64_t n, q128 alpha, const q128* x, int64_t incx, q128
                         cudaStream_t s);
 
 // ---- level 2 -----------------------------------------------------------
-// y_i = fma(alpha, round(sum_j op(A)(i,j) x_j), beta * y_i), i < m
-size_t gemv_scratch_bytes(int64_t m, int64_t n, MatView A);
+// y_i = fma(alpha, round(sum_j op(A)(i,j) x_j), beta * y_i), i < m.
+// method: 0 chooses (Ozaki split on the tensor cores for large matrices,
+// soft-float otherwise), 1 soft-float, 2 Ozaki; the results are identical.
+size_t gemv_scratch_bytes(int64_t m, int64_t n, MatView A, int method);
+// When set (pinned host memory), every qgemv call copies the number of rows
+// its exact pass recomputed there, in stream order; nullptr stops it.
+void gemv_count_exact_rows(unsigned* host_pinned);
 cudaError_t launch_gemv(int64_t m, int64_t n, q128 alpha, MatView A, const q128* x, int64_t incx,
-                        q128 beta, q128* y, int64_t incy, void* scratch, cudaStream_t s);
+                        q128 beta, q128* y, int64_t incy, void* scratch, cudaStream_t s, int method);
 
 // ---- level 3 -----------------------------------------------------------
 struct GemmArgs {

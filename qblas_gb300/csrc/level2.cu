@@ -25,30 +25,11 @@
 #include <stddef.h>
 
 #include "exact.cuh"
+#include "gemv_rows.cuh"
 #include "kernels.h"
 #include "reduce.cuh"
 
 namespace qb {
-
-// Every row's rounding is certified (exact.cuh).  Rows that cannot be
-// (sums cancelling below the wide accumulator's frame) are left untouched
-// and listed in scratch; qgemv_exact_kernel recomputes them exactly and
-// returns at once when the list is empty.  (The fast kernels keep no exact
-// accumulator in shared memory: the unpacked x is meant to stay in L1.)
-struct RowList {
-  unsigned count;
-  unsigned pad[63];
-  int64_t row[1];  // m entries
-};
-
-__device__ __forceinline__ void gemv_finish_row(q128 alpha, const wacc& acc, uint64_t err, q128 beta,
-                                                q128* yp, int64_t row, RowList* L) {
-  q128 r;
-  if (wacc_round_certified(acc, err, r))
-    *yp = q_epilogue(alpha, r, beta, *yp);
-  else
-    L->row[atomicAdd(&L->count, 1u)] = row;
-}
 
 __device__ __forceinline__ q128 gemv_epilogue(q128 alpha, q128 sum, q128 beta, q128 yv) {
   return q_epilogue(alpha, sum, beta, yv);
@@ -173,19 +154,38 @@ __global__ void __launch_bounds__(kColThreads)
   gemv_finish_row(alpha, acc, 2 * (uint64_t)n + 3 * ((uint64_t)nchunks + 2), beta, y + i * incy, i, L);
 }
 
-// Exact recomputation of the listed rows, one block per row.
+// Recomputation of the listed rows, one block per row.  With try_wide the
+// block first sums the row in wide accumulators (one per thread, merged in
+// shared memory) and certifies that rounding, which settles the rows whose
+// Ozaki bound was too loose; the rest (and every row when !try_wide: the
+// soft-float kernels already tried the wide accumulator) are summed exactly
+// by a Kulisch accumulator.
 __global__ void __launch_bounds__(256)
     qgemv_exact_kernel(const RowList* __restrict__ L, int64_t n, MatView A, const q128* __restrict__ x,
-                       int64_t incx, q128 alpha, q128 beta, q128* __restrict__ y, int64_t incy) {
+                       int64_t incx, q128 alpha, q128 beta, q128* __restrict__ y, int64_t incy, int try_wide) {
   __shared__ KulischBlock K;
+  __shared__ wacc sm[8];
+  __shared__ int done;
   const unsigned cnt = *reinterpret_cast<const volatile unsigned*>(&L->count);
   for (unsigned t = blockIdx.x; t < cnt; t += gridDim.x) {
     const int64_t i = L->row[t];
-    q128 r = block_exact_dot(K, n, A.p + i * A.si, A.sj, x, incx);
-    if (threadIdx.x == 0) {
-      q128* yp = y + i * incy;
-      *yp = q_epilogue(alpha, r, beta, *yp);
+    q128* yp = y + i * incy;
+    if (try_wide) {
+      wacc acc;
+      wacc_init(acc);
+      for (int64_t j = threadIdx.x; j < n; j += blockDim.x)
+        wacc_add_product(acc, qop_unpack(ld_cached(A.p + i * A.si + j * A.sj)), qop_unpack(ld_cached(x + j * incx)));
+      wacc_block_reduce(acc, sm);
+      if (threadIdx.x == 0) {
+        q128 r;
+        done = wacc_round_certified(acc, 2 * (uint64_t)n + 3 * 256, r);
+        if (done) *yp = q_epilogue(alpha, r, beta, *yp);
+      }
+      __syncthreads();
+      if (done) continue;
     }
+    q128 r = block_exact_dot(K, n, A.p + i * A.si, A.sj, x, incx);
+    if (threadIdx.x == 0) *yp = q_epilogue(alpha, r, beta, *yp);
   }
 }
 
@@ -209,13 +209,38 @@ static int64_t col_chunks(int64_t m, int64_t n, bool row_major) {
   return c;
 }
 
+static unsigned* g_exact_rows = nullptr;
+void gemv_count_exact_rows(unsigned* host_pinned) { g_exact_rows = host_pinned; }
+
+// Exact pass over the listed rows (returns at once when none), then the
+// optional record of how many there were.
+static cudaError_t launch_exact_rows(RowList* L, int64_t n, MatView A, const q128* x, int64_t incx, q128 alpha,
+                                     q128 beta, q128* y, int64_t incy, cudaStream_t s, bool try_wide) {
+  qgemv_exact_kernel<<<(unsigned)device_sm_count(), 256, 0, s>>>(L, n, A, x, incx, alpha, beta, y, incy,
+                                                                 try_wide ? 1 : 0);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess && g_exact_rows)
+    e = cudaMemcpyAsync(g_exact_rows, &L->count, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
+  return e;
+}
+
 static size_t round256(size_t b) { return (b + 255) & ~(size_t)255; }
 
 static size_t rowlist_bytes(int64_t m) { return round256(offsetof(RowList, row) + (size_t)m * 8); }
 
-// Scratch: [x significands: 16n][x exponents: 8n][uncertified rows] (+ column partials)
-size_t gemv_scratch_bytes(int64_t m, int64_t n, MatView A) {
+// The Ozaki kernels run when asked for (method 2); the library's own choice
+// stays with the soft-float kernels, which are faster at every size measured.
+static bool use_ozaki(int64_t m, int64_t n, int method) {
+  (void)m;
+  (void)n;
+  return method == 2;
+}
+
+// Scratch: [uncertified rows][Ozaki buffers], or
+// [x significands: 16n][x exponents: 8n][uncertified rows] (+ column partials)
+size_t gemv_scratch_bytes(int64_t m, int64_t n, MatView A, int method) {
   if (m <= 0 || n <= 0) return 0;
+  if (use_ozaki(m, n, method)) return rowlist_bytes(m) + gemv_ozaki_scratch_bytes(m, n);
   size_t xs = round256((size_t)n * 16) + round256((size_t)n * 8) + rowlist_bytes(m);
   if (!use_lanes(m, A)) return xs;
   int64_t c = col_chunks(m, n, A.sj == 1);
@@ -230,10 +255,16 @@ static int rows_wpr_log2(int64_t n) {
 }
 
 cudaError_t launch_gemv(int64_t m, int64_t n, q128 alpha, MatView A, const q128* x, int64_t incx,
-                        q128 beta, q128* y, int64_t incy, void* scratch, cudaStream_t s) {
+                        q128 beta, q128* y, int64_t incy, void* scratch, cudaStream_t s, int method) {
   if (m <= 0) return cudaSuccess;
   if (n <= 0) return cudaSuccess;  // the reference leaves y untouched (level2.hpp:21,61)
   char* base = static_cast<char*>(scratch);
+  if (use_ozaki(m, n, method)) {
+    RowList* L = reinterpret_cast<RowList*>(base);
+    cudaError_t e = launch_gemv_ozaki(m, n, alpha, A, x, incx, beta, y, incy, L, base + rowlist_bytes(m), s);
+    if (e != cudaSuccess) return e;
+    return launch_exact_rows(L, n, A, x, incx, alpha, beta, y, incy, s, true);
+  }
   uint4* xm = reinterpret_cast<uint4*>(base);
   int2* xe = reinterpret_cast<int2*>(base + round256((size_t)n * 16));
   RowList* L = reinterpret_cast<RowList*>(base + round256((size_t)n * 16) + round256((size_t)n * 8));
@@ -244,7 +275,6 @@ cudaError_t launch_gemv(int64_t m, int64_t n, q128 alpha, MatView A, const q128*
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
-  const unsigned exact_grid = (unsigned)device_sm_count();
   cudaError_t e;
   if (!use_lanes(m, A)) {
     int l = rows_wpr_log2(n);
@@ -275,8 +305,7 @@ cudaError_t launch_gemv(int64_t m, int64_t n, q128 alpha, MatView A, const q128*
       if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
   }
-  qgemv_exact_kernel<<<exact_grid, 256, 0, s>>>(L, n, A, x, incx, alpha, beta, y, incy);
-  return cudaGetLastError();
+  return launch_exact_rows(L, n, A, x, incx, alpha, beta, y, incy, s, false);
 }
 
 }  // namespace qb

@@ -251,16 +251,12 @@ QB_HD uint32_t special_product_flags(const qop& a, const qop& b) {
   return 0u;
 }
 
-// acc += a * b
-QB_HD void wacc_add_product(wacc& acc, const qop& a, const qop& b) {
-  if ((a.cls | b.cls) != kClsFinite) {
-    acc.flags |= special_product_flags(a, b);
-    return;
-  }
-  uint32_t p1, p2, p3, p4, p5, p6, p7;
-  mul128x128_top224(a, b, p1, p2, p3, p4, p5, p6, p7);
-  int pe = a.e + b.e + 32;  // exponent of p1's bit 0
-  int r = acc.e - pe;       // right shift that aligns the product to the frame
+// acc += (neg ? -P : P) * 2^pe for a magnitude P = (p7..p1) < 2^224: P is
+// aligned to the frame (moving the frame up when P's least significant bit
+// lies above it), dropping less than one unit of the frame's last bit.
+QB_HD void wacc_add_aligned(wacc& acc, uint32_t p1, uint32_t p2, uint32_t p3, uint32_t p4, uint32_t p5,
+                            uint32_t p6, uint32_t p7, int pe, uint32_t neg) {
+  int r = acc.e - pe;       // right shift that aligns P to the frame
   if (r < 0) {              // product above the frame top: move the frame up
     wacc_ashr(acc, -r);
     acc.e = pe;
@@ -289,7 +285,18 @@ QB_HD void wacc_add_product(wacc& acc, const qop& a, const qop& b) {
     q0 = q1; q1 = q2; q2 = q3; q3 = q4; q4 = q5; q5 = q6;
     q6 = 0;
   }
-  wacc_add_signed(acc, q0, q1, q2, q3, q4, q5, q6, 0u, a.s ^ b.s);
+  wacc_add_signed(acc, q0, q1, q2, q3, q4, q5, q6, 0u, neg);
+}
+
+// acc += a * b
+QB_HD void wacc_add_product(wacc& acc, const qop& a, const qop& b) {
+  if ((a.cls | b.cls) != kClsFinite) {
+    acc.flags |= special_product_flags(a, b);
+    return;
+  }
+  uint32_t p1, p2, p3, p4, p5, p6, p7;
+  mul128x128_top224(a, b, p1, p2, p3, p4, p5, p6, p7);
+  wacc_add_aligned(acc, p1, p2, p3, p4, p5, p6, p7, a.e + b.e + 32, a.s ^ b.s);
 }
 
 // a += b (b unchanged).  The smaller-exponent operand is aligned to the larger one's frame.  The

@@ -7,6 +7,7 @@
 #include "../qblas_gb300/csrc/wacc.cuh"
 #include "../qblas_gb300/csrc/ozaki.cuh"
 #include "../qblas_gb300/csrc/exact.cuh"
+#include "../qblas_gb300/csrc/ozgemv.cuh"
 
 using qb::q128;
 
@@ -112,5 +113,79 @@ void sq_ozaki_fold(int64_t m, int64_t n, int G, int b, const int64_t* C, const i
       for (int g = 0; g <= G; ++g) qb::fold_step(f, C[((int64_t)g * m + i) * n + j], b);
       out[i * n + j] = qb::fold_round(f, qb::ozaki_fold_exp(S[i], F[j], G, b));
     }
+}
+// Ozaki qgemv arithmetic (ozgemv.cuh): windows W of n elements against
+// exponents E[i] (five words each).
+void sq_og_window(int64_t n, const q128* a, const int32_t* E, uint32_t* W) {
+  for (int64_t i = 0; i < n; ++i) {
+    uint32_t w[5];
+    qb::og_window((uint32_t)a[i].lo, (uint32_t)(a[i].lo >> 32), (uint32_t)a[i].hi,
+                  (uint32_t)(a[i].hi >> 32), E[i], w);
+    for (int k = 0; k < 5; ++k) W[5 * i + k] = w[k];
+  }
+}
+static int og_lead_x(const q128& x) {  // nonzero finite x: its lead exponent; else kOgNoExp
+  const uint32_t top = (uint32_t)(x.hi >> 32);
+  if (qb::og_special_top(top)) return qb::kOgNoExp;
+  if (((x.hi & 0x7FFFFFFFFFFFFFFFull) | x.lo) == 0) return qb::kOgNoExp;
+  return qb::og_lead_top(top);
+}
+// One chunk (n <= 32 terms): E, F, the diagonal sums D[0..31] and T.
+void sq_og_chunk(int n, const q128* a, const q128* x, int32_t* EF, int64_t* D, uint32_t* T) {
+  int E = -16382, F = qb::kOgNoExp;
+  for (int j = 0; j < n; ++j) {
+    int l = qb::og_lead_top((uint32_t)(a[j].hi >> 32));
+    E = l > E ? l : E;
+    int f = og_lead_x(x[j]);
+    F = f > F ? f : F;
+  }
+  for (int g = 0; g < 32; ++g) D[g] = 0;
+  for (int j = 0; j < n; ++j) {
+    uint32_t wa[5], wx[5];
+    qb::og_window((uint32_t)a[j].lo, (uint32_t)(a[j].lo >> 32), (uint32_t)a[j].hi, (uint32_t)(a[j].hi >> 32), E, wa);
+    qb::og_window((uint32_t)x[j].lo, (uint32_t)(x[j].lo >> 32), (uint32_t)x[j].hi, (uint32_t)(x[j].hi >> 32),
+                  F == qb::kOgNoExp ? -16382 : F, wx);
+    for (int t = 0; t < qb::kOgPlanes; ++t)
+      for (int u = 0; u < qb::kOgPlanes; ++u)
+        if (t + u < 32) D[t + u] += (int64_t)qb::og_digit(wa, t) * qb::og_digit(wx, u);
+  }
+  int32_t D32[qb::kOgDiags];
+  for (int g = 0; g < qb::kOgDiags; ++g) D32[g] = (int32_t)D[g];
+  uint32_t t6[6];
+  qb::og_fold(D32, t6);
+  for (int k = 0; k < 6; ++k) T[k] = t6[k];
+  EF[0] = E;
+  EF[1] = F;
+}
+// A whole row the way the kernels treat it (one partial, no merges):
+// out = the certified rounding, returns 1 when certified, 0 otherwise.
+int sq_og_row(int64_t n, const q128* a, const q128* x, q128* out) {
+  qb::wacc acc;
+  qb::wacc_init(acc);
+  const int kNone = 2 * qb::kOgNoExp;
+  int gmax = kNone;
+  uint32_t nch = 0;
+  bool spec = false;
+  for (int64_t j0 = 0; j0 < n; j0 += qb::kOgChunk) {
+    const int c = (int)(n - j0 < qb::kOgChunk ? n - j0 : qb::kOgChunk);
+    for (int j = 0; j < c; ++j) spec = spec || qb::og_special_top((uint32_t)(a[j0 + j].hi >> 32)) ||
+                                         qb::og_special_top((uint32_t)(x[j0 + j].hi >> 32));
+    int32_t EF[2];
+    int64_t D[32];
+    uint32_t T[6];
+    sq_og_chunk(c, a + j0, x + j0, EF, D, T);
+    ++nch;
+    if (EF[1] == qb::kOgNoExp) continue;
+    gmax = EF[0] + EF[1] > gmax ? EF[0] + EF[1] : gmax;
+    qb::og_wacc_add(acc, T, EF[0] + EF[1] - qb::kOgFoldShift);
+  }
+  if (spec) return 0;
+  if (gmax == kNone) {
+    *out = qb::wacc_round(acc);  // every product is an exact zero
+    return 1;
+  }
+  if (acc.e == qb::kWaccEmptyExp) return 0;
+  uint64_t err = qb::og_row_error(acc, nch, gmax, 0);
+  return qb::wacc_round_certified(acc, err, *out) ? 1 : 0;
 }
 }
