@@ -63,30 +63,38 @@
 namespace qb {
 
 constexpr int kOgRows = 128;                 // rows per tile (MMA M)
-constexpr int kOgSplitWarps = 8;
+constexpr int kOgSplitWarps = 16;            // four per tensor-memory lane quadrant
 constexpr int kOgEpiWarps = 4;
-constexpr int kOgMmaWarp = kOgSplitWarps;    // warp 8: tcgen05.mma and the TMA loads of A
-constexpr int kOgThreads = (kOgSplitWarps + 1 + kOgEpiWarps) * 32;  // 416
-constexpr int kOgKStep = 16;                 // columns per MMA (K)
-constexpr int kOgPlaneBytes = kOgRows * kOgKStep * 2;  // 4096
-constexpr int kOgALbo = kOgPlaneBytes / 2;   // 2048: core matrices of columns 8..15
-constexpr int kOgXRows = 56;
-constexpr int kOgXLbo = kOgXRows * 16;       // 896
-constexpr int kOgXBytes = 2 * kOgXLbo;       // 1792 per k-step
-constexpr int kOgXBase = kOgPlanes - 1;      // x plane u at B row 17 + u
-constexpr int kOgDigitBytes = kOgPlanes * kOgPlaneBytes + kOgXBytes;  // 75520: one operand stage
-constexpr int kOgSlotBytes = kOgRows * kOgKStep * 16;  // 32768: A elements of one k-step
-constexpr int kOgSlots = 4;                  // TMA ring: two chunks
-constexpr int kOgExpSlots = 4;
-constexpr int kOgTmemCols = 64;              // two 32-column accumulators
+constexpr int kOgMmaWarp = kOgSplitWarps;    // warp 16: tcgen05.mma
+constexpr int kOgLoadWarp = kOgSplitWarps + 1;  // warp 17: TMA loads of A
+constexpr int kOgThreads = (kOgSplitWarps + 2 + kOgEpiWarps) * 32;  // 704
+constexpr int kOgKStep = 8;                  // columns per k-step: MMA K = 8 elements x 2 planes
+constexpr int kOgKSteps = kOgChunk / kOgKStep;  // 4 per chunk
+constexpr int kOgPairs = kOgPlanes / 2;     // 9 plane pairs: one MMA each per k-step
+// tensor memory: four 32-column accumulators (items in flight between the
+// MMAs and the epilogue), then the A operand stages: 9 tiles of 8 columns
+// (128 lanes x 16 fp16 values) per k-step
+constexpr int kOgAccBufs = 4;
+constexpr int kOgAccCols = kOgAccBufs * 32;  // 128
+constexpr int kOgTileCols = 8;
+constexpr int kOgStageCols = kOgPairs * kOgTileCols;  // 72
+constexpr int kOgStages = 4;                 // operand stages in flight
+constexpr int kOgTmemCols = 512;             // 128 + 4 * 72 = 416 used
+constexpr int kOgXRows = 48;                 // B rows: diagonal g of pair p at row g + 16 - 2p
+constexpr int kOgXLbo = kOgXRows * 16;       // 768
+constexpr int kOgXBytes = 2 * kOgXLbo;       // 1536: B operand of one k-step (shared memory)
+constexpr int kOgSlotBytes = kOgRows * kOgKStep * 16;  // 16384: A elements of one k-step
+constexpr int kOgSlots = 12;                 // TMA ring: three chunks
+constexpr int kOgExpSlots = 8;
 constexpr int kOgXSpecial = 0x7FFFFFFF;      // x chunk holding NaN or inf
 constexpr int kOgNoGmax = 2 * kOgNoExp;
 // kind::f16, fp16 A and B (K-major), fp32 D, N = 32, M = 128
 constexpr uint32_t kOgIdesc = (1u << 4) | ((32u >> 3) << 17) | ((uint32_t)(kOgRows >> 4) << 24);
-// barriers: full[4] (TMA), ready, free (operand stage), tfull[2], tempty[2], exp[4], drain
-constexpr int kOgBars = kOgSlots + 2 + 4 + kOgExpSlots + 1;
-constexpr size_t kOgSmem = 1024 + (size_t)kOgSlots * kOgSlotBytes + kOgDigitBytes + kOgExpSlots * kOgRows * 4 +
-                           kOgBars * 8 + 16;
+// barriers: full[slots], empty[slots] (TMA ring), ready[stages], free[stages], tfull[accs],
+// tempty[accs], exp[8], rowmax[2][4] (the four split warps of a lane quadrant), drain
+constexpr int kOgBars = 2 * kOgSlots + 2 * kOgStages + 2 * kOgAccBufs + kOgExpSlots + 8 + 1;
+constexpr size_t kOgSmem = 1024 + (size_t)kOgSlots * kOgSlotBytes + (size_t)kOgStages * kOgXBytes +
+                           kOgExpSlots * kOgRows * 4 + 2 * 4 * kOgRows * 4 + kOgBars * 8 + 16;
 
 struct OgPartial {
   wacc acc;
@@ -98,7 +106,7 @@ struct OgPartial {
 
 struct OgParams {
   int64_t m, n;
-  const uint8_t* xdig;      // [2 * nchunks][kOgXBytes]
+  const uint8_t* xdig;      // [4 * nchunks][kOgXBytes]
   const int32_t* xexp;      // [nchunks]: F_c, kOgNoExp, or kOgXSpecial
   int64_t tiles, nchunks, work;  // work = tiles * nchunks items
   int segs;                 // partial slots per tile
@@ -113,7 +121,9 @@ QB_HD int64_t og_cta_of(int64_t work, int64_t G, int64_t X) { return ((X + 1) * 
 // ---------------------------------------------------------------------------
 // x digits
 // ---------------------------------------------------------------------------
-// One warp per chunk of 32 elements of x.
+// One warp per chunk of 32 elements of x: F_c, and the B operand of each
+// k-step (8 columns): row rho, K = 2 * (column % 8) + tt holds x's digit
+// rho - 16 - tt (zero outside 0..17), K-major core matrices (LBO 768).
 __global__ void __launch_bounds__(256)
     og_x_split_kernel(int64_t n, int64_t nchunks, const q128* __restrict__ x, int64_t incx,
                       uint8_t* __restrict__ xdig, int32_t* __restrict__ xexp, RowList* __restrict__ L) {
@@ -128,21 +138,23 @@ __global__ void __launch_bounds__(256)
   const uint32_t top = (uint32_t)(v.hi >> 32);
   const bool special = og_special_top(top);
   const bool nonzero = ((v.hi & 0x7FFFFFFFFFFFFFFFull) | v.lo) != 0;
-  int f = (nonzero && !special) ? og_lead_top(top) : kOgNoExp;
+  int f = nonzero ? og_lead_top(top) : kOgNoExp;  // chunks with NaN / inf are marked below
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) f = max(f, __shfl_xor_sync(0xFFFFFFFFu, f, o));
   const bool any_special = __any_sync(0xFFFFFFFFu, special);
   if (lane == 0) xexp[c] = any_special ? kOgXSpecial : f;
   uint32_t W[5];
   og_window((uint32_t)v.lo, (uint32_t)(v.lo >> 32), (uint32_t)v.hi, top, f == kOgNoExp ? -16382 : f, W);
-  // B tile of k-step 2c + lane/16, column lane%16
-  uint8_t* tile = xdig + (size_t)(2 * c + (lane >> 4)) * kOgXBytes;
-  const int kk = lane & 15;
-  __half* col = reinterpret_cast<__half*>(tile + (kk >> 3) * kOgXLbo + (kk & 7) * 2);
-  for (int rho = 0; rho < kOgXRows; ++rho) {
-    const int u = rho - kOgXBase;
-    const int d = (u >= 0 && u < kOgPlanes) ? og_digit(W, u) : 0;
-    col[rho * 8] = __int2half_rn(d);  // rows are 16 bytes apart
+  const uint32_t neg = top >> 31;
+  uint8_t* tile = xdig + (size_t)(kOgKSteps * c + (lane >> 3)) * kOgXBytes;
+  for (int tt = 0; tt < 2; ++tt) {
+    const int kk = 2 * (lane & 7) + tt;
+    __half* col = reinterpret_cast<__half*>(tile + (kk >> 3) * kOgXLbo + (kk & 7) * 2);
+    for (int rho = 0; rho < kOgXRows; ++rho) {
+      const int u = rho - 16 - tt;
+      const int d = (u >= 0 && u < kOgPlanes) ? og_digit(W, u, neg) : 0;
+      col[rho * 8] = __int2half_rn(d);  // rows are 16 bytes apart
+    }
   }
 }
 
@@ -166,41 +178,42 @@ __device__ __forceinline__ uint32_t ld_shared_u32(uint32_t addr) {
   return v;
 }
 
-// Two digits of plane t (byte 17 - t of the windows of two elements) as an
-// fp16 pair: (1024 + byte) - 1152.
-template <int kT>
-__device__ __forceinline__ uint32_t og_digit_pair(const uint32_t (&Wa)[5], const uint32_t (&Wb)[5]) {
-  constexpr int beta = 17 - kT, w = beta >> 2, by = beta & 3;
-  const uint32_t p = __byte_perm(Wa[w], Wb[w], (uint32_t)(by | ((4 + by) << 4)));
-  uint32_t q = __byte_perm(p, 0x64646464u, 0x5140u);
-  uint32_t bias = 0xE480E480u;  // fp16 -1152 twice
-  __half2 h = __hadd2(*reinterpret_cast<__half2*>(&q), *reinterpret_cast<__half2*>(&bias));
+// Digits 2p and 2p+1 of one element (bytes 17-2p and 16-2p of its window)
+// as an fp16 pair: sign * ((1024 + byte) - 1152), with sg = (sign, sign)
+// and bs = (-1152 sign, -1152 sign).
+template <int kP>
+__device__ __forceinline__ uint32_t og_digit_pair(const uint32_t (&W)[5], uint32_t sg, uint32_t bs) {
+  constexpr int lo = 16 - 2 * kP, w = lo >> 2, by = lo & 3;
+  uint32_t q = __byte_perm(W[w], 0x64646464u, (uint32_t)((by + 1) | (4 << 4) | (by << 8) | (4 << 12)));
+  __half2 h = __hfma2(*reinterpret_cast<__half2*>(&q), *reinterpret_cast<__half2*>(&sg),
+                      *reinterpret_cast<__half2*>(&bs));
   return *reinterpret_cast<uint32_t*>(&h);
 }
 
-template <int kT>
-__device__ __forceinline__ void og_store_plane(uint32_t addr, const uint32_t (&W)[8][5]) {
-  st_shared_v4(addr + kT * kOgPlaneBytes, og_digit_pair<kT>(W[0], W[1]), og_digit_pair<kT>(W[2], W[3]),
-               og_digit_pair<kT>(W[4], W[5]), og_digit_pair<kT>(W[6], W[7]));
-  if constexpr (kT + 1 < kOgPlanes) og_store_plane<kT + 1>(addr, W);
+// The nine digit pairs of two elements into the nine A tiles of a stage
+// (tensor memory columns 8p + 2g, 8p + 2g + 1 of this thread's lane).
+template <int kP>
+__device__ __forceinline__ void og_store_pairs(uint32_t taddr, const uint32_t (&W)[2][5], const uint32_t (&sg)[2],
+                                               const uint32_t (&bs)[2]) {
+  tmem_st2(taddr + kP * kOgTileCols, og_digit_pair<kP>(W[0], sg[0], bs[0]), og_digit_pair<kP>(W[1], sg[1], bs[1]));
+  if constexpr (kP + 1 < kOgPairs) og_store_pairs<kP + 1>(taddr, W, sg, bs);
 }
 
 // A's elements of one k-step arrive by TMA (128-byte swizzle: the 16-byte
 // piece p of a 128-byte smem row q sits at piece p ^ (q % 8)).
-//   row-major A: two boxes of 128 rows x 8 columns (columns 8h..8h+7 at
-//                h * 16384; element (r, 8h + i) at r * 128 + piece i)
-//   column-major A: sixteen boxes of 8 rows x 16 columns (rows 8g..8g+7 at
-//                g * 2048; element (8g + e, j) at j * 128 + piece e)
-// Offset of thread (row r, half h)'s element i within a slot:
+//   row-major A: one box of 128 rows x 8 columns (element (r, i) at
+//                r * 128 + piece i)
+//   column-major A: sixteen boxes of 8 rows x 8 columns (rows 8g..8g+7 at
+//                g * 1024; element (8g + e, i) at i * 128 + piece e)
+// Offset of element (r, i) within a slot:
 template <bool kRowMajor>
-__device__ __forceinline__ uint32_t og_elem_offset(int r, int h, int i) {
-  if (kRowMajor) return (uint32_t)(h * 16384 + r * 128 + ((i ^ (r & 7)) << 4));
-  const int j = 8 * h + i;
-  return (uint32_t)((r >> 3) * 2048 + j * 128 + (((r & 7) ^ (j & 7)) << 4));
+__device__ __forceinline__ uint32_t og_elem_offset(int r, int i) {
+  if (kRowMajor) return (uint32_t)(r * 128 + ((i ^ (r & 7)) << 4));
+  return (uint32_t)((r >> 3) * 1024 + i * 128 + (((r & 7) ^ i) << 4));
 }
 
-// 13 warps: four share one SM sub-partition's 16384 registers, so at most
-// 128 registers per thread; one CTA per SM.
+// 21 warps: six share one SM sub-partition's 16384 registers, so at most
+// 80 registers per thread; one CTA per SM (all 512 tensor-memory columns).
 template <bool kRowMajor>
 __global__ void __launch_bounds__(kOgThreads, 1)
     og_gemv_kernel(const __grid_constant__ CUtensorMap tmA, OgParams P) {
@@ -208,27 +221,47 @@ __global__ void __launch_bounds__(kOgThreads, 1)
   const uint32_t raw = smem_u32(smem_raw);
   const uint32_t base = (raw + 1023u) & ~1023u;  // slots: 1024-byte aligned for the swizzle
   uint8_t* gbase = smem_raw + (base - raw);
-  const uint32_t dstage = base + kOgSlots * kOgSlotBytes;  // digit planes + x tile
-  int32_t* exps = reinterpret_cast<int32_t*>(gbase + kOgSlots * kOgSlotBytes + kOgDigitBytes);  // [4][128]
-  const uint32_t bar0 = dstage + kOgDigitBytes + kOgExpSlots * kOgRows * 4;
+  const uint32_t xstage0 = base + kOgSlots * kOgSlotBytes;  // B operand of each stage
+  uint8_t* after = gbase + kOgSlots * kOgSlotBytes + kOgStages * kOgXBytes;
+  int32_t* exps = reinterpret_cast<int32_t*>(after);                        // [8][128]
+  uint32_t* emax = reinterpret_cast<uint32_t*>(after + kOgExpSlots * kOgRows * 4);  // [2][4][128]
+  const uint32_t bar0 = base + (uint32_t)(after - gbase) + kOgExpSlots * kOgRows * 4 + 2 * 4 * kOgRows * 4;
   auto full_bar = [&](int s) { return bar0 + 8u * s; };
-  const uint32_t ready_bar = bar0 + 8u * kOgSlots, free_bar = ready_bar + 8u;
-  auto tfull_bar = [&](int b) { return bar0 + 8u * (kOgSlots + 2 + b); };
-  auto tempty_bar = [&](int b) { return bar0 + 8u * (kOgSlots + 4 + b); };
-  auto exp_bar = [&](int s) { return bar0 + 8u * (kOgSlots + 6 + s); };
+  auto empty_bar = [&](int s) { return bar0 + 8u * (kOgSlots + s); };
+  const uint32_t bar1 = bar0 + 8u * (2 * kOgSlots);
+  auto ready_bar = [&](int s) { return bar1 + 8u * s; };
+  auto free_bar = [&](int s) { return bar1 + 8u * (kOgStages + s); };
+  auto tfull_bar = [&](int b) { return bar1 + 8u * (2 * kOgStages + b); };
+  auto tempty_bar = [&](int b) { return bar1 + 8u * (2 * kOgStages + kOgAccBufs + b); };
+  auto exp_bar = [&](int s) { return bar1 + 8u * (2 * kOgStages + 2 * kOgAccBufs + s); };
+  auto rowmax_bar = [&](int b, int quad) {
+    return bar1 + 8u * (2 * kOgStages + 2 * kOgAccBufs + kOgExpSlots + 4 * b + quad);
+  };
   const uint32_t drain_bar = bar0 + 8u * (kOgBars - 1);
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(gbase + (bar0 - base) + kOgBars * 8);
+  // k-step q uses TMA slot q % kOgSlots (fill q / kOgSlots) and operand
+  // stage q % kOgStages (use q / kOgStages)
+  auto slot_of = [](uint32_t kq) { return (int)(kq % kOgSlots); };
+  auto fill_parity = [](uint32_t kq) { return (kq / kOgSlots) & 1u; };
+  auto stage_of = [](uint32_t kq) { return (int)(kq % kOgStages); };
+  auto use_parity = [](uint32_t kq) { return (kq / kOgStages) & 1u; };
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (threadIdx.x == 0) {
-    for (int s = 0; s < kOgSlots; ++s) mbar_init(full_bar(s), 1);
-    mbar_init(ready_bar, kOgSplitWarps);
-    mbar_init(free_bar, 1);
-    for (int b = 0; b < 2; ++b) {
+    for (int s = 0; s < kOgSlots; ++s) {
+      mbar_init(full_bar(s), 1);
+      mbar_init(empty_bar(s), kOgSplitWarps);
+    }
+    for (int s = 0; s < kOgStages; ++s) {
+      mbar_init(ready_bar(s), kOgSplitWarps);
+      mbar_init(free_bar(s), 1);
+    }
+    for (int b = 0; b < kOgAccBufs; ++b) {
       mbar_init(tfull_bar(b), 1);
       mbar_init(tempty_bar(b), kOgEpiWarps);
     }
     for (int s = 0; s < kOgExpSlots; ++s) mbar_init(exp_bar(s), 1);
+    for (int b = 0; b < 8; ++b) mbar_init(rowmax_bar(b >> 2, b & 3), 4);
     mbar_init(drain_bar, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -245,111 +278,173 @@ __global__ void __launch_bounds__(kOgThreads, 1)
 
   const int64_t G = gridDim.x;
   const int64_t w0 = og_range_begin(P.work, G, blockIdx.x), w1 = og_range_begin(P.work, G, blockIdx.x + 1);
-  const uint32_t nks = (uint32_t)(2 * (w1 - w0));  // k-steps of this CTA
+  const uint32_t nks = (uint32_t)(kOgKSteps * (w1 - w0));  // k-steps of this CTA
   bool ok = true;
 
   if (warp < kOgSplitWarps) {
-    // ---------------- split: two threads per row ----------------
-    const int r = warp * 16 + (lane >> 1), h = lane & 1;
+    // ---------------- split: thread per row (its tensor-memory lane), 2 columns per k-step ----------------
+    const int qd = warp & 3, grp = warp >> 2;  // lane quadrant; columns 2*grp, 2*grp+1 of each k-step
+    const int r = qd * 32 + lane;
     const int tid = threadIdx.x;
-    uint32_t off[8];
-#pragma unroll
-    for (int i = 0; i < 8; ++i) off[i] = og_elem_offset<kRowMajor>(r, h, i);
+    const uint32_t off0 = og_elem_offset<kRowMajor>(r, 2 * grp), off1 = og_elem_offset<kRowMajor>(r, 2 * grp + 1);
+    const uint32_t tlane = tmem + ((uint32_t)(qd * 32) << 16) + kOgAccCols + 2 * grp;
+    const bool xcopy = tid < kOgXBytes / 16;
+    // chunk of the item being split, kept by counting (no 64-bit division in the loop)
+    const int nch = (int)P.nchunks;
+    int cw = (int)(w0 % P.nchunks);
+    uint4 xv_next = make_uint4(0, 0, 0, 0);
+    if (xcopy && w0 < w1)
+      xv_next = __ldg(reinterpret_cast<const uint4*>(P.xdig + (size_t)(kOgKSteps * cw) * kOgXBytes) + tid);
     uint32_t q = 0, it = 0;
     for (int64_t w = w0; w < w1 && ok; ++w, ++it) {
-      // both k-steps of the chunk are needed for its row exponents
-      if (!mbar_wait(full_bar(q & 3), (q >> 2) & 1u) || !mbar_wait(full_bar((q + 1) & 3), ((q + 1) >> 2) & 1u)) {
+      // all k-steps of the chunk are needed for its row exponents
+      bool got = true;
+#pragma unroll
+      for (int ks = 0; ks < kOgKSteps; ++ks) got = got && mbar_wait(full_bar(slot_of(q + ks)), fill_parity(q + ks));
+      if (!got) {
         ok = false;
         break;
       }
-      int E = -16382;
-      uint32_t sp = 0;
+      // largest exponent field: the maximum of top << 1 (sign dropped,
+      // exponent first) over the row's 32 columns, which the four warps of
+      // this lane quadrant exchange through shared memory (a bounded
+      // mbarrier wait, per item parity); the all-ones field marks a NaN or
+      // infinity
+      uint32_t mx = 0;
 #pragma unroll
-      for (int ks = 0; ks < 2; ++ks) {
-        const uint32_t slot = base + ((q + ks) & 3) * kOgSlotBytes;
-#pragma unroll
-        for (int i = 0; i < 8; ++i) {
-          const uint32_t top = ld_shared_u32(slot + off[i] + 12);
-          E = max(E, og_lead_top(top));
-          sp |= og_special_top(top) ? 1u : 0u;
-        }
+      for (int ks = 0; ks < kOgKSteps; ++ks) {
+        const uint32_t slot = base + slot_of(q + ks) * kOgSlotBytes;
+        mx = max(mx, max(ld_shared_u32(slot + off0 + 12) << 1, ld_shared_u32(slot + off1 + 12) << 1));
       }
-      E = max(E, __shfl_xor_sync(0xFFFFFFFFu, E, 1));
-      sp |= __shfl_xor_sync(0xFFFFFFFFu, sp, 1);
-      const int64_t c = w % P.nchunks;
+      uint32_t* em = emax + (it & 1) * 4 * kOgRows;
+      em[grp * kOgRows + r] = mx;
+      __syncwarp();
+      if (lane == 0) mbar_arrive(rowmax_bar(it & 1, qd));
+      if (!mbar_wait(rowmax_bar(it & 1, qd), (it >> 1) & 1u)) {
+        ok = false;
+        break;
+      }
+      mx = max(max(em[r], em[kOgRows + r]), max(em[2 * kOgRows + r], em[3 * kOgRows + r]));
+      const uint32_t bmax = mx >> 17;
+      const int E = (int)(bmax > 1u ? bmax : 1u) - 16383;
+      const uint32_t sp = bmax == 0x7FFFu ? 1u : 0u;
 #pragma unroll 1
-      for (int ks = 0; ks < 2; ++ks, ++q) {
-        uint4 xv = make_uint4(0, 0, 0, 0);
-        if (tid < kOgXBytes / 16)
-          xv = __ldg(reinterpret_cast<const uint4*>(P.xdig + (size_t)(2 * c + ks) * kOgXBytes) + tid);
-        const uint32_t slot = base + (q & 3) * kOgSlotBytes;
-        uint32_t W[8][5];
-#pragma unroll
-        for (int i = 0; i < 8; ++i) {
-          const uint4 v = ld_shared_v4(slot + off[i]);
-          og_window(v.x, v.y, v.z, v.w, E, W[i]);
+      for (int ks = 0; ks < kOgKSteps; ++ks, ++q) {
+        // x's B tile of this k-step was fetched one k-step ahead; fetch the next
+        const uint4 xv = xv_next;
+        if (xcopy) {
+          const bool last = ks == kOgKSteps - 1;
+          const int nc = last ? (cw + 1 == nch ? 0 : cw + 1) : cw;
+          if (!last || w + 1 < w1)
+            xv_next = __ldg(reinterpret_cast<const uint4*>(
+                                P.xdig + (size_t)(kOgKSteps * nc + (last ? 0 : ks + 1)) * kOgXBytes) +
+                            tid);
         }
-        // the operand stage is free once the previous k-step's MMAs completed
-        if (!mbar_wait(free_bar, (q & 1u) ^ 1u)) {
-          ok = false;
-          break;
-        }
-        if (ks == 0 && h == 0) exps[(it & 3) * kOgRows + r] = (E << 1) | (int)sp;
-        og_store_plane<0>(dstage + h * kOgALbo + (r >> 3) * 128 + (r & 7) * 16, W);
-        if (tid < kOgXBytes / 16)
-          st_shared_v4(dstage + kOgPlanes * kOgPlaneBytes + tid * 16, xv.x, xv.y, xv.z, xv.w);
-        fence_proxy_async_smem();
+        const uint32_t slot = base + slot_of(q) * kOgSlotBytes;
+        const uint4 v0 = ld_shared_v4(slot + off0), v1 = ld_shared_v4(slot + off1);
         __syncwarp();
-        if (lane == 0) mbar_arrive(ready_bar);
-      }
-    }
-    if (!ok && lane == 0) atomicExch(P.err, 1);
-  } else if (warp == kOgMmaWarp) {
-    // ---------------- TMA loads of A and MMA issue ----------------
-    if (lane == 0) {
-      auto load_kstep = [&](uint32_t kq) {  // k-step kq of this CTA into slot kq % 4
-        const int64_t w = w0 + kq / 2;
-        const int64_t tile = w / P.nchunks, c = w % P.nchunks;
-        const int col0 = (int)(c * kOgChunk + (kq & 1) * kOgKStep);
-        const uint32_t slot = base + (kq & 3) * kOgSlotBytes, bar = full_bar(kq & 3);
-        mbar_expect_tx(bar, kOgSlotBytes);
-        if (kRowMajor) {
-          for (int hh = 0; hh < 2; ++hh)
-            tma_load_2d(slot + hh * 16384, &tmA, bar, 4 * (col0 + 8 * hh), (int)(tile * kOgRows));
-        } else {
-          for (int g = 0; g < kOgRows / 8; ++g)
-            tma_load_2d(slot + g * 2048, &tmA, bar, 4 * (int)(tile * kOgRows + 8 * g), col0);
+        if (lane == 0) mbar_arrive(empty_bar(slot_of(q)));  // this k-step's elements are in registers
+        uint32_t W[2][5], sg[2], bs[2];
+#pragma unroll
+        for (int i = 0; i < 2; ++i) {
+          const uint4 v = i ? v1 : v0;
+          og_window(v.x, v.y, v.z, v.w, E, W[i]);
+          const uint32_t neg = v.w >> 31;
+          sg[i] = 0x3C003C00u + neg * 0x80008000u;  // (+-1, +-1)
+          bs[i] = 0xE480E480u - neg * 0x80008000u;  // (-+1152, -+1152)
         }
-      };
-      uint32_t issued = 0;
-      for (; issued < nks && issued < (uint32_t)kOgSlots; ++issued) load_kstep(issued);
-      uint32_t q = 0, it = 0;
-      bool any_mma = false;
-      for (int64_t w = w0; w < w1 && ok; ++w, ++it) {
-        const int tb = it & 1;
-        if (!mbar_wait(tempty_bar(tb), ((it >> 1) & 1u) ^ 1u)) {
+        const int st = stage_of(q);
+        if (!mbar_wait(free_bar(st), use_parity(q) ^ 1u)) {  // the MMAs of the stage's last use completed
           ok = false;
           break;
         }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        for (int ks = 0; ks < 2 && ok; ++ks, ++q) {
-          if (!mbar_wait(ready_bar, q & 1u)) {
+        if (ks == 0 && grp == 0) exps[(it % kOgExpSlots) * kOgRows + r] = (E << 1) | (int)sp;
+        og_store_pairs<0>(tlane + st * kOgStageCols, W, sg, bs);
+        if (xcopy) {
+          st_shared_v4(xstage0 + st * kOgXBytes + tid * 16, xv.x, xv.y, xv.z, xv.w);
+          fence_proxy_async_smem();
+        }
+        tmem_st_wait();
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncwarp();
+        if (lane == 0) mbar_arrive(ready_bar(st));
+      }
+      if (++cw == nch) cw = 0;
+    }
+    if (!ok && lane == 0) atomicExch(P.err, 1);
+  } else if (warp == kOgLoadWarp) {
+    // ---------------- TMA loads of A into the slot ring ----------------
+    if (lane == 0) {
+      // TMA cursor: tile, chunk and k-step of the next load, kept by counting
+      const int nch = (int)P.nchunks;
+      int ld_tile = (int)(w0 / P.nchunks), ld_c = (int)(w0 % P.nchunks), ld_ks = 0;
+      auto load_kstep = [&](uint32_t kq) {  // k-step kq of this CTA (loaded in order) into its slot
+        const int64_t tile = ld_tile;
+        const int col0 = ld_c * kOgChunk + ld_ks * kOgKStep;
+        if (++ld_ks == kOgKSteps) {
+          ld_ks = 0;
+          if (++ld_c == nch) {
+            ld_c = 0;
+            ++ld_tile;
+          }
+        }
+        const uint32_t slot = base + slot_of(kq) * kOgSlotBytes, bar = full_bar(slot_of(kq));
+        mbar_expect_tx(bar, kOgSlotBytes);
+        if (kRowMajor) {
+          tma_load_2d(slot, &tmA, bar, 4 * col0, (int)(tile * kOgRows));
+        } else {
+          for (int g = 0; g < kOgRows / 8; ++g)
+            tma_load_2d(slot + g * 1024, &tmA, bar, 4 * (int)(tile * kOgRows + 8 * g), col0);
+        }
+      };
+      uint32_t issued = 0;
+      for (; issued < nks && ok; ++issued) {
+        // the split warps released this slot's previous k-step
+        if (!mbar_wait(empty_bar(slot_of(issued)), fill_parity(issued) ^ 1u)) {
+          ok = false;
+          break;
+        }
+        load_kstep(issued);
+      }
+      if (!ok) {
+        atomicExch(P.err, 1);
+        // copies still in flight: the last (up to) kOgSlots issued
+        for (uint32_t j = (issued > (uint32_t)kOgSlots ? issued - kOgSlots : 0); j < issued; ++j)
+          mbar_wait(full_bar(slot_of(j)), fill_parity(j));
+      }
+    }
+  } else if (warp == kOgMmaWarp) {
+    // ---------------- MMA issue ----------------
+    if (lane == 0) {
+      const uint64_t db0 = smem_desc_noswizzle(xstage0 + 16 * 16, kOgXLbo, 128);
+      uint32_t q = 0, it = 0;
+      bool any_mma = false;
+      for (int64_t w = w0; w < w1 && ok; ++w, ++it) {
+        const int tb = it % kOgAccBufs;
+        if (!mbar_wait(tempty_bar(tb), ((it / kOgAccBufs) & 1u) ^ 1u)) {
+          ok = false;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        for (int ks = 0; ks < kOgKSteps && ok; ++ks, ++q) {
+          const int st = stage_of(q);
+          if (!mbar_wait(ready_bar(st), use_parity(q))) {
             ok = false;
             break;
           }
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-          if (ks == 0) mbar_arrive(exp_bar(it & 3));  // this item's row exponents are written
-          // slot q % 4 has been read: refill it with k-step q + 4
-          if (issued < nks) load_kstep(issued++);
-          const uint32_t xb = dstage + kOgPlanes * kOgPlaneBytes;
+          if (ks == 0) mbar_arrive(exp_bar(it % kOgExpSlots));  // this item's row exponents are written
+          const uint32_t ta = tmem + kOgAccCols + st * kOgStageCols;
+          // B of pair pp: 16 - 2pp rows into the stage's tile (the descriptor
+          // address field counts 16-byte units)
+          const uint64_t dbs = db0 + (uint64_t)(st * (kOgXBytes / 16));
 #pragma unroll
-          for (int t = 0; t < kOgPlanes; ++t) {
-            const uint64_t da = smem_desc_noswizzle(dstage + t * kOgPlaneBytes, kOgALbo, 128);
-            const uint64_t db = smem_desc_noswizzle(xb + (kOgXBase - t) * 16, kOgXLbo, 128);
-            mma_f16kind(tmem + (uint32_t)(tb * 32), da, db, kOgIdesc, (ks | t) ? 1u : 0u);
-          }
+          for (int pp = 0; pp < kOgPairs; ++pp)
+            mma_f16kind_ta(tmem + (uint32_t)(tb * 32), ta + pp * kOgTileCols, dbs - (uint64_t)(2 * pp), kOgIdesc,
+                           (ks | pp) ? 1u : 0u);
           any_mma = true;
-          mma_commit(free_bar);
+          mma_commit(free_bar(st));
         }
         if (!ok) break;
         mma_commit(tfull_bar(tb));
@@ -360,9 +455,6 @@ __global__ void __launch_bounds__(kOgThreads, 1)
           mma_commit(drain_bar);
           mbar_wait(drain_bar, 0);
         }
-        // copies still in flight: the last (up to) four issued
-        for (uint32_t j = (issued > (uint32_t)kOgSlots ? issued - kOgSlots : 0); j < issued; ++j)
-          mbar_wait(full_bar(j & 3), (j >> 2) & 1u);
       }
     }
   } else {
@@ -384,8 +476,14 @@ __global__ void __launch_bounds__(kOgThreads, 1)
       o.pad = 0;
     };
     uint32_t it = 0;
+    const int chunks = (int)P.nchunks;
+    int64_t tile = w0 / P.nchunks;
+    int c = (int)(w0 % P.nchunks) - 1;
     for (int64_t w = w0; w < w1 && ok; ++w, ++it) {
-      const int64_t tile = w / P.nchunks, c = w % P.nchunks;
+      if (++c == chunks) {
+        c = 0;
+        ++tile;
+      }
       if (tile != cur) {
         if (cur >= 0) flush(cur);
         wacc_init(acc);
@@ -393,31 +491,33 @@ __global__ void __launch_bounds__(kOgThreads, 1)
         nch = spec = 0;
         cur = tile;
       }
-      const int tb = it & 1;
-      if (!mbar_wait(exp_bar(it & 3), (it >> 2) & 1u)) {
+      const int F = __ldg(P.xexp + c);  // read early: its latency overlaps the waits
+      const int tb = it % kOgAccBufs;
+      if (!mbar_wait(exp_bar(it % kOgExpSlots), (it / kOgExpSlots) & 1u)) {
         ok = false;
         break;
       }
-      const int ev = exps[(it & 3) * kOgRows + rit];
-      if (!mbar_wait(tfull_bar(tb), (it >> 1) & 1u)) {
+      const int ev = exps[(it % kOgExpSlots) * kOgRows + rit];
+      if (!mbar_wait(tfull_bar(tb), (it / kOgAccBufs) & 1u)) {
         ok = false;
         break;
       }
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      uint32_t rr[32];
-      tmem_ld32(tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(tb * 32), rr);
+      int32_t D[kOgDiags];
+      {
+        uint32_t rr[kOgDiags];
+        tmem_ld20(tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(tb * 32), rr);
+#pragma unroll
+        for (int g = 0; g < kOgDiags; ++g) D[g] = __float2int_rn(__uint_as_float(rr[g]));
+      }
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
       __syncwarp();
       if (lane == 0) mbar_arrive(tempty_bar(tb));
       const int E = ev >> 1;
       spec |= (uint32_t)ev & 1u;
-      const int F = __ldg(P.xexp + c);
       if (F == kOgXSpecial) {
         spec = 1;
       } else if (F != kOgNoExp) {
-        int32_t D[kOgDiags];
-#pragma unroll
-        for (int g = 0; g < kOgDiags; ++g) D[g] = __float2int_rn(__uint_as_float(rr[g]));
         uint32_t T[6];
         og_fold(D, T);
         og_wacc_add(acc, T, E + F - kOgFoldShift);
@@ -498,7 +598,7 @@ static OgLayout og_layout(int64_t m, int64_t n) {
     if (k > L.segs) L.segs = (int)k;
   }
   L.xdig = 0;
-  L.xexp = L.xdig + og_round256((size_t)L.nchunks * 2 * kOgXBytes);
+  L.xexp = L.xdig + og_round256((size_t)L.nchunks * kOgKSteps * kOgXBytes);
   L.err = L.xexp + og_round256((size_t)L.nchunks * 4);
   L.part = L.err + 256;
   L.total = L.part + og_round256((size_t)L.tiles * L.segs * kOgRows * sizeof(OgPartial));
@@ -523,7 +623,7 @@ cudaError_t launch_gemv_ozaki(int64_t m, int64_t n, q128 alpha, MatView A, const
     const int64_t inner = row_major ? n : m, outer = row_major ? m : n;
     cuuint64_t dims[2] = {(cuuint64_t)(4 * inner), (cuuint64_t)outer};
     cuuint64_t strides[1] = {(cuuint64_t)ld * 16};
-    cuuint32_t box[2] = {32, row_major ? (cuuint32_t)kOgRows : (cuuint32_t)kOgKStep};
+    cuuint32_t box[2] = {32, row_major ? (cuuint32_t)kOgRows : (cuuint32_t)kOgKStep};  // 128 B x rows / columns
     cuuint32_t estr[2] = {1, 1};
     if (fn(&map, CU_TENSOR_MAP_DATA_TYPE_UINT32, 2, const_cast<q128*>(A.p), dims, strides, box, estr,
            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,

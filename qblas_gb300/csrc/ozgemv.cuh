@@ -5,12 +5,13 @@
 // chunk, row i's elements are scaled by their largest lead-bit exponent E
 // (subnormals and zeros counted as -16382) and x's by its largest F, and
 // each element a becomes a 144-bit fixed-point integer
-//   V = sign(a) * floor(|a| / 2^(E - 141)),   |V| < 2^142,
+//   V = floor(|a| / 2^(E - 141)),   V < 2^142,
 // cut into 18 balanced 8-bit digits d_0 (most significant) .. d_17:
-//   V = sum_t d_t 256^(17 - t),   d_t in [-128, 128).
-// The digits are the bytes of W = V + R, R = sum_t 128 * 256^t, minus 128:
-// a digit costs one byte select, and as an fp16 value it is
-// (1024 + byte) - 1152, exact.
+//   V = sum_t d_t 256^(17 - t),   d_t in [-128, 128),
+// and a's digits are sign(a) * d_t.  The d_t are the bytes of W = V + R,
+// R = sum_t 128 * 256^t, minus 128: as fp16 values a digit is
+// sign * ((1024 + byte) - 1152), one byte select and one fused multiply-add
+// of a pair of halves, exact.
 //
 // Digit products are exact in fp16 x fp16 -> fp32 (|d_t d_u| <= 2^14), and a
 // chunk's diagonal sums D_g = sum_j sum_{t+u=g} d_t(a_j) d_u(x_j) stay below
@@ -44,66 +45,55 @@ QB_HD int og_lead_top(uint32_t top) {
 QB_HD bool og_special_top(uint32_t top) { return ((top >> 16) & 0x7FFFu) == 0x7FFFu; }
 
 // W = R + V for the element with 32-bit words w0 (least significant) .. w3
-// and a chunk exponent E >= its lead exponent.  W < 2^144: five words,
-// W[4] < 2^16.  NaN and infinity give V = 0 (their rows are recomputed).
-// Branch-free (lanes of a warp hold elements of different exponents): the
-// word part of the shift is three mask-select levels.
+// and a chunk exponent E >= its lead exponent: V = (M << 32) >> s with
+// s = E - lead + 3 (V = 0 from s = 160 on), where M is the 113-bit
+// significand (hidden bit set iff the exponent field is nonzero).
+// W < 2^144: five words, W[4] < 2^16.  Branch-free (lanes of a warp hold
+// elements of different exponents): the word part of the shift is three
+// mask-select levels.  NaN and infinity give bounded garbage (their rows
+// are recomputed exactly).
 QB_HD void og_window(uint32_t w0, uint32_t w1, uint32_t w2, uint32_t w3, int E, uint32_t (&W)[5]) {
   const uint32_t be = (w3 >> 16) & 0x7FFFu;
-  const uint32_t fin = be != 0x7FFFu ? 0xFFFFFFFFu : 0u;
-  const uint32_t m3 = ((w3 & 0xFFFFu) | (be != 0 ? 0x10000u : 0u)) & fin;
-  const uint32_t m0 = w0 & fin, m1 = w1 & fin, m2 = w2 & fin;
-  const int delta = E - ((int)(be ? be : 1u) - 16383);  // >= 0
-  const uint32_t keep = delta < 160 ? 0xFFFFFFFFu : 0u;
-  const int d = delta < 160 ? delta : 159;
-  // X = M << 29 (M < 2^113, so X < 2^142), then V = X >> delta
-  const uint32_t x0 = m0 << 29, x1 = fshl32(m0, m1, 29), x2 = fshl32(m1, m2, 29), x3 = fshl32(m2, m3, 29),
-                 x4 = m3 >> 3;
-  const uint32_t b = (uint32_t)d & 31u;
-  uint32_t y0 = fshr32(x0, x1, b), y1 = fshr32(x1, x2, b), y2 = fshr32(x2, x3, b), y3 = fshr32(x3, x4, b),
-           y4 = x4 >> b;
-  const uint32_t k = (uint32_t)d >> 5;
-  const uint32_t s4 = 0u - ((k >> 2) & 1u), s2 = 0u - ((k >> 1) & 1u), s1 = 0u - (k & 1u);
-  y0 = (y4 & s4) | (y0 & ~s4);
-  y1 &= ~s4;
-  y2 &= ~s4;
-  y3 &= ~s4;
-  y4 &= ~s4;
-  y0 = (y2 & s2) | (y0 & ~s2);
-  y1 = (y3 & s2) | (y1 & ~s2);
-  y2 = (y4 & s2) | (y2 & ~s2);
-  y3 &= ~s2;
-  y4 &= ~s2;
-  y0 = (y1 & s1) | (y0 & ~s1);
-  y1 = (y2 & s1) | (y1 & ~s1);
-  y2 = (y3 & s1) | (y2 & ~s1);
-  y3 = (y4 & s1) | (y3 & ~s1);
-  y4 &= ~s1;
-  // W = R + (sign ? -V : V) = R + (V ^ mask) + sign  (mod 2^160)
-  const uint32_t mask = (0u - (w3 >> 31)) & keep;
-  y0 = (y0 & keep) ^ mask;
-  y1 = (y1 & keep) ^ mask;
-  y2 = (y2 & keep) ^ mask;
-  y3 = (y3 & keep) ^ mask;
-  y4 = (y4 & keep) ^ mask;
+  const uint32_t hb = be + 0xFFFFu;  // bit 16 set iff be != 0 (hb < 2^17)
+  const uint32_t m3 = (w3 & 0xFFFFu) | (hb & 0x10000u);
+  int s = E + 16386 - (int)(be > 1u ? be : 1u);  // >= 3: E is at least the element's lead exponent
+  s = s < 160 ? s : 160;
+  const uint32_t b = (uint32_t)s & 31u, k = (uint32_t)s >> 5;
+  uint32_t y0 = fshr32(0u, w0, b), y1 = fshr32(w0, w1, b), y2 = fshr32(w1, w2, b), y3 = fshr32(w2, m3, b),
+           y4 = m3 >> b;
+  // word shift by k = 0..5 in three select levels (selects, not branches)
+  const bool k4 = (k & 4u) != 0, k2 = (k & 2u) != 0, k1 = (k & 1u) != 0;
+  y0 = k4 ? y4 : y0;
+  y1 = k4 ? 0u : y1;
+  y2 = k4 ? 0u : y2;
+  y3 = k4 ? 0u : y3;
+  y4 = k4 ? 0u : y4;
+  y0 = k2 ? y2 : y0;
+  y1 = k2 ? y3 : y1;
+  y2 = k2 ? y4 : y2;
+  y3 = k2 ? 0u : y3;
+  y4 = k2 ? 0u : y4;
+  y0 = k1 ? y1 : y0;
+  y1 = k1 ? y2 : y1;
+  y2 = k1 ? y3 : y2;
+  y3 = k1 ? y4 : y3;
+  y4 = k1 ? 0u : y4;
 #if defined(__CUDA_ARCH__)
   uint32_t r0, r1, r2, r3, r4;
-  asm("{\n\t.reg .u32 t;\n\t"
-      "add.cc.u32  t, %10, %10;\n\t"  // carry-in = sign (mask + mask overflows iff mask != 0)
-      "addc.cc.u32 %0, %5, 0x80808080;\n\t"
+  asm("add.cc.u32  %0, %5, 0x80808080;\n\t"
       "addc.cc.u32 %1, %6, 0x80808080;\n\t"
       "addc.cc.u32 %2, %7, 0x80808080;\n\t"
       "addc.cc.u32 %3, %8, 0x80808080;\n\t"
-      "addc.u32    %4, %9, 0x8080;\n\t}"
+      "addc.u32    %4, %9, 0x8080;"
       : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3), "=r"(r4)
-      : "r"(y0), "r"(y1), "r"(y2), "r"(y3), "r"(y4), "r"(mask));
+      : "r"(y0), "r"(y1), "r"(y2), "r"(y3), "r"(y4));
   W[0] = r0;
   W[1] = r1;
   W[2] = r2;
   W[3] = r3;
   W[4] = r4 & 0xFFFFu;
 #else
-  uint64_t t = (uint64_t)0x80808080u + y0 + (mask & 1u);
+  uint64_t t = (uint64_t)0x80808080u + y0;
   W[0] = (uint32_t)t;
   t = (t >> 32) + 0x80808080u + y1;
   W[1] = (uint32_t)t;
@@ -116,10 +106,12 @@ QB_HD void og_window(uint32_t w0, uint32_t w1, uint32_t w2, uint32_t w3, int E, 
 #endif
 }
 
-// Digit t (0 = most significant) of a window: byte 17 - t of W, minus 128.
-QB_HD int og_digit(const uint32_t (&W)[5], int t) {
+// Digit t (0 = most significant) of an element with window W and sign bit
+// neg: sign * (byte 17 - t of W, minus 128).
+QB_HD int og_digit(const uint32_t (&W)[5], int t, uint32_t neg) {
   const int beta = 17 - t;
-  return (int)((W[beta >> 2] >> (8 * (beta & 3))) & 0xFFu) - 128;
+  const int d = (int)((W[beta >> 2] >> (8 * (beta & 3))) & 0xFFu) - 128;
+  return neg ? -d : d;
 }
 
 // T = sum_{g<20} D_g 256^(19 - g) as six little-endian 32-bit words, two's

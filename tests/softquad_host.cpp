@@ -147,7 +147,9 @@ void sq_og_chunk(int n, const q128* a, const q128* x, int32_t* EF, int64_t* D, u
                   F == qb::kOgNoExp ? -16382 : F, wx);
     for (int t = 0; t < qb::kOgPlanes; ++t)
       for (int u = 0; u < qb::kOgPlanes; ++u)
-        if (t + u < 32) D[t + u] += (int64_t)qb::og_digit(wa, t) * qb::og_digit(wx, u);
+        if (t + u < 32)
+          D[t + u] += (int64_t)qb::og_digit(wa, t, (uint32_t)(a[j].hi >> 63)) *
+                      qb::og_digit(wx, u, (uint32_t)(x[j].hi >> 63));
   }
   int32_t D32[qb::kOgDiags];
   for (int g = 0; g < qb::kOgDiags; ++g) D32[g] = (int32_t)D[g];
