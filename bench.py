@@ -270,6 +270,7 @@ NCU_TRAFFIC = {
     "qgemm4096": (2 * (9.84e9 + 1.01e9), "profiles/ozaki_mma_kernel_4096_traffic.md"),  # 15 x 9 bit, 2 passes
     "qdot26": (2.147608e9 + 4.091e6, "profiles/qdot_partial_kernel_n2p26.md"),
     "qgemv8192": (1.074079e9 + 1.8140e7, "profiles/qgemv_lane_kernel_8192.md"),
+    "qgemv8192_ozaki": (1.086090e9 + 3.979e6, "profiles/og_gemv_kernel_8192.md"),
 }
 
 
@@ -578,12 +579,15 @@ def main():
         if not args.no_secondary and size == 4096:
             del W
             torch.cuda.empty_cache()
-            for name, mk in [("qgemv8192", lambda: Qgemv(torch, 8192, 8192, 11 + rank)),
-                             ("qdot26", lambda: Qdot(torch, 1 << 26, 13 + rank))]:
+            # qgemv by both methods (identical, correctly rounded results) and qdot
+            for name, mk, meth in [("qgemv8192", lambda: Qgemv(torch, 8192, 8192, 11 + rank), 1),
+                                   ("qgemv8192_ozaki", lambda: Qgemv(torch, 8192, 8192, 11 + rank), 2),
+                                   ("qdot26", lambda: Qdot(torch, 1 << 26, 13 + rank), 1)]:
+                api.set_method(meth)
                 S = mk()
                 ms2 = time_steps(torch, S.step, args.steps, 3, dist) / args.steps
                 secondary[name] = {"value": round(S.bytes() / (ms2 * 1e-3) / 1e9, 1), "unit": "GB/s",
-                                   "ms_per_step": round(ms2, 4),
+                                   "ms_per_step": round(ms2, 4), "method": "ozaki" if meth == 2 else "softfloat",
                                    "roofline": hbm_roofline(pk, pk_src, S.bytes(), ms2, name)}
                 del S
                 torch.cuda.empty_cache()
@@ -601,11 +605,16 @@ def main():
         ms_step = ms / args.steps
         value = whole_job_rate(W.bytes(), world, ms_step * 1e-3) / 1e9
         metric, unit = "qgemv binary128 GB/s (8192^2 row-major)", "GB/s"
-        launches = 4 * args.steps  # x unpack, thread-per-row kernel, chunk merge, exact pass (returns at once)
-        roof = hbm_roofline(pk, pk_src, W.bytes(), ms_step, wl)
-        e2e, dtype = None, "u32 (soft-float integer limbs)"
+        # soft-float: x unpack, thread-per-row kernel, chunk merge, exact pass;
+        # Ozaki: x digits, split + tensor-core kernel, row finish, exact pass
+        # (the exact pass returns at once when every row was certified)
+        launches = 4 * args.steps
+        roof = hbm_roofline(pk, pk_src, W.bytes(), ms_step, wl + ("_ozaki" if method == 2 else ""))
+        e2e = None
+        dtype = ("fp16 digits x fp16 digits -> fp32 on tcgen05, u32 integer limbs" if method == 2
+                 else "u32 (soft-float integer limbs)")
         cfg = {"workload": "qgemv 8192x8192 row-major alpha=1 beta=0, wide-exponent values",
-               "l2": "inputs larger than L2 (no flush)"}
+               "method": args.method, "l2": "inputs larger than L2 (no flush)"}
     else:
         W = Qdot(torch, 1 << 26, seed=13 + rank)
         with ClockSampler(local) as clk:
