@@ -160,11 +160,13 @@ __global__ void __launch_bounds__(kColThreads)
 // Ozaki bound was too loose; the rest (and every row when !try_wide: the
 // soft-float kernels already tried the wide accumulator) are summed exactly
 // by a Kulisch accumulator.
-__global__ void __launch_bounds__(256)
+constexpr int kExactThreads = 512;
+
+__global__ void __launch_bounds__(kExactThreads)
     qgemv_exact_kernel(const RowList* __restrict__ L, int64_t n, MatView A, const q128* __restrict__ x,
                        int64_t incx, q128 alpha, q128 beta, q128* __restrict__ y, int64_t incy, int try_wide) {
   __shared__ KulischBlock K;
-  __shared__ wacc sm[8];
+  __shared__ wacc sm[kExactThreads / 32];
   __shared__ int done;
   const unsigned cnt = *reinterpret_cast<const volatile unsigned*>(&L->count);
   for (unsigned t = blockIdx.x; t < cnt; t += gridDim.x) {
@@ -173,12 +175,24 @@ __global__ void __launch_bounds__(256)
     if (try_wide) {
       wacc acc;
       wacc_init(acc);
-      for (int64_t j = threadIdx.x; j < n; j += blockDim.x)
-        wacc_add_product(acc, qop_unpack(ld_cached(A.p + i * A.si + j * A.sj)), qop_unpack(ld_cached(x + j * incx)));
+      const q128* Ar = A.p + i * A.si;
+      const int64_t step = blockDim.x;
+      int64_t j = threadIdx.x;
+      for (; j + 3 * step < n; j += 4 * step) {  // four element pairs in flight
+        q128 a0 = ld_cached(Ar + j * A.sj), a1 = ld_cached(Ar + (j + step) * A.sj);
+        q128 a2 = ld_cached(Ar + (j + 2 * step) * A.sj), a3 = ld_cached(Ar + (j + 3 * step) * A.sj);
+        q128 x0 = ld_cached(x + j * incx), x1 = ld_cached(x + (j + step) * incx);
+        q128 x2 = ld_cached(x + (j + 2 * step) * incx), x3 = ld_cached(x + (j + 3 * step) * incx);
+        wacc_add_product(acc, qop_unpack(a0), qop_unpack(x0));
+        wacc_add_product(acc, qop_unpack(a1), qop_unpack(x1));
+        wacc_add_product(acc, qop_unpack(a2), qop_unpack(x2));
+        wacc_add_product(acc, qop_unpack(a3), qop_unpack(x3));
+      }
+      for (; j < n; j += step) wacc_add_product(acc, qop_unpack(ld_cached(Ar + j * A.sj)), qop_unpack(ld_cached(x + j * incx)));
       wacc_block_reduce(acc, sm);
       if (threadIdx.x == 0) {
         q128 r;
-        done = wacc_round_certified(acc, 2 * (uint64_t)n + 3 * 256, r);
+        done = wacc_round_certified(acc, 2 * (uint64_t)n + 3 * kExactThreads, r);
         if (done) *yp = q_epilogue(alpha, r, beta, *yp);
       }
       __syncthreads();
@@ -216,8 +230,8 @@ void gemv_count_exact_rows(unsigned* host_pinned) { g_exact_rows = host_pinned; 
 // optional record of how many there were.
 static cudaError_t launch_exact_rows(RowList* L, int64_t n, MatView A, const q128* x, int64_t incx, q128 alpha,
                                      q128 beta, q128* y, int64_t incy, cudaStream_t s, bool try_wide) {
-  qgemv_exact_kernel<<<(unsigned)device_sm_count(), 256, 0, s>>>(L, n, A, x, incx, alpha, beta, y, incy,
-                                                                 try_wide ? 1 : 0);
+  qgemv_exact_kernel<<<(unsigned)device_sm_count(), kExactThreads, 0, s>>>(L, n, A, x, incx, alpha, beta, y,
+                                                                           incy, try_wide ? 1 : 0);
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess && g_exact_rows)
     e = cudaMemcpyAsync(g_exact_rows, &L->count, sizeof(unsigned), cudaMemcpyDeviceToHost, s);

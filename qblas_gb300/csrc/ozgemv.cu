@@ -121,15 +121,18 @@ QB_HD int64_t og_cta_of(int64_t work, int64_t G, int64_t X) { return ((X + 1) * 
 // ---------------------------------------------------------------------------
 // x digits
 // ---------------------------------------------------------------------------
-// One warp per chunk of 32 elements of x: F_c, and the B operand of each
-// k-step (8 columns): row rho, K = 2 * (column % 8) + tt holds x's digit
-// rho - 16 - tt (zero outside 0..17), K-major core matrices (LBO 768).
-__global__ void __launch_bounds__(256)
+// One warp (one block) per chunk of 32 elements of x: F_c, and the B operand
+// of each k-step (8 columns): row rho, K = 2 * (column % 8) + tt holds x's
+// digit rho - 16 - tt (zero outside 0..17), K-major core matrices (LBO 768);
+// the chunk's four tiles are built in shared memory and written with
+// 16-byte stores.
+__global__ void __launch_bounds__(32)
     og_x_split_kernel(int64_t n, int64_t nchunks, const q128* __restrict__ x, int64_t incx,
                       uint8_t* __restrict__ xdig, int32_t* __restrict__ xexp, RowList* __restrict__ L) {
+  __shared__ __align__(16) __half tiles[kOgKSteps * kOgXBytes / 2];
   if (blockIdx.x == 0 && threadIdx.x == 0) L->count = 0;
-  const int lane = threadIdx.x & 31;
-  const int64_t c = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x;
+  const int64_t c = blockIdx.x;
   if (c >= nchunks) return;
   const int64_t j = c * kOgChunk + lane;
   q128 v;
@@ -146,16 +149,20 @@ __global__ void __launch_bounds__(256)
   uint32_t W[5];
   og_window((uint32_t)v.lo, (uint32_t)(v.lo >> 32), (uint32_t)v.hi, top, f == kOgNoExp ? -16382 : f, W);
   const uint32_t neg = top >> 31;
-  uint8_t* tile = xdig + (size_t)(kOgKSteps * c + (lane >> 3)) * kOgXBytes;
+  __half* tile = tiles + (lane >> 3) * (kOgXBytes / 2);
   for (int tt = 0; tt < 2; ++tt) {
     const int kk = 2 * (lane & 7) + tt;
-    __half* col = reinterpret_cast<__half*>(tile + (kk >> 3) * kOgXLbo + (kk & 7) * 2);
+    __half* col = tile + (kk >> 3) * (kOgXLbo / 2) + (kk & 7);
     for (int rho = 0; rho < kOgXRows; ++rho) {
       const int u = rho - 16 - tt;
       const int d = (u >= 0 && u < kOgPlanes) ? og_digit(W, u, neg) : 0;
       col[rho * 8] = __int2half_rn(d);  // rows are 16 bytes apart
     }
   }
+  __syncwarp();
+  const uint4* src = reinterpret_cast<const uint4*>(tiles);
+  uint4* dst = reinterpret_cast<uint4*>(xdig + (size_t)(kOgKSteps * c) * kOgXBytes);
+  for (int k = lane; k < kOgKSteps * kOgXBytes / 16; k += 32) dst[k] = src[k];
 }
 
 // ---------------------------------------------------------------------------
@@ -541,7 +548,7 @@ __global__ void __launch_bounds__(kOgThreads, 1)
 // ---------------------------------------------------------------------------
 // Finish
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(64)
     og_finish_kernel(int64_t m, int64_t nchunks, int64_t work, int64_t G, int segs,
                      const OgPartial* __restrict__ part, const int* __restrict__ err, q128 alpha, q128 beta,
                      q128* __restrict__ y, int64_t incy, RowList* __restrict__ L) {
@@ -645,12 +652,9 @@ cudaError_t launch_gemv_ozaki(int64_t m, int64_t n, q128 alpha, MatView A, const
   P.err = reinterpret_cast<int*>(base + Lo.err);
   cudaError_t e = cudaMemsetAsync(P.err, 0, sizeof(int), s);
   if (e != cudaSuccess) return e;
-  {
-    const int64_t warps = Lo.nchunks, per_block = 8;
-    og_x_split_kernel<<<(unsigned)((warps + per_block - 1) / per_block), 256, 0, s>>>(
-        n, Lo.nchunks, x, incx, const_cast<uint8_t*>(P.xdig), const_cast<int32_t*>(P.xexp), list);
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  }
+  og_x_split_kernel<<<(unsigned)Lo.nchunks, 32, 0, s>>>(n, Lo.nchunks, x, incx, const_cast<uint8_t*>(P.xdig),
+                                                        const_cast<int32_t*>(P.xexp), list);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
   static bool attr = false;
   if (!attr) {
     if ((e = cudaFuncSetAttribute(og_gemv_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -665,7 +669,7 @@ cudaError_t launch_gemv_ozaki(int64_t m, int64_t n, q128 alpha, MatView A, const
   else
     og_gemv_kernel<false><<<(unsigned)Lo.G, kOgThreads, kOgSmem, s>>>(map, P);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  og_finish_kernel<<<(unsigned)((m + 127) / 128), 128, 0, s>>>(m, Lo.nchunks, Lo.work, Lo.G, Lo.segs, P.part,
+  og_finish_kernel<<<(unsigned)((m + 63) / 64), 64, 0, s>>>(m, Lo.nchunks, Lo.work, Lo.G, Lo.segs, P.part,
                                                               P.err, alpha, beta, y, incy, list);
   return cudaGetLastError();
 }
