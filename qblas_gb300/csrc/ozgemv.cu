@@ -114,10 +114,6 @@ struct OgParams {
   int* err;
 };
 
-// First item of CTA b's range, and the CTA whose range holds item X.
-QB_HD int64_t og_range_begin(int64_t work, int64_t G, int64_t b) { return work * b / G; }
-QB_HD int64_t og_cta_of(int64_t work, int64_t G, int64_t X) { return ((X + 1) * G + work - 1) / work - 1; }
-
 // ---------------------------------------------------------------------------
 // x digits
 // ---------------------------------------------------------------------------

@@ -35,6 +35,12 @@ constexpr int kOgFoldShift = 162;   // chunk value = T * 2^(E + F - 162)
 constexpr int kOgErrShift = 133;    // |chunk error| < 2^(E + F - 133)
 constexpr int kOgNoExp = -(1 << 20);  // x chunk without a nonzero element
 
+// Balanced ranges of (row tile, chunk) items over G CTAs: CTA b takes items
+// [og_range_begin(b), og_range_begin(b + 1)); og_cta_of(X) is the CTA whose
+// range holds item X (the smallest b with og_range_begin(b + 1) > X).
+QB_HD int64_t og_range_begin(int64_t work, int64_t G, int64_t b) { return work * b / G; }
+QB_HD int64_t og_cta_of(int64_t work, int64_t G, int64_t X) { return ((X + 1) * G + work - 1) / work - 1; }
+
 // Lead-bit exponent of an element from its top 32 bits (sign, exponent,
 // fraction bits 111..96); zeros and subnormals give -16382 (an upper bound).
 QB_HD int og_lead_top(uint32_t top) {

@@ -159,6 +159,12 @@ void sq_og_chunk(int n, const q128* a, const q128* x, int32_t* EF, int64_t* D, u
   EF[0] = E;
   EF[1] = F;
 }
+// The work partition of the Ozaki qgemv kernel: begin[b] for b = 0..G and
+// cta[X] for every item X < work.
+void sq_og_partition(int64_t work, int64_t G, int64_t* begin, int64_t* cta) {
+  for (int64_t b = 0; b <= G; ++b) begin[b] = qb::og_range_begin(work, G, b);
+  for (int64_t X = 0; X < work; ++X) cta[X] = qb::og_cta_of(work, G, X);
+}
 // A whole row the way the kernels treat it (one partial, no merges):
 // out = the certified rounding, returns 1 when certified, 0 otherwise.
 int sq_og_row(int64_t n, const q128* a, const q128* x, q128* out) {

@@ -155,3 +155,54 @@ def test_certified_rows(qlib, O, ozaki, kind):
     rows = np.arange(0, m, 61)
     R, _, _ = O.exact_gemv(m, n, A, n, 1, x, 1)
     assert Q.same_bits(got[rows], R[rows]).all()
+
+
+@pytest.mark.parametrize("cond", [1e10, 1e20, 1e30, 1e40])
+def test_ozgemv_gendot_rows(qlib, O, ozaki, cond):
+    """A row of prescribed condition (GenDot) among random rows: the Ozaki bound
+    cannot certify heavy cancellation, so that row goes to the exact pass."""
+    n, m = 8192, 300
+    X, Y = O.gendot_batch(n, np.array([cond]), np.array([77], dtype=np.uint64))
+    rng = G.rng_for(160)
+    A = G.uniform_full(rng, m * n).reshape(m, n, 2)
+    A[5] = X.reshape(n, 2)
+    A = A.reshape(-1, 2)
+    x = np.ascontiguousarray(Y.reshape(n, 2))
+    api.debug_count_exact_rows(True)
+    try:
+        got, exp = run(O, "R", "N", m, n, A, n, x, 1, G.uniform_full(rng, m), 1, 1.0, 0.0)
+        listed = api.debug_exact_rows()
+    finally:
+        api.debug_count_exact_rows(False)
+    assert Q.same_bits(got, exp).all()
+    if cond >= 1e30:
+        assert listed >= 1
+
+
+def test_ozgemv_no_memory(qlib, O, ozaki, torch_cuda):
+    """An injected allocation failure: status NO_MEMORY, y untouched, then a
+    normal call."""
+    import ctypes
+
+    from conftest import to_dev, to_host
+    torch = torch_cuda
+    rng = G.rng_for(161)
+    m, n = 256, 640
+    A, x, y0 = G.uniform_full(rng, m * n), G.uniform_full(rng, n), G.uniform_full(rng, m)
+    dA, dx, dy = to_dev(torch, A), to_dev(torch, x), to_dev(torch, y0)
+    s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    one, zero = Q.scalar(1.0), Q.scalar(0.0)
+    P = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    D = lambda t: ctypes.c_void_p(t.data_ptr())
+    qlib.quadblas_debug_fail_allocations(1)
+    try:
+        rc = qlib.quadblas_qgemv_dev(b"R", b"N", m, n, P(one), D(dA), n, D(dx), 1, P(zero), D(dy), 1, s)
+    finally:
+        qlib.quadblas_debug_fail_allocations(0)
+    assert rc == 3
+    torch.cuda.synchronize()
+    assert Q.same_bits(to_host(dy), y0).all()
+    assert qlib.quadblas_qgemv_dev(b"R", b"N", m, n, P(one), D(dA), n, D(dx), 1, P(zero), D(dy), 1, s) == 0
+    torch.cuda.synchronize()
+    R, _, _ = O.exact_gemv(m, n, A, n, 1, x, 1)
+    assert Q.same_bits(to_host(dy), R).all()

@@ -6,7 +6,10 @@ host) against exact rationals:
 * chunk: the diagonal sums stay below 2^24 (exact in fp32), T is
   sum_{g<20} D_g 256^(19-g), and |T 2^(E+F-162) - sum_j a_j x_j| < 2^(E+F-133);
 * row: every certified rounding equals the correctly rounded exact sum (the
-  exact oracle), and wide-exponent rows are almost all certified.
+  exact oracle), and wide-exponent rows are almost all certified;
+* partition: the CTAs' item ranges tile [0, work) in order and og_cta_of
+  names the range that holds each item (row partials are written and read
+  by that index).
 """
 import ctypes
 from fractions import Fraction
@@ -136,3 +139,14 @@ def test_row_zeros_and_specials(sq, O):
     a[7] = Q.as_quad(np.array([[0, 0x7FFF << 48]], dtype=np.uint64))[0]  # +inf in the row
     ok, _ = row(sq, a, G.uniform_full(rng, 100))
     assert not ok
+
+
+@pytest.mark.parametrize("work,G", [(1, 1), (5, 5), (7, 3), (16384, 152), (1000, 152), (152, 152),
+                                    (153, 152), (64 * 257, 152), (12345, 97)])
+def test_work_partition(sq, work, G):
+    begin = np.zeros(G + 1, dtype=np.int64)
+    cta = np.zeros(work, dtype=np.int64)
+    sq.sq_og_partition(ctypes.c_int64(work), ctypes.c_int64(G), P(begin), P(cta))
+    assert begin[0] == 0 and begin[G] == work and np.all(np.diff(begin) >= 0)
+    want = np.searchsorted(begin, np.arange(work), side="right") - 1
+    assert np.array_equal(cta, want)
