@@ -348,11 +348,18 @@ __global__ void __launch_bounds__(kOgThreads, 1)
         __syncwarp();
         if (lane == 0) mbar_arrive(empty_bar(slot_of(q)));  // this k-step's elements are in registers
         uint32_t W[2][5], sg[2], bs[2];
+        const int sh0 = og_shift(E, v0.w), sh1 = og_shift(E, v1.w);
+        // the four-word level of the shift only when a lane of the warp needs it
+        if (__any_sync(0xFFFFFFFFu, max(sh0, sh1) >= 128)) {
+          og_window_s<false>(v0.x, v0.y, v0.z, v0.w, sh0, W[0]);
+          og_window_s<false>(v1.x, v1.y, v1.z, v1.w, sh1, W[1]);
+        } else {
+          og_window_s<true>(v0.x, v0.y, v0.z, v0.w, sh0, W[0]);
+          og_window_s<true>(v1.x, v1.y, v1.z, v1.w, sh1, W[1]);
+        }
 #pragma unroll
         for (int i = 0; i < 2; ++i) {
-          const uint4 v = i ? v1 : v0;
-          og_window(v.x, v.y, v.z, v.w, E, W[i]);
-          const uint32_t neg = v.w >> 31;
+          const uint32_t neg = (i ? v1.w : v0.w) >> 31;
           sg[i] = 0x3C003C00u + neg * 0x80008000u;  // (+-1, +-1)
           bs[i] = 0xE480E480u - neg * 0x80008000u;  // (-+1152, -+1152)
         }

@@ -50,30 +50,39 @@ QB_HD int og_lead_top(uint32_t top) {
 
 QB_HD bool og_special_top(uint32_t top) { return ((top >> 16) & 0x7FFFu) == 0x7FFFu; }
 
+// Shift that places an element's significand in the window of chunk
+// exponent E: V = (M << 32) >> og_shift(E, w3), M the 113-bit significand.
+// At least 3 (E is at least the element's lead exponent); from 160 on, V = 0.
+QB_HD int og_shift(int E, uint32_t w3) {
+  const uint32_t be = (w3 >> 16) & 0x7FFFu;
+  return E + 16386 - (int)(be > 1u ? be : 1u);
+}
+
 // W = R + V for the element with 32-bit words w0 (least significant) .. w3
-// and a chunk exponent E >= its lead exponent: V = (M << 32) >> s with
-// s = E - lead + 3 (V = 0 from s = 160 on), where M is the 113-bit
-// significand (hidden bit set iff the exponent field is nonzero).
-// W < 2^144: five words, W[4] < 2^16.  Branch-free (lanes of a warp hold
-// elements of different exponents): the word part of the shift is three
-// mask-select levels.  NaN and infinity give bounded garbage (their rows
-// are recomputed exactly).
-QB_HD void og_window(uint32_t w0, uint32_t w1, uint32_t w2, uint32_t w3, int E, uint32_t (&W)[5]) {
+// and shift s = og_shift(E, w3) (hidden bit set iff the exponent field is
+// nonzero).  W < 2^144: five words, W[4] < 2^16.  Branch-free (lanes of a
+// warp hold elements of different exponents): the word part of the shift is
+// three select levels; kShort drops the level for 4 words and the clamp, valid
+// when s < 128.  NaN and infinity give bounded garbage (their rows are
+// recomputed exactly).
+template <bool kShort>
+QB_HD void og_window_s(uint32_t w0, uint32_t w1, uint32_t w2, uint32_t w3, int s, uint32_t (&W)[5]) {
   const uint32_t be = (w3 >> 16) & 0x7FFFu;
   const uint32_t hb = be + 0xFFFFu;  // bit 16 set iff be != 0 (hb < 2^17)
   const uint32_t m3 = (w3 & 0xFFFFu) | (hb & 0x10000u);
-  int s = E + 16386 - (int)(be > 1u ? be : 1u);  // >= 3: E is at least the element's lead exponent
-  s = s < 160 ? s : 160;
+  if (!kShort) s = s < 160 ? s : 160;
   const uint32_t b = (uint32_t)s & 31u, k = (uint32_t)s >> 5;
   uint32_t y0 = fshr32(0u, w0, b), y1 = fshr32(w0, w1, b), y2 = fshr32(w1, w2, b), y3 = fshr32(w2, m3, b),
            y4 = m3 >> b;
-  // word shift by k = 0..5 in three select levels (selects, not branches)
-  const bool k4 = (k & 4u) != 0, k2 = (k & 2u) != 0, k1 = (k & 1u) != 0;
-  y0 = k4 ? y4 : y0;
-  y1 = k4 ? 0u : y1;
-  y2 = k4 ? 0u : y2;
-  y3 = k4 ? 0u : y3;
-  y4 = k4 ? 0u : y4;
+  const bool k2 = (k & 2u) != 0, k1 = (k & 1u) != 0;
+  if (!kShort) {
+    const bool k4 = (k & 4u) != 0;
+    y0 = k4 ? y4 : y0;
+    y1 = k4 ? 0u : y1;
+    y2 = k4 ? 0u : y2;
+    y3 = k4 ? 0u : y3;
+    y4 = k4 ? 0u : y4;
+  }
   y0 = k2 ? y2 : y0;
   y1 = k2 ? y3 : y1;
   y2 = k2 ? y4 : y2;
@@ -110,6 +119,11 @@ QB_HD void og_window(uint32_t w0, uint32_t w1, uint32_t w2, uint32_t w3, int E, 
   t = (t >> 32) + 0x8080u + y4;
   W[4] = (uint32_t)t & 0xFFFFu;
 #endif
+}
+
+// The window for a chunk exponent E >= the element's lead exponent.
+QB_HD void og_window(uint32_t w0, uint32_t w1, uint32_t w2, uint32_t w3, int E, uint32_t (&W)[5]) {
+  og_window_s<false>(w0, w1, w2, w3, og_shift(E, w3), W);
 }
 
 // Digit t (0 = most significant) of an element with window W and sign bit

@@ -159,6 +159,16 @@ void sq_og_chunk(int n, const q128* a, const q128* x, int32_t* EF, int64_t* D, u
   EF[0] = E;
   EF[1] = F;
 }
+// Windows by the short form (valid for shifts below 128), else 0xFFFFFFFF.
+void sq_og_window_short(int64_t n, const q128* a, const int32_t* E, uint32_t* W) {
+  for (int64_t i = 0; i < n; ++i) {
+    const uint32_t w3 = (uint32_t)(a[i].hi >> 32);
+    const int s = qb::og_shift(E[i], w3);
+    uint32_t w[5] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu};
+    if (s < 128) qb::og_window_s<true>((uint32_t)a[i].lo, (uint32_t)(a[i].lo >> 32), (uint32_t)a[i].hi, w3, s, w);
+    for (int k = 0; k < 5; ++k) W[5 * i + k] = w[k];
+  }
+}
 // The work partition of the Ozaki qgemv kernel: begin[b] for b = 0..G and
 // cta[X] for every item X < work.
 void sq_og_partition(int64_t work, int64_t G, int64_t* begin, int64_t* cta) {

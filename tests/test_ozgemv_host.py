@@ -68,6 +68,22 @@ def test_window_digits(sq):
         assert sum(x << (8 * (17 - t)) for t, x in enumerate(d)) == V
 
 
+def test_window_short_form(sq):
+    """The kernel's short window (no four-word shift level) equals the general
+    one whenever the shift is below 128."""
+    rng = G.rng_for(95)
+    a = sample(rng, 400)
+    leads = np.array([lead_top(w) for w in a])
+    E = np.ascontiguousarray((leads + rng.integers(0, 125, size=len(a))).astype(np.int32))
+    W = np.zeros((len(a), 5), dtype=np.uint32)
+    sq.sq_og_window_short(ctypes.c_int64(len(a)), P(np.ascontiguousarray(a)), P(E), P(W))
+    full = windows(sq, a, E)
+    for i, w in enumerate(W):
+        if int(w[0]) == 0xFFFFFFFF and int(w[4]) == 0xFFFFFFFF:
+            continue  # shift of 128 or more (zeros and subnormals against a large E)
+        assert sum(int(w[k]) << (32 * k) for k in range(5)) == full[i], i
+
+
 def chunk(sq, a, x):
     EF = np.zeros(2, dtype=np.int32)
     D = np.zeros(32, dtype=np.int64)
