@@ -180,11 +180,16 @@ int quadblas_batch_autotune(int64_t *grain_out);
 int quadblas_batch_set_grain(int64_t grain);
 
 /* ---- Configuration and errors (no reference counterpart) -------------- */
-/* qgemm method: QBLAS_METHOD_AUTO, _SOFTFLOAT or _OZAKI. */
+/* Method of qgemm and qgemv: QBLAS_METHOD_AUTO (soft-float for both),
+ * _SOFTFLOAT or _OZAKI.  Ozaki qgemm is normwise accurate (set by the digit
+ * count); Ozaki qgemv certifies every row's rounding and recomputes the rest
+ * exactly, so its results equal the soft-float ones bit for bit. */
 int quadblas_set_method(int method);
 int quadblas_get_method(void);
-/* Ozaki digit (slice) count per operand: 0 = default (18 for 8-bit digits,
- * 20 for 7-bit), else 2..20 (8-bit) or 2..22 (7-bit). */
+/* Ozaki qgemm digit (slice) count per operand: 0 = default (16 of 9 bits, 18
+ * of 8, 20 of 7), else 2..22; each call caps it by what the k dimension
+ * allows (18 of 9 bits, 20 of 8, 22 of 7 at most).  qgemv uses its own fixed
+ * split. */
 int quadblas_set_ozaki_slices(int slices);
 int quadblas_get_ozaki_slices(void);
 /* Ozaki digit width: 0 = default (9), 7 or 8 bits per balanced digit (bf16
