@@ -8,9 +8,12 @@
 // 16-byte loads, every thread keeps one wide accumulator (wacc.cuh), the
 // block merges its threads' accumulators (warp shuffles + shared memory),
 // and a second single-block kernel merges the per-block partials in a
-// fixed order and rounds once.  That rounding is certified (exact.cuh); if
-// the sum cancels below what the 256-bit frame holds, a third kernel
-// recomputes it exactly (Kulisch accumulator) — it returns at once otherwise.
+// fixed order and rounds once.  The products skip the partial products that
+// only feed their lowest 64 bits (three multiplies of 31, on the saturated
+// fmaheavy pipe), which adds less than 2^34 units of the frame's last bit per
+// term to the error budget.  The rounding is certified against that budget
+// (exact.cuh); if the sum cancels below it, a third kernel recomputes the
+// sum exactly (Kulisch accumulator) — it returns at once otherwise.
 #include "exact.cuh"
 #include "kernels.h"
 #include "reduce.cuh"
@@ -59,14 +62,14 @@ __global__ void __launch_bounds__(kDotThreads, 4)
       q128 xb = ld_stream(x + i + stride), yb = ld_stream(y + i + stride);
       q128 xc = ld_stream(x + i + 2 * stride), yc = ld_stream(y + i + 2 * stride);
       q128 xd = ld_stream(x + i + 3 * stride), yd = ld_stream(y + i + 3 * stride);
-      wacc_add_product(acc, qop_unpack(xa), qop_unpack(ya));
-      wacc_add_product(acc, qop_unpack(xb), qop_unpack(yb));
-      wacc_add_product(acc, qop_unpack(xc), qop_unpack(yc));
-      wacc_add_product(acc, qop_unpack(xd), qop_unpack(yd));
+      wacc_add_product_trunc(acc, qop_unpack(xa), qop_unpack(ya));
+      wacc_add_product_trunc(acc, qop_unpack(xb), qop_unpack(yb));
+      wacc_add_product_trunc(acc, qop_unpack(xc), qop_unpack(yc));
+      wacc_add_product_trunc(acc, qop_unpack(xd), qop_unpack(yd));
     }
   }
   for (; i < n; i += stride)
-    wacc_add_product(acc, qop_unpack(ld_stream(x + i * incx)), qop_unpack(ld_stream(y + i * incy)));
+    wacc_add_product_trunc(acc, qop_unpack(ld_stream(x + i * incx)), qop_unpack(ld_stream(y + i * incy)));
   wacc_block_reduce(acc, sm);
   if (threadIdx.x == 0) partials[blockIdx.x] = acc;
 }
@@ -149,7 +152,10 @@ cudaError_t launch_dot(int64_t n, const q128* x, int64_t incx, const q128* y, in
   if (e != cudaSuccess) return e;
   // truncation budget: 2 units per product, 3 per merge (every thread's
   // accumulator, the block partials and the final block's merges)
-  const uint64_t err = 2 * (uint64_t)n + 3 * ((uint64_t)nb * kDotThreads + (uint64_t)nb + 2 * kDotThreads + 64);
+  // budget: 2^34 + 2 units per (truncated) product, 3 per merge; beyond
+  // 2^29 terms it saturates and the exact pass decides
+  const uint64_t merges = 3 * ((uint64_t)nb * kDotThreads + (uint64_t)nb + 2 * kDotThreads + 64);
+  const uint64_t err = n > ((int64_t)1 << 29) ? ~0ull : (uint64_t)n * ((1ull << 34) + 2) + merges;
   wacc_finalize_kernel<<<1, kDotThreads, 0, s>>>(partials, nb, out, take_sqrt, err, G);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   int64_t gx = (n + 4 * kDotThreads - 1) / (4 * kDotThreads);

@@ -205,6 +205,77 @@ QB_HD void mul128x128_top224(const qop& a, const qop& b, uint32_t& p1, uint32_t&
 #endif
 }
 
+// Limbs 2..7 of the 256-bit product of two 128-bit significands, without
+// the partial products that feed only limbs 0 and 1 (lo(a0 b0), hi(a0 b0),
+// lo(a0 b1), lo(a1 b0)) and their carries: the result is below the exact
+// top 192 bits by less than 4, i.e. less than 2^34 units of limb 1.  Three
+// multiplies fewer than mul128x128_top224.
+QB_HD void mul128x128_top192(const qop& a, const qop& b, uint32_t& p2, uint32_t& p3, uint32_t& p4,
+                             uint32_t& p5, uint32_t& p6, uint32_t& p7) {
+#if defined(__CUDA_ARCH__)
+  uint32_t r2, r3, r4, r5, r6, r7;
+  asm("{\n\t"
+      // row 0: lo(a0 b2), lo(a0 b3); hi(a0 b1), hi(a0 b2), hi(a0 b3)
+      "mul.lo.u32      %0, %6, %12;\n\t"
+      "mul.lo.u32      %1, %6, %13;\n\t"
+      "mad.hi.cc.u32   %0, %6, %11, %0;\n\t"
+      "madc.hi.cc.u32  %1, %6, %12, %1;\n\t"
+      "madc.hi.u32     %2, %6, %13, 0;\n\t"
+      // row 1: lo(a1 b1..b3) into limbs 2..4, hi(a1 b0..b3) into limbs 2..5
+      "mad.lo.cc.u32   %0, %7, %11, %0;\n\t"
+      "madc.lo.cc.u32  %1, %7, %12, %1;\n\t"
+      "madc.lo.cc.u32  %2, %7, %13, %2;\n\t"
+      "addc.u32        %3, 0, 0;\n\t"
+      "mad.hi.cc.u32   %0, %7, %10, %0;\n\t"
+      "madc.hi.cc.u32  %1, %7, %11, %1;\n\t"
+      "madc.hi.cc.u32  %2, %7, %12, %2;\n\t"
+      "madc.hi.u32     %3, %7, %13, %3;\n\t"
+      // row 2: lo(a2 b0..b3) into limbs 2..5, hi into limbs 3..6
+      "mad.lo.cc.u32   %0, %8, %10, %0;\n\t"
+      "madc.lo.cc.u32  %1, %8, %11, %1;\n\t"
+      "madc.lo.cc.u32  %2, %8, %12, %2;\n\t"
+      "madc.lo.cc.u32  %3, %8, %13, %3;\n\t"
+      "addc.u32        %4, 0, 0;\n\t"
+      "mad.hi.cc.u32   %1, %8, %10, %1;\n\t"
+      "madc.hi.cc.u32  %2, %8, %11, %2;\n\t"
+      "madc.hi.cc.u32  %3, %8, %12, %3;\n\t"
+      "madc.hi.u32     %4, %8, %13, %4;\n\t"
+      // row 3: lo(a3 b0..b3) into limbs 3..6, hi into limbs 4..7
+      "mad.lo.cc.u32   %1, %9, %10, %1;\n\t"
+      "madc.lo.cc.u32  %2, %9, %11, %2;\n\t"
+      "madc.lo.cc.u32  %3, %9, %12, %3;\n\t"
+      "madc.lo.cc.u32  %4, %9, %13, %4;\n\t"
+      "addc.u32        %5, 0, 0;\n\t"
+      "mad.hi.cc.u32   %2, %9, %10, %2;\n\t"
+      "madc.hi.cc.u32  %3, %9, %11, %3;\n\t"
+      "madc.hi.cc.u32  %4, %9, %12, %4;\n\t"
+      "madc.hi.u32     %5, %9, %13, %5;\n\t"
+      "}"
+      : "=&r"(r2), "=&r"(r3), "=&r"(r4), "=&r"(r5), "=&r"(r6), "=&r"(r7)
+      : "r"(a.m0), "r"(a.m1), "r"(a.m2), "r"(a.m3), "r"(b.m0), "r"(b.m1), "r"(b.m2), "r"(b.m3));
+  p2 = r2; p3 = r3; p4 = r4; p5 = r5; p6 = r6; p7 = r7;
+#else
+  uint32_t A[4] = {a.m0, a.m1, a.m2, a.m3}, B[4] = {b.m0, b.m1, b.m2, b.m3};
+  uint32_t r[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  // lo(a_i b_j) belongs to limb i + j, hi(a_i b_j) to limb i + j + 1; the
+  // halves in limbs 0 and 1 are dropped, the rest summed column by column
+  uint64_t col[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  for (int i = 0; i < 4; ++i)
+    for (int j = 0; j < 4; ++j) {
+      const uint64_t prod = (uint64_t)A[i] * B[j];
+      if (i + j >= 2) col[i + j] += (uint32_t)prod;
+      if (i + j + 1 >= 2) col[i + j + 1] += prod >> 32;
+    }
+  uint64_t c = 0;
+  for (int k = 2; k < 8; ++k) {
+    const uint64_t t = col[k] + c;
+    r[k] = (uint32_t)t;
+    c = t >> 32;
+  }
+  p2 = r[2]; p3 = r[3]; p4 = r[4]; p5 = r[5]; p6 = r[6]; p7 = r[7];
+#endif
+}
+
 // W += (neg ? -Q : Q) for a 256-bit Q = (q7..q0).
 QB_HD void wacc_add_signed(wacc& a, uint32_t q0, uint32_t q1, uint32_t q2, uint32_t q3, uint32_t q4,
                            uint32_t q5, uint32_t q6, uint32_t q7, uint32_t neg) {
@@ -297,6 +368,18 @@ QB_HD void wacc_add_product(wacc& acc, const qop& a, const qop& b) {
   uint32_t p1, p2, p3, p4, p5, p6, p7;
   mul128x128_top224(a, b, p1, p2, p3, p4, p5, p6, p7);
   wacc_add_aligned(acc, p1, p2, p3, p4, p5, p6, p7, a.e + b.e + 32, a.s ^ b.s);
+}
+
+// acc += a * b with mul128x128_top192: each product adds less than 2^34 + 2
+// units of the frame's last bit to the error (instead of 2).
+QB_HD void wacc_add_product_trunc(wacc& acc, const qop& a, const qop& b) {
+  if ((a.cls | b.cls) != kClsFinite) {
+    acc.flags |= special_product_flags(a, b);
+    return;
+  }
+  uint32_t p2, p3, p4, p5, p6, p7;
+  mul128x128_top192(a, b, p2, p3, p4, p5, p6, p7);
+  wacc_add_aligned(acc, 0u, p2, p3, p4, p5, p6, p7, a.e + b.e + 32, a.s ^ b.s);
 }
 
 // a += b (b unchanged).  The smaller-exponent operand is aligned to the larger one's frame.  The

@@ -68,6 +68,33 @@ void sq_wacc_dot_certified(int64_t n, const q128* x, const q128* y, int64_t nspl
   }
   *certified = qb::wacc_round_certified(tot, 2 * (uint64_t)n + 3 * (uint64_t)nsplit + 3, *out) ? 1 : 0;
 }
+// As sq_wacc_dot_certified with the truncated products of the qdot kernel
+// (mul128x128_top192) and its budget of 2^34 + 2 units per product.
+void sq_wacc_dot_trunc_certified(int64_t n, const q128* x, const q128* y, int64_t nsplit, q128* out,
+                                 int32_t* certified) {
+  qb::wacc tot;
+  qb::wacc_init(tot);
+  if (nsplit < 1) nsplit = 1;
+  int64_t chunk = (n + nsplit - 1) / nsplit;
+  for (int64_t s = 0; s < nsplit; ++s) {
+    qb::wacc a;
+    qb::wacc_init(a);
+    for (int64_t i = s * chunk; i < n && i < (s + 1) * chunk; ++i)
+      qb::wacc_add_product_trunc(a, qb::qop_unpack(x[i]), qb::qop_unpack(y[i]));
+    qb::wacc_merge(tot, a);
+  }
+  const uint64_t err = (uint64_t)n * ((1ull << 34) + 2) + 3 * (uint64_t)nsplit + 3;
+  *certified = qb::wacc_round_certified(tot, err, *out) ? 1 : 0;
+}
+// Limbs 2..7 of the truncated significand product (mul128x128_top192) of
+// n pairs, six words each.
+void sq_mul_top192(int64_t n, const q128* x, const q128* y, uint32_t* out) {
+  for (int64_t i = 0; i < n; ++i) {
+    qb::qop a = qb::qop_unpack(x[i]), b = qb::qop_unpack(y[i]);
+    qb::mul128x128_top192(a, b, out[6 * i], out[6 * i + 1], out[6 * i + 2], out[6 * i + 3], out[6 * i + 4],
+                          out[6 * i + 5]);
+  }
+}
 // Exact dot through the Kulisch accumulator (the device fallback's arithmetic).
 void sq_kulisch_dot(int64_t n, const q128* x, int64_t incx, const q128* y, int64_t incy, q128* out) {
   static int64_t d[qb::kKDigits];

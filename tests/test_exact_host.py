@@ -99,3 +99,51 @@ def test_certificate_is_not_vacuous(O, sq):
     y = np.concatenate([Q.scalar(1.0), Q.scalar(1.0)])
     got, ok = certified(sq, x, y, 1)
     assert Q.same_bits(got, Q.scalar(1.0)).all()
+
+
+def trunc_certified(sq, x, y, nsplit):
+    x, y = np.ascontiguousarray(x), np.ascontiguousarray(y)
+    out, ok = Q.empty(1), np.zeros(1, np.int32)
+    sq.sq_wacc_dot_trunc_certified(c64(len(x)), P(x), P(y), c64(nsplit), P(out), P(ok))
+    return out, bool(ok[0])
+
+
+def test_truncated_product_bound(sq):
+    """The qdot kernel's products (limbs 2..7 without the partial products of
+    limbs 0 and 1) are at most 4 units of limb 2 below the exact top bits."""
+    rng = G.rng_for(34)
+    x = np.concatenate([G.uniform_full(rng, 300), V.subnormal(rng, 50)])
+    y = np.concatenate([G.uniform_full(rng, 300), V.finite(rng, 50, -10, 10)])
+    x[:20, 0] = np.uint64(0xFFFFFFFFFFFFFFFF)  # all-ones low words: the largest dropped carries
+    y[:20, 0] = np.uint64(0xFFFFFFFFFFFFFFFF)
+    out = np.zeros((len(x), 6), dtype=np.uint32)
+    sq.sq_mul_top192(c64(len(x)), P(x), P(y), P(out))
+
+    def sig(w):  # significand shifted to bit 127, as the device unpacks it
+        lo, hi = int(w[0]), int(w[1])
+        be = (hi >> 48) & 0x7FFF
+        m = ((hi & ((1 << 48) - 1)) << 64) | lo
+        if be:
+            m |= 1 << 112
+        return m << (127 - (m.bit_length() - 1)) if m else 0
+
+    for i in range(len(x)):
+        exact = (sig(x[i]) * sig(y[i])) >> 64
+        got = sum(int(out[i, k]) << (32 * k) for k in range(6))
+        assert 0 <= exact - got < 4, i
+
+
+@pytest.mark.parametrize("nsplit", [1, 256])
+def test_truncated_certificate_is_sound(O, sq, nsplit):
+    """Certified sums of truncated products equal the correctly rounded exact sum."""
+    n_cert = 0
+    for name, x, y in cases(O):
+        got, ok = trunc_certified(sq, x, y, nsplit)
+        if ok:
+            n_cert += 1
+            R, _, _ = O.exact_dot(x, y)
+            assert Q.same_bits(got, R).all(), name
+    assert n_cert >= 6
+    rng = G.rng_for(35)
+    x, y = G.cancelling_dot(rng, 4096)  # the benchmark's data kind certifies
+    assert trunc_certified(sq, x, y, nsplit)[1]
