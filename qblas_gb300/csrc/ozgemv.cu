@@ -204,20 +204,28 @@ __device__ __forceinline__ void og_store_pairs(uint32_t taddr, const uint32_t (&
 
 // A's elements of one k-step arrive by TMA (128-byte swizzle: the 16-byte
 // piece p of a 128-byte smem row q sits at piece p ^ (q % 8)).
-//   row-major A: one box of 128 rows x 8 columns (element (r, i) at
+//   kOgRowMajor: one box of 128 rows x 8 columns (element (r, i) at
 //                r * 128 + piece i)
-//   column-major A: sixteen boxes of 8 rows x 8 columns (rows 8g..8g+7 at
-//                g * 1024; element (8g + e, i) at i * 128 + piece e)
-// Offset of element (r, i) within a slot:
-template <bool kRowMajor>
+//   kOgColGroups: column-major A with m a multiple of 8, as a 3-D tensor
+//                (8 rows = 128 bytes, row groups, columns): one box of 16 row
+//                groups x 8 columns (element (8g + e, i) at
+//                (16 i + g) * 128 + piece e)
+//   kOgColBoxes: column-major A otherwise: sixteen 2-D boxes of 8 rows x 8
+//                columns (rows 8g..8g+7 at g * 1024; element (8g + e, i) at
+//                i * 128 + piece e)
+enum : int { kOgRowMajor = 0, kOgColGroups = 1, kOgColBoxes = 2 };
+
+template <int kLayout>
 __device__ __forceinline__ uint32_t og_elem_offset(int r, int i) {
-  if (kRowMajor) return (uint32_t)(r * 128 + ((i ^ (r & 7)) << 4));
-  return (uint32_t)((r >> 3) * 1024 + i * 128 + (((r & 7) ^ i) << 4));
+  if (kLayout == kOgRowMajor) return (uint32_t)(r * 128 + ((i ^ (r & 7)) << 4));
+  const int g = r >> 3, e = r & 7;
+  if (kLayout == kOgColGroups) return (uint32_t)((16 * i + g) * 128 + ((e ^ (g & 7)) << 4));
+  return (uint32_t)(g * 1024 + i * 128 + ((e ^ i) << 4));
 }
 
 // 21 warps: six share one SM sub-partition's 16384 registers, so at most
 // 80 registers per thread; one CTA per SM (all 512 tensor-memory columns).
-template <bool kRowMajor>
+template <int kLayout>
 __global__ void __launch_bounds__(kOgThreads, 1)
     og_gemv_kernel(const __grid_constant__ CUtensorMap tmA, OgParams P) {
   extern __shared__ uint8_t smem_raw[];
@@ -289,7 +297,7 @@ __global__ void __launch_bounds__(kOgThreads, 1)
     const int qd = warp & 3, grp = warp >> 2;  // lane quadrant; columns 2*grp, 2*grp+1 of each k-step
     const int r = qd * 32 + lane;
     const int tid = threadIdx.x;
-    const uint32_t off0 = og_elem_offset<kRowMajor>(r, 2 * grp), off1 = og_elem_offset<kRowMajor>(r, 2 * grp + 1);
+    const uint32_t off0 = og_elem_offset<kLayout>(r, 2 * grp), off1 = og_elem_offset<kLayout>(r, 2 * grp + 1);
     const uint32_t tlane = tmem + ((uint32_t)(qd * 32) << 16) + kOgAccCols + 2 * grp;
     const bool xcopy = tid < kOgXBytes / 16;
     // chunk of the item being split, kept by counting (no 64-bit division in the loop)
@@ -401,8 +409,10 @@ __global__ void __launch_bounds__(kOgThreads, 1)
         }
         const uint32_t slot = base + slot_of(kq) * kOgSlotBytes, bar = full_bar(slot_of(kq));
         mbar_expect_tx(bar, kOgSlotBytes);
-        if (kRowMajor) {
+        if (kLayout == kOgRowMajor) {
           tma_load_2d(slot, &tmA, bar, 4 * col0, (int)(tile * kOgRows));
+        } else if (kLayout == kOgColGroups) {
+          tma_load_3d(slot, &tmA, bar, 0, (int)(tile * (kOgRows / 8)), col0);
         } else {
           for (int g = 0; g < kOgRows / 8; ++g)
             tma_load_2d(slot + g * 1024, &tmA, bar, 4 * (int)(tile * kOgRows + 8 * g), col0);
@@ -625,20 +635,33 @@ cudaError_t launch_gemv_ozaki(int64_t m, int64_t n, q128 alpha, MatView A, const
   const bool row_major = A.sj == 1;
   const int64_t ld = row_major ? A.si : A.sj;
   if (!row_major && A.si != 1) return cudaErrorInvalidValue;
-  // A as 32-bit words, [rows][4 * cols] (row-major) or [cols][4 * rows]
+  // column-major A as (8 rows, row groups, columns) when m is a multiple of 8
+  // (a box never reaches past the last row), else as 2-D (rows, columns)
+  const int layout = row_major ? kOgRowMajor : (m % 8 == 0 ? kOgColGroups : kOgColBoxes);
   CUtensorMap map;
   {
     EncodeTiledFn fn = encode_fn();
     if (!fn) return cudaErrorNotSupported;
-    const int64_t inner = row_major ? n : m, outer = row_major ? m : n;
-    cuuint64_t dims[2] = {(cuuint64_t)(4 * inner), (cuuint64_t)outer};
-    cuuint64_t strides[1] = {(cuuint64_t)ld * 16};
-    cuuint32_t box[2] = {32, row_major ? (cuuint32_t)kOgRows : (cuuint32_t)kOgKStep};  // 128 B x rows / columns
-    cuuint32_t estr[2] = {1, 1};
-    if (fn(&map, CU_TENSOR_MAP_DATA_TYPE_UINT32, 2, const_cast<q128*>(A.p), dims, strides, box, estr,
-           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
-      return cudaErrorInvalidValue;
+    cuuint32_t estr[3] = {1, 1, 1};
+    CUresult rc;
+    if (layout == kOgColGroups) {
+      cuuint64_t dims[3] = {32, (cuuint64_t)(m / 8), (cuuint64_t)n};
+      cuuint64_t strides[2] = {128, (cuuint64_t)ld * 16};
+      cuuint32_t box[3] = {32, kOgRows / 8, (cuuint32_t)kOgKStep};
+      rc = fn(&map, CU_TENSOR_MAP_DATA_TYPE_UINT32, 3, const_cast<q128*>(A.p), dims, strides, box, estr,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    } else {
+      // A as 32-bit words, [rows][4 * cols] (row-major) or [cols][4 * rows]
+      const int64_t inner = row_major ? n : m, outer = row_major ? m : n;
+      cuuint64_t dims[2] = {(cuuint64_t)(4 * inner), (cuuint64_t)outer};
+      cuuint64_t strides[1] = {(cuuint64_t)ld * 16};
+      cuuint32_t box[2] = {32, row_major ? (cuuint32_t)kOgRows : (cuuint32_t)kOgKStep};  // 128 B x rows / columns
+      rc = fn(&map, CU_TENSOR_MAP_DATA_TYPE_UINT32, 2, const_cast<q128*>(A.p), dims, strides, box, estr,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    }
+    if (rc != CUDA_SUCCESS) return cudaErrorInvalidValue;
   }
   const OgLayout Lo = og_layout(m, n);
   char* base = static_cast<char*>(scratch);
@@ -660,17 +683,21 @@ cudaError_t launch_gemv_ozaki(int64_t m, int64_t n, q128 alpha, MatView A, const
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   static bool attr = false;
   if (!attr) {
-    if ((e = cudaFuncSetAttribute(og_gemv_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    if ((e = cudaFuncSetAttribute(og_gemv_kernel<kOgRowMajor>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)kOgSmem)) != cudaSuccess ||
-        (e = cudaFuncSetAttribute(og_gemv_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        (e = cudaFuncSetAttribute(og_gemv_kernel<kOgColGroups>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)kOgSmem)) != cudaSuccess ||
+        (e = cudaFuncSetAttribute(og_gemv_kernel<kOgColBoxes>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)kOgSmem)) != cudaSuccess)
       return e;
     attr = true;
   }
-  if (row_major)
-    og_gemv_kernel<true><<<(unsigned)Lo.G, kOgThreads, kOgSmem, s>>>(map, P);
+  if (layout == kOgRowMajor)
+    og_gemv_kernel<kOgRowMajor><<<(unsigned)Lo.G, kOgThreads, kOgSmem, s>>>(map, P);
+  else if (layout == kOgColGroups)
+    og_gemv_kernel<kOgColGroups><<<(unsigned)Lo.G, kOgThreads, kOgSmem, s>>>(map, P);
   else
-    og_gemv_kernel<false><<<(unsigned)Lo.G, kOgThreads, kOgSmem, s>>>(map, P);
+    og_gemv_kernel<kOgColBoxes><<<(unsigned)Lo.G, kOgThreads, kOgSmem, s>>>(map, P);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   og_finish_kernel<<<(unsigned)((m + 63) / 64), 64, 0, s>>>(m, Lo.nchunks, Lo.work, Lo.G, Lo.segs, P.part,
                                                               P.err, alpha, beta, y, incy, list);
