@@ -21,34 +21,44 @@
 //
 // Kernels:
 //   og_x_split_kernel : x's chunk exponents F_c (NaN / inf marked) and its
-//                       digits as the MMA's B operand, one 1792-byte tile per
-//                       16 columns; resets the list of uncertified rows
+//                       digits as the MMA's B operand, one 1536-byte tile per
+//                       8-column k-step; resets the list of uncertified rows
 //   og_gemv_kernel    : persistent, one CTA per SM over a balanced range of
-//                       (row tile, chunk) items, warp-specialised:
-//                       warps 0-7  split A (two threads per row, 8 columns
-//                                  each per 16-column k-step): load, scale,
-//                                  byte-select digits, st.shared into a
-//                                  double-buffered operand stage;
-//                       warp 8     issues 18 tcgen05.mma (M=128, N=32,
-//                                  K=16) per k-step, one per A digit plane
-//                                  t, with B = x's planes shifted down by t
-//                                  (a descriptor offset), so the one
-//                                  accumulator collects every diagonal;
-//                       warps 9-12 read the accumulator (tcgen05.ld), fold
+//                       (row tile, chunk) items, 22 warps, warp-specialised:
+//                       warps 0-15 split A: thread per row (its tensor-memory
+//                                  lane; warp % 4 is the lane quadrant),
+//                                  two columns per 8-column k-step (warp / 4
+//                                  picks which); the four warps of a quadrant
+//                                  exchange the row's largest exponent, then
+//                                  each builds its elements' windows, turns
+//                                  digit pairs into fp16 pairs (byte select +
+//                                  HFMA2) and writes them to the A operand
+//                                  stage in tensor memory (tcgen05.st);
+//                       warp 16    issues 9 tcgen05.mma (M=128, N=32,
+//                                  K=16: 8 elements x 2 digit planes) per
+//                                  k-step, one per plane pair p, A from
+//                                  tensor memory, B = x's tile read 16 - 2p
+//                                  rows down (a descriptor offset), so the
+//                                  one accumulator collects every diagonal;
+//                       warp 17    TMA loads of A's k-steps into a ring of
+//                                  12 shared-memory slots (16 KB each,
+//                                  128-byte swizzle);
+//                       warps 18-21 read the accumulator (tcgen05.ld), fold
 //                                  the diagonals and add into the row's
 //                                  wide accumulator; one partial per
 //                                  (row, CTA range).
-//                       Every mbarrier wait is bounded (1 s): on timeout the
-//                       kernel records an error and returns, after draining
-//                       its MMAs and freeing tensor memory.
+//                       Four operand stages and four accumulators are in
+//                       flight.  Every mbarrier wait is bounded (1 s): on
+//                       timeout the kernel records an error and returns,
+//                       after waiting (bounded) for its copies and MMAs and
+//                       freeing tensor memory.
 //   og_finish_kernel  : per row: merge the partials in order, certify, apply
 //                       the epilogue or list the row.
 //
-// Shared memory of one operand stage (no swizzle, K-major core matrices of
-// 8 rows x 16 bytes): 18 A planes of 128 rows x 16 columns (plane t at
-// t * 4096, columns 8..15 at +2048, row r at (r/8)*128 + (r%8)*16), then the
-// B tile: 56 rows x 16 columns (row 17 + u holds x's plane u, the rest zero;
-// columns 8..15 at +896), so B for plane t starts at row 17 - t.
+// A reaches shared memory in one of three TMA layouts (og_elem_offset):
+// row-major A as a 2-D box of 128 rows x 8 columns; column-major A with m a
+// multiple of 8 as one 3-D box (8-row groups x columns); other column-major
+// A as sixteen 2-D boxes of 8 rows.
 #include <cuda.h>
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
@@ -223,7 +233,7 @@ __device__ __forceinline__ uint32_t og_elem_offset(int r, int i) {
   return (uint32_t)(g * 1024 + i * 128 + ((e ^ i) << 4));
 }
 
-// 21 warps: six share one SM sub-partition's 16384 registers, so at most
+// 22 warps: six share one SM sub-partition's 16384 registers, so at most
 // 80 registers per thread; one CTA per SM (all 512 tensor-memory columns).
 template <int kLayout>
 __global__ void __launch_bounds__(kOgThreads, 1)
