@@ -197,6 +197,19 @@ int quadblas_get_ozaki_slices(void);
  * bits, more k passes). */
 int quadblas_set_ozaki_digit_bits(int bits);
 int quadblas_get_ozaki_digit_bits(void);
+/* Ozaki qgemm scheme: both truncate each operand to T = bits * slices - 1
+ * bits after its row (column) scaling.  QBLAS_OZAKI_DIGITS multiplies every
+ * digit pair whose weight the slice count keeps (slices (slices + 1) / 2
+ * tensor-core products).  QBLAS_OZAKI_RESIDUES (Ozaki scheme II) multiplies
+ * the operands' residues modulo N pairwise coprime moduli (N tensor-core
+ * products, N about (2T + log2 k + 3) / 8.8) and recovers the exact integer
+ * sum by the Chinese remainder theorem, so its only error is the
+ * truncation.  QBLAS_OZAKI_AUTO (0, the default) takes residues whenever the
+ * moduli table covers T and k (T <= 191 and at most 48 moduli), else
+ * digits. */
+enum { QBLAS_OZAKI_AUTO = 0, QBLAS_OZAKI_DIGITS = 1, QBLAS_OZAKI_RESIDUES = 2 };
+int quadblas_set_ozaki_scheme(int scheme);
+int quadblas_get_ozaki_scheme(void);
 /* Phase timing of Ozaki qgemm calls (no reference counterpart): when
  * enabled, each call records CUDA events on its stream; read returns the
  * summed times in ms since the last read — out4[0] scaling and digit split,

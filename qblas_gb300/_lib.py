@@ -55,6 +55,8 @@ _SIGS = {
     "quadblas_get_ozaki_slices": (ci, []),
     "quadblas_set_ozaki_digit_bits": (ci, [ci]),
     "quadblas_get_ozaki_digit_bits": (ci, []),
+    "quadblas_set_ozaki_scheme": (ci, [ci]),
+    "quadblas_get_ozaki_scheme": (ci, []),
     "quadblas_profile_enable": (ci, [ci]),
     "quadblas_profile_read": (ci, [vp, vp]),
     "quadblas_release_buffers": (ci, []),

@@ -141,6 +141,15 @@ def set_ozaki_digit_bits(b: int) -> None:
     check(load().quadblas_set_ozaki_digit_bits(b))
 
 
+def set_ozaki_scheme(scheme: int) -> None:
+    """0 automatic (residues when they fit), 1 digit pairs, 2 residues (CRT)."""
+    check(load().quadblas_set_ozaki_scheme(scheme))
+
+
+def get_ozaki_scheme() -> int:
+    return load().quadblas_get_ozaki_scheme()
+
+
 def release_buffers() -> None:
     check(load().quadblas_release_buffers())
 

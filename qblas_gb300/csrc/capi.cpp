@@ -33,6 +33,7 @@ thread_local int g_last_error = 0;
 std::atomic<int> g_num_threads{0};
 std::atomic<int> g_method{0};   // 0 auto, 1 soft-float, 2 Ozaki
 std::atomic<int> g_slices{0};   // 0 = automatic
+std::atomic<int> g_ozaki_scheme{0};  // 0 = automatic (residues when they fit), 1 digit pairs, 2 residues
 std::atomic<int> g_digit_bits{0};  // 0 = automatic (8)
 
 int fail(int code) {
@@ -363,7 +364,7 @@ int gemm_digits(int64_t k) {
 
 size_t gemm_scratch_bytes(const GemmPlan& p, int method) {
   if (method != 2) return 0;
-  return qb::ozaki_scratch_bytes(p.g.m, p.g.n, p.g.k, gemm_digits(p.g.k), gemm_digit_bits());
+  return qb::ozaki_scratch_bytes(p.g.m, p.g.n, p.g.k, gemm_digits(p.g.k), gemm_digit_bits(), g_ozaki_scheme.load());
 }
 
 int dev_gemm(GemmPlan p, int method, const void* alpha, const void* dA, const void* dB,
@@ -385,7 +386,8 @@ int dev_gemm(GemmPlan p, int method, const void* alpha, const void* dA, const vo
       return cuda_status(e);
     }
   }
-  cudaError_t e = qb::launch_gemm_ozaki(p.g, gemm_digits(p.g.k), gemm_digit_bits(), scratch, s, overlap);
+  cudaError_t e = qb::launch_gemm_ozaki(p.g, gemm_digits(p.g.k), gemm_digit_bits(), scratch, s, overlap,
+                                        g_ozaki_scheme.load());
   if (!scratch_or_null) cudaFreeAsync(scratch, s);
   return cuda_status(e);
 }
@@ -806,6 +808,12 @@ QBLAS_EXPORT int quadblas_set_ozaki_digit_bits(int bits) {
   return fail(qb::kOk);
 }
 QBLAS_EXPORT int quadblas_get_ozaki_digit_bits(void) { return g_digit_bits.load(); }
+QBLAS_EXPORT int quadblas_set_ozaki_scheme(int scheme) {
+  if (scheme < 0 || scheme > 2) return fail(qb::kErrInvalidValue);
+  g_ozaki_scheme.store(scheme);
+  return fail(qb::kOk);
+}
+QBLAS_EXPORT int quadblas_get_ozaki_scheme(void) { return g_ozaki_scheme.load(); }
 QBLAS_EXPORT int quadblas_profile_enable(int on) {
   qb::ozaki_profile_enable(on != 0);
   return qb::kOk;

@@ -63,15 +63,19 @@ struct GemmArgs {
 // C = fma(alpha, round(sum_l op(A)(i,l) op(B)(l,j)), beta * C), soft-float
 cudaError_t launch_gemm_softfloat(const GemmArgs& g, cudaStream_t s);
 
-// C = fma(alpha, round(sum), beta * C) with the sum from the Ozaki digit
-// split on the tensor cores (`digits` balanced digits of `bits` = 7 or 8
-// bits per operand).
+// C = fma(alpha, round(sum), beta * C) with the sum from an Ozaki split on
+// the tensor cores, both schemes truncating the operands to T = bits *
+// digits - 1 bits: `scheme` 1 = balanced digits of `bits` = 7, 8 or 9 bits
+// and their digit-pair products (ozaki.cuh); 0 or 2 = residues modulo
+// pairwise coprime moduli and the Chinese remainder theorem (ozcrt.cuh)
+// whenever its table fits T and k, else digit pairs.
 int ozaki_default_digit_bits();
 int ozaki_default_digits(int bits);
 // Largest digit count whose 192-bit fold cannot overflow for inner dimension k.
 int ozaki_digit_cap(int bits, int64_t k);
-size_t ozaki_scratch_bytes(int64_t m, int64_t n, int64_t k, int digits, int bits);
-size_t ozaki_error_flag_offset(int64_t m, int64_t n, int64_t k, int digits, int bits);
+size_t ozaki_scratch_bytes(int64_t m, int64_t n, int64_t k, int digits, int bits, int scheme);
+size_t ozaki_error_flag_offset(int64_t m, int64_t n, int64_t k, int digits, int bits, int scheme);
+bool ozaki_uses_crt(int64_t k, int digits, int bits, int scheme);
 // Optional overlap for callers that copy op(B) and C to the device
 // themselves: the op(B) side (its scales and digits) runs on `b_stream`,
 // in stream order after the copy of B that the caller put there, while op(A)
@@ -100,7 +104,7 @@ struct OzakiOverlap {
   cudaEvent_t a_done;
 };
 cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scratch,
-                              cudaStream_t s, const OzakiOverlap* overlap = nullptr);
+                              cudaStream_t s, const OzakiOverlap* overlap = nullptr, int scheme = 0);
 // Phase timing of Ozaki calls with CUDA events (off by default).
 void ozaki_profile_enable(bool on);
 int ozaki_profile_read(double* out4, int* calls);

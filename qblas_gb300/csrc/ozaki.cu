@@ -39,6 +39,7 @@
 //                         semantics
 #include <cuda.h>
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -47,6 +48,7 @@
 
 #include "kernels.h"
 #include "ozaki.cuh"
+#include "ozcrt.cuh"
 #include "reduce.cuh"
 #include "umma.cuh"
 
@@ -131,6 +133,58 @@ __global__ void __launch_bounds__(256)
   ozaki_digits_emit2<B>(v0, v1, Sr, s, [&](int t, int d0, int d1) { out[t * plane2] = pack_digits<B>(d0, d1); });
 }
 
+// Residues for the CRT scheme (ozcrt.cuh), same view, padding and thread
+// mapping as ozaki_split_kernel: residue q of element (r, c) goes to
+// D[q * plane + r * cols_pad + c] as fp16.  A thread computes the scaled
+// integers of its two elements once and their 18-bit pieces (NP of them,
+// T <= 18 NP), then per modulus x = sum_j h_j (2^(18 j) mod p) < 2^31,
+// one remainder by a magic multiplier and the balanced residue r, |r| <= 256.
+// The fp16 value: the bits 0x6600 + r are 1536 + r (exponent 2^10, mantissa
+// 512 + r in [256, 768]), and one fused multiply-add of the pair,
+// (1536 + r) * sign - 1536 * sign, is sign * r exactly.
+template <int NP>
+__global__ void __launch_bounds__(256)
+    ozaki_crt_split_kernel(int64_t rows, int64_t cols, int64_t rows_pad, int64_t cols_pad, int64_t plane,
+                           const q128* __restrict__ p, int64_t sr, int64_t sc, const int* __restrict__ S,
+                           const __grid_constant__ CrtTable tab, uint16_t* __restrict__ D) {
+  __shared__ __align__(16) CrtMod mods[kCrtMaxMods];
+  const int tid = threadIdx.y * 32 + threadIdx.x;
+  const int nvec = tab.n * (int)(sizeof(CrtMod) / 16);
+  for (int i = tid; i < nvec; i += 256)
+    reinterpret_cast<uint4*>(mods)[i] = reinterpret_cast<const uint4*>(tab.mod)[i];
+  __syncthreads();
+  const int64_t c = ((int64_t)blockIdx.x * 32 + threadIdx.x) * 2;
+  const int64_t r = (int64_t)blockIdx.y * 8 + threadIdx.y;
+  if (c >= cols_pad || r >= rows_pad) return;
+  uint32_t* out = reinterpret_cast<uint32_t*>(D + r * cols_pad + c);
+  const int64_t plane2 = plane / 2;
+  q128 v0 = q_zero(0), v1 = q_zero(0);
+  int Sr = kOzakiScaleEmpty;
+  if (r < rows) {
+    Sr = S[r];
+    if (c < cols) v0 = ld_cached(p + r * sr + c * sc);
+    if (c + 1 < cols) v1 = ld_cached(p + r * sr + (c + 1) * sc);
+  }
+  uint64_t a0, a1, a2, b0, b1, b2;
+  bool na, nb;
+  ozaki_scaled_bits(v0, Sr, tab.T, a0, a1, a2, na);
+  ozaki_scaled_bits(v1, Sr, tab.T, b0, b1, b2, nb);
+  uint32_t ha[NP], hb[NP];
+  crt_pieces<NP>(a0, a1, a2, ha);
+  crt_pieces<NP>(b0, b1, b2, hb);
+  const uint32_t sg = (na ? 0xBC00u : 0x3C00u) | ((nb ? 0xBC00u : 0x3C00u) << 16);
+  const uint32_t bs = (na ? 0x6600u : 0xE600u) | ((nb ? 0x6600u : 0xE600u) << 16);
+  const __half2 hsg = *reinterpret_cast<const __half2*>(&sg), hbs = *reinterpret_cast<const __half2*>(&bs);
+#pragma unroll 2
+  for (int q = 0; q < tab.n; ++q) {
+    const CrtMod& m = mods[q];
+    // (0x6600 + ra) | (0x6600 + rb) << 16 from the shifted residues
+    const uint32_t bits = crt_residue_shifted<NP>(ha, m) + (crt_residue_shifted<NP>(hb, m) << 16) + m.bias2;
+    const __half2 v = __hfma2(*reinterpret_cast<const __half2*>(&bits), hsg, hbs);
+    out[q * plane2] = *reinterpret_cast<const uint32_t*>(&v);
+  }
+}
+
 // ---------------------------------------------------------------------------
 // tcgen05 digit GEMM
 // ---------------------------------------------------------------------------
@@ -152,8 +206,13 @@ struct OzakiMmaParams {
   int m_pad, n_pad;
   int kb_begin, kb_end;  // k-blocks of this pass
   int chunk_kb;          // k-blocks summed exactly in fp32 before a readout
-  int32_t* C;            // [G+1][m_pad][n_pad]
+  int32_t* C;            // [G+1][m_pad][n_pad] (digit pairs)
   int* err;              // set to nonzero on a timeout
+  // CRT scheme: unit g is the single pair (g, g), the residue product of
+  // modulus g, and the epilogue stores y = (C mod p) u mod p (16 bits) in Y
+  int crt;
+  uint16_t* Y;                  // [G+1][m_pad][n_pad]
+  uint32_t crt_p[kCrtMaxMods], crt_magic[kCrtMaxMods], crt_K[kCrtMaxMods], crt_u[kCrtMaxMods];
 };
 
 // Instruction descriptors: kind::f16, D = f32, K-major A and B, N = 256,
@@ -243,8 +302,8 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
         int tile, g;
         cta_unit(P, j, tile, g);
         const int tm = tile / P.tiles_n, tn = tile % P.tiles_n;
-        for (int t = 0; t <= g && ok; ++t) {
-          const int u = g - t;
+        for (int t = P.crt ? g : 0; t <= g && ok; ++t) {
+          const int u = P.crt ? g : g - t;
           for (int kb = P.kb_begin; kb < P.kb_end && ok; ++kb, ++it) {
             const int s = it % kStages;
             const uint32_t round = it / kStages;
@@ -274,7 +333,7 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
       for (int j = 0; j < nun && ok; ++j) {
         int tile, g;
         cta_unit(P, j, tile, g);
-        for (int t = 0; t <= g && ok; ++t) {
+        for (int t = P.crt ? g : 0; t <= g && ok; ++t) {
           for (int ch = 0; ch < nchunks && ok; ++ch) {
             const int kb0 = P.kb_begin + ch * P.chunk_kb;
             const int kb1 = kb0 + P.chunk_kb < P.kb_end ? kb0 + P.chunk_kb : P.kb_end;
@@ -332,7 +391,7 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
       int tile, g;
       cta_unit(P, j, tile, g);
       const int tm = tile / P.tiles_n, tn = tile % P.tiles_n;
-      for (int t = 0; t <= g && ok; ++t) {
+      for (int t = P.crt ? g : 0; t <= g && ok; ++t) {
         for (int ch = 0; ch < nchunks && ok; ++ch) {
           const int buf = acc_it & 1;
           if (!mbar_wait(tfull_bar(buf), (acc_it >> 1) & 1u)) {
@@ -357,12 +416,30 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
       }
       if (!ok) break;
       // store diagonal g of this tile: row (tm*128 + row_in_tile), 128 columns
-      int32_t* dst = P.C + ((size_t)g * P.m_pad + (size_t)tm * kBM + row_in_tile) * P.n_pad +
-                     (size_t)tn * kBN + half * (kBN / 2);
+      const size_t off = ((size_t)g * P.m_pad + (size_t)tm * kBM + row_in_tile) * P.n_pad + (size_t)tn * kBN +
+                         half * (kBN / 2);
+      if (P.crt) {
+        // |acc| <= 2^29 (a pass holds 8192 of k): y = ((acc mod p) u) mod p < 2^16
+        const uint32_t p = P.crt_p[g], mg = P.crt_magic[g], K = P.crt_K[g], u = P.crt_u[g];
+        uint16_t* dst = P.Y + off;
 #pragma unroll
-      for (int i = 0; i < kBN / 2; i += 4) {
-        *reinterpret_cast<int4*>(dst + i) = make_int4(acc[i], acc[i + 1], acc[i + 2], acc[i + 3]);
-        acc[i] = acc[i + 1] = acc[i + 2] = acc[i + 3] = 0;
+        for (int i = 0; i < kBN / 2; ++i)
+          acc[i] = (int32_t)crt_mod(crt_mod((uint32_t)(acc[i] + (int32_t)K), p, mg) * u, p, mg);
+#pragma unroll
+        for (int i = 0; i < kBN / 2; i += 8) {
+          *reinterpret_cast<uint4*>(dst + i) =
+              make_uint4((uint32_t)acc[i] | ((uint32_t)acc[i + 1] << 16), (uint32_t)acc[i + 2] | ((uint32_t)acc[i + 3] << 16),
+                         (uint32_t)acc[i + 4] | ((uint32_t)acc[i + 5] << 16), (uint32_t)acc[i + 6] | ((uint32_t)acc[i + 7] << 16));
+#pragma unroll
+          for (int h = 0; h < 8; ++h) acc[i + h] = 0;
+        }
+      } else {
+        int32_t* dst = P.C + off;
+#pragma unroll
+        for (int i = 0; i < kBN / 2; i += 4) {
+          *reinterpret_cast<int4*>(dst + i) = make_int4(acc[i], acc[i + 1], acc[i + 2], acc[i + 3]);
+          acc[i] = acc[i + 1] = acc[i + 2] = acc[i + 3] = 0;
+        }
       }
     }
     if (!ok && lane == 0) atomicExch(P.err, 1);
@@ -385,6 +462,7 @@ struct OzakiFoldParams {
   int G, npass, b;
   int64_t m_pad, n_pad;
   const int32_t* C;      // [npass][G+1][m_pad][n_pad]
+  const uint16_t* Y;     // CRT: [npass][nmod][m_pad][n_pad] reduced residue products
   const int* S;          // row scales of op(A)
   const int* F;          // column scales of op(B)
   const uint32_t* fa;    // row special flags
@@ -446,6 +524,90 @@ __global__ void __launch_bounds__(256, 3) ozaki_fold_kernel(OzakiFoldParams P) {
   }
 }
 
+// CRT reconstruction per output (ozcrt.cuh).  The digit-product epilogue
+// stored y_q = (C_q mod p_q) u_q mod p_q per k pass (16 bits); y is linear in
+// C, so the passes' values add modulo p_q.  A thread takes two neighbouring
+// columns (one 32-bit copy per modulus and pass; a warp reads 128 contiguous
+// bytes of a plane, and all of a thread's copies are in flight at once),
+// accumulates the moduli in pairs, (y_q p_q' + y_q' p_q) M /
+// (p_q p_q'), into NW 64-bit word sums, then X = Y - Q M, one rounding at
+// 2^(S_i + F_j - 2T) and the reference epilogue.  The per-modulus constants
+// and the pair multiples of M are read from shared memory (broadcast).
+template <int NW>
+__global__ void __launch_bounds__(256) ozaki_crt_fold_kernel(OzakiFoldParams P, const __grid_constant__ CrtTable tab) {
+  __shared__ __align__(16) uint32_t smod[kCrtMaxMods][8];  // p, magic, K, u, P24
+  __shared__ __align__(16) uint32_t spair[kCrtMaxMods / 2][kCrtMaxWords];
+  __shared__ __align__(16) uint32_t snegM[kCrtMaxWords];
+  extern __shared__ uint32_t sy[];  // this block's y values, [modulus][thread] (dynamic: n * 1 KB)
+  const int tid = threadIdx.y * 32 + threadIdx.x;
+  for (int i = tid; i < tab.n * 2; i += 256)
+    reinterpret_cast<uint4*>(smod)[i] = reinterpret_cast<const uint4*>(&tab.mod[i >> 1])[i & 1];
+  for (int i = tid; i < (kCrtMaxMods / 2) * kCrtMaxWords; i += 256) (&spair[0][0])[i] = (&tab.Mpair[0][0])[i];
+  if (tid < kCrtMaxWords) snegM[tid] = tab.negM[tid];
+  __syncthreads();
+  const int64_t j0 = ((int64_t)blockIdx.x * 32 + threadIdx.x) * 2;
+  const int64_t i = (int64_t)blockIdx.y * 8 + threadIdx.y;
+  if (i >= P.m || j0 >= P.n) return;
+  const int n = tab.n;
+  const size_t plane = (size_t)P.m_pad * P.n_pad / 2;  // 32-bit words (two columns)
+  const size_t pass = (size_t)n * plane;
+  const uint32_t* src = reinterpret_cast<const uint32_t*>(P.Y + (size_t)i * P.n_pad + j0);
+  // every y of this thread's two columns into shared memory at once (one
+  // asynchronous 4-byte copy per modulus, all in flight together); with
+  // several k passes their values are added modulo p instead
+  if (P.npass == 1) {
+    for (int q = 0; q < n; ++q)
+      asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(&sy[q * 256 + tid])),
+                   "l"(src + q * plane)
+                   : "memory");
+    asm volatile("cp.async.wait_all;" ::: "memory");
+  } else {
+    for (int q = 0; q < n; ++q) {
+      const uint32_t p = smod[q][0], mg = smod[q][1];
+      uint32_t lo = 0, hi = 0;
+      for (int ps = 0; ps < P.npass; ++ps) {
+        const uint32_t w = __ldcs(src + ps * pass + q * plane);
+        lo += w & 0xFFFFu;
+        hi += w >> 16;
+      }
+      sy[q * 256 + tid] = crt_mod(lo, p, mg) | (crt_mod(hi, p, mg) << 16);
+    }
+  }
+  CrtAcc<NW> A0, A1;
+  crt_acc_init(A0);
+  crt_acc_init(A1);
+  for (int q0 = 0; q0 < n; q0 += 2) {
+    const int q1 = q0 + 1;
+    const uint32_t c0 = sy[q0 * 256 + tid], c1 = q1 < n ? sy[q1 * 256 + tid] : 0u;
+    const uint32_t p0 = smod[q0][0], P0 = smod[q0][4];
+    const uint32_t p1 = q1 < n ? smod[q1][0] : 1u, P1 = q1 < n ? smod[q1][4] : 0u;
+    uint32_t W[kCrtMaxWords];
+#pragma unroll
+    for (int v = 0; v < kCrtMaxWords / 4; ++v) {
+      const uint4 t = reinterpret_cast<const uint4*>(spair[q0 >> 1])[v];
+      W[4 * v] = t.x;
+      W[4 * v + 1] = t.y;
+      W[4 * v + 2] = t.z;
+      W[4 * v + 3] = t.w;
+    }
+    crt_acc_pair(A0, c0 & 0xFFFFu, c1 & 0xFFFFu, p0, p1, P0, P1, W);
+    crt_acc_pair(A1, c0 >> 16, c1 >> 16, p0, p1, P0, P1, W);
+  }
+  const bool failed = *P.err != 0;
+  const int Si = P.S[i];
+  const uint32_t fai = P.fa[i];
+#pragma unroll
+  for (int c = 0; c < 2; ++c) {
+    const int64_t j = j0 + c;
+    if (j < P.n && !(fai | P.fb[j])) {  // NaN / inf rows and columns: ozaki_special_kernel
+      q128* cp = P.Cout + i * P.sci + j * P.scj;
+      const q128 cold = *cp;
+      const q128 sum = failed ? q_nan() : crt_acc_round(c ? A1 : A0, snegM, Si + P.F[j] - 2 * tab.T);
+      *cp = q_epilogue(P.alpha, sum, P.beta, cold);
+    }
+  }
+}
+
 // Outputs in a row of op(A) or a column of op(B) that holds a NaN or an
 // infinity: a direct wide-accumulator dot, so IEEE special-value semantics
 // are kept (every such sum contains a special product, so it is exact).
@@ -496,21 +658,36 @@ static int pass_kblocks(int s, int b) {
   return chunks * chunk_kblocks(b);
 }
 
+// The CRT scheme's table for this call, or false for the digit pairs:
+// scheme 1 asks for digit pairs; otherwise residues whenever the table for
+// T = bits * digits - 1 and this k fits (ozcrt.cuh).
+static bool ozaki_crt_table(int scheme, int digits, int bits, int64_t k, CrtTable& tab) {
+  if (scheme == 1) return false;
+  return crt_build(bits * digits - 1, k, tab);
+}
+
 struct OzakiLayout {
   int64_t m_pad, n_pad, k_pad;
   int s, b, G, npass;
+  int nmod;   // CRT moduli (0: digit pairs)
+  int kbp;    // k-blocks per pass
   size_t off_S, off_F, off_fa, off_fb, off_err, off_DA, off_DB, off_C, total;
 };
 
-static OzakiLayout ozaki_layout(int64_t m, int64_t n, int64_t k, int s, int b) {
+// Scratch layout: s digit planes per operand and G + 1 = s diagonal planes
+// per k pass, or (CRT) nmod residue planes per operand and per k pass.
+static OzakiLayout ozaki_layout(int64_t m, int64_t n, int64_t k, int s, int b, int nmod) {
   OzakiLayout L;
   L.s = s;
   L.b = b;
-  L.G = s - 1;
+  L.nmod = nmod;
+  const int planes = nmod ? nmod : s;
+  L.G = planes - 1;
   L.m_pad = rup(m, kBM);
   L.n_pad = rup(n, kBN);
   L.k_pad = rup(k, kBK);
-  int64_t kbp = pass_kblocks(s, b);
+  L.kbp = nmod ? kCrtPassK / kBK : pass_kblocks(s, b);
+  const int64_t kbp = L.kbp;
   L.npass = (int)((L.k_pad / kBK + kbp - 1) / kbp);
   size_t o = 0;
   L.off_S = o;  o += align256((size_t)m * 4);
@@ -518,9 +695,9 @@ static OzakiLayout ozaki_layout(int64_t m, int64_t n, int64_t k, int s, int b) {
   L.off_fa = o; o += align256((size_t)m * 4);
   L.off_fb = o; o += align256((size_t)n * 4);
   L.off_err = o; o += 256;
-  L.off_DA = o; o += align256((size_t)s * L.m_pad * L.k_pad * 2);
-  L.off_DB = o; o += align256((size_t)s * L.n_pad * L.k_pad * 2);
-  L.off_C = o;  o += align256((size_t)L.npass * (L.G + 1) * L.m_pad * L.n_pad * 4);
+  L.off_DA = o; o += align256((size_t)planes * L.m_pad * L.k_pad * 2);
+  L.off_DB = o; o += align256((size_t)planes * L.n_pad * L.k_pad * 2);
+  L.off_C = o;  o += align256((size_t)L.npass * (L.G + 1) * L.m_pad * L.n_pad * (nmod ? 2 : 4));
   L.total = o;
   return L;
 }
@@ -582,9 +759,18 @@ int ozaki_profile_read(double* out, int* calls) {
   return 0;
 }
 
-size_t ozaki_scratch_bytes(int64_t m, int64_t n, int64_t k, int digits, int bits) {
+static int ozaki_nmod(int scheme, int digits, int bits, int64_t k) {
+  CrtTable tab;
+  return ozaki_crt_table(scheme, digits, bits, k, tab) ? tab.n : 0;
+}
+
+size_t ozaki_scratch_bytes(int64_t m, int64_t n, int64_t k, int digits, int bits, int scheme) {
   if (m <= 0 || n <= 0 || k <= 0) return 0;
-  return ozaki_layout(m, n, k, digits, bits).total;
+  return ozaki_layout(m, n, k, digits, bits, ozaki_nmod(scheme, digits, bits, k)).total;
+}
+
+bool ozaki_uses_crt(int64_t k, int digits, int bits, int scheme) {
+  return ozaki_nmod(scheme, digits, bits, k) > 0;
 }
 
 // Launches for the digit width b (7, 8 or 9).
@@ -609,12 +795,51 @@ static void launch_fold(int b, cudaStream_t st, const OzakiFoldParams& F) {
     ozaki_fold_kernel<9><<<grid, blk, 0, st>>>(F);
 }
 
+// CRT residues: 8 pieces of 18 bits cover T <= 144, 11 cover T <= 191.
+static void launch_crt_split(const CrtTable& tab, dim3 grid, dim3 blk, cudaStream_t st, int64_t rows,
+                             int64_t cols, int64_t rows_pad, int64_t cols_pad, int64_t plane, const q128* p,
+                             int64_t sr, int64_t sc, const int* S, uint16_t* D) {
+  if (tab.T <= 144)
+    ozaki_crt_split_kernel<8><<<grid, blk, 0, st>>>(rows, cols, rows_pad, cols_pad, plane, p, sr, sc, S, tab, D);
+  else
+    ozaki_crt_split_kernel<11><<<grid, blk, 0, st>>>(rows, cols, rows_pad, cols_pad, plane, p, sr, sc, S, tab, D);
+}
+
+static cudaError_t launch_crt_fold(const CrtTable& tab, cudaStream_t st, const OzakiFoldParams& F) {
+  dim3 blk(32, 8), grid((unsigned)((F.n + 63) / 64), (unsigned)((F.m + 7) / 8));
+  const size_t dyn = (size_t)tab.n * 256 * 4;
+  static bool attr_set[64] = {false};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev >= 0 && dev < 64 && !attr_set[dev]) {
+    const int mx = kCrtMaxMods * 256 * 4;
+    cudaError_t e;
+    if ((e = cudaFuncSetAttribute(ozaki_crt_fold_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx)) !=
+            cudaSuccess ||
+        (e = cudaFuncSetAttribute(ozaki_crt_fold_kernel<10>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx)) !=
+            cudaSuccess ||
+        (e = cudaFuncSetAttribute(ozaki_crt_fold_kernel<12>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx)) !=
+            cudaSuccess)
+      return e;
+    attr_set[dev] = true;
+  }
+  if (tab.nw <= 8)
+    ozaki_crt_fold_kernel<8><<<grid, blk, dyn, st>>>(F, tab);
+  else if (tab.nw <= 10)
+    ozaki_crt_fold_kernel<10><<<grid, blk, dyn, st>>>(F, tab);
+  else
+    ozaki_crt_fold_kernel<12><<<grid, blk, dyn, st>>>(F, tab);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scratch, cudaStream_t st,
-                              const OzakiOverlap* ov) {
+                              const OzakiOverlap* ov, int scheme) {
   if (g.m <= 0 || g.n <= 0 || g.k <= 0) return cudaSuccess;
   if ((bits < 7 || bits > 9) || digits < 2 || digits > ozaki_max_digits_for_k(bits, g.k))
     return cudaErrorInvalidValue;
-  OzakiLayout L = ozaki_layout(g.m, g.n, g.k, digits, bits);
+  CrtTable tab;
+  const bool crt = ozaki_crt_table(scheme, digits, bits, g.k, tab);
+  OzakiLayout L = ozaki_layout(g.m, g.n, g.k, digits, bits, crt ? tab.n : 0);
   char* base = static_cast<char*>(scratch);
   int* S = reinterpret_cast<int*>(base + L.off_S);
   int* F = reinterpret_cast<int*>(base + L.off_F);
@@ -624,6 +849,7 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scr
   uint16_t* DA = reinterpret_cast<uint16_t*>(base + L.off_DA);
   uint16_t* DB = reinterpret_cast<uint16_t*>(base + L.off_DB);
   int32_t* Cg = reinterpret_cast<int32_t*>(base + L.off_C);
+  uint16_t* Yq = reinterpret_cast<uint16_t*>(base + L.off_C);  // CRT: the same space as 16-bit planes
   cudaError_t e;
   const int sms = device_sm_count();
   PhaseEvents pev;
@@ -634,7 +860,7 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scr
       bool okev = true;
       for (int i = 0; i < 4; ++i) okev = okev && cudaEventCreate(&pev.ev[i]) == cudaSuccess;
       if (okev) pe = &pev;
-      int64_t pairs = (int64_t)L.s * (L.s + 1) / 2;
+      int64_t pairs = crt ? (int64_t)tab.n : (int64_t)L.s * (L.s + 1) / 2;
       pev.mma_flop_units = (int64_t)((2.0 * g.m * g.n * g.k * pairs) / 1048576.0);
     }
   }
@@ -656,7 +882,10 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scr
     unsigned bb = (unsigned)std::min<int64_t>((wb + 255) / 256, (int64_t)sms * 8);
     ozaki_scale_kernel<<<bb, 256, 0, sb>>>(g.n, g.k, g.B, g.sbj, g.sbl, F, fb);
     dim3 gb((unsigned)(L.k_pad / 64), (unsigned)(L.n_pad / 8));
-    launch_split(L.b, gb, blk, sb, g.n, g.k, L.n_pad, L.k_pad, plane_b, g.B, g.sbj, g.sbl, F, L.s, DB);
+    if (crt)
+      launch_crt_split(tab, gb, blk, sb, g.n, g.k, L.n_pad, L.k_pad, plane_b, g.B, g.sbj, g.sbl, F, DB);
+    else
+      launch_split(L.b, gb, blk, sb, g.n, g.k, L.n_pad, L.k_pad, plane_b, g.B, g.sbj, g.sbl, F, L.s, DB);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     if (ov) {
       if ((e = cudaEventRecord(ov->b_done, sb)) != cudaSuccess) return e;
@@ -674,8 +903,12 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scr
     if (rows > 0) ozaki_scale_kernel<<<ba, 256, 0, sa>>>(rows, g.k, g.A + r0 * g.sai, g.sai, g.sal, S + r0, fa + r0);
     dim3 ga((unsigned)(L.k_pad / 64), (unsigned)((r1 - r0) / 8));
     const q128* Ab = g.A + r0 * g.sai;
-    launch_split(L.b, ga, blk, sa, rows, g.k, r1 - r0, L.k_pad, plane_a, Ab, g.sai, g.sal, S + r0, L.s,
-                 DA + r0 * L.k_pad);
+    if (crt)
+      launch_crt_split(tab, ga, blk, sa, rows, g.k, r1 - r0, L.k_pad, plane_a, Ab, g.sai, g.sal, S + r0,
+                       DA + r0 * L.k_pad);
+    else
+      launch_split(L.b, ga, blk, sa, rows, g.k, r1 - r0, L.k_pad, plane_a, Ab, g.sai, g.sal, S + r0, L.s,
+                   DA + r0 * L.k_pad);
     if ((ee = cudaGetLastError()) != cudaSuccess) return ee;
     if (banded) {
       if ((ee = cudaEventRecord(ov->a_done, sa)) != cudaSuccess) return ee;
@@ -688,8 +921,8 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scr
   // the bands are whole waves of tiles (one tile per SM), at most 8, and
   // each band's digit products start as soon as its rows of op(A) are cut.
   CUtensorMap tmA, tmB;
-  if (!make_map(&tmA, DA, (int64_t)L.s * L.m_pad, L.k_pad, kBM, L.b == 9) ||
-      !make_map(&tmB, DB, (int64_t)L.s * L.n_pad, L.k_pad, kBN, L.b == 9))
+  if (!make_map(&tmA, DA, (int64_t)(L.G + 1) * L.m_pad, L.k_pad, kBM, crt || L.b == 9) ||
+      !make_map(&tmB, DB, (int64_t)(L.G + 1) * L.n_pad, L.k_pad, kBN, crt || L.b == 9))
     return cudaErrorInvalidValue;
   static bool attr_set[64] = {false};
   int dev = 0;
@@ -702,7 +935,7 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scr
   }
   const int tiles_m = (int)(L.m_pad / kBM), tiles_n = (int)(L.n_pad / kBN);
   const int tiles = tiles_m * tiles_n;
-  const int kb_total = (int)(L.k_pad / kBK), kbp = pass_kblocks(L.s, L.b);
+  const int kb_total = (int)(L.k_pad / kBK), kbp = L.kbp;
   int band_tiles = tiles;
   if (banded) {
     const int waves = (tiles + sms - 1) / sms;
@@ -715,7 +948,7 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scr
   F2.m = g.m; F2.n = g.n; F2.k = g.k;
   F2.G = L.G; F2.npass = L.npass; F2.b = L.b;
   F2.m_pad = L.m_pad; F2.n_pad = L.n_pad;
-  F2.C = Cg; F2.S = S; F2.F = F; F2.fa = fa; F2.fb = fb;
+  F2.C = Cg; F2.Y = Yq; F2.S = S; F2.F = F; F2.fa = fa; F2.fb = fb;
   F2.A = g.A; F2.sai = g.sai; F2.sal = g.sal;
   F2.B = g.B; F2.sbl = g.sbl; F2.sbj = g.sbj;
   F2.Cout = g.C; F2.sci = g.sci; F2.scj = g.scj;
@@ -733,11 +966,16 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scr
     OzakiFoldParams Fb = F2;
     Fb.m = i1 - i0;
     Fb.C = Cg + (size_t)i0 * L.n_pad;
+    Fb.Y = Yq + (size_t)i0 * L.n_pad;
     Fb.S = S + i0;
     Fb.fa = fa + i0;
     Fb.A = g.A + i0 * g.sai;
     Fb.Cout = g.C + i0 * g.sci;
-    launch_fold(L.b, st, Fb);
+    if (crt) {
+      if ((ee = launch_crt_fold(tab, st, Fb)) != cudaSuccess) return ee;
+    } else {
+      launch_fold(L.b, st, Fb);
+    }
     dim3 fblk(32, 8), fgrid((unsigned)((g.n + 31) / 32), (unsigned)((Fb.m + 7) / 8));
     if ((ee = cudaGetLastError()) != cudaSuccess) return ee;
     ozaki_special_kernel<<<fgrid, fblk, 0, st>>>(Fb);
@@ -762,14 +1000,23 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scr
       P.tiles_n = tiles_n;
       P.tile_begin = t0;
       P.tile_end = t1;
-      P.idesc = L.b == 9 ? kIdescF16 : kIdescBf16;
+      P.idesc = (crt || L.b == 9) ? kIdescF16 : kIdescBf16;
       P.G = L.G;
       P.m_pad = (int)L.m_pad;
       P.n_pad = (int)L.n_pad;
       P.kb_begin = p * kbp;
       P.kb_end = std::min(kb_total, (p + 1) * kbp);
-      P.chunk_kb = chunk_kblocks(L.b);
+      P.chunk_kb = crt ? chunk_kblocks(9) : chunk_kblocks(L.b);
+      P.crt = crt ? 1 : 0;
+      for (int q = 0; q < kCrtMaxMods; ++q) {
+        const bool on = crt && q < tab.n;
+        P.crt_p[q] = on ? tab.mod[q].p : 1u;
+        P.crt_magic[q] = on ? tab.mod[q].magic : 0u;
+        P.crt_K[q] = on ? tab.mod[q].K : 0u;
+        P.crt_u[q] = on ? tab.mod[q].u : 0u;
+      }
       P.C = Cg + (size_t)p * (L.G + 1) * L.m_pad * L.n_pad;
+      P.Y = Yq + (size_t)p * (L.G + 1) * L.m_pad * L.n_pad;
       P.err = err;
       ozaki_mma_kernel<<<(unsigned)std::min(units, sms), kMmaThreads, kMmaSmem, st>>>(tmA, tmB, P);
       if ((e = cudaGetLastError()) != cudaSuccess) return e;
@@ -802,8 +1049,8 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scr
   return e;
 }
 
-size_t ozaki_error_flag_offset(int64_t m, int64_t n, int64_t k, int digits, int bits) {
-  return ozaki_layout(m, n, k, digits, bits).off_err;
+size_t ozaki_error_flag_offset(int64_t m, int64_t n, int64_t k, int digits, int bits, int scheme) {
+  return ozaki_layout(m, n, k, digits, bits, ozaki_nmod(scheme, digits, bits, k)).off_err;
 }
 
 }  // namespace qb

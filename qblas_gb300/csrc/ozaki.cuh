@@ -89,18 +89,17 @@ QB_HD uint32_t ozaki_field(uint64_t v0, uint64_t v1, uint64_t v2, int p) {
   return (uint32_t)(x & mask);
 }
 
-// V = trunc(|a| * 2^(B*s - 1 - S)) as three 64-bit words and the sign of a;
-// V = 0 for zero, NaN, infinity and an empty scale.
-template <int B>
-QB_HD void ozaki_scaled(q128 a, int S, int s, uint64_t& v0, uint64_t& v1, uint64_t& v2, bool& neg) {
+// V = trunc(|a| * 2^(T - S)) (V < 2^T, T <= 191) as three 64-bit words and
+// the sign of a; V = 0 for zero, NaN, infinity and an empty scale.
+QB_HD void ozaki_scaled_bits(q128 a, int S, int T, uint64_t& v0, uint64_t& v1, uint64_t& v2, bool& neg) {
   v0 = v1 = v2 = 0;
   neg = q_sign(a) != 0;
   if (q_bexp(a) == kExpField || q_iszero(a) || S == kOzakiScaleEmpty) return;
   uint64_t mh, ml;
   int E;
   q_unpack_norm(a, mh, ml, E);
-  // V = trunc(m * 2^(E + B*s - 113 - S)); the shift is at most B*s - 114.
-  int sh = E + B * s - 113 - S;
+  // V = trunc(m * 2^(E + T - 112 - S)); the shift is at most T - 113.
+  int sh = E + T - 112 - S;
   if (sh >= 0) {
     u256 t = u256_shl(u256_make(0, 0, mh, ml), sh);
     v0 = t.w0;
@@ -112,6 +111,12 @@ QB_HD void ozaki_scaled(q128 a, int S, int s, uint64_t& v0, uint64_t& v1, uint64
     v0 = t.w0;
     v1 = t.w1;
   }
+}
+
+// The digit split's scaled integer: T = B*s - 1.
+template <int B>
+QB_HD void ozaki_scaled(q128 a, int S, int s, uint64_t& v0, uint64_t& v1, uint64_t& v2, bool& neg) {
+  ozaki_scaled_bits(a, S, B * s - 1, v0, v1, v2, neg);
 }
 
 // Digit j (0 = least significant) of V from its raw field and the running

@@ -1,0 +1,343 @@
+// Ozaki scheme II for qgemm: exact integer products through residues.
+//
+// Published method: K. Ozaki, Y. Uchino, T. Imamura, "Ozaki Scheme II: A
+// GEMM-oriented emulation of floating-point matrix multiplication using an
+// integer modular technique" (2025).  Restated here for binary128 operands
+// and fp16 digit products on the tensor cores.
+//
+// Rows of op(A) are scaled as in the digit split (ozaki.cuh): with S_i the
+// row scale, a_il becomes the integer A'_il = sign * trunc(|a_il| 2^(T-S_i)),
+// |A'| < 2^T, and the columns of op(B) likewise (scale F_j).  The exact
+// integer X_ij = sum_l A'_il B'_lj (|X| < k 2^(2T)) is then computed modulo N
+// pairwise coprime moduli p_q in (256, 513]: for each q the balanced
+// residues of A' and B' (|r| <= 256, exact in fp16) are multiplied on the
+// tensor cores (an fp32 sum of 256 products of at most 2^16 is exact), and
+// C_q = sum_l r_q(A'_il) r_q(B'_lj) == X_ij (mod p_q).  With M = prod p_q >
+// 8 k 2^(2T), the Chinese remainder theorem gives X_ij back exactly:
+//     Y = sum_q y_q M / p_q,   y_q = (C_q mod p_q) (M / p_q)^-1 mod p_q,
+//     X = Y - Q M,             Q = round(sum_q y_q / p_q),
+// and sum_l a_il b_lj ~= X 2^(S_i + F_j - 2T) is rounded once.  The only
+// error is the truncation of the operands to T bits, the same truncation as
+// the digit split with b*s - 1 = T bits, without its dropped digit pairs; the
+// number of tensor-core products is N (about (2T + log2 k + 3) / 8.8) instead
+// of s(s+1)/2.
+#pragma once
+#include <stdint.h>
+
+#include "ozaki.cuh"
+
+namespace qb {
+
+constexpr int kCrtMaxMods = 48;    // moduli (about 414 bits)
+constexpr int kCrtMaxWords = 12;   // 32-bit words of the reconstruction (384 bits)
+constexpr int kCrtPieces = 11;     // 18-bit pieces of a scaled operand (T <= 191)
+constexpr int kCrtPassK = 8192;    // k per pass: |C_q| <= 8192 * 2^16 = 2^29
+
+struct alignas(16) CrtMod {
+  uint32_t p;      // modulus, 257..513
+  uint32_t magic;  // ceil(2^40 / p): x mod p = x - p ((x magic) >> 40) for x < 2^40 / 513
+  uint32_t K;      // p ceil(2^29 / p): c + K >= 0 for |c| <= 2^29
+  uint32_t u;      // (M / p)^-1 mod p
+  uint32_t P24;    // round(2^24 / p), for the estimate of Q
+  uint32_t half;   // floor(p / 2): balanced residues are ((x + half) mod p) - half
+  uint32_t bias2;  // (0x6600 - half) * 0x10001: two shifted residues to fp16 bits 0x6600 + r
+  uint32_t pad;
+  uint32_t c18[kCrtPieces];  // 2^(18 j) mod p
+  uint32_t pad2;
+};
+
+// 16-byte aligned (also as a kernel parameter): the kernels copy it with
+// 16-byte loads.
+struct alignas(16) CrtTable {
+  int n;   // moduli in use
+  int nw;  // 32-bit words of the reconstruction (8, 10 or 12; M < 2^(32 nw))
+  int T;   // |A'|, |B'| < 2^T
+  int pad;
+  CrtMod mod[kCrtMaxMods];
+  // M / (p_2i p_2i+1) (M / p_2i for a last unpaired modulus), little-endian words
+  uint32_t Mpair[kCrtMaxMods / 2][kCrtMaxWords];
+  uint32_t negM[kCrtMaxWords];  // 2^(32 nw) - M
+};
+static_assert(sizeof(CrtMod) == 80 && sizeof(CrtTable) <= 8192, "CRT table layout (a kernel parameter)");
+
+// ---------------------------------------------------------------------------
+// Host: the moduli and the table
+// ---------------------------------------------------------------------------
+// Pairwise coprime moduli, greedily from 513 down: 513, 512, 511, 509, 505,
+// 503, 499, 493, ... (50 of them above 256).
+inline int crt_moduli(uint32_t* out, int cap) {
+  int n = 0;
+  for (uint32_t p = 513; p > 256 && n < cap; --p) {
+    bool ok = true;
+    for (int i = 0; i < n && ok; ++i) {
+      uint32_t a = p, b = out[i];
+      while (b) {
+        const uint32_t t = a % b;
+        a = b;
+        b = t;
+      }
+      ok = a == 1;
+    }
+    if (ok) out[n++] = p;
+  }
+  return n;
+}
+
+// little-endian multiword helpers (host)
+inline void crt_big_mul_small(uint32_t* w, int nw, uint32_t f) {
+  uint64_t c = 0;
+  for (int i = 0; i < nw; ++i) {
+    c += (uint64_t)w[i] * f;
+    w[i] = (uint32_t)c;
+    c >>= 32;
+  }
+}
+
+inline int crt_big_bits(const uint32_t* w, int nw) {
+  for (int i = nw - 1; i >= 0; --i)
+    if (w[i]) {
+      int b = 32;
+      while (!((w[i] >> (b - 1)) & 1u)) --b;
+      return 32 * i + b;
+    }
+  return 0;
+}
+
+inline uint32_t crt_inverse(uint32_t a, uint32_t p) {  // a^-1 mod p, gcd(a, p) = 1
+  int64_t t = 0, nt = 1, r = p, nr = a % p;
+  while (nr) {
+    const int64_t q = r / nr, tt = t - q * nt, rr = r - q * nr;
+    t = nt;
+    nt = tt;
+    r = nr;
+    nr = rr;
+  }
+  return (uint32_t)(t < 0 ? t + p : t);
+}
+
+// Bits the moduli product must exceed for operands of T bits and inner
+// dimension k: |X| < k 2^(2T) <= M / 8.
+inline int crt_needed_bits(int T, int64_t k) {
+  int lk = 0;
+  while (lk < 62 && ((int64_t)1 << lk) < k) ++lk;
+  return 2 * T + lk + 3;
+}
+
+// Fills `tab` for T-bit operands and inner dimension k; false when more than
+// kCrtMaxMods moduli or kCrtMaxWords words would be needed (or T > 191).
+inline bool crt_build(int T, int64_t k, CrtTable& tab) {
+  if (T < 2 || T > 191 || k < 1) return false;
+  uint32_t P[64];
+  const int avail = crt_moduli(P, 64);
+  const int need = crt_needed_bits(T, k);
+  uint32_t M[kCrtMaxWords + 2] = {1};
+  int n = 0;
+  while (crt_big_bits(M, kCrtMaxWords + 2) <= need) {
+    if (n == kCrtMaxMods || n == avail) return false;
+    crt_big_mul_small(M, kCrtMaxWords + 2, P[n++]);
+  }
+  int nw = (crt_big_bits(M, kCrtMaxWords + 2) + 31) / 32;
+  nw += nw & 1;
+  if (nw < 8) nw = 8;  // the reconstruction runs on 8, 10 or 12 words
+  if (nw > kCrtMaxWords) return false;
+  tab = CrtTable();
+  tab.n = n;
+  tab.nw = nw;
+  tab.T = T;
+  for (int q = 0; q < n; ++q) {
+    CrtMod& m = tab.mod[q];
+    const uint32_t p = P[q];
+    m.p = p;
+    m.magic = (uint32_t)(((1ull << 40) + p - 1) / p);
+    m.K = p * (uint32_t)(((1u << 29) + p - 1) / p);
+    m.P24 = (uint32_t)(((1u << 24) + p / 2) / p);
+    m.half = p / 2;
+    m.bias2 = (0x6600u - p / 2) * 0x10001u;
+    uint32_t c = 1 % p;
+    for (int j = 0; j < kCrtPieces; ++j) {
+      m.c18[j] = c;
+      c = (uint32_t)(((uint64_t)c << 18) % p);
+    }
+    uint64_t Mq = 1;  // (M / p) mod p
+    for (int r = 0; r < n; ++r)
+      if (r != q) Mq = Mq * P[r] % p;
+    m.u = crt_inverse((uint32_t)Mq, p);
+  }
+  for (int i = 0; 2 * i < n; ++i) {
+    uint32_t W[kCrtMaxWords + 2] = {1};
+    for (int r = 0; r < n; ++r)
+      if (r != 2 * i && r != 2 * i + 1) crt_big_mul_small(W, kCrtMaxWords + 2, P[r]);
+    for (int w = 0; w < kCrtMaxWords; ++w) tab.Mpair[i][w] = w < nw ? W[w] : 0u;
+  }
+  uint64_t b = 1;  // 2^(32 nw) - M = ~M + 1 over nw words
+  for (int w = 0; w < nw; ++w) {
+    b += (uint64_t)(uint32_t)~M[w];
+    tab.negM[w] = (uint32_t)b;
+    b >>= 32;
+  }
+  return true;
+}
+
+// ---------------------------------------------------------------------------
+// Residues and reconstruction (host and device)
+// ---------------------------------------------------------------------------
+// x mod p for x < 2^31: with magic = ceil(2^40 / p) = (2^40 + e) / p,
+// 0 <= e < p <= 513, x magic / 2^40 = x / p + x e / (p 2^40) and x e < 2^40,
+// so the floor is floor(x / p).
+QB_HD uint32_t crt_mod(uint32_t x, uint32_t p, uint32_t magic) {
+#if defined(__CUDA_ARCH__)
+  const uint32_t q = __umulhi(x, magic) >> 8;
+#else
+  const uint32_t q = (uint32_t)(((uint64_t)x * magic) >> 40);
+#endif
+  return x - q * p;
+}
+
+// The 18-bit pieces of V = (v2:v1:v0), least significant first (NP = 8
+// covers T <= 144, 11 covers T <= 198); the shifts are constants once the
+// loop is unrolled.
+template <int NP>
+QB_HD void crt_pieces(uint64_t v0, uint64_t v1, uint64_t v2, uint32_t (&h)[NP]) {
+#pragma unroll
+  for (int j = 0; j < NP; ++j) {
+    const int b = 18 * j, w = b >> 6, o = b & 63;
+    uint64_t x = (w == 0 ? v0 : (w == 1 ? v1 : v2)) >> o;
+    if (o > 46 && w < 2) x |= (w == 0 ? v1 : v2) << (64 - o);
+    h[j] = (uint32_t)x & 0x3FFFFu;
+  }
+}
+
+// The balanced residue r == V (mod p), |r| <= floor(p/2) <= 256, of V with
+// pieces h, plus floor(p/2): (V + floor(p/2)) mod p, from
+// x = floor(p/2) + sum_j h_j (2^(18 j) mod p) < 256 + 11 * 2^18 * 512 < 2^31.
+template <int NP>
+QB_HD uint32_t crt_residue_shifted(const uint32_t (&h)[NP], const CrtMod& m) {
+  uint32_t x = m.half;
+#pragma unroll
+  for (int j = 0; j < NP; ++j) x += h[j] * m.c18[j];
+  return crt_mod(x, m.p, m.magic);
+}
+
+template <int NP>
+QB_HD int crt_residue(const uint32_t (&h)[NP], const CrtMod& m) {
+  return (int)crt_residue_shifted<NP>(h, m) - (int)m.half;
+}
+
+// The N balanced residues of a (sign included) for row scale S, T bits.
+QB_HD void crt_residues(q128 a, int S, const CrtTable& tab, int* r) {
+  uint64_t v0, v1, v2;
+  bool neg;
+  ozaki_scaled_bits(a, S, tab.T, v0, v1, v2, neg);
+  uint32_t h[kCrtPieces];
+  crt_pieces<kCrtPieces>(v0, v1, v2, h);
+  for (int q = 0; q < tab.n; ++q) {
+    const int x = crt_residue<kCrtPieces>(h, tab.mod[q]);
+    r[q] = neg ? -x : x;
+  }
+}
+
+// C_q mod p for |C_q| <= 2^29 (one pass), and y_q = (C_q mod p) u_q mod p.
+QB_HD uint32_t crt_reduce(int32_t c, const CrtMod& m) {
+  return crt_mod((uint32_t)(c + (int32_t)m.K), m.p, m.magic);
+}
+QB_HD uint32_t crt_y(uint32_t r, const CrtMod& m) { return crt_mod(r * m.u, m.p, m.magic); }
+
+// Reconstruction accumulators of one output: Y = sum_q y_q M / p_q by 32-bit
+// word position (each word sum stays below 2^57), and sum_q y_q round(2^24 /
+// p_q), whose rounding to a multiple of 2^24 is Q (its error is below
+// 48 * 513 * 2^-25 < 2^-10 units of 2^24, and |X / M| < 1/8).
+template <int NW>
+struct CrtAcc {
+  uint64_t a[NW];
+  uint32_t q;
+};
+
+template <int NW>
+QB_HD void crt_acc_init(CrtAcc<NW>& A) {
+#pragma unroll
+  for (int w = 0; w < NW; ++w) A.a[w] = 0;
+  A.q = 0;
+}
+
+// Adds moduli p0 and p1 (residue terms y0, y1) with W = M / (p0 p1):
+// y0 M / p0 + y1 M / p1 = (y0 p1 + y1 p0) W.  A last unpaired modulus is
+// passed with y1 = 0, p1 = 1, P1 = 0 and W = M / p0.
+template <int NW>
+QB_HD void crt_acc_pair(CrtAcc<NW>& A, uint32_t y0, uint32_t y1, uint32_t p0, uint32_t p1, uint32_t P0,
+                        uint32_t P1, const uint32_t* W) {
+  A.q += y0 * P0 + y1 * P1;
+  const uint32_t z = y0 * p1 + y1 * p0;  // < 2 * 513^2 < 2^20
+#pragma unroll
+  for (int w = 0; w < NW; ++w) A.a[w] += (uint64_t)z * W[w];
+}
+
+// X = Y - Q M (two's complement modulo 2^(32 NW); |X| < M / 8), and
+// X 2^e rounded to binary128 (RNE).
+template <int NW>
+QB_HD q128 crt_acc_round(const CrtAcc<NW>& A, const uint32_t* negM, int e) {
+  static_assert(NW % 2 == 0 && NW >= 8, "reconstruction of 8, 10 or 12 words");
+  constexpr int H = NW / 2;
+  const uint64_t Q = (A.q + (1u << 23)) >> 24;
+  uint32_t X[NW];
+  uint64_t c = 0;
+#pragma unroll
+  for (int w = 0; w < NW; ++w) {
+    c += A.a[w] + Q * negM[w];
+    X[w] = (uint32_t)c;
+    c >>= 32;
+  }
+  const uint32_t neg = X[NW - 1] >> 31;
+  if (neg) {
+    uint64_t b = 1;
+#pragma unroll
+    for (int w = 0; w < NW; ++w) {
+      b += (uint32_t)~X[w];
+      X[w] = (uint32_t)b;
+      b >>= 32;
+    }
+  }
+  uint64_t V[H];
+#pragma unroll
+  for (int i = 0; i < H; ++i) V[i] = (uint64_t)X[2 * i] | ((uint64_t)X[2 * i + 1] << 32);
+  // the top four 64-bit words holding the leading one; lower words go to sticky
+  u256 m = u256_make(V[3], V[2], V[1], V[0]);
+  int drop = 0;
+#pragma unroll
+  for (int d = 1; d <= H - 4; ++d)
+    if (V[3 + d] != 0) {
+      m = u256_make(V[3 + d], V[2 + d], V[1 + d], V[d]);
+      drop = d;
+    }
+  bool sticky = false;
+#pragma unroll
+  for (int i = 0; i < H - 4; ++i) sticky = sticky || (i < drop && V[i] != 0);
+  return round_pack(neg, m, sticky, e + 64 * drop);
+}
+
+// Host and test form: the binary128 value of X 2^e for the residue sums
+// C_q (one pass, |C_q| <= 2^29) of one output.
+template <int NW>
+QB_HD q128 crt_reconstruct(const int32_t* C, const CrtTable& tab, int e) {
+  CrtAcc<NW> A;
+  crt_acc_init(A);
+  for (int i = 0; 2 * i < tab.n; ++i) {
+    const CrtMod& m0 = tab.mod[2 * i];
+    const uint32_t y0 = crt_y(crt_reduce(C[2 * i], m0), m0);
+    if (2 * i + 1 < tab.n) {
+      const CrtMod& m1 = tab.mod[2 * i + 1];
+      const uint32_t y1 = crt_y(crt_reduce(C[2 * i + 1], m1), m1);
+      crt_acc_pair(A, y0, y1, m0.p, m1.p, m0.P24, m1.P24, tab.Mpair[i]);
+    } else {
+      crt_acc_pair(A, y0, 0u, m0.p, 1u, m0.P24, 0u, tab.Mpair[i]);
+    }
+  }
+  return crt_acc_round(A, tab.negM, e);
+}
+
+QB_HD q128 crt_reconstruct_any(const int32_t* C, const CrtTable& tab, int e) {
+  if (tab.nw <= 8) return crt_reconstruct<8>(C, tab, e);
+  if (tab.nw <= 10) return crt_reconstruct<10>(C, tab, e);
+  return crt_reconstruct<12>(C, tab, e);
+}
+
+}  // namespace qb

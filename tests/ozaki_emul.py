@@ -47,3 +47,27 @@ def gemm_sum(sq, m, n, k, A, sai, sal, B, sbl, sbj, s, b=8):
     SA, DA = split(sq, A, m, k, sai, sal, s, b)
     SB, DB = split(sq, B, n, k, sbj, sbl, s, b)  # op(B)^T rows = columns of op(B)
     return fold(sq, diagonals(DA, DB), SA, SB, b)
+
+
+def crt_split(sq, X, rows, cols, sr, sc, T, k):
+    """Row scales and the balanced residues R[q][r][c] of the CRT scheme."""
+    nmax = 48
+    S = np.zeros(rows, dtype=np.int32)
+    R = np.zeros((nmax, rows, cols), dtype=np.int32)
+    n = sq.sq_crt_split(c64(rows), c64(cols), P(np.ascontiguousarray(X)), c64(sr), c64(sc), ctypes.c_int(T),
+                        c64(k), P(S), P(R))
+    assert n > 0
+    return S, R[:n]
+
+
+def crt_gemm_sum(sq, m, n, k, A, sai, sal, B, sbl, sbj, T):
+    """round(sum_l op(A)(i,l) op(B)(l,j)) as the CRT scheme computes it for
+    T-bit operands: host residues, exact int64 residue products per modulus,
+    host reconstruction; row-major (m*n, 2)."""
+    SA, RA = crt_split(sq, A, m, k, sai, sal, T, k)
+    SB, RB = crt_split(sq, B, n, k, sbj, sbl, T, k)
+    C = np.stack([RA[q].astype(np.int64) @ RB[q].astype(np.int64).T for q in range(RA.shape[0])])
+    out = np.zeros((m * n, 2), dtype=np.uint64)
+    assert sq.sq_crt_fold(c64(m), c64(n), ctypes.c_int(T), c64(k), P(np.ascontiguousarray(C)), P(SA), P(SB),
+                          P(out)) > 0
+    return out

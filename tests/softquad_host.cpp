@@ -8,6 +8,7 @@
 #include "../qblas_gb300/csrc/ozaki.cuh"
 #include "../qblas_gb300/csrc/exact.cuh"
 #include "../qblas_gb300/csrc/ozgemv.cuh"
+#include "../qblas_gb300/csrc/ozcrt.cuh"
 
 using qb::q128;
 
@@ -233,4 +234,95 @@ int sq_og_row(int64_t n, const q128* a, const q128* x, q128* out) {
   uint64_t err = qb::og_row_error(acc, nch, gmax, 0);
   return qb::wacc_round_certified(acc, err, *out) ? 1 : 0;
 }
+
+// ---- Ozaki scheme II (ozcrt.cuh) ------------------------------------------
+// The table for T-bit operands and inner dimension k: returns n (moduli) or 0,
+// and writes n, nw, then p, u, c18[11] per modulus, then Mpair[24][12] and
+// negM[12] as uint32 (out must hold 4 + 48 * 13 + 24 * 12 + 12 words).
+int sq_crt_table(int T, int64_t k, uint32_t* out) {
+  qb::CrtTable t;
+  if (!qb::crt_build(T, k, t)) return 0;
+  int o = 0;
+  out[o++] = (uint32_t)t.n;
+  out[o++] = (uint32_t)t.nw;
+  out[o++] = (uint32_t)t.T;
+  out[o++] = 0;
+  for (int q = 0; q < qb::kCrtMaxMods; ++q) {
+    out[o++] = t.mod[q].p;
+    out[o++] = t.mod[q].u;
+    for (int j = 0; j < qb::kCrtPieces; ++j) out[o++] = t.mod[q].c18[j];
+  }
+  for (int i = 0; i < qb::kCrtMaxMods / 2; ++i)
+    for (int w = 0; w < qb::kCrtMaxWords; ++w) out[o++] = t.Mpair[i][w];
+  for (int w = 0; w < qb::kCrtMaxWords; ++w) out[o++] = t.negM[w];
+  return t.n;
 }
+
+// x mod p by the magic multiplier, for x[i], i < n.
+void sq_crt_mod(int64_t n, const uint32_t* x, uint32_t p, uint32_t* r) {
+  const uint32_t magic = (uint32_t)(((1ull << 40) + p - 1) / p);
+  for (int64_t i = 0; i < n; ++i) r[i] = qb::crt_mod(x[i], p, magic);
+}
+
+// Balanced residues r[i][q] (sign included) of a[i] for scale S and T bits,
+// and the scaled integer V (3 words) with its sign.
+int sq_crt_residues(int64_t n, const q128* a, const int* S, int T, int64_t k, int* r, uint64_t* V) {
+  qb::CrtTable t;
+  if (!qb::crt_build(T, k, t)) return 0;
+  for (int64_t i = 0; i < n; ++i) {
+    qb::crt_residues(a[i], S[i], t, r + i * t.n);
+    bool neg;
+    qb::ozaki_scaled_bits(a[i], S[i], T, V[4 * i], V[4 * i + 1], V[4 * i + 2], neg);
+    V[4 * i + 3] = neg;
+  }
+  return t.n;
+}
+
+// Reconstruction of X 2^e[i] from C[i][q] (one pass) for each output i.
+int sq_crt_reconstruct(int64_t n, const int32_t* C, const int* e, int T, int64_t k, q128* out) {
+  qb::CrtTable t;
+  if (!qb::crt_build(T, k, t)) return 0;
+  for (int64_t i = 0; i < n; ++i) out[i] = qb::crt_reconstruct_any(C + i * t.n, t, e[i]);
+  return t.n;
+}
+
+// CRT split of a view as the device does it: row scales S[r] and balanced
+// residues R[q][r][c] for T-bit operands and the table of inner dimension k.
+int sq_crt_split(int64_t rows, int64_t cols, const q128* X, int64_t sr, int64_t sc, int T, int64_t k,
+                 int32_t* S, int32_t* R) {
+  qb::CrtTable t;
+  if (!qb::crt_build(T, k, t)) return 0;
+  int r_q[qb::kCrtMaxMods];
+  for (int64_t r = 0; r < rows; ++r) {
+    int mx = qb::kOzakiScaleEmpty;
+    for (int64_t c = 0; c < cols; ++c) {
+      int e = qb::ozaki_exp_plus1(X[r * sr + c * sc]);
+      mx = e > mx ? e : mx;
+    }
+    S[r] = mx;
+    for (int64_t c = 0; c < cols; ++c) {
+      qb::crt_residues(X[r * sr + c * sc], mx, t, r_q);
+      for (int q = 0; q < t.n; ++q) R[((int64_t)q * rows + r) * cols + c] = r_q[q];
+    }
+  }
+  return t.n;
+}
+
+// CRT reconstruction of exact residue-product sums C[q][i][j] (int64) with
+// scales S[i], F[j].
+int sq_crt_fold(int64_t m, int64_t n, int T, int64_t k, const int64_t* C, const int32_t* S, const int32_t* F,
+                q128* out) {
+  qb::CrtTable t;
+  if (!qb::crt_build(T, k, t)) return 0;
+  int32_t c[qb::kCrtMaxMods];
+  for (int64_t i = 0; i < m; ++i)
+    for (int64_t j = 0; j < n; ++j) {
+      for (int q = 0; q < t.n; ++q) {
+        const int64_t p = t.mod[q].p, v = C[((int64_t)q * m + i) * n + j] % p;
+        c[q] = (int32_t)(v < 0 ? v + p : v);
+      }
+      out[i * n + j] = qb::crt_reconstruct_any(c, t, S[i] + F[j] - 2 * T);
+    }
+  return t.n;
+}
+}  // extern "C"

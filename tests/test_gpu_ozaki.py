@@ -1,4 +1,4 @@
-"""GPU parity of the Ozaki qgemm (tcgen05 digit products).
+"""GPU parity of the Ozaki qgemm, digit-pair scheme (tcgen05 digit products).
 
 * Bit-exact against the CPU emulation of the same algorithm (ozaki_emul:
   the digit split and fold of ozaki.cuh built for the host, digit products
@@ -27,8 +27,10 @@ pytestmark = pytest.mark.gpu
 @pytest.fixture
 def ozaki(qlib):
     api.set_method(2)
+    api.set_ozaki_scheme(1)  # digit pairs (the residue scheme: test_gpu_ozcrt.py)
     yield qlib
     api.set_method(0)
+    api.set_ozaki_scheme(0)
     api.set_ozaki_slices(0)
     api.set_ozaki_digit_bits(0)
 

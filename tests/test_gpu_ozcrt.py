@@ -1,0 +1,163 @@
+"""GPU parity of the Ozaki qgemm, residue (CRT) scheme: quadblas_set_ozaki_scheme(2).
+
+* Bit-exact against the CPU emulation of the same algorithm
+  (ozaki_emul.crt_gemm_sum: the residue split and reconstruction of
+  ozcrt.cuh built for the host, residue products as exact numpy int64
+  GEMMs).  The emulation itself equals the correctly rounded exact sum of the
+  T-bit truncated products (tests/test_ozcrt_host.py), so the tolerance is
+  none.
+* Accuracy against the exact oracle: with T = 134 bits (15 slices of 9
+  bits, the 4096^3 benchmark setting) every sampled entry is within 1 ulp
+  (u_q = 2^-113) of the exact sum on spread-exponent data.
+* NaN / infinity rows and columns follow the exact-oracle semantics.
+"""
+import numpy as np
+import pytest
+
+import ozaki_emul as E
+from conftest import to_dev, to_host
+from gpu_helpers import epilogue
+from qblas_gb300 import api
+from qblas_gb300 import gen as G
+from qblas_gb300 import quad as Q
+from test_gpu_ozaki import strides
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture
+def crt(qlib):
+    api.set_method(2)
+    api.set_ozaki_scheme(2)
+    yield qlib
+    api.set_method(0)
+    api.set_ozaki_scheme(0)
+    api.set_ozaki_slices(0)
+    api.set_ozaki_digit_bits(0)
+
+
+def run_case(O, sq, rng, layout, transa, transb, m, n, k, s, gen, al_d, be_d, b=9):
+    col = layout == "C"
+    ta, tb = transa == "T", transb == "T"
+    ar, ac = (k, m) if ta else (m, k)
+    br, bc = (n, k) if tb else (k, n)
+    lda = (ar if col else ac) + 1
+    ldb = (br if col else bc) + 2
+    ldc = (m if col else n) + 1
+    A = gen(rng, (ac if col else ar) * lda)
+    B = gen(rng, (bc if col else br) * ldb)
+    C = G.uniform_full(rng, (n if col else m) * ldc)
+    alpha, beta = Q.scalar(al_d), Q.scalar(be_d)
+    api.set_ozaki_slices(s)
+    api.set_ozaki_digit_bits(b)
+    got = C.copy()
+    api.gemm(layout, transa, transb, m, n, k, alpha, A, lda, B, ldb, beta, got, ldc)
+    (sai, sal), (sbl, sbj), (sci, scj) = strides(layout, ta, tb, lda, ldb, ldc)
+    sums = E.crt_gemm_sum(sq, m, n, k, A, sai, sal, B, sbl, sbj, b * s - 1)
+    rows, cols = np.meshgrid(np.arange(m), np.arange(n), indexing="ij")
+    idx = rows.ravel() * sci + cols.ravel() * scj
+    exp = epilogue(O, alpha, sums, beta, C[idx])
+    return got, idx, exp
+
+
+def test_crt_one_tile_bit_exact(crt, O, sq):
+    """Smallest case first: one 128 x 256 tile, one K block."""
+    rng = G.rng_for(401)
+    got, idx, exp = run_case(O, sq, rng, "R", "N", "N", 128, 256, 64, 15, G.spread_uniform, 1.0, 0.0)
+    assert Q.same_bits(got[idx], exp).all()
+
+
+# T = b*s - 1: 71 and 103 (8-word reconstruction), 134 and 143 (10 words, 9
+# pieces), 153 (12 pieces), 161 (12 pieces, 12 words)
+@pytest.mark.parametrize("s,b", [(8, 9), (13, 8), (15, 9), (16, 9), (22, 7), (18, 9)])
+def test_crt_bit_exact_vs_emulation(crt, O, sq, s, b):
+    rng = G.rng_for(410 + s + 100 * b)
+    cases = [("R", "N", "N", 1, 1, 1), ("R", "N", "N", 5, 7, 9), ("R", "T", "N", 130, 257, 70),
+             ("C", "N", "N", 200, 100, 300), ("C", "T", "T", 33, 290, 129), ("R", "N", "T", 129, 255, 65)]
+    for layout, ta, tb, m, n, k in cases:
+        got, idx, exp = run_case(O, sq, rng, layout, ta, tb, m, n, k, s, G.spread_uniform, 2.5, -1.5, b)
+        assert Q.same_bits(got[idx], exp).all(), (layout, ta, tb, m, n, k, s, b)
+
+
+def test_crt_several_chunks_and_passes(crt, O, sq):
+    """k above the fp32-exact chunk (256) and above one pass (8192: the int32
+    residue sums stay within 2^29); each pass writes its own planes and the
+    reconstruction adds their residues."""
+    rng = G.rng_for(420)
+    for layout, ta, tb, m, n, k in (("R", "N", "N", 128, 256, 5 * 256 + 69),
+                                     ("R", "N", "N", 24, 40, 8192 + 300), ("C", "T", "N", 17, 33, 2 * 8192 + 65)):
+        got, idx, exp = run_case(O, sq, rng, layout, ta, tb, m, n, k, 15, G.spread_uniform, 1.0, 0.5)
+        assert Q.same_bits(got[idx], exp).all(), (layout, k)
+
+
+def test_crt_mixed_magnitudes(crt, O, sq):
+    """Zero rows, subnormal and huge entries go through the same split."""
+    rng = G.rng_for(421)
+
+    def gen(rng, n):
+        q = G.wide_exponent(rng, n, -16000, 16000)
+        q[: n // 7] = 0
+        return q
+
+    for b, s in ((9, 16), (8, 18), (7, 20)):
+        got, idx, exp = run_case(O, sq, rng, "R", "N", "N", 67, 301, 45, s, gen, 1.0, 0.0, b)
+        assert Q.same_bits(got[idx], exp).all(), b
+
+
+@pytest.mark.parametrize("size", [512, 4096])
+def test_crt_accuracy_spread(crt, O, torch_cuda, size):
+    """size^3 on e-uniform-[-20, 20] data at the benchmark setting (15 slices
+    of 9 bits: T = 134): every sampled entry is within 1 ulp of the exact sum."""
+    torch = torch_cuda
+    m = n = k = size
+    rng = G.rng_for(0xC0FFEE + 2)
+    A, B = G.spread_uniform(rng, m * k), G.spread_uniform(rng, k * n)
+    C = Q.from_double(np.zeros(m * n))
+    dA, dB, dC = to_dev(torch, A), to_dev(torch, B), to_dev(torch, C)
+    api.set_ozaki_slices(15)
+    api.set_ozaki_digit_bits(9)
+    api.gemm_dev("R", "N", "N", m, n, k, Q.scalar(1.0), dA, k, dB, n, Q.scalar(0.0), dC, n)
+    torch.cuda.synchronize()
+    got = to_host(dC)
+    nsamp = 20000 if size <= 512 else 6000
+    rows, cols = rng.integers(0, m, nsamp), rng.integers(0, n, nsamp)
+    R, r, _ = O.exact_gemm(k, A, k, 1, B, n, 1, rows, cols, nthreads=16)
+    err = O.ulp_err(got[rows * n + cols], R, r)
+    assert err.max() <= 1.0, err.max()
+
+
+def test_crt_special_values(crt, O):
+    rng = G.rng_for(422)
+    m, n, k = 9, 11, 13
+    A, B = G.uniform_full(rng, m * k), G.uniform_full(rng, k * n)
+    A[2 * k + 3] = [0, 0x7FFF800000000000]   # NaN in row 2
+    A[5 * k + 1] = [0, 0x7FFF000000000000]   # +inf in row 5
+    B[4 * n + 7] = [0, 0xFFFF000000000000]   # -inf in column 7
+    C = Q.from_double(np.zeros(m * n))
+    got = C.copy()
+    api.gemm("R", "N", "N", m, n, k, Q.scalar(1.0), A, k, B, n, Q.scalar(0.0), got, n)
+    rows, cols = np.meshgrid(np.arange(m), np.arange(n), indexing="ij")
+    R, _, _ = O.exact_gemm(k, A, k, 1, B, n, 1, rows.ravel(), cols.ravel())
+    special = np.zeros((m, n), bool)
+    special[[2, 5], :] = True
+    special[:, 7] = True
+    sp = special.ravel()
+    assert Q.same_bits(got[sp], R[sp]).all()
+    assert Q.is_nan(got[~sp]).sum() == 0
+
+
+def test_crt_default_scheme_and_c_interface(qlib, O, sq):
+    """quadblas_qgemm with the Ozaki method and every setting at its default
+    (automatic scheme: residues; 16 slices of 9 bits, T = 143)."""
+    rng = G.rng_for(423)
+    m, n, k = 40, 50, 60
+    A, B, C = G.spread_uniform(rng, m * k), G.spread_uniform(rng, k * n), G.uniform_full(rng, m * n)
+    api.set_method(2)
+    try:
+        assert api.get_ozaki_scheme() == 0
+        got = C.copy()
+        api.qgemm("R", "N", "N", m, n, k, 2.0, A, k, B, n, 0.5, got, n)
+    finally:
+        api.set_method(0)
+    sums = E.crt_gemm_sum(sq, m, n, k, A, k, 1, B, n, 1, 16 * 9 - 1)
+    assert Q.same_bits(got, epilogue(O, Q.scalar(2.0), sums, Q.scalar(0.5), C)).all()

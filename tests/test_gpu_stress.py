@@ -124,19 +124,25 @@ def test_qgemm_gendot_softfloat(qlib, O, gendot_matrices):
     assert ulp.max() <= 0.5
 
 
-@pytest.mark.parametrize("s,b", [(15, 9), (17, 8), (20, 8), (22, 7)])
-def test_qgemm_gendot_ozaki(qlib, O, gendot_matrices, s, b):
+@pytest.mark.parametrize("s,b,scheme", [(15, 9, 1), (17, 8, 1), (20, 8, 1), (22, 7, 1), (15, 9, 2), (22, 7, 2)])
+def test_qgemm_gendot_ozaki(qlib, O, gendot_matrices, s, b, scheme):
+    """Both Ozaki schemes truncate the operands to b*s - 1 bits; the residue
+    scheme (2) has no further error, the digit pairs (1) drop the pairs below
+    the digit count."""
     M = gendot_matrices
     api.set_method(2)
     api.set_ozaki_slices(s)
     api.set_ozaki_digit_bits(b)
+    api.set_ozaki_scheme(scheme)
     try:
         got = run_gemm(M)
     finally:
         api.set_method(0)
         api.set_ozaki_slices(0)
         api.set_ozaki_digit_bits(0)
-    ulp = record(O, M, f"ozaki s={s} b={b}", got)
+        api.set_ozaki_scheme(0)
+    label = f"ozaki s={s} b={b}" + (" residues" if scheme == 2 else "")
+    ulp = record(O, M, label, got)
     # normwise bound of the split, in log2, with the final rounding's ulp
     err_log2 = np.log2(np.maximum(ulp, 1e-300)) + (exponents(M["R"]) - 112)
     Sab = M["Sa"][M["rows"]] + M["Sb"][M["cols"]]

@@ -1,0 +1,212 @@
+"""The Ozaki scheme II arithmetic (qblas_gb300/csrc/ozcrt.cuh, compiled for
+the host) against Python integers and rationals:
+
+* table: pairwise coprime moduli whose product M exceeds 8 k 2^(2T) (and
+  the shortest such prefix), the inverses (M/p)^-1 mod p, M / (p p') per
+  pair, 2^(32 nw) - M and the 2^(18 j) mod p tables;
+* crt_mod: the magic-multiplier remainder equals x % p for x < 2^31;
+* residues: V = trunc(|a| 2^(T - S)) and balanced residues r == sign * V
+  (mod p), |r| <= 256;
+* reconstruction: from C_q == X (mod p_q), |C_q| <= 2^29, the result is X 2^e
+  correctly rounded (ties to even), for X across (-M/8, M/8).
+"""
+import ctypes
+import math
+from fractions import Fraction
+
+import numpy as np
+import pytest
+
+from qblas_gb300 import gen as G
+from test_oracle import fraction_to_q, q_to_fraction
+
+MAXMODS, MAXWORDS, PIECES = 48, 12, 11
+TABLE_WORDS = 4 + MAXMODS * (2 + PIECES) + (MAXMODS // 2) * MAXWORDS + MAXWORDS
+
+
+def P(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def words(ws):
+    return sum(int(w) << (32 * i) for i, w in enumerate(ws))
+
+
+def table(sq, T, k):
+    out = np.zeros(TABLE_WORDS, dtype=np.uint32)
+    n = sq.sq_crt_table(ctypes.c_int(T), ctypes.c_int64(k), P(out))
+    if n == 0:
+        return None
+    nw = int(out[1])
+    o = 4
+    mods = []
+    for q in range(MAXMODS):
+        p, u = int(out[o]), int(out[o + 1])
+        mods.append((p, u, [int(c) for c in out[o + 2:o + 2 + PIECES]]))
+        o += 2 + PIECES
+    mpair = [words(out[o + i * MAXWORDS:o + (i + 1) * MAXWORDS]) for i in range(MAXMODS // 2)]
+    o += (MAXMODS // 2) * MAXWORDS
+    negm = words(out[o:o + MAXWORDS])
+    return n, nw, mods[:n], mpair, negm
+
+
+CASES = [(134, 4096), (143, 4096), (143, 1 << 20), (118, 64), (161, 8192), (80, 1), (170, 1 << 30)]
+
+
+@pytest.mark.parametrize("T,k", CASES)
+def test_table(sq, T, k):
+    t = table(sq, T, k)
+    assert t is not None
+    n, nw, mods, mpair, negm = t
+    ps = [m[0] for m in mods]
+    assert all(256 < p <= 513 for p in ps)
+    assert all(math.gcd(a, b) == 1 for i, a in enumerate(ps) for b in ps[i + 1:])
+    M = math.prod(ps)
+    need = 2 * T + math.ceil(math.log2(k)) + 3 if k > 1 else 2 * T + 3
+    assert M >= 1 << need and math.prod(ps[:-1]) < 1 << need
+    assert M < 1 << (32 * nw) and nw % 2 == 0 and nw <= MAXWORDS
+    for p, u, c18 in mods:
+        assert (M // p) * u % p == 1
+        assert c18 == [pow(2, 18 * j, p) for j in range(PIECES)]
+    for i in range(0, n, 2):
+        div = ps[i] * (ps[i + 1] if i + 1 < n else 1)
+        assert mpair[i // 2] == M // div
+    assert negm == (1 << (32 * nw)) - M
+
+
+def test_table_limits(sq):
+    assert table(sq, 192, 16) is None       # more bits than the split's three 64-bit words hold
+    assert table(sq, 191, 1 << 40) is None  # more moduli than the table holds
+
+
+def test_crt_mod(sq):
+    rng = np.random.default_rng(7)
+    x = np.concatenate([rng.integers(0, 1 << 31, 20000, dtype=np.uint64),
+                        np.arange(0, 5000, dtype=np.uint64),
+                        (1 << 31) - 1 - np.arange(0, 5000, dtype=np.uint64)]).astype(np.uint32)
+    for p in [513, 512, 511, 509, 505, 257, 263, 269, 277, 281, 283, 293, 307, 311, 317]:
+        r = np.zeros_like(x)
+        sq.sq_crt_mod(ctypes.c_int64(len(x)), P(x), ctypes.c_uint32(p), P(r))
+        assert np.array_equal(r, x % np.uint32(p)), p
+
+
+def lead_exp(w):
+    f = q_to_fraction(w)
+    if f == 0:
+        return None
+    e = abs(f).numerator.bit_length() - abs(f).denominator.bit_length()
+    return e if Fraction(2) ** e <= abs(f) else e - 1
+
+
+@pytest.mark.parametrize("T", [134, 143, 161])
+def test_residues(sq, T):
+    rng = G.rng_for(301)
+    a = np.concatenate([G.wide_exponent(rng, 300), G.uniform_full(rng, 300),
+                        G.spread_uniform(rng, 300, -400, 400), np.zeros((4, 2), dtype=np.uint64)])
+    a[-1, 1] = np.uint64(1 << 63)  # -0
+    sub = G.uniform_full(rng, 20)
+    sub[:, 1] &= ~np.uint64(0x7FFF << 48)
+    a = np.ascontiguousarray(np.concatenate([a, sub]))
+    S = []
+    for w in a:
+        e = lead_exp(w)
+        S.append(-(1 << 29) if e is None else e + 1 + int(rng.integers(0, 60)))
+    S = np.array(S, dtype=np.int32)
+    k = 4096
+    n, _, mods, _, _ = table(sq, T, k)
+    r = np.zeros((len(a), n), dtype=np.int32)
+    V = np.zeros((len(a), 4), dtype=np.uint64)
+    assert sq.sq_crt_residues(ctypes.c_int64(len(a)), P(a), P(S), ctypes.c_int(T), ctypes.c_int64(k), P(r), P(V)) == n
+    for i, w in enumerate(a):
+        v = int(V[i, 0]) | (int(V[i, 1]) << 64) | (int(V[i, 2]) << 128)
+        f = abs(q_to_fraction(w))
+        if S[i] == -(1 << 29):
+            assert v == 0
+        else:
+            exact = f * Fraction(2) ** (T - int(S[i]))
+            assert v == exact.numerator // exact.denominator and v < 1 << T
+        sv = -v if V[i, 3] else v
+        for q, (p, _, _) in enumerate(mods):
+            assert abs(int(r[i, q])) <= 256
+            assert (int(r[i, q]) - sv) % p == 0
+
+
+def test_reconstruct(sq):
+    T, k = 134, 4096
+    n, nw, mods, _, _ = table(sq, T, k)
+    ps = [m[0] for m in mods]
+    M = math.prod(ps)
+    rng = np.random.default_rng(11)
+    Xs = [0, 1, -1, 2, (1 << 113) - 1, -(1 << 113) + 1, (1 << 114) + 1, (1 << 114) + 3, -((1 << 114) + 3),
+          (1 << 200) + (1 << 87), (1 << 200) + (1 << 87) + 1, M // 8 - 1, -(M // 8) + 1]
+    for b in range(1, M.bit_length() - 4, 7):
+        x = int(rng.integers(0, 1 << 62)) << max(0, b - 62)
+        x = x % (1 << b) | (1 << (b - 1))
+        Xs += [x, -x]
+    Xs = [x for x in Xs if abs(x) < M // 8]
+    C = np.zeros((len(Xs), n), dtype=np.int32)
+    for i, x in enumerate(Xs):
+        for q, p in enumerate(ps):
+            c = x % p + p * int(rng.integers(-(1 << 29) // p, (1 << 29) // p - 1))
+            assert abs(c) <= 1 << 29
+            C[i, q] = c
+    e = rng.integers(-300, 100, size=len(Xs)).astype(np.int32)
+    out = np.zeros((len(Xs), 2), dtype=np.uint64)
+    assert sq.sq_crt_reconstruct(ctypes.c_int64(len(Xs)), P(C), P(e), ctypes.c_int(T), ctypes.c_int64(k), P(out)) == n
+    for i, x in enumerate(Xs):
+        want = fraction_to_q(Fraction(x) * Fraction(2) ** int(e[i]))
+        assert (int(out[i, 0]), int(out[i, 1])) == want, (i, x)
+
+
+def test_reconstruct_all_word_counts(sq):
+    """8, 10 and 12 words (small T, the bench's T, large T)."""
+    rng = np.random.default_rng(12)
+    for T, k in [(100, 64), (134, 4096), (170, 1 << 20)]:
+        n, nw, mods, _, _ = table(sq, T, k)
+        ps = [m[0] for m in mods]
+        X = [int(rng.integers(1, 1 << 62)) << int(rng.integers(0, 2 * T - 62)) for _ in range(50)]
+        X = [x if j % 2 else -x for j, x in enumerate(X)]
+        C = np.array([[x % p for p in ps] for x in X], dtype=np.int32)
+        e = np.full(len(X), -2 * T, dtype=np.int32)
+        out = np.zeros((len(X), 2), dtype=np.uint64)
+        sq.sq_crt_reconstruct(ctypes.c_int64(len(X)), P(C), P(e), ctypes.c_int(T), ctypes.c_int64(k), P(out))
+        for i, x in enumerate(X):
+            assert (int(out[i, 0]), int(out[i, 1])) == fraction_to_q(Fraction(x, 1 << (2 * T))), (T, nw, i)
+
+
+def scaled(f, S, T):
+    """sign * trunc(|f| 2^(T - S)) as a Python integer."""
+    v = abs(f) * Fraction(2) ** (T - S)
+    v = v.numerator // v.denominator
+    return -v if f < 0 else v
+
+
+def row_scale(ws):
+    es = [lead_exp(w) for w in ws]
+    es = [e for e in es if e is not None]
+    return max(es) + 1 if es else -(1 << 29)
+
+
+@pytest.mark.parametrize("T,k", [(134, 40), (143, 33), (71, 17), (161, 9000)])
+def test_crt_gemm_emulation_exact(sq, T, k):
+    """Host residues + exact residue products + host reconstruction equal the
+    correctly rounded exact sum of the T-bit truncated products."""
+    import ozaki_emul as E
+    rng = G.rng_for(302 + T)
+    m, n = (3, 2) if k > 1000 else (5, 4)
+    A = G.spread_uniform(rng, m * k, -30, 30)
+    B = G.spread_uniform(rng, k * n, -30, 30)
+    A[1 * k:2 * k] = 0  # an all-zero row
+    got = E.crt_gemm_sum(sq, m, n, k, A, k, 1, B, n, 1, T)
+    fa = [[q_to_fraction(A[i * k + l]) for l in range(k)] for i in range(m)]
+    fb = [[q_to_fraction(B[l * n + j]) for l in range(k)] for j in range(n)]
+    S = [row_scale(A[i * k:(i + 1) * k]) for i in range(m)]
+    F = [row_scale(B[j::n]) for j in range(n)]
+    for i in range(m):
+        for j in range(n):
+            if S[i] == -(1 << 29) or F[j] == -(1 << 29):
+                want = (0, 0)
+            else:
+                X = sum(scaled(fa[i][l], S[i], T) * scaled(fb[j][l], F[j], T) for l in range(k))
+                want = fraction_to_q(Fraction(X) * Fraction(2) ** (S[i] + F[j] - 2 * T))
+            assert (int(got[i * n + j, 0]), int(got[i * n + j, 1])) == want, (i, j)
