@@ -218,7 +218,10 @@ int quadblas_get_ozaki_scheme(void);
 int quadblas_profile_enable(int on);
 int quadblas_profile_read(double *out4, int *calls);
 /* Frees the staging buffers that host-pointer calls keep on the current
- * device (they are allocated again, grown to need, by the next call). */
+ * device (they are allocated again, grown to need, by the next call), and
+ * returns the unused memory of the library's scratch pool on that device
+ * (device-pointer calls take their scratch from this pool in stream order
+ * and give it back to the pool, which keeps it for the next call). */
 int quadblas_release_buffers(void);
 /* Testing aid for callers' failure handling: the next `count` device
  * allocations the library attempts fail as if the device were out of memory

@@ -601,12 +601,47 @@ cudaError_t dev_malloc(void** p, size_t bytes) {
   }
   return cudaMalloc(p, bytes);
 }
+// Stream-ordered scratch comes from a memory pool of the library's own per
+// device (not the device's default pool, which other code in the process
+// may use), created on first use and told to keep freed memory: with the
+// default release threshold of 0 a pool hands its memory back at every
+// synchronisation and maps it again at the next allocation, which took
+// about 0.5 ms per 4096^3 Ozaki qgemm call.  quadblas_release_buffers()
+// trims it.
+cudaMemPool_t scratch_pool(int dev) {
+  static std::mutex mu;
+  static cudaMemPool_t pools[64] = {};
+  if (dev < 0 || dev >= 64) return nullptr;
+  std::lock_guard<std::mutex> l(mu);
+  if (!pools[dev]) {
+    cudaMemPoolProps props = {};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.handleTypes = cudaMemHandleTypeNone;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = dev;
+    cudaMemPool_t pool = nullptr;
+    if (cudaMemPoolCreate(&pool, &props) != cudaSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
+    uint64_t keep = ~0ull;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    pools[dev] = pool;
+  }
+  return pools[dev];
+}
+
 cudaError_t dev_malloc_async(void** p, size_t bytes, cudaStream_t s) {
   if (take_injected_failure()) {
     *p = nullptr;
     return cudaErrorMemoryAllocation;
   }
-  return cudaMallocAsync(p, bytes, s);
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  cudaMemPool_t pool = scratch_pool(dev);
+  if (!pool) return cudaMallocAsync(p, bytes, s);
+  return cudaMallocFromPoolAsync(p, bytes, pool, s);
 }
 }  // namespace qb
 
@@ -766,6 +801,8 @@ QBLAS_EXPORT int quadblas_release_buffers(void) {
     st.buf[i] = nullptr;
     st.cap[i] = 0;
   }
+  // the scratch pool's unused memory (frees still pending in stream order stay)
+  if (cudaMemPool_t pool = qb::scratch_pool(dev)) cudaMemPoolTrimTo(pool, 0);
   cudaGetLastError();
   return fail(qb::kOk);
 }

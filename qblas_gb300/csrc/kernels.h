@@ -115,6 +115,9 @@ int ozaki_profile_read(double* out4, int* calls);
 // failure count (quadblas_debug_fail_allocations) is pending.
 cudaError_t dev_malloc(void** p, size_t bytes);
 cudaError_t dev_malloc_async(void** p, size_t bytes, cudaStream_t s);
+// The library's stream-ordered scratch pool of device `dev` (keeps freed
+// memory until quadblas_release_buffers), or null.
+cudaMemPool_t scratch_pool(int dev);
 int device_sm_count();
 
 // Blocks of `kernel` (with `threads` threads and `smem` dynamic shared

@@ -210,3 +210,4 @@ def test_crt_gemm_emulation_exact(sq, T, k):
                 X = sum(scaled(fa[i][l], S[i], T) * scaled(fb[j][l], F[j], T) for l in range(k))
                 want = fraction_to_q(Fraction(X) * Fraction(2) ** (S[i] + F[j] - 2 * T))
             assert (int(got[i * n + j, 0]), int(got[i * n + j, 1])) == want, (i, j)
+
