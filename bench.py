@@ -2,19 +2,22 @@
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
                     [--workload qgemm4096|qgemm2048|qgemm512|qgemv8192|qdot26]
-                    [--method ozaki|softfloat] [--slices S]
+                    [--method ozaki|softfloat] [--slices S] [--bits B]
+                    [--scheme auto|digits|residues]
 
 Default: qgemm m = n = k = 4096, row-major 'N','N', alpha = 1, beta = 0,
 entries u * 2^e (u uniform in [-1, 1) with a full 113-bit significand, e a
-uniform integer in [-20, 20]), Ozaki method with 17 balanced 8-bit digits
-per operand (the smallest count that keeps this workload within 1 ulp);
-metric binary128 GFLOP/s (2mnk per second).  One step is one qgemm with the
-inputs resident in HBM (A and B are 256 MB each, larger than L2, so no
-flush is needed).  Beside it ("secondary"): the soft-float qgemm of the
-same problem (the speed-up the Ozaki path is judged by), a digit-count
-sweep with the ulp distance of each result from the correctly rounded
-soft-float result, qgemv 8192^2 and qdot 2^26 (HBM rooflines) and the
-512^3 soft-float qgemm.
+uniform integer in [-20, 20]), Ozaki method with each operand truncated to
+T = 9 * 15 - 1 = 134 bits after its row (column) scaling, multiplied by the
+automatic scheme: residues modulo 33 coprime moduli (Ozaki scheme II, one
+fp16 tensor-core GEMM per modulus, exact CRT reconstruction; <= 1 ulp on
+this workload); metric binary128 GFLOP/s (2mnk per second).  One step is
+one qgemm with the inputs resident in HBM (A and B are 256 MB each, larger
+than L2, so no flush is needed).  Beside it ("secondary"): the soft-float
+qgemm of the same problem (the speed-up the Ozaki path is judged by), a
+sweep over T and both schemes with the ulp distance of each result from
+the correctly rounded soft-float result, qgemv 8192^2 and qdot 2^26 (HBM
+rooflines) and the 512^3 soft-float qgemm.
 
 Each rank runs its own problem (weak scaling; the path needs no
 collective); rank 0 prints one JSON line.
@@ -43,8 +46,12 @@ from qblas_gb300 import gen as G  # noqa: E402
 from qblas_gb300 import quad as Q  # noqa: E402
 
 FALLBACK = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}
-SWEEP = ((8, 8), (8, 10), (8, 12), (8, 13), (8, 14), (8, 15), (8, 16), (8, 17), (8, 18), (8, 19), (8, 20),
-         (7, 19), (7, 20), (9, 13), (9, 14), (9, 15), (9, 16))
+# (scheme, digit bits, digits): the truncation is T = bits * digits - 1 bits
+# per operand; "digits" multiplies digit pairs, "residues" moduli (CRT)
+SWEEP = (("residues", 9, 11), ("residues", 9, 12), ("residues", 9, 13), ("residues", 9, 14),
+         ("residues", 9, 15), ("residues", 9, 16), ("residues", 9, 18), ("residues", 8, 20),
+         ("digits", 8, 12), ("digits", 8, 16), ("digits", 8, 17), ("digits", 9, 14), ("digits", 9, 15))
+SCHEMES = {"auto": 0, "digits": 1, "residues": 2}
 HEADLINE_DIGITS, HEADLINE_BITS = 15, 9  # <= 1 ulp on this workload (tests/test_gpu_ozaki.py)
 
 
@@ -125,14 +132,18 @@ def to_host(t) -> np.ndarray:
     return np.ascontiguousarray(t.cpu().numpy()).view(np.uint64)
 
 
-def ozaki_launches(k, s, b):
+def ozaki_launches(k, s, b, crt):
     """Kernels per device-pointer Ozaki qgemm call: fill, scale and split for
-    each operand, one digit-product launch per k pass, fold, special values.
-    A k pass holds as many fp32-exact k-chunks as an int32 diagonal sum of s
-    pairs of chunk sums (each < 2^24) allows."""
-    chunk_kb = (1 << (24 - 2 * (b - 1))) // 64
-    kbp = max(1, (2 ** 31 - 1) // (s << 24)) * chunk_kb
-    npass = -(-(-(-k // 64)) // kbp)
+    each operand, one tensor-core launch per k pass, fold, special values.
+    Digit pairs: a k pass holds as many fp32-exact k-chunks as an int32
+    diagonal sum of s pairs of chunk sums (each < 2^24) allows.  Residues: a
+    k pass is 8192 (the residue product sums stay below 2^29)."""
+    if crt:
+        npass = -(-k // 8192)
+    else:
+        chunk_kb = (1 << (24 - 2 * (b - 1))) // 64
+        kbp = max(1, (2 ** 31 - 1) // (s << 24)) * chunk_kb
+        npass = -(-(-(-k // 64)) // kbp)
     return 6 + npass + 2
 
 
@@ -267,7 +278,8 @@ class Qdot:
 # DRAM bytes (read + write) per launch of the dominant kernel, from one ncu
 # capture of the same workload (profiles/ holds the summaries and commands).
 NCU_TRAFFIC = {
-    "qgemm4096": (2 * (9.84e9 + 1.01e9), "profiles/ozaki_mma_kernel_4096_traffic.md"),  # 15 x 9 bit, 2 passes
+    "qgemm4096": (2 * (9.84e9 + 1.01e9), "profiles/ozaki_mma_kernel_4096_traffic.md"),  # 15 x 9 bit digit pairs, 2 passes
+    "qgemm4096_crt": (2.468784e9 + 1.109550e9, "profiles/ozaki_crt_qgemm4096_launches.md"),  # T = 134, 33 moduli
     "qdot26": (2.147608e9 + 4.091e6, "profiles/qdot_partial_kernel_n2p26.md"),
     "qgemv8192": (1.074079e9 + 1.8140e7, "profiles/qgemv_lane_kernel_8192.md"),
     "qgemv8192_ozaki": (1.086090e9 + 3.979e6, "profiles/og_gemv_kernel_8192.md"),
@@ -463,6 +475,7 @@ def main():
     ap.add_argument("--method", default="ozaki", choices=["softfloat", "ozaki"])
     ap.add_argument("--slices", type=int, default=0)
     ap.add_argument("--bits", type=int, default=0, help="digit width for the Ozaki method (7, 8 or 9)")
+    ap.add_argument("--scheme", default="auto", choices=sorted(SCHEMES))
     ap.add_argument("--no-secondary", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
@@ -488,6 +501,7 @@ def main():
     bits = args.bits or HEADLINE_BITS
     api.set_ozaki_slices(slices)
     api.set_ozaki_digit_bits(bits)
+    api.set_ozaki_scheme(SCHEMES[args.scheme])
 
     line = {}
     secondary = {}
@@ -507,18 +521,29 @@ def main():
             tot_calls = max(calls, 1)
             mma_ms = ph[1] / tot_calls
             tflops = (ph[3] / tot_calls) / (mma_ms * 1e-3) / 1e12
+            # tensor-core products per call, from the profiler's flop count:
+            # s(s+1)/2 digit pairs, or one residue product per modulus
+            products = int(round(ph[3] / tot_calls / W.flops()))
+            crt = products != slices * (slices + 1) // 2 or args.scheme == "residues"
             peak = float(pk.get("bf16_tflops_sustained", FALLBACK["bf16_tflops_sustained"]))
             roof = {"bound": "tensor", "achieved": round(tflops, 1), "peak": peak, "unit": "TFLOP/s",
-                    "frac": round(tflops / peak, 4), "traffic": traffic(wl)[0],
-                    "traffic_source": traffic(wl)[1], "peak_source": pk_src + " (sustained bf16)",
+                    "frac": round(tflops / peak, 4), "traffic": traffic(wl + ("_crt" if crt else ""))[0],
+                    "traffic_source": traffic(wl + ("_crt" if crt else ""))[1],
+                    "peak_source": pk_src + " (sustained bf16)",
                     "kernel": "ozaki_mma_kernel", "kernel_ms": round(mma_ms, 4),
-                    "algorithmic": "2*m*n*k*pairs bf16 flops, pairs = s(s+1)/2 digit products",
+                    "algorithmic": (f"2*m*n*k*{products} fp16 flops: one product per CRT modulus" if crt else
+                                    f"2*m*n*k*{products} flops: s(s+1)/2 digit-pair products"),
                     "phases_ms": {"scale_split": round(ph[0] / tot_calls, 4), "digit_products": round(mma_ms, 4),
                                   "fold": round(ph[2] / tot_calls, 4)}}
-            launches = ozaki_launches(size, slices, bits) * args.steps
-            dtype = (f"{'fp16' if bits == 9 else 'bf16'} digit products of {bits}-bit digits "
-                     "(fp32 accumulate, int32/192-bit fold)")
+            launches = ozaki_launches(size, slices, bits, crt) * args.steps
+            if crt:
+                dtype = (f"fp16 residue products modulo {products} moduli in (256, 513] (fp32 accumulate, "
+                         "u16 reduced residues, u32-limb CRT reconstruction)")
+            else:
+                dtype = (f"{'fp16' if bits == 9 else 'bf16'} digit products of {bits}-bit digits "
+                         "(fp32 accumulate, int32/192-bit fold)")
         else:
+            crt, products = False, None
             roof = {"bound": "int", "achieved": round(W.flops() / (ms_step * 1e-3) / 1e9, 3), "peak": None,
                     "unit": "quad GFLOP/s", "frac": None, "traffic": None,
                     "note": "soft-float kernel is integer-pipe bound"}
@@ -537,6 +562,9 @@ def main():
                f"qgemm m=n=k={size} row-major NN alpha=1 beta=0, full-mantissa uniform [-1,1)",
                "method": args.method, "digits_per_operand": slices if method == 2 else None,
                "digit_bits": bits if method == 2 else None,
+               "truncation_bits": bits * slices - 1 if method == 2 else None,
+               "ozaki_scheme": (("residues (CRT)" if crt else "digit pairs") if method == 2 else None),
+               "tensor_products": products if method == 2 else None,
                "l2": "inputs larger than L2 (no flush)" if size >= 2048 else "inputs fit in L2",
                "parallelism": f"replicas x{world}"}
 
@@ -561,21 +589,32 @@ def main():
                                                              "reference": "soft-float GPU qgemm (correctly rounded)"}
             api.set_method(2)
             sweep = []
-            for b, s in SWEEP:
-                api.set_ozaki_slices(s)
-                api.set_ozaki_digit_bits(b)
-                ms_s = time_steps(torch, W.step, 2, 1, dist) / 2
+            lib.quadblas_profile_enable(1)
+            for sch, b, s_ in SWEEP:
+                try:
+                    api.set_ozaki_scheme(SCHEMES[sch])
+                    api.set_ozaki_slices(s_)
+                    api.set_ozaki_digit_bits(b)
+                    profile_read(lib)
+                    ms_s = time_steps(torch, W.step, 2, 1, dist) / 2
+                except _lib.QblasError as ex:  # a setting this k does not allow
+                    sweep.append({"scheme": sch, "digit_bits": b, "digits": s_, "error": str(ex)})
+                    continue
+                phs, ncalls = profile_read(lib)
                 Cs = to_host(W.dC)[idx]
                 ds = ulp_distance(Cs, C_sf[idx])
-                sweep.append({"digit_bits": b, "digits": s, "pairs": s * (s + 1) // 2, "ms": round(ms_s, 3),
-                              "gflops": round(W.flops() / (ms_s * 1e-3) / 1e9, 1),
+                sweep.append({"scheme": sch, "truncation_bits": b * s_ - 1, "digit_bits": b, "digits": s_,
+                              "tensor_products": int(round(phs[3] / max(ncalls, 1) / W.flops())),
+                              "ms": round(ms_s, 3), "gflops": round(W.flops() / (ms_s * 1e-3) / 1e9, 1),
                               "speedup_vs_softfloat": round(ms_sf / ms_s, 2),
                               "max_ulp_from_correctly_rounded": float(ds.max()),
                               "max_rel": float(relative_error(Cs, C_sf[idx]).max()),
                               "exact_frac": float((ds == 0).mean())})
+            lib.quadblas_profile_enable(0)
+            api.set_ozaki_scheme(SCHEMES[args.scheme])
             api.set_ozaki_slices(slices)
             api.set_ozaki_digit_bits(bits)
-            secondary["digit_sweep"] = sweep
+            secondary["ozaki_sweep"] = sweep
         if not args.no_secondary and size == 4096:
             del W
             torch.cuda.empty_cache()

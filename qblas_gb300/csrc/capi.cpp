@@ -91,7 +91,6 @@ struct DevState {
   cudaEvent_t ev[kNumEvents] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   void* buf[kNumSlots] = {nullptr};
   size_t cap[kNumSlots] = {0};
-  bool pool_ready = false;
 };
 
 constexpr int kMaxDevices = 64;
@@ -102,18 +101,6 @@ int current_device(int& dev) {
   if (e != cudaSuccess) return cuda_status(e);
   if (dev < 0 || dev >= kMaxDevices) return qb::kErrNoDevice;
   return qb::kOk;
-}
-
-// Keeps memory freed by cudaFreeAsync cached in the device's default pool so
-// per-call scratch does not return to the driver between calls.
-void ensure_pool(DevState& st, int dev) {
-  if (st.pool_ready) return;
-  cudaMemPool_t pool;
-  if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
-    uint64_t thr = UINT64_MAX;
-    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
-  }
-  st.pool_ready = true;
 }
 
 int ensure_slot(DevState& st, Slot s, size_t bytes) {
@@ -147,7 +134,6 @@ struct HostCall {
     if (status) return;
     st = &g_dev[dev];
     lock = std::unique_lock<std::mutex>(st->mu);
-    ensure_pool(*st, dev);
     if (!st->stream) {
       cudaError_t e = cudaStreamCreateWithFlags(&st->stream, cudaStreamNonBlocking);
       if (e != cudaSuccess) {

@@ -221,15 +221,24 @@ constexpr uint32_t kIdescShape = (1u << 4) | ((uint32_t)(kBN >> 3) << 17) | ((ui
 constexpr uint32_t kIdescBf16 = kIdescShape | (1u << 7) | (1u << 10);
 constexpr uint32_t kIdescF16 = kIdescShape;
 
-// The (tile, diagonal) units of one CTA, in order.  Tiles come in full
-// waves of gridDim.x: CTA c takes tile w * gridDim.x + c and runs all its
-// diagonals, highest first, so every CTA of a wave issues the same sequence
-// of (diagonal, pair, k block) loads at the same time and the digit panels
-// they share (A_t of a tile row, B_u of a tile column) are read from DRAM
-// once per wave rather than once per CTA.  The tiles left over after the
+// The (tile, diagonal) units of one CTA, in order.  Digit pairs: tiles come
+// in full waves of gridDim.x: CTA c takes tile w * gridDim.x + c and runs all
+// its diagonals, highest first, so every CTA of a wave issues the same
+// sequence of (diagonal, pair, k block) loads at the same time and the digit
+// panels they share (A_t of a tile row, B_u of a tile column) are read from
+// DRAM once per wave rather than once per CTA.  The tiles left over after the
 // full waves are spread as (tile, diagonal) units, highest diagonal first.
+// Residues: each modulus's planes are used by one unit per tile and by no
+// other modulus, so units are dealt modulus-major (unit v = c + j gridDim.x
+// is modulus G - v / tiles of tile v % tiles): all tiles of a modulus run
+// before the next modulus starts, and its two planes (2 x 32 MB at 4096^2)
+// stay in L2 across the waves instead of being streamed again per wave.
 __device__ __forceinline__ int cta_unit_count(const OzakiMmaParams& P) {
   const int tiles = P.tile_end - P.tile_begin, G1 = P.G + 1;
+  if (P.crt) {
+    const int left = tiles * G1 - (int)blockIdx.x;
+    return left > 0 ? (left + (int)gridDim.x - 1) / (int)gridDim.x : 0;
+  }
   const int waves = tiles / (int)gridDim.x, rem = tiles - waves * (int)gridDim.x;
   const int tail = rem * G1 - (int)blockIdx.x;
   return waves * G1 + (tail > 0 ? (tail + (int)gridDim.x - 1) / (int)gridDim.x : 0);
@@ -237,6 +246,12 @@ __device__ __forceinline__ int cta_unit_count(const OzakiMmaParams& P) {
 
 __device__ __forceinline__ void cta_unit(const OzakiMmaParams& P, int j, int& tile, int& g) {
   const int tiles = P.tile_end - P.tile_begin, G1 = P.G + 1;
+  if (P.crt) {
+    const int v = (int)blockIdx.x + j * (int)gridDim.x;
+    g = P.G - v / tiles;
+    tile = P.tile_begin + v % tiles;
+    return;
+  }
   const int waves = tiles / (int)gridDim.x, rem = tiles - waves * (int)gridDim.x;
   if (j < waves * G1) {
     tile = P.tile_begin + (j / G1) * (int)gridDim.x + (int)blockIdx.x;
