@@ -1036,8 +1036,11 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scr
       ozaki_mma_kernel<<<(unsigned)std::min(units, sms), kMmaThreads, kMmaSmem, st>>>(tmA, tmB, P);
       if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
-    // rows whose tiles are all done can be folded while later bands multiply
-    if (banded && fold_banded && t1 < tiles) {
+    // rows whose tiles are all done can be folded while later bands multiply,
+    // but only once every row of op(A) has been handed to the caller: the
+    // caller queues the copy of C (and records c_ready) with the last rows,
+    // and a fold enqueued before that record would not wait for C
+    if (banded && fold_banded && t1 < tiles && rows_cut >= L.m_pad) {
       const int64_t rows_done = std::min<int64_t>(g.m, (int64_t)(t1 / tiles_n) * kBM);
       if (rows_done > rows_folded) {
         if ((e = fold_rows(rows_folded, rows_done)) != cudaSuccess) return e;

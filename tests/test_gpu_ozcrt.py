@@ -126,6 +126,33 @@ def test_crt_accuracy_spread(crt, O, torch_cuda, size):
     assert err.max() <= 1.0, err.max()
 
 
+@pytest.mark.parametrize("scheme", [2, 1])
+def test_host_pointer_row_bands_match_device(crt, torch_cuda, scheme):
+    """A host-pointer qgemm with more 128 x 256 tiles than the GPU has SMs
+    (13 x 12 = 156 tiles) runs in row bands: A is copied band by band, C after
+    A, and C is folded and copied back in row bands.  With beta != 0 and a
+    random C the result must equal the device-pointer call's bit for bit; a
+    fold that ran before C arrived would read the staging buffer's previous
+    contents (another call's result, left there on purpose)."""
+    torch = torch_cuda
+    api.set_ozaki_scheme(scheme)
+    api.set_ozaki_slices(15)
+    api.set_ozaki_digit_bits(9)
+    m, n, k = 1664, 3072, 96
+    rng = G.rng_for(424 + scheme)
+    A, B, C = G.spread_uniform(rng, m * k), G.spread_uniform(rng, k * n), G.uniform_full(rng, m * n)
+    alpha, beta = Q.scalar(1.25), Q.scalar(-0.75)
+    dA, dB, dC = to_dev(torch, A), to_dev(torch, B), to_dev(torch, C)
+    api.gemm_dev("R", "N", "N", m, n, k, alpha, dA, k, dB, n, beta, dC, n)
+    torch.cuda.synchronize()
+    ref = to_host(dC)
+    other = G.uniform_full(rng, m * n)
+    api.gemm("R", "N", "N", m, n, k, alpha, A, k, B, n, Q.scalar(0.0), other, n)
+    got = C.copy()
+    api.gemm("R", "N", "N", m, n, k, alpha, A, k, B, n, beta, got, n)
+    assert Q.same_bits(got, ref).all(), int((~Q.same_bits(got, ref)).sum())
+
+
 def test_crt_special_values(crt, O):
     rng = G.rng_for(422)
     m, n, k = 9, 11, 13
