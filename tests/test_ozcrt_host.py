@@ -79,6 +79,18 @@ def test_table_limits(sq):
     assert table(sq, 191, 1 << 40) is None  # more moduli than the table holds
 
 
+def test_table_covers_every_digit_setting(sq):
+    """The automatic scheme takes residues for every digit count the library
+    accepts: 2..22 digits of 7 bits, 2..20 of 8, 2..18 of 9 (T <= 161), for k
+    up to 2^31 - 1; at most 41 moduli and 12 words are needed."""
+    for bits, smax in ((7, 22), (8, 20), (9, 18)):
+        for s in range(2, smax + 1):
+            for k in (1, 64, 4096, 1 << 20, (1 << 31) - 1):
+                t = table(sq, bits * s - 1, k)
+                assert t is not None, (bits, s, k)
+                assert t[0] <= 41 and t[1] <= MAXWORDS, (bits, s, k, t[0], t[1])
+
+
 def test_crt_mod(sq):
     rng = np.random.default_rng(7)
     x = np.concatenate([rng.integers(0, 1 << 31, 20000, dtype=np.uint64),
