@@ -2,7 +2,8 @@
 // not allocate device memory.
 //
 // quadblas_qdot_dev takes its scratch (one partial accumulator per block of
-// the first qdot kernel) from the stream-ordered pool with cudaMallocAsync.
+// the first qdot kernel) from the library's stream-ordered memory pool
+// (cudaMallocFromPoolAsync).
 // Some callers cannot let a library do that: programs that hand all device
 // memory to their own allocator or memory plan up front (so a cudaMalloc from
 // a library would fail or fragment their pool), and latency-sensitive loops
