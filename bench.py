@@ -228,11 +228,16 @@ class Qgemm:
         self.api.gemm_dev("R", "N", "N", self.m, self.n, self.k, self.alpha, self.dA, self.k, self.dB, self.n,
                           self.beta, self.dC, self.n)
 
-    def e2e(self, steps):
+    def e2e(self, steps, pinned=True):
         """Public host-pointer API (quadblas_qgemm_q): H2D of A, B, C and D2H of C
-        from pinned host memory inside the timed region."""
+        inside the timed region, from pinned host memory or (pinned=False) from
+        ordinary pageable memory, as a reference caller's Matrix<L> allocates
+        it (posix_memalign, include/quadblas/memory/allocation.hpp:25)."""
         torch, api = self.torch, self.api
-        pin = lambda a: torch.from_numpy(a.view(np.int64)).pin_memory().numpy().view(np.uint64)  # noqa: E731
+        if pinned:
+            pin = lambda a: torch.from_numpy(a.view(np.int64)).pin_memory().numpy().view(np.uint64)  # noqa: E731
+        else:
+            pin = lambda a: np.array(a, copy=True)  # noqa: E731
         hA, hB, hC = pin(self.A), pin(self.B), pin(self.C)
         api.gemm("R", "N", "N", self.m, self.n, self.k, self.alpha, hA, self.k, hB, self.n, self.beta, hC, self.n)
         t0 = time.perf_counter()
@@ -304,43 +309,15 @@ def batched_config4(torch, api, rank, reps=3):
     """10,000 qgemm (m, n, k log-uniform in [8, 256]), 10,000 qgemv (m, n in
     [16, 2048]) and 10,000 qdot (n in [64, 65536]) with full-mantissa uniform
     values, row-major 'N', alpha = 1, beta = 0: one persistent launch (CUDA
-    graph replay) against the same problems launched one call at a time."""
-    rng = G.rng_for(4000 + rank)
-    gm = G.log_uniform_int(rng, 8, 256, 3 * 10000).reshape(3, 10000)
-    gv = G.log_uniform_int(rng, 16, 2048, 2 * 10000).reshape(2, 10000)
-    dn = G.log_uniform_int(rng, 64, 65536, 10000)
-    sizes = []
-    for i in range(10000):
-        m, n, k = int(gm[0, i]), int(gm[1, i]), int(gm[2, i])
-        sizes.append((0, m, n, k, m * k, k * n, m * n))
-    for i in range(10000):
-        m, n = int(gv[0, i]), int(gv[1, i])
-        sizes.append((1, m, n, 0, m * n, n, m))
-    for i in range(10000):
-        n = int(dn[i])
-        sizes.append((2, 0, n, 0, n, n, 1))
-    total = sum(a + b + c for _, _, _, _, a, b, c in sizes)
-    buf = G.uniform_full_device(torch, total, seed=4100 + rank)
-    base = buf.data_ptr()
-    probs = np.zeros(len(sizes), dtype=api.PROBLEM_DTYPE)
-    one, zero = Q.scalar(1.0)[0], Q.scalar(0.0)[0]
-    off = 0
+    graph replay) against the same problems launched one device-pointer call
+    at a time from a C loop (quadblas_batch_run_serial).  Outside the timed
+    regions the two sets of outputs are compared bit for bit (both are the
+    correctly rounded sums)."""
+    probs, inp, out, lay = G.config4_batch(torch, 4000 + rank)
     flops = 0.0
-    for p, (op, m, n, k, sa, sb, sc) in zip(probs, sizes):
-        p["op"], p["layout"], p["transa"], p["transb"] = op, b"R", b"N", b"N"
-        p["m"], p["n"], p["k"] = m, n, k
-        p["alpha"], p["beta"] = one, zero
-        p["A"], p["B"], p["C"] = base + 16 * off, base + 16 * (off + sa), base + 16 * (off + sa + sb)
-        if op == 0:
-            p["lda"], p["ldb"], p["ldc"] = k, n, n
-            flops += 2.0 * m * n * k
-        elif op == 1:
-            p["lda"], p["ldb"], p["ldc"] = n, 1, 1
-            flops += 2.0 * m * n
-        else:
-            p["lda"], p["ldb"], p["ldc"] = 1, 1, 1
-            flops += 2.0 * n
-        off += sa + sb + sc
+    for op, m, n, k, *_ in lay:
+        flops += 2.0 * (m * n * k if op == 0 else (m * n if op == 1 else n))
+    c0 = out.clone()
     # the work-item granularity comes from the autotuner (cached per GPU model)
     t0 = time.perf_counter()
     grain = api.batch_autotune()
@@ -367,43 +344,51 @@ def batched_config4(torch, api, rank, reps=3):
     e1.record()
     torch.cuda.synchronize()
     ms_batched = e0.elapsed_time(e1) / reps
-    # the same problems, one library call each, on the current stream
-    lib = api.load()
-    cs = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
-    a_p, b_p = one.ctypes.data_as(ctypes.c_void_p), zero.ctypes.data_as(ctypes.c_void_p)
-    A_, B_, C_ = (ctypes.c_void_p(int(v)) for v in (0, 0, 0))
-
-    def one_by_one():
-        for p in probs:
-            op = int(p["op"])
-            A_, B_, C_ = ctypes.c_void_p(int(p["A"])), ctypes.c_void_p(int(p["B"])), ctypes.c_void_p(int(p["C"]))
-            if op == 0:
-                lib.quadblas_qgemm_dev(b"R", b"N", b"N", int(p["m"]), int(p["n"]), int(p["k"]), a_p, A_,
-                                       int(p["lda"]), B_, int(p["ldb"]), b_p, C_, int(p["ldc"]), cs)
-            elif op == 1:
-                lib.quadblas_qgemv_dev(b"R", b"N", int(p["m"]), int(p["n"]), a_p, A_, int(p["lda"]), B_, 1, b_p,
-                                       C_, 1, cs)
-            else:
-                lib.quadblas_qdot_dev(int(p["n"]), A_, 1, B_, 1, C_, cs)
-
-    one_by_one()
+    out.copy_(c0)
+    graph.replay()
+    torch.cuda.synchronize()
+    batched = out.clone()
+    # the same problems, one library call each from a C loop, on the current stream
+    api.batch_run_serial(probs)  # warm-up (the scratch pool grows to need)
+    torch.cuda.synchronize()
+    out.copy_(c0)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     e0.record()
-    one_by_one()
+    api.batch_run_serial(probs)
     e1.record()
     torch.cuda.synchronize()
     wall_single = time.perf_counter() - t0
     ms_single = max(e0.elapsed_time(e1), wall_single * 1e3)
+    same = bool(torch.equal(batched, out))
     plan.close()
-    del buf
+    del graph, inp, out, c0, batched
     torch.cuda.empty_cache()
-    return {"problems": len(sizes), "gflops": round(flops / (ms_batched * 1e-3) / 1e9, 2),
+    return {"problems": len(probs), "gflops": round(flops / (ms_batched * 1e-3) / 1e9, 2),
             "ms_batched_graph_replay": round(ms_batched, 3), "ms_one_call_per_problem": round(ms_single, 3),
+            "one_by_one": "quadblas_batch_run_serial (C loop of device-pointer calls)",
             "speedup_vs_one_by_one": round(ms_single / ms_batched, 2), "plan_ms": round(plan_s * 1e3, 1),
             "work_items": info["items"], "grain": info["grain"], "autotuned_grain": grain,
             "autotune_ms": round(tune_s * 1e3, 1), "launches_per_batch": 1,
+            "parity": "bit-identical to one-by-one" if same else "MISMATCH against one-by-one",
             "method": "soft-float wide accumulator for every problem", "quad_flops": flops}
+
+
+def oracle_accuracy(W, C, rank, samples=512):
+    """Max ulp and max relative error of the qgemm result C against the exact
+    oracle (correctly rounded exact sums) on a seeded sample of entries;
+    runs after the timed region (the oracle checks, it is not measured)."""
+    from oracle import oracle as O
+    O.build()
+    rng = np.random.default_rng(900 + rank)
+    rows = rng.integers(0, W.m, samples)
+    cols = rng.integers(0, W.n, samples)
+    R, _, _ = O.exact_gemm(W.k, W.A, W.k, 1, W.B, W.n, 1, rows, cols)
+    got = C[rows * W.n + cols]
+    d = ulp_distance(got, R)
+    return {"max": float(d.max()), "max_rel": float(relative_error(got, R).max()),
+            "exact_frac": float((d == 0).mean()), "samples": int(samples),
+            "reference": "exact oracle (Kulisch accumulator, correctly rounded)"}
 
 
 def profile_read(lib):
@@ -550,10 +535,17 @@ def main():
             launches = args.steps
             dtype = "u32 (soft-float integer limbs)"
         metric, unit = f"qgemm binary128 GFLOP/s ({size}^3)", "GFLOP/s"
-        e2e_s, h2d, d2h = W.e2e(max(1, min(args.steps, 3)))
+        # the same number of calls as the device-timed headline
+        e2e_s, h2d, d2h = W.e2e(max(1, args.steps))
         if dist is not None:
             dist.barrier()
         e2e_s = max_over_ranks(dist, e2e_s)
+        if not args.no_secondary and size == 4096:
+            pg_s, _, _ = W.e2e(max(1, args.steps), pinned=False)
+            pg_s = max_over_ranks(dist, pg_s)
+            secondary["e2e_pageable"] = {"value": round(whole_job_rate(W.flops(), world, pg_s) / 1e9, 3),
+                                         "unit": unit, "ms_per_step": round(pg_s * 1e3, 3),
+                                         "host_buffers": "pageable (not registered with CUDA)"}
         e2e = {"value": round(whole_job_rate(W.flops(), world, e2e_s) / 1e9, 3), "unit": unit,
                "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": int(d2h)}
@@ -580,6 +572,7 @@ def main():
                                                 "ozaki_speedup": round(value / world / sf_gflops, 2)}
             rng = np.random.default_rng(5)
             idx = rng.integers(0, size * size, 4096)
+            secondary["ozaki_ulp_vs_exact_oracle"] = oracle_accuracy(W, C_oz, rank)
             d = ulp_distance(C_oz[idx], C_sf[idx])
             secondary["ozaki_ulp_from_correctly_rounded"] = {"max": float(d.max()),
                                                              "max_rel": float(relative_error(C_oz[idx],
@@ -611,6 +604,18 @@ def main():
                               "max_rel": float(relative_error(Cs, C_sf[idx]).max()),
                               "exact_frac": float((ds == 0).mean())})
             lib.quadblas_profile_enable(0)
+            # the library's own default setting (every Ozaki knob at 0)
+            api.set_ozaki_scheme(0)
+            api.set_ozaki_slices(0)
+            api.set_ozaki_digit_bits(0)
+            ms_d = time_steps(torch, W.step, args.steps, 1, dist) / args.steps
+            C_d = to_host(W.dC)
+            dd = ulp_distance(C_d[idx], C_sf[idx])
+            secondary["ozaki_library_default"] = {
+                "value": round(whole_job_rate(W.flops(), world, ms_d * 1e-3) / 1e9, 3), "unit": "GFLOP/s",
+                "ms_per_step": round(ms_d, 4), "setting": "scheme auto, 16 digits of 9 bits (T = 143)",
+                "max_ulp_from_correctly_rounded": float(dd.max()), "exact_frac": float((dd == 0).mean()),
+                "ulp_vs_exact_oracle": oracle_accuracy(W, C_d, rank, samples=256)}
             api.set_ozaki_scheme(SCHEMES[args.scheme])
             api.set_ozaki_slices(slices)
             api.set_ozaki_digit_bits(bits)
@@ -678,6 +683,8 @@ def main():
                 "scaling": "weak", "vs_baseline": None, "dtype": dtype, "data": "synthetic (seeded)",
                 "config": cfg, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
                 "clocks": clk.summary(), "gpu_launches": launches}
+        if "ozaki_ulp_vs_exact_oracle" in secondary:
+            line["ozaki_ulp_vs_exact_oracle"] = secondary["ozaki_ulp_vs_exact_oracle"]
         if secondary:
             line["secondary"] = secondary
         print(json.dumps(line), flush=True)

@@ -47,7 +47,10 @@ enum {
   QBLAS_ERR_NO_MEMORY = 3,
   QBLAS_ERR_NOT_SUPPORTED = 4,
   QBLAS_ERR_NO_DEVICE = 5,
-  QBLAS_ERR_MISALIGNED = 6
+  QBLAS_ERR_MISALIGNED = 6,
+  /* a wait inside an Ozaki qgemm kernel gave up (1 s without progress); the
+   * call's C holds NaN where a result was due */
+  QBLAS_ERR_TIMEOUT = 7
 };
 
 enum { QBLAS_METHOD_AUTO = 0, QBLAS_METHOD_SOFTFLOAT = 1, QBLAS_METHOD_OZAKI = 2 };
@@ -178,6 +181,14 @@ int quadblas_batch_destroy(void *plan);
 int quadblas_batch_info(void *plan, int64_t *info4);
 int quadblas_batch_autotune(int64_t *grain_out);
 int quadblas_batch_set_grain(int64_t grain);
+/* The same problems without the batch: one device-pointer call per problem
+ * (quadblas_qgemm_dev with the soft-float method, quadblas_qgemv_dev,
+ * quadblas_qdot_dev), in order, on `stream`, from a C loop.  It is the
+ * one-call-per-problem baseline the batched launch is measured against, and
+ * its results are bit-identical to quadblas_batch_execute's (both are the
+ * correctly rounded sums through the single-call epilogues).  Returns the
+ * first failing call's status. */
+int quadblas_batch_run_serial(const qblas_problem *problems, int64_t count, void *stream);
 
 /* ---- Configuration and errors (no reference counterpart) -------------- */
 /* Method of qgemm and qgemv: QBLAS_METHOD_AUTO (soft-float for both),
@@ -235,6 +246,18 @@ int quadblas_debug_fail_allocations(int count);
  * enabled). */
 int quadblas_debug_count_exact_rows(int on);
 long long quadblas_debug_exact_rows(void);
+/* Device-side failures of device-pointer calls (no reference counterpart).
+ * The part 3 calls return before their kernels run, so a failure found on
+ * the GPU cannot be their return value: an Ozaki qgemm whose tensor-core
+ * kernel gave up on a wait (1 s without progress) writes NaN to its C and
+ * sets a flag of the current device.  After synchronising the streams of the
+ * calls in question, quadblas_device_status returns QBLAS_ERR_TIMEOUT if the
+ * flag is set (QBLAS_OK otherwise) and clears it when `clear` is nonzero.
+ * Host-pointer calls (parts 1 and 2) check their own call and return
+ * QBLAS_ERR_TIMEOUT directly; they do not touch this flag.  (A qgemv whose
+ * Ozaki kernel gives up still returns correct results: every row is then
+ * recomputed exactly.) */
+int quadblas_device_status(int clear);
 /* Status of the calling thread's last call (part 1 calls record it too). */
 int quadblas_last_error(void);
 const char *quadblas_error_string(int code);

@@ -23,9 +23,16 @@ c_i64 = ctypes.c_int64
 c_vp = ctypes.c_void_p
 
 
+# The reference checkout whose headers oracle/_ref is compiled from: the
+# directory in QBLAS_REFERENCE_DIR, else the read-only mount the reference is
+# checked out at on the build machine.  Where neither exists, _ref is skipped.
+REFERENCE_DIR = os.environ.get("QBLAS_REFERENCE_DIR", "/root/reference")
+
+
 def build(quiet: bool = True) -> None:
     """Compile the oracle (and oracle/_ref where the reference tree exists)."""
-    out = subprocess.run(["make", "-C", HERE], capture_output=True, text=True)
+    ref = REFERENCE_DIR if os.path.isfile(os.path.join(REFERENCE_DIR, "include", "quadblas", "quadblas.hpp")) else ""
+    out = subprocess.run(["make", "-C", HERE, f"REF={ref}"], capture_output=True, text=True)
     if out.returncode != 0:
         raise RuntimeError("oracle build failed:\n" + out.stdout + out.stderr)
     if not quiet:

@@ -48,6 +48,7 @@ _SIGS = {
     "quadblas_batch_info": (ci, [vp, vp]),
     "quadblas_batch_autotune": (ci, [vp]),
     "quadblas_batch_set_grain": (ci, [i64]),
+    "quadblas_batch_run_serial": (ci, [vp, i64, vp]),
     # configuration
     "quadblas_set_method": (ci, [ci]),
     "quadblas_get_method": (ci, []),
@@ -63,6 +64,7 @@ _SIGS = {
     "quadblas_debug_fail_allocations": (ci, [ci]),
     "quadblas_debug_count_exact_rows": (ci, [ci]),
     "quadblas_debug_exact_rows": (ctypes.c_longlong, []),
+    "quadblas_device_status": (ci, [ci]),
     "quadblas_last_error": (ci, []),
     "quadblas_error_string": (ctypes.c_char_p, [ci]),
 }

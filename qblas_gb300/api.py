@@ -150,6 +150,12 @@ def get_ozaki_scheme() -> int:
     return load().quadblas_get_ozaki_scheme()
 
 
+def device_status(clear: bool = True) -> int:
+    """QBLAS_ERR_TIMEOUT (7) if a device-pointer Ozaki qgemm on the current
+    device timed out since the last clear, else 0 (read after syncing)."""
+    return int(load().quadblas_device_status(1 if clear else 0))
+
+
 def release_buffers() -> None:
     check(load().quadblas_release_buffers())
 
@@ -175,6 +181,13 @@ PROBLEM_DTYPE = np.dtype([("op", "<i4"), ("layout", "S1"), ("transa", "S1"), ("t
                           ("alpha", "<u8", (2,)), ("beta", "<u8", (2,)), ("A", "<u8"), ("lda", "<i8"),
                           ("B", "<u8"), ("ldb", "<i8"), ("C", "<u8"), ("ldc", "<i8")], align=True)
 assert PROBLEM_DTYPE.itemsize == 112
+
+
+def batch_run_serial(problems: np.ndarray, stream=None) -> None:
+    """Each problem by its own device-pointer call, in order (C loop)."""
+    problems = np.ascontiguousarray(problems, dtype=PROBLEM_DTYPE)
+    check(load().quadblas_batch_run_serial(problems.ctypes.data_as(ctypes.c_void_p), len(problems),
+                                           _stream(stream)))
 
 
 class BatchPlan:

@@ -24,6 +24,7 @@
 #include <thread>
 
 #include "kernels.h"
+#include "quadblas_gpu.h"
 
 using qb::q128;
 
@@ -91,6 +92,7 @@ struct DevState {
   cudaEvent_t ev[kNumEvents] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   void* buf[kNumSlots] = {nullptr};
   size_t cap[kNumSlots] = {0};
+  int* err_host = nullptr;  // pinned: the last host-pointer Ozaki call's error word
 };
 
 constexpr int kMaxDevices = 64;
@@ -101,6 +103,38 @@ int current_device(int& dev) {
   if (e != cudaSuccess) return cuda_status(e);
   if (dev < 0 || dev >= kMaxDevices) return qb::kErrNoDevice;
   return qb::kOk;
+}
+
+// Per-device timeout flag of device-pointer calls: mapped pinned host
+// memory that the Ozaki fold kernel sets (quadblas_device_status reads it).
+struct TimeoutFlag {
+  std::mutex mu;
+  int* host = nullptr;
+  int* dev = nullptr;
+};
+TimeoutFlag g_timeout[kMaxDevices];
+
+int* device_timeout_flag(int dev) {
+  if (dev < 0 || dev >= kMaxDevices) return nullptr;
+  TimeoutFlag& f = g_timeout[dev];
+  std::lock_guard<std::mutex> l(f.mu);
+  if (!f.dev) {
+    void* h = nullptr;
+    if (cudaHostAlloc(&h, sizeof(int), cudaHostAllocMapped) != cudaSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
+    void* d = nullptr;
+    if (cudaHostGetDevicePointer(&d, h, 0) != cudaSuccess) {
+      cudaGetLastError();
+      cudaFreeHost(h);
+      return nullptr;
+    }
+    *static_cast<volatile int*>(h) = 0;
+    f.host = static_cast<int*>(h);
+    f.dev = static_cast<int*>(d);
+  }
+  return f.dev;
 }
 
 int ensure_slot(DevState& st, Slot s, size_t bytes) {
@@ -317,12 +351,11 @@ int dev_gemv(const GemvPlan& p0, const void* alpha, const void* dA, const void* 
 int gemm_method() {
   int m = g_method.load();
   if (m != 0) return m;
-  static int env = -1;
-  if (env < 0) {
+  // read once (a function-local static is initialised once, thread-safely)
+  static const int env = [] {
     const char* v = getenv("QBLAS_METHOD");
-    env = 1;
-    if (v && (strcmp(v, "ozaki") == 0 || strcmp(v, "2") == 0)) env = 2;
-  }
+    return (v && (strcmp(v, "ozaki") == 0 || strcmp(v, "2") == 0)) ? 2 : 1;
+  }();
   return env;
 }
 
@@ -339,12 +372,11 @@ int gemm_digits(int64_t k) {
   int smax = qb::ozaki_digit_cap(b, k);
   int s = g_slices.load();
   if (s > 0) return std::min(s, smax);
-  static int env = -1;
-  if (env < 0) {
+  static const int env = [] {
     const char* v = getenv("QBLAS_SLICES");
-    env = v ? atoi(v) : 0;
-    if (env < 2 || env > 22) env = 0;
-  }
+    const int e = v ? atoi(v) : 0;
+    return (e < 2 || e > 22) ? 0 : e;
+  }();
   return std::min(env ? env : qb::ozaki_default_digits(b), smax);
 }
 
@@ -353,9 +385,11 @@ size_t gemm_scratch_bytes(const GemmPlan& p, int method) {
   return qb::ozaki_scratch_bytes(p.g.m, p.g.n, p.g.k, gemm_digits(p.g.k), gemm_digit_bits(), g_ozaki_scheme.load());
 }
 
+// report: a device-accessible word the fold sets on a timed-out wait, or
+// nullptr (the caller checks the call's own error word instead).
 int dev_gemm(GemmPlan p, int method, const void* alpha, const void* dA, const void* dB,
              const void* beta, void* dC, cudaStream_t s, void* scratch_or_null,
-             const qb::OzakiOverlap* overlap = nullptr) {
+             const qb::OzakiOverlap* overlap = nullptr, int* report = nullptr) {
   if (!aligned16(dA) || !aligned16(dB) || !aligned16(dC)) return qb::kErrMisaligned;
   p.g.A = (const q128*)dA;
   p.g.B = (const q128*)dB;
@@ -373,7 +407,7 @@ int dev_gemm(GemmPlan p, int method, const void* alpha, const void* dA, const vo
     }
   }
   cudaError_t e = qb::launch_gemm_ozaki(p.g, gemm_digits(p.g.k), gemm_digit_bits(), scratch, s, overlap,
-                                        g_ozaki_scheme.load());
+                                        g_ozaki_scheme.load(), report);
   if (!scratch_or_null) cudaFreeAsync(scratch, s);
   return cuda_status(e);
 }
@@ -534,6 +568,28 @@ int host_gemm(char layout, char transa, char transb, int64_t m, int64_t n, int64
       (rc = ensure_slot(st, kSlotC, p.extC * 16)) ||
       (rc = ensure_slot(st, kSlotScratch, gemm_scratch_bytes(p, method))))
     return rc;
+  if (method == 2 && !st.err_host) {
+    void* h = nullptr;
+    if (cudaMallocHost(&h, 256) != cudaSuccess) {
+      cudaGetLastError();
+      return qb::kErrNoMemory;
+    }
+    st.err_host = static_cast<int*>(h);
+  }
+  // this call's error word (in its scratch), copied back after the fold and
+  // checked once the stream is done; the device-pointer flag is not involved
+  auto timed_out = [&]() -> int {
+    if (method != 2) return qb::kOk;
+    const size_t off = qb::ozaki_error_flag_offset(p.g.m, p.g.n, p.g.k, gemm_digits(p.g.k), gemm_digit_bits(),
+                                                   g_ozaki_scheme.load());
+    *static_cast<volatile int*>(st.err_host) = 0;
+    return cuda_status(cudaMemcpyAsync(st.err_host, static_cast<char*>(st.buf[kSlotScratch]) + off, sizeof(int),
+                                       cudaMemcpyDeviceToHost, st.stream));
+  };
+  auto check_timeout = [&](int status) -> int {
+    if (status || method != 2) return status;
+    return *static_cast<volatile int*>(st.err_host) ? qb::kErrTimeout : qb::kOk;
+  };
   if (method == 2) {
     // Ozaki, with the host link kept busy in the order the GPU needs the
     // data: B first (copied and cut into digits on kSideB), then A in row
@@ -550,12 +606,13 @@ int host_gemm(char layout, char transa, char transb, int64_t m, int64_t n, int64
       return rc;
     rc = dev_gemm(p, method, alpha, st.buf[kSlotA], st.buf[kSlotB], beta, st.buf[kSlotC], st.stream,
                   st.buf[kSlotScratch], &ov);
+    if (!rc) rc = timed_out();
     if (!rc && bc.copied_rows > 0) {
       // the bands covered C; wait for their copies
       if (bc.copied_rows != p.g.m) rc = qb::kErrCuda;
       int rc2 = cuda_status(cudaStreamSynchronize(st.side[kSideC]));
       int rc3 = cuda_status(cudaStreamSynchronize(st.stream));
-      return rc ? rc : (rc2 ? rc2 : rc3);
+      return check_timeout(rc ? rc : (rc2 ? rc2 : rc3));
     }
   } else {
     if ((rc = h2d(st.buf[kSlotA], A, p.extA, st.stream)) ||
@@ -574,7 +631,8 @@ int host_gemm(char layout, char transa, char transb, int64_t m, int64_t n, int64
     return rc;
   }
   if ((rc = d2h(C, st.buf[kSlotC], p.extC, st.stream))) return rc;
-  return cuda_status(cudaStreamSynchronize(st.stream));
+  if ((rc = timed_out())) return rc;
+  return check_timeout(cuda_status(cudaStreamSynchronize(st.stream)));
 }
 
 }  // namespace
@@ -761,7 +819,38 @@ QBLAS_EXPORT int quadblas_qgemm_dev(char layout, char transa, char transb, int64
   if (rc) return fail(rc);
   if (m == 0 || n == 0 || k == 0) return fail(qb::kOk);
   if (!alpha || !beta) return fail(qb::kErrInvalidValue);
-  return fail(dev_gemm(p, gemm_method(), alpha, dA, dB, beta, dC, (cudaStream_t)stream, nullptr));
+  int dev = 0;
+  int* report = cudaGetDevice(&dev) == cudaSuccess ? device_timeout_flag(dev) : nullptr;
+  return fail(dev_gemm(p, gemm_method(), alpha, dA, dB, beta, dC, (cudaStream_t)stream, nullptr, nullptr,
+                       report));
+}
+
+// ===========================================================================
+// Batched problems, one call each (the batch's serial baseline)
+// ===========================================================================
+QBLAS_EXPORT int quadblas_batch_run_serial(const qblas_problem* problems, int64_t count, void* stream) {
+  if (count < 0 || (count > 0 && !problems)) return fail(qb::kErrInvalidValue);
+  cudaStream_t s = (cudaStream_t)stream;
+  for (int64_t i = 0; i < count; ++i) {
+    const qblas_problem& q = problems[i];
+    int rc = qb::kOk;
+    if (q.op == QBLAS_OP_GEMM) {
+      GemmPlan p;
+      rc = plan_gemm(q.layout, q.transa, q.transb, q.m, q.n, q.k, q.lda, q.ldb, q.ldc, p);
+      if (!rc && q.m > 0 && q.n > 0 && q.k > 0)
+        rc = dev_gemm(p, 1, q.alpha, q.A, q.B, q.beta, q.C, s, nullptr);  // soft-float, as the batch
+    } else if (q.op == QBLAS_OP_GEMV) {
+      GemvPlan p;
+      rc = plan_gemv(q.layout, q.transa, q.m, q.n, q.lda, p);
+      if (!rc && p.m > 0 && p.n > 0) rc = dev_gemv(p, q.alpha, q.A, q.B, q.ldb, q.beta, q.C, q.ldc, s, nullptr);
+    } else if (q.op == QBLAS_OP_DOT) {
+      rc = dev_dot(q.n, q.A, q.lda, q.B, q.ldb, q.C, 0, s, nullptr);
+    } else {
+      rc = qb::kErrInvalidValue;
+    }
+    if (rc) return fail(rc);
+  }
+  return fail(qb::kOk);
 }
 
 // ===========================================================================
@@ -845,6 +934,18 @@ QBLAS_EXPORT int quadblas_profile_read(double* out4, int* calls) {
   if (!out4 || !calls) return fail(qb::kErrInvalidValue);
   return qb::ozaki_profile_read(out4, calls);
 }
+QBLAS_EXPORT int quadblas_device_status(int clear) {
+  int dev = 0;
+  int rc = current_device(dev);
+  if (rc) return fail(rc);
+  TimeoutFlag& f = g_timeout[dev];
+  std::lock_guard<std::mutex> l(f.mu);
+  if (!f.host) return fail(qb::kOk);  // no device-pointer Ozaki call yet
+  volatile int* h = f.host;
+  const int set = *h;
+  if (clear) *h = 0;
+  return fail(set ? qb::kErrTimeout : qb::kOk);
+}
 QBLAS_EXPORT int quadblas_last_error(void) { return g_last_error; }
 QBLAS_EXPORT const char* quadblas_error_string(int code) {
   switch (code) {
@@ -855,6 +956,7 @@ QBLAS_EXPORT const char* quadblas_error_string(int code) {
     case qb::kErrNotSupported: return "not supported";
     case qb::kErrNoDevice: return "no usable CUDA device";
     case qb::kErrMisaligned: return "device pointer not 16-byte aligned";
+    case qb::kErrTimeout: return "a device-side wait timed out (outputs of that call are NaN)";
     default: return "unknown error";
   }
 }

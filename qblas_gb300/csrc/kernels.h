@@ -21,6 +21,7 @@ enum Status : int {
   kErrNotSupported = 4,
   kErrNoDevice = 5,
   kErrMisaligned = 6,
+  kErrTimeout = 7,
 };
 
 // op(A) is an m x n matrix with element (i, j) at A[i*si + j*sj].
@@ -103,8 +104,11 @@ struct OzakiOverlap {
   cudaStream_t a_stream;
   cudaEvent_t a_done;
 };
+// `report`, when not null, is a device-accessible word (mapped host memory)
+// that the fold sets to 1 if a wait of the tensor-core kernel timed out.
 cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scratch,
-                              cudaStream_t s, const OzakiOverlap* overlap = nullptr, int scheme = 0);
+                              cudaStream_t s, const OzakiOverlap* overlap = nullptr, int scheme = 0,
+                              int* report = nullptr);
 // Phase timing of Ozaki calls with CUDA events (off by default).
 void ozaki_profile_enable(bool on);
 int ozaki_profile_read(double* out4, int* calls);

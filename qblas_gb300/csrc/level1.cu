@@ -14,6 +14,8 @@
 // term to the error budget.  The rounding is certified against that budget
 // (exact.cuh); if the sum cancels below it, a third kernel recomputes the
 // sum exactly (Kulisch accumulator) — it returns at once otherwise.
+#include <atomic>
+
 #include "exact.cuh"
 #include "kernels.h"
 #include "reduce.cuh"
@@ -23,17 +25,19 @@ namespace qb {
 constexpr int kDotThreads = 256;
 constexpr int kDotBlocksPerSm = 4;
 
+// Per-device caches below are atomics: host threads may call on one device
+// at the same time; they compute the same value, so the last store wins.
 int device_sm_count() {
-  static int cached[64] = {0};
+  static std::atomic<int> cached[64];
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 148;
-  if (!cached[dev]) {
-    int v = 0;
+  int v = cached[dev].load(std::memory_order_relaxed);
+  if (!v) {
     if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0)
       v = 148;
-    cached[dev] = v;
+    cached[dev].store(v, std::memory_order_relaxed);
   }
-  return cached[dev];
+  return v;
 }
 
 int resident_blocks_per_sm(const void* kernel, int threads, size_t smem) {
@@ -110,14 +114,17 @@ __global__ void __launch_bounds__(kDotThreads)
 
 // One wave of resident blocks (no tail wave), fewer for short vectors.
 static int64_t dot_blocks(int64_t n) {
-  static int cached[64] = {0};
+  static std::atomic<int> cached[64];
   int dev = 0;
   cudaGetDevice(&dev);
   int per_sm = kDotBlocksPerSm;
   if (dev >= 0 && dev < 64) {
-    if (!cached[dev])
-      cached[dev] = resident_blocks_per_sm((const void*)qdot_partial_kernel, kDotThreads, 0);
-    per_sm = cached[dev] < kDotBlocksPerSm ? cached[dev] : kDotBlocksPerSm;
+    int c = cached[dev].load(std::memory_order_relaxed);
+    if (!c) {
+      c = resident_blocks_per_sm((const void*)qdot_partial_kernel, kDotThreads, 0);
+      cached[dev].store(c, std::memory_order_relaxed);
+    }
+    per_sm = c < kDotBlocksPerSm ? c : kDotBlocksPerSm;
   }
   int64_t per_block = (int64_t)kDotThreads * 4;  // at least 4 terms per thread
   int64_t want = (n + per_block - 1) / per_block;

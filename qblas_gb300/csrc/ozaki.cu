@@ -43,6 +43,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <mutex>
 #include <vector>
 
@@ -490,6 +491,7 @@ struct OzakiFoldParams {
   int64_t sci, scj;
   q128 alpha, beta;
   const int* err;
+  int* report;  // set to 1 when err is (mapped host memory; may be null)
 };
 
 // Each thread folds four neighbouring columns j0..j0+3 of one row: one
@@ -525,6 +527,7 @@ __global__ void __launch_bounds__(256, 3) ozaki_fold_kernel(OzakiFoldParams P) {
     fold_step_t<B>(f[3], t3);
   }
   const bool failed = *P.err != 0;
+  if (failed && P.report && i == 0 && j0 == 0) *reinterpret_cast<volatile int*>(P.report) = 1;
   const int Si = P.S[i];
   const uint32_t fai = P.fa[i];
 #pragma unroll
@@ -609,6 +612,7 @@ __global__ void __launch_bounds__(256) ozaki_crt_fold_kernel(OzakiFoldParams P, 
     crt_acc_pair(A1, c0 >> 16, c1 >> 16, p0, p1, P0, P1, W);
   }
   const bool failed = *P.err != 0;
+  if (failed && P.report && i == 0 && j0 == 0) *reinterpret_cast<volatile int*>(P.report) = 1;
   const int Si = P.S[i];
   const uint32_t fai = P.fa[i];
 #pragma unroll
@@ -823,10 +827,10 @@ static void launch_crt_split(const CrtTable& tab, dim3 grid, dim3 blk, cudaStrea
 static cudaError_t launch_crt_fold(const CrtTable& tab, cudaStream_t st, const OzakiFoldParams& F) {
   dim3 blk(32, 8), grid((unsigned)((F.n + 63) / 64), (unsigned)((F.m + 7) / 8));
   const size_t dyn = (size_t)tab.n * 256 * 4;
-  static bool attr_set[64] = {false};
+  static std::atomic<bool> attr_set[64];
   int dev = 0;
   cudaGetDevice(&dev);
-  if (dev >= 0 && dev < 64 && !attr_set[dev]) {
+  if (dev >= 0 && dev < 64 && !attr_set[dev].load(std::memory_order_acquire)) {
     const int mx = kCrtMaxMods * 256 * 4;
     cudaError_t e;
     if ((e = cudaFuncSetAttribute(ozaki_crt_fold_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx)) !=
@@ -836,7 +840,7 @@ static cudaError_t launch_crt_fold(const CrtTable& tab, cudaStream_t st, const O
         (e = cudaFuncSetAttribute(ozaki_crt_fold_kernel<12>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx)) !=
             cudaSuccess)
       return e;
-    attr_set[dev] = true;
+    attr_set[dev].store(true, std::memory_order_release);
   }
   if (tab.nw <= 8)
     ozaki_crt_fold_kernel<8><<<grid, blk, dyn, st>>>(F, tab);
@@ -848,7 +852,7 @@ static cudaError_t launch_crt_fold(const CrtTable& tab, cudaStream_t st, const O
 }
 
 cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scratch, cudaStream_t st,
-                              const OzakiOverlap* ov, int scheme) {
+                              const OzakiOverlap* ov, int scheme, int* report) {
   if (g.m <= 0 || g.n <= 0 || g.k <= 0) return cudaSuccess;
   if ((bits < 7 || bits > 9) || digits < 2 || digits > ozaki_max_digits_for_k(bits, g.k))
     return cudaErrorInvalidValue;
@@ -939,14 +943,14 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scr
   if (!make_map(&tmA, DA, (int64_t)(L.G + 1) * L.m_pad, L.k_pad, kBM, crt || L.b == 9) ||
       !make_map(&tmB, DB, (int64_t)(L.G + 1) * L.n_pad, L.k_pad, kBN, crt || L.b == 9))
     return cudaErrorInvalidValue;
-  static bool attr_set[64] = {false};
+  static std::atomic<bool> attr_set[64];
   int dev = 0;
   cudaGetDevice(&dev);
-  if (dev >= 0 && dev < 64 && !attr_set[dev]) {
+  if (dev >= 0 && dev < 64 && !attr_set[dev].load(std::memory_order_acquire)) {
     if ((e = cudaFuncSetAttribute(ozaki_mma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)kMmaSmem)) != cudaSuccess)
       return e;
-    attr_set[dev] = true;
+    attr_set[dev].store(true, std::memory_order_release);
   }
   const int tiles_m = (int)(L.m_pad / kBM), tiles_n = (int)(L.n_pad / kBN);
   const int tiles = tiles_m * tiles_n;
@@ -969,6 +973,7 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scr
   F2.Cout = g.C; F2.sci = g.sci; F2.scj = g.scj;
   F2.alpha = g.alpha; F2.beta = g.beta;
   F2.err = err;
+  F2.report = report;
   if ((g.m + 7) / 8 > 65535) return cudaErrorInvalidConfiguration;
   const bool fold_banded = ov && ov->band_done && g.scj == 1 && g.sci >= g.n && g.m >= 64;
   bool c_waited = false;

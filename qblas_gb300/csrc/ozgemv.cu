@@ -63,6 +63,8 @@
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include "exact.cuh"
 #include "gemv_rows.cuh"
 #include "kernels.h"
@@ -691,8 +693,12 @@ cudaError_t launch_gemv_ozaki(int64_t m, int64_t n, q128 alpha, MatView A, const
   og_x_split_kernel<<<(unsigned)Lo.nchunks, 32, 0, s>>>(n, Lo.nchunks, x, incx, const_cast<uint8_t*>(P.xdig),
                                                         const_cast<int32_t*>(P.xexp), list);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  static bool attr = false;
-  if (!attr) {
+  // the attribute is per device (and per host thread race-free)
+  static std::atomic<bool> attr_set[64];
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  if (!attr_set[dev].load(std::memory_order_acquire)) {
     if ((e = cudaFuncSetAttribute(og_gemv_kernel<kOgRowMajor>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)kOgSmem)) != cudaSuccess ||
         (e = cudaFuncSetAttribute(og_gemv_kernel<kOgColGroups>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -700,7 +706,7 @@ cudaError_t launch_gemv_ozaki(int64_t m, int64_t n, q128 alpha, MatView A, const
         (e = cudaFuncSetAttribute(og_gemv_kernel<kOgColBoxes>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)kOgSmem)) != cudaSuccess)
       return e;
-    attr = true;
+    attr_set[dev].store(true, std::memory_order_release);
   }
   if (layout == kOgRowMajor)
     og_gemv_kernel<kOgRowMajor><<<(unsigned)Lo.G, kOgThreads, kOgSmem, s>>>(map, P);

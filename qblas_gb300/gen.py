@@ -115,3 +115,58 @@ def uniform_full_device(torch, n: int, seed: int, chunk: int = 1 << 26):
         out[s:e, 0] = torch.where(zero, torch.zeros_like(lo), lo)
         out[s:e, 1] = torch.where(zero, sign << 63, hi)
     return out
+
+
+def config4_shapes(rng: np.random.Generator, count: int = 10000):
+    """Shapes of the batched workload: `count` qgemm problems with m, n, k
+    log-uniform in [8, 256], `count` qgemv problems with m, n log-uniform in
+    [16, 2048] and `count` qdot problems with n log-uniform in [64, 65536].
+    Returns (gemm (count, 3) [m, n, k], gemv (count, 2) [m, n], dot (count,))."""
+    gm = log_uniform_int(rng, 8, 256, 3 * count).reshape(3, count).T.copy()
+    gv = log_uniform_int(rng, 16, 2048, 2 * count).reshape(2, count).T.copy()
+    dn = log_uniform_int(rng, 64, 65536, count)
+    return gm, gv, dn
+
+
+def config4_batch(torch, seed: int):
+    """The batched workload on the current CUDA device: config4_shapes(seed)
+    with full-mantissa uniform values, row-major 'N', alpha = 1, beta = 0.
+    Returns (problems, inputs, outputs, layout): `problems` a PROBLEM_DTYPE
+    array for quadblas_batch_plan; A and B of every problem in the device
+    tensor `inputs`, C in `outputs` (both (count, 2) int64, uniform_full
+    values); layout[i] = (op, m, n, k, offset of A, of B, of C, length of C)
+    in elements."""
+    from .api import PROBLEM_DTYPE
+    from .quad import scalar
+    gm, gv, dn = config4_shapes(rng_for(seed))
+    lay = []
+    oi = oo = 0
+    for m, n, k in gm:
+        lay.append((0, int(m), int(n), int(k), oi, oi + m * k, oo, int(m * n)))
+        oi += m * k + k * n
+        oo += m * n
+    for m, n in gv:
+        lay.append((1, int(m), int(n), 0, oi, oi + m * n, oo, int(m)))
+        oi += m * n + n
+        oo += m
+    for n in dn:
+        lay.append((2, 0, int(n), 0, oi, oi + n, oo, 1))
+        oi += 2 * n
+        oo += 1
+    inp = uniform_full_device(torch, int(oi), seed=seed + 1)
+    out = uniform_full_device(torch, int(oo), seed=seed + 2)
+    bi, bo = inp.data_ptr(), out.data_ptr()
+    probs = np.zeros(len(lay), dtype=PROBLEM_DTYPE)
+    one, zero = scalar(1.0)[0], scalar(0.0)[0]
+    for p, (op, m, n, k, a, b, c, _) in zip(probs, lay):
+        p["op"], p["layout"], p["transa"], p["transb"] = op, b"R", b"N", b"N"
+        p["m"], p["n"], p["k"] = m, n, k
+        p["alpha"], p["beta"] = one, zero
+        p["A"], p["B"], p["C"] = bi + 16 * int(a), bi + 16 * int(b), bo + 16 * int(c)
+        if op == 0:
+            p["lda"], p["ldb"], p["ldc"] = k, n, n
+        elif op == 1:
+            p["lda"], p["ldb"], p["ldc"] = n, 1, 1
+        else:
+            p["lda"], p["ldb"], p["ldc"] = 1, 1, 1
+    return probs, inp, out, lay

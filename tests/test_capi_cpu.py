@@ -48,6 +48,7 @@ def test_utilities(qlib):
     assert qlib.quadblas_set_ozaki_slices(12) == 0 and qlib.quadblas_get_ozaki_slices() == 12
     qlib.quadblas_set_ozaki_slices(0)
     assert qlib.quadblas_error_string(6) == b"device pointer not 16-byte aligned"
+    assert qlib.quadblas_error_string(7).startswith(b"a device-side wait timed out")
 
 
 def test_argument_validation_on_host(qlib):
@@ -85,6 +86,9 @@ def test_no_cpu_fallback_without_gpu(qlib):
     assert rc in (2, 5)  # CUDA error / no device: the call fails instead of computing on the CPU
     assert qlib.quadblas_qdot(10, P(x), 1, P(x), 1) == 0.0
     assert qlib.quadblas_last_error() in (2, 5)
+    assert qlib.quadblas_device_status(1) in (2, 5)
+    # the serial batch runner fails the same way (and checks its arguments first)
+    assert qlib.quadblas_batch_run_serial(None, -1, None) == 1
 
 
 def test_cpp_header_compiles(tmp_path):

@@ -8,9 +8,14 @@ Checked through the C ABI against quadblas_qdot_dev on two calls in a row,
 with the tolerance of the other qdot tests: bit-identical results (both are
 the correctly rounded exact sum).  The first call is large (it uses every
 block's partial); the second is small, so stale partials left by the first
-call would show if they were read.  This file is collected last so that a
-run stopping at the first failure has already run every other test; it
-also passes on its own in a fresh process.
+call would show if they were read.  A second test runs two dots of
+condition 1e40 back to back — sums the wide accumulator cannot round alone,
+so each arms the exact (Kulisch) pass whose digits live in the static array
+— and then a well-conditioned dot: digits left by one exact pass must not
+leak into the next, and a certified call must not read a stale exact-pass
+flag.  This file is collected last so that a run stopping at the first
+failure has already run every other test; it also passes on its own in a
+fresh process.
 """
 import ctypes
 
@@ -47,6 +52,22 @@ def test_noalloc_qdot_matches_qdot_dev_twice(qlib, O, torch_cuda):
         assert Q.same_bits(got, ref).all(), (n, got, ref)
         R, _, _ = O.exact_dot(x, y, n, incx, incy)
         assert Q.same_bits(got, R).all()
+
+
+def test_noalloc_exact_pass_twice_then_certified(qlib, O, torch_cuda):
+    torch = torch_cuda
+    rng = G.rng_for(4343)
+    cases = [O.gendot(8192, 1e40, 11), O.gendot(8192, 1e40, 12), G.cancelling_dot(rng, 100003)]
+    for i, (x, y) in enumerate(cases):
+        n = len(x)
+        dx, dy = to_dev(torch, x), to_dev(torch, y)
+        got = _dot(qlib.quadblas_qdot_dev_noalloc, torch, n, dx, dy)
+        ref = _dot(qlib.quadblas_qdot_dev, torch, n, dx, dy)
+        R, _, _ = O.exact_dot(x, y)
+        assert Q.same_bits(got, ref).all(), (i, got, ref)
+        assert Q.same_bits(got, R).all(), (i, got, R)
+    # the two ill-conditioned sums differ, so a stale result would show
+    assert not Q.same_bits(O.exact_dot(*cases[0])[0], O.exact_dot(*cases[1])[0]).all()
 
 
 def test_noalloc_rejects_bad_arguments(qlib, torch_cuda):
