@@ -582,13 +582,15 @@ int host_gemm(char layout, char transa, char transb, int64_t m, int64_t n, int64
     if (method != 2) return qb::kOk;
     const size_t off = qb::ozaki_error_flag_offset(p.g.m, p.g.n, p.g.k, gemm_digits(p.g.k), gemm_digit_bits(),
                                                    g_ozaki_scheme.load());
-    *static_cast<volatile int*>(st.err_host) = 0;
-    return cuda_status(cudaMemcpyAsync(st.err_host, static_cast<char*>(st.buf[kSlotScratch]) + off, sizeof(int),
-                                       cudaMemcpyDeviceToHost, st.stream));
+    volatile int* h = st.err_host;
+    h[0] = h[1] = h[2] = 0;
+    return cuda_status(cudaMemcpyAsync(st.err_host, static_cast<char*>(st.buf[kSlotScratch]) + off,
+                                       3 * sizeof(int), cudaMemcpyDeviceToHost, st.stream));
   };
   auto check_timeout = [&](int status) -> int {
     if (status || method != 2) return status;
-    return *static_cast<volatile int*>(st.err_host) ? qb::kErrTimeout : qb::kOk;
+    volatile int* h = st.err_host;
+    return (h[0] | h[1] | h[2]) ? qb::kErrTimeout : qb::kOk;
   };
   if (method == 2) {
     // Ozaki, with the host link kept busy in the order the GPU needs the

@@ -134,56 +134,152 @@ __global__ void __launch_bounds__(256)
   ozaki_digits_emit2<B>(v0, v1, Sr, s, [&](int t, int d0, int d1) { out[t * plane2] = pack_digits<B>(d0, d1); });
 }
 
-// Residues for the CRT scheme (ozcrt.cuh), same view, padding and thread
-// mapping as ozaki_split_kernel: residue q of element (r, c) goes to
-// D[q * plane + r * cols_pad + c] as fp16.  A thread computes the scaled
-// integers of its two elements once and their 18-bit pieces (NP of them,
-// T <= 18 NP), then per modulus x = sum_j h_j (2^(18 j) mod p) < 2^31,
-// one remainder by a magic multiplier and the balanced residue r, |r| <= 256.
-// The fp16 value: the bits 0x6600 + r are 1536 + r (exponent 2^10, mantissa
-// 512 + r in [256, 768]), and one fused multiply-add of the pair,
-// (1536 + r) * sign - 1536 * sign, is sign * r exactly.
-template <int NP>
-__global__ void __launch_bounds__(256)
-    ozaki_crt_split_kernel(int64_t rows, int64_t cols, int64_t rows_pad, int64_t cols_pad, int64_t plane,
-                           const q128* __restrict__ p, int64_t sr, int64_t sc, const int* __restrict__ S,
-                           const __grid_constant__ CrtTable tab, uint16_t* __restrict__ D) {
-  __shared__ __align__(16) CrtMod mods[kCrtMaxMods];
-  const int tid = threadIdx.y * 32 + threadIdx.x;
-  const int nvec = tab.n * (int)(sizeof(CrtMod) / 16);
-  for (int i = tid; i < nvec; i += 256)
-    reinterpret_cast<uint4*>(mods)[i] = reinterpret_cast<const uint4*>(tab.mod)[i];
+// Residues for the CRT scheme on the tensor cores (ozcrt.cuh, "Residue split
+// on the tensor cores"): residue q of element (r, c) of the same view goes to
+// D[q * plane + r * cols_pad + c] as fp16, rows in [rows, rows_pad) and
+// columns in [cols, cols_pad) as zeros.  Persistent CTAs of 4 warps walk
+// tiles of 4 rows x 64 columns: warp w takes row 4t + w, lane l its columns
+// 2l, 2l + 1 (one tensor-memory lane, two elements).  Per tile each thread
+// writes its elements' operand row (64 fp16: s (1024 + b_j), -s, zeros) to
+// tensor memory, one thread issues four MMAs (M = 128, K = 16, N = 2 NP)
+// against the table in shared memory, and each thread reads back x_q of its
+// two elements, rounds r = x - p round(x / p) in fp32 (exact, |r| <= 256)
+// and stores the two residues of modulus q as one 32-bit word.  The next
+// tile's elements are loaded while the MMA runs.  The wait for the MMA is
+// bounded (1 s); on a timeout the CTA stops, records it in *err and frees
+// its tensor memory.
+struct CrtSplitParams {
+  int64_t rows, cols, rows_pad, cols_pad, plane;
+  const q128* p;
+  int64_t sr, sc;
+  const int* S;
+  int* err;
+  uint16_t* D;
+};
+
+constexpr int kSplitThreads = 128;
+constexpr int kSplitTmemCols = 128;        // D: columns [0, N), N <= 96; A: [96, 128)
+constexpr int kSplitAcol = 96;
+constexpr size_t kSplitSmem = 48 * 1024;   // table + barrier; also holds residency to 4 CTAs per SM
+
+template <int NB>
+__device__ __forceinline__ void crt_operand_row(q128 v, int Sr, int T, uint32_t* a) {
+  uint64_t v0, v1, v2;
+  bool neg;
+  ozaki_scaled_bits(v, Sr, T, v0, v1, v2, neg);
+  const uint32_t w[6] = {(uint32_t)v0, (uint32_t)(v0 >> 32), (uint32_t)v1, (uint32_t)(v1 >> 32), (uint32_t)v2,
+                         (uint32_t)(v2 >> 32)};
+  const uint32_t sgn = neg ? 0xE4E4E4E4u : 0x64646464u;
+#pragma unroll
+  for (int i = 0; i < NB / 2; ++i)  // bytes 2i, 2i+1 as fp16 s (1024 + b)
+    a[i] = __byte_perm(w[i >> 1], sgn, (i & 1) ? 0x4342u : 0x4140u);
+  a[NB / 2] = neg ? 0x3C00u : 0xBC00u;  // -s, then zeros
+#pragma unroll
+  for (int i = NB / 2 + 1; i < 16; ++i) a[i] = 0u;
+}
+
+template <int NB>
+__global__ void __launch_bounds__(kSplitThreads)
+    ozaki_crt_split_tc_kernel(const __grid_constant__ CrtSplitParams P, const __grid_constant__ CrtSplitTable tab) {
+  extern __shared__ __align__(128) uint8_t split_smem[];
+  uint8_t* sbase = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(split_smem) + 127) & ~(uintptr_t)127);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(sbase + kCrtSplitK * kCrtSplitMaxN * 2);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar + 1);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int N = tab.N, nmod = tab.nmod;
+  // the table (B operand) into shared memory, visible to the tensor cores
+  for (int i = threadIdx.x; i < N * kCrtSplitK / 8; i += kSplitThreads)
+    reinterpret_cast<uint4*>(sbase)[i] = reinterpret_cast<const uint4*>(tab.b)[i];
+  fence_proxy_async_smem();
+  if (threadIdx.x == 0) {
+    mbar_init(smem_u32(bar), 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(kSplitTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
-  const int64_t c = ((int64_t)blockIdx.x * 32 + threadIdx.x) * 2;
-  const int64_t r = (int64_t)blockIdx.y * 8 + threadIdx.y;
-  if (c >= cols_pad || r >= rows_pad) return;
-  uint32_t* out = reinterpret_cast<uint32_t*>(D + r * cols_pad + c);
-  const int64_t plane2 = plane / 2;
-  q128 v0 = q_zero(0), v1 = q_zero(0);
-  int Sr = kOzakiScaleEmpty;
-  if (r < rows) {
-    Sr = S[r];
-    if (c < cols) v0 = ld_cached(p + r * sr + c * sc);
-    if (c + 1 < cols) v1 = ld_cached(p + r * sr + (c + 1) * sc);
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+  const uint32_t tlane = tmem + ((uint32_t)(warp * 32) << 16);
+  const uint32_t idesc = (1u << 4) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+  const uint32_t sb = smem_u32(sbase), lbo = (uint32_t)N * 16u;
+
+  const int64_t tiles_c = P.cols_pad / 64, ntiles = (P.rows_pad / 4) * tiles_c;
+  auto load = [&](int64_t t, q128& v0, q128& v1, int& Sr) {
+    v0 = v1 = q_zero(0);
+    Sr = kOzakiScaleEmpty;
+    if (t >= ntiles) return;
+    const int64_t r = (t / tiles_c) * 4 + warp, c = (t % tiles_c) * 64 + 2 * lane;
+    if (r < P.rows) {
+      Sr = P.S[r];
+      if (c < P.cols) v0 = ld_cached(P.p + r * P.sr + c * P.sc);
+      if (c + 1 < P.cols) v1 = ld_cached(P.p + r * P.sr + (c + 1) * P.sc);
+    }
+  };
+  q128 v0, v1;
+  int Sr;
+  int64_t t = blockIdx.x;
+  load(t, v0, v1, Sr);
+  uint32_t phase = 0;
+  bool ok = true;
+  for (; t < ntiles; t += gridDim.x) {
+    {
+      uint32_t a[32];
+      crt_operand_row<NB>(v0, Sr, tab.T, a);
+      crt_operand_row<NB>(v1, Sr, tab.T, a + 16);
+      tmem_st32(tlane + kSplitAcol, a);
+    }
+    tmem_st_wait();
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();  // every operand row written; every thread done with the last tile's x
+    if (threadIdx.x == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+      for (int kt = 0; kt < 4; ++kt)
+        mma_f16kind_ta(tmem, tmem + kSplitAcol + 8 * kt, smem_desc_noswizzle(sb + 2 * kt * lbo, lbo, 128), idesc,
+                       kt ? 1u : 0u);
+      mma_commit(smem_u32(bar));
+    }
+    const int64_t r = (t / tiles_c) * 4 + warp, c = (t % tiles_c) * 64 + 2 * lane;
+    load(t + gridDim.x, v0, v1, Sr);  // in flight while the MMAs run
+    ok = mbar_wait(smem_u32(bar), phase);
+    phase ^= 1u;
+    if (!__syncthreads_and(ok)) {
+      ok = false;
+      break;
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    uint32_t* out = reinterpret_cast<uint32_t*>(P.D + r * P.cols_pad + c);
+    const int64_t plane2 = P.plane / 2;
+    for (int g = 0; g < N / 16; ++g) {
+      uint32_t x[16];
+      tmem_ld16(tlane + 16 * g, x);
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        const int q = 8 * g + i;
+        if (q < nmod) {
+          const float p = tab.p[q], ip = tab.inv_p[q];
+          const float x0 = __uint_as_float(x[2 * i]), x1 = __uint_as_float(x[2 * i + 1]);
+          const float q0 = __fadd_rn(__fmaf_rn(x0, ip, 12582912.0f), -12582912.0f);
+          const float q1 = __fadd_rn(__fmaf_rn(x1, ip, 12582912.0f), -12582912.0f);
+          const __half2 h = __floats2half2_rn(__fmaf_rn(-q0, p, x0), __fmaf_rn(-q1, p, x1));
+          out[q * plane2] = *reinterpret_cast<const uint32_t*>(&h);
+        }
+      }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   }
-  uint64_t a0, a1, a2, b0, b1, b2;
-  bool na, nb;
-  ozaki_scaled_bits(v0, Sr, tab.T, a0, a1, a2, na);
-  ozaki_scaled_bits(v1, Sr, tab.T, b0, b1, b2, nb);
-  uint32_t ha[NP], hb[NP];
-  crt_pieces<NP>(a0, a1, a2, ha);
-  crt_pieces<NP>(b0, b1, b2, hb);
-  const uint32_t sg = (na ? 0xBC00u : 0x3C00u) | ((nb ? 0xBC00u : 0x3C00u) << 16);
-  const uint32_t bs = (na ? 0x6600u : 0xE600u) | ((nb ? 0x6600u : 0xE600u) << 16);
-  const __half2 hsg = *reinterpret_cast<const __half2*>(&sg), hbs = *reinterpret_cast<const __half2*>(&bs);
-#pragma unroll 2
-  for (int q = 0; q < tab.n; ++q) {
-    const CrtMod& m = mods[q];
-    // (0x6600 + ra) | (0x6600 + rb) << 16 from the shifted residues
-    const uint32_t bits = crt_residue_shifted<NP>(ha, m) + (crt_residue_shifted<NP>(hb, m) << 16) + m.bias2;
-    const __half2 v = __hfma2(*reinterpret_cast<const __half2*>(&bits), hsg, hbs);
-    out[q * plane2] = *reinterpret_cast<const uint32_t*>(&v);
-  }
+  if (!ok && threadIdx.x == 0) atomicExch(P.err, 1);
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kSplitTmemCols)
+                 : "memory");
 }
 
 // ---------------------------------------------------------------------------
@@ -526,7 +622,7 @@ __global__ void __launch_bounds__(256, 3) ozaki_fold_kernel(OzakiFoldParams P) {
     fold_step_t<B>(f[2], t2);
     fold_step_t<B>(f[3], t3);
   }
-  const bool failed = *P.err != 0;
+  const bool failed = (P.err[0] | P.err[1] | P.err[2]) != 0;
   if (failed && P.report && i == 0 && j0 == 0) *reinterpret_cast<volatile int*>(P.report) = 1;
   const int Si = P.S[i];
   const uint32_t fai = P.fa[i];
@@ -611,7 +707,7 @@ __global__ void __launch_bounds__(256) ozaki_crt_fold_kernel(OzakiFoldParams P, 
     crt_acc_pair(A0, c0 & 0xFFFFu, c1 & 0xFFFFu, p0, p1, P0, P1, W);
     crt_acc_pair(A1, c0 >> 16, c1 >> 16, p0, p1, P0, P1, W);
   }
-  const bool failed = *P.err != 0;
+  const bool failed = (P.err[0] | P.err[1] | P.err[2]) != 0;
   if (failed && P.report && i == 0 && j0 == 0) *reinterpret_cast<volatile int*>(P.report) = 1;
   const int Si = P.S[i];
   const uint32_t fai = P.fa[i];
@@ -814,14 +910,32 @@ static void launch_fold(int b, cudaStream_t st, const OzakiFoldParams& F) {
     ozaki_fold_kernel<9><<<grid, blk, 0, st>>>(F);
 }
 
-// CRT residues: 8 pieces of 18 bits cover T <= 144, 11 cover T <= 191.
-static void launch_crt_split(const CrtTable& tab, dim3 grid, dim3 blk, cudaStream_t st, int64_t rows,
-                             int64_t cols, int64_t rows_pad, int64_t cols_pad, int64_t plane, const q128* p,
-                             int64_t sr, int64_t sc, const int* S, uint16_t* D) {
-  if (tab.T <= 144)
-    ozaki_crt_split_kernel<8><<<grid, blk, 0, st>>>(rows, cols, rows_pad, cols_pad, plane, p, sr, sc, S, tab, D);
+// CRT residues on the tensor cores: 18 bytes of V cover T <= 144, 24 cover
+// T <= 191.  Persistent: four CTAs per SM (their tensor memory is 128
+// columns each; the dynamic shared memory keeps a fifth off the SM).
+static cudaError_t launch_crt_split(const CrtSplitTable& stab, cudaStream_t st, int64_t rows, int64_t cols,
+                                    int64_t rows_pad, int64_t cols_pad, int64_t plane, const q128* p, int64_t sr,
+                                    int64_t sc, const int* S, uint16_t* D, int* err) {
+  CrtSplitParams P;
+  P.rows = rows;
+  P.cols = cols;
+  P.rows_pad = rows_pad;
+  P.cols_pad = cols_pad;
+  P.plane = plane;
+  P.p = p;
+  P.sr = sr;
+  P.sc = sc;
+  P.S = S;
+  P.err = err;
+  P.D = D;
+  const int64_t ntiles = (rows_pad / 4) * (cols_pad / 64);
+  if (ntiles <= 0) return cudaSuccess;
+  const unsigned grid = (unsigned)std::min<int64_t>(ntiles, 4 * (int64_t)device_sm_count());
+  if (stab.NB == 18)
+    ozaki_crt_split_tc_kernel<18><<<grid, kSplitThreads, kSplitSmem, st>>>(P, stab);
   else
-    ozaki_crt_split_kernel<11><<<grid, blk, 0, st>>>(rows, cols, rows_pad, cols_pad, plane, p, sr, sc, S, tab, D);
+    ozaki_crt_split_tc_kernel<24><<<grid, kSplitThreads, kSplitSmem, st>>>(P, stab);
+  return cudaGetLastError();
 }
 
 static cudaError_t launch_crt_fold(const CrtTable& tab, cudaStream_t st, const OzakiFoldParams& F) {
@@ -858,6 +972,8 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scr
     return cudaErrorInvalidValue;
   CrtTable tab;
   const bool crt = ozaki_crt_table(scheme, digits, bits, g.k, tab);
+  CrtSplitTable stab;
+  if (crt) crt_split_table(tab, stab);
   OzakiLayout L = ozaki_layout(g.m, g.n, g.k, digits, bits, crt ? tab.n : 0);
   char* base = static_cast<char*>(scratch);
   int* S = reinterpret_cast<int*>(base + L.off_S);
@@ -893,7 +1009,10 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scr
   cudaStream_t sa = banded ? ov->a_stream : st;  // op(A): scales and digits, band by band
   ozaki_fill_kernel<<<(unsigned)((g.m + 255) / 256), 256, 0, sa>>>(g.m, S, fa);
   ozaki_fill_kernel<<<(unsigned)((g.n + 255) / 256), 256, 0, sb>>>(g.n, F, fb);
+  // error words: [0] tensor-core products (main stream), [1] op(B)'s residue
+  // split, [2] op(A)'s; each is reset on the stream of its writer
   if ((e = cudaMemsetAsync(err, 0, 4, st)) != cudaSuccess) return e;
+  if ((e = cudaMemsetAsync(err + 1, 0, 4, sb)) != cudaSuccess) return e;
   const dim3 blk(32, 8);
   const int64_t plane_a = L.m_pad * L.k_pad, plane_b = L.n_pad * L.k_pad;
   {
@@ -902,10 +1021,10 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scr
     ozaki_scale_kernel<<<bb, 256, 0, sb>>>(g.n, g.k, g.B, g.sbj, g.sbl, F, fb);
     dim3 gb((unsigned)(L.k_pad / 64), (unsigned)(L.n_pad / 8));
     if (crt)
-      launch_crt_split(tab, gb, blk, sb, g.n, g.k, L.n_pad, L.k_pad, plane_b, g.B, g.sbj, g.sbl, F, DB);
+      e = launch_crt_split(stab, sb, g.n, g.k, L.n_pad, L.k_pad, plane_b, g.B, g.sbj, g.sbl, F, DB, err + 1);
     else
       launch_split(L.b, gb, blk, sb, g.n, g.k, L.n_pad, L.k_pad, plane_b, g.B, g.sbj, g.sbl, F, L.s, DB);
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if (e != cudaSuccess || (e = cudaGetLastError()) != cudaSuccess) return e;
     if (ov) {
       if ((e = cudaEventRecord(ov->b_done, sb)) != cudaSuccess) return e;
       if ((e = cudaStreamWaitEvent(st, ov->b_done, 0)) != cudaSuccess) return e;
@@ -917,18 +1036,20 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scr
     const int64_t rows = std::min(r1, g.m) - r0;
     cudaError_t ee;
     if (banded && ov->a_rows(ov->a_ctx, r0, r0 + rows, sa) != 0) return cudaErrorUnknown;
+    if (r0 == 0 && (ee = cudaMemsetAsync(err + 2, 0, 4, sa)) != cudaSuccess) return ee;
     int64_t wa = rows * ((g.k + 63) / 64);
     unsigned ba = (unsigned)std::max<int64_t>(1, std::min<int64_t>((wa + 255) / 256, (int64_t)sms * 8));
     if (rows > 0) ozaki_scale_kernel<<<ba, 256, 0, sa>>>(rows, g.k, g.A + r0 * g.sai, g.sai, g.sal, S + r0, fa + r0);
     dim3 ga((unsigned)(L.k_pad / 64), (unsigned)((r1 - r0) / 8));
     const q128* Ab = g.A + r0 * g.sai;
+    ee = cudaSuccess;
     if (crt)
-      launch_crt_split(tab, ga, blk, sa, rows, g.k, r1 - r0, L.k_pad, plane_a, Ab, g.sai, g.sal, S + r0,
-                       DA + r0 * L.k_pad);
+      ee = launch_crt_split(stab, sa, rows, g.k, r1 - r0, L.k_pad, plane_a, Ab, g.sai, g.sal, S + r0,
+                            DA + r0 * L.k_pad, err + 2);
     else
       launch_split(L.b, ga, blk, sa, rows, g.k, r1 - r0, L.k_pad, plane_a, Ab, g.sai, g.sal, S + r0, L.s,
                    DA + r0 * L.k_pad);
-    if ((ee = cudaGetLastError()) != cudaSuccess) return ee;
+    if (ee != cudaSuccess || (ee = cudaGetLastError()) != cudaSuccess) return ee;
     if (banded) {
       if ((ee = cudaEventRecord(ov->a_done, sa)) != cudaSuccess) return ee;
       if ((ee = cudaStreamWaitEvent(st, ov->a_done, 0)) != cudaSuccess) return ee;

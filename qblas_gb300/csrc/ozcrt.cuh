@@ -179,6 +179,89 @@ inline bool crt_build(int T, int64_t k, CrtTable& tab) {
 }
 
 // ---------------------------------------------------------------------------
+// Residue split on the tensor cores: the table (host)
+// ---------------------------------------------------------------------------
+// For the split kernel, an element's scaled integer V (NB bytes b_j, V =
+// sum_j b_j 256^j, NB = 18 for T <= 144 and 24 for T <= 191) becomes one row
+// of an MMA operand A: the fp16 values s (1024 + b_j) (one byte select each:
+// the bits 0x64 | sign above the byte), then -s, then zeros (32 per
+// element; s = +-1 the sign of the element).  B holds, per modulus q, the
+// balanced c_jq = 256^j mod p_q and beta_q = (1024 sum_j c_jq) mod p_q, both
+// of magnitude at most 256, so that
+//   x_q = s sum_j (1024 + b_j) c_jq - s beta_q == s V  (mod p_q),
+//   |x_q| <= NB * 1279 * 256 + 256 < 2^23,
+// an integer the fp32 accumulation holds exactly.  The balanced residue is
+// then r = x - p * round(x / p) in fp32: the error of x * fl(1/p) is below
+// |x| 2^-33 < 9.2e-4, less than the distance 1 / (2p) >= 9.78e-4 of x / p
+// from a half-integer for odd p, so round() picks the nearest integer and
+// |r| <= floor(p / 2) (for p = 512 a tie gives +-256).  Two elements share
+// an operand row (K = 32 each) with block-diagonal B (N = 2 NP columns,
+// element e of modulus q in column 2q + e, NP = nmod rounded up to 8).
+constexpr int kCrtSplitK = 64;                   // K: 32 per element, two elements
+constexpr int kCrtSplitMaxN = 2 * kCrtMaxMods;   // 96
+
+struct alignas(16) CrtSplitTable {
+  int nmod, N, NB, T;
+  float p[kCrtMaxMods];
+  float inv_p[kCrtMaxMods];
+  // B in the shared-memory layout of a K-major operand without swizzle: the
+  // 16 bytes of (row n, k-block kb) at kb * (N * 16) + n * 16
+  uint16_t b[kCrtSplitK * kCrtSplitMaxN];
+};
+
+// fp16 bits of an integer |v| <= 2048 (exact)
+inline uint16_t crt_half_bits(int v) {
+  if (v == 0) return 0;
+  const uint16_t sign = v < 0 ? 0x8000u : 0u;
+  uint32_t a = (uint32_t)(v < 0 ? -v : v);
+  int e = 0;
+  while ((a >> e) > 1) ++e;  // a in [2^e, 2^(e+1))
+  const uint32_t frac = (a << (10 - e)) & 0x3FFu;
+  return (uint16_t)(sign | ((uint32_t)(e + 15) << 10) | frac);
+}
+
+inline int crt_balanced(int64_t v, uint32_t p) {
+  int64_t r = v % (int64_t)p;
+  if (r < 0) r += p;
+  if (r > (int64_t)(p / 2)) r -= p;
+  return (int)r;
+}
+
+inline void crt_split_table(const CrtTable& tab, CrtSplitTable& st) {
+  st = CrtSplitTable();
+  st.nmod = tab.n;
+  st.T = tab.T;
+  st.NB = tab.T <= 144 ? 18 : 24;
+  const int NP = (tab.n + 7) / 8 * 8;
+  st.N = 2 * NP;
+  for (int q = 0; q < tab.n; ++q) {
+    const uint32_t p = tab.mod[q].p;
+    st.p[q] = (float)p;
+    st.inv_p[q] = (float)(1.0 / (double)p);
+  }
+  for (int n = 0; n < st.N; ++n) {
+    const int q = n / 2, e = n % 2;
+    int64_t csum = 0;
+    int c[32] = {0};
+    if (q < tab.n) {
+      const uint32_t p = tab.mod[q].p;
+      int64_t pw = 1 % p;
+      for (int j = 0; j < st.NB; ++j) {
+        c[j] = crt_balanced(pw, p);
+        csum += c[j];
+        pw = pw * 256 % p;
+      }
+      c[st.NB] = crt_balanced(1024 * csum, p);
+    }
+    for (int k = 0; k < kCrtSplitK; ++k) {
+      const int ek = k / 32, j = k % 32;
+      const int v = (q < tab.n && ek == e && j <= st.NB) ? c[j] : 0;
+      st.b[(k / 8) * (st.N * 8) + n * 8 + (k % 8)] = crt_half_bits(v);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Residues and reconstruction (host and device)
 // ---------------------------------------------------------------------------
 // x mod p for x < 2^31: with magic = ceil(2^40 / p) = (2^40 + e) / p,

@@ -1,6 +1,7 @@
 // Test harness: the device soft-float core (qblas_gb300/csrc/softquad.cuh)
 // compiled as plain host C++, so its bit patterns can be compared with the
 // host binary128 library on a machine without a GPU.
+#include <string.h>
 #include <stdint.h>
 
 #include "../qblas_gb300/csrc/softquad.cuh"
@@ -275,6 +276,25 @@ int sq_crt_residues(int64_t n, const q128* a, const int* S, int T, int64_t k, in
     qb::ozaki_scaled_bits(a[i], S[i], T, V[4 * i], V[4 * i + 1], V[4 * i + 2], neg);
     V[4 * i + 3] = neg;
   }
+  return t.n;
+}
+
+// The tensor-core residue split's table for T-bit operands and inner
+// dimension k: header {nmod, N, NB, T}, p and 1/p as fp32 bit patterns
+// (kCrtMaxMods each), and the B operand (kCrtSplitK x kCrtSplitMaxN fp16
+// bit patterns in the shared-memory layout).  Returns the number of moduli.
+int sq_crt_split_table(int T, int64_t k, int32_t* head4, uint32_t* p_bits, uint32_t* inv_bits, uint16_t* b) {
+  qb::CrtTable t;
+  if (!qb::crt_build(T, k, t)) return 0;
+  qb::CrtSplitTable st;
+  qb::crt_split_table(t, st);
+  head4[0] = st.nmod;
+  head4[1] = st.N;
+  head4[2] = st.NB;
+  head4[3] = st.T;
+  memcpy(p_bits, st.p, sizeof(st.p));
+  memcpy(inv_bits, st.inv_p, sizeof(st.inv_p));
+  memcpy(b, st.b, sizeof(st.b));
   return t.n;
 }
 

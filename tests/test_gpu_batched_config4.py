@@ -6,7 +6,10 @@ log-uniform in [64, 65536]), row-major 'N', alpha = 1, beta = 0, with
 full-mantissa uniform values: the shapes and item sizes (split-k tiles,
 column-split rows, chunked dots) that the benchmark runs, not a reduced
 case.  The batch goes through the autotuned plan, recorded in a CUDA graph
-and replayed.
+and replayed.  At the autotuned granularity no item of this workload is
+split, so the batch is also planned at granularity 2^14, where qgemm tiles
+split along k, long qgemv rows along the columns and long dots into chunks,
+and that execution must give the same bits.
 
 Every output must be bit-identical to the same problem run by its own
 device-pointer call (quadblas_batch_run_serial): both claim the correctly
@@ -41,7 +44,7 @@ def test_config4_batched_equals_one_by_one_and_oracle(qlib, O, torch_cuda, tmp_p
         grain = api.batch_autotune()
         plan = api.BatchPlan(probs)
         info = plan.info()
-        assert info["grain"] == grain and info["split_groups"] > 0
+        assert info["grain"] == grain
         st = torch.cuda.Stream()
         st.wait_stream(torch.cuda.current_stream())
         with torch.cuda.stream(st):
@@ -68,8 +71,18 @@ def test_config4_batched_equals_one_by_one_and_oracle(qlib, O, torch_cuda, tmp_p
             pytest.fail(f"{diff.size} outputs differ, in {len(bad)} problems, first {[lay[i][:4] for i in bad[:5]]}")
         plan.close()
         del graph
+        # small items: split-k tiles, column-split rows, chunked dots, merged in order
+        api.batch_set_grain(1 << 14)
+        plan = api.BatchPlan(probs)
+        assert plan.info()["split_groups"] > 0
+        out.copy_(c0)
+        plan.execute()
+        torch.cuda.synchronize()
+        assert torch.equal(batched, out), "split-item execution differs"
+        plan.close()
     finally:
         api.set_method(0)
+        api.batch_set_grain(1 << 16)
 
     # a seeded sample of each kind against the exact oracle
     rng = np.random.default_rng(44)

@@ -223,3 +223,70 @@ def test_crt_gemm_emulation_exact(sq, T, k):
                 want = fraction_to_q(Fraction(X) * Fraction(2) ** (S[i] + F[j] - 2 * T))
             assert (int(got[i * n + j, 0]), int(got[i * n + j, 1])) == want, (i, j)
 
+
+
+def half_to_int(h):
+    """Integer value of fp16 bit patterns that hold integers (|v| <= 2048)."""
+    h = h.astype(np.int64)
+    e = (h >> 10) & 0x1F
+    m = (h & 0x3FF) | 0x400
+    v = np.where(e == 0, 0, np.where(e >= 25, m << np.maximum(e - 25, 0), m >> np.maximum(25 - e, 0)))
+    return np.where(h & 0x8000, -v, v)
+
+
+@pytest.mark.parametrize("T,k", [(134, 4096), (143, 4096), (161, 8192), (180, 64)])
+def test_tensor_core_split(sq, T, k):
+    """The residue split as the tensor cores compute it (ozaki_crt_split_tc_kernel):
+    the operand row of an element (fp16 s(1024 + b_j) for the NB bytes of V,
+    then -s) times the table's B must be an integer below 2^24 (exact in the
+    fp32 accumulation) congruent to s V modulo each p, and the fp32 rounding
+    r = x - p round(x fl(1/p)) (emulated exactly with integers: fl(1/p) = M
+    2^E, the fused multiply-add with 1.5 * 2^23 rounds to the nearest integer,
+    ties to even) must give the balanced residue, |r| <= 256."""
+    head = np.zeros(4, dtype=np.int32)
+    pb = np.zeros(MAXMODS, dtype=np.uint32)
+    ib = np.zeros(MAXMODS, dtype=np.uint32)
+    b = np.zeros(64 * 2 * MAXMODS, dtype=np.uint16)
+    n = sq.sq_crt_split_table(ctypes.c_int(T), ctypes.c_int64(k), P(head), P(pb), P(ib), P(b))
+    assert n > 0
+    nmod, N, NB, TT = (int(v) for v in head)
+    assert nmod == n and TT == T and NB == (18 if T <= 144 else 24) and N % 16 == 0 and N >= 2 * n
+    # B[k][col] from the shared-memory layout: (k-block, row n, k % 8)
+    B = np.zeros((64, N), dtype=np.int64)
+    for kk in range(64):
+        for col in range(N):
+            B[kk, col] = half_to_int(np.array([b[(kk // 8) * (N * 8) + col * 8 + kk % 8]]))[0]
+    p = pb[:n].view(np.float32).astype(np.int64)
+    # V: random T-bit integers, edge values, both signs
+    rng = np.random.default_rng(T)
+    cnt = 3000
+    Vs = [int(rng.integers(0, 1 << 62)) | (int(rng.integers(0, 1 << 62)) << 62) | (int(rng.integers(0, 1 << 62)) << 124)
+          for _ in range(cnt)]
+    Vs = [v & ((1 << T) - 1) for v in Vs] + [0, (1 << T) - 1, 1, 1 << (T - 1), int("80" * 24, 16) & ((1 << T) - 1)]
+    signs = [int(rng.integers(0, 2)) for _ in Vs[:-5]] + [1, 0, 1, 0, 1]
+    A = np.zeros((len(Vs), 64), dtype=np.int64)
+    for i, (v, s) in enumerate(zip(Vs, signs)):
+        sg = -1 if s else 1
+        for j in range(NB):
+            A[i, j] = sg * (1024 + ((v >> (8 * j)) & 0xFF))
+        A[i, NB] = -sg
+        A[i, 32:] = A[i, :32]  # the second element of the row: the same value
+    X = A @ B
+    assert np.abs(X).max() < 1 << 23
+    for e in (0, 1):
+        x = X[:, e::2][:, :n]
+        for q in range(n):
+            bits = int(ib[q])
+            M = (bits & 0x7FFFFF) | 0x800000
+            E = ((bits >> 23) & 0xFF) - 127 - 23  # 1/p = M 2^E
+            sh = -E
+            t = x[:, q] * M  # x / p ~= t / 2^sh, |t| < 2^47
+            qf = t >> sh
+            rem = t - (qf << sh)
+            half = 1 << (sh - 1)
+            qq = qf + ((rem > half) | ((rem == half) & (qf & 1 == 1))).astype(np.int64)
+            r = x[:, q] - qq * p[q]
+            assert np.abs(r).max() <= 256, (T, q, int(p[q]))
+            for i, (v, s) in enumerate(zip(Vs, signs)):
+                sv = -v if s else v
+                assert (int(r[i]) - sv) % int(p[q]) == 0
