@@ -138,16 +138,16 @@ __global__ void __launch_bounds__(256)
 // on the tensor cores"): residue q of element (r, c) of the same view goes to
 // D[q * plane + r * cols_pad + c] as fp16, rows in [rows, rows_pad) and
 // columns in [cols, cols_pad) as zeros.  Persistent CTAs of 4 warps walk
-// tiles of 4 rows x 64 columns: warp w takes row 4t + w, lane l its columns
-// 2l, 2l + 1 (one tensor-memory lane, two elements).  Per tile each thread
-// writes its elements' operand row (64 fp16: s (1024 + b_j), -s, zeros) to
-// tensor memory, one thread issues four MMAs (M = 128, K = 16, N = 2 NP)
-// against the table in shared memory, and each thread reads back x_q of its
-// two elements, rounds r = x - p round(x / p) in fp32 (exact, |r| <= 256)
-// and stores the two residues of modulus q as one 32-bit word.  The next
-// tile's elements are loaded while the MMA runs.  The wait for the MMA is
-// bounded (1 s); on a timeout the CTA stops, records it in *err and frees
-// its tensor memory.
+// tiles of 4 rows x 32 columns: warp w takes row 4t + w, lane l column l
+// (one tensor-memory lane per element).  Per tile each thread writes its
+// element's operand row (32 fp16: s (1024 + b_j), -s, zeros) to tensor
+// memory, one thread issues two MMAs (M = 128, K = 16, N = nmod rounded up
+// to 16) against the table in shared memory, and each thread reads back its
+// x_q, rounds r = x - p round(x / p) in fp32 (exact, |r| <= 256) and stores
+// it.  The next tile's element is loaded while the MMAs run.  A CTA holds 64
+// tensor-memory columns (D: [0, 48), A: [48, 64)), so eight fit on an SM.
+// The wait for the MMAs is bounded (1 s); on a timeout the CTA stops,
+// records it in *err and frees its tensor memory.
 struct CrtSplitParams {
   int64_t rows, cols, rows_pad, cols_pad, plane;
   const q128* p;
@@ -158,12 +158,13 @@ struct CrtSplitParams {
 };
 
 constexpr int kSplitThreads = 128;
-constexpr int kSplitTmemCols = 128;        // D: columns [0, N), N <= 96; A: [96, 128)
-constexpr int kSplitAcol = 96;
-constexpr size_t kSplitSmem = 48 * 1024;   // table + barrier; also holds residency to 4 CTAs per SM
+constexpr int kSplitTmemCols = 64;
+constexpr int kSplitAcol = 48;
+constexpr int kSplitCtasPerSm = 8;
+constexpr size_t kSplitSmem = 26 * 1024;  // table + barrier; also keeps a ninth CTA off the SM
 
 template <int NB>
-__device__ __forceinline__ void crt_operand_row(q128 v, int Sr, int T, uint32_t* a) {
+__device__ __forceinline__ void crt_operand_row(q128 v, int Sr, int T, uint32_t (&a)[16]) {
   uint64_t v0, v1, v2;
   bool neg;
   ozaki_scaled_bits(v, Sr, T, v0, v1, v2, neg);
@@ -209,44 +210,40 @@ __global__ void __launch_bounds__(kSplitThreads)
   const uint32_t idesc = (1u << 4) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
   const uint32_t sb = smem_u32(sbase), lbo = (uint32_t)N * 16u;
 
-  const int64_t tiles_c = P.cols_pad / 64, ntiles = (P.rows_pad / 4) * tiles_c;
-  auto load = [&](int64_t t, q128& v0, q128& v1, int& Sr) {
-    v0 = v1 = q_zero(0);
+  const int64_t tiles_c = P.cols_pad / 32, ntiles = (P.rows_pad / 4) * tiles_c;
+  auto load = [&](int64_t t, q128& v, int& Sr) {
+    v = q_zero(0);
     Sr = kOzakiScaleEmpty;
     if (t >= ntiles) return;
-    const int64_t r = (t / tiles_c) * 4 + warp, c = (t % tiles_c) * 64 + 2 * lane;
+    const int64_t r = (t / tiles_c) * 4 + warp, c = (t % tiles_c) * 32 + lane;
     if (r < P.rows) {
       Sr = P.S[r];
-      if (c < P.cols) v0 = ld_cached(P.p + r * P.sr + c * P.sc);
-      if (c + 1 < P.cols) v1 = ld_cached(P.p + r * P.sr + (c + 1) * P.sc);
+      if (c < P.cols) v = ld_cached(P.p + r * P.sr + c * P.sc);
     }
   };
-  q128 v0, v1;
+  q128 v;
   int Sr;
   int64_t t = blockIdx.x;
-  load(t, v0, v1, Sr);
+  load(t, v, Sr);
   uint32_t phase = 0;
   bool ok = true;
   for (; t < ntiles; t += gridDim.x) {
     {
-      uint32_t a[32];
-      crt_operand_row<NB>(v0, Sr, tab.T, a);
-      crt_operand_row<NB>(v1, Sr, tab.T, a + 16);
-      tmem_st32(tlane + kSplitAcol, a);
+      uint32_t a[16];
+      crt_operand_row<NB>(v, Sr, tab.T, a);
+      tmem_st16(tlane + kSplitAcol, a);
     }
     tmem_st_wait();
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();  // every operand row written; every thread done with the last tile's x
     if (threadIdx.x == 0) {
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-#pragma unroll
-      for (int kt = 0; kt < 4; ++kt)
-        mma_f16kind_ta(tmem, tmem + kSplitAcol + 8 * kt, smem_desc_noswizzle(sb + 2 * kt * lbo, lbo, 128), idesc,
-                       kt ? 1u : 0u);
+      mma_f16kind_ta(tmem, tmem + kSplitAcol, smem_desc_noswizzle(sb, lbo, 128), idesc, 0u);
+      mma_f16kind_ta(tmem, tmem + kSplitAcol + 8, smem_desc_noswizzle(sb + 2 * lbo, lbo, 128), idesc, 1u);
       mma_commit(smem_u32(bar));
     }
-    const int64_t r = (t / tiles_c) * 4 + warp, c = (t % tiles_c) * 64 + 2 * lane;
-    load(t + gridDim.x, v0, v1, Sr);  // in flight while the MMAs run
+    const int64_t r = (t / tiles_c) * 4 + warp, c = (t % tiles_c) * 32 + lane;
+    load(t + gridDim.x, v, Sr);  // in flight while the MMAs run
     ok = mbar_wait(smem_u32(bar), phase);
     phase ^= 1u;
     if (!__syncthreads_and(ok)) {
@@ -254,21 +251,19 @@ __global__ void __launch_bounds__(kSplitThreads)
       break;
     }
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    uint32_t* out = reinterpret_cast<uint32_t*>(P.D + r * P.cols_pad + c);
-    const int64_t plane2 = P.plane / 2;
+    uint16_t* out = P.D + r * P.cols_pad + c;
     for (int g = 0; g < N / 16; ++g) {
       uint32_t x[16];
       tmem_ld16(tlane + 16 * g, x);
 #pragma unroll
-      for (int i = 0; i < 8; ++i) {
-        const int q = 8 * g + i;
+      for (int i = 0; i < 16; ++i) {
+        const int q = 16 * g + i;
         if (q < nmod) {
           const float p = tab.p[q], ip = tab.inv_p[q];
-          const float x0 = __uint_as_float(x[2 * i]), x1 = __uint_as_float(x[2 * i + 1]);
-          const float q0 = __fadd_rn(__fmaf_rn(x0, ip, 12582912.0f), -12582912.0f);
-          const float q1 = __fadd_rn(__fmaf_rn(x1, ip, 12582912.0f), -12582912.0f);
-          const __half2 h = __floats2half2_rn(__fmaf_rn(-q0, p, x0), __fmaf_rn(-q1, p, x1));
-          out[q * plane2] = *reinterpret_cast<const uint32_t*>(&h);
+          const float xf = __uint_as_float(x[i]);
+          const float qf = __fadd_rn(__fmaf_rn(xf, ip, 12582912.0f), -12582912.0f);
+          const __half h = __float2half_rn(__fmaf_rn(-qf, p, xf));
+          out[q * P.plane] = __half_as_ushort(h);
         }
       }
     }
@@ -911,8 +906,8 @@ static void launch_fold(int b, cudaStream_t st, const OzakiFoldParams& F) {
 }
 
 // CRT residues on the tensor cores: 18 bytes of V cover T <= 144, 24 cover
-// T <= 191.  Persistent: four CTAs per SM (their tensor memory is 128
-// columns each; the dynamic shared memory keeps a fifth off the SM).
+// T <= 191.  Persistent: eight CTAs per SM (their tensor memory is 64
+// columns each; the dynamic shared memory keeps a ninth off the SM).
 static cudaError_t launch_crt_split(const CrtSplitTable& stab, cudaStream_t st, int64_t rows, int64_t cols,
                                     int64_t rows_pad, int64_t cols_pad, int64_t plane, const q128* p, int64_t sr,
                                     int64_t sc, const int* S, uint16_t* D, int* err) {
@@ -928,9 +923,9 @@ static cudaError_t launch_crt_split(const CrtSplitTable& stab, cudaStream_t st, 
   P.S = S;
   P.err = err;
   P.D = D;
-  const int64_t ntiles = (rows_pad / 4) * (cols_pad / 64);
+  const int64_t ntiles = (rows_pad / 4) * (cols_pad / 32);
   if (ntiles <= 0) return cudaSuccess;
-  const unsigned grid = (unsigned)std::min<int64_t>(ntiles, 4 * (int64_t)device_sm_count());
+  const unsigned grid = (unsigned)std::min<int64_t>(ntiles, kSplitCtasPerSm * (int64_t)device_sm_count());
   if (stab.NB == 18)
     ozaki_crt_split_tc_kernel<18><<<grid, kSplitThreads, kSplitSmem, st>>>(P, stab);
   else

@@ -183,22 +183,20 @@ inline bool crt_build(int T, int64_t k, CrtTable& tab) {
 // ---------------------------------------------------------------------------
 // For the split kernel, an element's scaled integer V (NB bytes b_j, V =
 // sum_j b_j 256^j, NB = 18 for T <= 144 and 24 for T <= 191) becomes one row
-// of an MMA operand A: the fp16 values s (1024 + b_j) (one byte select each:
-// the bits 0x64 | sign above the byte), then -s, then zeros (32 per
-// element; s = +-1 the sign of the element).  B holds, per modulus q, the
-// balanced c_jq = 256^j mod p_q and beta_q = (1024 sum_j c_jq) mod p_q, both
-// of magnitude at most 256, so that
+// of an MMA operand A (K = 32): the fp16 values s (1024 + b_j) (one byte
+// select each: the bits 0x64 | sign above the byte), then -s, then zeros
+// (s = +-1 the sign of the element).  B (K x N, N = nmod rounded up to 16)
+// holds, per modulus q, the balanced c_jq = 256^j mod p_q and
+// beta_q = (1024 sum_j c_jq) mod p_q, both of magnitude at most 256, so that
 //   x_q = s sum_j (1024 + b_j) c_jq - s beta_q == s V  (mod p_q),
 //   |x_q| <= NB * 1279 * 256 + 256 < 2^23,
 // an integer the fp32 accumulation holds exactly.  The balanced residue is
 // then r = x - p * round(x / p) in fp32: the error of x * fl(1/p) is below
 // |x| 2^-33 < 9.2e-4, less than the distance 1 / (2p) >= 9.78e-4 of x / p
 // from a half-integer for odd p, so round() picks the nearest integer and
-// |r| <= floor(p / 2) (for p = 512 a tie gives +-256).  Two elements share
-// an operand row (K = 32 each) with block-diagonal B (N = 2 NP columns,
-// element e of modulus q in column 2q + e, NP = nmod rounded up to 8).
-constexpr int kCrtSplitK = 64;                   // K: 32 per element, two elements
-constexpr int kCrtSplitMaxN = 2 * kCrtMaxMods;   // 96
+// |r| <= floor(p / 2) (for p = 512 a tie gives +-256).
+constexpr int kCrtSplitK = 32;
+constexpr int kCrtSplitMaxN = 48;  // kCrtMaxMods
 
 struct alignas(16) CrtSplitTable {
   int nmod, N, NB, T;
@@ -232,15 +230,14 @@ inline void crt_split_table(const CrtTable& tab, CrtSplitTable& st) {
   st.nmod = tab.n;
   st.T = tab.T;
   st.NB = tab.T <= 144 ? 18 : 24;
-  const int NP = (tab.n + 7) / 8 * 8;
-  st.N = 2 * NP;
+  st.N = (tab.n + 15) / 16 * 16;
   for (int q = 0; q < tab.n; ++q) {
     const uint32_t p = tab.mod[q].p;
     st.p[q] = (float)p;
     st.inv_p[q] = (float)(1.0 / (double)p);
   }
   for (int n = 0; n < st.N; ++n) {
-    const int q = n / 2, e = n % 2;
+    const int q = n;
     int64_t csum = 0;
     int c[32] = {0};
     if (q < tab.n) {
@@ -254,8 +251,7 @@ inline void crt_split_table(const CrtTable& tab, CrtSplitTable& st) {
       c[st.NB] = crt_balanced(1024 * csum, p);
     }
     for (int k = 0; k < kCrtSplitK; ++k) {
-      const int ek = k / 32, j = k % 32;
-      const int v = (q < tab.n && ek == e && j <= st.NB) ? c[j] : 0;
+      const int v = (q < tab.n && k <= st.NB) ? c[k] : 0;
       st.b[(k / 8) * (st.N * 8) + n * 8 + (k % 8)] = crt_half_bits(v);
     }
   }
