@@ -144,10 +144,11 @@ __global__ void __launch_bounds__(256)
 // memory, one thread issues two MMAs (M = 128, K = 16, N = nmod rounded up
 // to 16) against the table in shared memory, and each thread reads back its
 // x_q, rounds r = x - p round(x / p) in fp32 (exact, |r| <= 256) and stores
-// it.  The next tile's element is loaded while the MMAs run.  A CTA holds 64
-// tensor-memory columns (D: [0, 48), A: [48, 64)), so eight fit on an SM.
-// The wait for the MMAs is bounded (1 s); on a timeout the CTA stops,
-// records it in *err and frees its tensor memory.
+// it.  Two stages (operand row and accumulator, 64 tensor-memory columns
+// each; four CTAs fit on an SM): the MMAs of a tile run while the residues
+// of the tile before are rounded and stored, and the next tile's element is
+// loaded meanwhile.  The waits for the MMAs are bounded (1 s); on a timeout
+// the CTA stops, records it in *err and frees its tensor memory.
 struct CrtSplitParams {
   int64_t rows, cols, rows_pad, cols_pad, plane;
   const q128* p;
@@ -158,10 +159,11 @@ struct CrtSplitParams {
 };
 
 constexpr int kSplitThreads = 128;
-constexpr int kSplitTmemCols = 64;
+constexpr int kSplitStageCols = 64;   // D: [0, 48), A: [48, 64) of each stage
+constexpr int kSplitTmemCols = 128;
 constexpr int kSplitAcol = 48;
-constexpr int kSplitCtasPerSm = 8;
-constexpr size_t kSplitSmem = 26 * 1024;  // table + barrier; also keeps a ninth CTA off the SM
+constexpr int kSplitCtasPerSm = 4;
+constexpr size_t kSplitSmem = 48 * 1024;  // table + barriers; also keeps a fifth CTA off the SM
 
 template <int NB>
 __device__ __forceinline__ void crt_operand_row(q128 v, int Sr, int T, uint32_t (&a)[16]) {
@@ -184,8 +186,8 @@ __global__ void __launch_bounds__(kSplitThreads)
     ozaki_crt_split_tc_kernel(const __grid_constant__ CrtSplitParams P, const __grid_constant__ CrtSplitTable tab) {
   extern __shared__ __align__(128) uint8_t split_smem[];
   uint8_t* sbase = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(split_smem) + 127) & ~(uintptr_t)127);
-  uint64_t* bar = reinterpret_cast<uint64_t*>(sbase + kCrtSplitK * kCrtSplitMaxN * 2);
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar + 1);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(sbase + kCrtSplitK * kCrtSplitMaxN * 2);  // [2]
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar + 2);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int N = tab.N, nmod = tab.nmod;
   // the table (B operand) into shared memory, visible to the tensor cores
@@ -194,6 +196,7 @@ __global__ void __launch_bounds__(kSplitThreads)
   fence_proxy_async_smem();
   if (threadIdx.x == 0) {
     mbar_init(smem_u32(bar), 1);
+    mbar_init(smem_u32(bar + 1), 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 0) {
@@ -221,55 +224,84 @@ __global__ void __launch_bounds__(kSplitThreads)
       if (c < P.cols) v = ld_cached(P.p + r * P.sr + c * P.sc);
     }
   };
+  // rounds and stores the residues of tile t from stage st (after its MMAs)
+  auto finish = [&](int64_t t, int st) {
+    const int64_t r = (t / tiles_c) * 4 + warp, c = (t % tiles_c) * 32 + lane;
+    uint16_t* out = P.D + r * P.cols_pad + c;
+    uint32_t x[kCrtSplitMaxN];
+    const uint32_t d = tlane + (uint32_t)(st * kSplitStageCols);
+    tmem_ld16_nowait(d, x);
+    if (N > 16) tmem_ld16_nowait(d + 16, x + 16);
+    if (N > 32) tmem_ld16_nowait(d + 32, x + 32);
+    tmem_ld_wait();
+#pragma unroll
+    for (int q = 0; q < kCrtSplitMaxN; ++q) {
+      if (q < nmod) {
+        const float p = tab.p[q], ip = tab.inv_p[q];
+        const float xf = __uint_as_float(x[q]);
+        const float qf = __fadd_rn(__fmaf_rn(xf, ip, 12582912.0f), -12582912.0f);
+        const __half h = __float2half_rn(__fmaf_rn(-qf, p, xf));
+        out[q * P.plane] = __half_as_ushort(h);
+      }
+    }
+  };
   q128 v;
   int Sr;
-  int64_t t = blockIdx.x;
-  load(t, v, Sr);
-  uint32_t phase = 0;
+  load(blockIdx.x, v, Sr);
+  uint32_t phases = 0u;  // bit s: parity of the next phase of stage s's barrier
   bool ok = true;
-  for (; t < ntiles; t += gridDim.x) {
+  int64_t prev = -1;  // tile whose MMAs were issued last iteration
+  int last = 0;       // stage of the last MMAs issued
+  int i = 0;
+  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x, ++i) {
+    const int st = i & 1;
+    last = st;
     {
       uint32_t a[16];
       crt_operand_row<NB>(v, Sr, tab.T, a);
-      tmem_st16(tlane + kSplitAcol, a);
+      tmem_st16(tlane + (uint32_t)(st * kSplitStageCols + kSplitAcol), a);
     }
     tmem_st_wait();
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    __syncthreads();  // every operand row written; every thread done with the last tile's x
+    __syncthreads();  // operand rows written; stage st's accumulator read two tiles ago
     if (threadIdx.x == 0) {
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      mma_f16kind_ta(tmem, tmem + kSplitAcol, smem_desc_noswizzle(sb, lbo, 128), idesc, 0u);
-      mma_f16kind_ta(tmem, tmem + kSplitAcol + 8, smem_desc_noswizzle(sb + 2 * lbo, lbo, 128), idesc, 1u);
-      mma_commit(smem_u32(bar));
+      const uint32_t dcol = tmem + (uint32_t)(st * kSplitStageCols), acol = dcol + kSplitAcol;
+      mma_f16kind_ta(dcol, acol, smem_desc_noswizzle(sb, lbo, 128), idesc, 0u);
+      mma_f16kind_ta(dcol, acol + 8, smem_desc_noswizzle(sb + 2 * lbo, lbo, 128), idesc, 1u);
+      mma_commit(smem_u32(bar + st));
     }
-    const int64_t r = (t / tiles_c) * 4 + warp, c = (t % tiles_c) * 32 + lane;
     load(t + gridDim.x, v, Sr);  // in flight while the MMAs run
-    ok = mbar_wait(smem_u32(bar), phase);
-    phase ^= 1u;
-    if (!__syncthreads_and(ok)) {
-      ok = false;
-      break;
+    if (prev >= 0) {
+      const int ps = st ^ 1;
+      ok = mbar_wait(smem_u32(bar + ps), (phases >> ps) & 1u);
+      phases ^= 1u << ps;
+      if (!__syncthreads_and(ok)) {
+        ok = false;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      finish(prev, ps);
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     }
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    uint16_t* out = P.D + r * P.cols_pad + c;
-    for (int g = 0; g < N / 16; ++g) {
-      uint32_t x[16];
-      tmem_ld16(tlane + 16 * g, x);
-#pragma unroll
-      for (int i = 0; i < 16; ++i) {
-        const int q = 16 * g + i;
-        if (q < nmod) {
-          const float p = tab.p[q], ip = tab.inv_p[q];
-          const float xf = __uint_as_float(x[i]);
-          const float qf = __fadd_rn(__fmaf_rn(xf, ip, 12582912.0f), -12582912.0f);
-          const __half h = __float2half_rn(__fmaf_rn(-qf, p, xf));
-          out[q * P.plane] = __half_as_ushort(h);
-        }
+    prev = t;
+  }
+  // the last MMAs issued: the last tile's, finished here; after a timeout they
+  // are still waited for (bounded), so that none is in flight when the
+  // tensor memory is freed
+  if (prev >= 0) {
+    const bool got = mbar_wait(smem_u32(bar + last), (phases >> last) & 1u);
+    if (ok) {
+      if (__syncthreads_and(got)) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        finish(prev, last);
+      } else {
+        ok = false;
       }
     }
-    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   }
   if (!ok && threadIdx.x == 0) atomicExch(P.err, 1);
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   if (warp == 0)
@@ -906,8 +938,8 @@ static void launch_fold(int b, cudaStream_t st, const OzakiFoldParams& F) {
 }
 
 // CRT residues on the tensor cores: 18 bytes of V cover T <= 144, 24 cover
-// T <= 191.  Persistent: eight CTAs per SM (their tensor memory is 64
-// columns each; the dynamic shared memory keeps a ninth off the SM).
+// T <= 191.  Persistent: four CTAs per SM (their tensor memory is 128
+// columns each; the dynamic shared memory keeps a fifth off the SM).
 static cudaError_t launch_crt_split(const CrtSplitTable& stab, cudaStream_t st, int64_t rows, int64_t cols,
                                     int64_t rows_pad, int64_t cols_pad, int64_t plane, const q128* p, int64_t sr,
                                     int64_t sc, const int* S, uint16_t* D, int* err) {
