@@ -138,17 +138,18 @@ __global__ void __launch_bounds__(256)
 // on the tensor cores"): residue q of element (r, c) of the same view goes to
 // D[q * plane + r * cols_pad + c] as fp16, rows in [rows, rows_pad) and
 // columns in [cols, cols_pad) as zeros.  Persistent CTAs of 4 warps walk
-// tiles of 4 rows x 32 columns: warp w takes row 4t + w, lane l column l
-// (one tensor-memory lane per element).  Per tile each thread writes its
-// element's operand row (32 fp16: s (1024 + b_j), -s, zeros) to tensor
-// memory, one thread issues two MMAs (M = 128, K = 16, N = nmod rounded up
-// to 16) against the table in shared memory, and each thread reads back its
-// x_q, rounds r = x - p round(x / p) in fp32 (exact, |r| <= 256) and stores
-// it.  Two stages (operand row and accumulator, 64 tensor-memory columns
-// each; four CTAs fit on an SM): the MMAs of a tile run while the residues
-// of the tile before are rounded and stored, and the next tile's element is
-// loaded meanwhile.  The waits for the MMAs are bounded (1 s); on a timeout
-// the CTA stops, records it in *err and frees its tensor memory.
+// tiles of 4 rows x 64 columns: warp w takes row 4t + w, lane l columns 2l
+// and 2l + 1 (one tensor-memory lane, two elements).  Per tile each thread
+// scales its two elements (crt_scaled_words, branch-free), writes their
+// operand rows (32 fp16 each: s (1024 + b_j), -s, zeros) to tensor memory;
+// one thread issues four MMAs (M = 128, K = 16, N = 2 NP, block-diagonal B:
+// element e of modulus q in column 2q + e) against the table in shared
+// memory and waits for them; then each thread reads its x_q, rounds
+// r = x - p round(x / p) in fp32 (exact, |r| <= 256) and stores the two
+// residues of a modulus as one 32-bit word.  The next tile's elements are
+// loaded while the MMAs run.  128 tensor-memory columns per CTA (D: [0, 96),
+// A: [96, 128)), four CTAs per SM.  The wait for the MMAs is bounded (1 s);
+// on a timeout the CTA stops, records it in *err and frees its tensor memory.
 struct CrtSplitParams {
   int64_t rows, cols, rows_pad, cols_pad, plane;
   const q128* p;
@@ -159,24 +160,23 @@ struct CrtSplitParams {
 };
 
 constexpr int kSplitThreads = 128;
-constexpr int kSplitStageCols = 64;   // D: [0, 48), A: [48, 64) of each stage
 constexpr int kSplitTmemCols = 128;
-constexpr int kSplitAcol = 48;
+constexpr int kSplitAcol = 96;
 constexpr int kSplitCtasPerSm = 4;
-constexpr size_t kSplitSmem = 48 * 1024;  // table + barriers; also keeps a fifth CTA off the SM
+constexpr size_t kSplitSmem = 48 * 1024;  // table + barrier; also keeps a fifth CTA off the SM
 
+// Operand row of one element: bytes 2i, 2i+1 of V as fp16 s (1024 + b),
+// then -s, then zeros.
 template <int NB>
-__device__ __forceinline__ void crt_operand_row(q128 v, int Sr, int T, uint32_t (&a)[16]) {
-  uint64_t v0, v1, v2;
+__device__ __forceinline__ void crt_operand_row(q128 v, int Sr, int T, uint32_t* a) {
+  constexpr int NW = (NB + 3) / 4;
+  uint32_t w[NW];
   bool neg;
-  ozaki_scaled_bits(v, Sr, T, v0, v1, v2, neg);
-  const uint32_t w[6] = {(uint32_t)v0, (uint32_t)(v0 >> 32), (uint32_t)v1, (uint32_t)(v1 >> 32), (uint32_t)v2,
-                         (uint32_t)(v2 >> 32)};
+  crt_scaled_words<NW>(v, Sr, T, w, neg);
   const uint32_t sgn = neg ? 0xE4E4E4E4u : 0x64646464u;
 #pragma unroll
-  for (int i = 0; i < NB / 2; ++i)  // bytes 2i, 2i+1 as fp16 s (1024 + b)
-    a[i] = __byte_perm(w[i >> 1], sgn, (i & 1) ? 0x4342u : 0x4140u);
-  a[NB / 2] = neg ? 0x3C00u : 0xBC00u;  // -s, then zeros
+  for (int i = 0; i < NB / 2; ++i) a[i] = __byte_perm(w[i >> 1], sgn, (i & 1) ? 0x4342u : 0x4140u);
+  a[NB / 2] = neg ? 0x3C00u : 0xBC00u;
 #pragma unroll
   for (int i = NB / 2 + 1; i < 16; ++i) a[i] = 0u;
 }
@@ -186,8 +186,9 @@ __global__ void __launch_bounds__(kSplitThreads)
     ozaki_crt_split_tc_kernel(const __grid_constant__ CrtSplitParams P, const __grid_constant__ CrtSplitTable tab) {
   extern __shared__ __align__(128) uint8_t split_smem[];
   uint8_t* sbase = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(split_smem) + 127) & ~(uintptr_t)127);
-  uint64_t* bar = reinterpret_cast<uint64_t*>(sbase + kCrtSplitK * kCrtSplitMaxN * 2);  // [2]
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar + 2);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(sbase + kCrtSplitK * kCrtSplitMaxN * 2);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar + 1);
+  int* flag = reinterpret_cast<int*>(bar + 2);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int N = tab.N, nmod = tab.nmod;
   // the table (B operand) into shared memory, visible to the tensor cores
@@ -196,7 +197,6 @@ __global__ void __launch_bounds__(kSplitThreads)
   fence_proxy_async_smem();
   if (threadIdx.x == 0) {
     mbar_init(smem_u32(bar), 1);
-    mbar_init(smem_u32(bar + 1), 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 0) {
@@ -212,96 +212,84 @@ __global__ void __launch_bounds__(kSplitThreads)
   const uint32_t tlane = tmem + ((uint32_t)(warp * 32) << 16);
   const uint32_t idesc = (1u << 4) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
   const uint32_t sb = smem_u32(sbase), lbo = (uint32_t)N * 16u;
+  const int64_t plane2 = P.plane / 2;
 
-  const int64_t tiles_c = P.cols_pad / 32, ntiles = (P.rows_pad / 4) * tiles_c;
-  auto load = [&](int64_t t, q128& v, int& Sr) {
-    v = q_zero(0);
+  // tiles t = blockIdx.x, + gridDim.x, ...: (row tile tr, column tile tc),
+  // advanced by counting (no division in the loop)
+  const int tiles_c = (int)(P.cols_pad / 64), tiles_r = (int)(P.rows_pad / 4);
+  const int step_r = (int)gridDim.x / tiles_c, step_c = (int)gridDim.x % tiles_c;
+  int tr = (int)blockIdx.x / tiles_c, tc = (int)blockIdx.x % tiles_c;
+  auto load = [&](int r_t, int c_t, q128& v0, q128& v1, int& Sr) {
+    v0 = v1 = q_zero(0);
     Sr = kOzakiScaleEmpty;
-    if (t >= ntiles) return;
-    const int64_t r = (t / tiles_c) * 4 + warp, c = (t % tiles_c) * 32 + lane;
+    if (r_t >= tiles_r) return;
+    const int64_t r = (int64_t)r_t * 4 + warp, c = (int64_t)c_t * 64 + 2 * lane;
     if (r < P.rows) {
       Sr = P.S[r];
-      if (c < P.cols) v = ld_cached(P.p + r * P.sr + c * P.sc);
+      const q128* e = P.p + r * P.sr + c * P.sc;
+      if (c < P.cols) v0 = ld_cached(e);
+      if (c + 1 < P.cols) v1 = ld_cached(e + P.sc);
     }
   };
-  // rounds and stores the residues of tile t from stage st (after its MMAs)
-  auto finish = [&](int64_t t, int st) {
-    const int64_t r = (t / tiles_c) * 4 + warp, c = (t % tiles_c) * 32 + lane;
-    uint16_t* out = P.D + r * P.cols_pad + c;
-    uint32_t x[kCrtSplitMaxN];
-    const uint32_t d = tlane + (uint32_t)(st * kSplitStageCols);
-    tmem_ld16_nowait(d, x);
-    if (N > 16) tmem_ld16_nowait(d + 16, x + 16);
-    if (N > 32) tmem_ld16_nowait(d + 32, x + 32);
-    tmem_ld_wait();
-#pragma unroll
-    for (int q = 0; q < kCrtSplitMaxN; ++q) {
-      if (q < nmod) {
-        const float p = tab.p[q], ip = tab.inv_p[q];
-        const float xf = __uint_as_float(x[q]);
-        const float qf = __fadd_rn(__fmaf_rn(xf, ip, 12582912.0f), -12582912.0f);
-        const __half h = __float2half_rn(__fmaf_rn(-qf, p, xf));
-        out[q * P.plane] = __half_as_ushort(h);
-      }
-    }
-  };
-  q128 v;
+  q128 v0, v1;
   int Sr;
-  load(blockIdx.x, v, Sr);
-  uint32_t phases = 0u;  // bit s: parity of the next phase of stage s's barrier
+  load(tr, tc, v0, v1, Sr);
+  uint32_t phase = 0;
   bool ok = true;
-  int64_t prev = -1;  // tile whose MMAs were issued last iteration
-  int last = 0;       // stage of the last MMAs issued
-  int i = 0;
-  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x, ++i) {
-    const int st = i & 1;
-    last = st;
+  while (tr < tiles_r) {
     {
-      uint32_t a[16];
-      crt_operand_row<NB>(v, Sr, tab.T, a);
-      tmem_st16(tlane + (uint32_t)(st * kSplitStageCols + kSplitAcol), a);
+      uint32_t a[32];
+      crt_operand_row<NB>(v0, Sr, tab.T, a);
+      crt_operand_row<NB>(v1, Sr, tab.T, a + 16);
+      tmem_st32(tlane + kSplitAcol, a);
     }
     tmem_st_wait();
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    __syncthreads();  // operand rows written; stage st's accumulator read two tiles ago
+    __syncthreads();  // operand rows written; the last tile's accumulator read
+    const int64_t r = (int64_t)tr * 4 + warp, c = (int64_t)tc * 64 + 2 * lane;
+    tc += step_c;
+    tr += step_r;
+    if (tc >= tiles_c) {
+      tc -= tiles_c;
+      ++tr;
+    }
     if (threadIdx.x == 0) {
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const uint32_t dcol = tmem + (uint32_t)(st * kSplitStageCols), acol = dcol + kSplitAcol;
-      mma_f16kind_ta(dcol, acol, smem_desc_noswizzle(sb, lbo, 128), idesc, 0u);
-      mma_f16kind_ta(dcol, acol + 8, smem_desc_noswizzle(sb + 2 * lbo, lbo, 128), idesc, 1u);
-      mma_commit(smem_u32(bar + st));
+#pragma unroll
+      for (int kt = 0; kt < 4; ++kt)
+        mma_f16kind_ta(tmem, tmem + kSplitAcol + 8 * kt, smem_desc_noswizzle(sb + 2 * kt * lbo, lbo, 128), idesc,
+                       kt ? 1u : 0u);
+      mma_commit(smem_u32(bar));
     }
-    load(t + gridDim.x, v, Sr);  // in flight while the MMAs run
-    if (prev >= 0) {
-      const int ps = st ^ 1;
-      ok = mbar_wait(smem_u32(bar + ps), (phases >> ps) & 1u);
-      phases ^= 1u << ps;
-      if (!__syncthreads_and(ok)) {
-        ok = false;
-        break;
+    load(tr, tc, v0, v1, Sr);  // the next tile's elements, in flight while the MMAs run
+    if (threadIdx.x == 0) *flag = mbar_wait(smem_u32(bar), phase) ? 1 : 0;
+    phase ^= 1u;
+    __syncthreads();
+    if (!*flag) {
+      ok = false;
+      break;
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    uint32_t* out = reinterpret_cast<uint32_t*>(P.D + r * P.cols_pad + c);
+    for (int g = 0; 8 * g < nmod; ++g) {
+      uint32_t x[16];
+      tmem_ld16(tlane + 16 * g, x);
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        const int q = 8 * g + i;
+        if (q < nmod) {
+          const float p = tab.p[q], ip = tab.inv_p[q];
+          const float x0 = __uint_as_float(x[2 * i]), x1 = __uint_as_float(x[2 * i + 1]);
+          const float q0 = __fadd_rn(__fmaf_rn(x0, ip, 12582912.0f), -12582912.0f);
+          const float q1 = __fadd_rn(__fmaf_rn(x1, ip, 12582912.0f), -12582912.0f);
+          const __half2 h = __floats2half2_rn(__fmaf_rn(-q0, p, x0), __fmaf_rn(-q1, p, x1));
+          out[q * plane2] = *reinterpret_cast<const uint32_t*>(&h);
+        }
       }
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      finish(prev, ps);
-      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     }
-    prev = t;
-  }
-  // the last MMAs issued: the last tile's, finished here; after a timeout they
-  // are still waited for (bounded), so that none is in flight when the
-  // tensor memory is freed
-  if (prev >= 0) {
-    const bool got = mbar_wait(smem_u32(bar + last), (phases >> last) & 1u);
-    if (ok) {
-      if (__syncthreads_and(got)) {
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        finish(prev, last);
-      } else {
-        ok = false;
-      }
-    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   }
   if (!ok && threadIdx.x == 0) atomicExch(P.err, 1);
-  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   if (warp == 0)
@@ -955,8 +943,9 @@ static cudaError_t launch_crt_split(const CrtSplitTable& stab, cudaStream_t st, 
   P.S = S;
   P.err = err;
   P.D = D;
-  const int64_t ntiles = (rows_pad / 4) * (cols_pad / 32);
+  const int64_t ntiles = (rows_pad / 4) * (cols_pad / 64);
   if (ntiles <= 0) return cudaSuccess;
+  if (ntiles > INT32_MAX) return cudaErrorInvalidValue;
   const unsigned grid = (unsigned)std::min<int64_t>(ntiles, kSplitCtasPerSm * (int64_t)device_sm_count());
   if (stab.NB == 18)
     ozaki_crt_split_tc_kernel<18><<<grid, kSplitThreads, kSplitSmem, st>>>(P, stab);

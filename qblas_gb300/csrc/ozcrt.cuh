@@ -25,6 +25,7 @@
 #include <stdint.h>
 
 #include "ozaki.cuh"
+#include "wacc.cuh"
 
 namespace qb {
 
@@ -182,21 +183,23 @@ inline bool crt_build(int T, int64_t k, CrtTable& tab) {
 // Residue split on the tensor cores: the table (host)
 // ---------------------------------------------------------------------------
 // For the split kernel, an element's scaled integer V (NB bytes b_j, V =
-// sum_j b_j 256^j, NB = 18 for T <= 144 and 24 for T <= 191) becomes one row
-// of an MMA operand A (K = 32): the fp16 values s (1024 + b_j) (one byte
-// select each: the bits 0x64 | sign above the byte), then -s, then zeros
-// (s = +-1 the sign of the element).  B (K x N, N = nmod rounded up to 16)
-// holds, per modulus q, the balanced c_jq = 256^j mod p_q and
-// beta_q = (1024 sum_j c_jq) mod p_q, both of magnitude at most 256, so that
+// sum_j b_j 256^j, NB = 18 for T <= 144 and 24 for T <= 191) becomes 32
+// values of one row of an MMA operand A: the fp16 values s (1024 + b_j) (one
+// byte select each: the bits 0x64 | sign above the byte), then -s, then
+// zeros (s = +-1 the sign of the element).  B holds, per modulus q, the
+// balanced c_jq = 256^j mod p_q and beta_q = (1024 sum_j c_jq) mod p_q, both
+// of magnitude at most 256, so that
 //   x_q = s sum_j (1024 + b_j) c_jq - s beta_q == s V  (mod p_q),
 //   |x_q| <= NB * 1279 * 256 + 256 < 2^23,
 // an integer the fp32 accumulation holds exactly.  The balanced residue is
 // then r = x - p * round(x / p) in fp32: the error of x * fl(1/p) is below
 // |x| 2^-33 < 9.2e-4, less than the distance 1 / (2p) >= 9.78e-4 of x / p
 // from a half-integer for odd p, so round() picks the nearest integer and
-// |r| <= floor(p / 2) (for p = 512 a tie gives +-256).
-constexpr int kCrtSplitK = 32;
-constexpr int kCrtSplitMaxN = 48;  // kCrtMaxMods
+// |r| <= floor(p / 2) (for p = 512 a tie gives +-256).  Two elements share
+// an operand row (K = 32 each) with block-diagonal B (N = 2 NP columns,
+// element e of modulus q in column 2q + e, NP = nmod rounded up to 8).
+constexpr int kCrtSplitK = 64;                   // K: 32 per element, two elements
+constexpr int kCrtSplitMaxN = 2 * kCrtMaxMods;   // 96
 
 struct alignas(16) CrtSplitTable {
   int nmod, N, NB, T;
@@ -206,6 +209,43 @@ struct alignas(16) CrtSplitTable {
   // 16 bytes of (row n, k-block kb) at kb * (N * 16) + n * 16
   uint16_t b[kCrtSplitK * kCrtSplitMaxN];
 };
+
+// The 32-bit words of V = trunc(|a| 2^(T - S)) (as ozaki_scaled_bits) for
+// the split kernel, without data-dependent branches on the common path:
+// |a| = M 2^(E - 112) with M the 113-bit significand (subnormals are
+// normalised in a branch that warps rarely take), and V = (M << 96) >> R with
+// R = 208 - T + S - E, at least 18 because S > E; V is read from an 8-word
+// frame by a three-level word select and one funnel shift per word.  Zeros,
+// infinities, NaNs and empty rows (S = kOzakiScaleEmpty) give V = 0.
+template <int NW>
+QB_HD void crt_scaled_words(q128 a, int S, int T, uint32_t (&w)[NW], bool& neg) {
+  neg = (a.hi >> 63) != 0;
+  const int be = (int)((a.hi >> 48) & 0x7FFFu);
+  uint64_t mh = a.hi & kMantHiMask, ml = a.lo;
+  int E = be - kBias;
+  bool zero = be == kExpField || S == kOzakiScaleEmpty;
+  if (be != 0) {
+    mh |= kHiddenBit;
+  } else if ((mh | ml) == 0) {
+    zero = true;
+  } else {
+    q_unpack_norm(a, mh, ml, E);
+  }
+  int R = 208 - T + S - E;
+  R = zero ? 255 : (R < 0 ? 0 : (R > 255 ? 255 : R));
+  const uint32_t k = (uint32_t)R >> 5, b = (uint32_t)R & 31u;
+  const uint32_t x[16] = {0u, 0u, 0u, (uint32_t)ml, (uint32_t)(ml >> 32), (uint32_t)mh, (uint32_t)(mh >> 32), 0u,
+                          0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u};
+  uint32_t z[NW + 4], u[NW + 2], y[NW + 1];
+#pragma unroll
+  for (int j = 0; j < NW + 4; ++j) z[j] = (k & 4u) ? x[j + 4] : x[j];
+#pragma unroll
+  for (int j = 0; j < NW + 2; ++j) u[j] = (k & 2u) ? z[j + 2] : z[j];
+#pragma unroll
+  for (int j = 0; j < NW + 1; ++j) y[j] = (k & 1u) ? u[j + 1] : u[j];
+#pragma unroll
+  for (int i = 0; i < NW; ++i) w[i] = fshr32(y[i], y[i + 1], b);
+}
 
 // fp16 bits of an integer |v| <= 2048 (exact)
 inline uint16_t crt_half_bits(int v) {
@@ -230,14 +270,14 @@ inline void crt_split_table(const CrtTable& tab, CrtSplitTable& st) {
   st.nmod = tab.n;
   st.T = tab.T;
   st.NB = tab.T <= 144 ? 18 : 24;
-  st.N = (tab.n + 15) / 16 * 16;
+  st.N = 2 * ((tab.n + 7) / 8 * 8);
   for (int q = 0; q < tab.n; ++q) {
     const uint32_t p = tab.mod[q].p;
     st.p[q] = (float)p;
     st.inv_p[q] = (float)(1.0 / (double)p);
   }
   for (int n = 0; n < st.N; ++n) {
-    const int q = n;
+    const int q = n / 2, e = n % 2;
     int64_t csum = 0;
     int c[32] = {0};
     if (q < tab.n) {
@@ -251,7 +291,8 @@ inline void crt_split_table(const CrtTable& tab, CrtSplitTable& st) {
       c[st.NB] = crt_balanced(1024 * csum, p);
     }
     for (int k = 0; k < kCrtSplitK; ++k) {
-      const int v = (q < tab.n && k <= st.NB) ? c[k] : 0;
+      const int ek = k / 32, j = k % 32;
+      const int v = (q < tab.n && ek == e && j <= st.NB) ? c[j] : 0;
       st.b[(k / 8) * (st.N * 8) + n * 8 + (k % 8)] = crt_half_bits(v);
     }
   }

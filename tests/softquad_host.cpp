@@ -298,6 +298,21 @@ int sq_crt_split_table(int T, int64_t k, int32_t* head4, uint32_t* p_bits, uint3
   return t.n;
 }
 
+// crt_scaled_words (6 words) and ozaki_scaled_bits of each a[i] with scale
+// S[i]: out[i] = {6 words, neg} and ref[i] = {v0, v1, v2, neg}.
+void sq_crt_scaled_words(int64_t n, const q128* a, const int* S, int T, uint32_t* out, uint64_t* ref) {
+  for (int64_t i = 0; i < n; ++i) {
+    uint32_t w[6];
+    bool neg;
+    qb::crt_scaled_words<6>(a[i], S[i], T, w, neg);
+    for (int j = 0; j < 6; ++j) out[7 * i + j] = w[j];
+    out[7 * i + 6] = neg;
+    bool neg2;
+    qb::ozaki_scaled_bits(a[i], S[i], T, ref[4 * i], ref[4 * i + 1], ref[4 * i + 2], neg2);
+    ref[4 * i + 3] = neg2;
+  }
+}
+
 // Reconstruction of X 2^e[i] from C[i][q] (one pass) for each output i.
 int sq_crt_reconstruct(int64_t n, const int32_t* C, const int* e, int T, int64_t k, q128* out) {
   qb::CrtTable t;

@@ -246,14 +246,14 @@ def test_tensor_core_split(sq, T, k):
     head = np.zeros(4, dtype=np.int32)
     pb = np.zeros(MAXMODS, dtype=np.uint32)
     ib = np.zeros(MAXMODS, dtype=np.uint32)
-    b = np.zeros(32 * MAXMODS, dtype=np.uint16)
+    b = np.zeros(64 * 2 * MAXMODS, dtype=np.uint16)
     n = sq.sq_crt_split_table(ctypes.c_int(T), ctypes.c_int64(k), P(head), P(pb), P(ib), P(b))
     assert n > 0
     nmod, N, NB, TT = (int(v) for v in head)
-    assert nmod == n and TT == T and NB == (18 if T <= 144 else 24) and N % 16 == 0 and n <= N < n + 16
+    assert nmod == n and TT == T and NB == (18 if T <= 144 else 24) and N % 16 == 0 and 2 * n <= N < 2 * n + 16
     # B[k][col] from the shared-memory layout: (k-block, row n, k % 8)
-    B = np.zeros((32, N), dtype=np.int64)
-    for kk in range(32):
+    B = np.zeros((64, N), dtype=np.int64)
+    for kk in range(64):
         for col in range(N):
             B[kk, col] = half_to_int(np.array([b[(kk // 8) * (N * 8) + col * 8 + kk % 8]]))[0]
     p = pb[:n].view(np.float32).astype(np.int64)
@@ -264,17 +264,19 @@ def test_tensor_core_split(sq, T, k):
           for _ in range(cnt)]
     Vs = [v & ((1 << T) - 1) for v in Vs] + [0, (1 << T) - 1, 1, 1 << (T - 1), int("80" * 24, 16) & ((1 << T) - 1)]
     signs = [int(rng.integers(0, 2)) for _ in Vs[:-5]] + [1, 0, 1, 0, 1]
-    A = np.zeros((len(Vs), 32), dtype=np.int64)
+    A = np.zeros((len(Vs), 64), dtype=np.int64)
     for i, (v, s) in enumerate(zip(Vs, signs)):
         sg = -1 if s else 1
         for j in range(NB):
             A[i, j] = sg * (1024 + ((v >> (8 * j)) & 0xFF))
         A[i, NB] = -sg
+    A[:-1, 32:] = A[1:, :32]  # the second element of each row: the next value
     X = A @ B
     assert np.abs(X).max() < 1 << 23
-    assert not X[:, n:].any()  # padding columns
-    if True:
-        x = X[:, :n]
+    assert not X[:, 2 * n:].any()  # padding columns
+    for e in (0, 1):
+        x = X[:-1, e::2][:, :n]
+        vs, sgs = (Vs[:-1], signs[:-1]) if e == 0 else (Vs[1:], signs[1:])
         for q in range(n):
             bits = int(ib[q])
             M = (bits & 0x7FFFFF) | 0x800000
@@ -287,6 +289,46 @@ def test_tensor_core_split(sq, T, k):
             qq = qf + ((rem > half) | ((rem == half) & (qf & 1 == 1))).astype(np.int64)
             r = x[:, q] - qq * p[q]
             assert np.abs(r).max() <= 256, (T, q, int(p[q]))
-            for i, (v, s) in enumerate(zip(Vs, signs)):
+            for i, (v, s) in enumerate(zip(vs, sgs)):
                 sv = -v if s else v
                 assert (int(r[i]) - sv) % int(p[q]) == 0
+
+
+@pytest.mark.parametrize("T", [98, 134, 143, 180])
+def test_scaled_words_match_scaled_bits(sq, T):
+    """The split kernel's branch-free scaling (crt_scaled_words) gives the
+    same V and sign as ozaki_scaled_bits for normal, subnormal, zero, -0,
+    infinite and NaN elements, and scales from just above the element's
+    exponent to far beyond it (V = 0)."""
+    rng = G.rng_for(700 + T)
+    a = np.concatenate([G.wide_exponent(rng, 2000), G.spread_uniform(rng, 2000, -400, 400),
+                        np.zeros((4, 2), dtype=np.uint64)])
+    sub = G.uniform_full(rng, 200)
+    sub[:, 1] &= ~np.uint64(0x7FFF << 48)
+    sub[:100, 1] &= np.uint64(0x8000000000000000)  # subnormals whose leading one is in the low word
+    spec = np.zeros((3, 2), dtype=np.uint64)
+    spec[0, 1] = np.uint64(0x7FFF << 48)  # +inf
+    spec[1, 1] = np.uint64(0xFFFF << 48)  # -inf
+    spec[2, 1] = np.uint64(0x7FFF8 << 44)  # NaN
+    a = np.ascontiguousarray(np.concatenate([a, sub, spec]))
+    a[2005, 1] = np.uint64(1 << 63)  # -0
+    S = []
+    for w in a:
+        special = (int(w[1]) >> 48) & 0x7FFF == 0x7FFF
+        e = None if special else lead_exp(w)
+        r = int(rng.integers(0, 4))
+        if e is None:
+            S.append(-(1 << 29) if r == 0 else int(rng.integers(-100, 100)))
+        else:
+            S.append(e + 1 + [0, 1, int(rng.integers(0, 200)), int(rng.integers(0, 20000))][r])
+    S = np.array(S, dtype=np.int32)
+    S[:7] = -(1 << 29)  # empty rows
+    out = np.zeros((len(a), 7), dtype=np.uint32)
+    ref = np.zeros((len(a), 4), dtype=np.uint64)
+    sq.sq_crt_scaled_words(ctypes.c_int64(len(a)), P(a), P(S), ctypes.c_int(T), P(out), P(ref))
+    for i in range(len(a)):
+        v = sum(int(out[i, j]) << (32 * j) for j in range(6))
+        r = int(ref[i, 0]) | (int(ref[i, 1]) << 64) | (int(ref[i, 2]) << 128)
+        assert v == r, (i, hex(v), hex(r))
+        if r:
+            assert out[i, 6] == ref[i, 3]
