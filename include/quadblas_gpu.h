@@ -49,7 +49,8 @@ enum {
   QBLAS_ERR_NO_DEVICE = 5,
   QBLAS_ERR_MISALIGNED = 6,
   /* a wait inside an Ozaki qgemm kernel gave up (1 s without progress); the
-   * call's C holds NaN where a result was due */
+   * call's C is not valid (NaN, or left unwritten where the reconstruction
+   * itself gave up) */
   QBLAS_ERR_TIMEOUT = 7
 };
 
@@ -249,8 +250,8 @@ long long quadblas_debug_exact_rows(void);
 /* Device-side failures of device-pointer calls (no reference counterpart).
  * The part 3 calls return before their kernels run, so a failure found on
  * the GPU cannot be their return value: an Ozaki qgemm whose tensor-core
- * kernel gave up on a wait (1 s without progress) writes NaN to its C and
- * sets a flag of the current device.  After synchronising the streams of the
+ * kernels gave up on a wait (1 s without progress) leaves its C invalid (NaN
+ * or unwritten) and sets a flag of the current device.  After synchronising the streams of the
  * calls in question, quadblas_device_status returns QBLAS_ERR_TIMEOUT if the
  * flag is set (QBLAS_OK otherwise) and clears it when `clear` is nonzero.
  * Host-pointer calls (parts 1 and 2) check their own call and return

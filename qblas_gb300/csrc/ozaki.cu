@@ -271,19 +271,25 @@ __global__ void __launch_bounds__(kSplitThreads)
     }
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     uint32_t* out = reinterpret_cast<uint32_t*>(P.D + r * P.cols_pad + c);
-    for (int g = 0; 8 * g < nmod; ++g) {
-      uint32_t x[16];
-      tmem_ld16(tlane + 16 * g, x);
+    // groups of 8 moduli (16 columns), unrolled so that every modulus index is
+    // a constant and its p and 1/p come straight from the parameter bank
 #pragma unroll
-      for (int i = 0; i < 8; ++i) {
-        const int q = 8 * g + i;
-        if (q < nmod) {
-          const float p = tab.p[q], ip = tab.inv_p[q];
-          const float x0 = __uint_as_float(x[2 * i]), x1 = __uint_as_float(x[2 * i + 1]);
-          const float q0 = __fadd_rn(__fmaf_rn(x0, ip, 12582912.0f), -12582912.0f);
-          const float q1 = __fadd_rn(__fmaf_rn(x1, ip, 12582912.0f), -12582912.0f);
-          const __half2 h = __floats2half2_rn(__fmaf_rn(-q0, p, x0), __fmaf_rn(-q1, p, x1));
-          out[q * plane2] = *reinterpret_cast<const uint32_t*>(&h);
+    for (int g = 0; g < kCrtMaxMods / 8; ++g) {
+      if (8 * g < nmod) {
+        uint32_t x[16];
+        tmem_ld16(tlane + 16 * g, x);
+        const bool whole = 8 * g + 8 <= nmod;
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+          const int q = 8 * g + i;
+          if (whole || q < nmod) {
+            const float p = tab.p[q], ip = tab.inv_p[q];
+            const float x0 = __uint_as_float(x[2 * i]), x1 = __uint_as_float(x[2 * i + 1]);
+            const float q0 = __fadd_rn(__fmaf_rn(x0, ip, 12582912.0f), -12582912.0f);
+            const float q1 = __fadd_rn(__fmaf_rn(x1, ip, 12582912.0f), -12582912.0f);
+            const __half2 h = __floats2half2_rn(__fmaf_rn(-q0, p, x0), __fmaf_rn(-q1, p, x1));
+            out[q * plane2] = *reinterpret_cast<const uint32_t*>(&h);
+          }
         }
       }
     }
@@ -603,6 +609,7 @@ struct OzakiFoldParams {
   q128 alpha, beta;
   const int* err;
   int* report;  // set to 1 when err is (mapped host memory; may be null)
+  int T;        // CRT: operand truncation (the rounding is at 2^(S_i + F_j - 2T))
 };
 
 // Each thread folds four neighbouring columns j0..j0+3 of one row: one
@@ -653,89 +660,205 @@ __global__ void __launch_bounds__(256, 3) ozaki_fold_kernel(OzakiFoldParams P) {
   }
 }
 
-// CRT reconstruction per output (ozcrt.cuh).  The digit-product epilogue
-// stored y_q = (C_q mod p_q) u_q mod p_q per k pass (16 bits); y is linear in
-// C, so the passes' values add modulo p_q.  A thread takes two neighbouring
-// columns (one 32-bit copy per modulus and pass; a warp reads 128 contiguous
-// bytes of a plane, and all of a thread's copies are in flight at once),
-// accumulates the moduli in pairs, (y_q p_q' + y_q' p_q) M /
-// (p_q p_q'), into NW 64-bit word sums, then X = Y - Q M, one rounding at
-// 2^(S_i + F_j - 2T) and the reference epilogue.  The per-modulus constants
-// and the pair multiples of M are read from shared memory (broadcast).
+// Sums the residue planes of the k passes into the first pass's planes,
+// modulo p_q (y is linear in C), for `rows` rows from Y (each plane `plane`
+// values apart, a pass nmod planes), so that the reconstruction reads one
+// pass.
+__global__ void __launch_bounds__(256)
+    ozaki_crt_pass_sum_kernel(uint16_t* __restrict__ Y, int64_t rows, int64_t n_pad, int64_t plane, int nmod,
+                              int npass, const __grid_constant__ CrtTable tab) {
+  const int64_t per = rows * n_pad, total = (int64_t)nmod * per, pass = (int64_t)nmod * plane;
+  for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < total; x += (int64_t)gridDim.x * blockDim.x) {
+    const int q = (int)(x / per);
+    uint16_t* y = Y + q * plane + (x - q * per);
+    uint32_t v = *y;
+    for (int ps = 1; ps < npass; ++ps) v += y[ps * pass];
+    *y = (uint16_t)crt_mod(v, tab.mod[q].p, tab.mod[q].magic);
+  }
+}
+
+// CRT reconstruction on the tensor cores (ozcrt.cuh, "Reconstruction on the
+// tensor cores").  The product kernel stored y_q = (C_q mod p_q) u_q mod p_q
+// (16 bits; one k pass, or the passes summed by ozaki_crt_pass_sum_kernel).
+// Persistent CTAs of 4 warps walk tiles of 4 rows x 32 columns of C: warp w
+// takes row 4t + w, lane l column l (one tensor-memory lane per output).  A
+// tile's y values arrive by TMA (boxes of 32 columns x 4 rows x 16 moduli,
+// moduli beyond nmod zero-filled) two tiles ahead into two shared-memory
+// buffers.  Per tile each thread writes its output's y_q (fp16, exact) as an
+// operand row (K = 48) to tensor memory; one thread issues three MMAs
+// (M = 128, K = 16, N = crt_fold_n(NW)) against the byte table of M / p_q in
+// shared memory and waits for them; each thread then reads its column sums
+// (exact integers below 2^23, made integers by adding 2^23), 32 columns at a
+// time, assembles Y with carries (crt_fold_column), rounds X = Y - Q M once
+// at 2^(S_i + F_j - 2T) and applies the reference epilogue.  128
+// tensor-memory columns per CTA (D: [0, 64), A: [64, 88)), four CTAs per SM.
+// Every wait is bounded (1 s); on a timeout the CTA stops, waits (bounded)
+// for its copies in flight, records it in err[0] and frees its tensor memory
+// (its remaining outputs stay unwritten, and the call reports the timeout).
+constexpr int kFoldThreads = 128;
+constexpr int kFoldTmemCols = 128;
+constexpr int kFoldAcol = 64;
+constexpr int kFoldCtasPerSm = 4;
+constexpr int kFoldBoxBytes = 32 * 4 * 16 * 2;                 // one TMA box: 16 moduli of a tile
+constexpr int kFoldBufBytes = kFoldBoxBytes * (kCrtMaxMods / 16);  // 12 KiB: every modulus of a tile
+constexpr size_t kFoldSmem = 48 * 1024;  // table, two y buffers, barriers; keeps a fifth CTA off the SM
+
 template <int NW>
-__global__ void __launch_bounds__(256) ozaki_crt_fold_kernel(OzakiFoldParams P, const __grid_constant__ CrtTable tab) {
-  __shared__ __align__(16) uint32_t smod[kCrtMaxMods][8];  // p, magic, K, u, P24
-  __shared__ __align__(16) uint32_t spair[kCrtMaxMods / 2][kCrtMaxWords];
-  __shared__ __align__(16) uint32_t snegM[kCrtMaxWords];
-  extern __shared__ uint32_t sy[];  // this block's y values, [modulus][thread] (dynamic: n * 1 KB)
-  const int tid = threadIdx.y * 32 + threadIdx.x;
-  for (int i = tid; i < tab.n * 2; i += 256)
-    reinterpret_cast<uint4*>(smod)[i] = reinterpret_cast<const uint4*>(&tab.mod[i >> 1])[i & 1];
-  for (int i = tid; i < (kCrtMaxMods / 2) * kCrtMaxWords; i += 256) (&spair[0][0])[i] = (&tab.Mpair[0][0])[i];
-  if (tid < kCrtMaxWords) snegM[tid] = tab.negM[tid];
+__global__ void __launch_bounds__(kFoldThreads, kFoldCtasPerSm)
+    ozaki_crt_fold_tc_kernel(const __grid_constant__ CUtensorMap tmY, const __grid_constant__ OzakiFoldParams P,
+                             const __grid_constant__ CrtFoldTable tab) {
+  constexpr int N = crt_fold_n(NW);
+  extern __shared__ __align__(128) uint8_t fold_smem[];
+  uint8_t* sbase = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(fold_smem) + 1023) & ~(uintptr_t)1023);
+  uint8_t* ybuf = sbase;                                      // [2][48][4][32] u16
+  uint8_t* tbase = sbase + 2 * kFoldBufBytes;                 // the B table
+  uint64_t* bar = reinterpret_cast<uint64_t*>(tbase + kCrtFoldK * kCrtFoldMaxN * 2);  // mma, full[2]
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar + 3);
+  int* flag = reinterpret_cast<int*>(bar + 4);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nmod = tab.nmod, nboxes = (nmod + 15) / 16;
+  for (int i = threadIdx.x; i < N * kCrtFoldK / 8; i += kFoldThreads)
+    reinterpret_cast<uint4*>(tbase)[i] = reinterpret_cast<const uint4*>(tab.b)[i];
+  fence_proxy_async_smem();
+  if (threadIdx.x == 0) {
+    mbar_init(smem_u32(bar), 1);
+    mbar_init(smem_u32(bar + 1), 1);
+    mbar_init(smem_u32(bar + 2), 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(kFoldTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
-  const int64_t j0 = ((int64_t)blockIdx.x * 32 + threadIdx.x) * 2;
-  const int64_t i = (int64_t)blockIdx.y * 8 + threadIdx.y;
-  if (i >= P.m || j0 >= P.n) return;
-  const int n = tab.n;
-  const size_t plane = (size_t)P.m_pad * P.n_pad / 2;  // 32-bit words (two columns)
-  const size_t pass = (size_t)n * plane;
-  const uint32_t* src = reinterpret_cast<const uint32_t*>(P.Y + (size_t)i * P.n_pad + j0);
-  // every y of this thread's two columns into shared memory at once (one
-  // asynchronous 4-byte copy per modulus, all in flight together); with
-  // several k passes their values are added modulo p instead
-  if (P.npass == 1) {
-    for (int q = 0; q < n; ++q)
-      asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(&sy[q * 256 + tid])),
-                   "l"(src + q * plane)
-                   : "memory");
-    asm volatile("cp.async.wait_all;" ::: "memory");
-  } else {
-    for (int q = 0; q < n; ++q) {
-      const uint32_t p = smod[q][0], mg = smod[q][1];
-      uint32_t lo = 0, hi = 0;
-      for (int ps = 0; ps < P.npass; ++ps) {
-        const uint32_t w = __ldcs(src + ps * pass + q * plane);
-        lo += w & 0xFFFFu;
-        hi += w >> 16;
-      }
-      sy[q * 256 + tid] = crt_mod(lo, p, mg) | (crt_mod(hi, p, mg) << 16);
-    }
-  }
-  CrtAcc<NW> A0, A1;
-  crt_acc_init(A0);
-  crt_acc_init(A1);
-  for (int q0 = 0; q0 < n; q0 += 2) {
-    const int q1 = q0 + 1;
-    const uint32_t c0 = sy[q0 * 256 + tid], c1 = q1 < n ? sy[q1 * 256 + tid] : 0u;
-    const uint32_t p0 = smod[q0][0], P0 = smod[q0][4];
-    const uint32_t p1 = q1 < n ? smod[q1][0] : 1u, P1 = q1 < n ? smod[q1][4] : 0u;
-    uint32_t W[kCrtMaxWords];
-#pragma unroll
-    for (int v = 0; v < kCrtMaxWords / 4; ++v) {
-      const uint4 t = reinterpret_cast<const uint4*>(spair[q0 >> 1])[v];
-      W[4 * v] = t.x;
-      W[4 * v + 1] = t.y;
-      W[4 * v + 2] = t.z;
-      W[4 * v + 3] = t.w;
-    }
-    crt_acc_pair(A0, c0 & 0xFFFFu, c1 & 0xFFFFu, p0, p1, P0, P1, W);
-    crt_acc_pair(A1, c0 >> 16, c1 >> 16, p0, p1, P0, P1, W);
-  }
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+  const uint32_t tlane = tmem + ((uint32_t)(warp * 32) << 16);
+  constexpr uint32_t idesc = (1u << 4) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+  const uint32_t sb = smem_u32(tbase), lbo = (uint32_t)N * 16u;
   const bool failed = (P.err[0] | P.err[1] | P.err[2]) != 0;
-  if (failed && P.report && i == 0 && j0 == 0) *reinterpret_cast<volatile int*>(P.report) = 1;
-  const int Si = P.S[i];
-  const uint32_t fai = P.fa[i];
+  if (failed && P.report && blockIdx.x == 0 && threadIdx.x == 0) *reinterpret_cast<volatile int*>(P.report) = 1;
+
+  // tiles t = blockIdx.x, + gridDim.x, ...: (row tile, column tile), by counting
+  const int tiles_c = (int)((P.n + 31) / 32), tiles_r = (int)((P.m + 3) / 4);
+  const int step_r = (int)gridDim.x / tiles_c, step_c = (int)gridDim.x % tiles_c;
+  auto advance = [&](int& r_t, int& c_t) {
+    c_t += step_c;
+    r_t += step_r;
+    if (c_t >= tiles_c) {
+      c_t -= tiles_c;
+      ++r_t;
+    }
+  };
+  int tr = (int)blockIdx.x / tiles_c, tc = (int)blockIdx.x % tiles_c;  // this tile
+  int pr = tr, pc = tc;                                                 // the next tile to fetch
+  uint32_t issued = 0, used = 0;  // tiles fetched / consumed (buffer = count & 1)
+  auto fetch = [&]() {             // thread 0: the next tile's y into its buffer
+    const uint32_t b = issued & 1u, fb = smem_u32(bar + 1 + b), dst = smem_u32(ybuf + b * kFoldBufBytes);
+    mbar_expect_tx(fb, (uint32_t)(nboxes * kFoldBoxBytes));
+    for (int x = 0; x < nboxes; ++x) tma_load_3d(dst + x * kFoldBoxBytes, &tmY, fb, 32 * pc, 4 * pr, 16 * x);
+    ++issued;
+    advance(pr, pc);
+  };
+  if (threadIdx.x == 0) {
+    if (pr < tiles_r) fetch();
+    if (pr < tiles_r) fetch();
+  }
+  uint32_t phase = 0;
+  bool ok = true;
+  while (tr < tiles_r) {
+    const uint32_t b = used & 1u;
+    ok = mbar_wait(smem_u32(bar + 1 + b), (used >> 1) & 1u);
+    if (!__syncthreads_and(ok)) {
+      ok = false;
+      break;
+    }
+    ++used;
+    {
+      // y_q of this thread's output, fp16: the bits 0x6400 + y are 1024 + y
+      // (y <= 512), minus 1024 in pairs
+      const uint16_t* yb = reinterpret_cast<const uint16_t*>(ybuf + b * kFoldBufBytes) + warp * 32 + lane;
+      uint32_t a[24];
 #pragma unroll
-  for (int c = 0; c < 2; ++c) {
-    const int64_t j = j0 + c;
-    if (j < P.n && !(fai | P.fb[j])) {  // NaN / inf rows and columns: ozaki_special_kernel
-      q128* cp = P.Cout + i * P.sci + j * P.scj;
-      const q128 cold = *cp;
-      const q128 sum = failed ? q_nan() : crt_acc_round(c ? A1 : A0, snegM, Si + P.F[j] - 2 * tab.T);
+      for (int h = 0; h < 24; ++h) {
+        // moduli beyond nmod: zero (a buffer holds only the boxes fetched)
+        const uint32_t y0 = 2 * h < nmod ? (uint32_t)yb[(2 * h) * 128] : 0u;
+        const uint32_t y1 = 2 * h + 1 < nmod ? (uint32_t)yb[(2 * h + 1) * 128] : 0u;
+        const uint32_t w = (y0 | (y1 << 16)) + 0x64006400u;
+        const uint32_t k1024 = 0x64006400u;
+        const __half2 v =
+            __hsub2(*reinterpret_cast<const __half2*>(&w), *reinterpret_cast<const __half2*>(&k1024));
+        a[h] = *reinterpret_cast<const uint32_t*>(&v);
+      }
+      tmem_st16(tlane + kFoldAcol, *reinterpret_cast<uint32_t(*)[16]>(a));
+      tmem_st8(tlane + kFoldAcol + 16, *reinterpret_cast<uint32_t(*)[8]>(a + 16));
+    }
+    tmem_st_wait();
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();  // operand rows written; buffer b read; the last tile's sums read
+    const int64_t i = (int64_t)tr * 4 + warp, j = (int64_t)tc * 32 + lane;
+    advance(tr, tc);
+    if (threadIdx.x == 0) {
+      if (pr < tiles_r) fetch();  // into buffer b, two tiles ahead
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+      for (int kt = 0; kt < 3; ++kt)
+        mma_f16kind_ta(tmem, tmem + kFoldAcol + 8 * kt, smem_desc_noswizzle(sb + 2 * kt * lbo, lbo, 128), idesc,
+                       kt ? 1u : 0u);
+      mma_commit(smem_u32(bar));
+    }
+    const bool mine = i < P.m && j < P.n;
+    q128* cp = P.Cout + (mine ? i * P.sci + j * P.scj : 0);
+    q128 cold = q_zero(0);
+    int e = 0;
+    bool special = true;
+    if (mine) {
+      special = (P.fa[i] | P.fb[j]) != 0;  // NaN / inf rows and columns: ozaki_special_kernel
+      e = P.S[i] + P.F[j] - 2 * P.T;
+      if (!special) cold = ld_stream(cp);
+    }
+    if (threadIdx.x == 0) *flag = mbar_wait(smem_u32(bar), phase) ? 1 : 0;
+    phase ^= 1u;
+    __syncthreads();
+    if (!*flag) {
+      ok = false;
+      break;
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    CrtFoldAcc<NW> acc;
+    crt_fold_init(acc);
+#pragma unroll
+    for (int h = 0; h < (N + 31) / 32; ++h) {
+      uint32_t z[32];
+      tmem_ld16_nowait(tlane + 32 * h, z);
+      if (32 * h + 16 < N) tmem_ld16_nowait(tlane + 32 * h + 16, z + 16);
+      tmem_ld_wait();
+#pragma unroll
+      for (int c = 0; c < 32; ++c) {
+        const int w = 32 * h + c;
+        if (w < N) crt_fold_column(acc, w, __float_as_uint(__fadd_rn(__uint_as_float(z[c]), 8388608.0f)) - 0x4B000000u);
+      }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    if (mine && !special) {
+      const q128 sum = failed ? q_nan() : crt_fold_finish(acc, tab.negM, e);
       *cp = q_epilogue(P.alpha, sum, P.beta, cold);
     }
   }
+  if (!ok && threadIdx.x == 0) {
+    atomicExch(const_cast<int*>(P.err), 1);
+    if (P.report) *reinterpret_cast<volatile int*>(P.report) = 1;
+    // copies still in flight: the tiles fetched but not consumed (at most two)
+    for (uint32_t u = used; u < issued; ++u) mbar_wait(smem_u32(bar + 1 + (u & 1u)), (u >> 1) & 1u);
+  }
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kFoldTmemCols)
+                 : "memory");
 }
 
 // Outputs in a row of op(A) or a column of op(B) that holds a NaN or an
@@ -954,30 +1077,49 @@ static cudaError_t launch_crt_split(const CrtSplitTable& stab, cudaStream_t st, 
   return cudaGetLastError();
 }
 
-static cudaError_t launch_crt_fold(const CrtTable& tab, cudaStream_t st, const OzakiFoldParams& F) {
-  dim3 blk(32, 8), grid((unsigned)((F.n + 63) / 64), (unsigned)((F.m + 7) / 8));
-  const size_t dyn = (size_t)tab.n * 256 * 4;
+// The reconstruction of rows [0, F.m) of F (its Y already offset to the
+// band's first row; y_rows rows of each plane remain from there).
+static cudaError_t launch_crt_fold(const CrtFoldTable& ft, cudaStream_t st, const OzakiFoldParams& F,
+                                   int64_t y_rows) {
+  const int64_t tiles = ((F.m + 3) / 4) * ((F.n + 31) / 32);
+  if (tiles <= 0) return cudaSuccess;
+  if (tiles > INT32_MAX || ft.N != crt_fold_n(ft.nw)) return cudaErrorInvalidValue;
+  // y planes as a 3-D tensor (columns, rows, moduli) of 16-bit values; boxes
+  // of 32 columns x 4 rows x 16 moduli (the moduli beyond nmod read as zero)
+  CUtensorMap map;
+  {
+    EncodeTiledFn fn = encode_fn();
+    if (!fn) return cudaErrorNotSupported;
+    cuuint64_t dims[3] = {(cuuint64_t)F.n_pad, (cuuint64_t)y_rows, (cuuint64_t)ft.nmod};
+    cuuint64_t strides[2] = {(cuuint64_t)F.n_pad * 2, (cuuint64_t)F.m_pad * F.n_pad * 2};
+    cuuint32_t box[3] = {32, 4, 16};
+    cuuint32_t estr[3] = {1, 1, 1};
+    if (fn(&map, CU_TENSOR_MAP_DATA_TYPE_UINT16, 3, const_cast<uint16_t*>(F.Y), dims, strides, box, estr,
+           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+      return cudaErrorInvalidValue;
+  }
   static std::atomic<bool> attr_set[64];
   int dev = 0;
   cudaGetDevice(&dev);
   if (dev >= 0 && dev < 64 && !attr_set[dev].load(std::memory_order_acquire)) {
-    const int mx = kCrtMaxMods * 256 * 4;
     cudaError_t e;
-    if ((e = cudaFuncSetAttribute(ozaki_crt_fold_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx)) !=
-            cudaSuccess ||
-        (e = cudaFuncSetAttribute(ozaki_crt_fold_kernel<10>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx)) !=
-            cudaSuccess ||
-        (e = cudaFuncSetAttribute(ozaki_crt_fold_kernel<12>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx)) !=
-            cudaSuccess)
+    if ((e = cudaFuncSetAttribute(ozaki_crt_fold_tc_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)kFoldSmem)) != cudaSuccess ||
+        (e = cudaFuncSetAttribute(ozaki_crt_fold_tc_kernel<10>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)kFoldSmem)) != cudaSuccess ||
+        (e = cudaFuncSetAttribute(ozaki_crt_fold_tc_kernel<12>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)kFoldSmem)) != cudaSuccess)
       return e;
     attr_set[dev].store(true, std::memory_order_release);
   }
-  if (tab.nw <= 8)
-    ozaki_crt_fold_kernel<8><<<grid, blk, dyn, st>>>(F, tab);
-  else if (tab.nw <= 10)
-    ozaki_crt_fold_kernel<10><<<grid, blk, dyn, st>>>(F, tab);
+  const unsigned grid = (unsigned)std::min<int64_t>(tiles, kFoldCtasPerSm * (int64_t)device_sm_count());
+  if (ft.nw <= 8)
+    ozaki_crt_fold_tc_kernel<8><<<grid, kFoldThreads, kFoldSmem, st>>>(map, F, ft);
+  else if (ft.nw <= 10)
+    ozaki_crt_fold_tc_kernel<10><<<grid, kFoldThreads, kFoldSmem, st>>>(map, F, ft);
   else
-    ozaki_crt_fold_kernel<12><<<grid, blk, dyn, st>>>(F, tab);
+    ozaki_crt_fold_tc_kernel<12><<<grid, kFoldThreads, kFoldSmem, st>>>(map, F, ft);
   return cudaGetLastError();
 }
 
@@ -989,7 +1131,11 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scr
   CrtTable tab;
   const bool crt = ozaki_crt_table(scheme, digits, bits, g.k, tab);
   CrtSplitTable stab;
-  if (crt) crt_split_table(tab, stab);
+  CrtFoldTable ftab;
+  if (crt) {
+    crt_split_table(tab, stab);
+    crt_fold_table(tab, ftab);
+  }
   OzakiLayout L = ozaki_layout(g.m, g.n, g.k, digits, bits, crt ? tab.n : 0);
   char* base = static_cast<char*>(scratch);
   int* S = reinterpret_cast<int*>(base + L.off_S);
@@ -1111,6 +1257,7 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scr
   F2.alpha = g.alpha; F2.beta = g.beta;
   F2.err = err;
   F2.report = report;
+  F2.T = crt ? tab.T : 0;
   if ((g.m + 7) / 8 > 65535) return cudaErrorInvalidConfiguration;
   const bool fold_banded = ov && ov->band_done && g.scj == 1 && g.sci >= g.n && g.m >= 64;
   bool c_waited = false;
@@ -1129,7 +1276,14 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scr
     Fb.A = g.A + i0 * g.sai;
     Fb.Cout = g.C + i0 * g.sci;
     if (crt) {
-      if ((ee = launch_crt_fold(tab, st, Fb)) != cudaSuccess) return ee;
+      if (L.npass > 1) {  // the k passes' residues summed into the first
+        const int64_t total = (int64_t)tab.n * Fb.m * L.n_pad;
+        const unsigned gb = (unsigned)std::min<int64_t>((total + 255) / 256, (int64_t)sms * 8);
+        ozaki_crt_pass_sum_kernel<<<gb, 256, 0, st>>>(Yq + (size_t)i0 * L.n_pad, Fb.m, L.n_pad,
+                                                       L.m_pad * L.n_pad, tab.n, L.npass, tab);
+        if ((ee = cudaGetLastError()) != cudaSuccess) return ee;
+      }
+      if ((ee = launch_crt_fold(ftab, st, Fb, L.m_pad - i0)) != cudaSuccess) return ee;
     } else {
       launch_fold(L.b, st, Fb);
     }

@@ -391,21 +391,11 @@ QB_HD void crt_acc_pair(CrtAcc<NW>& A, uint32_t y0, uint32_t y1, uint32_t p0, ui
   for (int w = 0; w < NW; ++w) A.a[w] += (uint64_t)z * W[w];
 }
 
-// X = Y - Q M (two's complement modulo 2^(32 NW); |X| < M / 8), and
-// X 2^e rounded to binary128 (RNE).
+// X 2^e rounded to binary128 (RNE), X in two's complement over NW words.
 template <int NW>
-QB_HD q128 crt_acc_round(const CrtAcc<NW>& A, const uint32_t* negM, int e) {
+QB_HD q128 crt_round_x(uint32_t (&X)[NW], int e) {
   static_assert(NW % 2 == 0 && NW >= 8, "reconstruction of 8, 10 or 12 words");
   constexpr int H = NW / 2;
-  const uint64_t Q = (A.q + (1u << 23)) >> 24;
-  uint32_t X[NW];
-  uint64_t c = 0;
-#pragma unroll
-  for (int w = 0; w < NW; ++w) {
-    c += A.a[w] + Q * negM[w];
-    X[w] = (uint32_t)c;
-    c >>= 32;
-  }
   const uint32_t neg = X[NW - 1] >> 31;
   if (neg) {
     uint64_t b = 1;
@@ -432,6 +422,135 @@ QB_HD q128 crt_acc_round(const CrtAcc<NW>& A, const uint32_t* negM, int e) {
 #pragma unroll
   for (int i = 0; i < H - 4; ++i) sticky = sticky || (i < drop && V[i] != 0);
   return round_pack(neg, m, sticky, e + 64 * drop);
+}
+
+// X = Y - Q M (two's complement modulo 2^(32 NW); |X| < M / 8), and
+// X 2^e rounded to binary128 (RNE).
+template <int NW>
+QB_HD q128 crt_acc_round(const CrtAcc<NW>& A, const uint32_t* negM, int e) {
+  const uint64_t Q = (A.q + (1u << 23)) >> 24;
+  uint32_t X[NW];
+  uint64_t c = 0;
+#pragma unroll
+  for (int w = 0; w < NW; ++w) {
+    c += A.a[w] + Q * negM[w];
+    X[w] = (uint32_t)c;
+    c >>= 32;
+  }
+  return crt_round_x<NW>(X, e);
+}
+
+// ---------------------------------------------------------------------------
+// Reconstruction on the tensor cores: the table (host) and the column sums
+// ---------------------------------------------------------------------------
+// Y = sum_q y_q M / p_q with M / p_q = sum_w W_qw 256^w (bytes) is
+// Y = sum_w Z_w 256^w, Z_w = sum_q y_q W_qw: a product of the reduced
+// residues y (one MMA operand row per output, fp16, y <= 512) and the bytes
+// W (fp16) with Z_w <= 48 * 512 * 255 < 2^23, exact in fp32.  Two more
+// columns carry the bytes of P24_q = round(2^24 / p_q) (< 2^16), whose sums
+// give Q as crt_acc_round does.  nbytes = 4 NW - 1 bytes hold M / p_q <
+// 2^(32 NW) / 257.  Columns: bytes 0 .. nbytes-1, then P24's low and high
+// byte; N = nbytes + 2 rounded up to 16.
+// MMA width of the reconstruction for NW words: nbytes + 2 columns rounded
+// up to 16.
+QB_HD constexpr int crt_fold_n(int NW) { return (4 * NW + 1 + 15) / 16 * 16; }
+
+constexpr int kCrtFoldK = kCrtMaxMods;  // 48: K of the MMA (moduli, zero beyond nmod)
+constexpr int kCrtFoldMaxN = 64;
+
+struct alignas(16) CrtFoldTable {
+  int nmod, N, nbytes, nw;
+  uint32_t negM[kCrtMaxWords];
+  uint32_t p[kCrtMaxMods], magic[kCrtMaxMods];
+  // B (N rows, K = modulus) in the shared-memory layout of a K-major operand
+  // without swizzle: the 16 bytes of (row n, k-block kb) at kb * (N * 16) + n * 16
+  uint16_t b[kCrtFoldK * kCrtFoldMaxN];
+};
+
+inline void crt_fold_table(const CrtTable& tab, CrtFoldTable& ft) {
+  ft = CrtFoldTable();
+  ft.nmod = tab.n;
+  ft.nw = tab.nw;
+  ft.nbytes = 4 * tab.nw - 1;
+  ft.N = crt_fold_n(tab.nw);
+  for (int w = 0; w < kCrtMaxWords; ++w) ft.negM[w] = tab.negM[w];
+  for (int q = 0; q < tab.n; ++q) {
+    ft.p[q] = tab.mod[q].p;
+    ft.magic[q] = tab.mod[q].magic;
+  }
+  for (int q = 0; q < tab.n; ++q) {
+    uint32_t Mq[kCrtMaxWords + 2] = {1};
+    for (int r = 0; r < tab.n; ++r)
+      if (r != q) crt_big_mul_small(Mq, kCrtMaxWords + 2, tab.mod[r].p);
+    for (int n = 0; n < ft.N; ++n) {
+      int v = 0;
+      if (n < ft.nbytes)
+        v = (int)((Mq[n / 4] >> (8 * (n % 4))) & 0xFFu);
+      else if (n == ft.nbytes)
+        v = (int)(tab.mod[q].P24 & 0xFFu);
+      else if (n == ft.nbytes + 1)
+        v = (int)(tab.mod[q].P24 >> 8);
+      ft.b[(q / 8) * (ft.N * 8) + n * 8 + (q % 8)] = crt_half_bits(v);
+    }
+  }
+}
+
+// The reconstruction from the column sums, one column at a time (columns in
+// order; w a constant once unrolled): byte columns w < nbytes = 4 NW - 1 add
+// Z_w 256^w into Y with carries, the two columns after them make
+// S = sum_q y_q P24_q; then Q, X = Y - Q M, and X rounded at 2^e.
+template <int NW>
+struct CrtFoldAcc {
+  uint64_t t;     // carry into the current word
+  uint32_t X[NW];
+  uint32_t S;
+};
+
+template <int NW>
+QB_HD void crt_fold_init(CrtFoldAcc<NW>& A) {
+  A.t = 0;
+  A.S = 0;
+#pragma unroll
+  for (int i = 0; i < NW; ++i) A.X[i] = 0;
+}
+
+template <int NW>
+QB_HD void crt_fold_column(CrtFoldAcc<NW>& A, int w, uint32_t z) {
+  constexpr int nbytes = 4 * NW - 1;
+  if (w < nbytes) {
+    A.t += (uint64_t)z << (8 * (w & 3));
+    if ((w & 3) == 3) {
+      A.X[w >> 2] = (uint32_t)A.t;
+      A.t >>= 32;
+    }
+  } else if (w == nbytes) {
+    A.S += z;
+  } else if (w == nbytes + 1) {
+    A.S += z << 8;
+  }
+}
+
+template <int NW>
+QB_HD q128 crt_fold_finish(CrtFoldAcc<NW>& A, const uint32_t* negM, int e) {
+  A.X[NW - 1] = (uint32_t)A.t;  // byte 4 NW - 2 ended the last word
+  const uint64_t Q = (A.S + (1u << 23)) >> 24;
+  uint64_t c = 0;
+#pragma unroll
+  for (int w = 0; w < NW; ++w) {
+    c += A.X[w] + Q * negM[w];
+    A.X[w] = (uint32_t)c;
+    c >>= 32;
+  }
+  return crt_round_x<NW>(A.X, e);
+}
+
+// All columns at once (host form): Z[0 .. nbytes + 1].
+template <int NW>
+QB_HD q128 crt_fold_columns(const uint32_t* Z, int nbytes, const uint32_t* negM, int e) {
+  CrtFoldAcc<NW> A;
+  crt_fold_init(A);
+  for (int w = 0; w < nbytes + 2; ++w) crt_fold_column(A, w, Z[w]);
+  return crt_fold_finish(A, negM, e);
 }
 
 // Host and test form: the binary128 value of X 2^e for the residue sums

@@ -525,8 +525,23 @@ QB_HD q128 q_sqrt(q128 a) {
 // level3.hpp:107).  fma(1, s, t) is s + t with one rounding, so alpha == 1
 // takes the cheaper addition; the result bits are identical.
 QB_HD q128 q_epilogue(q128 alpha, q128 sum, q128 beta, q128 y) {
+  const bool one = alpha.hi == 0x3FFF000000000000ull && alpha.lo == 0;
+  if (q_iszero(beta) && q_bexp(y) != kExpField) {
+    // beta * y is a zero of sign sb ^ sy (y finite), so fma(alpha, sum, t)
+    // is the rounded product alpha * sum, except where that product is
+    // exactly zero: then IEEE addition of two zeros gives -0 only for two -0
+    // (round to nearest).  NaN and infinite products are unchanged by a zero.
+    const uint32_t st = q_sign(beta) ^ q_sign(y);
+    if (one) {
+      if (q_isnan(sum)) return q_nan();
+      return q_iszero(sum) ? q_zero(q_sign(sum) & st) : sum;
+    }
+    const q128 p = q_mul(alpha, sum);
+    if (q_bexp(p) == kExpField) return p;
+    return (q_iszero(alpha) || q_iszero(sum)) ? q_zero(q_sign(p) & st) : p;
+  }
   q128 t = q_mul(beta, y);
-  if (alpha.hi == 0x3FFF000000000000ull && alpha.lo == 0) return q_add(sum, t);
+  if (one) return q_add(sum, t);
   return q_fma(alpha, sum, t);
 }
 

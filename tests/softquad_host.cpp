@@ -26,6 +26,9 @@ void sq_add_n(int64_t n, const q128* a, const q128* b, q128* out) {
 void sq_sub_n(int64_t n, const q128* a, const q128* b, q128* out) {
   for (int64_t i = 0; i < n; ++i) out[i] = qb::q_sub(a[i], b[i]);
 }
+void sq_epilogue_n(int64_t n, const q128* alpha, const q128* sum, const q128* beta, const q128* y, q128* out) {
+  for (int64_t i = 0; i < n; ++i) out[i] = qb::q_epilogue(alpha[i], sum[i], beta[i], y[i]);
+}
 void sq_sqrt_n(int64_t n, const q128* a, q128* out) {
   for (int64_t i = 0; i < n; ++i) out[i] = qb::q_sqrt(a[i]);
 }
@@ -311,6 +314,43 @@ void sq_crt_scaled_words(int64_t n, const q128* a, const int* S, int T, uint32_t
     qb::ozaki_scaled_bits(a[i], S[i], T, ref[4 * i], ref[4 * i + 1], ref[4 * i + 2], neg2);
     ref[4 * i + 3] = neg2;
   }
+}
+
+// The tensor-core reconstruction for outputs whose residue sums are C[i][q]
+// (one pass): y_q reduced as the product kernel stores it, the column sums
+// Z_w = sum_q y_q B[w][q] taken from the fp16 table (decoded here, exact
+// integers), then crt_fold_columns; also returns the largest Z seen.
+static int half_int(uint16_t h) {
+  if ((h & 0x7FFF) == 0) return 0;
+  const int e = (h >> 10) & 0x1F, m = (h & 0x3FF) | 0x400;
+  const int v = e >= 25 ? m << (e - 25) : m >> (25 - e);
+  return (h & 0x8000) ? -v : v;
+}
+int sq_crt_fold_tc(int64_t n, const int32_t* C, const int* e, int T, int64_t k, q128* out, int64_t* zmax) {
+  qb::CrtTable t;
+  if (!qb::crt_build(T, k, t)) return 0;
+  qb::CrtFoldTable ft;
+  qb::crt_fold_table(t, ft);
+  *zmax = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    uint32_t y[qb::kCrtMaxMods] = {0};
+    for (int q = 0; q < t.n; ++q) y[q] = qb::crt_y(qb::crt_reduce(C[i * t.n + q], t.mod[q]), t.mod[q]);
+    uint32_t Z[qb::kCrtFoldMaxN] = {0};
+    for (int col = 0; col < ft.N; ++col) {
+      int64_t z = 0;
+      for (int q = 0; q < qb::kCrtFoldK; ++q)
+        z += (int64_t)y[q] * half_int(ft.b[(q / 8) * (ft.N * 8) + col * 8 + (q % 8)]);
+      if (z > *zmax) *zmax = z;
+      Z[col] = (uint32_t)z;
+    }
+    if (ft.nw <= 8)
+      out[i] = qb::crt_fold_columns<8>(Z, ft.nbytes, ft.negM, e[i]);
+    else if (ft.nw <= 10)
+      out[i] = qb::crt_fold_columns<10>(Z, ft.nbytes, ft.negM, e[i]);
+    else
+      out[i] = qb::crt_fold_columns<12>(Z, ft.nbytes, ft.negM, e[i]);
+  }
+  return t.n;
 }
 
 // Reconstruction of X 2^e[i] from C[i][q] (one pass) for each output i.

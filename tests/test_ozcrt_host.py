@@ -332,3 +332,37 @@ def test_scaled_words_match_scaled_bits(sq, T):
         assert v == r, (i, hex(v), hex(r))
         if r:
             assert out[i, 6] == ref[i, 3]
+
+
+@pytest.mark.parametrize("T,k", [(100, 64), (134, 4096), (143, 4096), (170, 1 << 20)])
+def test_tensor_core_reconstruction(sq, T, k):
+    """The reconstruction as the tensor cores compute it (ozaki_crt_fold_tc_kernel):
+    column sums of the reduced residues times the bytes of M / p_q (and of
+    round(2^24 / p_q)) from the fp16 table, assembled with carries, equal
+    X 2^e correctly rounded, and every column sum stays below 2^23 (exact in
+    the fp32 accumulation and in the 2^23 conversion)."""
+    n, nw, mods, _, _ = table(sq, T, k)
+    ps = [m[0] for m in mods]
+    M = math.prod(ps)
+    rng = np.random.default_rng(T + 5)
+    Xs = [0, 1, -1, M // 8 - 1, -(M // 8) + 1]
+    for _ in range(300):
+        b = int(rng.integers(1, M.bit_length() - 4))
+        x = (int(rng.integers(0, 1 << 62)) << max(0, b - 62)) % (1 << b) | (1 << (b - 1))
+        Xs.append(x if rng.integers(2) else -x)
+    Xs = [x for x in Xs if abs(x) < M // 8]
+    C = np.zeros((len(Xs), n), dtype=np.int32)
+    for i, x in enumerate(Xs):
+        for q, p in enumerate(ps):
+            C[i, q] = x % p + p * int(rng.integers(-(1 << 29) // p, (1 << 29) // p - 1))
+    e = rng.integers(-2 * T - 50, -2 * T + 50, size=len(Xs)).astype(np.int32)
+    out = np.zeros((len(Xs), 2), dtype=np.uint64)
+    ref = np.zeros((len(Xs), 2), dtype=np.uint64)
+    zmax = ctypes.c_int64(0)
+    assert sq.sq_crt_fold_tc(ctypes.c_int64(len(Xs)), P(C), P(e), ctypes.c_int(T), ctypes.c_int64(k), P(out),
+                             ctypes.byref(zmax)) == n
+    sq.sq_crt_reconstruct(ctypes.c_int64(len(Xs)), P(C), P(e), ctypes.c_int(T), ctypes.c_int64(k), P(ref))
+    assert 0 < zmax.value < 1 << 23
+    assert (out == ref).all()
+    for i, x in enumerate(Xs):
+        assert (int(out[i, 0]), int(out[i, 1])) == fraction_to_q(Fraction(x) * Fraction(2) ** int(e[i])), (i, x)

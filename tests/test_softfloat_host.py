@@ -83,3 +83,33 @@ def test_wide_accumulator_correctly_rounded(O, sq):
                            y.ctypes.data_as(ctypes.c_void_p), ctypes.c_int64(1), ctypes.c_int64(nsplit),
                            g.ctypes.data_as(ctypes.c_void_p))
             assert Q.same_bits(g, R).all(), (t, kind, nsplit, O.ulp_err(g, R, r))
+
+
+def test_epilogue_fast_paths(O, sq):
+    """y = fma(alpha, sum, beta * y) (the reference epilogue, level2.hpp:48,
+    level3.hpp:107) with its shortcuts for beta = +-0 (beta * y a signed zero
+    when y is finite; alpha = 1 or any alpha) against the oracle's fma and mul:
+    signed zeros, infinities, NaNs, subnormals and underflowing products."""
+    rng = np.random.default_rng(31)
+    N = 30000
+    vals = V.mixed(rng, N)
+    special = Q.from_double([0.0, -0.0, np.inf, -np.inf, np.nan, 1.0, -1.0, 2.0 ** -1070, -(2.0 ** -1070)])
+    tiny = V.finite(rng, 64, -16400, -16300)
+    pool = np.concatenate([vals, special, tiny])
+    pick = lambda: pool[rng.integers(0, len(pool), N)]  # noqa: E731
+    zeros = Q.from_double(rng.choice([0.0, -0.0], N))
+    ones = Q.from_double(np.ones(N))
+    for alpha, beta in [(ones, zeros), (pick(), zeros), (ones, pick()), (pick(), pick())]:
+        s_, y = pick(), pick()
+        s_[:50] = Q.from_double(rng.choice([0.0, -0.0], 50))
+        got = np.zeros((N, 2), dtype=np.uint64)
+        P = lambda a: np.ascontiguousarray(a).ctypes.data_as(ctypes.c_void_p)  # noqa: E731
+        a_, b_ = np.ascontiguousarray(alpha), np.ascontiguousarray(beta)
+        sq.sq_epilogue_n(ctypes.c_int64(N), P(a_), P(s_), P(b_), P(y), got.ctypes.data_as(ctypes.c_void_p))
+        ref = O.fma(a_, s_, O.mul(b_, y))
+        nan_ref = ((ref[:, 1] >> np.uint64(48)) & np.uint64(0x7FFF) == 0x7FFF) & \
+                  (((ref[:, 1] & np.uint64((1 << 48) - 1)) | ref[:, 0]) != 0)
+        nan_got = ((got[:, 1] >> np.uint64(48)) & np.uint64(0x7FFF) == 0x7FFF) & \
+                  (((got[:, 1] & np.uint64((1 << 48) - 1)) | got[:, 0]) != 0)
+        assert (nan_ref == nan_got).all()
+        assert Q.same_bits(got[~nan_ref], ref[~nan_ref]).all()
