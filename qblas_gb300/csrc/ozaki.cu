@@ -839,12 +839,12 @@ __global__ void __launch_bounds__(kFoldThreads, kFoldCtasPerSm)
 #pragma unroll
       for (int c = 0; c < 32; ++c) {
         const int w = 32 * h + c;
-        if (w < N) crt_fold_column(acc, w, __float_as_uint(__fadd_rn(__uint_as_float(z[c]), 8388608.0f)) - 0x4B000000u);
+        if (w < N) crt_fold_column(acc, w, __float_as_uint(__fadd_rn(__uint_as_float(z[c]), 8388608.0f)), true);
       }
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     if (mine && !special) {
-      const q128 sum = failed ? q_nan() : crt_fold_finish(acc, tab.negM, e);
+      const q128 sum = failed ? q_nan() : crt_fold_finish(acc, tab.negM, e, true);
       *cp = q_epilogue(P.alpha, sum, P.beta, cold);
     }
   }

@@ -392,36 +392,80 @@ QB_HD void crt_acc_pair(CrtAcc<NW>& A, uint32_t y0, uint32_t y1, uint32_t p0, ui
 }
 
 // X 2^e rounded to binary128 (RNE), X in two's complement over NW words.
+// The magnitude's highest nonzero word k (a warp's outputs mostly share it)
+// gives a window of five words, normalised by one count of leading zeros:
+// the significand's 113 bits, the round bit and the sticky bits are fixed
+// positions of it.  Results below the normal range or above it take the
+// general rounding (round_pack).
 template <int NW>
 QB_HD q128 crt_round_x(uint32_t (&X)[NW], int e) {
   static_assert(NW % 2 == 0 && NW >= 8, "reconstruction of 8, 10 or 12 words");
-  constexpr int H = NW / 2;
-  const uint32_t neg = X[NW - 1] >> 31;
-  if (neg) {
-    uint64_t b = 1;
+  const uint32_t neg = X[NW - 1] >> 31, mask = 0u - neg;
+  {
+    uint64_t c = neg;
 #pragma unroll
     for (int w = 0; w < NW; ++w) {
-      b += (uint32_t)~X[w];
-      X[w] = (uint32_t)b;
-      b >>= 32;
+      c += (uint32_t)(X[w] ^ mask);
+      X[w] = (uint32_t)c;
+      c >>= 32;
     }
   }
-  uint64_t V[H];
+  uint32_t h4 = 0, h3 = 0, h2 = 0, h1 = 0, h0 = 0;
+  bool below = false;
+  int k = -1;
 #pragma unroll
-  for (int i = 0; i < H; ++i) V[i] = (uint64_t)X[2 * i] | ((uint64_t)X[2 * i + 1] << 32);
-  // the top four 64-bit words holding the leading one; lower words go to sticky
-  u256 m = u256_make(V[3], V[2], V[1], V[0]);
-  int drop = 0;
+  for (int w = NW - 1; w >= 0; --w) {
+    if (k < 0 && X[w] != 0) {
+      k = w;
+      h4 = X[w];
+      h3 = w >= 1 ? X[w - 1] : 0u;
+      h2 = w >= 2 ? X[w - 2] : 0u;
+      h1 = w >= 3 ? X[w - 3] : 0u;
+      h0 = w >= 4 ? X[w - 4] : 0u;
 #pragma unroll
-  for (int d = 1; d <= H - 4; ++d)
-    if (V[3 + d] != 0) {
-      m = u256_make(V[3 + d], V[2 + d], V[1 + d], V[d]);
-      drop = d;
+      for (int v = 0; v < w - 4; ++v) below = below || X[v] != 0;
     }
-  bool sticky = false;
+  }
+  if (k < 0) return q_zero(neg);
+  const int lz = clz32(h4);
+  // the window shifted left by lz: its top bit is X's leading one
+  const uint32_t g4 = fshl32_any(h3, h4, lz), g3 = fshl32_any(h2, h3, lz), g2 = fshl32_any(h1, h2, lz),
+                 g1 = fshl32_any(h0, h1, lz), g0 = h0 << lz;
+  const int E = e + 32 * k + 31 - lz;  // exponent of the leading one
+  const int be = E + kBias;
+  if (be <= 0 || be >= kExpField) {  // subnormal or overflowing result: the general rounding
+    uint64_t V[NW / 2];
 #pragma unroll
-  for (int i = 0; i < H - 4; ++i) sticky = sticky || (i < drop && V[i] != 0);
-  return round_pack(neg, m, sticky, e + 64 * drop);
+    for (int i = 0; i < NW / 2; ++i) V[i] = (uint64_t)X[2 * i] | ((uint64_t)X[2 * i + 1] << 32);
+    u256 m = u256_make(V[3], V[2], V[1], V[0]);
+    int drop = 0;
+#pragma unroll
+    for (int d = 1; d <= NW / 2 - 4; ++d)
+      if (V[3 + d] != 0) {
+        m = u256_make(V[3 + d], V[2 + d], V[1 + d], V[d]);
+        drop = d;
+      }
+    bool sticky = false;
+#pragma unroll
+    for (int i = 0; i < NW / 2 - 4; ++i) sticky = sticky || (i < drop && V[i] != 0);
+    return round_pack(neg, m, sticky, e + 64 * drop);
+  }
+  // significand: g4, g3, g2 and the top 17 bits of g1; round bit: bit 14 of g1
+  uint64_t rh = ((uint64_t)g4 << 17) | (g3 >> 15);
+  uint64_t rl = ((uint64_t)((g3 << 17) | (g2 >> 15)) << 32) | (uint32_t)((g2 << 17) | (g1 >> 15));
+  const bool rbit = (g1 >> 14) & 1u;
+  const bool st = below || (g1 & 0x3FFFu) != 0 || g0 != 0;
+  int bexp = be;
+  if (rbit && (st || (rl & 1))) {
+    rl += 1;
+    if (rl == 0) rh += 1;
+    if (rh >> 49) {  // carried into bit 113: the significand is 2^113
+      rh >>= 1;
+      bexp += 1;
+      if (bexp >= kExpField) return q_inf(neg);
+    }
+  }
+  return make_q(((uint64_t)neg << 63) | ((uint64_t)bexp << 48) | (rh & kMantHiMask), rl);
 }
 
 // X = Y - Q M (two's complement modulo 2^(32 NW); |X| < M / 8), and
@@ -514,30 +558,47 @@ QB_HD void crt_fold_init(CrtFoldAcc<NW>& A) {
   for (int i = 0; i < NW; ++i) A.X[i] = 0;
 }
 
+// t + (uint64_t)a * b in one wide multiply-add
+QB_HD uint64_t crt_mad_wide(uint32_t a, uint32_t b, uint64_t t) {
+#if defined(__CUDA_ARCH__)
+  uint64_t r;
+  asm("mad.wide.u32 %0, %1, %2, %3;" : "=l"(r) : "r"(a), "r"(b), "l"(t));
+  return r;
+#else
+  return t + (uint64_t)a * b;
+#endif
+}
+
+// Byte column w with sum z.  bias != 0: z is given as 2^23 + z (the bits of
+// the fp32 value z + 2^23) and the 2^23 of each column is taken off once per
+// word.
 template <int NW>
-QB_HD void crt_fold_column(CrtFoldAcc<NW>& A, int w, uint32_t z) {
+QB_HD void crt_fold_column(CrtFoldAcc<NW>& A, int w, uint32_t z, bool bias = false) {
   constexpr int nbytes = 4 * NW - 1;
   if (w < nbytes) {
-    A.t += (uint64_t)z << (8 * (w & 3));
+    A.t = crt_mad_wide(z, 1u << (8 * (w & 3)), A.t);
     if ((w & 3) == 3) {
+      if (bias) A.t -= 0x4B000000ull * 0x01010101ull;
       A.X[w >> 2] = (uint32_t)A.t;
       A.t >>= 32;
     }
   } else if (w == nbytes) {
-    A.S += z;
+    A.S += bias ? z - 0x4B000000u : z;
   } else if (w == nbytes + 1) {
-    A.S += z << 8;
+    A.S += (bias ? z - 0x4B000000u : z) << 8;
   }
 }
 
 template <int NW>
-QB_HD q128 crt_fold_finish(CrtFoldAcc<NW>& A, const uint32_t* negM, int e) {
-  A.X[NW - 1] = (uint32_t)A.t;  // byte 4 NW - 2 ended the last word
-  const uint64_t Q = (A.S + (1u << 23)) >> 24;
+QB_HD q128 crt_fold_finish(CrtFoldAcc<NW>& A, const uint32_t* negM, int e, bool bias = false) {
+  // byte 4 NW - 2 ended the last word (three columns of it)
+  if (bias) A.t -= 0x4B000000ull * 0x00010101ull;
+  A.X[NW - 1] = (uint32_t)A.t;
+  const uint32_t Q = (A.S + (1u << 23)) >> 24;  // below 2^8
   uint64_t c = 0;
 #pragma unroll
   for (int w = 0; w < NW; ++w) {
-    c += A.X[w] + Q * negM[w];
+    c = crt_mad_wide(Q, negM[w], c + A.X[w]);
     A.X[w] = (uint32_t)c;
     c >>= 32;
   }

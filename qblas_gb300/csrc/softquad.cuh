@@ -75,6 +75,23 @@ QB_HD void mul64(uint64_t a, uint64_t b, uint64_t& hi, uint64_t& lo) {
 #endif
 }
 
+QB_HD int clz32(uint32_t x) {  // x != 0
+#if defined(__CUDA_ARCH__)
+  return __clz((int)x);
+#else
+  return __builtin_clz(x);
+#endif
+}
+
+// ((hi:lo) << s) >> 32 for 0 <= s < 32
+QB_HD uint32_t fshl32_any(uint32_t lo, uint32_t hi, int s) {
+#if defined(__CUDA_ARCH__)
+  return __funnelshift_l(lo, hi, (uint32_t)s);
+#else
+  return s ? (hi << s) | (lo >> (32 - s)) : hi;
+#endif
+}
+
 QB_HD int clz64(uint64_t x) {  // x != 0
 #if defined(__CUDA_ARCH__)
   return __clzll((long long)x);

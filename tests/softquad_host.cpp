@@ -326,6 +326,21 @@ static int half_int(uint16_t h) {
   const int v = e >= 25 ? m << (e - 25) : m >> (25 - e);
   return (h & 0x8000) ? -v : v;
 }
+extern "C++" {
+template <int NW>
+static q128 fold_biased(const uint32_t* Z, const qb::CrtFoldTable& ft, int e) {
+  qb::CrtFoldAcc<NW> A;
+  qb::crt_fold_init(A);
+  for (int w = 0; w < ft.N; ++w) {
+    float f = (float)Z[w] + 8388608.0f;
+    uint32_t bits;
+    memcpy(&bits, &f, 4);
+    qb::crt_fold_column(A, w, bits, true);
+  }
+  return qb::crt_fold_finish(A, ft.negM, e, true);
+}
+}
+
 int sq_crt_fold_tc(int64_t n, const int32_t* C, const int* e, int T, int64_t k, q128* out, int64_t* zmax) {
   qb::CrtTable t;
   if (!qb::crt_build(T, k, t)) return 0;
@@ -343,12 +358,24 @@ int sq_crt_fold_tc(int64_t n, const int32_t* C, const int* e, int T, int64_t k, 
       if (z > *zmax) *zmax = z;
       Z[col] = (uint32_t)z;
     }
+    q128 r;
     if (ft.nw <= 8)
-      out[i] = qb::crt_fold_columns<8>(Z, ft.nbytes, ft.negM, e[i]);
+      r = qb::crt_fold_columns<8>(Z, ft.nbytes, ft.negM, e[i]);
     else if (ft.nw <= 10)
-      out[i] = qb::crt_fold_columns<10>(Z, ft.nbytes, ft.negM, e[i]);
+      r = qb::crt_fold_columns<10>(Z, ft.nbytes, ft.negM, e[i]);
     else
-      out[i] = qb::crt_fold_columns<12>(Z, ft.nbytes, ft.negM, e[i]);
+      r = qb::crt_fold_columns<12>(Z, ft.nbytes, ft.negM, e[i]);
+    // the kernel's form: each sum as the bits of the fp32 value 2^23 + z, the
+    // offsets taken off per word
+    q128 rb;
+    if (ft.nw <= 8)
+      rb = fold_biased<8>(Z, ft, e[i]);
+    else if (ft.nw <= 10)
+      rb = fold_biased<10>(Z, ft, e[i]);
+    else
+      rb = fold_biased<12>(Z, ft, e[i]);
+    if (rb.lo != r.lo || rb.hi != r.hi) return -1;
+    out[i] = r;
   }
   return t.n;
 }

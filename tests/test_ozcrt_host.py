@@ -366,3 +366,42 @@ def test_tensor_core_reconstruction(sq, T, k):
     assert (out == ref).all()
     for i, x in enumerate(Xs):
         assert (int(out[i, 0]), int(out[i, 1])) == fraction_to_q(Fraction(x) * Fraction(2) ** int(e[i])), (i, x)
+
+
+def test_reconstruct_rounding_edges(sq):
+    """The reconstruction's rounding of X 2^e: ties (even and odd), sticky
+    bits far below, carries into a new binade, subnormal and overflowing
+    results (the general path), against exact rational rounding."""
+    T, k = 134, 4096
+    n, nw, mods, _, _ = table(sq, T, k)
+    ps = [m[0] for m in mods]
+    M = math.prod(ps)
+    rng = np.random.default_rng(99)
+    cases = []
+    for top in (113, 114, 120, 150, 200, 250):
+        base = 1 << (top - 1)
+        cases += [base, base + 1, base | ((1 << (top - 113)) - 1), (1 << top) - 1,
+                  base + (1 << (top - 114)) if top > 113 else base,                  # tie, even
+                  base + (1 << (top - 113)) + (1 << (top - 114)) if top > 113 else base,  # tie, odd
+                  base + (1 << (top - 114)) + 1 if top > 114 else base]
+    for _ in range(200):
+        top = int(rng.integers(1, M.bit_length() - 4))
+        cases.append(int(rng.integers(1, 1 << 62)) << max(0, top - 62) | 1)
+    cases = [c for c in cases if 0 < c < M // 8]
+    Xs, es = [], []
+    for c in cases:
+        for sgn in (1, -1):
+            for e in (-2 * T, -2 * T - 16400, -2 * T + 16000, 0):
+                Xs.append(sgn * c)
+                es.append(e)
+    keep = []
+    for x, e in zip(Xs, es):
+        f = Fraction(x) * Fraction(2) ** e
+        if abs(f) < Fraction(2) ** 16384 * (1 - Fraction(1, 2 ** 114)):  # below the overflow threshold
+            keep.append((x, e))
+    C = np.array([[x % p for p in ps] for x, _ in keep], dtype=np.int32)
+    e = np.array([e for _, e in keep], dtype=np.int32)
+    out = np.zeros((len(keep), 2), dtype=np.uint64)
+    sq.sq_crt_reconstruct(ctypes.c_int64(len(keep)), P(C), P(e), ctypes.c_int(T), ctypes.c_int64(k), P(out))
+    for i, (x, ee) in enumerate(keep):
+        assert (int(out[i, 0]), int(out[i, 1])) == fraction_to_q(Fraction(x) * Fraction(2) ** ee), (i, x, ee)
