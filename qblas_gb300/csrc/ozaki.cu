@@ -681,27 +681,29 @@ __global__ void __launch_bounds__(256)
 // tensor cores").  The product kernel stored y_q = (C_q mod p_q) u_q mod p_q
 // (16 bits; one k pass, or the passes summed by ozaki_crt_pass_sum_kernel).
 // Persistent CTAs of 4 warps walk tiles of 4 rows x 32 columns of C: warp w
-// takes row 4t + w, lane l column l (one tensor-memory lane per output).  A
+// takes row 4t + w, lane l column l (one accumulator lane per output).  A
 // tile's y values arrive by TMA (boxes of 32 columns x 4 rows x 16 moduli,
 // moduli beyond nmod zero-filled) two tiles ahead into two shared-memory
-// buffers.  Per tile each thread writes its output's y_q (fp16, exact) as an
-// operand row (K = 48) to tensor memory; one thread issues three MMAs
-// (M = 128, K = 16, N = crt_fold_n(NW)) against the byte table of M / p_q in
-// shared memory and waits for them; each thread then reads its column sums
-// (exact integers below 2^23, made integers by adding 2^23), 32 columns at a
-// time, assembles Y with carries (crt_fold_column), rounds X = Y - Q M once
-// at 2^(S_i + F_j - 2T) and applies the reference epilogue.  128
-// tensor-memory columns per CTA (D: [0, 64), A: [64, 88)), four CTAs per SM.
-// Every wait is bounded (1 s); on a timeout the CTA stops, waits (bounded)
-// for its copies in flight, records it in err[0] and frees its tensor memory
-// (its remaining outputs stay unwritten, and the call reports the timeout).
+// buffers.  Two stages: each thread writes its output's y_q (fp16, exact) as
+// an operand row (K = 48, K-major, no swizzle) to the stage's shared-memory
+// operand; one thread issues three MMAs (M = 128, K = 16, N = crt_fold_n(NW))
+// against the byte table of M / p_q into the stage's accumulator; while they
+// run, each thread finishes the tile before: reads its column sums (exact
+// integers below 2^23, made integers by adding 2^23), 32 at a time,
+// assembles Y with carries (crt_fold_column), rounds X = Y - Q M once at
+// 2^(S_i + F_j - 2T) and applies the reference epilogue.  Two 64-column
+// accumulators per CTA, four CTAs per SM.  Every wait is bounded (1 s); on a
+// timeout the CTA stops, waits (bounded) for its copies and MMAs in flight,
+// records it in err[0] and frees its tensor memory (its remaining outputs
+// stay unwritten, and the call reports the timeout).
 constexpr int kFoldThreads = 128;
-constexpr int kFoldTmemCols = 128;
-constexpr int kFoldAcol = 64;
+constexpr int kFoldTmemCols = 128;  // two accumulators of 64 columns
 constexpr int kFoldCtasPerSm = 4;
-constexpr int kFoldBoxBytes = 32 * 4 * 16 * 2;                 // one TMA box: 16 moduli of a tile
+constexpr int kFoldBoxBytes = 32 * 4 * 16 * 2;                     // one TMA box: 16 moduli of a tile
 constexpr int kFoldBufBytes = kFoldBoxBytes * (kCrtMaxMods / 16);  // 12 KiB: every modulus of a tile
-constexpr size_t kFoldSmem = 48 * 1024;  // table, two y buffers, barriers; keeps a fifth CTA off the SM
+constexpr int kFoldABytes = 128 * kCrtFoldK * 2;                   // 12 KiB: a stage's operand rows
+constexpr size_t kFoldSmem =
+    128 + 2 * kFoldBufBytes + 2 * kFoldABytes + kCrtFoldK * kCrtFoldMaxN * 2 + 64;  // about 54 KiB
 
 template <int NW>
 __global__ void __launch_bounds__(kFoldThreads, kFoldCtasPerSm)
@@ -709,21 +711,20 @@ __global__ void __launch_bounds__(kFoldThreads, kFoldCtasPerSm)
                              const __grid_constant__ CrtFoldTable tab) {
   constexpr int N = crt_fold_n(NW);
   extern __shared__ __align__(128) uint8_t fold_smem[];
-  uint8_t* sbase = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(fold_smem) + 1023) & ~(uintptr_t)1023);
-  uint8_t* ybuf = sbase;                                      // [2][48][4][32] u16
-  uint8_t* tbase = sbase + 2 * kFoldBufBytes;                 // the B table
-  uint64_t* bar = reinterpret_cast<uint64_t*>(tbase + kCrtFoldK * kCrtFoldMaxN * 2);  // mma, full[2]
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar + 3);
-  int* flag = reinterpret_cast<int*>(bar + 4);
+  uint8_t* sbase = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(fold_smem) + 127) & ~(uintptr_t)127);
+  uint8_t* ybuf = sbase;                                  // [2][48][4][32] u16 (TMA)
+  uint8_t* abuf = ybuf + 2 * kFoldBufBytes;               // [2] operand rows
+  uint8_t* tbase = abuf + 2 * kFoldABytes;                // the B table
+  uint64_t* bar = reinterpret_cast<uint64_t*>(tbase + kCrtFoldK * kCrtFoldMaxN * 2);  // mma[2], full[2]
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar + 4);
+  int* flag = reinterpret_cast<int*>(bar + 5);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nmod = tab.nmod, nboxes = (nmod + 15) / 16;
   for (int i = threadIdx.x; i < N * kCrtFoldK / 8; i += kFoldThreads)
     reinterpret_cast<uint4*>(tbase)[i] = reinterpret_cast<const uint4*>(tab.b)[i];
   fence_proxy_async_smem();
   if (threadIdx.x == 0) {
-    mbar_init(smem_u32(bar), 1);
-    mbar_init(smem_u32(bar + 1), 1);
-    mbar_init(smem_u32(bar + 2), 1);
+    for (int b = 0; b < 4; ++b) mbar_init(smem_u32(bar + b), 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 0) {
@@ -738,7 +739,8 @@ __global__ void __launch_bounds__(kFoldThreads, kFoldCtasPerSm)
   const uint32_t tmem = *tmem_slot;
   const uint32_t tlane = tmem + ((uint32_t)(warp * 32) << 16);
   constexpr uint32_t idesc = (1u << 4) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
-  const uint32_t sb = smem_u32(tbase), lbo = (uint32_t)N * 16u;
+  const uint32_t sb = smem_u32(tbase), lbo = (uint32_t)N * 16u, sa = smem_u32(abuf);
+  constexpr uint32_t albo = 128 * 16;  // K-adjacent core matrices of the operand rows
   const bool failed = (P.err[0] | P.err[1] | P.err[2]) != 0;
   if (failed && P.report && blockIdx.x == 0 && threadIdx.x == 0) *reinterpret_cast<volatile int*>(P.report) = 1;
 
@@ -753,11 +755,11 @@ __global__ void __launch_bounds__(kFoldThreads, kFoldCtasPerSm)
       ++r_t;
     }
   };
-  int tr = (int)blockIdx.x / tiles_c, tc = (int)blockIdx.x % tiles_c;  // this tile
+  int tr = (int)blockIdx.x / tiles_c, tc = (int)blockIdx.x % tiles_c;  // the tile to pack
   int pr = tr, pc = tc;                                                 // the next tile to fetch
-  uint32_t issued = 0, used = 0;  // tiles fetched / consumed (buffer = count & 1)
+  uint32_t issued = 0, used = 0;  // tiles fetched / packed (y buffer = count & 1)
   auto fetch = [&]() {             // thread 0: the next tile's y into its buffer
-    const uint32_t b = issued & 1u, fb = smem_u32(bar + 1 + b), dst = smem_u32(ybuf + b * kFoldBufBytes);
+    const uint32_t b = issued & 1u, fb = smem_u32(bar + 2 + b), dst = smem_u32(ybuf + b * kFoldBufBytes);
     mbar_expect_tx(fb, (uint32_t)(nboxes * kFoldBoxBytes));
     for (int x = 0; x < nboxes; ++x) tma_load_3d(dst + x * kFoldBoxBytes, &tmY, fb, 32 * pc, 4 * pr, 16 * x);
     ++issued;
@@ -767,74 +769,24 @@ __global__ void __launch_bounds__(kFoldThreads, kFoldCtasPerSm)
     if (pr < tiles_r) fetch();
     if (pr < tiles_r) fetch();
   }
-  uint32_t phase = 0;
+  // the packed tile waiting to be finished: its output, exponent, old C value
+  bool pend = false, pmine = false, pspecial = true;
+  int pe = 0;
+  q128* pcp = P.Cout;
+  q128 pcold = q_zero(0);
+  uint32_t mma_phase = 0;    // bit s: parity of stage s's next MMA completion
+  uint32_t outstanding = 0;  // bit s: stage s's MMAs issued and not yet waited for
+  int stage = 0;
   bool ok = true;
-  while (tr < tiles_r) {
-    const uint32_t b = used & 1u;
-    ok = mbar_wait(smem_u32(bar + 1 + b), (used >> 1) & 1u);
-    if (!__syncthreads_and(ok)) {
-      ok = false;
-      break;
-    }
-    ++used;
-    {
-      // y_q of this thread's output, fp16: the bits 0x6400 + y are 1024 + y
-      // (y <= 512), minus 1024 in pairs
-      const uint16_t* yb = reinterpret_cast<const uint16_t*>(ybuf + b * kFoldBufBytes) + warp * 32 + lane;
-      uint32_t a[24];
-#pragma unroll
-      for (int h = 0; h < 24; ++h) {
-        // moduli beyond nmod: zero (a buffer holds only the boxes fetched)
-        const uint32_t y0 = 2 * h < nmod ? (uint32_t)yb[(2 * h) * 128] : 0u;
-        const uint32_t y1 = 2 * h + 1 < nmod ? (uint32_t)yb[(2 * h + 1) * 128] : 0u;
-        const uint32_t w = (y0 | (y1 << 16)) + 0x64006400u;
-        const uint32_t k1024 = 0x64006400u;
-        const __half2 v =
-            __hsub2(*reinterpret_cast<const __half2*>(&w), *reinterpret_cast<const __half2*>(&k1024));
-        a[h] = *reinterpret_cast<const uint32_t*>(&v);
-      }
-      tmem_st16(tlane + kFoldAcol, *reinterpret_cast<uint32_t(*)[16]>(a));
-      tmem_st8(tlane + kFoldAcol + 16, *reinterpret_cast<uint32_t(*)[8]>(a + 16));
-    }
-    tmem_st_wait();
-    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    __syncthreads();  // operand rows written; buffer b read; the last tile's sums read
-    const int64_t i = (int64_t)tr * 4 + warp, j = (int64_t)tc * 32 + lane;
-    advance(tr, tc);
-    if (threadIdx.x == 0) {
-      if (pr < tiles_r) fetch();  // into buffer b, two tiles ahead
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-#pragma unroll
-      for (int kt = 0; kt < 3; ++kt)
-        mma_f16kind_ta(tmem, tmem + kFoldAcol + 8 * kt, smem_desc_noswizzle(sb + 2 * kt * lbo, lbo, 128), idesc,
-                       kt ? 1u : 0u);
-      mma_commit(smem_u32(bar));
-    }
-    const bool mine = i < P.m && j < P.n;
-    q128* cp = P.Cout + (mine ? i * P.sci + j * P.scj : 0);
-    q128 cold = q_zero(0);
-    int e = 0;
-    bool special = true;
-    if (mine) {
-      special = (P.fa[i] | P.fb[j]) != 0;  // NaN / inf rows and columns: ozaki_special_kernel
-      e = P.S[i] + P.F[j] - 2 * P.T;
-      if (!special) cold = ld_stream(cp);
-    }
-    if (threadIdx.x == 0) *flag = mbar_wait(smem_u32(bar), phase) ? 1 : 0;
-    phase ^= 1u;
-    __syncthreads();
-    if (!*flag) {
-      ok = false;
-      break;
-    }
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  // reads the column sums of stage st and writes the finished output
+  auto finish = [&](int st) {
     CrtFoldAcc<NW> acc;
     crt_fold_init(acc);
 #pragma unroll
     for (int h = 0; h < (N + 31) / 32; ++h) {
       uint32_t z[32];
-      tmem_ld16_nowait(tlane + 32 * h, z);
-      if (32 * h + 16 < N) tmem_ld16_nowait(tlane + 32 * h + 16, z + 16);
+      tmem_ld16_nowait(tlane + (uint32_t)(64 * st + 32 * h), z);
+      if (32 * h + 16 < N) tmem_ld16_nowait(tlane + (uint32_t)(64 * st + 32 * h + 16), z + 16);
       tmem_ld_wait();
 #pragma unroll
       for (int c = 0; c < 32; ++c) {
@@ -842,18 +794,109 @@ __global__ void __launch_bounds__(kFoldThreads, kFoldCtasPerSm)
         if (w < N) crt_fold_column(acc, w, __float_as_uint(__fadd_rn(__uint_as_float(z[c]), 8388608.0f)), true);
       }
     }
+    if (pmine && !pspecial) {
+      const q128 sum = failed ? q_nan() : crt_fold_finish(acc, tab.negM, pe, true);
+      *pcp = q_epilogue(P.alpha, sum, P.beta, pcold);
+    }
+  };
+  auto wait_mma = [&](int st) -> bool {
+    if (threadIdx.x == 0) *flag = mbar_wait(smem_u32(bar + st), (mma_phase >> st) & 1u) ? 1 : 0;
+    __syncthreads();
+    const bool got = *flag != 0;
+    if (got) {
+      mma_phase ^= 1u << st;
+      outstanding &= ~(1u << st);
+    }
+    return got;
+  };
+  while (tr < tiles_r) {
+    const uint32_t b = used & 1u;
+    ok = mbar_wait(smem_u32(bar + 2 + b), (used >> 1) & 1u);
+    if (!__syncthreads_and(ok)) {
+      ok = false;
+      break;
+    }
+    ++used;
+    {
+      // y_q of this thread's output, fp16: the bits 0x6400 + y are 1024 + y
+      // (y <= 512), minus 1024 in pairs; moduli beyond nmod are zero (a
+      // buffer holds only the boxes fetched)
+      const uint16_t* yb = reinterpret_cast<const uint16_t*>(ybuf + b * kFoldBufBytes) + warp * 32 + lane;
+      uint32_t a[24];
+#pragma unroll
+      for (int h = 0; h < 24; ++h) {
+        const uint32_t y0 = 2 * h < nmod ? (uint32_t)yb[(2 * h) * 128] : 0u;
+        const uint32_t y1 = 2 * h + 1 < nmod ? (uint32_t)yb[(2 * h + 1) * 128] : 0u;
+        const uint32_t w = (y0 | (y1 << 16)) + 0x64006400u, k1024 = 0x64006400u;
+        const __half2 v =
+            __hsub2(*reinterpret_cast<const __half2*>(&w), *reinterpret_cast<const __half2*>(&k1024));
+        a[h] = *reinterpret_cast<const uint32_t*>(&v);
+      }
+      // the operand row: K-block kb (8 moduli) at kb * 2048 + 16 * row
+      uint8_t* arow = abuf + stage * kFoldABytes + 16 * threadIdx.x;
+#pragma unroll
+      for (int kb = 0; kb < kCrtFoldK / 8; ++kb)
+        *reinterpret_cast<uint4*>(arow + kb * albo) = make_uint4(a[4 * kb], a[4 * kb + 1], a[4 * kb + 2], a[4 * kb + 3]);
+    }
+    fence_proxy_async_smem();
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    if (mine && !special) {
-      const q128 sum = failed ? q_nan() : crt_fold_finish(acc, tab.negM, e, true);
-      *cp = q_epilogue(P.alpha, sum, P.beta, cold);
+    __syncthreads();  // operand rows written; y buffer b read; this stage's sums read two tiles ago
+    const int64_t i = (int64_t)tr * 4 + warp, j = (int64_t)tc * 32 + lane;
+    advance(tr, tc);
+    if (threadIdx.x == 0) {
+      if (pr < tiles_r) fetch();  // into buffer b, two tiles ahead
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t d = tmem + (uint32_t)(64 * stage), a0 = sa + stage * kFoldABytes;
+#pragma unroll
+      for (int kt = 0; kt < 3; ++kt)
+        mma_f16kind(d, smem_desc_noswizzle(a0 + 2 * kt * albo, albo, 128),
+                    smem_desc_noswizzle(sb + 2 * kt * lbo, lbo, 128), idesc, kt ? 1u : 0u);
+      mma_commit(smem_u32(bar + stage));
+    }
+    outstanding |= 1u << stage;
+    // this tile's output: its loads are in flight while the tile before is finished
+    const bool mine = i < P.m && j < P.n;
+    const int64_t ii = mine ? i : 0, jj = mine ? j : 0;
+    q128* cp = P.Cout + ii * P.sci + jj * P.scj;
+    const uint32_t fl = P.fa[ii] | P.fb[jj];
+    const int e = P.S[ii] + P.F[jj] - 2 * P.T;
+    const q128 cold = ld_stream(cp);
+    if (pend) {
+      if (!wait_mma(stage ^ 1)) {
+        ok = false;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      finish(stage ^ 1);
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    }
+    pend = true;
+    pmine = mine;
+    pspecial = fl != 0;  // NaN / inf rows and columns: ozaki_special_kernel
+    pe = e;
+    pcp = cp;
+    pcold = cold;
+    stage ^= 1;
+  }
+  // the last tile (its MMAs were issued by the last iteration)
+  if (ok && pend) {
+    if (wait_mma(stage ^ 1)) {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      finish(stage ^ 1);
+    } else {
+      ok = false;
     }
   }
+  // after a timeout, the copies and MMAs still in flight are waited for
+  // (bounded), so that none is outstanding when the tensor memory is freed
   if (!ok && threadIdx.x == 0) {
     atomicExch(const_cast<int*>(P.err), 1);
     if (P.report) *reinterpret_cast<volatile int*>(P.report) = 1;
-    // copies still in flight: the tiles fetched but not consumed (at most two)
-    for (uint32_t u = used; u < issued; ++u) mbar_wait(smem_u32(bar + 1 + (u & 1u)), (u >> 1) & 1u);
+    for (int st = 0; st < 2; ++st)
+      if ((outstanding >> st) & 1u) mbar_wait(smem_u32(bar + st), (mma_phase >> st) & 1u);
+    for (uint32_t u = used; u < issued; ++u) mbar_wait(smem_u32(bar + 2 + (u & 1u)), (u >> 1) & 1u);
   }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   if (warp == 0)
