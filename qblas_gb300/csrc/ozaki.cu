@@ -58,10 +58,11 @@ namespace qb {
 // ---------------------------------------------------------------------------
 // Scaling and splitting
 // ---------------------------------------------------------------------------
-// One thread per (row, chunk of 64 columns) of the view X(r, c) = p[r*sr + c*sc].
+// One thread per (row, chunk of 64 columns) of the view X(r, c) = p[r*sr + c*sc];
+// *any is set when a NaN or infinity is seen.
 __global__ void ozaki_scale_kernel(int64_t rows, int64_t cols, const q128* __restrict__ p,
                                    int64_t sr, int64_t sc, int* __restrict__ S,
-                                   uint32_t* __restrict__ flags) {
+                                   uint32_t* __restrict__ flags, int* __restrict__ any) {
   const int64_t nchunk = (cols + 63) / 64;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < rows * nchunk; w += stride) {
@@ -83,7 +84,63 @@ __global__ void ozaki_scale_kernel(int64_t rows, int64_t cols, const q128* __res
       fl |= ozaki_special_flags(v);
     }
     if (mx != kOzakiScaleEmpty) atomicMax(S + r, mx);
-    if (fl) atomicOr(flags + r, fl);
+    if (fl) {
+      atomicOr(flags + r, fl);
+      atomicOr(any, 1);
+    }
+  }
+}
+
+// The same for views whose columns are contiguous (sc = 1): one warp per
+// (row, chunk of 256 columns), each lane reading every 32nd element, so that
+// a warp's loads cover 512 contiguous bytes; warp maximum by shuffles.
+__global__ void __launch_bounds__(256)
+    ozaki_scale_rows_kernel(int64_t rows, int64_t cols, const q128* __restrict__ p, int64_t sr,
+                            int* __restrict__ S, uint32_t* __restrict__ flags, int* __restrict__ any) {
+  const int lane = threadIdx.x & 31;
+  const int64_t nchunk = (cols + 255) / 256;
+  const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x / 32);
+  for (int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32; w < rows * nchunk; w += nwarps) {
+    const int64_t r = w / nchunk, c0 = (w % nchunk) * 256;
+    const q128* row = p + r * sr;
+    int mx = kOzakiScaleEmpty;
+    uint32_t fl = 0;
+#pragma unroll
+    for (int t = 0; t < 8; ++t) {
+      const int64_t c = c0 + lane + 32 * t;
+      if (c < cols) {
+        const q128 v = ld_stream(row + c);
+        mx = max(mx, ozaki_exp_plus1(v));
+        fl |= ozaki_special_flags(v);
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      mx = max(mx, __shfl_xor_sync(0xFFFFFFFFu, mx, o));
+      fl |= __shfl_xor_sync(0xFFFFFFFFu, fl, o);
+    }
+    if (lane == 0) {
+      if (mx != kOzakiScaleEmpty) atomicMax(S + r, mx);
+      if (fl) {
+        atomicOr(flags + r, fl);
+        atomicOr(any, 1);
+      }
+    }
+  }
+}
+
+// Scales and flags of a view (rows x cols), on stream st.
+static void launch_scale(int64_t rows, int64_t cols, const q128* p, int64_t sr, int64_t sc, int* S,
+                         uint32_t* flags, int* any, int sms, cudaStream_t st) {
+  if (rows <= 0) return;
+  if (sc == 1) {
+    const int64_t warps = rows * ((cols + 255) / 256);
+    const unsigned b = (unsigned)std::max<int64_t>(1, std::min<int64_t>((warps + 7) / 8, (int64_t)sms * 8));
+    ozaki_scale_rows_kernel<<<b, 256, 0, st>>>(rows, cols, p, sr, S, flags, any);
+  } else {
+    const int64_t w = rows * ((cols + 63) / 64);
+    const unsigned b = (unsigned)std::max<int64_t>(1, std::min<int64_t>((w + 255) / 256, (int64_t)sms * 8));
+    ozaki_scale_kernel<<<b, 256, 0, st>>>(rows, cols, p, sr, sc, S, flags, any);
   }
 }
 
@@ -231,9 +288,22 @@ __global__ void __launch_bounds__(kSplitThreads)
       if (c + 1 < P.cols) v1 = ld_cached(e + P.sc);
     }
   };
-  q128 v0, v1;
-  int Sr;
+  // elements of this tile (v0, v1, Sr), the next (n*) and the one after it,
+  // loaded while the MMAs of this tile run: two tiles in flight
+  q128 v0, v1, n0, n1;
+  int Sr, nS;
   load(tr, tc, v0, v1, Sr);
+  int fr = tr, fc = tc;  // the tile whose elements were loaded last
+  auto advance = [&](int& r_t, int& c_t) {
+    c_t += step_c;
+    r_t += step_r;
+    if (c_t >= tiles_c) {
+      c_t -= tiles_c;
+      ++r_t;
+    }
+  };
+  advance(fr, fc);
+  load(fr, fc, n0, n1, nS);
   uint32_t phase = 0;
   bool ok = true;
   while (tr < tiles_r) {
@@ -247,12 +317,7 @@ __global__ void __launch_bounds__(kSplitThreads)
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();  // operand rows written; the last tile's accumulator read
     const int64_t r = (int64_t)tr * 4 + warp, c = (int64_t)tc * 64 + 2 * lane;
-    tc += step_c;
-    tr += step_r;
-    if (tc >= tiles_c) {
-      tc -= tiles_c;
-      ++tr;
-    }
+    advance(tr, tc);
     if (threadIdx.x == 0) {
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 #pragma unroll
@@ -261,7 +326,11 @@ __global__ void __launch_bounds__(kSplitThreads)
                        kt ? 1u : 0u);
       mma_commit(smem_u32(bar));
     }
-    load(tr, tc, v0, v1, Sr);  // the next tile's elements, in flight while the MMAs run
+    v0 = n0;
+    v1 = n1;
+    Sr = nS;
+    advance(fr, fc);
+    load(fr, fc, n0, n1, nS);  // two tiles ahead, in flight while the MMAs run
     if (threadIdx.x == 0) *flag = mbar_wait(smem_u32(bar), phase) ? 1 : 0;
     phase ^= 1u;
     __syncthreads();
@@ -907,19 +976,23 @@ __global__ void __launch_bounds__(kFoldThreads, kFoldCtasPerSm)
 // Outputs in a row of op(A) or a column of op(B) that holds a NaN or an
 // infinity: a direct wide-accumulator dot, so IEEE special-value semantics
 // are kept (every such sum contains a special product, so it is exact).
-// Threads of other outputs return at once.
-__global__ void __launch_bounds__(256) ozaki_special_kernel(OzakiFoldParams P) {
-  const int64_t j = (int64_t)blockIdx.x * 32 + threadIdx.x;
-  const int64_t i = (int64_t)blockIdx.y * 8 + threadIdx.y;
-  if (i >= P.m || j >= P.n) return;
-  if (!(P.fa[i] | P.fb[j])) return;
-  q128* cp = P.Cout + i * P.sci + j * P.scj;
-  wacc acc;
-  wacc_init(acc);
-  for (int64_t l = 0; l < P.k; ++l)
-    wacc_add_product(acc, qop_unpack(ld_cached(P.A + i * P.sai + l * P.sal)),
-                     qop_unpack(ld_cached(P.B + l * P.sbl + j * P.sbj)));
-  *cp = q_epilogue(P.alpha, wacc_round(acc), P.beta, *cp);
+// any[0] | any[1] (set by the scale kernels of both operands) says whether
+// there is one at all; without, the launch returns at once.  Grid-stride
+// over the outputs; threads of other outputs skip them.
+__global__ void __launch_bounds__(256) ozaki_special_kernel(OzakiFoldParams P, const int* __restrict__ any) {
+  if ((any[0] | any[1]) == 0) return;
+  const int64_t total = P.m * P.n;
+  for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < total; x += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = x / P.n, j = x % P.n;
+    if (!(P.fa[i] | P.fb[j])) continue;
+    q128* cp = P.Cout + i * P.sci + j * P.scj;
+    wacc acc;
+    wacc_init(acc);
+    for (int64_t l = 0; l < P.k; ++l)
+      wacc_add_product(acc, qop_unpack(ld_cached(P.A + i * P.sai + l * P.sal)),
+                       qop_unpack(ld_cached(P.B + l * P.sbl + j * P.sbj)));
+    *cp = q_epilogue(P.alpha, wacc_round(acc), P.beta, *cp);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -1217,13 +1290,13 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scr
   // error words: [0] tensor-core products (main stream), [1] op(B)'s residue
   // split, [2] op(A)'s; each is reset on the stream of its writer
   if ((e = cudaMemsetAsync(err, 0, 4, st)) != cudaSuccess) return e;
+  // [4], [5]: a NaN or infinity in op(B), in op(A)
   if ((e = cudaMemsetAsync(err + 1, 0, 4, sb)) != cudaSuccess) return e;
+  if ((e = cudaMemsetAsync(err + 4, 0, 4, sb)) != cudaSuccess) return e;
   const dim3 blk(32, 8);
   const int64_t plane_a = L.m_pad * L.k_pad, plane_b = L.n_pad * L.k_pad;
   {
-    int64_t wb = g.n * ((g.k + 63) / 64);
-    unsigned bb = (unsigned)std::min<int64_t>((wb + 255) / 256, (int64_t)sms * 8);
-    ozaki_scale_kernel<<<bb, 256, 0, sb>>>(g.n, g.k, g.B, g.sbj, g.sbl, F, fb);
+    launch_scale(g.n, g.k, g.B, g.sbj, g.sbl, F, fb, err + 4, sms, sb);
     dim3 gb((unsigned)(L.k_pad / 64), (unsigned)(L.n_pad / 8));
     if (crt)
       e = launch_crt_split(stab, sb, g.n, g.k, L.n_pad, L.k_pad, plane_b, g.B, g.sbj, g.sbl, F, DB, err + 1);
@@ -1241,10 +1314,10 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scr
     const int64_t rows = std::min(r1, g.m) - r0;
     cudaError_t ee;
     if (banded && ov->a_rows(ov->a_ctx, r0, r0 + rows, sa) != 0) return cudaErrorUnknown;
-    if (r0 == 0 && (ee = cudaMemsetAsync(err + 2, 0, 4, sa)) != cudaSuccess) return ee;
-    int64_t wa = rows * ((g.k + 63) / 64);
-    unsigned ba = (unsigned)std::max<int64_t>(1, std::min<int64_t>((wa + 255) / 256, (int64_t)sms * 8));
-    if (rows > 0) ozaki_scale_kernel<<<ba, 256, 0, sa>>>(rows, g.k, g.A + r0 * g.sai, g.sai, g.sal, S + r0, fa + r0);
+    if (r0 == 0 && ((ee = cudaMemsetAsync(err + 2, 0, 4, sa)) != cudaSuccess ||
+                    (ee = cudaMemsetAsync(err + 5, 0, 4, sa)) != cudaSuccess))
+      return ee;
+    launch_scale(rows, g.k, g.A + r0 * g.sai, g.sai, g.sal, S + r0, fa + r0, err + 5, sms, sa);
     dim3 ga((unsigned)(L.k_pad / 64), (unsigned)((r1 - r0) / 8));
     const q128* Ab = g.A + r0 * g.sai;
     ee = cudaSuccess;
@@ -1330,9 +1403,9 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scr
     } else {
       launch_fold(L.b, st, Fb);
     }
-    dim3 fblk(32, 8), fgrid((unsigned)((g.n + 31) / 32), (unsigned)((Fb.m + 7) / 8));
     if ((ee = cudaGetLastError()) != cudaSuccess) return ee;
-    ozaki_special_kernel<<<fgrid, fblk, 0, st>>>(Fb);
+    const unsigned sgrid = (unsigned)std::max<int64_t>(1, std::min<int64_t>((Fb.m * g.n + 255) / 256, (int64_t)sms * 2));
+    ozaki_special_kernel<<<sgrid, 256, 0, st>>>(Fb, err + 4);
     if ((ee = cudaGetLastError()) != cudaSuccess) return ee;
     if (fold_banded && ov->band_done(ov->band_ctx, i0, i1) != 0) return cudaErrorUnknown;
     return cudaSuccess;
