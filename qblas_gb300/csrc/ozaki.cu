@@ -400,6 +400,12 @@ struct OzakiMmaParams {
   int crt;
   uint16_t* Y;                  // [G+1][m_pad][n_pad]
   uint32_t crt_p[kCrtMaxMods], crt_magic[kCrtMaxMods], crt_K[kCrtMaxMods], crt_u[kCrtMaxMods];
+  // Paired CTAs (launched as clusters of two): the two CTAs of a cluster
+  // take tile rows 2r and 2r + 1 of the same tile column in lockstep, each
+  // loads its A tile and one half (128 rows) of the shared B tile with a
+  // multicast copy to both, and a stage is refilled once both CTAs' MMAs
+  // released it.  tile_begin and tile_end are then whole tile rows.
+  int pair;
 };
 
 // Instruction descriptors: kind::f16, D = f32, K-major A and B, N = 256,
@@ -420,39 +426,81 @@ constexpr uint32_t kIdescF16 = kIdescShape;
 // is modulus G - v / tiles of tile v % tiles): all tiles of a modulus run
 // before the next modulus starts, and its two planes (2 x 32 MB at 4096^2)
 // stay in L2 across the waves instead of being streamed again per wave.
-__device__ __forceinline__ int cta_unit_count(const OzakiMmaParams& P) {
-  const int tiles = P.tile_end - P.tile_begin, G1 = P.G + 1;
-  if (P.crt) {
-    const int left = tiles * G1 - (int)blockIdx.x;
-    return left > 0 ? (left + (int)gridDim.x - 1) / (int)gridDim.x : 0;
+//
+// A CTA's place in the deal: its index and the count among the dealers (the
+// cluster index and count for paired CTAs), and the tiles dealt (tile-row
+// pairs x tile columns for paired CTAs).
+struct UnitDeal {
+  int c, G, tiles, rank;
+};
+
+__device__ __forceinline__ UnitDeal unit_deal(const OzakiMmaParams& P) {
+  UnitDeal d;
+  const int tiles = P.tile_end - P.tile_begin;
+  if (P.pair) {
+    d.rank = (int)cluster_ctarank();
+    d.c = (int)blockIdx.x >> 1;
+    d.G = (int)gridDim.x >> 1;
+    d.tiles = (tiles / P.tiles_n + 1) / 2 * P.tiles_n;
+  } else {
+    d.rank = 0;
+    d.c = (int)blockIdx.x;
+    d.G = (int)gridDim.x;
+    d.tiles = tiles;
   }
-  const int waves = tiles / (int)gridDim.x, rem = tiles - waves * (int)gridDim.x;
-  const int tail = rem * G1 - (int)blockIdx.x;
-  return waves * G1 + (tail > 0 ? (tail + (int)gridDim.x - 1) / (int)gridDim.x : 0);
+  return d;
 }
 
-__device__ __forceinline__ void cta_unit(const OzakiMmaParams& P, int j, int& tile, int& g) {
-  const int tiles = P.tile_end - P.tile_begin, G1 = P.G + 1;
+__device__ __forceinline__ int cta_unit_count(const OzakiMmaParams& P, const UnitDeal& d) {
+  const int tiles = d.tiles, G1 = P.G + 1;
   if (P.crt) {
-    const int v = (int)blockIdx.x + j * (int)gridDim.x;
+    const int left = tiles * G1 - d.c;
+    return left > 0 ? (left + d.G - 1) / d.G : 0;
+  }
+  const int waves = tiles / d.G, rem = tiles - waves * d.G;
+  const int tail = rem * G1 - d.c;
+  return waves * G1 + (tail > 0 ? (tail + d.G - 1) / d.G : 0);
+}
+
+// Unit j of this CTA: its tile (tm, tn), diagonal or modulus g, and whether
+// the tile exists (the second CTA of a pair past an odd last tile row
+// computes a tile of its own that is not stored).
+__device__ __forceinline__ void cta_unit(const OzakiMmaParams& P, const UnitDeal& d, int j, int& tm, int& tn,
+                                         int& g, bool& real) {
+  const int tiles = d.tiles, G1 = P.G + 1;
+  int vt;
+  if (P.crt) {
+    const int v = d.c + j * d.G;
     g = P.G - v / tiles;
-    tile = P.tile_begin + v % tiles;
+    vt = v % tiles;
+  } else {
+    const int waves = tiles / d.G, rem = tiles - waves * d.G;
+    if (j < waves * G1) {
+      vt = (j / G1) * d.G + d.c;
+      g = P.G - j % G1;
+    } else {
+      const int v = d.c + (j - waves * G1) * d.G;
+      g = P.G - v / rem;
+      vt = waves * d.G + v % rem;
+    }
+  }
+  if (!P.pair) {
+    const int tile = P.tile_begin + vt;
+    tm = tile / P.tiles_n;
+    tn = tile % P.tiles_n;
+    real = true;
     return;
   }
-  const int waves = tiles / (int)gridDim.x, rem = tiles - waves * (int)gridDim.x;
-  if (j < waves * G1) {
-    tile = P.tile_begin + (j / G1) * (int)gridDim.x + (int)blockIdx.x;
-    g = P.G - j % G1;
-  } else {
-    const int v = (int)blockIdx.x + (j - waves * G1) * (int)gridDim.x;
-    g = P.G - v / rem;
-    tile = P.tile_begin + waves * (int)gridDim.x + v % rem;
-  }
+  const int row0 = P.tile_begin / P.tiles_n, rows = (P.tile_end - P.tile_begin) / P.tiles_n;
+  const int r = 2 * (vt / P.tiles_n) + d.rank;
+  tn = vt % P.tiles_n;
+  tm = row0 + r;
+  real = r < rows;
 }
 
-__global__ void __launch_bounds__(kMmaThreads, 1)
+__global__ void __maxnreg__(200)
     ozaki_mma_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
-                     OzakiMmaParams P) {
+                     const __grid_constant__ CUtensorMap tmBh, OzakiMmaParams P) {
   extern __shared__ uint8_t smem_raw[];
   const uint32_t raw = smem_u32(smem_raw);
   const uint32_t base = (raw + 1023u) & ~1023u;  // 128B swizzle needs 1024-byte alignment
@@ -470,7 +518,7 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
   if (threadIdx.x == 0) {
     for (int s = 0; s < kStages; ++s) {
       mbar_init(full_bar(s), 1);
-      mbar_init(empty_bar(s), 1);
+      mbar_init(empty_bar(s), P.pair ? 2 : 1);  // paired: both CTAs' MMAs release a stage
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(tfull_bar(b), 1);
@@ -490,8 +538,11 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmem_slot;
+  // paired: the peer's barriers are initialised before any copy or commit reaches them
+  if (P.pair) cluster_sync_all();
 
-  const int nun = cta_unit_count(P);
+  const UnitDeal deal = unit_deal(P);
+  const int nun = cta_unit_count(P, deal);
   const int nkb = P.kb_end - P.kb_begin;
   const int nchunks = (nkb + P.chunk_kb - 1) / P.chunk_kb;
   bool ok = true;
@@ -501,9 +552,9 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
     if (lane == 0) {
       uint32_t it = 0;
       for (int j = 0; j < nun && ok; ++j) {
-        int tile, g;
-        cta_unit(P, j, tile, g);
-        const int tm = tile / P.tiles_n, tn = tile % P.tiles_n;
+        int tm, tn, g;
+        bool real;
+        cta_unit(P, deal, j, tm, tn, g, real);
         for (int t = P.crt ? g : 0; t <= g && ok; ++t) {
           const int u = P.crt ? g : g - t;
           for (int kb = P.kb_begin; kb < P.kb_end && ok; ++kb, ++it) {
@@ -516,7 +567,11 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
             mbar_expect_tx(full_bar(s), kStageBytes);
             const uint32_t sa = base + s * kStageBytes, sb = sa + kStageA;
             tma_load_2d(sa, &tmA, full_bar(s), kb * kBK, t * P.m_pad + tm * kBM);
-            tma_load_2d(sb, &tmB, full_bar(s), kb * kBK, u * P.n_pad + tn * kBN);
+            if (P.pair)  // this CTA's half of B, to both CTAs
+              tma_load_2d_mc(sb + deal.rank * (kStageB / 2), &tmBh, full_bar(s), kb * kBK,
+                             u * P.n_pad + tn * kBN + deal.rank * (kBN / 2), (uint16_t)3);
+            else
+              tma_load_2d(sb, &tmB, full_bar(s), kb * kBK, u * P.n_pad + tn * kBN);
           }
         }
       }
@@ -533,8 +588,9 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
       uint32_t it = 0, acc_it = 0;
       bool issued_any = false;
       for (int j = 0; j < nun && ok; ++j) {
-        int tile, g;
-        cta_unit(P, j, tile, g);
+        int tm, tn, g;
+        bool real;
+        cta_unit(P, deal, j, tm, tn, g, real);
         for (int t = P.crt ? g : 0; t <= g && ok; ++t) {
           for (int ch = 0; ch < nchunks && ok; ++ch) {
             const int kb0 = P.kb_begin + ch * P.chunk_kb;
@@ -563,7 +619,10 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
                             (kb > kb0 || k > 0) ? 1u : 0u);
               }
               issued_any = true;
-              mma_commit(empty_bar(s));
+              if (P.pair)
+                mma_commit_mc(empty_bar(s), (uint16_t)3);  // the stage is free here and in the peer
+              else
+                mma_commit(empty_bar(s));
             }
             if (!ok) break;
             mma_commit(tfull_bar(buf));
@@ -590,9 +649,9 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
     for (int i = 0; i < kBN / 2; ++i) acc[i] = 0;
     uint32_t acc_it = 0;
     for (int j = 0; j < nun && ok; ++j) {
-      int tile, g;
-      cta_unit(P, j, tile, g);
-      const int tm = tile / P.tiles_n, tn = tile % P.tiles_n;
+      int tm, tn, g;
+      bool real;
+      cta_unit(P, deal, j, tm, tn, g, real);
       for (int t = P.crt ? g : 0; t <= g && ok; ++t) {
         for (int ch = 0; ch < nchunks && ok; ++ch) {
           const int buf = acc_it & 1;
@@ -620,7 +679,9 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
       // store diagonal g of this tile: row (tm*128 + row_in_tile), 128 columns
       const size_t off = ((size_t)g * P.m_pad + (size_t)tm * kBM + row_in_tile) * P.n_pad + (size_t)tn * kBN +
                          half * (kBN / 2);
-      if (P.crt) {
+      // (a pair's second CTA past an odd last tile row computed a tile that
+      // does not exist: nothing is stored)
+      if (P.crt && real) {
         // |acc| <= 2^29 (a pass holds 8192 of k): y = ((acc mod p) u) mod p < 2^16
         const uint32_t p = P.crt_p[g], mg = P.crt_magic[g], K = P.crt_K[g], u = P.crt_u[g];
         uint16_t* dst = P.Y + off;
@@ -628,21 +689,18 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
         for (int i = 0; i < kBN / 2; ++i)
           acc[i] = (int32_t)crt_mod(crt_mod((uint32_t)(acc[i] + (int32_t)K), p, mg) * u, p, mg);
 #pragma unroll
-        for (int i = 0; i < kBN / 2; i += 8) {
+        for (int i = 0; i < kBN / 2; i += 8)
           *reinterpret_cast<uint4*>(dst + i) =
               make_uint4((uint32_t)acc[i] | ((uint32_t)acc[i + 1] << 16), (uint32_t)acc[i + 2] | ((uint32_t)acc[i + 3] << 16),
                          (uint32_t)acc[i + 4] | ((uint32_t)acc[i + 5] << 16), (uint32_t)acc[i + 6] | ((uint32_t)acc[i + 7] << 16));
-#pragma unroll
-          for (int h = 0; h < 8; ++h) acc[i + h] = 0;
-        }
-      } else {
+      } else if (real) {
         int32_t* dst = P.C + off;
 #pragma unroll
-        for (int i = 0; i < kBN / 2; i += 4) {
+        for (int i = 0; i < kBN / 2; i += 4)
           *reinterpret_cast<int4*>(dst + i) = make_int4(acc[i], acc[i + 1], acc[i + 2], acc[i + 3]);
-          acc[i] = acc[i + 1] = acc[i + 2] = acc[i + 3] = 0;
-        }
       }
+#pragma unroll
+      for (int i = 0; i < kBN / 2; ++i) acc[i] = 0;
     }
     if (!ok && lane == 0) atomicExch(P.err, 1);
   }
@@ -654,6 +712,9 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols)
                  : "memory");
   }
+  // paired: neither CTA leaves while the other may still send it a copy or a
+  // stage release (every wait above is bounded, so both get here)
+  if (P.pair) cluster_sync_all();
 }
 
 // ---------------------------------------------------------------------------
@@ -1239,6 +1300,35 @@ static cudaError_t launch_crt_fold(const CrtFoldTable& ft, cudaStream_t st, cons
   return cudaGetLastError();
 }
 
+// Clusters of two product-kernel CTAs that can be resident at once on the
+// current device (0 when clusters cannot be launched), looked up once.
+static int mma_pair_clusters() {
+  static std::atomic<int> cached[64];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 0;
+  int v = cached[dev].load(std::memory_order_relaxed);
+  if (v) return v - 1;
+  cudaError_t e = cudaFuncSetAttribute(ozaki_mma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMmaSmem);
+  int n = 0;
+  if (e == cudaSuccess) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(2);
+    cfg.blockDim = dim3(kMmaThreads);
+    cfg.dynamicSmemBytes = kMmaSmem;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = 2;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    if (cudaOccupancyMaxActiveClusters(&n, (const void*)ozaki_mma_kernel, &cfg) != cudaSuccess) n = 0;
+  }
+  cudaGetLastError();
+  cached[dev].store(n + 1, std::memory_order_relaxed);
+  return n;
+}
+
 cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scratch, cudaStream_t st,
                               const OzakiOverlap* ov, int scheme, int* report) {
   if (g.m <= 0 || g.n <= 0 || g.k <= 0) return cudaSuccess;
@@ -1338,9 +1428,10 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scr
   // Without a caller delivering op(A) by rows there is one band; with one,
   // the bands are whole waves of tiles (one tile per SM), at most 8, and
   // each band's digit products start as soon as its rows of op(A) are cut.
-  CUtensorMap tmA, tmB;
+  CUtensorMap tmA, tmB, tmBh;
   if (!make_map(&tmA, DA, (int64_t)(L.G + 1) * L.m_pad, L.k_pad, kBM, crt || L.b == 9) ||
-      !make_map(&tmB, DB, (int64_t)(L.G + 1) * L.n_pad, L.k_pad, kBN, crt || L.b == 9))
+      !make_map(&tmB, DB, (int64_t)(L.G + 1) * L.n_pad, L.k_pad, kBN, crt || L.b == 9) ||
+      !make_map(&tmBh, DB, (int64_t)(L.G + 1) * L.n_pad, L.k_pad, kBN / 2, crt || L.b == 9))
     return cudaErrorInvalidValue;
   static std::atomic<bool> attr_set[64];
   int dev = 0;
@@ -1354,10 +1445,15 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scr
   const int tiles_m = (int)(L.m_pad / kBM), tiles_n = (int)(L.n_pad / kBN);
   const int tiles = tiles_m * tiles_n;
   const int kb_total = (int)(L.k_pad / kBK), kbp = L.kbp;
+  // paired CTAs (clusters of two sharing B) whenever there are two tile rows,
+  // as many clusters as can be resident at once (the kernel is persistent)
+  const int clusters = mma_pair_clusters();
+  const bool pair = tiles_m >= 2 && clusters >= 1;
   int band_tiles = tiles;
   if (banded) {
     const int waves = (tiles + sms - 1) / sms;
     band_tiles = ((waves + 7) / 8) * sms;
+    if (pair) band_tiles = (band_tiles + 2 * tiles_n - 1) / (2 * tiles_n) * (2 * tiles_n);  // whole tile-row pairs
   }
   // 3. fold + epilogue of rows [i0, i1) (the diagonal planes keep their
   // m_pad x n_pad shape); with a caller copying C out band by band, each
@@ -1445,7 +1541,25 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scr
       P.C = Cg + (size_t)p * (L.G + 1) * L.m_pad * L.n_pad;
       P.Y = Yq + (size_t)p * (L.G + 1) * L.m_pad * L.n_pad;
       P.err = err;
-      ozaki_mma_kernel<<<(unsigned)std::min(units, sms), kMmaThreads, kMmaSmem, st>>>(tmA, tmB, P);
+      P.pair = pair ? 1 : 0;
+      if (pair) {
+        const int vunits = (L.G + 1) * ((t1 - t0) / tiles_n + 1) / 2 * tiles_n;
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3((unsigned)(2 * std::min(vunits, clusters)));
+        cfg.blockDim = dim3(kMmaThreads);
+        cfg.dynamicSmemBytes = kMmaSmem;
+        cfg.stream = st;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = 2;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        if ((e = cudaLaunchKernelEx(&cfg, ozaki_mma_kernel, tmA, tmB, tmBh, P)) != cudaSuccess) return e;
+      } else {
+        ozaki_mma_kernel<<<(unsigned)std::min(units, sms), kMmaThreads, kMmaSmem, st>>>(tmA, tmB, tmBh, P);
+      }
       if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
     // rows whose tiles are all done can be folded while later bands multiply,
