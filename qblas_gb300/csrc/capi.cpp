@@ -15,6 +15,7 @@
 // outputs unchanged and record the error for quadblas_last_error()).
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -53,6 +54,9 @@ bool take_injected_failure() {
 
 int cuda_status(cudaError_t e) {
   if (e == cudaSuccess) return qb::kOk;
+  // QBLAS_DEBUG set: name the CUDA error behind a failing status on stderr
+  static const bool debug = getenv("QBLAS_DEBUG") != nullptr;
+  if (debug) fprintf(stderr, "qblas: CUDA error %d: %s\n", (int)e, cudaGetErrorString(e));
   if (e == cudaErrorMemoryAllocation) return qb::kErrNoMemory;
   if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return qb::kErrNoDevice;
   return qb::kErrCuda;

@@ -498,7 +498,7 @@ __device__ __forceinline__ void cta_unit(const OzakiMmaParams& P, const UnitDeal
   real = r < rows;
 }
 
-__global__ void __maxnreg__(192)
+__global__ void __launch_bounds__(kMmaThreads, 1)
     ozaki_mma_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                      const __grid_constant__ CUtensorMap tmBh, OzakiMmaParams P) {
   extern __shared__ uint8_t smem_raw[];
