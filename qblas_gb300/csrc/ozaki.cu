@@ -42,6 +42,9 @@
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
+#include <stdio.h>
+#include <stdlib.h>
+
 #include <algorithm>
 #include <atomic>
 #include <mutex>
@@ -1449,6 +1452,12 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scr
   // as many clusters as can be resident at once (the kernel is persistent)
   const int clusters = mma_pair_clusters();
   const bool pair = tiles_m >= 2 && clusters >= 1;
+  {
+    static const bool debug = getenv("QBLAS_DEBUG") != nullptr;
+    if (debug)
+      fprintf(stderr, "qblas: Ozaki products %dx%d tiles, %s (%d resident clusters of two)\n", tiles_m, tiles_n,
+              pair ? "paired CTAs" : "single CTAs", clusters);
+  }
   int band_tiles = tiles;
   if (banded) {
     const int waves = (tiles + sms - 1) / sms;
