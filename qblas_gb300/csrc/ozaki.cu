@@ -26,7 +26,7 @@
 //                         B_u) into a 4-stage shared-memory ring, warp 1
 //                         issues tcgen05.mma (M=128, N=256, K=16) into one
 //                         of two 256-column fp32 accumulators in tensor
-//                         memory, warps 2..17 read the accumulators with
+//                         memory, warps 2..9 read the accumulators with
 //                         tcgen05.ld, convert to int32 and sum a diagonal
 //                         in registers, then store C_g[row][col] (int32).
 //                         Every mbarrier wait is bounded (1 s); on timeout
@@ -383,9 +383,8 @@ constexpr int kStages = 4;
 constexpr int kStageA = kBM * kBK * 2;          // 16 KiB
 constexpr int kStageB = kBN * kBK * 2;          // 32 KiB
 constexpr int kStageBytes = kStageA + kStageB;  // 48 KiB
-constexpr int kEpiWarps = 16;                   // four per tensor-memory lane quadrant
-constexpr int kMmaThreads = (2 + kEpiWarps) * 32;  // producer, MMA issuer, epilogue
-constexpr int kEpiCols = kBN / 4;                // accumulator columns per epilogue thread
+constexpr int kMmaThreads = 320;                // 10 warps
+constexpr int kEpiWarps = 8;
 constexpr int kTmemCols = 512;                  // two 256-column fp32 accumulators
 constexpr size_t kMmaSmem = (size_t)kStages * kStageBytes + 1024 + 256;
 
@@ -643,14 +642,14 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
       }
     }
   } else {
-    // ---------------- epilogue: 16 warps ----------------
+    // ---------------- epilogue: 8 warps ----------------
     const int e = warp - 2;
     const int quad = warp & 3;           // tensor-memory lane quadrant of this warp
-    const int quarter = e >> 2;          // column quarter of the accumulator
+    const int half = e >> 2;             // column half: [0,128) or [128,256)
     const int row_in_tile = quad * 32 + lane;
-    int32_t acc[kEpiCols];
+    int32_t acc[kBN / 2];
 #pragma unroll
-    for (int i = 0; i < kEpiCols; ++i) acc[i] = 0;
+    for (int i = 0; i < kBN / 2; ++i) acc[i] = 0;
     uint32_t acc_it = 0;
     for (int j = 0; j < nun && ok; ++j) {
       int tm, tn, g;
@@ -665,9 +664,9 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
           }
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
           const uint32_t taddr =
-              tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(buf * kBN + quarter * kEpiCols);
+              tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(buf * kBN + half * (kBN / 2));
 #pragma unroll
-          for (int c = 0; c < kEpiCols; c += 32) {
+          for (int c = 0; c < kBN / 2; c += 32) {
             uint32_t r[32];
             tmem_ld32(taddr + (uint32_t)c, r);
 #pragma unroll
@@ -682,7 +681,7 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
       if (!ok) break;
       // store diagonal g of this tile: row (tm*128 + row_in_tile), 128 columns
       const size_t off = ((size_t)g * P.m_pad + (size_t)tm * kBM + row_in_tile) * P.n_pad + (size_t)tn * kBN +
-                         quarter * kEpiCols;
+                         half * (kBN / 2);
       // (a pair's second CTA past an odd last tile row computed a tile that
       // does not exist: nothing is stored)
       if (P.crt && real) {
@@ -690,21 +689,21 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
         const uint32_t p = P.crt_p[g], mg = P.crt_magic[g], K = P.crt_K[g], u = P.crt_u[g];
         uint16_t* dst = P.Y + off;
 #pragma unroll
-        for (int i = 0; i < kEpiCols; ++i)
+        for (int i = 0; i < kBN / 2; ++i)
           acc[i] = (int32_t)crt_mod(crt_mod((uint32_t)(acc[i] + (int32_t)K), p, mg) * u, p, mg);
 #pragma unroll
-        for (int i = 0; i < kEpiCols; i += 8)
+        for (int i = 0; i < kBN / 2; i += 8)
           *reinterpret_cast<uint4*>(dst + i) =
               make_uint4((uint32_t)acc[i] | ((uint32_t)acc[i + 1] << 16), (uint32_t)acc[i + 2] | ((uint32_t)acc[i + 3] << 16),
                          (uint32_t)acc[i + 4] | ((uint32_t)acc[i + 5] << 16), (uint32_t)acc[i + 6] | ((uint32_t)acc[i + 7] << 16));
       } else if (real) {
         int32_t* dst = P.C + off;
 #pragma unroll
-        for (int i = 0; i < kEpiCols; i += 4)
+        for (int i = 0; i < kBN / 2; i += 4)
           *reinterpret_cast<int4*>(dst + i) = make_int4(acc[i], acc[i + 1], acc[i + 2], acc[i + 3]);
       }
 #pragma unroll
-      for (int i = 0; i < kEpiCols; ++i) acc[i] = 0;
+      for (int i = 0; i < kBN / 2; ++i) acc[i] = 0;
     }
     if (!ok && lane == 0) atomicExch(P.err, 1);
   }
