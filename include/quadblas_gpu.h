@@ -240,6 +240,17 @@ int quadblas_release_buffers(void);
  * (the call returns QBLAS_ERR_NO_MEMORY and leaves its outputs untouched);
  * 0 clears it.  Nothing is allocated for a failed attempt. */
 int quadblas_debug_fail_allocations(int count);
+/* Testing aid for callers' handling of device-side timeouts, without a
+ * stalled GPU: the next Ozaki qgemm (which = 1; its tensor-core product
+ * kernel) or Ozaki qgemv (which = 2) withholds one completion signal inside
+ * its kernel and shortens that kernel's pipeline waits to 1 ms, so that a
+ * wait runs out as it would on a real stall; the kernel then stops, waits
+ * for its own copies and tensor-core operations in flight (1 s limit) and
+ * frees its resources.  The qgemm then returns QBLAS_ERR_TIMEOUT (host
+ * pointers) or sets the device flag read by quadblas_device_status, with NaN
+ * in C; the qgemv recomputes every row exactly and returns correct results.
+ * Calls after that one run normally. */
+int quadblas_debug_stall_next_call(int which);
 /* Testing aid for the certified rounding of qgemv: while on, every qgemv
  * records (in stream order) how many rows its exact pass recomputed because
  * their rounding could not be certified; quadblas_debug_exact_rows returns

@@ -62,6 +62,7 @@ _SIGS = {
     "quadblas_profile_read": (ci, [vp, vp]),
     "quadblas_release_buffers": (ci, []),
     "quadblas_debug_fail_allocations": (ci, [ci]),
+    "quadblas_debug_stall_next_call": (ci, [ci]),
     "quadblas_debug_count_exact_rows": (ci, [ci]),
     "quadblas_debug_exact_rows": (ctypes.c_longlong, []),
     "quadblas_device_status": (ci, [ci]),

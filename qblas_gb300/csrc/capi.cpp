@@ -894,6 +894,16 @@ QBLAS_EXPORT int quadblas_debug_fail_allocations(int count) {
   return fail(qb::kOk);
 }
 
+QBLAS_EXPORT int quadblas_debug_stall_next_call(int which) {
+  if (which == 1)
+    qb::ozaki_debug_stall_next();
+  else if (which == 2)
+    qb::ozgemv_debug_stall_next();
+  else
+    return fail(qb::kErrInvalidValue);
+  return fail(qb::kOk);
+}
+
 static unsigned* g_exact_rows_host = nullptr;
 
 QBLAS_EXPORT int quadblas_debug_count_exact_rows(int on) {

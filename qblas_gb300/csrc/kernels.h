@@ -109,6 +109,10 @@ struct OzakiOverlap {
 cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scratch,
                               cudaStream_t s, const OzakiOverlap* overlap = nullptr, int scheme = 0,
                               int* report = nullptr);
+// Test hooks: the next Ozaki qgemm product launch / Ozaki qgemv launch
+// withholds one accumulator-full commit with 1 ms pipeline waits.
+void ozaki_debug_stall_next();
+void ozgemv_debug_stall_next();
 // Phase timing of Ozaki calls with CUDA events (off by default).
 void ozaki_profile_enable(bool on);
 int ozaki_profile_read(double* out4, int* calls);

@@ -409,6 +409,11 @@ struct OzakiMmaParams {
   // multicast copy to both, and a stage is refilled once both CTAs' MMAs
   // released it.  tile_begin and tile_end are then whole tile rows.
   int pair;
+  // test hook (quadblas_debug_stall_next_call): pipeline waits give up after
+  // wait_ns; withhold = 1 makes the MMA issuer skip the accumulator-full
+  // commit of its first chunk, so that the epilogue's wait runs out
+  unsigned long long wait_ns;
+  int withhold;
 };
 
 // Instruction descriptors: kind::f16, D = f32, K-major A and B, N = 256,
@@ -563,7 +568,7 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
           for (int kb = P.kb_begin; kb < P.kb_end && ok; ++kb, ++it) {
             const int s = it % kStages;
             const uint32_t round = it / kStages;
-            if (!mbar_wait(empty_bar(s), (round & 1u) ^ 1u)) {
+            if (!mbar_wait_ns(empty_bar(s), (round & 1u) ^ 1u, P.wait_ns)) {
               ok = false;
               break;
             }
@@ -600,7 +605,7 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
             const int kb1 = kb0 + P.chunk_kb < P.kb_end ? kb0 + P.chunk_kb : P.kb_end;
             const int buf = acc_it & 1;
             const uint32_t round = acc_it >> 1;
-            if (!mbar_wait(tempty_bar(buf), (round & 1u) ^ 1u)) {
+            if (!mbar_wait_ns(tempty_bar(buf), (round & 1u) ^ 1u, P.wait_ns)) {
               ok = false;
               break;
             }
@@ -608,7 +613,7 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
             const uint32_t dcol = tmem + (uint32_t)(buf * kBN);
             for (int kb = kb0; kb < kb1; ++kb, ++it) {
               const int s = it % kStages;
-              if (!mbar_wait(full_bar(s), (it / kStages) & 1u)) {
+              if (!mbar_wait_ns(full_bar(s), (it / kStages) & 1u, P.wait_ns)) {
                 ok = false;
                 break;
               }
@@ -628,17 +633,18 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
                 mma_commit(empty_bar(s));
             }
             if (!ok) break;
-            mma_commit(tfull_bar(buf));
+            if (!(P.withhold && acc_it == 0)) mma_commit(tfull_bar(buf));
             ++acc_it;
           }
         }
       }
-      if (!ok) {
-        atomicExch(P.err, 1);
-        if (issued_any) {
-          mma_commit(drain_bar);
-          mbar_wait(drain_bar, 0);
-        }
+      if (!ok) atomicExch(P.err, 1);
+      // after a timeout, or with a withheld commit (nobody else then waits
+      // for the last MMAs), the MMAs in flight complete before the tensor
+      // memory is freed
+      if ((!ok || P.withhold) && issued_any) {
+        mma_commit(drain_bar);
+        mbar_wait(drain_bar, 0);
       }
     }
   } else {
@@ -658,7 +664,7 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
       for (int t = P.crt ? g : 0; t <= g && ok; ++t) {
         for (int ch = 0; ch < nchunks && ok; ++ch) {
           const int buf = acc_it & 1;
-          if (!mbar_wait(tfull_bar(buf), (acc_it >> 1) & 1u)) {
+          if (!mbar_wait_ns(tfull_bar(buf), (acc_it >> 1) & 1u, P.wait_ns)) {
             ok = false;
             break;
           }
@@ -1303,6 +1309,12 @@ static cudaError_t launch_crt_fold(const CrtFoldTable& ft, cudaStream_t st, cons
   return cudaGetLastError();
 }
 
+// Test hook of quadblas_debug_stall_next_call: set, the next Ozaki qgemm's
+// products withhold one accumulator-full commit with 1 ms pipeline waits.
+static std::atomic<int> g_stall_qgemm{0};
+void ozaki_debug_stall_next() { g_stall_qgemm.store(1); }
+static bool ozaki_take_stall() { return g_stall_qgemm.exchange(0) != 0; }
+
 // Clusters of two product-kernel CTAs that can be resident at once on the
 // current device (0 when clusters cannot be launched), looked up once.
 static int mma_pair_clusters() {
@@ -1451,7 +1463,8 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scr
   // paired CTAs (clusters of two sharing B) whenever there are two tile rows,
   // as many clusters as can be resident at once (the kernel is persistent)
   const int clusters = mma_pair_clusters();
-  const bool pair = tiles_m >= 2 && clusters >= 1;
+  const bool stall = ozaki_take_stall();  // test hook: this call's products time out
+  const bool pair = tiles_m >= 2 && clusters >= 1 && !stall;
   {
     static const bool debug = getenv("QBLAS_DEBUG") != nullptr;
     if (debug)
@@ -1551,6 +1564,8 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scr
       P.Y = Yq + (size_t)p * (L.G + 1) * L.m_pad * L.n_pad;
       P.err = err;
       P.pair = pair ? 1 : 0;
+      P.withhold = (stall && t0 == 0 && p == 0) ? 1 : 0;
+      P.wait_ns = stall ? kStallWaitNs : kWaitLimitNs;
       if (pair) {
         const int vunits = (L.G + 1) * ((t1 - t0) / tiles_n + 1) / 2 * tiles_n;
         cudaLaunchConfig_t cfg = {};

@@ -124,6 +124,11 @@ struct OgParams {
   int segs;                 // partial slots per tile
   OgPartial* part;          // [tiles][segs][128]
   int* err;
+  // test hook (quadblas_debug_stall_next_call): pipeline waits give up after
+  // wait_ns; withhold = 1 makes the MMA issuer skip the accumulator-full
+  // commit of its first item, so that the epilogue's wait runs out
+  unsigned long long wait_ns;
+  int withhold;
 };
 
 // ---------------------------------------------------------------------------
@@ -323,7 +328,7 @@ __global__ void __launch_bounds__(kOgThreads, 1)
       // all k-steps of the chunk are needed for its row exponents
       bool got = true;
 #pragma unroll
-      for (int ks = 0; ks < kOgKSteps; ++ks) got = got && mbar_wait(full_bar(slot_of(q + ks)), fill_parity(q + ks));
+      for (int ks = 0; ks < kOgKSteps; ++ks) got = got && mbar_wait_ns(full_bar(slot_of(q + ks)), fill_parity(q + ks), P.wait_ns);
       if (!got) {
         ok = false;
         break;
@@ -343,7 +348,7 @@ __global__ void __launch_bounds__(kOgThreads, 1)
       em[grp * kOgRows + r] = mx;
       __syncwarp();
       if (lane == 0) mbar_arrive(rowmax_bar(it & 1, qd));
-      if (!mbar_wait(rowmax_bar(it & 1, qd), (it >> 1) & 1u)) {
+      if (!mbar_wait_ns(rowmax_bar(it & 1, qd), (it >> 1) & 1u, P.wait_ns)) {
         ok = false;
         break;
       }
@@ -384,7 +389,7 @@ __global__ void __launch_bounds__(kOgThreads, 1)
           bs[i] = 0xE480E480u - neg * 0x80008000u;  // (-+1152, -+1152)
         }
         const int st = stage_of(q);
-        if (!mbar_wait(free_bar(st), use_parity(q) ^ 1u)) {  // the MMAs of the stage's last use completed
+        if (!mbar_wait_ns(free_bar(st), use_parity(q) ^ 1u, P.wait_ns)) {  // the MMAs of the stage's last use completed
           ok = false;
           break;
         }
@@ -433,7 +438,7 @@ __global__ void __launch_bounds__(kOgThreads, 1)
       uint32_t issued = 0;
       for (; issued < nks && ok; ++issued) {
         // the split warps released this slot's previous k-step
-        if (!mbar_wait(empty_bar(slot_of(issued)), fill_parity(issued) ^ 1u)) {
+        if (!mbar_wait_ns(empty_bar(slot_of(issued)), fill_parity(issued) ^ 1u, P.wait_ns)) {
           ok = false;
           break;
         }
@@ -454,14 +459,14 @@ __global__ void __launch_bounds__(kOgThreads, 1)
       bool any_mma = false;
       for (int64_t w = w0; w < w1 && ok; ++w, ++it) {
         const int tb = it % kOgAccBufs;
-        if (!mbar_wait(tempty_bar(tb), ((it / kOgAccBufs) & 1u) ^ 1u)) {
+        if (!mbar_wait_ns(tempty_bar(tb), ((it / kOgAccBufs) & 1u) ^ 1u, P.wait_ns)) {
           ok = false;
           break;
         }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         for (int ks = 0; ks < kOgKSteps && ok; ++ks, ++q) {
           const int st = stage_of(q);
-          if (!mbar_wait(ready_bar(st), use_parity(q))) {
+          if (!mbar_wait_ns(ready_bar(st), use_parity(q), P.wait_ns)) {
             ok = false;
             break;
           }
@@ -479,14 +484,15 @@ __global__ void __launch_bounds__(kOgThreads, 1)
           mma_commit(free_bar(st));
         }
         if (!ok) break;
-        mma_commit(tfull_bar(tb));
+        if (!(P.withhold && it == 0)) mma_commit(tfull_bar(tb));
       }
-      if (!ok) {
-        atomicExch(P.err, 1);
-        if (any_mma) {
-          mma_commit(drain_bar);
-          mbar_wait(drain_bar, 0);
-        }
+      if (!ok) atomicExch(P.err, 1);
+      // after a timeout, or with a withheld commit (nobody else then waits
+      // for the last MMAs), the MMAs in flight complete before the tensor
+      // memory is freed
+      if ((!ok || P.withhold) && any_mma) {
+        mma_commit(drain_bar);
+        mbar_wait(drain_bar, 0);
       }
     }
   } else {
@@ -525,12 +531,12 @@ __global__ void __launch_bounds__(kOgThreads, 1)
       }
       const int F = __ldg(P.xexp + c);  // read early: its latency overlaps the waits
       const int tb = it % kOgAccBufs;
-      if (!mbar_wait(exp_bar(it % kOgExpSlots), (it / kOgExpSlots) & 1u)) {
+      if (!mbar_wait_ns(exp_bar(it % kOgExpSlots), (it / kOgExpSlots) & 1u, P.wait_ns)) {
         ok = false;
         break;
       }
       const int ev = exps[(it % kOgExpSlots) * kOgRows + rit];
-      if (!mbar_wait(tfull_bar(tb), (it / kOgAccBufs) & 1u)) {
+      if (!mbar_wait_ns(tfull_bar(tb), (it / kOgAccBufs) & 1u, P.wait_ns)) {
         ok = false;
         break;
       }
@@ -637,6 +643,10 @@ static OgLayout og_layout(int64_t m, int64_t n) {
   return L;
 }
 
+// Test hook of quadblas_debug_stall_next_call (Ozaki qgemv).
+static std::atomic<int> g_stall_qgemv{0};
+void ozgemv_debug_stall_next() { g_stall_qgemv.store(1); }
+
 size_t gemv_ozaki_scratch_bytes(int64_t m, int64_t n) {
   if (m <= 0 || n <= 0) return 0;
   return og_layout(m, n).total;
@@ -688,6 +698,9 @@ cudaError_t launch_gemv_ozaki(int64_t m, int64_t n, q128 alpha, MatView A, const
   P.segs = Lo.segs;
   P.part = reinterpret_cast<OgPartial*>(base + Lo.part);
   P.err = reinterpret_cast<int*>(base + Lo.err);
+  const bool stall = g_stall_qgemv.exchange(0) != 0;  // test hook: this call's kernel times out
+  P.wait_ns = stall ? kStallWaitNs : kWaitLimitNs;
+  P.withhold = stall ? 1 : 0;
   cudaError_t e = cudaMemsetAsync(P.err, 0, sizeof(int), s);
   if (e != cudaSuccess) return e;
   og_x_split_kernel<<<(unsigned)Lo.nchunks, 32, 0, s>>>(n, Lo.nchunks, x, incx, const_cast<uint8_t*>(P.xdig),

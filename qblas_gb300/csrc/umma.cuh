@@ -60,15 +60,27 @@ __device__ __forceinline__ bool mbar_try_sleep(uint32_t bar, uint32_t parity, ui
   return ok != 0;
 }
 
-// Bounded wait for the phase with the given parity to complete (1 s).
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+// Bounded wait for the phase with the given parity to complete: false after
+// limit_ns nanoseconds without it.
+__device__ __forceinline__ bool mbar_wait_ns(uint32_t bar, uint32_t parity, unsigned long long limit_ns) {
   if (mbar_try(bar, parity)) return true;
   unsigned long long t0 = global_timer();
+  const uint32_t hint = limit_ns < 1000000ull ? (uint32_t)limit_ns : 1000000u;
   while (true) {
-    if (mbar_try_sleep(bar, parity, 1000000u)) return true;
-    if (global_timer() - t0 > kWaitLimitNs) return false;
+    if (mbar_try_sleep(bar, parity, hint)) return true;
+    if (global_timer() - t0 > limit_ns) return false;
   }
 }
+
+// The same with the standard limit (1 s).
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+  return mbar_wait_ns(bar, parity, kWaitLimitNs);
+}
+
+// Limit of the pipeline waits of a launch whose test hook shortened them
+// (quadblas_debug_stall_next_call), else the standard one; the waits that
+// drain copies and MMAs in flight always keep the standard limit.
+constexpr unsigned long long kStallWaitNs = 1000000ull;  // 1 ms
 
 __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, uint32_t bar,
                                             int c0, int c1) {
