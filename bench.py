@@ -318,10 +318,11 @@ def batched_config4(torch, api, rank, reps=3):
     for op, m, n, k, *_ in lay:
         flops += 2.0 * (m * n * k if op == 0 else (m * n if op == 1 else n))
     c0 = out.clone()
-    # the work-item granularity comes from the autotuner (cached per GPU model)
+    # gemm tile edge and work-item granularity come from the autotuner
     t0 = time.perf_counter()
-    grain = api.batch_autotune()
+    api.batch_autotune()
     tune_s = time.perf_counter() - t0
+    grain, tile = api.batch_setting()
     t0 = time.perf_counter()
     plan = api.BatchPlan(probs)
     plan_s = time.perf_counter() - t0
@@ -368,10 +369,11 @@ def batched_config4(torch, api, rank, reps=3):
             "ms_batched_graph_replay": round(ms_batched, 3), "ms_one_call_per_problem": round(ms_single, 3),
             "one_by_one": "quadblas_batch_run_serial (C loop of device-pointer calls)",
             "speedup_vs_one_by_one": round(ms_single / ms_batched, 2), "plan_ms": round(plan_s * 1e3, 1),
-            "work_items": info["items"], "grain": info["grain"], "autotuned_grain": grain,
+            "work_items": info["items"], "grain": info["grain"], "tile": info["tile"],
+            "autotuned": {"grain": grain, "tile": tile, "candidates": "tile {16, 32} x grain 2^14..2^20"},
             "autotune_ms": round(tune_s * 1e3, 1), "launches_per_batch": 1,
             "parity": "bit-identical to one-by-one" if same else "MISMATCH against one-by-one",
-            "method": "soft-float wide accumulator for every problem", "quad_flops": flops}
+            "method_mix": {"softfloat_wide_accumulator": len(probs), "ozaki": 0}, "quad_flops": flops}
 
 
 def oracle_accuracy(W, C, rank, samples=512):

@@ -153,13 +153,14 @@ int quadblas_qdot_dev_noalloc(int64_t n, const void *dx, int64_t incx, const voi
  *                  (incy = ldb), n elements.
  * All pointers are device pointers (16-byte aligned); alpha and beta hold
  * binary128 values (low word first).  quadblas_batch_plan cuts the problems
- * into equal-cost work items (granularity from the autotuner) and uploads
- * them; quadblas_batch_execute runs the whole batch on `stream` with one
- * memset and one persistent kernel and allocates nothing, so it can be
- * recorded in a CUDA graph and replayed; concurrent executions of one plan
- * must not overlap.  quadblas_batch_autotune times a calibration batch at
- * several granularities and caches the best per device (in memory and in
- * $QBLAS_AUTOTUNE_CACHE, default $HOME/.cache/qblas_gb300_autotune.txt). */
+ * into equal-cost work items (granularity and gemm tile edge from the
+ * autotuner) and uploads them; quadblas_batch_execute runs the whole batch on
+ * `stream` with one memset and one persistent kernel and allocates nothing,
+ * so it can be recorded in a CUDA graph and replayed; concurrent executions
+ * of one plan must not overlap.  quadblas_batch_autotune times a calibration
+ * batch at every pair of gemm tile edge (16, 32) and granularity (2^14 ..
+ * 2^20 products per item) and caches the best pair per device (in memory and
+ * in $QBLAS_AUTOTUNE_CACHE, default $HOME/.cache/qblas_gb300_autotune.txt). */
 enum { QBLAS_OP_GEMM = 0, QBLAS_OP_GEMV = 1, QBLAS_OP_DOT = 2 };
 
 typedef struct {
@@ -180,7 +181,13 @@ int quadblas_batch_execute(void *plan, void *stream);
 int quadblas_batch_destroy(void *plan);
 /* info4: work items, granularity (products per item), blocks, split groups */
 int quadblas_batch_info(void *plan, int64_t *info4);
+/* info[0..n): work items, granularity, blocks, split groups, gemm tile edge */
+int quadblas_batch_info_ex(void *plan, int64_t *info, int64_t n);
 int quadblas_batch_autotune(int64_t *grain_out);
+/* The current device's setting for new plans (tuned, set, cached or default). */
+int quadblas_batch_setting(int64_t *grain, int *tile);
+/* Sets granularity (>= 256) and gemm tile edge (16 or 32; 0 keeps it). */
+int quadblas_batch_configure(int64_t grain, int tile);
 int quadblas_batch_set_grain(int64_t grain);
 /* The same problems without the batch: one device-pointer call per problem
  * (quadblas_qgemm_dev with the soft-float method, quadblas_qgemv_dev,

@@ -205,9 +205,9 @@ class BatchPlan:
         check(load().quadblas_batch_execute(self.handle, _stream(stream)))
 
     def info(self) -> dict:
-        out = (ctypes.c_int64 * 4)()
-        check(load().quadblas_batch_info(self.handle, out))
-        return {"items": out[0], "grain": out[1], "blocks": out[2], "split_groups": out[3]}
+        out = (ctypes.c_int64 * 5)()
+        check(load().quadblas_batch_info_ex(self.handle, out, 5))
+        return {"items": out[0], "grain": out[1], "blocks": out[2], "split_groups": out[3], "tile": out[4]}
 
     def close(self) -> None:
         if self.handle:
@@ -229,3 +229,14 @@ def batch_autotune() -> int:
 
 def batch_set_grain(grain: int) -> None:
     check(load().quadblas_batch_set_grain(grain))
+
+
+def batch_setting() -> tuple:
+    """(granularity, gemm tile edge) that new plans on this device use."""
+    g, t = ctypes.c_int64(0), ctypes.c_int(0)
+    check(load().quadblas_batch_setting(ctypes.byref(g), ctypes.byref(t)))
+    return g.value, t.value
+
+
+def batch_configure(grain: int, tile: int = 0) -> None:
+    check(load().quadblas_batch_configure(grain, tile))

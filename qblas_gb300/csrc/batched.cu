@@ -44,9 +44,9 @@
 namespace qb {
 
 constexpr int kBThreads = 256;
-constexpr int kBTile = 32;   // gemm tile edge
-constexpr int kBTK = 16;     // gemm k slice staged in shared memory
-constexpr int kBRows = 8;    // gemv rows per item (one warp each)
+constexpr int kBTileMax = 32; // gemm tile edges: 16 (one output per thread) or 32 (2 x 2)
+constexpr int kBTK = 16;      // gemm k slice staged in shared memory
+constexpr int kBRows = 8;     // gemv rows per item (one warp each)
 
 enum : int32_t { kOpGemm = 0, kOpGemv = 1, kOpDot = 2 };
 
@@ -76,16 +76,19 @@ struct BItem {
 // ---------------------------------------------------------------------------
 // device
 // ---------------------------------------------------------------------------
+template <int T>
 struct BTile {
-  uint32_t m0[kBTK][kBTile], m1[kBTK][kBTile], m2[kBTK][kBTile], m3[kBTK][kBTile];
-  int32_t e[kBTK][kBTile];
-  uint32_t sc[kBTK][kBTile];
+  uint32_t m0[kBTK][T], m1[kBTK][T], m2[kBTK][T], m3[kBTK][T];
+  int32_t e[kBTK][T];
+  uint32_t sc[kBTK][T];
 };
 
+template <int T>
 struct BShared {
+  static constexpr int kTile = T;
   union {
     struct {
-      BTile a, b;
+      BTile<T> a, b;
     } t;
     KulischBlock K;  // exact recomputation after an item's accumulation
   } u;
@@ -93,10 +96,11 @@ struct BShared {
   int item;
   int last;
   int nlist;
-  short list[kBTile * kBTile];  // uncertified outputs of the current item
+  short list[kBTileMax * kBTileMax];  // uncertified outputs of the current item
 };
 
-__device__ __forceinline__ void btile_put(BTile& t, int kk, int idx, q128 v) {
+template <int T>
+__device__ __forceinline__ void btile_put(BTile<T>& t, int kk, int idx, q128 v) {
   qop o = qop_unpack(v);
   t.m0[kk][idx] = o.m0;
   t.m1[kk][idx] = o.m1;
@@ -106,7 +110,8 @@ __device__ __forceinline__ void btile_put(BTile& t, int kk, int idx, q128 v) {
   t.sc[kk][idx] = o.s | (o.cls << 1);
 }
 
-__device__ __forceinline__ qop btile_get(const BTile& t, int kk, int idx) {
+template <int T>
+__device__ __forceinline__ qop btile_get(const BTile<T>& t, int kk, int idx) {
   qop o;
   o.m0 = t.m0[kk][idx];
   o.m1 = t.m1[kk][idx];
@@ -138,7 +143,8 @@ __device__ __forceinline__ wacc wacc_ldcg(const wacc* p) {
 // Marks one item of a split group done; true in every thread of the block
 // that completed the group.  Partials written before the call are visible
 // to that block afterwards.
-__device__ __forceinline__ bool group_arrive(BShared& sh, int* counter, int nparts) {
+template <class SH>
+__device__ __forceinline__ bool group_arrive(SH& sh, int* counter, int nparts) {
   __threadfence();
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -152,21 +158,25 @@ __device__ __forceinline__ bool group_arrive(BShared& sh, int* counter, int npar
   return last;
 }
 
-__device__ void run_gemm_item(BShared& sh, const BProb& P, const BItem& it, wacc* partials,
+// A T x T tile of C (T = 16 or 32): thread (tx, ty) of the 16 x 16 grid
+// owns the R x R outputs (R*ty + a, R*tx + b), R = T / 16.
+template <int T>
+__device__ void run_gemm_item(BShared<T>& sh, const BProb& P, const BItem& it, wacc* partials,
                               int* counters) {
+  constexpr int R = T / 16;
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
   const q128 zero = q_zero(0);
-  wacc c[4];
+  wacc c[R * R];
 #pragma unroll
-  for (int q = 0; q < 4; ++q) wacc_init(c[q]);
+  for (int q = 0; q < R * R; ++q) wacc_init(c[q]);
   for (int64_t l0 = it.l0; l0 < it.l1; l0 += kBTK) {
 #pragma unroll
-    for (int r = 0; r < 2; ++r) {
+    for (int r = 0; r < R; ++r) {
       int e = tid + r * kBThreads;
       int ar = e >> 4, ak = e & 15;
       int64_t gi = it.i0 + ar, gl = l0 + ak;
       q128 av = (gi < P.m && gl < it.l1) ? ld_cached(P.A + gi * P.sai + gl * P.sal) : zero;
-      int bk = e >> 5, bc = e & 31;
+      int bk = e / T, bc = e % T;
       int64_t bl = l0 + bk, gj = it.j0 + bc;
       q128 bv = (bl < it.l1 && gj < P.n) ? ld_cached(P.B + bl * P.sbl + gj * P.sbj) : zero;
       btile_put(sh.u.t.a, ak, ar, av);
@@ -175,46 +185,49 @@ __device__ void run_gemm_item(BShared& sh, const BProb& P, const BItem& it, wacc
     __syncthreads();
 #pragma unroll 2
     for (int kk = 0; kk < kBTK; ++kk) {
-      qop a0 = btile_get(sh.u.t.a, kk, 2 * ty), a1 = btile_get(sh.u.t.a, kk, 2 * ty + 1);
-      qop b0 = btile_get(sh.u.t.b, kk, 2 * tx), b1 = btile_get(sh.u.t.b, kk, 2 * tx + 1);
-      wacc_add_product(c[0], a0, b0);
-      wacc_add_product(c[1], a0, b1);
-      wacc_add_product(c[2], a1, b0);
-      wacc_add_product(c[3], a1, b1);
+      qop a[R], b[R];
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        a[r] = btile_get(sh.u.t.a, kk, R * ty + r);
+        b[r] = btile_get(sh.u.t.b, kk, R * tx + r);
+      }
+#pragma unroll
+      for (int q = 0; q < R * R; ++q) wacc_add_product(c[q], a[q / R], b[q % R]);
     }
     __syncthreads();
   }
   if (P.nparts > 1) {
-    // partial slot layout: [group][part][thread][4]
-    wacc* mine = partials + P.part_base + ((it.group * P.nparts + it.part) * kBThreads + tid) * 4;
+    // partial slot layout: [group][part][thread][R * R]
+    wacc* mine = partials + P.part_base + ((it.group * P.nparts + it.part) * kBThreads + tid) * (R * R);
 #pragma unroll
-    for (int q = 0; q < 4; ++q) mine[q] = c[q];
+    for (int q = 0; q < R * R; ++q) mine[q] = c[q];
     if (!group_arrive(sh, counters + P.group_base + it.group, P.nparts)) return;
 #pragma unroll
-    for (int q = 0; q < 4; ++q) wacc_init(c[q]);
+    for (int q = 0; q < R * R; ++q) wacc_init(c[q]);
     for (int p = 0; p < P.nparts; ++p) {
-      const wacc* src = partials + P.part_base + ((it.group * P.nparts + p) * kBThreads + tid) * 4;
+      const wacc* src = partials + P.part_base + ((it.group * P.nparts + p) * kBThreads + tid) * (R * R);
 #pragma unroll
-      for (int q = 0; q < 4; ++q) wacc_merge(c[q], wacc_ldcg(src + q));
+      for (int q = 0; q < R * R; ++q) wacc_merge(c[q], wacc_ldcg(src + q));
     }
   }
   const uint64_t err = 2 * (uint64_t)P.k + 3 * (uint64_t)P.nparts + 2;
 #pragma unroll
-  for (int q = 0; q < 4; ++q) {
-    int64_t i = it.i0 + 2 * ty + (q >> 1), j = it.j0 + 2 * tx + (q & 1);
+  for (int q = 0; q < R * R; ++q) {
+    const int li = R * ty + q / R, lj = R * tx + q % R;
+    int64_t i = it.i0 + li, j = it.j0 + lj;
     if (i < P.m && j < P.n) {
       q128* p = P.C + i * P.sci + j * P.scj;
       q128 r;
       if (wacc_round_certified(c[q], err, r))
         *p = q_epilogue(P.alpha, r, P.beta, *p);
       else
-        sh.list[atomicAdd(&sh.nlist, 1)] = (short)((2 * ty + (q >> 1)) * kBTile + 2 * tx + (q & 1));
+        sh.list[atomicAdd(&sh.nlist, 1)] = (short)(li * T + lj);
     }
   }
   __syncthreads();
   const int cnt = sh.nlist;
   for (int t = 0; t < cnt; ++t) {
-    const int64_t i = it.i0 + sh.list[t] / kBTile, j = it.j0 + sh.list[t] % kBTile;
+    const int64_t i = it.i0 + sh.list[t] / T, j = it.j0 + sh.list[t] % T;
     q128 r = block_exact_dot(sh.u.K, P.k, P.A + i * P.sai, P.sal, P.B + j * P.sbj, P.sbl);
     if (threadIdx.x == 0) {
       q128* p = P.C + i * P.sci + j * P.scj;
@@ -223,7 +236,8 @@ __device__ void run_gemm_item(BShared& sh, const BProb& P, const BItem& it, wacc
   }
 }
 
-__device__ void run_gemv_item(BShared& sh, const BProb& P, const BItem& it, wacc* partials,
+template <class SH>
+__device__ void run_gemv_item(SH& sh, const BProb& P, const BItem& it, wacc* partials,
                               int* counters) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int64_t row = it.i0 + warp;
@@ -277,7 +291,8 @@ __device__ void run_gemv_item(BShared& sh, const BProb& P, const BItem& it, wacc
   }
 }
 
-__device__ void run_dot_item(BShared& sh, const BProb& P, const BItem& it, wacc* partials,
+template <class SH>
+__device__ void run_dot_item(SH& sh, const BProb& P, const BItem& it, wacc* partials,
                              int* counters) {
   wacc acc;
   wacc_init(acc);
@@ -316,10 +331,11 @@ __device__ void run_dot_item(BShared& sh, const BProb& P, const BItem& it, wacc*
   }
 }
 
+template <int T>
 __global__ void __launch_bounds__(kBThreads, 2)
     batched_persistent_kernel(const BProb* __restrict__ probs, const BItem* __restrict__ items,
                               int64_t nitems, int* queue, int* counters, wacc* partials) {
-  __shared__ BShared sh;
+  __shared__ BShared<T> sh;
   while (true) {
     if (threadIdx.x == 0) {
       sh.item = atomicAdd(queue, 1);
@@ -348,6 +364,7 @@ struct BatchPlan {
   int device = -1;
   int64_t nitems = 0, nprobs = 0, ngroups = 0, nparts = 0;
   int64_t grain = 0;
+  int tile = 32;  // gemm C tile edge (16 or 32)
   BProb* d_probs = nullptr;
   BItem* d_items = nullptr;
   int* d_counters = nullptr;  // [0] = queue head, [1..] group counters
@@ -432,8 +449,9 @@ static int resolve(const qblas_problem& q, BProb& P) {
 
 static int64_t cdiv(int64_t a, int64_t b) { return (a + b - 1) / b; }
 
-// Items of all problems for a granularity `grain` (products per item).
-static int build_items(std::vector<BProb>& probs, int64_t grain, std::vector<BItem>& items,
+// Items of all problems for a granularity `grain` (products per item) and a
+// gemm tile edge `tile`.
+static int build_items(std::vector<BProb>& probs, int64_t grain, int tile, std::vector<BItem>& items,
                        std::vector<int64_t>& cost, int64_t& ngroups, int64_t& nparts_total) {
   items.clear();
   cost.clear();
@@ -446,9 +464,9 @@ static int build_items(std::vector<BProb>& probs, int64_t grain, std::vector<BIt
     P.nparts = 1;
     if (P.op == kOpGemm) {
       if (P.m == 0 || P.n == 0 || P.k == 0) continue;  // level3.hpp:221
-      int64_t tm = cdiv(P.m, kBTile), tn = cdiv(P.n, kBTile);
+      int64_t tm = cdiv(P.m, tile), tn = cdiv(P.n, tile);
       int64_t kslices = cdiv(P.k, kBTK);
-      int64_t per = (int64_t)kBTile * kBTile * P.k;
+      int64_t per = (int64_t)tile * tile * P.k;
       int64_t parts = std::min<int64_t>(std::max<int64_t>(1, cdiv(per, grain)), kslices);
       int64_t kper = cdiv(kslices, parts) * kBTK;
       parts = cdiv(P.k, kper);
@@ -459,17 +477,17 @@ static int build_items(std::vector<BProb>& probs, int64_t grain, std::vector<BIt
             BItem it;
             it.prob = (int32_t)pi;
             it.part = (int32_t)p;
-            it.i0 = a * kBTile;
-            it.j0 = b * kBTile;
+            it.i0 = a * tile;
+            it.j0 = b * tile;
             it.l0 = p * kper;
             it.l1 = std::min(P.k, (p + 1) * kper);
             it.group = a * tn + b;
             items.push_back(it);
-            cost.push_back((int64_t)kBTile * kBTile * (it.l1 - it.l0));
+            cost.push_back((int64_t)tile * tile * (it.l1 - it.l0));
           }
       if (parts > 1) {
         ngroups += tm * tn;
-        nparts_total += tm * tn * parts * kBThreads * 4;
+        nparts_total += tm * tn * parts * tile * tile;  // one wide accumulator per output
       }
     } else if (P.op == kOpGemv) {
       if (P.m == 0 || P.n == 0) continue;  // level2.hpp:21,61
@@ -547,9 +565,13 @@ static int cuda_rc(cudaError_t e) {
   return kErrCuda;
 }
 
-static int plan_build(const qblas_problem* problems, int64_t count, int64_t grain, BatchPlan** out) {
+static const void* persistent_kernel(int tile) {
+  return tile == 16 ? (const void*)batched_persistent_kernel<16> : (const void*)batched_persistent_kernel<32>;
+}
+
+static int plan_build(const qblas_problem* problems, int64_t count, int64_t grain, int tile, BatchPlan** out) {
   *out = nullptr;
-  if (count < 0 || (count > 0 && !problems)) return kErrInvalidValue;
+  if (count < 0 || (count > 0 && !problems) || (tile != 16 && tile != 32)) return kErrInvalidValue;
   std::vector<BProb> probs((size_t)count);
   for (int64_t i = 0; i < count; ++i) {
     int rc = resolve(problems[i], probs[i]);
@@ -558,7 +580,7 @@ static int plan_build(const qblas_problem* problems, int64_t count, int64_t grai
   std::vector<BItem> items;
   std::vector<int64_t> cost;
   int64_t ngroups = 0, nparts = 0;
-  build_items(probs, grain, items, cost, ngroups, nparts);
+  build_items(probs, grain, tile, items, cost, ngroups, nparts);
   BatchPlan* p = new BatchPlan();
   cudaGetDevice(&p->device);
   p->nitems = (int64_t)items.size();
@@ -566,6 +588,7 @@ static int plan_build(const qblas_problem* problems, int64_t count, int64_t grai
   p->ngroups = ngroups;
   p->nparts = nparts;
   p->grain = grain;
+  p->tile = tile;
   int rc = kOk;
   if ((rc = cuda_rc(dev_malloc((void**)&p->d_probs, sizeof(BProb) * std::max<int64_t>(1, count)))) ||
       (rc = cuda_rc(dev_malloc((void**)&p->d_items, sizeof(BItem) * std::max<int64_t>(1, p->nitems)))) ||
@@ -588,7 +611,7 @@ static int plan_build(const qblas_problem* problems, int64_t count, int64_t grai
     plan_free(p);
     return rc;
   }
-  int per_sm = resident_blocks_per_sm((const void*)batched_persistent_kernel, kBThreads, 0);
+  int per_sm = resident_blocks_per_sm(persistent_kernel(tile), kBThreads, 0);
   p->blocks = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)device_sm_count() * per_sm, p->nitems));
   *out = p;
   return kOk;
@@ -599,21 +622,32 @@ static int plan_execute(BatchPlan* p, cudaStream_t s) {
   if (p->nitems == 0) return kOk;
   cudaError_t e = cudaMemsetAsync(p->d_counters, 0, sizeof(int) * (1 + p->ngroups), s);
   if (e != cudaSuccess) return cuda_rc(e);
-  batched_persistent_kernel<<<p->blocks, kBThreads, 0, s>>>(p->d_probs, p->d_items, p->nitems, p->d_counters,
-                                                            p->d_counters, p->d_partials);
+  if (p->tile == 16)
+    batched_persistent_kernel<16><<<p->blocks, kBThreads, 0, s>>>(p->d_probs, p->d_items, p->nitems, p->d_counters,
+                                                                  p->d_counters, p->d_partials);
+  else
+    batched_persistent_kernel<32><<<p->blocks, kBThreads, 0, s>>>(p->d_probs, p->d_items, p->nitems, p->d_counters,
+                                                                  p->d_counters, p->d_partials);
   return cuda_rc(cudaGetLastError());
 }
 
 // ---- autotuner ------------------------------------------------------------
-// Granularity (products per work item) candidates; the tuner times a fixed
-// calibration batch (shapes like the batched benchmark, sizes scaled down,
-// data generated on the device) at each and keeps the fastest.  The result
-// is cached per device in memory and in the file $QBLAS_AUTOTUNE_CACHE
-// (default $HOME/.cache/qblas_gb300_autotune.txt) as "<device name> <grain>".
-static const int64_t kGrains[] = {1 << 14, 1 << 15, 1 << 16, 1 << 17, 1 << 18};
+// Candidates: gemm tile edge (16, 32) x granularity (products per work item,
+// 2^14 .. 2^20).  The tuner times a fixed calibration batch (the shapes of
+// the batched benchmark, fewer problems, data generated on the device) at
+// each pair and keeps the fastest.  The result is cached per device in
+// memory and in the file $QBLAS_AUTOTUNE_CACHE (default
+// $HOME/.cache/qblas_gb300_autotune.txt) as "<device name> <grain> <tile>".
+static const int64_t kGrains[] = {1 << 14, 1 << 15, 1 << 16, 1 << 17, 1 << 18, 1 << 19, 1 << 20};
+static const int kTiles[] = {16, 32};
 static const int64_t kDefaultGrain = 1 << 16;
+static const int kDefaultTile = 32;
 static std::mutex g_tune_mu;
-static int64_t g_grain[64] = {0};
+struct TuneSetting {
+  int64_t grain;
+  int tile;
+};
+static TuneSetting g_setting[64] = {};
 
 static std::string cache_path() {
   const char* e = getenv("QBLAS_AUTOTUNE_CACHE");
@@ -631,20 +665,27 @@ static std::string device_key(int dev) {
   return k + "_sm" + std::to_string(prop.multiProcessorCount);
 }
 
-static int64_t cached_grain(int dev) {
+// The device's setting: tuned or set in this process, else the last line of
+// the cache file for this device, else the defaults.  A line without a tile
+// (an older cache) keeps the default tile.
+static TuneSetting cached_setting(int dev) {
   std::lock_guard<std::mutex> l(g_tune_mu);
-  if (dev < 0 || dev >= 64) return kDefaultGrain;
-  if (g_grain[dev]) return g_grain[dev];
+  if (dev < 0 || dev >= 64) return {kDefaultGrain, kDefaultTile};
+  if (g_setting[dev].grain) return g_setting[dev];
   FILE* f = fopen(cache_path().c_str(), "r");
   if (f) {
-    char name[256];
-    long long g;
+    char line[512], name[256];
     std::string key = device_key(dev);
-    while (fscanf(f, "%255s %lld", name, &g) == 2)
-      if (key == name && g > 0) g_grain[dev] = g;
+    while (fgets(line, sizeof line, f)) {
+      long long g = 0;
+      int t = kDefaultTile;
+      int n = sscanf(line, "%255s %lld %d", name, &g, &t);
+      if (n >= 2 && key == name && g >= 256 && (t == 16 || t == 32)) g_setting[dev] = {(int64_t)g, t};
+    }
     fclose(f);
   }
-  return g_grain[dev] ? g_grain[dev] : kDefaultGrain;
+  if (!g_setting[dev].grain) return {kDefaultGrain, kDefaultTile};
+  return g_setting[dev];
 }
 
 __global__ void fill_bits_kernel(uint64_t* p, int64_t n, uint64_t seed) {
@@ -662,9 +703,10 @@ __global__ void fill_bits_kernel(uint64_t* p, int64_t n, uint64_t seed) {
     p[i] = z;
 }
 
-static int run_autotune(int dev, int64_t* best_out) {
-  // calibration batch: 600 gemm (8..128), 600 gemv (16..1024), 600 dot (64..16384)
-  const int nper = 600;
+static int run_autotune(int dev, TuneSetting* best_out) {
+  // calibration batch: 800 each of gemm (m, n, k in 8..256), gemv (m, n in
+  // 16..2048) and dot (n in 64..65536), log-uniform sizes (about 2.5 GB)
+  const int nper = 800;
   uint64_t st = 0x2545F4914F6CDD1Dull;
   auto rnd = [&]() {
     st ^= st << 13;
@@ -686,9 +728,9 @@ static int run_autotune(int dev, int64_t* best_out) {
   };
   std::vector<Sz> sz;
   for (int i = 0; i < nper; ++i) {
-    Sz a{QBLAS_OP_GEMM, logu(8, 128), logu(8, 128), logu(8, 128)};
-    Sz b{QBLAS_OP_GEMV, logu(16, 1024), logu(16, 1024), 0};
-    Sz c{QBLAS_OP_DOT, 0, logu(64, 16384), 0};
+    Sz a{QBLAS_OP_GEMM, logu(8, 256), logu(8, 256), logu(8, 256)};
+    Sz b{QBLAS_OP_GEMV, logu(16, 2048), logu(16, 2048), 0};
+    Sz c{QBLAS_OP_DOT, 0, logu(64, 65536), 0};
     sz.push_back(a);
     sz.push_back(b);
     sz.push_back(c);
@@ -742,23 +784,24 @@ static int run_autotune(int dev, int64_t* best_out) {
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   float best_ms = 1e30f;
-  int64_t best = kDefaultGrain;
-  for (int64_t g : kGrains) {
-    BatchPlan* p = nullptr;
-    if (plan_build(probs.data(), (int64_t)probs.size(), g, &p) != kOk) continue;
-    plan_execute(p, s);  // warm-up
-    cudaEventRecord(e0, s);
-    for (int r = 0; r < 3; ++r) plan_execute(p, s);
-    cudaEventRecord(e1, s);
-    cudaEventSynchronize(e1);
-    float ms = 0;
-    cudaEventElapsedTime(&ms, e0, e1);
-    if (ms < best_ms) {
-      best_ms = ms;
-      best = g;
+  TuneSetting best = {kDefaultGrain, kDefaultTile};
+  for (int t : kTiles)
+    for (int64_t g : kGrains) {
+      BatchPlan* p = nullptr;
+      if (plan_build(probs.data(), (int64_t)probs.size(), g, t, &p) != kOk) continue;
+      plan_execute(p, s);  // warm-up
+      cudaEventRecord(e0, s);
+      for (int r = 0; r < 3; ++r) plan_execute(p, s);
+      cudaEventRecord(e1, s);
+      cudaEventSynchronize(e1);
+      float ms = 0;
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (ms < best_ms) {
+        best_ms = ms;
+        best = {g, t};
+      }
+      plan_free(p);
     }
-    plan_free(p);
-  }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   cudaStreamDestroy(s);
@@ -766,7 +809,7 @@ static int run_autotune(int dev, int64_t* best_out) {
   *best_out = best;
   {
     std::lock_guard<std::mutex> l(g_tune_mu);
-    g_grain[dev] = best;
+    g_setting[dev] = best;
   }
   std::string path = cache_path();
   std::string dir = path.substr(0, path.find_last_of('/'));
@@ -774,7 +817,7 @@ static int run_autotune(int dev, int64_t* best_out) {
   if (system(cmd.c_str()) == 0) {
     FILE* f = fopen(path.c_str(), "a");
     if (f) {
-      fprintf(f, "%s %lld\n", device_key(dev).c_str(), (long long)best);
+      fprintf(f, "%s %lld %d\n", device_key(dev).c_str(), (long long)best.grain, best.tile);
       fclose(f);
     }
   }
@@ -793,7 +836,8 @@ QBLAS_EXPORT int quadblas_batch_plan(const qblas_problem* problems, int64_t coun
     return QBLAS_ERR_NO_DEVICE;
   }
   qb::BatchPlan* p = nullptr;
-  int rc = qb::plan_build(problems, count, qb::cached_grain(dev), &p);
+  const qb::TuneSetting t = qb::cached_setting(dev);
+  int rc = qb::plan_build(problems, count, t.grain, t.tile, &p);
   *plan = p;
   return rc;
 }
@@ -816,25 +860,51 @@ QBLAS_EXPORT int quadblas_batch_info(void* plan, int64_t* info4) {
   return QBLAS_OK;
 }
 
+QBLAS_EXPORT int quadblas_batch_info_ex(void* plan, int64_t* info, int64_t n) {
+  qb::BatchPlan* p = static_cast<qb::BatchPlan*>(plan);
+  if (!p || (n > 0 && !info) || n < 0) return QBLAS_ERR_INVALID_VALUE;
+  const int64_t v[5] = {p->nitems, p->grain, p->blocks, p->ngroups, p->tile};
+  for (int64_t i = 0; i < n && i < 5; ++i) info[i] = v[i];
+  return QBLAS_OK;
+}
+
 QBLAS_EXPORT int quadblas_batch_autotune(int64_t* grain_out) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) {
     cudaGetLastError();
     return QBLAS_ERR_NO_DEVICE;
   }
-  int64_t g = 0;
-  int rc = qb::run_autotune(dev, &g);
-  if (grain_out) *grain_out = g;
+  qb::TuneSetting t = {0, 0};
+  int rc = qb::run_autotune(dev, &t);
+  if (grain_out) *grain_out = t.grain;
   return rc;
 }
 
-QBLAS_EXPORT int quadblas_batch_set_grain(int64_t grain) {
+QBLAS_EXPORT int quadblas_batch_setting(int64_t* grain, int* tile) {
   int dev = 0;
-  if (grain < 256 || cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    return QBLAS_ERR_NO_DEVICE;
+  }
+  const qb::TuneSetting t = qb::cached_setting(dev);
+  if (grain) *grain = t.grain;
+  if (tile) *tile = t.tile;
+  return QBLAS_OK;
+}
+
+// Sets the current device's granularity (>= 256 products per item) and gemm
+// tile edge (16 or 32; 0 keeps the current edge) for plans built afterwards.
+QBLAS_EXPORT int quadblas_batch_configure(int64_t grain, int tile) {
+  int dev = 0;
+  if (grain < 256 || (tile != 0 && tile != 16 && tile != 32) || cudaGetDevice(&dev) != cudaSuccess || dev < 0 ||
+      dev >= 64) {
     cudaGetLastError();
     return QBLAS_ERR_INVALID_VALUE;
   }
+  const qb::TuneSetting cur = qb::cached_setting(dev);
   std::lock_guard<std::mutex> l(qb::g_tune_mu);
-  qb::g_grain[dev] = grain;
+  qb::g_setting[dev] = {grain, tile ? tile : cur.tile};
   return QBLAS_OK;
 }
+
+QBLAS_EXPORT int quadblas_batch_set_grain(int64_t grain) { return quadblas_batch_configure(grain, 0); }

@@ -8,7 +8,6 @@ long accumulator), qdot = R.  A small work-item granularity forces split-k
 gemm tiles, column-split gemv rows and chunked dots, so the in-order merge
 of partials is exercised; a re-execution, a CUDA-graph replay and the
 autotuner are checked too."""
-import os
 
 import numpy as np
 import pytest
@@ -140,18 +139,22 @@ def check_all(O, ar, specs):
         assert Q.same_bits(g, expected(O, s)).all(), (s["op"], s["m"], s["n"], s["k"], s["layout"], s["ta"])
 
 
-def test_batch_mixed_with_splits(qlib, O, torch_cuda):
+@pytest.mark.parametrize("tile", [16, 32])
+def test_batch_mixed_with_splits(qlib, O, torch_cuda, tile):
     torch = torch_cuda
     rng = G.rng_for(777)
     ar, specs, probs = make_batch(torch, rng, 40, 40, 40)
-    api.batch_set_grain(1024)  # tiny items: split-k, split rows and chunked dots
-    plan = api.BatchPlan(probs)
-    info = plan.info()
-    assert info["split_groups"] > 0 and info["grain"] == 1024
-    plan.execute()
-    torch.cuda.synchronize()
-    check_all(O, ar, specs)
-    plan.close()
+    api.batch_configure(1024, tile)  # tiny items: split-k, split rows and chunked dots
+    try:
+        plan = api.BatchPlan(probs)
+        info = plan.info()
+        assert info["split_groups"] > 0 and info["grain"] == 1024 and info["tile"] == tile
+        plan.execute()
+        torch.cuda.synchronize()
+        check_all(O, ar, specs)
+        plan.close()
+    finally:
+        api.batch_configure(1 << 16, 32)
 
 
 def test_batch_reexecute_and_graph_replay(qlib, O, torch_cuda):
@@ -184,9 +187,14 @@ def test_batch_reexecute_and_graph_replay(qlib, O, torch_cuda):
     plan.close()
 
 
-def test_batch_autotune(qlib, torch_cuda, tmp_path):
-    os.environ["QBLAS_AUTOTUNE_CACHE"] = str(tmp_path / "tune.txt")
+def test_batch_autotune(qlib, torch_cuda, tmp_path, monkeypatch):
+    """Tile edge x granularity: the winner is in the candidate grid, set for
+    new plans and appended to the cache file as "<device> <grain> <tile>"."""
+    monkeypatch.setenv("QBLAS_AUTOTUNE_CACHE", str(tmp_path / "tune.txt"))
     g = api.batch_autotune()
-    assert g in (1 << 14, 1 << 15, 1 << 16, 1 << 17, 1 << 18)
+    assert g in [1 << e for e in range(14, 21)]
+    grain, tile = api.batch_setting()
+    assert grain == g and tile in (16, 32)
     text = (tmp_path / "tune.txt").read_text().split()
-    assert int(text[-1]) == g
+    assert int(text[-2]) == g and int(text[-1]) == tile
+    print({"grain": grain, "tile": tile})

@@ -7,9 +7,10 @@ full-mantissa uniform values: the shapes and item sizes (split-k tiles,
 column-split rows, chunked dots) that the benchmark runs, not a reduced
 case.  The batch goes through the autotuned plan, recorded in a CUDA graph
 and replayed.  At the autotuned granularity no item of this workload is
-split, so the batch is also planned at granularity 2^14, where qgemm tiles
-split along k, long qgemv rows along the columns and long dots into chunks,
-and that execution must give the same bits.
+split, so the batch is also planned with the other qgemm tile edge (16 or
+32) and at granularity 2^14, where qgemm tiles split along k, long qgemv rows
+along the columns and long dots into chunks; those executions must give the
+same bits.
 
 Every output must be bit-identical to the same problem run by its own
 device-pointer call (quadblas_batch_run_serial): both claim the correctly
@@ -71,6 +72,16 @@ def test_config4_batched_equals_one_by_one_and_oracle(qlib, O, torch_cuda, tmp_p
             pytest.fail(f"{diff.size} outputs differ, in {len(bad)} problems, first {[lay[i][:4] for i in bad[:5]]}")
         plan.close()
         del graph
+        # the other gemm tile edge at the same granularity
+        _, tile = api.batch_setting()
+        api.batch_configure(grain, 48 - tile)
+        plan = api.BatchPlan(probs)
+        assert plan.info()["tile"] == 48 - tile
+        out.copy_(c0)
+        plan.execute()
+        torch.cuda.synchronize()
+        assert torch.equal(batched, out), f"tile {48 - tile} execution differs"
+        plan.close()
         # small items: split-k tiles, column-split rows, chunked dots, merged in order
         api.batch_set_grain(1 << 14)
         plan = api.BatchPlan(probs)
@@ -82,7 +93,7 @@ def test_config4_batched_equals_one_by_one_and_oracle(qlib, O, torch_cuda, tmp_p
         plan.close()
     finally:
         api.set_method(0)
-        api.batch_set_grain(1 << 16)
+        api.batch_configure(1 << 16, 32)
 
     # a seeded sample of each kind against the exact oracle
     rng = np.random.default_rng(44)
