@@ -450,6 +450,10 @@ struct LongAcc {
     if (gb >= 32 * lo) {
       int d = (gb >> 5) - lo;
       uint32_t mask = (gb & 31) == 31 ? 0xffffffffu : ((1u << ((gb & 31) + 1)) - 1);
+      if (d >= n) {  // a result far below the subnormal range: every digit is below gb
+        d = n - 1;
+        mask = 0xffffffffu;
+      }
       st = (mag[d] & mask) != 0;
       for (int q = d - 1; q >= 0 && !st; --q) st = mag[q] != 0;
     }

@@ -27,12 +27,16 @@ c_vp = ctypes.c_void_p
 # directory in QBLAS_REFERENCE_DIR, else the read-only mount the reference is
 # checked out at on the build machine.  Where neither exists, _ref is skipped.
 REFERENCE_DIR = os.environ.get("QBLAS_REFERENCE_DIR", "/root/reference")
+# QBLAS_SANITIZE=1: the AddressSanitizer + UndefinedBehaviorSanitizer build
+SANITIZE = os.environ.get("QBLAS_SANITIZE", "") not in ("", "0")
+BUILD_DIR = os.path.join(HERE, "_build_san" if SANITIZE else "_build")
 
 
 def build(quiet: bool = True) -> None:
     """Compile the oracle (and oracle/_ref where the reference tree exists)."""
     ref = REFERENCE_DIR if os.path.isfile(os.path.join(REFERENCE_DIR, "include", "quadblas", "quadblas.hpp")) else ""
-    out = subprocess.run(["make", "-C", HERE, f"REF={ref}"], capture_output=True, text=True)
+    san = ["SAN=1"] if SANITIZE else []
+    out = subprocess.run(["make", "-C", HERE, f"REF={ref}"] + san, capture_output=True, text=True)
     if out.returncode != 0:
         raise RuntimeError("oracle build failed:\n" + out.stdout + out.stderr)
     if not quiet:
@@ -42,7 +46,7 @@ def build(quiet: bool = True) -> None:
 def lib():
     global _LIB
     if _LIB is None:
-        path = os.path.join(HERE, "_build", "liboracle.so")
+        path = os.path.join(BUILD_DIR, "liboracle.so")
         if not os.path.exists(path):
             build()
         _LIB = ctypes.CDLL(path)

@@ -1,6 +1,11 @@
 """Builds libquadblas_gpu.so in-tree (qblas_gb300/_build/) with nvcc for
 sm_103a only.  Translation units are compiled in parallel and linked with
-the static CUDA runtime, so the library needs nothing but the driver."""
+the static CUDA runtime, so the library needs nothing but the driver.
+
+With QBLAS_SANITIZE=1 in the environment the host code is instrumented with
+AddressSanitizer and UndefinedBehaviorSanitizer and the library goes to
+qblas_gb300/_build_san/ instead (load it with libasan and libubsan preloaded,
+as tests/run_sanitized.sh does)."""
 from __future__ import annotations
 
 import concurrent.futures as cf
@@ -12,13 +17,16 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
-BUILD = os.path.join(HERE, "_build")
+SANITIZE = os.environ.get("QBLAS_SANITIZE", "") not in ("", "0")
+BUILD = os.path.join(HERE, "_build_san" if SANITIZE else "_build")
 LIB = os.path.join(BUILD, "libquadblas_gpu.so")
+SAN_FLAGS = ["-Xcompiler", "-fsanitize=address", "-Xcompiler", "-fsanitize=undefined", "-Xcompiler",
+             "-fno-omit-frame-pointer", "-Xcompiler", "-fno-sanitize-recover=undefined"]
 
 SOURCES = ["level1.cu", "level2.cu", "level3.cu", "ozaki.cu", "ozgemv.cu", "batched.cu", "noalloc.cu", "capi.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-fvisibility=hidden",
-          "-I", CSRC, "-I", os.path.join(ROOT, "include")]
+          "-I", CSRC, "-I", os.path.join(ROOT, "include")] + (SAN_FLAGS if SANITIZE else [])
 
 
 def nvcc() -> str:
@@ -64,7 +72,7 @@ def build(verbose: bool = False) -> str:
     newest = max(os.path.getmtime(o) for o in objs)
     if not (os.path.exists(LIB) and os.path.getmtime(LIB) >= newest):
         tmp = LIB + ".tmp"
-        cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + objs + ["-cudart", "static"]
+        cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + objs + ["-cudart", "static"] + (SAN_FLAGS if SANITIZE else [])
         out = subprocess.run(cmd, capture_output=True, text=True)
         if out.returncode != 0:
             raise RuntimeError(f"link failed:\n{out.stdout}\n{out.stderr}")

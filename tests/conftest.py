@@ -36,12 +36,15 @@ def qlib():
 def sq():
     """The device soft-float core compiled as host C++ (tests/softquad_host.cpp)."""
     import ctypes
-    out = os.path.join(TESTS, "_build", "libsoftquad_host.so")
+    san = os.environ.get("QBLAS_SANITIZE", "") not in ("", "0")
+    out = os.path.join(TESTS, "_build_san" if san else "_build", "libsoftquad_host.so")
     src = os.path.join(TESTS, "softquad_host.cpp")
     deps = [src] + [os.path.join(ROOT, "qblas_gb300", "csrc", f) for f in ("softquad.cuh", "wacc.cuh", "exact.cuh", "ozaki.cuh", "ozgemv.cuh", "ozcrt.cuh")]
     if not os.path.exists(out) or os.path.getmtime(out) < max(os.path.getmtime(d) for d in deps):
         os.makedirs(os.path.dirname(out), exist_ok=True)
-        subprocess.run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-o", out, src], check=True)
+        flags = ["-fsanitize=address,undefined", "-fno-omit-frame-pointer", "-fno-sanitize-recover=undefined"]
+        subprocess.run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-o", out, src] + (flags if san else []),
+                       check=True)
     return ctypes.CDLL(out)
 
 
