@@ -42,7 +42,11 @@
 //                                  one accumulator collects every diagonal;
 //                       warp 17    TMA loads of A's k-steps into a ring of
 //                                  12 shared-memory slots (16 KB each,
-//                                  128-byte swizzle);
+//                                  128-byte swizzle), each with a bulk
+//                                  copy of x's B tile for the k-step into
+//                                  a ring of 16 B slots (a B slot is
+//                                  reused once the MMAs that read it
+//                                  completed);
 //                       warps 18-21 read the accumulator (tcgen05.ld), fold
 //                                  the diagonals and add into the row's
 //                                  wide accumulator; one partial per
@@ -94,19 +98,22 @@ constexpr int kOgStages = 4;                 // operand stages in flight
 constexpr int kOgTmemCols = 512;             // 128 + 4 * 72 = 416 used
 constexpr int kOgXRows = 48;                 // B rows: diagonal g of pair p at row g + 16 - 2p
 constexpr int kOgXLbo = kOgXRows * 16;       // 768
-constexpr int kOgXBytes = 2 * kOgXLbo;       // 1536: B operand of one k-step (shared memory)
+constexpr int kOgXBytes = 2 * kOgXLbo;       // 1536: B operand of one k-step
 constexpr int kOgSlotBytes = kOgRows * kOgKStep * 16;  // 16384: A elements of one k-step
 constexpr int kOgSlots = 12;                 // TMA ring: three chunks
+constexpr int kOgXSlots = 16;                // x's B tiles: k-step q in slot q % 16, reused after q's MMAs
 constexpr int kOgExpSlots = 8;
 constexpr int kOgXSpecial = 0x7FFFFFFF;      // x chunk holding NaN or inf
 constexpr int kOgNoGmax = 2 * kOgNoExp;
 // kind::f16, fp16 A and B (K-major), fp32 D, N = 32, M = 128
 constexpr uint32_t kOgIdesc = (1u << 4) | ((32u >> 3) << 17) | ((uint32_t)(kOgRows >> 4) << 24);
-// barriers: full[slots], empty[slots] (TMA ring), ready[stages], free[stages], tfull[accs],
-// tempty[accs], exp[8], rowmax[2][4] (the four split warps of a lane quadrant), drain
-constexpr int kOgBars = 2 * kOgSlots + 2 * kOgStages + 2 * kOgAccBufs + kOgExpSlots + 8 + 1;
-constexpr size_t kOgSmem = 1024 + (size_t)kOgSlots * kOgSlotBytes + (size_t)kOgStages * kOgXBytes +
+// barriers: full[slots], empty[slots] (TMA ring: A elements and x's B tile), ready[stages],
+// free[stages], tfull[accs], tempty[accs], exp[8], rowmax[2][4] (the four split warps of a
+// lane quadrant), drain, bempty[x slots] (the MMAs reading a B tile completed)
+constexpr int kOgBars = 2 * kOgSlots + 2 * kOgStages + 2 * kOgAccBufs + kOgExpSlots + 8 + 1 + kOgXSlots;
+constexpr size_t kOgSmem = 1024 + (size_t)kOgSlots * kOgSlotBytes + (size_t)kOgXSlots * kOgXBytes +
                            kOgExpSlots * kOgRows * 4 + 2 * 4 * kOgRows * 4 + kOgBars * 8 + 16;
+static_assert(kOgSmem <= 232448, "og_gemv_kernel shared memory");
 
 struct OgPartial {
   wacc acc;
@@ -181,11 +188,6 @@ __global__ void __launch_bounds__(32)
 // ---------------------------------------------------------------------------
 // Main kernel
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void st_shared_v4(uint32_t addr, uint32_t a, uint32_t b, uint32_t c, uint32_t d) {
-  asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "r"(a), "r"(b), "r"(c), "r"(d)
-               : "memory");
-}
-
 __device__ __forceinline__ uint4 ld_shared_v4(uint32_t addr) {
   uint4 v;
   asm volatile("ld.shared.v4.b32 {%0, %1, %2, %3}, [%4];" : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w) : "r"(addr));
@@ -249,8 +251,8 @@ __global__ void __launch_bounds__(kOgThreads, 1)
   const uint32_t raw = smem_u32(smem_raw);
   const uint32_t base = (raw + 1023u) & ~1023u;  // slots: 1024-byte aligned for the swizzle
   uint8_t* gbase = smem_raw + (base - raw);
-  const uint32_t xstage0 = base + kOgSlots * kOgSlotBytes;  // B operand of each stage
-  uint8_t* after = gbase + kOgSlots * kOgSlotBytes + kOgStages * kOgXBytes;
+  const uint32_t xslot0 = base + kOgSlots * kOgSlotBytes;  // x's B tiles
+  uint8_t* after = gbase + kOgSlots * kOgSlotBytes + kOgXSlots * kOgXBytes;
   int32_t* exps = reinterpret_cast<int32_t*>(after);                        // [8][128]
   uint32_t* emax = reinterpret_cast<uint32_t*>(after + kOgExpSlots * kOgRows * 4);  // [2][4][128]
   const uint32_t bar0 = base + (uint32_t)(after - gbase) + kOgExpSlots * kOgRows * 4 + 2 * 4 * kOgRows * 4;
@@ -265,11 +267,14 @@ __global__ void __launch_bounds__(kOgThreads, 1)
   auto rowmax_bar = [&](int b, int quad) {
     return bar1 + 8u * (2 * kOgStages + 2 * kOgAccBufs + kOgExpSlots + 4 * b + quad);
   };
-  const uint32_t drain_bar = bar0 + 8u * (kOgBars - 1);
+  const uint32_t drain_bar = bar0 + 8u * (kOgBars - 1 - kOgXSlots);
+  auto bempty_bar = [&](int s) { return bar0 + 8u * (kOgBars - kOgXSlots + s); };
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(gbase + (bar0 - base) + kOgBars * 8);
   // k-step q uses TMA slot q % kOgSlots (fill q / kOgSlots) and operand
   // stage q % kOgStages (use q / kOgStages)
   auto slot_of = [](uint32_t kq) { return (int)(kq % kOgSlots); };
+  auto xslot_of = [](uint32_t kq) { return (int)(kq % kOgXSlots); };
+  auto xfill_parity = [](uint32_t kq) { return (kq / kOgXSlots) & 1u; };
   auto fill_parity = [](uint32_t kq) { return (kq / kOgSlots) & 1u; };
   auto stage_of = [](uint32_t kq) { return (int)(kq % kOgStages); };
   auto use_parity = [](uint32_t kq) { return (kq / kOgStages) & 1u; };
@@ -280,6 +285,7 @@ __global__ void __launch_bounds__(kOgThreads, 1)
       mbar_init(full_bar(s), 1);
       mbar_init(empty_bar(s), kOgSplitWarps);
     }
+    for (int s = 0; s < kOgXSlots; ++s) mbar_init(bempty_bar(s), 1);
     for (int s = 0; s < kOgStages; ++s) {
       mbar_init(ready_bar(s), kOgSplitWarps);
       mbar_init(free_bar(s), 1);
@@ -313,16 +319,8 @@ __global__ void __launch_bounds__(kOgThreads, 1)
     // ---------------- split: thread per row (its tensor-memory lane), 2 columns per k-step ----------------
     const int qd = warp & 3, grp = warp >> 2;  // lane quadrant; columns 2*grp, 2*grp+1 of each k-step
     const int r = qd * 32 + lane;
-    const int tid = threadIdx.x;
     const uint32_t off0 = og_elem_offset<kLayout>(r, 2 * grp), off1 = og_elem_offset<kLayout>(r, 2 * grp + 1);
     const uint32_t tlane = tmem + ((uint32_t)(qd * 32) << 16) + kOgAccCols + 2 * grp;
-    const bool xcopy = tid < kOgXBytes / 16;
-    // chunk of the item being split, kept by counting (no 64-bit division in the loop)
-    const int nch = (int)P.nchunks;
-    int cw = (int)(w0 % P.nchunks);
-    uint4 xv_next = make_uint4(0, 0, 0, 0);
-    if (xcopy && w0 < w1)
-      xv_next = __ldg(reinterpret_cast<const uint4*>(P.xdig + (size_t)(kOgKSteps * cw) * kOgXBytes) + tid);
     uint32_t q = 0, it = 0;
     for (int64_t w = w0; w < w1 && ok; ++w, ++it) {
       // all k-steps of the chunk are needed for its row exponents
@@ -358,16 +356,6 @@ __global__ void __launch_bounds__(kOgThreads, 1)
       const uint32_t sp = bmax == 0x7FFFu ? 1u : 0u;
 #pragma unroll 1
       for (int ks = 0; ks < kOgKSteps; ++ks, ++q) {
-        // x's B tile of this k-step was fetched one k-step ahead; fetch the next
-        const uint4 xv = xv_next;
-        if (xcopy) {
-          const bool last = ks == kOgKSteps - 1;
-          const int nc = last ? (cw + 1 == nch ? 0 : cw + 1) : cw;
-          if (!last || w + 1 < w1)
-            xv_next = __ldg(reinterpret_cast<const uint4*>(
-                                P.xdig + (size_t)(kOgKSteps * nc + (last ? 0 : ks + 1)) * kOgXBytes) +
-                            tid);
-        }
         const uint32_t slot = base + slot_of(q) * kOgSlotBytes;
         const uint4 v0 = ld_shared_v4(slot + off0), v1 = ld_shared_v4(slot + off1);
         __syncwarp();
@@ -396,20 +384,15 @@ __global__ void __launch_bounds__(kOgThreads, 1)
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         if (ks == 0 && grp == 0) exps[(it % kOgExpSlots) * kOgRows + r] = (E << 1) | (int)sp;
         og_store_pairs<0>(tlane + st * kOgStageCols, W, sg, bs);
-        if (xcopy) {
-          st_shared_v4(xstage0 + st * kOgXBytes + tid * 16, xv.x, xv.y, xv.z, xv.w);
-          fence_proxy_async_smem();
-        }
         tmem_st_wait();
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
         __syncwarp();
         if (lane == 0) mbar_arrive(ready_bar(st));
       }
-      if (++cw == nch) cw = 0;
     }
     if (!ok && lane == 0) atomicExch(P.err, 1);
   } else if (warp == kOgLoadWarp) {
-    // ---------------- TMA loads of A into the slot ring ----------------
+    // ---------------- TMA loads of A and x's B tiles into the slot ring ----------------
     if (lane == 0) {
       // TMA cursor: tile, chunk and k-step of the next load, kept by counting
       const int nch = (int)P.nchunks;
@@ -417,6 +400,7 @@ __global__ void __launch_bounds__(kOgThreads, 1)
       auto load_kstep = [&](uint32_t kq) {  // k-step kq of this CTA (loaded in order) into its slot
         const int64_t tile = ld_tile;
         const int col0 = ld_c * kOgChunk + ld_ks * kOgKStep;
+        const uint8_t* xsrc = P.xdig + (size_t)(kOgKSteps * ld_c + ld_ks) * kOgXBytes;
         if (++ld_ks == kOgKSteps) {
           ld_ks = 0;
           if (++ld_c == nch) {
@@ -425,7 +409,8 @@ __global__ void __launch_bounds__(kOgThreads, 1)
           }
         }
         const uint32_t slot = base + slot_of(kq) * kOgSlotBytes, bar = full_bar(slot_of(kq));
-        mbar_expect_tx(bar, kOgSlotBytes);
+        mbar_expect_tx(bar, kOgSlotBytes + kOgXBytes);
+        bulk_load(xslot0 + xslot_of(kq) * kOgXBytes, xsrc, kOgXBytes, bar);
         if (kLayout == kOgRowMajor) {
           tma_load_2d(slot, &tmA, bar, 4 * col0, (int)(tile * kOgRows));
         } else if (kLayout == kOgColGroups) {
@@ -437,8 +422,9 @@ __global__ void __launch_bounds__(kOgThreads, 1)
       };
       uint32_t issued = 0;
       for (; issued < nks && ok; ++issued) {
-        // the split warps released this slot's previous k-step
-        if (!mbar_wait_ns(empty_bar(slot_of(issued)), fill_parity(issued) ^ 1u, P.wait_ns)) {
+        // the split warps released this slot's previous k-step and its MMAs completed
+        if (!mbar_wait_ns(empty_bar(slot_of(issued)), fill_parity(issued) ^ 1u, P.wait_ns) ||
+            !mbar_wait_ns(bempty_bar(xslot_of(issued)), xfill_parity(issued) ^ 1u, P.wait_ns)) {
           ok = false;
           break;
         }
@@ -454,7 +440,7 @@ __global__ void __launch_bounds__(kOgThreads, 1)
   } else if (warp == kOgMmaWarp) {
     // ---------------- MMA issue ----------------
     if (lane == 0) {
-      const uint64_t db0 = smem_desc_noswizzle(xstage0 + 16 * 16, kOgXLbo, 128);
+      const uint64_t db0 = smem_desc_noswizzle(xslot0 + 16 * 16, kOgXLbo, 128);
       uint32_t q = 0, it = 0;
       bool any_mma = false;
       for (int64_t w = w0; w < w1 && ok; ++w, ++it) {
@@ -473,15 +459,16 @@ __global__ void __launch_bounds__(kOgThreads, 1)
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
           if (ks == 0) mbar_arrive(exp_bar(it % kOgExpSlots));  // this item's row exponents are written
           const uint32_t ta = tmem + kOgAccCols + st * kOgStageCols;
-          // B of pair pp: 16 - 2pp rows into the stage's tile (the descriptor
+          // B of pair pp: 16 - 2pp rows into the slot's tile (the descriptor
           // address field counts 16-byte units)
-          const uint64_t dbs = db0 + (uint64_t)(st * (kOgXBytes / 16));
+          const uint64_t dbs = db0 + (uint64_t)(xslot_of(q) * (kOgXBytes / 16));
 #pragma unroll
           for (int pp = 0; pp < kOgPairs; ++pp)
             mma_f16kind_ta(tmem + (uint32_t)(tb * 32), ta + pp * kOgTileCols, dbs - (uint64_t)(2 * pp), kOgIdesc,
                            (ks | pp) ? 1u : 0u);
           any_mma = true;
           mma_commit(free_bar(st));
+          mma_commit(bempty_bar(xslot_of(q)));
         }
         if (!ok) break;
         if (!(P.withhold && it == 0)) mma_commit(tfull_bar(tb));
