@@ -514,13 +514,16 @@ struct BandCopy {
 
 // Copies rows [r0, r1) of op(A) into the staged A on kSideACopy, after the
 // copy of B (which the first digit products need whole), and makes stream s
-// wait for them; the copy of C is queued behind the last band.  When op(A)'s
-// rows are not contiguous, the first band copies all of A.
+// wait for them.  When op(A)'s rows are not contiguous, the first band
+// copies all of A.  With c_banded (C's rows contiguous, as the fold's row
+// bands need) the same rows of C follow each band of A and c_ready is
+// recorded after them; otherwise all of C is queued behind the last band.
 struct ARowCopy {
   DevState* st;
   const void* host_A;
   const void* host_C;
   GemmPlan p;
+  bool c_banded;
   static int rows(void* ctx, int64_t r0, int64_t r1, cudaStream_t s) {
     ARowCopy* a = static_cast<ARowCopy*>(ctx);
     DevState& d = *a->st;
@@ -541,7 +544,13 @@ struct ARowCopy {
                           cudaMemcpyHostToDevice, cs);
     if (e == cudaSuccess) e = cudaEventRecord(d.ev[kEvACopied], cs);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(s, d.ev[kEvACopied], 0);
-    if (e == cudaSuccess && r1 == g.m) {
+    if (e == cudaSuccess && a->c_banded) {
+      const int64_t coff = r0 * g.sci, ccnt = (r1 - 1 - r0) * g.sci + g.n;
+      e = cudaMemcpyAsync(static_cast<char*>(d.buf[kSlotC]) + coff * 16,
+                          static_cast<const char*>(a->host_C) + coff * 16, (size_t)ccnt * 16,
+                          cudaMemcpyHostToDevice, cs);
+      if (e == cudaSuccess) e = cudaEventRecord(d.ev[kEvCReady], cs);
+    } else if (e == cudaSuccess && r1 == g.m) {
       cudaStream_t cc = d.side[kSideC];
       e = cudaStreamWaitEvent(cc, d.ev[kEvACopied], 0);
       if (e == cudaSuccess)
@@ -604,9 +613,12 @@ int host_gemm(char layout, char transa, char transb, int64_t m, int64_t n, int64
     // C comes back band by band on kSideC while later bands fold.
     if ((rc = ensure_side_streams(st))) return rc;
     BandCopy bc{&st, C, p, qb::kOk};
-    ARowCopy ac{&st, A, C, p};
-    qb::OzakiOverlap ov{st.side[kSideB], st.ev[kEvBDone], st.ev[kEvCReady], &BandCopy::done, &bc,
-                        &ARowCopy::rows, &ac, st.side[kSideA], st.ev[kEvADone]};
+    // C by row bands when its rows are contiguous and the fold goes by row bands
+    const bool c_banded = p.g.scj == 1 && p.g.sci >= p.g.n && p.g.m >= 64;
+    ARowCopy ac{&st, A, C, p, c_banded};
+    qb::OzakiOverlap ov{st.side[kSideB],      st.ev[kEvBDone], st.ev[kEvCReady], &BandCopy::done, &bc,
+                        &ARowCopy::rows,      &ac,             st.side[kSideA],  st.ev[kEvADone],
+                        c_banded ? 1 : 0};
     if ((rc = h2d(st.buf[kSlotB], B, p.extB, st.side[kSideB])) ||
         (rc = cuda_status(cudaEventRecord(st.ev[kEvBCopied], st.side[kSideB]))))
       return rc;

@@ -103,6 +103,9 @@ struct OzakiOverlap {
   void* a_ctx;
   cudaStream_t a_stream;
   cudaEvent_t a_done;
+  // nonzero: a_rows also copies the same rows of C and records c_ready after
+  // them, so rows of C can be folded as soon as their products are done
+  int c_banded;
 };
 // `report`, when not null, is a device-accessible word (mapped host memory)
 // that the fold sets to 1 if a wait of the tensor-core kernel timed out.

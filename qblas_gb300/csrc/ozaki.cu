@@ -16,27 +16,42 @@
 // tcgen05 kind::i8 does not exist on sm_103a, so integer digits travel as
 // 16-bit floats: bf16 holds every integer up to 256 exactly, fp16 up to 2048.
 //
+// The default scheme is the residue (CRT) form of the same splitting
+// (ozcrt.cuh): the truncated integers are reduced modulo N coprime moduli
+// p_q in (256, 513], one exact residue GEMM per modulus, and the integer
+// result is rebuilt by the Chinese remainder theorem before the rounding.
+//
 // Kernels:
-//   ozaki_scale_kernel  : S_i = max_l (exponent(x_il) + 1) per row of a
-//                         strided view (A, or B^T), plus NaN/inf flags
+//   ozaki_scale_kernel,   : S_i = max_l (exponent(x_il) + 1) per row of a
+//   ozaki_scale_rows_kernel strided view (A, or B^T), plus NaN/inf flags
 //   ozaki_split_kernel  : digits of every element, written digit-major and
 //                         K-major: D[t][row][l], zero padded
+//   ozaki_crt_split_tc_kernel: residues of every element on the tensor cores
+//                         (byte rows of the scaled integer times a table of
+//                         256^j mod p_q), one fp32 remainder per residue
 //   ozaki_mma_kernel    : persistent, warp-specialised: warp 0 issues TMA
 //                         loads (128B-swizzled 64-wide K slices of A_t and
 //                         B_u) into a 4-stage shared-memory ring, warp 1
 //                         issues tcgen05.mma (M=128, N=256, K=16) into one
 //                         of two 256-column fp32 accumulators in tensor
 //                         memory, warps 2..9 read the accumulators with
-//                         tcgen05.ld, convert to int32 and sum a diagonal
-//                         in registers, then store C_g[row][col] (int32).
-//                         Every mbarrier wait is bounded (1 s); on timeout
-//                         the kernel records an error, drains its own
-//                         copies and MMAs, frees tensor memory and exits.
+//                         tcgen05.ld and store a diagonal's int32 sum
+//                         (digit pairs) or a modulus's u16 residue (CRT).
+//                         With two or more tile rows, CTAs run in clusters
+//                         of two over vertically adjacent tiles and each
+//                         loads half of the shared B slice, multicast to
+//                         both.  Every mbarrier wait is bounded (1 s); on
+//                         timeout the kernel records an error, drains its
+//                         own copies and MMAs, frees tensor memory and exits.
 //   ozaki_fold_kernel   : Horner fold of C_0..C_G (and k passes) per output,
 //                         one rounding, reference epilogue
+//   ozaki_crt_pass_sum_kernel, ozaki_crt_fold_tc_kernel: the residues of k
+//                         passes summed mod p_q; the CRT reconstruction with
+//                         its word sums on the tensor cores (y_q times the
+//                         bytes of M / p_q), one rounding, reference epilogue
 //   ozaki_special_kernel: outputs whose row or column holds NaN or inf, by a
 //                         direct wide-accumulator dot, so specials keep IEEE
-//                         semantics
+//                         semantics (returns at once when there are none)
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
@@ -1475,7 +1490,10 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scr
   if (banded) {
     const int waves = (tiles + sms - 1) / sms;
     band_tiles = ((waves + 7) / 8) * sms;
-    if (pair) band_tiles = (band_tiles + 2 * tiles_n - 1) / (2 * tiles_n) * (2 * tiles_n);  // whole tile-row pairs
+    if (pair)
+      band_tiles = (band_tiles + 2 * tiles_n - 1) / (2 * tiles_n) * (2 * tiles_n);  // whole tile-row pairs
+    else
+      band_tiles = (band_tiles + tiles_n - 1) / tiles_n * tiles_n;  // whole tile rows
   }
   // 3. fold + epilogue of rows [i0, i1) (the diagonal planes keep their
   // m_pad x n_pad shape); with a caller copying C out band by band, each
@@ -1497,7 +1515,8 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scr
   bool c_waited = false;
   auto fold_rows = [&](int64_t i0, int64_t i1) -> cudaError_t {
     cudaError_t ee;
-    if (ov && !c_waited) {
+    // C whole: one wait; C by bands: the latest record covers every row cut so far
+    if (ov && (!c_waited || ov->c_banded)) {
       if ((ee = cudaStreamWaitEvent(st, ov->c_ready, 0)) != cudaSuccess) return ee;
       c_waited = true;
     }
@@ -1586,11 +1605,13 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scr
       }
       if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
-    // rows whose tiles are all done can be folded while later bands multiply,
-    // but only once every row of op(A) has been handed to the caller: the
-    // caller queues the copy of C (and records c_ready) with the last rows,
-    // and a fold enqueued before that record would not wait for C
-    if (banded && fold_banded && t1 < tiles && rows_cut >= L.m_pad) {
+    // rows whose tiles are all done are folded before the next band
+    // multiplies (so that their copy back overlaps the later bands), once
+    // their rows of C are on the device: with C copied band by band
+    // together with op(A)'s rows, at once; with C copied whole after op(A)'s
+    // last rows, only then (a fold enqueued before that record would not
+    // wait for C)
+    if (banded && fold_banded && t1 < tiles && (ov->c_banded || rows_cut >= L.m_pad)) {
       const int64_t rows_done = std::min<int64_t>(g.m, (int64_t)(t1 / tiles_n) * kBM);
       if (rows_done > rows_folded) {
         if ((e = fold_rows(rows_folded, rows_done)) != cudaSuccess) return e;
@@ -1599,11 +1620,12 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scr
     }
   }
   prof_record(pe, 2, st);
-  // the remaining rows (all of them without banding), in up to 4 bands when
-  // the caller copies C out band by band
+  // the remaining rows (all of them without banding), in up to 4 bands of at
+  // least 1024 rows when the caller copies C out band by band (a few rows
+  // left after the interleaved folds go in one band)
   {
     const int64_t left = g.m - rows_folded;
-    const int64_t nb = fold_banded ? 4 : 1;
+    const int64_t nb = fold_banded ? std::max<int64_t>(1, std::min<int64_t>(4, left / 1024)) : 1;
     const int64_t band_rows = ((left + nb - 1) / nb + 7) / 8 * 8;
     for (int64_t i0 = rows_folded; i0 < g.m; i0 += band_rows)
       if ((e = fold_rows(i0, std::min(g.m, i0 + band_rows))) != cudaSuccess) return e;

@@ -127,18 +127,23 @@ def test_crt_accuracy_spread(crt, O, torch_cuda, size):
 
 
 @pytest.mark.parametrize("scheme", [2, 1])
-def test_host_pointer_row_bands_match_device(crt, torch_cuda, scheme):
+@pytest.mark.parametrize("shape", [(1664, 3072, 96), (4000, 2100, 70)])
+def test_host_pointer_row_bands_match_device(crt, torch_cuda, scheme, shape):
     """A host-pointer qgemm with more 128 x 256 tiles than the GPU has SMs
-    (13 x 12 = 156 tiles) runs in row bands: A is copied band by band, C after
-    A, and C is folded and copied back in row bands.  With beta != 0 and a
-    random C the result must equal the device-pointer call's bit for bit; a
-    fold that ran before C arrived would read the staging buffer's previous
-    contents (another call's result, left there on purpose)."""
+    runs in row bands: A is copied band by band with the same rows of C
+    behind each band, and C is folded and copied back in row bands.  At
+    13 x 12 = 156 tiles the products are one band and the fold four; at
+    32 x 9 = 288 tiles (m and n off the tile grid) the products are two
+    bands, the rows of the first are folded before the second multiplies,
+    and the rest in one band.  With beta != 0 and a random C the result must
+    equal the device-pointer call's bit for bit; a fold that ran before its
+    rows of C arrived would read the staging buffer's previous contents
+    (another call's result, left there on purpose)."""
     torch = torch_cuda
     api.set_ozaki_scheme(scheme)
     api.set_ozaki_slices(15)
     api.set_ozaki_digit_bits(9)
-    m, n, k = 1664, 3072, 96
+    m, n, k = shape
     rng = G.rng_for(424 + scheme)
     A, B, C = G.spread_uniform(rng, m * k), G.spread_uniform(rng, k * n), G.uniform_full(rng, m * n)
     alpha, beta = Q.scalar(1.25), Q.scalar(-0.75)
