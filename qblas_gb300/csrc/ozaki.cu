@@ -686,13 +686,21 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
           const uint32_t taddr =
               tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(buf * kBN + half * (kBN / 2));
+          // 16 columns at a time, the next load in flight while these convert
+          uint32_t ra[16], rb[16];
+          tmem_ld16_nowait(taddr, ra);
 #pragma unroll
           for (int c = 0; c < kBN / 2; c += 32) {
-            uint32_t r[32];
-            tmem_ld32(taddr + (uint32_t)c, r);
+            tmem_ld_wait();
+            tmem_ld16_nowait(taddr + (uint32_t)(c + 16), rb);
 #pragma unroll
-            for (int i = 0; i < 32; ++i) acc[c + i] += __float2int_rn(__uint_as_float(r[i]));
+            for (int i = 0; i < 16; ++i) acc[c + i] += __float2int_rn(__uint_as_float(ra[i]));
+            tmem_ld_wait();
+            if (c + 32 < kBN / 2) tmem_ld16_nowait(taddr + (uint32_t)(c + 32), ra);
+#pragma unroll
+            for (int i = 0; i < 16; ++i) acc[c + 16 + i] += __float2int_rn(__uint_as_float(rb[i]));
           }
+          tmem_ld_wait();
           asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
           __syncwarp();
           if (lane == 0) mbar_arrive(tempty_bar(buf));
