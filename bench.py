@@ -373,7 +373,9 @@ def batched_config4(torch, api, rank, reps=3):
             "autotuned": {"grain": grain, "tile": tile, "candidates": "tile {16, 32} x grain 2^14..2^20"},
             "autotune_ms": round(tune_s * 1e3, 1), "launches_per_batch": 1,
             "parity": "bit-identical to one-by-one" if same else "MISMATCH against one-by-one",
-            "method_mix": {"softfloat_wide_accumulator": len(probs), "ozaki": 0}, "quad_flops": flops}
+            "method_mix": {"softfloat_wide_accumulator": len(probs) - info["ozaki_problems"],
+                           "ozaki_grouped_residues": info["ozaki_problems"], "ozaki_tiles": info["ozaki_tiles"]},
+            "quad_flops": flops}
 
 
 def oracle_accuracy(W, C, rank, samples=512):
@@ -639,6 +641,11 @@ def main():
                 torch.cuda.empty_cache()
             api.set_method(1)
             secondary["batched_config4"] = batched_config4(torch, api, rank)
+            # the same batch under the Ozaki method: qgemm problems with m n k >= 2^20 on the
+            # grouped residue path (normwise accurate, as their single calls), the rest as above
+            api.set_method(2)
+            secondary["batched_config4_ozaki"] = batched_config4(torch, api, rank)
+            api.set_method(1)
             S = Qgemm(torch, 512, 512, 512, seed=0xC0FFEE, spread=False)
             ms2 = time_steps(torch, S.step, 20, 3, dist) / 20
             secondary["qgemm512_softfloat"] = {"value": round(S.flops() / (ms2 * 1e-3) / 1e9, 3),

@@ -160,7 +160,14 @@ int quadblas_qdot_dev_noalloc(int64_t n, const void *dx, int64_t incx, const voi
  * of one plan must not overlap.  quadblas_batch_autotune times a calibration
  * batch at every pair of gemm tile edge (16, 32) and granularity (2^14 ..
  * 2^20 products per item) and caches the best pair per device (in memory and
- * in $QBLAS_AUTOTUNE_CACHE, default $HOME/.cache/qblas_gb300_autotune.txt). */
+ * in $QBLAS_AUTOTUNE_CACHE, default $HOME/.cache/qblas_gb300_autotune.txt).
+ * Under quadblas_set_method(QBLAS_METHOD_OZAKI), qgemm problems with
+ * m*n*k >= QBLAS_BATCH_OZAKI_MIN (environment, default 2^20) and k <= 8192
+ * run, as their single calls would, on the tensor cores: all of them in one
+ * grouped residue (CRT) chain of launches after the persistent kernel, in
+ * the same stream; the plan then allocates their stacked operands and
+ * residue planes (about 2 N (rows + 256-padded columns) k + 2 N 32768 x tiles
+ * bytes for N moduli). */
 enum { QBLAS_OP_GEMM = 0, QBLAS_OP_GEMV = 1, QBLAS_OP_DOT = 2 };
 
 typedef struct {
@@ -181,7 +188,8 @@ int quadblas_batch_execute(void *plan, void *stream);
 int quadblas_batch_destroy(void *plan);
 /* info4: work items, granularity (products per item), blocks, split groups */
 int quadblas_batch_info(void *plan, int64_t *info4);
-/* info[0..n): work items, granularity, blocks, split groups, gemm tile edge */
+/* info[0..n): work items, granularity, blocks, split groups, gemm tile edge,
+ * qgemm problems on the grouped tensor-core path, their 128 x 256 tiles */
 int quadblas_batch_info_ex(void *plan, int64_t *info, int64_t n);
 int quadblas_batch_autotune(int64_t *grain_out);
 /* The current device's setting for new plans (tuned, set, cached or default). */
@@ -189,12 +197,15 @@ int quadblas_batch_setting(int64_t *grain, int *tile);
 /* Sets granularity (>= 256) and gemm tile edge (16 or 32; 0 keeps it). */
 int quadblas_batch_configure(int64_t grain, int tile);
 int quadblas_batch_set_grain(int64_t grain);
+/* Smallest m*n*k routed to the grouped tensor-core path under the Ozaki
+ * method, for plans built afterwards (0: QBLAS_BATCH_OZAKI_MIN or 2^20). */
+int quadblas_batch_set_ozaki_min(int64_t products);
 /* The same problems without the batch: one device-pointer call per problem
- * (quadblas_qgemm_dev with the soft-float method, quadblas_qgemv_dev,
+ * (quadblas_qgemm_dev with the soft-float method, or the Ozaki method for the
+ * problems the batch gives to the tensor cores; quadblas_qgemv_dev,
  * quadblas_qdot_dev), in order, on `stream`, from a C loop.  It is the
  * one-call-per-problem baseline the batched launch is measured against, and
- * its results are bit-identical to quadblas_batch_execute's (both are the
- * correctly rounded sums through the single-call epilogues).  Returns the
+ * its results are bit-identical to quadblas_batch_execute's.  Returns the
  * first failing call's status. */
 int quadblas_batch_run_serial(const qblas_problem *problems, int64_t count, void *stream);
 

@@ -51,6 +51,7 @@ _SIGS = {
     "quadblas_batch_info_ex": (ci, [vp, vp, i64]),
     "quadblas_batch_setting": (ci, [vp, vp]),
     "quadblas_batch_configure": (ci, [i64, ci]),
+    "quadblas_batch_set_ozaki_min": (ci, [i64]),
     "quadblas_batch_run_serial": (ci, [vp, i64, vp]),
     # configuration
     "quadblas_set_method": (ci, [ci]),

@@ -205,9 +205,10 @@ class BatchPlan:
         check(load().quadblas_batch_execute(self.handle, _stream(stream)))
 
     def info(self) -> dict:
-        out = (ctypes.c_int64 * 5)()
-        check(load().quadblas_batch_info_ex(self.handle, out, 5))
-        return {"items": out[0], "grain": out[1], "blocks": out[2], "split_groups": out[3], "tile": out[4]}
+        out = (ctypes.c_int64 * 7)()
+        check(load().quadblas_batch_info_ex(self.handle, out, 7))
+        return {"items": out[0], "grain": out[1], "blocks": out[2], "split_groups": out[3], "tile": out[4],
+                "ozaki_problems": out[5], "ozaki_tiles": out[6]}
 
     def close(self) -> None:
         if self.handle:
@@ -240,3 +241,9 @@ def batch_setting() -> tuple:
 
 def batch_configure(grain: int, tile: int = 0) -> None:
     check(load().quadblas_batch_configure(grain, tile))
+
+
+def batch_set_ozaki_min(products: int) -> None:
+    """Smallest m*n*k of a qgemm problem that new plans run on the grouped
+    tensor-core path under the Ozaki method (0 = the default, 2^20)."""
+    check(load().quadblas_batch_set_ozaki_min(products))

@@ -32,6 +32,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -370,6 +371,10 @@ struct BatchPlan {
   int* d_counters = nullptr;  // [0] = queue head, [1..] group counters
   wacc* d_partials = nullptr;
   int blocks = 0;
+  // qgemm problems on the grouped residue path (method 2, large enough)
+  int64_t n_ozaki = 0;
+  OzakiGroup grp = {};
+  void* d_grp = nullptr;  // one allocation: rows, tiles, problems, stacked operands, scratch
 };
 
 static bool is_trans(char t) { return t == 'T' || t == 't' || t == 'C' || t == 'c'; }
@@ -547,16 +552,6 @@ static int build_items(std::vector<BProb>& probs, int64_t grain, int tile, std::
   return kOk;
 }
 
-static int plan_free(BatchPlan* p) {
-  if (!p) return kOk;
-  cudaFree(p->d_probs);
-  cudaFree(p->d_items);
-  cudaFree(p->d_counters);
-  cudaFree(p->d_partials);
-  delete p;
-  return kOk;
-}
-
 static int cuda_rc(cudaError_t e) {
   if (e == cudaSuccess) return kOk;
   cudaGetLastError();
@@ -565,22 +560,150 @@ static int cuda_rc(cudaError_t e) {
   return kErrCuda;
 }
 
+static int plan_free(BatchPlan* p) {
+  if (!p) return kOk;
+  cudaFree(p->d_probs);
+  cudaFree(p->d_items);
+  cudaFree(p->d_counters);
+  cudaFree(p->d_partials);
+  cudaFree(p->d_grp);
+  delete p;
+  return kOk;
+}
+
+// ---- qgemm problems on the grouped residue path ----------------------------
+// Under method 2 a qgemm problem with m n k at or above the threshold runs on
+// the tensor cores, like its single call: all such problems of the batch go
+// through one chain of launches (launch_gemm_ozaki_grouped) after the
+// persistent kernel, in the same stream, so the plan stays one graph.  The
+// digits are those of the single call; the moduli are taken for the largest
+// k of the group (more moduli than a problem needs reconstruct the same
+// integer), so every output is bit-identical to its single call's.
+constexpr int64_t kRouteMaxK = 8192;  // one k pass
+
+static std::atomic<int64_t> g_route_min{0};  // quadblas_batch_set_ozaki_min; 0: environment or default
+
+static int64_t route_min_products() {
+  const int64_t set = g_route_min.load();
+  if (set > 0) return set;
+  static const int64_t v = [] {
+    const char* e = getenv("QBLAS_BATCH_OZAKI_MIN");
+    const long long x = e ? atoll(e) : 0;
+    return x > 0 ? (int64_t)x : (int64_t)1 << 20;
+  }();
+  return v;
+}
+
+static int64_t rup64(int64_t v, int64_t a) { return (v + a - 1) / a * a; }
+
+static bool routed(const BProb& P) {
+  return P.op == kOpGemm && P.m > 0 && P.n > 0 && P.k > 0 && batch_gemm_routed(P.m, P.n, P.k);
+}
+
+// The stacked rows, tiles and problem table of the routed problems, the
+// stacked operand buffers (zeroed) and the scratch, in one allocation.
+static int build_group(const std::vector<BProb>& probs, const std::vector<char>& route, BatchPlan* p) {
+  std::vector<OzakiGroupRow> rows_a, rows_b;
+  std::vector<OzakiGroupTile> tiles;
+  std::vector<OzakiGroupProb> gp;
+  int64_t kmax = 0;
+  for (size_t i = 0; i < probs.size(); ++i)
+    if (route[i]) kmax = std::max(kmax, probs[i].k);
+  if (kmax == 0) return kOk;
+  const int64_t k_pad = rup64(kmax, 64);
+  for (size_t i = 0; i < probs.size(); ++i) {
+    if (!route[i]) continue;
+    const BProb& P = probs[i];
+    const int64_t m_pad = rup64(P.m, 128), n_pad = rup64(P.n, 256);
+    const int32_t a0 = (int32_t)(rows_a.size() / 128), b0 = (int32_t)(rows_b.size() / 256);
+    for (int64_t r = 0; r < m_pad; ++r)
+      rows_a.push_back(r < P.m ? OzakiGroupRow{P.A + r * P.sai, P.sal, P.k} : OzakiGroupRow{nullptr, 0, 0});
+    for (int64_t c = 0; c < n_pad; ++c)
+      rows_b.push_back(c < P.n ? OzakiGroupRow{P.B + c * P.sbj, P.sbl, P.k} : OzakiGroupRow{nullptr, 0, 0});
+    const int32_t pi = (int32_t)gp.size();
+    for (int64_t a = 0; a < m_pad / 128; ++a)
+      for (int64_t b = 0; b < n_pad / 256; ++b)
+        tiles.push_back(OzakiGroupTile{a0 + (int32_t)a, b0 + (int32_t)b, pi, (int32_t)(128 * a), (int32_t)(256 * b), {0, 0, 0}});
+    OzakiGroupProb q;
+    q.C = P.C;
+    q.sci = P.sci;
+    q.scj = P.scj;
+    q.m = P.m;
+    q.n = P.n;
+    q.k = P.k;
+    q.alpha = P.alpha;
+    q.beta = P.beta;
+    q.A = P.A;
+    q.sai = P.sai;
+    q.sal = P.sal;
+    q.B = P.B;
+    q.sbl = P.sbl;
+    q.sbj = P.sbj;
+    gp.push_back(q);
+  }
+  OzakiGroup& G = p->grp;
+  G.rows_a = (int64_t)rows_a.size();
+  G.rows_b = (int64_t)rows_b.size();
+  G.k_pad = k_pad;
+  G.ntiles = (int64_t)tiles.size();
+  G.k_max = kmax;
+  G.digits = gemm_digits_setting(kRouteMaxK);
+  G.bits = gemm_bits_setting();
+  const size_t sb = ozaki_group_scratch_bytes(G.rows_a, G.rows_b, k_pad, G.ntiles, kmax, G.digits, G.bits);
+  if (sb == 0) return kErrInvalidValue;
+  auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  const size_t o_rows = 0, o_tiles = o_rows + al(sizeof(OzakiGroupRow) * (rows_a.size() + rows_b.size()));
+  const size_t o_probs = o_tiles + al(sizeof(OzakiGroupTile) * tiles.size());
+  const size_t o_a = o_probs + al(sizeof(OzakiGroupProb) * gp.size());
+  const size_t o_b = o_a + al((size_t)G.rows_a * k_pad * 16);
+  const size_t o_s = o_b + al((size_t)G.rows_b * k_pad * 16);
+  const size_t total = o_s + sb;
+  int rc = cuda_rc(dev_malloc(&p->d_grp, total));
+  if (rc) return rc;
+  char* b = static_cast<char*>(p->d_grp);
+  std::vector<OzakiGroupRow> all(rows_a);
+  all.insert(all.end(), rows_b.begin(), rows_b.end());
+  if ((rc = cuda_rc(cudaMemcpy(b + o_rows, all.data(), sizeof(OzakiGroupRow) * all.size(), cudaMemcpyHostToDevice))) ||
+      (rc = cuda_rc(cudaMemcpy(b + o_tiles, tiles.data(), sizeof(OzakiGroupTile) * tiles.size(),
+                               cudaMemcpyHostToDevice))) ||
+      (rc = cuda_rc(cudaMemcpy(b + o_probs, gp.data(), sizeof(OzakiGroupProb) * gp.size(), cudaMemcpyHostToDevice))) ||
+      (rc = cuda_rc(cudaMemset(b + o_a, 0, o_s - o_a))))
+    return rc;
+  G.rows = reinterpret_cast<const OzakiGroupRow*>(b + o_rows);
+  G.tiles = reinterpret_cast<const OzakiGroupTile*>(b + o_tiles);
+  G.probs = reinterpret_cast<const OzakiGroupProb*>(b + o_probs);
+  G.a_all = reinterpret_cast<q128*>(b + o_a);
+  G.b_all = reinterpret_cast<q128*>(b + o_b);
+  G.scratch = b + o_s;
+  p->n_ozaki = (int64_t)gp.size();
+  return kOk;
+}
+
 static const void* persistent_kernel(int tile) {
   return tile == 16 ? (const void*)batched_persistent_kernel<16> : (const void*)batched_persistent_kernel<32>;
 }
 
-static int plan_build(const qblas_problem* problems, int64_t count, int64_t grain, int tile, BatchPlan** out) {
+// route = false (the autotuner's calibration): every problem on the persistent kernel.
+static int plan_build(const qblas_problem* problems, int64_t count, int64_t grain, int tile, BatchPlan** out,
+                      bool route_ok = true) {
   *out = nullptr;
   if (count < 0 || (count > 0 && !problems) || (tile != 16 && tile != 32)) return kErrInvalidValue;
   std::vector<BProb> probs((size_t)count);
+  std::vector<char> route((size_t)count, 0);
   for (int64_t i = 0; i < count; ++i) {
     int rc = resolve(problems[i], probs[i]);
     if (rc) return rc;
+    route[i] = route_ok && routed(probs[i]) ? 1 : 0;
   }
+  // the persistent kernel's items leave out the routed problems (a problem
+  // with m = 0 has no items)
+  std::vector<BProb> kept(probs);
+  for (int64_t i = 0; i < count; ++i)
+    if (route[i]) kept[i].m = 0;
   std::vector<BItem> items;
   std::vector<int64_t> cost;
   int64_t ngroups = 0, nparts = 0;
-  build_items(probs, grain, tile, items, cost, ngroups, nparts);
+  build_items(kept, grain, tile, items, cost, ngroups, nparts);
   BatchPlan* p = new BatchPlan();
   cudaGetDevice(&p->device);
   p->nitems = (int64_t)items.size();
@@ -597,8 +720,12 @@ static int plan_build(const qblas_problem* problems, int64_t count, int64_t grai
     plan_free(p);
     return rc;
   }
+  if ((rc = build_group(probs, route, p))) {
+    plan_free(p);
+    return rc;
+  }
   if (count > 0 &&
-      (rc = cuda_rc(cudaMemcpy(p->d_probs, probs.data(), sizeof(BProb) * count, cudaMemcpyHostToDevice)))) {
+      (rc = cuda_rc(cudaMemcpy(p->d_probs, kept.data(), sizeof(BProb) * count, cudaMemcpyHostToDevice)))) {
     plan_free(p);
     return rc;
   }
@@ -619,6 +746,10 @@ static int plan_build(const qblas_problem* problems, int64_t count, int64_t grai
 
 static int plan_execute(BatchPlan* p, cudaStream_t s) {
   if (!p) return kErrInvalidValue;
+  if (p->n_ozaki > 0) {
+    const int rc = cuda_rc(launch_gemm_ozaki_grouped(p->grp, s));
+    if (rc) return rc;
+  }
   if (p->nitems == 0) return kOk;
   cudaError_t e = cudaMemsetAsync(p->d_counters, 0, sizeof(int) * (1 + p->ngroups), s);
   if (e != cudaSuccess) return cuda_rc(e);
@@ -788,7 +919,7 @@ static int run_autotune(int dev, TuneSetting* best_out) {
   for (int t : kTiles)
     for (int64_t g : kGrains) {
       BatchPlan* p = nullptr;
-      if (plan_build(probs.data(), (int64_t)probs.size(), g, t, &p) != kOk) continue;
+      if (plan_build(probs.data(), (int64_t)probs.size(), g, t, &p, false) != kOk) continue;
       plan_execute(p, s);  // warm-up
       cudaEventRecord(e0, s);
       for (int r = 0; r < 3; ++r) plan_execute(p, s);
@@ -822,6 +953,13 @@ static int run_autotune(int dev, TuneSetting* best_out) {
     }
   }
   return kOk;
+}
+
+bool batch_gemm_routed(int64_t m, int64_t n, int64_t k) {
+  if (gemm_method_setting() != 2 || ozaki_scheme_setting() == 1 || k > kRouteMaxK) return false;
+  if ((double)m * (double)n * (double)k < (double)route_min_products()) return false;
+  const int d = gemm_digits_setting(kRouteMaxK), b = gemm_bits_setting();
+  return gemm_digits_setting(k) == d && ozaki_uses_crt(kRouteMaxK, d, b, 2);
 }
 
 }  // namespace qb
@@ -863,8 +1001,8 @@ QBLAS_EXPORT int quadblas_batch_info(void* plan, int64_t* info4) {
 QBLAS_EXPORT int quadblas_batch_info_ex(void* plan, int64_t* info, int64_t n) {
   qb::BatchPlan* p = static_cast<qb::BatchPlan*>(plan);
   if (!p || (n > 0 && !info) || n < 0) return QBLAS_ERR_INVALID_VALUE;
-  const int64_t v[5] = {p->nitems, p->grain, p->blocks, p->ngroups, p->tile};
-  for (int64_t i = 0; i < n && i < 5; ++i) info[i] = v[i];
+  const int64_t v[7] = {p->nitems, p->grain, p->blocks, p->ngroups, p->tile, p->n_ozaki, p->grp.ntiles};
+  for (int64_t i = 0; i < n && i < 7; ++i) info[i] = v[i];
   return QBLAS_OK;
 }
 
@@ -908,3 +1046,11 @@ QBLAS_EXPORT int quadblas_batch_configure(int64_t grain, int tile) {
 }
 
 QBLAS_EXPORT int quadblas_batch_set_grain(int64_t grain) { return quadblas_batch_configure(grain, 0); }
+
+// Smallest m*n*k of a qgemm problem that plans built afterwards give to the
+// grouped tensor-core path under the Ozaki method (0: QBLAS_BATCH_OZAKI_MIN or 2^20).
+QBLAS_EXPORT int quadblas_batch_set_ozaki_min(int64_t products) {
+  if (products < 0) return QBLAS_ERR_INVALID_VALUE;
+  qb::g_route_min.store(products);
+  return QBLAS_OK;
+}

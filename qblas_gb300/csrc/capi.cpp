@@ -485,6 +485,16 @@ int host_gemv(char layout, char trans, int64_t m, int64_t n, const void* alpha, 
   return cuda_status(cudaStreamSynchronize(st.stream));
 }
 
+// True when p is in page-locked (pinned or registered) host memory.
+bool host_page_locked(const void* p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeHost;
+}
+
 // Copies rows [i0, i1) of the staged C back to the caller once the fold of
 // that band (enqueued on the main stream) is done, on side[1].
 struct BandCopy {
@@ -613,8 +623,11 @@ int host_gemm(char layout, char transa, char transb, int64_t m, int64_t n, int64
     // C comes back band by band on kSideC while later bands fold.
     if ((rc = ensure_side_streams(st))) return rc;
     BandCopy bc{&st, C, p, qb::kOk};
-    // C by row bands when its rows are contiguous and the fold goes by row bands
-    const bool c_banded = p.g.scj == 1 && p.g.sci >= p.g.n && p.g.m >= 64;
+    // C by row bands when its rows are contiguous, the fold goes by row bands
+    // and C is page-locked: a copy from or to pageable memory returns only
+    // when it is done, so a band copied back before later bands are enqueued
+    // would hold the host until that band's fold, and the GPU would wait for it
+    const bool c_banded = p.g.scj == 1 && p.g.sci >= p.g.n && p.g.m >= 64 && host_page_locked(C);
     ARowCopy ac{&st, A, C, p, c_banded};
     qb::OzakiOverlap ov{st.side[kSideB],      st.ev[kEvBDone], st.ev[kEvCReady], &BandCopy::done, &bc,
                         &ARowCopy::rows,      &ac,             st.side[kSideA],  st.ev[kEvADone],
@@ -656,6 +669,11 @@ int host_gemm(char layout, char transa, char transb, int64_t m, int64_t n, int64
 }  // namespace
 
 namespace qb {
+int gemm_method_setting() { return gemm_method(); }
+int gemm_digits_setting(int64_t k) { return gemm_digits(k); }
+int gemm_bits_setting() { return gemm_digit_bits(); }
+int ozaki_scheme_setting() { return g_ozaki_scheme.load(); }
+
 cudaError_t dev_malloc(void** p, size_t bytes) {
   if (take_injected_failure()) {
     *p = nullptr;
@@ -855,8 +873,10 @@ QBLAS_EXPORT int quadblas_batch_run_serial(const qblas_problem* problems, int64_
     if (q.op == QBLAS_OP_GEMM) {
       GemmPlan p;
       rc = plan_gemm(q.layout, q.transa, q.transb, q.m, q.n, q.k, q.lda, q.ldb, q.ldc, p);
+      // soft-float, as the batch, except the problems the batch gives to the
+      // grouped residue path
       if (!rc && q.m > 0 && q.n > 0 && q.k > 0)
-        rc = dev_gemm(p, 1, q.alpha, q.A, q.B, q.beta, q.C, s, nullptr);  // soft-float, as the batch
+        rc = dev_gemm(p, qb::batch_gemm_routed(q.m, q.n, q.k) ? 2 : 1, q.alpha, q.A, q.B, q.beta, q.C, s, nullptr);
     } else if (q.op == QBLAS_OP_GEMV) {
       GemvPlan p;
       rc = plan_gemv(q.layout, q.transa, q.m, q.n, q.lda, p);

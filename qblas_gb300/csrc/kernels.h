@@ -112,6 +112,59 @@ struct OzakiOverlap {
 cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scratch,
                               cudaStream_t s, const OzakiOverlap* overlap = nullptr, int scheme = 0,
                               int* report = nullptr);
+// Grouped residue (CRT) qgemm: many problems through one chain of launches
+// (gather, scales, residues, products, reconstruction), bit-identical to
+// launch_gemm_ozaki of each problem with the same digits, bits and scheme.
+// op(A) rows of every problem are stacked (each problem padded to 128 rows)
+// into a_all, op(B)'s columns into b_all (256-row padding) as rows of
+// k_pad elements; the products run over a list of (128-row A tile, 256-row
+// B tile) pairs whose reduced residues are stored tile-major, and the
+// reconstruction writes each tile's outputs through its problem's C.
+struct OzakiGroupRow {      // one stacked row: len elements from p, stride apart
+  const q128* p;
+  int64_t stride, len;
+};
+struct OzakiGroupTile {     // a_tile: 128-row tile of a_all; b_tile: 256-row tile of b_all
+  int32_t a_tile, b_tile, prob, row0, col0, pad[3];
+};
+struct OzakiGroupProb {
+  q128* C;
+  int64_t sci, scj, m, n, k;
+  q128 alpha, beta;
+  const q128* A;
+  int64_t sai, sal;
+  const q128* B;
+  int64_t sbl, sbj;
+};
+struct OzakiGroup {
+  int64_t rows_a, rows_b, k_pad, ntiles;  // rows_a % 128 == 0, rows_b % 256 == 0, k_pad % 64 == 0
+  int64_t k_max;                          // largest k (sets the moduli)
+  int digits, bits;
+  const OzakiGroupRow* rows;              // rows_a + rows_b (device)
+  const OzakiGroupTile* tiles;            // ntiles (device)
+  const OzakiGroupProb* probs;            // (device)
+  q128* a_all;                            // rows_a x k_pad, zero where no row element is gathered
+  q128* b_all;                            // rows_b x k_pad, likewise
+  void* scratch;                          // ozaki_group_scratch_bytes
+};
+// 0 when the residue scheme has no table for these digits, bits and k.
+size_t ozaki_group_scratch_bytes(int64_t rows_a, int64_t rows_b, int64_t k_pad, int64_t ntiles, int64_t k_max,
+                                 int digits, int bits);
+cudaError_t launch_gemm_ozaki_grouped(const OzakiGroup& G, cudaStream_t s);
+// The library's current qgemm settings (quadblas_set_method, _ozaki_slices,
+// _ozaki_digit_bits, _ozaki_scheme and their environment defaults): method
+// (1 soft-float, 2 Ozaki), digits for inner dimension k, bits, scheme.
+int gemm_method_setting();
+int gemm_digits_setting(int64_t k);
+int gemm_bits_setting();
+int ozaki_scheme_setting();
+// Whether a batched qgemm problem of this shape runs on the grouped residue
+// path under the current settings (and the one-by-one baseline then makes
+// the Ozaki call for it): method 2, residue scheme available for k <= 8192
+// with the same digits as at k = 8192, and m n k at least the threshold
+// (QBLAS_BATCH_OZAKI_MIN, default 2^20 products).
+bool batch_gemm_routed(int64_t m, int64_t n, int64_t k);
+
 // Test hooks: the next Ozaki qgemm product launch / Ozaki qgemv launch
 // withholds one accumulator-full commit with 1 ms pipeline waits.
 void ozaki_debug_stall_next();

@@ -408,7 +408,11 @@ struct OzakiMmaParams {
   int tile_begin, tile_end;  // tiles of this launch (tile = tm * tiles_n + tn)
   uint32_t idesc;            // instruction descriptor (bf16 or fp16 digits)
   int G;                     // highest diagonal (s - 1)
-  int m_pad, n_pad;
+  int m_pad, n_pad;          // shape of the output planes (C or Y)
+  int pa, pb;                // rows of one digit / residue plane of A and of B
+  // grouped problems: tile v of the launch multiplies A tile list[v].a_tile
+  // by B tile list[v].b_tile and stores output tile (v, 0); null otherwise
+  const OzakiGroupTile* list;
   int kb_begin, kb_end;  // k-blocks of this pass
   int chunk_kb;          // k-blocks summed exactly in fp32 before a readout
   int32_t* C;            // [G+1][m_pad][n_pad] (digit pairs)
@@ -485,11 +489,12 @@ __device__ __forceinline__ int cta_unit_count(const OzakiMmaParams& P, const Uni
   return waves * G1 + (tail > 0 ? (tail + d.G - 1) / d.G : 0);
 }
 
-// Unit j of this CTA: its tile (tm, tn), diagonal or modulus g, and whether
-// the tile exists (the second CTA of a pair past an odd last tile row
-// computes a tile of its own that is not stored).
+// Unit j of this CTA: its operand tiles (tm of A, tn of B), output tile
+// (ym, yn), diagonal or modulus g, and whether the tile exists (the second
+// CTA of a pair past an odd last tile row computes a tile of its own that is
+// not stored).
 __device__ __forceinline__ void cta_unit(const OzakiMmaParams& P, const UnitDeal& d, int j, int& tm, int& tn,
-                                         int& g, bool& real) {
+                                         int& ym, int& yn, int& g, bool& real) {
   const int tiles = d.tiles, G1 = P.G + 1;
   int vt;
   if (P.crt) {
@@ -509,15 +514,22 @@ __device__ __forceinline__ void cta_unit(const OzakiMmaParams& P, const UnitDeal
   }
   if (!P.pair) {
     const int tile = P.tile_begin + vt;
-    tm = tile / P.tiles_n;
-    tn = tile % P.tiles_n;
+    if (P.list) {
+      tm = P.list[tile].a_tile;
+      tn = P.list[tile].b_tile;
+      ym = tile;
+      yn = 0;
+    } else {
+      tm = ym = tile / P.tiles_n;
+      tn = yn = tile % P.tiles_n;
+    }
     real = true;
     return;
   }
   const int row0 = P.tile_begin / P.tiles_n, rows = (P.tile_end - P.tile_begin) / P.tiles_n;
   const int r = 2 * (vt / P.tiles_n) + d.rank;
-  tn = vt % P.tiles_n;
-  tm = row0 + r;
+  tn = yn = vt % P.tiles_n;
+  tm = ym = row0 + r;
   real = r < rows;
 }
 
@@ -575,9 +587,9 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
     if (lane == 0) {
       uint32_t it = 0;
       for (int j = 0; j < nun && ok; ++j) {
-        int tm, tn, g;
+        int tm, tn, ym, yn, g;
         bool real;
-        cta_unit(P, deal, j, tm, tn, g, real);
+        cta_unit(P, deal, j, tm, tn, ym, yn, g, real);
         for (int t = P.crt ? g : 0; t <= g && ok; ++t) {
           const int u = P.crt ? g : g - t;
           for (int kb = P.kb_begin; kb < P.kb_end && ok; ++kb, ++it) {
@@ -589,12 +601,12 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
             }
             mbar_expect_tx(full_bar(s), kStageBytes);
             const uint32_t sa = base + s * kStageBytes, sb = sa + kStageA;
-            tma_load_2d(sa, &tmA, full_bar(s), kb * kBK, t * P.m_pad + tm * kBM);
+            tma_load_2d(sa, &tmA, full_bar(s), kb * kBK, t * P.pa + tm * kBM);
             if (P.pair)  // this CTA's half of B, to both CTAs
               tma_load_2d_mc(sb + deal.rank * (kStageB / 2), &tmBh, full_bar(s), kb * kBK,
-                             u * P.n_pad + tn * kBN + deal.rank * (kBN / 2), (uint16_t)3);
+                             u * P.pb + tn * kBN + deal.rank * (kBN / 2), (uint16_t)3);
             else
-              tma_load_2d(sb, &tmB, full_bar(s), kb * kBK, u * P.n_pad + tn * kBN);
+              tma_load_2d(sb, &tmB, full_bar(s), kb * kBK, u * P.pb + tn * kBN);
           }
         }
       }
@@ -611,9 +623,9 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
       uint32_t it = 0, acc_it = 0;
       bool issued_any = false;
       for (int j = 0; j < nun && ok; ++j) {
-        int tm, tn, g;
+        int tm, tn, ym, yn, g;
         bool real;
-        cta_unit(P, deal, j, tm, tn, g, real);
+        cta_unit(P, deal, j, tm, tn, ym, yn, g, real);
         for (int t = P.crt ? g : 0; t <= g && ok; ++t) {
           for (int ch = 0; ch < nchunks && ok; ++ch) {
             const int kb0 = P.kb_begin + ch * P.chunk_kb;
@@ -673,9 +685,9 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
     for (int i = 0; i < kBN / 2; ++i) acc[i] = 0;
     uint32_t acc_it = 0;
     for (int j = 0; j < nun && ok; ++j) {
-      int tm, tn, g;
+      int tm, tn, ym, yn, g;
       bool real;
-      cta_unit(P, deal, j, tm, tn, g, real);
+      cta_unit(P, deal, j, tm, tn, ym, yn, g, real);
       for (int t = P.crt ? g : 0; t <= g && ok; ++t) {
         for (int ch = 0; ch < nchunks && ok; ++ch) {
           const int buf = acc_it & 1;
@@ -709,7 +721,7 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
       }
       if (!ok) break;
       // store diagonal g of this tile: row (tm*128 + row_in_tile), 128 columns
-      const size_t off = ((size_t)g * P.m_pad + (size_t)tm * kBM + row_in_tile) * P.n_pad + (size_t)tn * kBN +
+      const size_t off = ((size_t)g * P.m_pad + (size_t)ym * kBM + row_in_tile) * P.n_pad + (size_t)yn * kBN +
                          half * (kBN / 2);
       // (a pair's second CTA past an odd last tile row computed a tile that
       // does not exist: nothing is stored)
@@ -772,6 +784,11 @@ struct OzakiFoldParams {
   const int* err;
   int* report;  // set to 1 when err is (mapped host memory; may be null)
   int T;        // CRT: operand truncation (the rounding is at 2^(S_i + F_j - 2T))
+  // grouped problems: output row i is row i % 128 of list tile i / 128
+  // (its problem, first local row and column, A and B tiles); the fields
+  // A .. beta above are then unused
+  const OzakiGroupTile* gtiles;
+  const OzakiGroupProb* gprobs;
 };
 
 // Each thread folds four neighbouring columns j0..j0+3 of one row: one
@@ -867,7 +884,7 @@ constexpr int kFoldABytes = 128 * kCrtFoldK * 2;                   // 12 KiB: a 
 constexpr size_t kFoldSmem =
     128 + 2 * kFoldBufBytes + 2 * kFoldABytes + kCrtFoldK * kCrtFoldMaxN * 2 + 64;  // about 54 KiB
 
-template <int NW>
+template <int NW, bool kGrouped>
 __global__ void __launch_bounds__(kFoldThreads, kFoldCtasPerSm)
     ozaki_crt_fold_tc_kernel(const __grid_constant__ CUtensorMap tmY, const __grid_constant__ OzakiFoldParams P,
                              const __grid_constant__ CrtFoldTable tab) {
@@ -936,6 +953,7 @@ __global__ void __launch_bounds__(kFoldThreads, kFoldCtasPerSm)
   int pe = 0;
   q128* pcp = P.Cout;
   q128 pcold = q_zero(0);
+  q128 palpha = P.alpha, pbeta = P.beta;  // grouped: the pending output's problem's
   uint32_t mma_phase = 0;    // bit s: parity of stage s's next MMA completion
   uint32_t outstanding = 0;  // bit s: stage s's MMAs issued and not yet waited for
   int stage = 0;
@@ -958,7 +976,10 @@ __global__ void __launch_bounds__(kFoldThreads, kFoldCtasPerSm)
     }
     if (pmine && !pspecial) {
       const q128 sum = failed ? q_nan() : crt_fold_finish(acc, tab.negM, pe, true);
-      *pcp = q_epilogue(P.alpha, sum, P.beta, pcold);
+      if constexpr (kGrouped)
+        *pcp = q_epilogue(palpha, sum, pbeta, pcold);
+      else
+        *pcp = q_epilogue(P.alpha, sum, P.beta, pcold);
     }
   };
   auto wait_mma = [&](int st) -> bool {
@@ -1017,11 +1038,32 @@ __global__ void __launch_bounds__(kFoldThreads, kFoldCtasPerSm)
     }
     outstanding |= 1u << stage;
     // this tile's output: its loads are in flight while the tile before is finished
-    const bool mine = i < P.m && j < P.n;
-    const int64_t ii = mine ? i : 0, jj = mine ? j : 0;
-    q128* cp = P.Cout + ii * P.sci + jj * P.scj;
-    const uint32_t fl = P.fa[ii] | P.fb[jj];
-    const int e = P.S[ii] + P.F[jj] - 2 * P.T;
+    bool mine;
+    q128* cp;
+    uint32_t fl;
+    int e;
+    q128 oal, obe;
+    if constexpr (kGrouped) {
+      // m = 128 x tiles and n = 256: every (i, j) is inside the tile list
+      const OzakiGroupTile gt = P.gtiles[i >> 7];
+      const OzakiGroupProb& pr = P.gprobs[gt.prob];
+      const int64_t li = gt.row0 + (i & 127), lj = gt.col0 + j;
+      const int64_t ai = (int64_t)gt.a_tile * 128 + (i & 127), bj = (int64_t)gt.b_tile * 256 + j;
+      mine = li < pr.m && lj < pr.n;
+      cp = pr.C + (mine ? li * pr.sci + lj * pr.scj : 0);
+      fl = P.fa[ai] | P.fb[bj];
+      e = P.S[ai] + P.F[bj] - 2 * P.T;
+      oal = pr.alpha;
+      obe = pr.beta;
+    } else {
+      mine = i < P.m && j < P.n;
+      const int64_t ii = mine ? i : 0, jj = mine ? j : 0;
+      cp = P.Cout + ii * P.sci + jj * P.scj;
+      fl = P.fa[ii] | P.fb[jj];
+      e = P.S[ii] + P.F[jj] - 2 * P.T;
+      oal = P.alpha;
+      obe = P.beta;
+    }
     const q128 cold = ld_stream(cp);
     if (pend) {
       if (!wait_mma(stage ^ 1)) {
@@ -1038,6 +1080,8 @@ __global__ void __launch_bounds__(kFoldThreads, kFoldCtasPerSm)
     pe = e;
     pcp = cp;
     pcold = cold;
+    palpha = oal;
+    pbeta = obe;
     stage ^= 1;
   }
   // the last tile (its MMAs were issued by the last iteration)
@@ -1085,6 +1129,45 @@ __global__ void __launch_bounds__(256) ozaki_special_kernel(OzakiFoldParams P, c
       wacc_add_product(acc, qop_unpack(ld_cached(P.A + i * P.sai + l * P.sal)),
                        qop_unpack(ld_cached(P.B + l * P.sbl + j * P.sbj)));
     *cp = q_epilogue(P.alpha, wacc_round(acc), P.beta, *cp);
+  }
+}
+
+// The same for grouped problems: output (i, j) of the tile list's planes
+// (row i % 128 of tile i / 128, column j) belongs to the tile's problem.
+__global__ void __launch_bounds__(256)
+    ozaki_special_grouped_kernel(OzakiFoldParams P, const int* __restrict__ any) {
+  if ((any[0] | any[1]) == 0) return;
+  const int64_t total = P.m * P.n;
+  for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < total; x += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = x / P.n, j = x % P.n;
+    const OzakiGroupTile gt = P.gtiles[i >> 7];
+    const int64_t ai = (int64_t)gt.a_tile * 128 + (i & 127), bj = (int64_t)gt.b_tile * 256 + j;
+    if (!(P.fa[ai] | P.fb[bj])) continue;
+    const OzakiGroupProb& pr = P.gprobs[gt.prob];
+    const int64_t li = gt.row0 + (i & 127), lj = gt.col0 + j;
+    if (li >= pr.m || lj >= pr.n) continue;
+    q128* cp = pr.C + li * pr.sci + lj * pr.scj;
+    wacc acc;
+    wacc_init(acc);
+    for (int64_t l = 0; l < pr.k; ++l)
+      wacc_add_product(acc, qop_unpack(ld_cached(pr.A + li * pr.sai + l * pr.sal)),
+                       qop_unpack(ld_cached(pr.B + l * pr.sbl + lj * pr.sbj)));
+    *cp = q_epilogue(pr.alpha, wacc_round(acc), pr.beta, *cp);
+  }
+}
+
+// Grouped problems: stacked row r (of a_all for r < rows_a, else of b_all)
+// receives rows[r].len elements, rows[r].stride apart; one warp per row.
+// The rest of the row stays as it is (zero).
+__global__ void __launch_bounds__(256)
+    ozaki_gather_kernel(const OzakiGroupRow* __restrict__ rows, int64_t nrows, int64_t rows_a, int64_t k_pad,
+                        q128* __restrict__ a_all, q128* __restrict__ b_all) {
+  const int lane = threadIdx.x & 31;
+  const int64_t nw = (int64_t)gridDim.x * (blockDim.x / 32);
+  for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32; r < nrows; r += nw) {
+    const OzakiGroupRow d = rows[r];
+    q128* dst = r < rows_a ? a_all + r * k_pad : b_all + (r - rows_a) * k_pad;
+    for (int64_t l = lane; l < d.len; l += 32) dst[l] = ld_stream(d.p + l * d.stride);
   }
 }
 
@@ -1312,23 +1395,33 @@ static cudaError_t launch_crt_fold(const CrtFoldTable& ft, cudaStream_t st, cons
   int dev = 0;
   cudaGetDevice(&dev);
   if (dev >= 0 && dev < 64 && !attr_set[dev].load(std::memory_order_acquire)) {
-    cudaError_t e;
-    if ((e = cudaFuncSetAttribute(ozaki_crt_fold_tc_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)kFoldSmem)) != cudaSuccess ||
-        (e = cudaFuncSetAttribute(ozaki_crt_fold_tc_kernel<10>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)kFoldSmem)) != cudaSuccess ||
-        (e = cudaFuncSetAttribute(ozaki_crt_fold_tc_kernel<12>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)kFoldSmem)) != cudaSuccess)
-      return e;
+    const void* k[6] = {(const void*)ozaki_crt_fold_tc_kernel<8, false>, (const void*)ozaki_crt_fold_tc_kernel<10, false>,
+                        (const void*)ozaki_crt_fold_tc_kernel<12, false>, (const void*)ozaki_crt_fold_tc_kernel<8, true>,
+                        (const void*)ozaki_crt_fold_tc_kernel<10, true>, (const void*)ozaki_crt_fold_tc_kernel<12, true>};
+    for (int i = 0; i < 6; ++i) {
+      cudaError_t e = cudaFuncSetAttribute(k[i], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFoldSmem);
+      if (e != cudaSuccess) return e;
+    }
     attr_set[dev].store(true, std::memory_order_release);
   }
   const unsigned grid = (unsigned)std::min<int64_t>(tiles, kFoldCtasPerSm * (int64_t)device_sm_count());
-  if (ft.nw <= 8)
-    ozaki_crt_fold_tc_kernel<8><<<grid, kFoldThreads, kFoldSmem, st>>>(map, F, ft);
-  else if (ft.nw <= 10)
-    ozaki_crt_fold_tc_kernel<10><<<grid, kFoldThreads, kFoldSmem, st>>>(map, F, ft);
-  else
-    ozaki_crt_fold_tc_kernel<12><<<grid, kFoldThreads, kFoldSmem, st>>>(map, F, ft);
+  const bool grouped = F.gtiles != nullptr;
+  if (ft.nw <= 8) {
+    if (grouped)
+      ozaki_crt_fold_tc_kernel<8, true><<<grid, kFoldThreads, kFoldSmem, st>>>(map, F, ft);
+    else
+      ozaki_crt_fold_tc_kernel<8, false><<<grid, kFoldThreads, kFoldSmem, st>>>(map, F, ft);
+  } else if (ft.nw <= 10) {
+    if (grouped)
+      ozaki_crt_fold_tc_kernel<10, true><<<grid, kFoldThreads, kFoldSmem, st>>>(map, F, ft);
+    else
+      ozaki_crt_fold_tc_kernel<10, false><<<grid, kFoldThreads, kFoldSmem, st>>>(map, F, ft);
+  } else {
+    if (grouped)
+      ozaki_crt_fold_tc_kernel<12, true><<<grid, kFoldThreads, kFoldSmem, st>>>(map, F, ft);
+    else
+      ozaki_crt_fold_tc_kernel<12, false><<<grid, kFoldThreads, kFoldSmem, st>>>(map, F, ft);
+  }
   return cudaGetLastError();
 }
 
@@ -1518,6 +1611,8 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scr
   F2.err = err;
   F2.report = report;
   F2.T = crt ? tab.T : 0;
+  F2.gtiles = nullptr;
+  F2.gprobs = nullptr;
   if ((g.m + 7) / 8 > 65535) return cudaErrorInvalidConfiguration;
   const bool fold_banded = ov && ov->band_done && g.scj == 1 && g.sci >= g.n && g.m >= 64;
   bool c_waited = false;
@@ -1576,6 +1671,9 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scr
       P.G = L.G;
       P.m_pad = (int)L.m_pad;
       P.n_pad = (int)L.n_pad;
+      P.pa = (int)L.m_pad;
+      P.pb = (int)L.n_pad;
+      P.list = nullptr;
       P.kb_begin = p * kbp;
       P.kb_end = std::min(kb_total, (p + 1) * kbp);
       P.chunk_kb = crt ? chunk_kblocks(9) : chunk_kblocks(L.b);
@@ -1649,6 +1747,132 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scr
 
 size_t ozaki_error_flag_offset(int64_t m, int64_t n, int64_t k, int digits, int bits, int scheme) {
   return ozaki_layout(m, n, k, digits, bits, ozaki_nmod(scheme, digits, bits, k)).off_err;
+}
+
+// ---- grouped problems (residues) --------------------------------------------
+// The single-call layout for the stacked operands (rows_a x k_pad and
+// rows_b x k_pad), with the reduced products stored tile-major: nmod planes
+// of (128 ntiles) x 256.  One k pass (k_pad <= 8192).
+static bool ozaki_group_layout(int64_t rows_a, int64_t rows_b, int64_t k_pad, int64_t ntiles, int64_t k_max,
+                               int digits, int bits, CrtTable& tab, OzakiLayout& L) {
+  if (rows_a <= 0 || rows_b <= 0 || ntiles <= 0 || rows_a % kBM || rows_b % kBN || k_pad % kBK || k_pad <= 0 ||
+      k_pad > kCrtPassK || k_max > k_pad || ntiles * kBM > INT32_MAX)
+    return false;
+  if (bits < 7 || bits > 9 || digits < 2 || digits > ozaki_max_digits_for_k(bits, k_max)) return false;
+  if (!ozaki_crt_table(2, digits, bits, k_max, tab)) return false;
+  L = ozaki_layout(rows_a, rows_b, k_pad, digits, bits, tab.n);
+  L.total = L.off_C + align256((size_t)tab.n * (size_t)ntiles * kBM * kBN * 2);
+  return true;
+}
+
+size_t ozaki_group_scratch_bytes(int64_t rows_a, int64_t rows_b, int64_t k_pad, int64_t ntiles, int64_t k_max,
+                                 int digits, int bits) {
+  CrtTable tab;
+  OzakiLayout L;
+  return ozaki_group_layout(rows_a, rows_b, k_pad, ntiles, k_max, digits, bits, tab, L) ? L.total : 0;
+}
+
+cudaError_t launch_gemm_ozaki_grouped(const OzakiGroup& Gp, cudaStream_t st) {
+  CrtTable tab;
+  OzakiLayout L;
+  if (!ozaki_group_layout(Gp.rows_a, Gp.rows_b, Gp.k_pad, Gp.ntiles, Gp.k_max, Gp.digits, Gp.bits, tab, L))
+    return cudaErrorInvalidValue;
+  CrtSplitTable stab;
+  CrtFoldTable ftab;
+  crt_split_table(tab, stab);
+  crt_fold_table(tab, ftab);
+  char* base = static_cast<char*>(Gp.scratch);
+  int* S = reinterpret_cast<int*>(base + L.off_S);
+  int* F = reinterpret_cast<int*>(base + L.off_F);
+  uint32_t* fa = reinterpret_cast<uint32_t*>(base + L.off_fa);
+  uint32_t* fb = reinterpret_cast<uint32_t*>(base + L.off_fb);
+  int* err = reinterpret_cast<int*>(base + L.off_err);
+  uint16_t* DA = reinterpret_cast<uint16_t*>(base + L.off_DA);
+  uint16_t* DB = reinterpret_cast<uint16_t*>(base + L.off_DB);
+  uint16_t* Yq = reinterpret_cast<uint16_t*>(base + L.off_C);
+  const int sms = device_sm_count();
+  const int64_t ra = Gp.rows_a, rb = Gp.rows_b, kp = Gp.k_pad, nrows = ra + rb;
+  cudaError_t e;
+  // 1. the problems' rows into the stacked operands
+  ozaki_gather_kernel<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>((nrows + 7) / 8, (int64_t)sms * 8)), 256, 0,
+                        st>>>(Gp.rows, nrows, ra, kp, Gp.a_all, Gp.b_all);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  // 2. scales, flags and residues of both (error words as in the single call)
+  ozaki_fill_kernel<<<(unsigned)((ra + 255) / 256), 256, 0, st>>>(ra, S, fa);
+  ozaki_fill_kernel<<<(unsigned)((rb + 255) / 256), 256, 0, st>>>(rb, F, fb);
+  if ((e = cudaMemsetAsync(err, 0, 6 * sizeof(int), st)) != cudaSuccess) return e;
+  launch_scale(rb, kp, Gp.b_all, kp, 1, F, fb, err + 4, sms, st);
+  if ((e = launch_crt_split(stab, st, rb, kp, rb, kp, rb * kp, Gp.b_all, kp, 1, F, DB, err + 1)) != cudaSuccess)
+    return e;
+  launch_scale(ra, kp, Gp.a_all, kp, 1, S, fa, err + 5, sms, st);
+  if ((e = launch_crt_split(stab, st, ra, kp, ra, kp, ra * kp, Gp.a_all, kp, 1, S, DA, err + 2)) != cudaSuccess)
+    return e;
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  // 3. residue products over the tile list
+  CUtensorMap tmA, tmB, tmBh;
+  if (!make_map(&tmA, DA, (int64_t)tab.n * ra, kp, kBM, true) || !make_map(&tmB, DB, (int64_t)tab.n * rb, kp, kBN, true) ||
+      !make_map(&tmBh, DB, (int64_t)tab.n * rb, kp, kBN / 2, true))
+    return cudaErrorInvalidValue;
+  if ((e = cudaFuncSetAttribute(ozaki_mma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMmaSmem)) !=
+      cudaSuccess)
+    return e;
+  OzakiMmaParams P;
+  P.tiles_m = (int)Gp.ntiles;
+  P.tiles_n = 1;
+  P.tile_begin = 0;
+  P.tile_end = (int)Gp.ntiles;
+  P.idesc = kIdescF16;
+  P.G = tab.n - 1;
+  P.m_pad = (int)(Gp.ntiles * kBM);
+  P.n_pad = kBN;
+  P.pa = (int)ra;
+  P.pb = (int)rb;
+  P.list = Gp.tiles;
+  P.kb_begin = 0;
+  P.kb_end = (int)(kp / kBK);
+  P.chunk_kb = chunk_kblocks(9);
+  P.crt = 1;
+  for (int q = 0; q < kCrtMaxMods; ++q) {
+    const bool on = q < tab.n;
+    P.crt_p[q] = on ? tab.mod[q].p : 1u;
+    P.crt_magic[q] = on ? tab.mod[q].magic : 0u;
+    P.crt_K[q] = on ? tab.mod[q].K : 0u;
+    P.crt_u[q] = on ? tab.mod[q].u : 0u;
+  }
+  P.C = nullptr;
+  P.Y = Yq;
+  P.err = err;
+  P.pair = 0;
+  P.withhold = 0;
+  P.wait_ns = kWaitLimitNs;
+  const int64_t units = (int64_t)tab.n * Gp.ntiles;
+  ozaki_mma_kernel<<<(unsigned)std::min<int64_t>(units, sms), kMmaThreads, kMmaSmem, st>>>(tmA, tmB, tmBh, P);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  // 4. reconstruction and special values through the problems' C
+  OzakiFoldParams F2 = {};
+  F2.m = Gp.ntiles * kBM;
+  F2.n = kBN;
+  F2.k = Gp.k_max;
+  F2.G = tab.n - 1;
+  F2.npass = 1;
+  F2.b = 9;
+  F2.m_pad = Gp.ntiles * kBM;
+  F2.n_pad = kBN;
+  F2.Y = Yq;
+  F2.S = S;
+  F2.F = F;
+  F2.fa = fa;
+  F2.fb = fb;
+  F2.Cout = nullptr;
+  F2.err = err;
+  F2.report = nullptr;
+  F2.T = tab.T;
+  F2.gtiles = Gp.tiles;
+  F2.gprobs = Gp.probs;
+  if ((e = launch_crt_fold(ftab, st, F2, F2.m_pad)) != cudaSuccess) return e;
+  const unsigned sgrid = (unsigned)std::max<int64_t>(1, std::min<int64_t>((F2.m * F2.n + 255) / 256, (int64_t)sms * 2));
+  ozaki_special_grouped_kernel<<<sgrid, 256, 0, st>>>(F2, err + 4);
+  return cudaGetLastError();
 }
 
 }  // namespace qb

@@ -198,3 +198,51 @@ def test_batch_autotune(qlib, torch_cuda, tmp_path, monkeypatch):
     text = (tmp_path / "tune.txt").read_text().split()
     assert int(text[-2]) == g and int(text[-1]) == tile
     print({"grain": grain, "tile": tile})
+
+
+def test_batch_ozaki_grouped_equals_single_calls(qlib, torch_cuda):
+    """Under the Ozaki method, qgemm problems at or above the routing
+    threshold run on the grouped residue path (stacked operands, one chain of
+    launches over a tile list).  With the threshold at one product every
+    qgemm problem of a mixed batch is routed (both layouts, all transposes,
+    padded leading dimensions, beta != 0, a NaN and an infinity in two
+    problems' operands); every output must equal, bit for bit, the same
+    problems made one by one by quadblas_batch_run_serial, which gives the
+    routed problems to the Ozaki single call (include/quadblas/algorithms/
+    level3.hpp:215 semantics), also after a CUDA-graph replay."""
+    torch = torch_cuda
+    rng = G.rng_for(779)
+    ar, specs, probs = make_batch(torch, rng, 40, 12, 12)
+    gemms = [s for s in specs if s["op"] == 0]
+    ar.dev[gemms[3]["oA"] + 2] = torch.tensor([0, 0x7FFF800000000000], dtype=torch.int64)   # NaN
+    ar.dev[gemms[7]["oB"] + 1] = torch.tensor([0, -0x1000000000000], dtype=torch.int64)     # -inf (0xFFFF0000...)
+    c0 = ar.dev.clone()
+    api.set_method(2)
+    api.batch_set_ozaki_min(1)
+    try:
+        plan = api.BatchPlan(probs)
+        info = plan.info()
+        assert info["ozaki_problems"] == len(gemms) and info["ozaki_tiles"] >= len(gemms)
+        plan.execute()
+        torch.cuda.synchronize()
+        batched = ar.dev.clone()
+        ar.dev.copy_(c0)
+        torch.cuda.synchronize()
+        api.batch_run_serial(probs)
+        torch.cuda.synchronize()
+        same = (batched == ar.dev).all(dim=1)
+        assert bool(same.all()), int((~same).sum())
+        # recorded in a CUDA graph and replayed
+        ar.dev.copy_(c0)
+        st = torch.cuda.Stream()
+        st.wait_stream(torch.cuda.current_stream())
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=st):
+            plan.execute(stream=st)
+        g.replay()
+        torch.cuda.synchronize()
+        assert torch.equal(batched, ar.dev)
+        plan.close()
+    finally:
+        api.set_method(0)
+        api.batch_set_ozaki_min(0)

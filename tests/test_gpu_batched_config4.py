@@ -116,3 +116,37 @@ def test_config4_batched_equals_one_by_one_and_oracle(qlib, O, torch_cuda, tmp_p
                 assert Q.same_bits(got, R).all(), (op, n)
                 continue
             assert Q.same_bits(got, epilogue(O, one, R, zero, cold)).all(), (op, m, n, k)
+
+
+def test_config4_ozaki_routing_equals_one_by_one(qlib, torch_cuda, tmp_path, monkeypatch):
+    """The same workload under the Ozaki method: the qgemm problems with
+    m n k >= 2^20 (the default threshold) run on the grouped residue path,
+    the rest of the batch on the persistent kernel.  Every output must be
+    bit-identical to quadblas_batch_run_serial, which makes the Ozaki single
+    call for the routed problems and the soft-float call for the others."""
+    torch = torch_cuda
+    monkeypatch.setenv("QBLAS_AUTOTUNE_CACHE", str(tmp_path / "tune.txt"))
+    probs, inp, out, lay = G.config4_batch(torch, 4001)
+    c0 = out.clone()
+    api.set_method(2)
+    api.batch_set_ozaki_min(0)
+    try:
+        plan = api.BatchPlan(probs)
+        info = plan.info()
+        routed = sum(1 for L in lay if L[0] == 0 and L[1] * L[2] * L[3] >= 1 << 20)
+        assert info["ozaki_problems"] == routed > 0
+        plan.execute()
+        torch.cuda.synchronize()
+        batched = out.clone()
+        out.copy_(c0)
+        torch.cuda.synchronize()
+        api.batch_run_serial(probs)
+        torch.cuda.synchronize()
+        same = (batched == out).all(dim=1)
+        if not bool(same.all()):
+            diff = (~same).nonzero().flatten().cpu().numpy()
+            bad = sorted({i for i, L in enumerate(lay) if np.any((diff >= L[6]) & (diff < L[6] + L[7]))})
+            pytest.fail(f"{diff.size} outputs differ, in {len(bad)} problems, first {[lay[i][:4] for i in bad[:5]]}")
+        plan.close()
+    finally:
+        api.set_method(0)

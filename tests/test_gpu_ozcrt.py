@@ -127,19 +127,25 @@ def test_crt_accuracy_spread(crt, O, torch_cuda, size):
 
 
 @pytest.mark.parametrize("scheme", [2, 1])
-@pytest.mark.parametrize("shape", [(1664, 3072, 96), (4000, 2100, 70)])
-def test_host_pointer_row_bands_match_device(crt, torch_cuda, scheme, shape):
+@pytest.mark.parametrize("shape,pinned", [((1664, 3072, 96), False), ((4000, 2100, 70), True),
+                                          ((4000, 2100, 70), False)])
+def test_host_pointer_row_bands_match_device(crt, torch_cuda, scheme, shape, pinned):
     """A host-pointer qgemm with more 128 x 256 tiles than the GPU has SMs
-    runs in row bands: A is copied band by band with the same rows of C
-    behind each band, and C is folded and copied back in row bands.  At
-    13 x 12 = 156 tiles the products are one band and the fold four; at
-    32 x 9 = 288 tiles (m and n off the tile grid) the products are two
-    bands, the rows of the first are folded before the second multiplies,
-    and the rest in one band.  With beta != 0 and a random C the result must
+    runs in row bands: A is copied band by band, and C is folded and copied
+    back in row bands.  At 13 x 12 = 156 tiles the products are one band and
+    the fold four.  At 32 x 9 = 288 tiles (m and n off the tile grid) the
+    products are two bands; from page-locked buffers the same rows of C
+    follow each band of A and the rows of the first band are folded before
+    the second multiplies (the rest in one band), from pageable buffers C
+    comes whole after A.  With beta != 0 and a random C the result must
     equal the device-pointer call's bit for bit; a fold that ran before its
     rows of C arrived would read the staging buffer's previous contents
     (another call's result, left there on purpose)."""
     torch = torch_cuda
+    if pinned:
+        keep = lambda a: torch.from_numpy(a.view(np.int64)).pin_memory().numpy().view(np.uint64)  # noqa: E731
+    else:
+        keep = lambda a: a  # noqa: E731
     api.set_ozaki_scheme(scheme)
     api.set_ozaki_slices(15)
     api.set_ozaki_digit_bits(9)
@@ -151,9 +157,10 @@ def test_host_pointer_row_bands_match_device(crt, torch_cuda, scheme, shape):
     api.gemm_dev("R", "N", "N", m, n, k, alpha, dA, k, dB, n, beta, dC, n)
     torch.cuda.synchronize()
     ref = to_host(dC)
-    other = G.uniform_full(rng, m * n)
+    A, B = keep(A), keep(B)
+    other = keep(G.uniform_full(rng, m * n))
     api.gemm("R", "N", "N", m, n, k, alpha, A, k, B, n, Q.scalar(0.0), other, n)
-    got = C.copy()
+    got = keep(C.copy())
     api.gemm("R", "N", "N", m, n, k, alpha, A, k, B, n, beta, got, n)
     assert Q.same_bits(got, ref).all(), int((~Q.same_bits(got, ref)).sum())
 
