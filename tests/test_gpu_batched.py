@@ -246,3 +246,59 @@ def test_batch_ozaki_grouped_equals_single_calls(qlib, torch_cuda):
     finally:
         api.set_method(0)
         api.batch_set_ozaki_min(0)
+
+
+def test_batch_ozaki_grouped_multi_tile_problems(qlib, torch_cuda):
+    """Routed qgemm problems that span several 128 x 256 tiles in both
+    directions (so tiles start at local rows and columns other than 0),
+    longer k (several exact 256-chunks, k_pad set by the largest k), a
+    column-major C with a padded leading dimension, and a problem below the
+    threshold that stays on the persistent kernel: bit-identical to the
+    single calls made by quadblas_batch_run_serial."""
+    torch = torch_cuda
+    rng = G.rng_for(780)
+    shapes = [(300, 600, 700, "R", "N", "N"), (130, 257, 1000, "C", "T", "N"), (1, 1000, 9, "R", "N", "T"),
+              (257, 3, 2049, "C", "N", "T"), (20, 20, 20, "R", "N", "N")]
+    ar = Arena(torch)
+    specs = []
+    for m, n, k, layout, ta, tb in shapes:
+        col = layout == "C"
+        a_r, a_c = (k, m) if ta == "T" else (m, k)
+        b_r, b_c = (n, k) if tb == "T" else (k, n)
+        lda, ldb = (a_r if col else a_c) + 1, (b_r if col else b_c) + 2
+        ldc = (m if col else n) + 3
+        A = G.spread_uniform(rng, (a_c if col else a_r) * lda)
+        B = G.spread_uniform(rng, (b_c if col else b_r) * ldb)
+        C = G.uniform_full(rng, (n if col else m) * ldc)
+        specs.append(dict(m=m, n=n, k=k, layout=layout, ta=ta, tb=tb, lda=lda, ldb=ldb, ldc=ldc,
+                          oA=ar.add(A), oB=ar.add(B), oC=ar.add(C)))
+    ar.upload()
+    probs = np.zeros(len(specs), dtype=api.PROBLEM_DTYPE)
+    for p, s in zip(probs, specs):
+        p["op"] = api.OP_GEMM
+        p["layout"], p["transa"], p["transb"] = s["layout"].encode(), s["ta"].encode(), s["tb"].encode()
+        p["m"], p["n"], p["k"] = s["m"], s["n"], s["k"]
+        p["alpha"], p["beta"] = Q.scalar(1.5)[0], Q.scalar(-0.25)[0]
+        p["A"], p["B"], p["C"] = ar.ptr(s["oA"]), ar.ptr(s["oB"]), ar.ptr(s["oC"])
+        p["lda"], p["ldb"], p["ldc"] = s["lda"], s["ldb"], s["ldc"]
+    c0 = ar.dev.clone()
+    api.set_method(2)
+    api.batch_set_ozaki_min(20 * 20 * 20 + 1)
+    try:
+        plan = api.BatchPlan(probs)
+        info = plan.info()
+        assert info["ozaki_problems"] == len(shapes) - 1
+        assert info["ozaki_tiles"] == 3 * 3 + 2 * 2 + 1 * 4 + 3 * 1
+        plan.execute()
+        torch.cuda.synchronize()
+        batched = ar.dev.clone()
+        ar.dev.copy_(c0)
+        torch.cuda.synchronize()
+        api.batch_run_serial(probs)
+        torch.cuda.synchronize()
+        same = (batched == ar.dev).all(dim=1)
+        assert bool(same.all()), int((~same).sum())
+        plan.close()
+    finally:
+        api.set_method(0)
+        api.batch_set_ozaki_min(0)
