@@ -332,8 +332,11 @@ __device__ void run_dot_item(SH& sh, const BProb& P, const BItem& it, wacc* part
   }
 }
 
+// Resident blocks per SM: four for the 16-wide tile (at most 64 registers; the
+// streaming qgemv and qdot items gain most from the extra loads in flight),
+// two for the 32-wide tile, whose four wide accumulators per thread need more.
 template <int T>
-__global__ void __launch_bounds__(kBThreads, 2)
+__global__ void __launch_bounds__(kBThreads, T == 16 ? 4 : 2)
     batched_persistent_kernel(const BProb* __restrict__ probs, const BItem* __restrict__ items,
                               int64_t nitems, int* queue, int* counters, wacc* partials) {
   __shared__ BShared<T> sh;
