@@ -184,6 +184,9 @@ typedef struct {
 } qblas_problem;
 
 int quadblas_batch_plan(const qblas_problem *problems, int64_t count, void **plan);
+/* One batch, once (no plan kept): plan, execute on `stream`, wait for the
+ * stream, free the plan.  For batches run more than once, keep a plan. */
+int quadblas_qgemm_batched_dev(const qblas_problem *problems, int64_t count, void *stream);
 int quadblas_batch_execute(void *plan, void *stream);
 int quadblas_batch_destroy(void *plan);
 /* info4: work items, granularity (products per item), blocks, split groups */

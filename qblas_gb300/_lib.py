@@ -53,6 +53,7 @@ _SIGS = {
     "quadblas_batch_configure": (ci, [i64, ci]),
     "quadblas_batch_set_ozaki_min": (ci, [i64]),
     "quadblas_batch_run_serial": (ci, [vp, i64, vp]),
+    "quadblas_qgemm_batched_dev": (ci, [vp, i64, vp]),
     # configuration
     "quadblas_set_method": (ci, [ci]),
     "quadblas_get_method": (ci, []),

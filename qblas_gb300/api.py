@@ -183,6 +183,13 @@ PROBLEM_DTYPE = np.dtype([("op", "<i4"), ("layout", "S1"), ("transa", "S1"), ("t
 assert PROBLEM_DTYPE.itemsize == 112
 
 
+def batched_dev(problems: np.ndarray, stream=None) -> None:
+    """One batch, once (quadblas_qgemm_batched_dev): plan, execute, wait, free."""
+    problems = np.ascontiguousarray(problems, dtype=PROBLEM_DTYPE)
+    check(load().quadblas_qgemm_batched_dev(problems.ctypes.data_as(ctypes.c_void_p), len(problems),
+                                            _stream(stream)))
+
+
 def batch_run_serial(problems: np.ndarray, stream=None) -> None:
     """Each problem by its own device-pointer call, in order (C loop)."""
     problems = np.ascontiguousarray(problems, dtype=PROBLEM_DTYPE)

@@ -47,7 +47,8 @@ namespace qb {
 constexpr int kBThreads = 256;
 constexpr int kBTileMax = 32; // gemm tile edges: 16 (one output per thread) or 32 (2 x 2)
 constexpr int kBTK = 16;      // gemm k slice staged in shared memory
-constexpr int kBRows = 8;     // gemv rows per item (one warp each)
+constexpr int kBRows = 32;    // gemv rows per item (8 lanes each, 4 per warp)
+constexpr int kBRowLanes = 8;
 
 enum : int32_t { kOpGemm = 0, kOpGemv = 1, kOpDot = 2 };
 
@@ -237,48 +238,63 @@ __device__ void run_gemm_item(BShared<T>& sh, const BProb& P, const BItem& it, w
   }
 }
 
+// Rows of a qgemv item: 8 lanes per row (4 rows per warp), each lane taking
+// every 8th column with four loads in flight; the 8 lanes' accumulators
+// merge in three shuffles and the row's first lane finishes it.  (Short rows
+// keep most lanes busy: one warp per row spent about as long in its
+// 32-lane reduction and one-lane finish as in the products of a row of a
+// few hundred columns.)
 template <class SH>
 __device__ void run_gemv_item(SH& sh, const BProb& P, const BItem& it, wacc* partials,
                               int* counters) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int64_t row = it.i0 + warp;
+  const int sl = lane & (kBRowLanes - 1);
+  const int r_in = warp * (32 / kBRowLanes) + lane / kBRowLanes;  // row within the item
+  const int64_t row = it.i0 + r_in;
   wacc acc;
   wacc_init(acc);
   if (row < P.m) {
     // four loads in flight per lane (A read once, x shared by the rows)
     const q128* Ar = P.A + row * P.sai;
-    int64_t j = it.l0 + lane;
-    for (; j + 96 < it.l1; j += 128) {
-      q128 a0 = ld_stream(Ar + j * P.sal), a1 = ld_stream(Ar + (j + 32) * P.sal);
-      q128 a2 = ld_stream(Ar + (j + 64) * P.sal), a3 = ld_stream(Ar + (j + 96) * P.sal);
-      q128 x0 = ld_cached(P.B + j * P.sbl), x1 = ld_cached(P.B + (j + 32) * P.sbl);
-      q128 x2 = ld_cached(P.B + (j + 64) * P.sbl), x3 = ld_cached(P.B + (j + 96) * P.sbl);
+    int64_t j = it.l0 + sl;
+    for (; j + 3 * kBRowLanes < it.l1; j += 4 * kBRowLanes) {
+      q128 a0 = ld_stream(Ar + j * P.sal), a1 = ld_stream(Ar + (j + kBRowLanes) * P.sal);
+      q128 a2 = ld_stream(Ar + (j + 2 * kBRowLanes) * P.sal), a3 = ld_stream(Ar + (j + 3 * kBRowLanes) * P.sal);
+      q128 x0 = ld_cached(P.B + j * P.sbl), x1 = ld_cached(P.B + (j + kBRowLanes) * P.sbl);
+      q128 x2 = ld_cached(P.B + (j + 2 * kBRowLanes) * P.sbl), x3 = ld_cached(P.B + (j + 3 * kBRowLanes) * P.sbl);
       wacc_add_product(acc, qop_unpack(a0), qop_unpack(x0));
       wacc_add_product(acc, qop_unpack(a1), qop_unpack(x1));
       wacc_add_product(acc, qop_unpack(a2), qop_unpack(x2));
       wacc_add_product(acc, qop_unpack(a3), qop_unpack(x3));
     }
-    for (; j < it.l1; j += 32)
+    for (; j < it.l1; j += kBRowLanes)
       wacc_add_product(acc, qop_unpack(ld_stream(Ar + j * P.sal)), qop_unpack(ld_cached(P.B + j * P.sbl)));
   }
-  wacc_warp_reduce(acc);
+  // the 8 lanes of a row into its first lane (lanes of other rows read by a
+  // shuffle are not used)
+#pragma unroll
+  for (int d = kBRowLanes / 2; d >= 1; d >>= 1) {
+    wacc b = wacc_shfl_down(acc, d);
+    wacc_merge(acc, b);
+  }
+  const bool lead = sl == 0;
   if (P.nparts > 1) {
-    wacc* slot = partials + P.part_base + (it.group * P.nparts + it.part) * kBRows + warp;
-    if (lane == 0) *slot = acc;
+    wacc* slot = partials + P.part_base + (it.group * P.nparts + it.part) * kBRows + r_in;
+    if (lead) *slot = acc;
     if (!group_arrive(sh, counters + P.group_base + it.group, P.nparts)) return;
-    if (lane == 0) {
+    if (lead) {
       wacc_init(acc);
       for (int p = 0; p < P.nparts; ++p)
-        wacc_merge(acc, wacc_ldcg(partials + P.part_base + (it.group * P.nparts + p) * kBRows + warp));
+        wacc_merge(acc, wacc_ldcg(partials + P.part_base + (it.group * P.nparts + p) * kBRows + r_in));
     }
   }
-  if (lane == 0 && row < P.m) {
+  if (lead && row < P.m) {
     q128* yp = P.C + row * P.sci;
     q128 r;
     if (wacc_round_certified(acc, 2 * (uint64_t)P.n + 3 * (33 * (uint64_t)P.nparts + 2), r))
       *yp = q_epilogue(P.alpha, r, P.beta, *yp);
     else
-      sh.list[atomicAdd(&sh.nlist, 1)] = (short)warp;
+      sh.list[atomicAdd(&sh.nlist, 1)] = (short)r_in;
   }
   __syncthreads();
   const int cnt = sh.nlist;
@@ -985,6 +1001,24 @@ QBLAS_EXPORT int quadblas_batch_plan(const qblas_problem* problems, int64_t coun
 
 QBLAS_EXPORT int quadblas_batch_execute(void* plan, void* stream) {
   return qb::plan_execute(static_cast<qb::BatchPlan*>(plan), static_cast<cudaStream_t>(stream));
+}
+
+// One batch, once: plan, execute on `stream`, wait for the stream, free the plan.
+QBLAS_EXPORT int quadblas_qgemm_batched_dev(const qblas_problem* problems, int64_t count, void* stream) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    return QBLAS_ERR_NO_DEVICE;
+  }
+  qb::BatchPlan* p = nullptr;
+  const qb::TuneSetting t = qb::cached_setting(dev);
+  int rc = qb::plan_build(problems, count, t.grain, t.tile, &p);
+  if (rc) return rc;
+  rc = qb::plan_execute(p, static_cast<cudaStream_t>(stream));
+  const cudaError_t e = cudaStreamSynchronize(static_cast<cudaStream_t>(stream));
+  qb::plan_free(p);
+  if (rc) return rc;
+  return qb::cuda_rc(e);
 }
 
 QBLAS_EXPORT int quadblas_batch_destroy(void* plan) {

@@ -302,3 +302,14 @@ def test_batch_ozaki_grouped_multi_tile_problems(qlib, torch_cuda):
     finally:
         api.set_method(0)
         api.batch_set_ozaki_min(0)
+
+
+def test_batched_dev_one_shot(qlib, O, torch_cuda):
+    """quadblas_qgemm_batched_dev (plan, execute, wait, free in one call) on a
+    mixed batch: every output equal to the exact oracle's single-call result."""
+    torch = torch_cuda
+    rng = G.rng_for(781)
+    ar, specs, probs = make_batch(torch, rng, 10, 10, 10)
+    api.batched_dev(probs)
+    torch.cuda.synchronize()
+    check_all(O, ar, specs)
