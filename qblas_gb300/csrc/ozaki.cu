@@ -420,7 +420,7 @@ struct OzakiMmaParams {
   // CRT scheme: unit g is the single pair (g, g), the residue product of
   // modulus g, and the epilogue stores y = (C mod p) u mod p (16 bits) in Y
   int crt;
-  uint16_t* Y;                  // [G+1][m_pad][n_pad]
+  uint16_t* Y;                  // [G+1][m_pad][n_pad], fp16 values
   uint32_t crt_p[kCrtMaxMods], crt_magic[kCrtMaxMods], crt_K[kCrtMaxMods], crt_u[kCrtMaxMods];
   // Paired CTAs (launched as clusters of two): the two CTAs of a cluster
   // take tile rows 2r and 2r + 1 of the same tile column in lockstep, each
@@ -732,11 +732,19 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
 #pragma unroll
         for (int i = 0; i < kBN / 2; ++i)
           acc[i] = (int32_t)crt_mod(crt_mod((uint32_t)(acc[i] + (int32_t)K), p, mg) * u, p, mg);
+        // stored as fp16 values (y <= 512 is exact): the bits 0x6400 + y are
+        // 1024 + y, minus 1024 in pairs; the reconstruction multiplies them
+        // on the tensor cores as they are
+        auto h2 = [](int32_t y0, int32_t y1) {
+          const uint32_t w = ((uint32_t)y0 | ((uint32_t)y1 << 16)) + 0x64006400u, k1024 = 0x64006400u;
+          const __half2 v = __hsub2(*reinterpret_cast<const __half2*>(&w), *reinterpret_cast<const __half2*>(&k1024));
+          return *reinterpret_cast<const uint32_t*>(&v);
+        };
 #pragma unroll
         for (int i = 0; i < kBN / 2; i += 8)
           *reinterpret_cast<uint4*>(dst + i) =
-              make_uint4((uint32_t)acc[i] | ((uint32_t)acc[i + 1] << 16), (uint32_t)acc[i + 2] | ((uint32_t)acc[i + 3] << 16),
-                         (uint32_t)acc[i + 4] | ((uint32_t)acc[i + 5] << 16), (uint32_t)acc[i + 6] | ((uint32_t)acc[i + 7] << 16));
+              make_uint4(h2(acc[i], acc[i + 1]), h2(acc[i + 2], acc[i + 3]), h2(acc[i + 4], acc[i + 5]),
+                         h2(acc[i + 6], acc[i + 7]));
       } else if (real) {
         int32_t* dst = P.C + off;
 #pragma unroll
@@ -769,7 +777,7 @@ struct OzakiFoldParams {
   int G, npass, b;
   int64_t m_pad, n_pad;
   const int32_t* C;      // [npass][G+1][m_pad][n_pad]
-  const uint16_t* Y;     // CRT: [npass][nmod][m_pad][n_pad] reduced residue products
+  const uint16_t* Y;     // CRT: [npass][nmod][m_pad][n_pad] reduced residue products (fp16 values)
   const int* S;          // row scales of op(A)
   const int* F;          // column scales of op(B)
   const uint32_t* fa;    // row special flags
@@ -842,7 +850,7 @@ __global__ void __launch_bounds__(256, 3) ozaki_fold_kernel(OzakiFoldParams P) {
 // Sums the residue planes of the k passes into the first pass's planes,
 // modulo p_q (y is linear in C), for `rows` rows from Y (each plane `plane`
 // values apart, a pass nmod planes), so that the reconstruction reads one
-// pass.
+// pass.  The values are fp16 (integers below 2^11).
 __global__ void __launch_bounds__(256)
     ozaki_crt_pass_sum_kernel(uint16_t* __restrict__ Y, int64_t rows, int64_t n_pad, int64_t plane, int nmod,
                               int npass, const __grid_constant__ CrtTable tab) {
@@ -850,27 +858,31 @@ __global__ void __launch_bounds__(256)
   for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < total; x += (int64_t)gridDim.x * blockDim.x) {
     const int q = (int)(x / per);
     uint16_t* y = Y + q * plane + (x - q * per);
-    uint32_t v = *y;
-    for (int ps = 1; ps < npass; ++ps) v += y[ps * pass];
-    *y = (uint16_t)crt_mod(v, tab.mod[q].p, tab.mod[q].magic);
+    // fp16 values of integers below 2^11 (exact both ways)
+    uint32_t v = (uint32_t)__half2float(__ushort_as_half(*y));
+    for (int ps = 1; ps < npass; ++ps) v += (uint32_t)__half2float(__ushort_as_half(y[ps * pass]));
+    *y = __half_as_ushort(__float2half_rn((float)crt_mod(v, tab.mod[q].p, tab.mod[q].magic)));
   }
 }
 
 // CRT reconstruction on the tensor cores (ozcrt.cuh, "Reconstruction on the
 // tensor cores").  The product kernel stored y_q = (C_q mod p_q) u_q mod p_q
-// (16 bits; one k pass, or the passes summed by ozaki_crt_pass_sum_kernel).
-// Persistent CTAs of 4 warps walk tiles of 4 rows x 32 columns of C: warp w
-// takes row 4t + w, lane l column l (one accumulator lane per output).  A
-// tile's y values arrive by TMA (boxes of 32 columns x 4 rows x 16 moduli,
-// moduli beyond nmod zero-filled) two tiles ahead into two shared-memory
-// buffers.  Two stages: each thread writes its output's y_q (fp16, exact) as
-// an operand row (K = 48, K-major, no swizzle) to the stage's shared-memory
-// operand; one thread issues three MMAs (M = 128, K = 16, N = crt_fold_n(NW))
-// against the byte table of M / p_q into the stage's accumulator; while they
-// run, each thread finishes the tile before: reads its column sums (exact
-// integers below 2^23, made integers by adding 2^23), 32 at a time,
-// assembles Y with carries (crt_fold_column), rounds X = Y - Q M once at
-// 2^(S_i + F_j - 2T) and applies the reference epilogue.  Two 64-column
+// as fp16 values (one k pass, or the passes summed by
+// ozaki_crt_pass_sum_kernel).  Persistent CTAs of 4 warps walk tiles of
+// 4 rows x 32 columns of C: warp w takes row 4t + w, lane l column l (one
+// accumulator lane per output, M index 32w + l).  A tile's y values arrive by
+// TMA straight into the MMA's A operand: the planes are read as a 4-D tensor
+// (8 columns, moduli, column groups of 8, rows), so that a box of
+// 8 x 16 x 4 x 4 lands as [row][column group][modulus][8 columns] — an
+// M-major operand without swizzle (8 outputs x 8 moduli per core matrix, the
+// next 8 outputs 256 bytes on, the next 8 moduli 128 bytes on); moduli
+// beyond nmod are zero-filled.  Three buffers, fetched two tiles ahead.  One
+// thread issues one MMA per 16 moduli (M = 128, K = 16, N = crt_fold_n(NW)) of a tile
+// against the byte table of M / p_q (K-major) into one of two accumulators;
+// while they run, every thread finishes the tile before: reads its column
+// sums (exact integers below 2^23, made integers by adding 2^23), 32 at a
+// time, assembles Y with carries (crt_fold_column), rounds X = Y - Q M once
+// at 2^(S_i + F_j - 2T) and applies the reference epilogue.  Two 64-column
 // accumulators per CTA, four CTAs per SM.  Every wait is bounded (1 s); on a
 // timeout the CTA stops, waits (bounded) for its copies and MMAs in flight,
 // records it in err[0] and frees its tensor memory (its remaining outputs
@@ -878,11 +890,15 @@ __global__ void __launch_bounds__(256)
 constexpr int kFoldThreads = 128;
 constexpr int kFoldTmemCols = 128;  // two accumulators of 64 columns
 constexpr int kFoldCtasPerSm = 4;
-constexpr int kFoldBoxBytes = 32 * 4 * 16 * 2;                     // one TMA box: 16 moduli of a tile
+constexpr int kFoldBufs = 3;
+constexpr int kFoldBoxBytes = 8 * 16 * 4 * 4 * 2;                  // one TMA box: 16 moduli of a tile (4 KiB)
 constexpr int kFoldBufBytes = kFoldBoxBytes * (kCrtMaxMods / 16);  // 12 KiB: every modulus of a tile
-constexpr int kFoldABytes = 128 * kCrtFoldK * 2;                   // 12 KiB: a stage's operand rows
-constexpr size_t kFoldSmem =
-    128 + 2 * kFoldBufBytes + 2 * kFoldABytes + kCrtFoldK * kCrtFoldMaxN * 2 + 64;  // about 54 KiB
+// M-major operand without swizzle: the descriptor's leading byte offset is
+// the step between core matrices along K, its stride byte offset the step
+// along M (the two swap roles against the K-major layout)
+constexpr uint32_t kFoldALbo = 128;  // next 8 moduli (K)
+constexpr uint32_t kFoldASbo = 256;  // next 8 outputs (M)
+constexpr size_t kFoldSmem = 128 + kFoldBufs * kFoldBufBytes + kCrtFoldK * kCrtFoldMaxN * 2 + 128;  // about 43 KiB
 
 template <int NW, bool kGrouped>
 __global__ void __launch_bounds__(kFoldThreads, kFoldCtasPerSm)
@@ -891,19 +907,17 @@ __global__ void __launch_bounds__(kFoldThreads, kFoldCtasPerSm)
   constexpr int N = crt_fold_n(NW);
   extern __shared__ __align__(128) uint8_t fold_smem[];
   uint8_t* sbase = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(fold_smem) + 127) & ~(uintptr_t)127);
-  uint8_t* ybuf = sbase;                                  // [2][48][4][32] u16 (TMA)
-  uint8_t* abuf = ybuf + 2 * kFoldBufBytes;               // [2] operand rows
-  uint8_t* tbase = abuf + 2 * kFoldABytes;                // the B table
-  uint64_t* bar = reinterpret_cast<uint64_t*>(tbase + kCrtFoldK * kCrtFoldMaxN * 2);  // mma[2], full[2]
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar + 4);
-  int* flag = reinterpret_cast<int*>(bar + 5);
+  uint8_t* ybuf = sbase;                                  // [3] A operands (TMA)
+  uint8_t* tbase = ybuf + kFoldBufs * kFoldBufBytes;      // the B table
+  uint64_t* bar = reinterpret_cast<uint64_t*>(tbase + kCrtFoldK * kCrtFoldMaxN * 2);  // mma[2], full[3]
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar + 5);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nmod = tab.nmod, nboxes = (nmod + 15) / 16;
   for (int i = threadIdx.x; i < N * kCrtFoldK / 8; i += kFoldThreads)
     reinterpret_cast<uint4*>(tbase)[i] = reinterpret_cast<const uint4*>(tab.b)[i];
   fence_proxy_async_smem();
   if (threadIdx.x == 0) {
-    for (int b = 0; b < 4; ++b) mbar_init(smem_u32(bar + b), 1);
+    for (int b = 0; b < 2 + kFoldBufs; ++b) mbar_init(smem_u32(bar + b), 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 0) {
@@ -917,11 +931,12 @@ __global__ void __launch_bounds__(kFoldThreads, kFoldCtasPerSm)
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmem_slot;
   const uint32_t tlane = tmem + ((uint32_t)(warp * 32) << 16);
-  constexpr uint32_t idesc = (1u << 4) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
-  const uint32_t sb = smem_u32(tbase), lbo = (uint32_t)N * 16u, sa = smem_u32(abuf);
-  constexpr uint32_t albo = 128 * 16;  // K-adjacent core matrices of the operand rows
+  // kind::f16, fp32 D, fp16 A (M-major: bit 15) and B (K-major), N, M = 128
+  constexpr uint32_t idesc = (1u << 4) | (1u << 15) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+  const uint32_t sb = smem_u32(tbase), lbo = (uint32_t)N * 16u, sy = smem_u32(ybuf);
   const bool failed = (P.err[0] | P.err[1] | P.err[2]) != 0;
   if (failed && P.report && blockIdx.x == 0 && threadIdx.x == 0) *reinterpret_cast<volatile int*>(P.report) = 1;
+  auto full_bar = [&](uint32_t u) { return smem_u32(bar + 2 + u % kFoldBufs); };
 
   // tiles t = blockIdx.x, + gridDim.x, ...: (row tile, column tile), by counting
   const int tiles_c = (int)((P.n + 31) / 32), tiles_r = (int)((P.m + 3) / 4);
@@ -934,13 +949,14 @@ __global__ void __launch_bounds__(kFoldThreads, kFoldCtasPerSm)
       ++r_t;
     }
   };
-  int tr = (int)blockIdx.x / tiles_c, tc = (int)blockIdx.x % tiles_c;  // the tile to pack
+  int tr = (int)blockIdx.x / tiles_c, tc = (int)blockIdx.x % tiles_c;  // the tile to multiply
   int pr = tr, pc = tc;                                                 // the next tile to fetch
-  uint32_t issued = 0, used = 0;  // tiles fetched / packed (y buffer = count & 1)
+  uint32_t issued = 0, used = 0;  // tiles fetched / multiplied (buffer = count % 3)
+  uint32_t landed = 0;             // thread 0: tiles whose copy it saw complete
   auto fetch = [&]() {             // thread 0: the next tile's y into its buffer
-    const uint32_t b = issued & 1u, fb = smem_u32(bar + 2 + b), dst = smem_u32(ybuf + b * kFoldBufBytes);
+    const uint32_t fb = full_bar(issued), dst = sy + (issued % kFoldBufs) * kFoldBufBytes;
     mbar_expect_tx(fb, (uint32_t)(nboxes * kFoldBoxBytes));
-    for (int x = 0; x < nboxes; ++x) tma_load_3d(dst + x * kFoldBoxBytes, &tmY, fb, 32 * pc, 4 * pr, 16 * x);
+    for (int x = 0; x < nboxes; ++x) tma_load_4d(dst + x * kFoldBoxBytes, &tmY, fb, 0, 16 * x, 4 * pc, 4 * pr);
     ++issued;
     advance(pr, pc);
   };
@@ -948,14 +964,14 @@ __global__ void __launch_bounds__(kFoldThreads, kFoldCtasPerSm)
     if (pr < tiles_r) fetch();
     if (pr < tiles_r) fetch();
   }
-  // the packed tile waiting to be finished: its output, exponent, old C value
+  // the multiplied tile waiting to be finished: its output, exponent, old C value
   bool pend = false, pmine = false, pspecial = true;
   int pe = 0;
   q128* pcp = P.Cout;
   q128 pcold = q_zero(0);
   q128 palpha = P.alpha, pbeta = P.beta;  // grouped: the pending output's problem's
   uint32_t mma_phase = 0;    // bit s: parity of stage s's next MMA completion
-  uint32_t outstanding = 0;  // bit s: stage s's MMAs issued and not yet waited for
+  uint32_t outstanding = 0;  // bit s: stage s's MMAs issued and not yet waited for (thread 0)
   int stage = 0;
   bool ok = true;
   // reads the column sums of stage st and writes the finished output
@@ -982,61 +998,28 @@ __global__ void __launch_bounds__(kFoldThreads, kFoldCtasPerSm)
         *pcp = q_epilogue(P.alpha, sum, P.beta, pcold);
     }
   };
-  auto wait_mma = [&](int st) -> bool {
-    if (threadIdx.x == 0) *flag = mbar_wait(smem_u32(bar + st), (mma_phase >> st) & 1u) ? 1 : 0;
-    __syncthreads();
-    const bool got = *flag != 0;
-    if (got) {
-      mma_phase ^= 1u << st;
-      outstanding &= ~(1u << st);
-    }
-    return got;
-  };
   while (tr < tiles_r) {
-    const uint32_t b = used & 1u;
-    ok = mbar_wait(smem_u32(bar + 2 + b), (used >> 1) & 1u);
-    if (!__syncthreads_and(ok)) {
-      ok = false;
-      break;
+    // thread 0: this tile's y has landed; its three MMAs into this stage
+    // (the stage's sums of two tiles ago were read before the last barrier)
+    if (threadIdx.x == 0) {
+      if (mbar_wait(full_bar(used), (used / kFoldBufs) & 1u)) {
+        ++landed;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        // one MMA per box fetched (moduli beyond nmod within a box are zero;
+        // boxes not fetched hold another tile's values and are not read)
+        const uint32_t d = tmem + (uint32_t)(64 * stage), a0 = sy + (used % kFoldBufs) * kFoldBufBytes;
+        for (int kt = 0; kt < nboxes; ++kt)
+          mma_f16kind(d, smem_desc_noswizzle(a0 + kt * kFoldBoxBytes, kFoldALbo, kFoldASbo),
+                      smem_desc_noswizzle(sb + 2 * kt * lbo, lbo, 128), idesc, kt ? 1u : 0u);
+        mma_commit(smem_u32(bar + stage));
+        outstanding |= 1u << stage;
+      } else {
+        ok = false;
+      }
     }
     ++used;
-    {
-      // y_q of this thread's output, fp16: the bits 0x6400 + y are 1024 + y
-      // (y <= 512), minus 1024 in pairs; moduli beyond nmod are zero (a
-      // buffer holds only the boxes fetched)
-      const uint16_t* yb = reinterpret_cast<const uint16_t*>(ybuf + b * kFoldBufBytes) + warp * 32 + lane;
-      uint32_t a[24];
-#pragma unroll
-      for (int h = 0; h < 24; ++h) {
-        const uint32_t y0 = 2 * h < nmod ? (uint32_t)yb[(2 * h) * 128] : 0u;
-        const uint32_t y1 = 2 * h + 1 < nmod ? (uint32_t)yb[(2 * h + 1) * 128] : 0u;
-        const uint32_t w = (y0 | (y1 << 16)) + 0x64006400u, k1024 = 0x64006400u;
-        const __half2 v =
-            __hsub2(*reinterpret_cast<const __half2*>(&w), *reinterpret_cast<const __half2*>(&k1024));
-        a[h] = *reinterpret_cast<const uint32_t*>(&v);
-      }
-      // the operand row: K-block kb (8 moduli) at kb * 2048 + 16 * row
-      uint8_t* arow = abuf + stage * kFoldABytes + 16 * threadIdx.x;
-#pragma unroll
-      for (int kb = 0; kb < kCrtFoldK / 8; ++kb)
-        *reinterpret_cast<uint4*>(arow + kb * albo) = make_uint4(a[4 * kb], a[4 * kb + 1], a[4 * kb + 2], a[4 * kb + 3]);
-    }
-    fence_proxy_async_smem();
-    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    __syncthreads();  // operand rows written; y buffer b read; this stage's sums read two tiles ago
     const int64_t i = (int64_t)tr * 4 + warp, j = (int64_t)tc * 32 + lane;
     advance(tr, tc);
-    if (threadIdx.x == 0) {
-      if (pr < tiles_r) fetch();  // into buffer b, two tiles ahead
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const uint32_t d = tmem + (uint32_t)(64 * stage), a0 = sa + stage * kFoldABytes;
-#pragma unroll
-      for (int kt = 0; kt < 3; ++kt)
-        mma_f16kind(d, smem_desc_noswizzle(a0 + 2 * kt * albo, albo, 128),
-                    smem_desc_noswizzle(sb + 2 * kt * lbo, lbo, 128), idesc, kt ? 1u : 0u);
-      mma_commit(smem_u32(bar + stage));
-    }
-    outstanding |= 1u << stage;
     // this tile's output: its loads are in flight while the tile before is finished
     bool mine;
     q128* cp;
@@ -1046,15 +1029,15 @@ __global__ void __launch_bounds__(kFoldThreads, kFoldCtasPerSm)
     if constexpr (kGrouped) {
       // m = 128 x tiles and n = 256: every (i, j) is inside the tile list
       const OzakiGroupTile gt = P.gtiles[i >> 7];
-      const OzakiGroupProb& pr = P.gprobs[gt.prob];
+      const OzakiGroupProb& pr_ = P.gprobs[gt.prob];
       const int64_t li = gt.row0 + (i & 127), lj = gt.col0 + j;
       const int64_t ai = (int64_t)gt.a_tile * 128 + (i & 127), bj = (int64_t)gt.b_tile * 256 + j;
-      mine = li < pr.m && lj < pr.n;
-      cp = pr.C + (mine ? li * pr.sci + lj * pr.scj : 0);
+      mine = li < pr_.m && lj < pr_.n;
+      cp = pr_.C + (mine ? li * pr_.sci + lj * pr_.scj : 0);
       fl = P.fa[ai] | P.fb[bj];
       e = P.S[ai] + P.F[bj] - 2 * P.T;
-      oal = pr.alpha;
-      obe = pr.beta;
+      oal = pr_.alpha;
+      obe = pr_.beta;
     } else {
       mine = i < P.m && j < P.n;
       const int64_t ii = mine ? i : 0, jj = mine ? j : 0;
@@ -1066,14 +1049,25 @@ __global__ void __launch_bounds__(kFoldThreads, kFoldCtasPerSm)
     }
     const q128 cold = ld_stream(cp);
     if (pend) {
-      if (!wait_mma(stage ^ 1)) {
+      // every thread waits for the previous tile's MMAs itself
+      const bool got = mbar_wait(smem_u32(bar + (stage ^ 1)), (mma_phase >> (stage ^ 1)) & 1u);
+      if (got) {
+        mma_phase ^= 1u << (stage ^ 1);
+        if (threadIdx.x == 0) outstanding &= ~(1u << (stage ^ 1));
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        finish(stage ^ 1);
+      } else {
         ok = false;
-        break;
       }
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      finish(stage ^ 1);
-      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    // the previous tile's sums are read and its MMAs are done (its y buffer
+    // is free): fetch two tiles ahead into it
+    if (!__syncthreads_and(ok)) {
+      ok = false;
+      break;
+    }
+    if (threadIdx.x == 0 && pr < tiles_r) fetch();
     pend = true;
     pmine = mine;
     pspecial = fl != 0;  // NaN / inf rows and columns: ozaki_special_kernel
@@ -1086,7 +1080,8 @@ __global__ void __launch_bounds__(kFoldThreads, kFoldCtasPerSm)
   }
   // the last tile (its MMAs were issued by the last iteration)
   if (ok && pend) {
-    if (wait_mma(stage ^ 1)) {
+    if (mbar_wait(smem_u32(bar + (stage ^ 1)), (mma_phase >> (stage ^ 1)) & 1u)) {
+      if (threadIdx.x == 0) outstanding &= ~(1u << (stage ^ 1));
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       finish(stage ^ 1);
     } else {
@@ -1095,12 +1090,15 @@ __global__ void __launch_bounds__(kFoldThreads, kFoldCtasPerSm)
   }
   // after a timeout, the copies and MMAs still in flight are waited for
   // (bounded), so that none is outstanding when the tensor memory is freed
-  if (!ok && threadIdx.x == 0) {
-    atomicExch(const_cast<int*>(P.err), 1);
-    if (P.report) *reinterpret_cast<volatile int*>(P.report) = 1;
+  const bool any_fail = __syncthreads_or(!ok) != 0;
+  if (threadIdx.x == 0) {
+    if (any_fail) {
+      atomicExch(const_cast<int*>(P.err), 1);
+      if (P.report) *reinterpret_cast<volatile int*>(P.report) = 1;
+    }
     for (int st = 0; st < 2; ++st)
       if ((outstanding >> st) & 1u) mbar_wait(smem_u32(bar + st), (mma_phase >> st) & 1u);
-    for (uint32_t u = used; u < issued; ++u) mbar_wait(smem_u32(bar + 2 + (u & 1u)), (u >> 1) & 1u);
+    for (uint32_t u = landed; u < issued; ++u) mbar_wait(full_bar(u), (u / kFoldBufs) & 1u);
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
@@ -1376,17 +1374,20 @@ static cudaError_t launch_crt_fold(const CrtFoldTable& ft, cudaStream_t st, cons
   const int64_t tiles = ((F.m + 3) / 4) * ((F.n + 31) / 32);
   if (tiles <= 0) return cudaSuccess;
   if (tiles > INT32_MAX || ft.N != crt_fold_n(ft.nw)) return cudaErrorInvalidValue;
-  // y planes as a 3-D tensor (columns, rows, moduli) of 16-bit values; boxes
-  // of 32 columns x 4 rows x 16 moduli (the moduli beyond nmod read as zero)
+  // y planes as a 4-D tensor of 16-bit values: (8 columns, moduli, column
+  // groups of 8, rows); a box of 8 x 16 x 4 x 4 lands as [row][column
+  // group][modulus][8 columns], the M-major operand of the kernel (the
+  // moduli beyond nmod read as zero)
+  if (F.n_pad % 32 || y_rows % 4) return cudaErrorInvalidValue;
   CUtensorMap map;
   {
     EncodeTiledFn fn = encode_fn();
     if (!fn) return cudaErrorNotSupported;
-    cuuint64_t dims[3] = {(cuuint64_t)F.n_pad, (cuuint64_t)y_rows, (cuuint64_t)ft.nmod};
-    cuuint64_t strides[2] = {(cuuint64_t)F.n_pad * 2, (cuuint64_t)F.m_pad * F.n_pad * 2};
-    cuuint32_t box[3] = {32, 4, 16};
-    cuuint32_t estr[3] = {1, 1, 1};
-    if (fn(&map, CU_TENSOR_MAP_DATA_TYPE_UINT16, 3, const_cast<uint16_t*>(F.Y), dims, strides, box, estr,
+    cuuint64_t dims[4] = {8, (cuuint64_t)ft.nmod, (cuuint64_t)F.n_pad / 8, (cuuint64_t)y_rows};
+    cuuint64_t strides[3] = {(cuuint64_t)F.m_pad * F.n_pad * 2, 16, (cuuint64_t)F.n_pad * 2};
+    cuuint32_t box[4] = {8, 16, 4, 4};
+    cuuint32_t estr[4] = {1, 1, 1, 1};
+    if (fn(&map, CU_TENSOR_MAP_DATA_TYPE_UINT16, 4, const_cast<uint16_t*>(F.Y), dims, strides, box, estr,
            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
       return cudaErrorInvalidValue;
