@@ -1,8 +1,11 @@
 """Python front end of the C ABI, mirroring the reference's C interface
 (include/quadblas/interface/c_interface.hpp) argument for argument.
 
-Host functions take numpy ``(n, 2)`` uint64 binary128 arrays (see
-``quad.py``) and update outputs in place, like the C calls.  Device
+Host functions take binary128 buffers — numpy ``(n, 2)`` uint64 arrays (see
+``quad.py``), arrays of a 16-byte binary128 dtype (numpy's longdouble where
+it is binary128, a quad-precision dtype exposing the buffer protocol,
+``V16``), or any contiguous buffer of 16-byte items — viewed without a copy
+(``quad.view``), and update outputs in place, like the C calls.  Device
 functions take CUDA tensors whose storage holds binary128 values (any
 dtype; 16 bytes per element, e.g. int64 of shape (n, 2)) and an optional
 CUDA stream (defaults to torch's current stream)."""
@@ -16,14 +19,22 @@ from . import quad
 from ._lib import check, load
 
 
-def _p(a: np.ndarray):
-    return a.ctypes.data_as(ctypes.c_void_p)
+def _p(a):
+    """Address of a binary128 buffer (viewed in place, never copied)."""
+    return quad.view(a).ctypes.data_as(ctypes.c_void_p)
 
 
 def _q1(v) -> np.ndarray:
+    """A binary128 scalar: a Python number (widened exactly from binary64), a
+    (1, 2) uint64 array, or a 16-byte binary128 value (e.g. numpy longdouble
+    where it is binary128)."""
     if isinstance(v, (float, int)):
         return quad.scalar(float(v))
-    return quad.as_quad(v)
+    if isinstance(v, np.ndarray) and v.dtype == np.uint64:
+        return quad.as_quad(v)
+    if isinstance(v, np.generic):
+        v = np.asarray(v).reshape(1)
+    return np.ascontiguousarray(quad.view(v))
 
 
 def _c(ch: str) -> bytes:
@@ -54,7 +65,7 @@ def qgemm(layout, transa, transb, m, n, k, alpha: float, A, lda, B, ldb, beta: f
 
 # ---- binary128 results and scalars (host pointers) ----------------------
 def dot(x, y, n=None, incx=1, incy=1) -> np.ndarray:
-    x, y = quad.as_quad(x), quad.as_quad(y)
+    x, y = quad.view(x), quad.view(y)
     if n is None:
         n = len(x) // incx
     out = quad.empty(1)
@@ -63,7 +74,7 @@ def dot(x, y, n=None, incx=1, incy=1) -> np.ndarray:
 
 
 def nrm2(x, n=None, incx=1) -> np.ndarray:
-    x = quad.as_quad(x)
+    x = quad.view(x)
     if n is None:
         n = len(x) // incx
     out = quad.empty(1)
@@ -72,7 +83,7 @@ def nrm2(x, n=None, incx=1) -> np.ndarray:
 
 
 def axpy(alpha, x, y, n=None, incx=1, incy=1) -> None:
-    x, y, a = quad.as_quad(x), quad.as_quad(y), _q1(alpha)
+    x, y, a = quad.view(x), quad.view(y), _q1(alpha)
     if n is None:
         n = len(x) // incx
     check(load().quadblas_qaxpy_q(n, _p(a), _p(x), incx, _p(y), incy))

@@ -28,6 +28,47 @@ def as_quad(a) -> np.ndarray:
     return a
 
 
+def longdouble_is_binary128() -> bool:
+    """True where numpy's longdouble is IEEE binary128 (AArch64 Linux), so
+    that its arrays hold binary128 values as they are."""
+    fi = np.finfo(np.longdouble)
+    return np.dtype(np.longdouble).itemsize == 16 and fi.nmant == 112 and fi.maxexp == 16384
+
+
+def view(a) -> np.ndarray:
+    """A zero-copy ``(n, 2)`` uint64 view of a buffer of binary128 values, so
+    that outputs written through it land in the caller's memory:
+
+    * ``(n, 2)`` (or ``(..., 2)``) uint64 arrays, as they are;
+    * numpy arrays of any 16-byte dtype that holds binary128 values: ``V16``,
+      a binary128 quad-precision dtype exposing the buffer protocol, or
+      ``longdouble`` where it is binary128 (``longdouble_is_binary128``;
+      elsewhere it is the x87 80-bit format, which is refused);
+    * any other object exporting a contiguous buffer of 16-byte items.
+
+    Non-contiguous buffers are refused rather than copied."""
+    if isinstance(a, np.ndarray):
+        if a.dtype == np.uint64 and a.ndim >= 1 and a.shape[-1] == 2:
+            if not a.flags.c_contiguous:
+                raise ValueError("binary128 arrays must be C-contiguous")
+            return a.reshape(-1, 2)
+        if a.dtype.itemsize != 16:
+            raise ValueError(f"dtype {a.dtype} does not hold binary128 values (16 bytes per element)")
+        if a.dtype == np.longdouble and not longdouble_is_binary128():
+            raise ValueError("numpy longdouble is not binary128 on this platform")
+        if a.dtype.kind in "iufc" and a.dtype != np.longdouble:
+            raise ValueError(f"dtype {a.dtype} does not hold binary128 values")
+        if not a.flags.c_contiguous:
+            raise ValueError("binary128 arrays must be C-contiguous")
+        return a.reshape(-1).view(np.uint64).reshape(-1, 2)
+    mv = memoryview(a)
+    if mv.itemsize != 16 and not (mv.itemsize == 1 and mv.nbytes % 16 == 0 and mv.format in ("B", "b", "c")):
+        raise ValueError("buffer items are not 16-byte binary128 values")
+    if not mv.c_contiguous:
+        raise ValueError("binary128 buffers must be contiguous")
+    return np.frombuffer(mv.cast("B"), dtype=np.uint64).reshape(-1, 2)
+
+
 def from_double(d) -> np.ndarray:
     """Exact binary64 -> binary128 widening (what Sleef_cast_from_doubleq1 does)."""
     d = np.ascontiguousarray(d, dtype=np.float64).ravel()
