@@ -14,10 +14,12 @@ fp16 tensor-core GEMM per modulus, exact CRT reconstruction; <= 1 ulp on
 this workload); metric binary128 GFLOP/s (2mnk per second).  One step is
 one qgemm with the inputs resident in HBM (A and B are 256 MB each, larger
 than L2, so no flush is needed).  Beside it ("secondary"): the soft-float
-qgemm of the same problem (the speed-up the Ozaki path is judged by), a
+qgemm of the same problem (the speed-up of the Ozaki path over it), a
 sweep over T and both schemes with the ulp distance of each result from
-the correctly rounded soft-float result, qgemv 8192^2 and qdot 2^26 (HBM
-rooflines) and the 512^3 soft-float qgemm.
+the correctly rounded soft-float result, the library's default setting,
+qgemv 8192^2 and qdot 2^26 (HBM rooflines), the 30,000-problem batch
+(soft-float, and under the Ozaki method with large qgemm problems on the
+grouped residue path) and the 512^3 soft-float qgemm.
 
 Each rank runs its own problem (weak scaling; the path needs no
 collective); rank 0 prints one JSON line.
