@@ -166,6 +166,7 @@ template <int T>
 __device__ void run_gemm_item(BShared<T>& sh, const BProb& P, const BItem& it, wacc* partials,
                               int* counters) {
   constexpr int R = T / 16;
+  constexpr int kUnroll = T == 16 ? 4 : 2;  // k steps in flight (measured: 16-wide 2 % faster at 4)
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
   const q128 zero = q_zero(0);
   wacc c[R * R];
@@ -185,7 +186,7 @@ __device__ void run_gemm_item(BShared<T>& sh, const BProb& P, const BItem& it, w
       btile_put(sh.u.t.b, bk, bc, bv);
     }
     __syncthreads();
-#pragma unroll 2
+#pragma unroll kUnroll
     for (int kk = 0; kk < kBTK; ++kk) {
       qop a[R], b[R];
 #pragma unroll
