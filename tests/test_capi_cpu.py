@@ -89,6 +89,11 @@ def test_no_cpu_fallback_without_gpu(qlib):
     assert qlib.quadblas_device_status(1) in (2, 5)
     # the serial batch runner fails the same way (and checks its arguments first)
     assert qlib.quadblas_batch_run_serial(None, -1, None) == 1
+    # batched controls: argument checks, then no device
+    assert qlib.quadblas_batch_set_ozaki_min(-1) == 1
+    assert qlib.quadblas_batch_set_ozaki_min(0) == 0
+    assert qlib.quadblas_batch_configure(1 << 16, 24) == 1  # tile edge 16 or 32 only
+    assert qlib.quadblas_qgemm_batched_dev(None, 0, None) in (2, 5)
 
 
 def test_cpp_header_compiles(tmp_path):

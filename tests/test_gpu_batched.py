@@ -306,10 +306,27 @@ def test_batch_ozaki_grouped_multi_tile_problems(qlib, torch_cuda):
 
 def test_batched_dev_one_shot(qlib, O, torch_cuda):
     """quadblas_qgemm_batched_dev (plan, execute, wait, free in one call) on a
-    mixed batch: every output equal to the exact oracle's single-call result."""
+    mixed batch: every output equal to the exact oracle's single-call result;
+    under the Ozaki method with every qgemm problem routed, equal to the
+    one-by-one calls."""
     torch = torch_cuda
     rng = G.rng_for(781)
     ar, specs, probs = make_batch(torch, rng, 10, 10, 10)
+    c0 = ar.dev.clone()
     api.batched_dev(probs)
     torch.cuda.synchronize()
     check_all(O, ar, specs)
+    api.set_method(2)
+    api.batch_set_ozaki_min(1)
+    try:
+        ar.dev.copy_(c0)
+        api.batched_dev(probs)
+        torch.cuda.synchronize()
+        batched = ar.dev.clone()
+        ar.dev.copy_(c0)
+        api.batch_run_serial(probs)
+        torch.cuda.synchronize()
+        assert torch.equal(batched, ar.dev)
+    finally:
+        api.set_method(0)
+        api.batch_set_ozaki_min(0)
