@@ -52,8 +52,15 @@ def test_refused_buffers():
 
 
 def test_entry_points_take_the_buffers(qlib):
-    """A V16 array reaches the library (which then reports that there is no
-    GPU here) rather than being refused or converted by the binding."""
+    """A V16 array reaches the library (which, without a GPU, then reports
+    that there is none) rather than being refused or converted by the
+    binding."""
+    try:
+        import torch
+        if torch.cuda.is_available():
+            pytest.skip("a GPU is present: test_buffers_on_the_gpu_path covers the calls")
+    except ImportError:
+        pass
     x = Q.from_double(np.arange(1.0, 5.0)).view(np.dtype("V16")).reshape(-1)
     with pytest.raises(QblasError):
         api.dot(x, x)
