@@ -9,7 +9,7 @@ Default: qgemm m = n = k = 4096, row-major 'N','N', alpha = 1, beta = 0,
 entries u * 2^e (u uniform in [-1, 1) with a full 113-bit significand, e a
 uniform integer in [-20, 20]), Ozaki method with each operand truncated to
 T = 9 * 15 - 1 = 134 bits after its row (column) scaling, multiplied by the
-automatic scheme: residues modulo 33 coprime moduli (Ozaki scheme II, one
+automatic scheme: residues modulo 32 coprime moduli (Ozaki scheme II, one
 fp16 tensor-core GEMM per modulus, exact CRT reconstruction; <= 1 ulp on
 this workload); metric binary128 GFLOP/s (2mnk per second).  One step is
 one qgemm with the inputs resident in HBM (A and B are 256 MB each, larger
@@ -286,7 +286,7 @@ class Qdot:
 # capture of the same workload (profiles/ holds the summaries and commands).
 NCU_TRAFFIC = {
     "qgemm4096": (2 * (9.84e9 + 1.01e9), "profiles/ozaki_mma_kernel_4096_traffic.md"),  # 15 x 9 bit digit pairs, 2 passes
-    "qgemm4096_crt": (3.037e9 + 1.086e9, "profiles/ozaki_crt_qgemm4096_launches.md"),  # T = 134, 33 moduli
+    "qgemm4096_crt": (2.994e9 + 1.054e9, "profiles/ozaki_crt_qgemm4096_launches.md"),  # T = 134, 32 moduli
     "qdot26": (2.147608e9 + 4.091e6, "profiles/qdot_partial_kernel_n2p26.md"),
     "qgemv8192": (1.074079e9 + 1.8140e7, "profiles/qgemv_lane_kernel_8192.md"),
     "qgemv8192_ozaki": (1.086039e9 + 3.946e6, "profiles/og_gemv_kernel_8192.md"),

@@ -235,7 +235,7 @@ int quadblas_get_ozaki_digit_bits(void);
  * digit pair whose weight the slice count keeps (slices (slices + 1) / 2
  * tensor-core products).  QBLAS_OZAKI_RESIDUES (Ozaki scheme II) multiplies
  * the operands' residues modulo N pairwise coprime moduli (N tensor-core
- * products, N about (2T + log2 k + 3) / 8.8) and recovers the exact integer
+ * products, N about (2T + log2 k + 1) / 8.9) and recovers the exact integer
  * sum by the Chinese remainder theorem, so its only error is the
  * truncation.  QBLAS_OZAKI_AUTO (0, the default) takes residues whenever the
  * moduli table covers T and k (T <= 191 and at most 48 moduli), else

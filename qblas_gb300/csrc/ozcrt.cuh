@@ -13,13 +13,13 @@
 // residues of A' and B' (|r| <= 256, exact in fp16) are multiplied on the
 // tensor cores (an fp32 sum of 256 products of at most 2^16 is exact), and
 // C_q = sum_l r_q(A'_il) r_q(B'_lj) == X_ij (mod p_q).  With M = prod p_q >
-// 8 k 2^(2T), the Chinese remainder theorem gives X_ij back exactly:
+// (65/32) k 2^(2T), the Chinese remainder theorem gives X_ij back exactly:
 //     Y = sum_q y_q M / p_q,   y_q = (C_q mod p_q) (M / p_q)^-1 mod p_q,
 //     X = Y - Q M,             Q = round(sum_q y_q / p_q),
 // and sum_l a_il b_lj ~= X 2^(S_i + F_j - 2T) is rounded once.  The only
 // error is the truncation of the operands to T bits, the same truncation as
 // the digit split with b*s - 1 = T bits, without its dropped digit pairs; the
-// number of tensor-core products is N (about (2T + log2 k + 3) / 8.8) instead
+// number of tensor-core products is N (about (2T + log2 k + 1) / 8.9) instead
 // of s(s+1)/2.
 #pragma once
 #include <stdint.h>
@@ -116,24 +116,43 @@ inline uint32_t crt_inverse(uint32_t a, uint32_t p) {  // a^-1 mod p, gcd(a, p) 
   return (uint32_t)(t < 0 ? t + p : t);
 }
 
-// Bits the moduli product must exceed for operands of T bits and inner
-// dimension k: |X| < k 2^(2T) <= M / 8.
-inline int crt_needed_bits(int T, int64_t k) {
-  int lk = 0;
-  while (lk < 62 && ((int64_t)1 << lk) < k) ++lk;
-  return 2 * T + lk + 3;
+// The moduli product M must exceed (65/32) k 2^(2T) for operands of T bits
+// and inner dimension k.  Then |X| < k 2^(2T) < (32/65) M, and Q is the
+// integer nearest to Y / M = Q + X / M.  Its estimate S 2^-24, S = sum_q y_q
+// P24_q with |P24_q - 2^24 / p_q| <= 1/2 and y_q < 512, is off by at most
+// n 2^-16 <= 48 2^-16 < 7.4e-4 from Y / M; |X / M| + 7.4e-4 < 32/65 + 7.4e-4
+// < 1/2, so rounding S 2^-24 gives Q.
+//
+// True when 32 M > 65 k 2^(2T) (M over `mw` little-endian words, k < 2^48,
+// 65 k 2^(2T) below 2^(32 mw)).
+inline bool crt_product_enough(const uint32_t* M, int mw, int T, int64_t k) {
+  uint32_t lhs[kCrtMaxWords + 3] = {0}, rhs[kCrtMaxWords + 3] = {0};
+  for (int w = 0; w < mw && w < kCrtMaxWords + 2; ++w) lhs[w] = M[w];
+  crt_big_mul_small(lhs, kCrtMaxWords + 3, 32u);
+  const uint64_t f = 65ull * (uint64_t)k;  // < 2^55
+  const int sh = 2 * T;
+  const int w0 = sh / 32, b0 = sh % 32;
+  const uint32_t parts[2] = {(uint32_t)f, (uint32_t)(f >> 32)};
+  for (int i = 0; i < 2; ++i) {
+    const uint64_t v = (uint64_t)parts[i] << b0;
+    if (w0 + i < kCrtMaxWords + 3) rhs[w0 + i] |= (uint32_t)v;
+    if (w0 + i + 1 < kCrtMaxWords + 3) rhs[w0 + i + 1] |= (uint32_t)(v >> 32);
+  }
+  for (int w = kCrtMaxWords + 2; w >= 0; --w)
+    if (lhs[w] != rhs[w]) return lhs[w] > rhs[w];
+  return false;
 }
 
 // Fills `tab` for T-bit operands and inner dimension k; false when more than
-// kCrtMaxMods moduli or kCrtMaxWords words would be needed (or T > 191).
+// kCrtMaxMods moduli or kCrtMaxWords words would be needed (or T > 191, or
+// k >= 2^48).
 inline bool crt_build(int T, int64_t k, CrtTable& tab) {
-  if (T < 2 || T > 191 || k < 1) return false;
+  if (T < 2 || T > 191 || k < 1 || k >= ((int64_t)1 << 48)) return false;
   uint32_t P[64];
   const int avail = crt_moduli(P, 64);
-  const int need = crt_needed_bits(T, k);
   uint32_t M[kCrtMaxWords + 2] = {1};
   int n = 0;
-  while (crt_big_bits(M, kCrtMaxWords + 2) <= need) {
+  while (!crt_product_enough(M, kCrtMaxWords + 2, T, k)) {
     if (n == kCrtMaxMods || n == avail) return false;
     crt_big_mul_small(M, kCrtMaxWords + 2, P[n++]);
   }
@@ -468,7 +487,7 @@ QB_HD q128 crt_round_x(uint32_t (&X)[NW], int e) {
   return make_q(((uint64_t)neg << 63) | ((uint64_t)bexp << 48) | (rh & kMantHiMask), rl);
 }
 
-// X = Y - Q M (two's complement modulo 2^(32 NW); |X| < M / 8), and
+// X = Y - Q M (two's complement modulo 2^(32 NW); |X| < (32/65) M), and
 // X 2^e rounded to binary128 (RNE).
 template <int NW>
 QB_HD q128 crt_acc_round(const CrtAcc<NW>& A, const uint32_t* negM, int e) {

@@ -1,14 +1,15 @@
 """The Ozaki scheme II arithmetic (qblas_gb300/csrc/ozcrt.cuh, compiled for
 the host) against Python integers and rationals:
 
-* table: pairwise coprime moduli whose product M exceeds 8 k 2^(2T) (and
-  the shortest such prefix), the inverses (M/p)^-1 mod p, M / (p p') per
+* table: pairwise coprime moduli whose product M exceeds (65/32) k 2^(2T)
+  (and the shortest such prefix), the inverses (M/p)^-1 mod p, M / (p p') per
   pair, 2^(32 nw) - M and the 2^(18 j) mod p tables;
 * crt_mod: the magic-multiplier remainder equals x % p for x < 2^31;
 * residues: V = trunc(|a| 2^(T - S)) and balanced residues r == sign * V
   (mod p), |r| <= 256;
 * reconstruction: from C_q == X (mod p_q), |C_q| <= 2^29, the result is X 2^e
-  correctly rounded (ties to even), for X across (-M/8, M/8).
+  correctly rounded (ties to even), for X across (-(32/65) M, (32/65) M),
+  the range k 2^(2T) < (32/65) M allows.
 """
 import ctypes
 import math
@@ -62,8 +63,8 @@ def test_table(sq, T, k):
     assert all(256 < p <= 513 for p in ps)
     assert all(math.gcd(a, b) == 1 for i, a in enumerate(ps) for b in ps[i + 1:])
     M = math.prod(ps)
-    need = 2 * T + math.ceil(math.log2(k)) + 3 if k > 1 else 2 * T + 3
-    assert M >= 1 << need and math.prod(ps[:-1]) < 1 << need
+    need = 65 * k << (2 * T)
+    assert 32 * M > need and 32 * math.prod(ps[:-1]) <= need
     assert M < 1 << (32 * nw) and nw % 2 == 0 and nw <= MAXWORDS
     for p, u, c18 in mods:
         assert (M // p) * u % p == 1
@@ -150,12 +151,14 @@ def test_reconstruct(sq):
     M = math.prod(ps)
     rng = np.random.default_rng(11)
     Xs = [0, 1, -1, 2, (1 << 113) - 1, -(1 << 113) + 1, (1 << 114) + 1, (1 << 114) + 3, -((1 << 114) + 3),
-          (1 << 200) + (1 << 87), (1 << 200) + (1 << 87) + 1, M // 8 - 1, -(M // 8) + 1]
-    for b in range(1, M.bit_length() - 4, 7):
+          (1 << 200) + (1 << 87), (1 << 200) + (1 << 87) + 1, M // 8 - 1, -(M // 8) + 1,
+          k << (2 * T), -(k << (2 * T)), (k << (2 * T)) - 1, -(k << (2 * T)) + 1,
+          32 * M // 65 - 1, -(32 * M // 65) + 1, 32 * M // 65 - 12345, -(32 * M // 65) + 98765]
+    for b in range(1, M.bit_length(), 7):
         x = int(rng.integers(0, 1 << 62)) << max(0, b - 62)
         x = x % (1 << b) | (1 << (b - 1))
         Xs += [x, -x]
-    Xs = [x for x in Xs if abs(x) < M // 8]
+    Xs = [x for x in Xs if 65 * abs(x) < 32 * M]
     C = np.zeros((len(Xs), n), dtype=np.int32)
     for i, x in enumerate(Xs):
         for q, p in enumerate(ps):
@@ -350,7 +353,7 @@ def test_tensor_core_reconstruction(sq, T, k):
         b = int(rng.integers(1, M.bit_length() - 4))
         x = (int(rng.integers(0, 1 << 62)) << max(0, b - 62)) % (1 << b) | (1 << (b - 1))
         Xs.append(x if rng.integers(2) else -x)
-    Xs = [x for x in Xs if abs(x) < M // 8]
+    Xs = [x for x in Xs if 65 * abs(x) < 32 * M]
     C = np.zeros((len(Xs), n), dtype=np.int32)
     for i, x in enumerate(Xs):
         for q, p in enumerate(ps):
