@@ -135,18 +135,22 @@ def to_host(t) -> np.ndarray:
 
 
 def ozaki_launches(k, s, b, crt):
-    """Kernels per device-pointer Ozaki qgemm call: fill, scale and split for
-    each operand, one tensor-core launch per k pass, fold, special values.
-    Digit pairs: a k pass holds as many fp32-exact k-chunks as an int32
-    diagonal sum of s pairs of chunk sums (each < 2^24) allows.  Residues: a
-    k pass is 8192 (the residue product sums stay below 2^29)."""
+    """Kernels per device-pointer Ozaki qgemm call on one stream, square and
+    row-major: one kernel setting the scales' starting values and error words,
+    op(B)'s scale and split, op(A)'s split (residues: op(A)'s scales come from
+    a side warp of op(B)'s split; digit pairs: a scale launch of their own),
+    one tensor-core launch per k pass (residues over several passes: one more
+    summing them), fold, special values.  Digit pairs: a k pass holds as many
+    fp32-exact k-chunks as an int32 diagonal sum of s pairs of chunk sums
+    (each < 2^24) allows.  Residues: a k pass is 8192 (the residue product
+    sums stay below 2^29)."""
     if crt:
         npass = -(-k // 8192)
-    else:
-        chunk_kb = (1 << (24 - 2 * (b - 1))) // 64
-        kbp = max(1, (2 ** 31 - 1) // (s << 24)) * chunk_kb
-        npass = -(-(-(-k // 64)) // kbp)
-    return 6 + npass + 2
+        return 4 + npass + (1 if npass > 1 else 0) + 2
+    chunk_kb = (1 << (24 - 2 * (b - 1))) // 64
+    kbp = max(1, (2 ** 31 - 1) // (s << 24)) * chunk_kb
+    npass = -(-(-(-k // 64)) // kbp)
+    return 5 + npass + 2
 
 
 def max_over_ranks(dist, x: float) -> float:

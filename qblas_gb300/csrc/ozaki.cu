@@ -22,6 +22,8 @@
 // result is rebuilt by the Chinese remainder theorem before the rounding.
 //
 // Kernels:
+//   ozaki_init_kernel,  : starting values of the scales and flags (and, on
+//   ozaki_fill_kernel     one stream, the error words)
 //   ozaki_scale_kernel,   : S_i = max_l (exponent(x_il) + 1) per row of a
 //   ozaki_scale_rows_kernel strided view (A, or B^T), plus NaN/inf flags
 //   ozaki_split_kernel  : digits of every element, written digit-major and
@@ -29,6 +31,9 @@
 //   ozaki_crt_split_tc_kernel: residues of every element on the tensor cores
 //                         (byte rows of the scaled integer times a table of
 //                         256^j mod p_q), one fp32 remainder per residue
+//                         (two elements per packed fp32 instruction); for
+//                         op(B) on one stream, a fifth warp takes op(A)'s
+//                         row scales meanwhile
 //   ozaki_mma_kernel    : persistent, warp-specialised: warp 0 issues TMA
 //                         loads (128B-swizzled 64-wide K slices of A_t and
 //                         B_u) into a 4-stage shared-memory ring, warp 1
@@ -162,6 +167,22 @@ static void launch_scale(int64_t rows, int64_t cols, const q128* p, int64_t sr, 
   }
 }
 
+// One-stream form of the two fills and the error-word resets: S, fa for m
+// rows, F, fb for n, and err[0], [1], [2], [4], [5] zeroed.
+__global__ void ozaki_init_kernel(int64_t m, int* __restrict__ S, uint32_t* __restrict__ fa, int64_t n,
+                                  int* __restrict__ F, uint32_t* __restrict__ fb, int* __restrict__ err) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < m) {
+    S[i] = kOzakiScaleEmpty;
+    fa[i] = 0u;
+  }
+  if (i < n) {
+    F[i] = kOzakiScaleEmpty;
+    fb[i] = 0u;
+  }
+  if (i == 0) err[0] = err[1] = err[2] = err[4] = err[5] = 0;
+}
+
 __global__ void ozaki_fill_kernel(int64_t n, int* __restrict__ S, uint32_t* __restrict__ flags) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) {
@@ -225,6 +246,11 @@ __global__ void __launch_bounds__(256)
 // loaded while the MMAs run.  128 tensor-memory columns per CTA (D: [0, 96),
 // A: [96, 128)), four CTAs per SM.  The wait for the MMAs is bounded (1 s);
 // on a timeout the CTA stops, records it in *err and frees its tensor memory.
+// Optionally a fifth warp per CTA computes, meanwhile, the row scales and
+// flags of the other operand (rows contiguous, as ozaki_scale_rows_kernel
+// does, one warp per whole row): that operand's own scale launch then goes,
+// and its reads use the bandwidth the split leaves.  The four split warps
+// synchronise among themselves (named barrier 1).
 struct CrtSplitParams {
   int64_t rows, cols, rows_pad, cols_pad, plane;
   const q128* p;
@@ -232,9 +258,18 @@ struct CrtSplitParams {
   const int* S;
   int* err;
   uint16_t* D;
+  // side job (xs_p null: none): rows [0, xs_rows) of xs_p, row r at
+  // xs_p + r * xs_sr, xs_cols contiguous elements; S and flags of each row
+  // are stored (the row is this warp's alone), *xs_any set on NaN or inf
+  const q128* xs_p;
+  int64_t xs_rows, xs_cols, xs_sr;
+  int* xs_S;
+  uint32_t* xs_flags;
+  int* xs_any;
 };
 
 constexpr int kSplitThreads = 128;
+constexpr int kSplitSideThreads = kSplitThreads + 32;  // with the side job's warp
 constexpr int kSplitTmemCols = 128;
 constexpr int kSplitAcol = 96;
 constexpr int kSplitCtasPerSm = 4;
@@ -256,8 +291,44 @@ __device__ __forceinline__ void crt_operand_row(q128 v, int Sr, int T, uint32_t*
   for (int i = NB / 2 + 1; i < 16; ++i) a[i] = 0u;
 }
 
+// The side job's rows [r0, r1): per row the largest exponent(x) + 1 and the
+// special-value flags, 8 loads of 16 bytes per lane in flight (a warp reads
+// 4 KiB of the row at a time).
+__device__ __forceinline__ void split_side_row_scales(const CrtSplitParams& P, int64_t r0, int64_t r1, int lane) {
+  for (int64_t r = r0; r < r1; ++r) {
+    const q128* row = P.xs_p + r * P.xs_sr;
+    int mx = kOzakiScaleEmpty;
+    uint32_t fl = 0;
+    for (int64_t c0 = 0; c0 < P.xs_cols; c0 += 256) {
+      q128 v[8];
+#pragma unroll
+      for (int t = 0; t < 8; ++t) {
+        const int64_t c = c0 + lane + 32 * t;
+        v[t] = c < P.xs_cols ? ld_stream(row + c) : q_zero(0);
+      }
+#pragma unroll
+      for (int t = 0; t < 8; ++t) {
+        mx = max(mx, ozaki_exp_plus1(v[t]));
+        fl |= ozaki_special_flags(v[t]);
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      mx = max(mx, __shfl_xor_sync(0xFFFFFFFFu, mx, o));
+      fl |= __shfl_xor_sync(0xFFFFFFFFu, fl, o);
+    }
+    if (lane == 0) {
+      P.xs_S[r] = mx;
+      P.xs_flags[r] = fl;
+      if (fl) atomicOr(P.xs_any, 1);
+    }
+  }
+}
+
+__device__ __forceinline__ void split_warps_sync() { asm volatile("bar.sync 1, 128;" ::: "memory"); }
+
 template <int NB>
-__global__ void __launch_bounds__(kSplitThreads)
+__global__ void __launch_bounds__(kSplitSideThreads)
     ozaki_crt_split_tc_kernel(const __grid_constant__ CrtSplitParams P, const __grid_constant__ CrtSplitTable tab) {
   extern __shared__ __align__(128) uint8_t split_smem[];
   uint8_t* sbase = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(split_smem) + 127) & ~(uintptr_t)127);
@@ -267,7 +338,7 @@ __global__ void __launch_bounds__(kSplitThreads)
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int N = tab.N, nmod = tab.nmod;
   // the table (B operand) into shared memory, visible to the tensor cores
-  for (int i = threadIdx.x; i < N * kCrtSplitK / 8; i += kSplitThreads)
+  for (int i = threadIdx.x; i < N * kCrtSplitK / 8 && warp < 4; i += kSplitThreads)
     reinterpret_cast<uint4*>(sbase)[i] = reinterpret_cast<const uint4*>(tab.b)[i];
   fence_proxy_async_smem();
   if (threadIdx.x == 0) {
@@ -306,6 +377,12 @@ __global__ void __launch_bounds__(kSplitThreads)
       if (c + 1 < P.cols) v1 = ld_cached(e + P.sc);
     }
   };
+  if (warp == 4) {
+    // the side job (launched with it only); this warp takes no tiles
+    const int64_t G = gridDim.x;
+    split_side_row_scales(P, P.xs_rows * blockIdx.x / G, P.xs_rows * (blockIdx.x + 1) / G, lane);
+    tr = tiles_r;
+  }
   // elements of this tile (v0, v1, Sr), the next (n*) and the one after it,
   // loaded while the MMAs of this tile run: two tiles in flight
   q128 v0, v1, n0, n1;
@@ -333,7 +410,7 @@ __global__ void __launch_bounds__(kSplitThreads)
     }
     tmem_st_wait();
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    __syncthreads();  // operand rows written; the last tile's accumulator read
+    split_warps_sync();  // operand rows written; the last tile's accumulator read
     const int64_t r = (int64_t)tr * 4 + warp, c = (int64_t)tc * 64 + 2 * lane;
     advance(tr, tc);
     if (threadIdx.x == 0) {
@@ -351,7 +428,7 @@ __global__ void __launch_bounds__(kSplitThreads)
     load(fr, fc, n0, n1, nS);  // two tiles ahead, in flight while the MMAs run
     if (threadIdx.x == 0) *flag = mbar_wait(smem_u32(bar), phase) ? 1 : 0;
     phase ^= 1u;
-    __syncthreads();
+    split_warps_sync();
     if (!*flag) {
       ok = false;
       break;
@@ -370,11 +447,14 @@ __global__ void __launch_bounds__(kSplitThreads)
         for (int i = 0; i < 8; ++i) {
           const int q = 8 * g + i;
           if (whole || q < nmod) {
-            const float p = tab.p[q], ip = tab.inv_p[q];
-            const float x0 = __uint_as_float(x[2 * i]), x1 = __uint_as_float(x[2 * i + 1]);
-            const float q0 = __fadd_rn(__fmaf_rn(x0, ip, 12582912.0f), -12582912.0f);
-            const float q1 = __fadd_rn(__fmaf_rn(x1, ip, 12582912.0f), -12582912.0f);
-            const __half2 h = __floats2half2_rn(__fmaf_rn(-q0, p, x0), __fmaf_rn(-q1, p, x1));
+            // both elements at once: u = round(x / p) (x fl(1/p) + 1.5 2^23,
+            // then - 1.5 2^23), r = x - u p
+            constexpr uint64_t kMagic = 0x4B4000004B400000ull, kNegMagic = 0xCB400000CB400000ull;
+            const uint64_t xx = f32x2_pack(x[2 * i], x[2 * i + 1]);
+            const uint64_t uu = f32x2_add(f32x2_fma(xx, tab.inv_p2[q], kMagic), kNegMagic);
+            uint32_t r0, r1;
+            f32x2_unpack(f32x2_fma(uu, tab.neg_p2[q], xx), r0, r1);
+            const __half2 h = __floats2half2_rn(__uint_as_float(r0), __uint_as_float(r1));
             out[q * plane2] = *reinterpret_cast<const uint32_t*>(&h);
           }
         }
@@ -876,20 +956,22 @@ __global__ void __launch_bounds__(256)
 // 8 x 16 x 4 x 4 lands as [row][column group][modulus][8 columns] — an
 // M-major operand without swizzle (8 outputs x 8 moduli per core matrix, the
 // next 8 outputs 256 bytes on, the next 8 moduli 128 bytes on); moduli
-// beyond nmod are zero-filled.  Three buffers, fetched two tiles ahead.  One
-// thread issues one MMA per 16 moduli (M = 128, K = 16, N = crt_fold_n(NW)) of a tile
-// against the byte table of M / p_q (K-major) into one of two accumulators;
-// while they run, every thread finishes the tile before: reads its column
-// sums (exact integers below 2^23, made integers by adding 2^23), 32 at a
-// time, assembles Y with carries (crt_fold_column), rounds X = Y - Q M once
-// at 2^(S_i + F_j - 2T) and applies the reference epilogue.  Two 64-column
-// accumulators per CTA, four CTAs per SM.  Every wait is bounded (1 s); on a
+// beyond nmod are zero-filled.  Three buffers, fetched up to three tiles
+// ahead.  One thread issues one MMA per 16 moduli (M = 128, K = 16,
+// N = crt_fold_n(NW)) of a tile against the byte table of M / p_q (K-major)
+// into the CTA's accumulator.  Every thread reads its column sums (exact
+// integers below 2^23, made integers by adding 2^23) into word sums
+// (crt_fold_column); once all have, the next tile's MMAs are issued into the
+// same accumulator and, while they run, each thread rounds X = Y - Q M once
+// at 2^(S_i + F_j - 2T) and applies the reference epilogue.  One 64-column
+// accumulator per CTA, five CTAs per SM (registers allow no more).  Every
+// wait is bounded (1 s); on a
 // timeout the CTA stops, waits (bounded) for its copies and MMAs in flight,
 // records it in err[0] and frees its tensor memory (its remaining outputs
 // stay unwritten, and the call reports the timeout).
 constexpr int kFoldThreads = 128;
-constexpr int kFoldTmemCols = 128;  // two accumulators of 64 columns
-constexpr int kFoldCtasPerSm = 4;
+constexpr int kFoldTmemCols = 64;  // one accumulator (N <= 64 columns)
+constexpr int kFoldCtasPerSm = 5;
 constexpr int kFoldBufs = 3;
 constexpr int kFoldBoxBytes = 8 * 16 * 4 * 4 * 2;                  // one TMA box: 16 moduli of a tile (4 KiB)
 constexpr int kFoldBufBytes = kFoldBoxBytes * (kCrtMaxMods / 16);  // 12 KiB: every modulus of a tile
@@ -909,15 +991,15 @@ __global__ void __launch_bounds__(kFoldThreads, kFoldCtasPerSm)
   uint8_t* sbase = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(fold_smem) + 127) & ~(uintptr_t)127);
   uint8_t* ybuf = sbase;                                  // [3] A operands (TMA)
   uint8_t* tbase = ybuf + kFoldBufs * kFoldBufBytes;      // the B table
-  uint64_t* bar = reinterpret_cast<uint64_t*>(tbase + kCrtFoldK * kCrtFoldMaxN * 2);  // mma[2], full[3]
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar + 5);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(tbase + kCrtFoldK * kCrtFoldMaxN * 2);  // mma, full[3]
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar + 1 + kFoldBufs);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nmod = tab.nmod, nboxes = (nmod + 15) / 16;
   for (int i = threadIdx.x; i < N * kCrtFoldK / 8; i += kFoldThreads)
     reinterpret_cast<uint4*>(tbase)[i] = reinterpret_cast<const uint4*>(tab.b)[i];
   fence_proxy_async_smem();
   if (threadIdx.x == 0) {
-    for (int b = 0; b < 2 + kFoldBufs; ++b) mbar_init(smem_u32(bar + b), 1);
+    for (int b = 0; b < 1 + kFoldBufs; ++b) mbar_init(smem_u32(bar + b), 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 0) {
@@ -936,7 +1018,7 @@ __global__ void __launch_bounds__(kFoldThreads, kFoldCtasPerSm)
   const uint32_t sb = smem_u32(tbase), lbo = (uint32_t)N * 16u, sy = smem_u32(ybuf);
   const bool failed = (P.err[0] | P.err[1] | P.err[2]) != 0;
   if (failed && P.report && blockIdx.x == 0 && threadIdx.x == 0) *reinterpret_cast<volatile int*>(P.report) = 1;
-  auto full_bar = [&](uint32_t u) { return smem_u32(bar + 2 + u % kFoldBufs); };
+  auto full_bar = [&](uint32_t u) { return smem_u32(bar + 1 + u % kFoldBufs); };
 
   // tiles t = blockIdx.x, + gridDim.x, ...: (row tile, column tile), by counting
   const int tiles_c = (int)((P.n + 31) / 32), tiles_r = (int)((P.m + 3) / 4);
@@ -949,7 +1031,7 @@ __global__ void __launch_bounds__(kFoldThreads, kFoldCtasPerSm)
       ++r_t;
     }
   };
-  int tr = (int)blockIdx.x / tiles_c, tc = (int)blockIdx.x % tiles_c;  // the tile to multiply
+  int tr = (int)blockIdx.x / tiles_c, tc = (int)blockIdx.x % tiles_c;  // the tile whose sums are read next
   int pr = tr, pc = tc;                                                 // the next tile to fetch
   uint32_t issued = 0, used = 0;  // tiles fetched / multiplied (buffer = count % 3)
   uint32_t landed = 0;             // thread 0: tiles whose copy it saw complete
@@ -960,133 +1042,126 @@ __global__ void __launch_bounds__(kFoldThreads, kFoldCtasPerSm)
     ++issued;
     advance(pr, pc);
   };
-  if (threadIdx.x == 0) {
-    if (pr < tiles_r) fetch();
-    if (pr < tiles_r) fetch();
-  }
-  // the multiplied tile waiting to be finished: its output, exponent, old C value
-  bool pend = false, pmine = false, pspecial = true;
-  int pe = 0;
-  q128* pcp = P.Cout;
-  q128 pcold = q_zero(0);
-  q128 palpha = P.alpha, pbeta = P.beta;  // grouped: the pending output's problem's
-  uint32_t mma_phase = 0;    // bit s: parity of stage s's next MMA completion
-  uint32_t outstanding = 0;  // bit s: stage s's MMAs issued and not yet waited for (thread 0)
-  int stage = 0;
-  bool ok = true;
-  // reads the column sums of stage st and writes the finished output
-  auto finish = [&](int st) {
-    CrtFoldAcc<NW> acc;
-    crt_fold_init(acc);
-#pragma unroll
-    for (int h = 0; h < (N + 31) / 32; ++h) {
-      uint32_t z[32];
-      tmem_ld16_nowait(tlane + (uint32_t)(64 * st + 32 * h), z);
-      if (32 * h + 16 < N) tmem_ld16_nowait(tlane + (uint32_t)(64 * st + 32 * h + 16), z + 16);
-      tmem_ld_wait();
-#pragma unroll
-      for (int c = 0; c < 32; ++c) {
-        const int w = 32 * h + c;
-        if (w < N) crt_fold_column(acc, w, __float_as_uint(__fadd_rn(__uint_as_float(z[c]), 8388608.0f)), true);
-      }
-    }
-    if (pmine && !pspecial) {
-      const q128 sum = failed ? q_nan() : crt_fold_finish(acc, tab.negM, pe, true);
-      if constexpr (kGrouped)
-        *pcp = q_epilogue(palpha, sum, pbeta, pcold);
-      else
-        *pcp = q_epilogue(P.alpha, sum, P.beta, pcold);
-    }
-  };
-  while (tr < tiles_r) {
-    // thread 0: this tile's y has landed; its three MMAs into this stage
-    // (the stage's sums of two tiles ago were read before the last barrier)
-    if (threadIdx.x == 0) {
-      if (mbar_wait(full_bar(used), (used / kFoldBufs) & 1u)) {
-        ++landed;
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        // one MMA per box fetched (moduli beyond nmod within a box are zero;
-        // boxes not fetched hold another tile's values and are not read)
-        const uint32_t d = tmem + (uint32_t)(64 * stage), a0 = sy + (used % kFoldBufs) * kFoldBufBytes;
-        for (int kt = 0; kt < nboxes; ++kt)
-          mma_f16kind(d, smem_desc_noswizzle(a0 + kt * kFoldBoxBytes, kFoldALbo, kFoldASbo),
-                      smem_desc_noswizzle(sb + 2 * kt * lbo, lbo, 128), idesc, kt ? 1u : 0u);
-        mma_commit(smem_u32(bar + stage));
-        outstanding |= 1u << stage;
-      } else {
-        ok = false;
-      }
-    }
+  bool outstanding = false;  // thread 0: an MMA group issued and not yet seen complete
+  // thread 0: tile `used` has landed; its MMAs (one per box fetched: moduli
+  // beyond nmod within a box are zero; boxes not fetched hold another tile's
+  // values and are not read) into the accumulator
+  auto multiply = [&]() -> bool {
+    if (!mbar_wait(full_bar(used), (used / kFoldBufs) & 1u)) return false;
+    ++landed;
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t a0 = sy + (used % kFoldBufs) * kFoldBufBytes;
+    for (int kt = 0; kt < nboxes; ++kt)
+      mma_f16kind(tmem, smem_desc_noswizzle(a0 + kt * kFoldBoxBytes, kFoldALbo, kFoldASbo),
+                  smem_desc_noswizzle(sb + 2 * kt * lbo, lbo, 128), idesc, kt ? 1u : 0u);
+    mma_commit(smem_u32(bar));
+    outstanding = true;
     ++used;
-    const int64_t i = (int64_t)tr * 4 + warp, j = (int64_t)tc * 32 + lane;
-    advance(tr, tc);
-    // this tile's output: its loads are in flight while the tile before is finished
-    bool mine;
+    return true;
+  };
+  bool ok = true;
+  if (threadIdx.x == 0 && tr < tiles_r) {
+    for (int f = 0; f < kFoldBufs && pr < tiles_r; ++f) fetch();
+    ok = multiply();
+  }
+  // a tile's outputs (one per thread): where it goes, its exponent, flags,
+  // old C value (and, grouped, its problem's alpha and beta), loaded a tile
+  // ahead of its rounding
+  struct OutInfo {
     q128* cp;
-    uint32_t fl;
+    q128 cold;
+    q128 al, be;
     int e;
-    q128 oal, obe;
+    bool mine, special;
+  };
+  auto out_info = [&](int r_t, int c_t) {
+    OutInfo o;
+    const int64_t i = (int64_t)r_t * 4 + warp, j = (int64_t)c_t * 32 + lane;
+    uint32_t fl;
     if constexpr (kGrouped) {
       // m = 128 x tiles and n = 256: every (i, j) is inside the tile list
       const OzakiGroupTile gt = P.gtiles[i >> 7];
       const OzakiGroupProb& pr_ = P.gprobs[gt.prob];
       const int64_t li = gt.row0 + (i & 127), lj = gt.col0 + j;
       const int64_t ai = (int64_t)gt.a_tile * 128 + (i & 127), bj = (int64_t)gt.b_tile * 256 + j;
-      mine = li < pr_.m && lj < pr_.n;
-      cp = pr_.C + (mine ? li * pr_.sci + lj * pr_.scj : 0);
+      o.mine = li < pr_.m && lj < pr_.n;
+      o.cp = pr_.C + (o.mine ? li * pr_.sci + lj * pr_.scj : 0);
       fl = P.fa[ai] | P.fb[bj];
-      e = P.S[ai] + P.F[bj] - 2 * P.T;
-      oal = pr_.alpha;
-      obe = pr_.beta;
+      o.e = P.S[ai] + P.F[bj] - 2 * P.T;
+      o.al = pr_.alpha;
+      o.be = pr_.beta;
     } else {
-      mine = i < P.m && j < P.n;
-      const int64_t ii = mine ? i : 0, jj = mine ? j : 0;
-      cp = P.Cout + ii * P.sci + jj * P.scj;
+      o.mine = i < P.m && j < P.n;
+      const int64_t ii = o.mine ? i : 0, jj = o.mine ? j : 0;
+      o.cp = P.Cout + ii * P.sci + jj * P.scj;
       fl = P.fa[ii] | P.fb[jj];
-      e = P.S[ii] + P.F[jj] - 2 * P.T;
-      oal = P.alpha;
-      obe = P.beta;
+      o.e = P.S[ii] + P.F[jj] - 2 * P.T;
+      o.al = P.alpha;
+      o.be = P.beta;
     }
-    const q128 cold = ld_stream(cp);
-    if (pend) {
-      // every thread waits for the previous tile's MMAs itself
-      const bool got = mbar_wait(smem_u32(bar + (stage ^ 1)), (mma_phase >> (stage ^ 1)) & 1u);
-      if (got) {
-        mma_phase ^= 1u << (stage ^ 1);
-        if (threadIdx.x == 0) outstanding &= ~(1u << (stage ^ 1));
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        finish(stage ^ 1);
-      } else {
-        ok = false;
+    o.special = fl != 0;  // NaN / inf rows and columns: ozaki_special_kernel
+    o.cold = ld_stream(o.cp);
+    return o;
+  };
+  uint32_t mma_phase = 0;
+  OutInfo cur;
+  if (tr < tiles_r) cur = out_info(tr, tc);
+  while (tr < tiles_r) {
+    int nr = tr, nc = tc;  // the next tile
+    advance(nr, nc);
+    OutInfo nxt;
+    if (nr < tiles_r) nxt = out_info(nr, nc);  // in flight while this tile is finished
+    // this tile's column sums (every thread waits for the MMAs itself), read
+    // into registers and folded into word sums
+    CrtFoldAcc<NW> acc;
+    crt_fold_init(acc);
+    if (mbar_wait(smem_u32(bar), mma_phase & 1u)) {
+      ++mma_phase;
+      if (threadIdx.x == 0) outstanding = false;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+      for (int h = 0; h < (N + 31) / 32; ++h) {
+        uint32_t z[32];
+        tmem_ld16_nowait(tlane + (uint32_t)(32 * h), z);
+        if (32 * h + 16 < N) tmem_ld16_nowait(tlane + (uint32_t)(32 * h + 16), z + 16);
+        tmem_ld_wait();
+        // two columns at a time (N is a multiple of 16): z + 2^23 in packed fp32
+#pragma unroll
+        for (int c = 0; c < 32; c += 2) {
+          const int w = 32 * h + c;
+          if (w < N) {
+            uint32_t b0, b1;
+            f32x2_unpack(f32x2_add(f32x2_pack(z[c], z[c + 1]), 0x4B0000004B000000ull), b0, b1);
+            crt_fold_column(acc, w, b0, true);
+            crt_fold_column(acc, w + 1, b1, true);
+          }
+        }
       }
+    } else {
+      ok = false;
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    // the previous tile's sums are read and its MMAs are done (its y buffer
-    // is free): fetch two tiles ahead into it
+    // the accumulator is read and this tile's y buffer is free: the next
+    // tile's MMAs run while this tile is rounded, and the tile three ahead is
+    // fetched into the free buffer
     if (!__syncthreads_and(ok)) {
       ok = false;
       break;
     }
-    if (threadIdx.x == 0 && pr < tiles_r) fetch();
-    pend = true;
-    pmine = mine;
-    pspecial = fl != 0;  // NaN / inf rows and columns: ozaki_special_kernel
-    pe = e;
-    pcp = cp;
-    pcold = cold;
-    palpha = oal;
-    pbeta = obe;
-    stage ^= 1;
-  }
-  // the last tile (its MMAs were issued by the last iteration)
-  if (ok && pend) {
-    if (mbar_wait(smem_u32(bar + (stage ^ 1)), (mma_phase >> (stage ^ 1)) & 1u)) {
-      if (threadIdx.x == 0) outstanding &= ~(1u << (stage ^ 1));
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      finish(stage ^ 1);
-    } else {
-      ok = false;
+    if (threadIdx.x == 0) {
+      if (nr < tiles_r && !multiply()) ok = false;
+      if (ok && pr < tiles_r) fetch();
     }
+    if (cur.mine && !cur.special) {
+      const q128 sum = failed ? q_nan() : crt_fold_finish(acc, tab.negM, cur.e, true);
+      if constexpr (kGrouped)
+        *cur.cp = q_epilogue(cur.al, sum, cur.be, cur.cold);
+      else
+        *cur.cp = q_epilogue(P.alpha, sum, P.beta, cur.cold);
+    }
+    cur = nxt;
+    tr = nr;
+    tc = nc;
   }
   // after a timeout, the copies and MMAs still in flight are waited for
   // (bounded), so that none is outstanding when the tensor memory is freed
@@ -1096,8 +1171,7 @@ __global__ void __launch_bounds__(kFoldThreads, kFoldCtasPerSm)
       atomicExch(const_cast<int*>(P.err), 1);
       if (P.report) *reinterpret_cast<volatile int*>(P.report) = 1;
     }
-    for (int st = 0; st < 2; ++st)
-      if ((outstanding >> st) & 1u) mbar_wait(smem_u32(bar + st), (mma_phase >> st) & 1u);
+    if (outstanding) mbar_wait(smem_u32(bar), mma_phase & 1u);
     for (uint32_t u = landed; u < issued; ++u) mbar_wait(full_bar(u), (u / kFoldBufs) & 1u);
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -1341,9 +1415,20 @@ static void launch_fold(int b, cudaStream_t st, const OzakiFoldParams& F) {
 // CRT residues on the tensor cores: 18 bytes of V cover T <= 144, 24 cover
 // T <= 191.  Persistent: four CTAs per SM (their tensor memory is 128
 // columns each; the dynamic shared memory keeps a fifth off the SM).
+// The side job of a split launch: row scales and flags of rows [0, rows) of
+// a view with contiguous rows (row r at p + r * sr).
+struct SplitSideScales {
+  const q128* p;
+  int64_t rows, cols, sr;
+  int* S;
+  uint32_t* flags;
+  int* any;
+};
+
 static cudaError_t launch_crt_split(const CrtSplitTable& stab, cudaStream_t st, int64_t rows, int64_t cols,
                                     int64_t rows_pad, int64_t cols_pad, int64_t plane, const q128* p, int64_t sr,
-                                    int64_t sc, const int* S, uint16_t* D, int* err) {
+                                    int64_t sc, const int* S, uint16_t* D, int* err,
+                                    const SplitSideScales* side = nullptr) {
   CrtSplitParams P;
   P.rows = rows;
   P.cols = cols;
@@ -1356,14 +1441,23 @@ static cudaError_t launch_crt_split(const CrtSplitTable& stab, cudaStream_t st, 
   P.S = S;
   P.err = err;
   P.D = D;
+  const bool with_side = side && side->rows > 0;
+  P.xs_p = with_side ? side->p : nullptr;
+  P.xs_rows = with_side ? side->rows : 0;
+  P.xs_cols = with_side ? side->cols : 0;
+  P.xs_sr = with_side ? side->sr : 0;
+  P.xs_S = with_side ? side->S : nullptr;
+  P.xs_flags = with_side ? side->flags : nullptr;
+  P.xs_any = with_side ? side->any : nullptr;
   const int64_t ntiles = (rows_pad / 4) * (cols_pad / 64);
   if (ntiles <= 0) return cudaSuccess;
   if (ntiles > INT32_MAX) return cudaErrorInvalidValue;
   const unsigned grid = (unsigned)std::min<int64_t>(ntiles, kSplitCtasPerSm * (int64_t)device_sm_count());
+  const int threads = with_side ? kSplitSideThreads : kSplitThreads;
   if (stab.NB == 18)
-    ozaki_crt_split_tc_kernel<18><<<grid, kSplitThreads, kSplitSmem, st>>>(P, stab);
+    ozaki_crt_split_tc_kernel<18><<<grid, threads, kSplitSmem, st>>>(P, stab);
   else
-    ozaki_crt_split_tc_kernel<24><<<grid, kSplitThreads, kSplitSmem, st>>>(P, stab);
+    ozaki_crt_split_tc_kernel<24><<<grid, threads, kSplitSmem, st>>>(P, stab);
   return cudaGetLastError();
 }
 
@@ -1507,21 +1601,34 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scr
   cudaStream_t sb = ov ? ov->b_stream : st;
   const bool banded = ov && ov->a_rows;
   cudaStream_t sa = banded ? ov->a_stream : st;  // op(A): scales and digits, band by band
-  ozaki_fill_kernel<<<(unsigned)((g.m + 255) / 256), 256, 0, sa>>>(g.m, S, fa);
-  ozaki_fill_kernel<<<(unsigned)((g.n + 255) / 256), 256, 0, sb>>>(g.n, F, fb);
   // error words: [0] tensor-core products (main stream), [1] op(B)'s residue
-  // split, [2] op(A)'s; each is reset on the stream of its writer
-  if ((e = cudaMemsetAsync(err, 0, 4, st)) != cudaSuccess) return e;
-  // [4], [5]: a NaN or infinity in op(B), in op(A)
-  if ((e = cudaMemsetAsync(err + 1, 0, 4, sb)) != cudaSuccess) return e;
-  if ((e = cudaMemsetAsync(err + 4, 0, 4, sb)) != cudaSuccess) return e;
+  // split, [2] op(A)'s; [4], [5]: a NaN or infinity in op(B), in op(A).
+  // On one stream one kernel sets the scales' starting values and resets
+  // them; with a caller's streams each is reset on the stream of its writer.
+  if (!ov) {
+    const int64_t mn = std::max<int64_t>(g.m, g.n);
+    ozaki_init_kernel<<<(unsigned)((mn + 255) / 256), 256, 0, st>>>(g.m, S, fa, g.n, F, fb, err);
+  } else {
+    ozaki_fill_kernel<<<(unsigned)((g.m + 255) / 256), 256, 0, sa>>>(g.m, S, fa);
+    ozaki_fill_kernel<<<(unsigned)((g.n + 255) / 256), 256, 0, sb>>>(g.n, F, fb);
+    if ((e = cudaMemsetAsync(err, 0, 4, st)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(err + 1, 0, 4, sb)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(err + 4, 0, 4, sb)) != cudaSuccess) return e;
+  }
   const dim3 blk(32, 8);
   const int64_t plane_a = L.m_pad * L.k_pad, plane_b = L.n_pad * L.k_pad;
+  // on one stream with op(A)'s rows contiguous, op(A)'s scales are taken by
+  // a fifth warp of op(B)'s residue split instead of a launch of their own:
+  // a warp streams whole rows of op(A) at about twice the rate a split CTA
+  // consumes op(B), so the side job ends within the split while m <= 2 n
+  const bool a_side = crt && !ov && g.sal == 1 && g.m <= 2 * g.n;
   {
     launch_scale(g.n, g.k, g.B, g.sbj, g.sbl, F, fb, err + 4, sms, sb);
     dim3 gb((unsigned)(L.k_pad / 64), (unsigned)(L.n_pad / 8));
+    const SplitSideScales side = {g.A, g.m, g.k, g.sai, S, fa, err + 5};
     if (crt)
-      e = launch_crt_split(stab, sb, g.n, g.k, L.n_pad, L.k_pad, plane_b, g.B, g.sbj, g.sbl, F, DB, err + 1);
+      e = launch_crt_split(stab, sb, g.n, g.k, L.n_pad, L.k_pad, plane_b, g.B, g.sbj, g.sbl, F, DB, err + 1,
+                           a_side ? &side : nullptr);
     else
       launch_split(L.b, gb, blk, sb, g.n, g.k, L.n_pad, L.k_pad, plane_b, g.B, g.sbj, g.sbl, F, L.s, DB);
     if (e != cudaSuccess || (e = cudaGetLastError()) != cudaSuccess) return e;
@@ -1536,10 +1643,10 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scr
     const int64_t rows = std::min(r1, g.m) - r0;
     cudaError_t ee;
     if (banded && ov->a_rows(ov->a_ctx, r0, r0 + rows, sa) != 0) return cudaErrorUnknown;
-    if (r0 == 0 && ((ee = cudaMemsetAsync(err + 2, 0, 4, sa)) != cudaSuccess ||
-                    (ee = cudaMemsetAsync(err + 5, 0, 4, sa)) != cudaSuccess))
+    if (ov && r0 == 0 &&
+        ((ee = cudaMemsetAsync(err + 2, 0, 4, sa)) != cudaSuccess || (ee = cudaMemsetAsync(err + 5, 0, 4, sa)) != cudaSuccess))
       return ee;
-    launch_scale(rows, g.k, g.A + r0 * g.sai, g.sai, g.sal, S + r0, fa + r0, err + 5, sms, sa);
+    if (!a_side) launch_scale(rows, g.k, g.A + r0 * g.sai, g.sai, g.sal, S + r0, fa + r0, err + 5, sms, sa);
     dim3 ga((unsigned)(L.k_pad / 64), (unsigned)((r1 - r0) / 8));
     const q128* Ab = g.A + r0 * g.sai;
     ee = cudaSuccess;

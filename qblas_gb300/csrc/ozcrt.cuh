@@ -23,6 +23,7 @@
 // of s(s+1)/2.
 #pragma once
 #include <stdint.h>
+#include <string.h>
 
 #include "ozaki.cuh"
 #include "wacc.cuh"
@@ -224,6 +225,10 @@ struct alignas(16) CrtSplitTable {
   int nmod, N, NB, T;
   float p[kCrtMaxMods];
   float inv_p[kCrtMaxMods];
+  // the same as pairs for the packed fp32 arithmetic (two elements at once):
+  // (fl(1/p), fl(1/p)) and (-p, -p) as the bits of two floats, low one first
+  uint64_t inv_p2[kCrtMaxMods];
+  uint64_t neg_p2[kCrtMaxMods];
   // B in the shared-memory layout of a K-major operand without swizzle: the
   // 16 bytes of (row n, k-block kb) at kb * (N * 16) + n * 16
   uint16_t b[kCrtSplitK * kCrtSplitMaxN];
@@ -294,6 +299,12 @@ inline void crt_split_table(const CrtTable& tab, CrtSplitTable& st) {
     const uint32_t p = tab.mod[q].p;
     st.p[q] = (float)p;
     st.inv_p[q] = (float)(1.0 / (double)p);
+    uint32_t ib, nb;
+    const float np = -(float)p;
+    memcpy(&ib, &st.inv_p[q], 4);
+    memcpy(&nb, &np, 4);
+    st.inv_p2[q] = ((uint64_t)ib << 32) | ib;
+    st.neg_p2[q] = ((uint64_t)nb << 32) | nb;
   }
   for (int n = 0; n < st.N; ++n) {
     const int q = n / 2, e = n % 2;
@@ -410,11 +421,51 @@ QB_HD void crt_acc_pair(CrtAcc<NW>& A, uint32_t y0, uint32_t y1, uint32_t p0, ui
   for (int w = 0; w < NW; ++w) A.a[w] += (uint64_t)z * W[w];
 }
 
+// Word i of X, zero outside [0, NW) (i a constant once inlined).
+template <int NW>
+QB_HD uint32_t crt_word_at(const uint32_t (&X)[NW], int i) {
+  return (i >= 0 && i < NW) ? X[(i >= 0 && i < NW) ? i : 0] : 0u;
+}
+
+// The five words X[k], X[k-1], ..., X[k-4] (zero below word 0): one branch
+// per value of k, each reading fixed registers (the outputs of a warp mostly
+// share k, so a warp mostly takes one branch).
+template <int NW>
+QB_HD void crt_window5(const uint32_t (&X)[NW], int k, uint32_t& h4, uint32_t& h3, uint32_t& h2, uint32_t& h1,
+                       uint32_t& h0) {
+  static_assert(NW <= 12, "at most 12 words");
+#define QB_CRT_WINDOW_CASE(K)                                                                        \
+  case K:                                                                                           \
+    h4 = crt_word_at<NW>(X, K);                                                                     \
+    h3 = crt_word_at<NW>(X, K - 1);                                                                 \
+    h2 = crt_word_at<NW>(X, K - 2);                                                                 \
+    h1 = crt_word_at<NW>(X, K - 3);                                                                 \
+    h0 = crt_word_at<NW>(X, K - 4);                                                                 \
+    break;
+  switch (k) {
+    QB_CRT_WINDOW_CASE(11)
+    QB_CRT_WINDOW_CASE(10)
+    QB_CRT_WINDOW_CASE(9)
+    QB_CRT_WINDOW_CASE(8)
+    QB_CRT_WINDOW_CASE(7)
+    QB_CRT_WINDOW_CASE(6)
+    QB_CRT_WINDOW_CASE(5)
+    QB_CRT_WINDOW_CASE(4)
+    QB_CRT_WINDOW_CASE(3)
+    QB_CRT_WINDOW_CASE(2)
+    QB_CRT_WINDOW_CASE(1)
+    default:
+      QB_CRT_WINDOW_CASE(0)
+  }
+#undef QB_CRT_WINDOW_CASE
+}
+
 // X 2^e rounded to binary128 (RNE), X in two's complement over NW words.
-// The magnitude's highest nonzero word k (a warp's outputs mostly share it)
+// The magnitude's highest nonzero word k (from a mask of the nonzero words)
 // gives a window of five words, normalised by one count of leading zeros:
 // the significand's 113 bits, the round bit and the sticky bits are fixed
-// positions of it.  Results below the normal range or above it take the
+// positions of it; the words below the window count only as sticky bits
+// (the mask again).  Results below the normal range or above it take the
 // general rounding (round_pack).
 template <int NW>
 QB_HD q128 crt_round_x(uint32_t (&X)[NW], int e) {
@@ -429,23 +480,14 @@ QB_HD q128 crt_round_x(uint32_t (&X)[NW], int e) {
       c >>= 32;
     }
   }
-  uint32_t h4 = 0, h3 = 0, h2 = 0, h1 = 0, h0 = 0;
-  bool below = false;
-  int k = -1;
+  uint32_t nz = 0;
 #pragma unroll
-  for (int w = NW - 1; w >= 0; --w) {
-    if (k < 0 && X[w] != 0) {
-      k = w;
-      h4 = X[w];
-      h3 = w >= 1 ? X[w - 1] : 0u;
-      h2 = w >= 2 ? X[w - 2] : 0u;
-      h1 = w >= 3 ? X[w - 3] : 0u;
-      h0 = w >= 4 ? X[w - 4] : 0u;
-#pragma unroll
-      for (int v = 0; v < w - 4; ++v) below = below || X[v] != 0;
-    }
-  }
-  if (k < 0) return q_zero(neg);
+  for (int w = 0; w < NW; ++w) nz |= (X[w] != 0u ? 1u : 0u) << w;
+  if (nz == 0) return q_zero(neg);
+  const int k = 31 - clz32(nz);
+  uint32_t h4, h3, h2, h1, h0;
+  crt_window5<NW>(X, k, h4, h3, h2, h1, h0);
+  const bool below = k >= 5 && (nz & ((1u << (k - 4)) - 1u)) != 0u;
   const int lz = clz32(h4);
   // the window shifted left by lz: its top bit is X's leading one
   const uint32_t g4 = fshl32_any(h3, h4, lz), g3 = fshl32_any(h2, h3, lz), g2 = fshl32_any(h1, h2, lz),
@@ -558,23 +600,24 @@ inline void crt_fold_table(const CrtTable& tab, CrtFoldTable& ft) {
   }
 }
 
-// The reconstruction from the column sums, one column at a time (columns in
-// order; w a constant once unrolled): byte columns w < nbytes = 4 NW - 1 add
-// Z_w 256^w into Y with carries, the two columns after them make
-// S = sum_q y_q P24_q; then Q, X = Y - Q M, and X rounded at 2^e.
+// The reconstruction from the column sums, one column at a time (w a
+// constant once unrolled): byte columns w < nbytes = 4 NW - 1 go into the
+// sum of their word, T_(w/4) += Z_w 256^(w mod 4) (each word's sum its own,
+// below 2^49, so that no carry chain runs through the columns), the two
+// columns after them make S = sum_q y_q P24_q; then Q, and one carry pass
+// over the words gives X = Y - Q M = sum_w (T_w + Q (2^(32 NW) - M)_w) 2^(32 w)
+// (mod 2^(32 NW)), which is rounded at 2^e.
 template <int NW>
 struct CrtFoldAcc {
-  uint64_t t;     // carry into the current word
-  uint32_t X[NW];
+  uint64_t T[NW];  // word sums (with the columns' offsets when biased)
   uint32_t S;
 };
 
 template <int NW>
 QB_HD void crt_fold_init(CrtFoldAcc<NW>& A) {
-  A.t = 0;
   A.S = 0;
 #pragma unroll
-  for (int i = 0; i < NW; ++i) A.X[i] = 0;
+  for (int i = 0; i < NW; ++i) A.T[i] = 0;
 }
 
 // t + (uint64_t)a * b in one wide multiply-add
@@ -595,12 +638,7 @@ template <int NW>
 QB_HD void crt_fold_column(CrtFoldAcc<NW>& A, int w, uint32_t z, bool bias = false) {
   constexpr int nbytes = 4 * NW - 1;
   if (w < nbytes) {
-    A.t = crt_mad_wide(z, 1u << (8 * (w & 3)), A.t);
-    if ((w & 3) == 3) {
-      if (bias) A.t -= 0x4B000000ull * 0x01010101ull;
-      A.X[w >> 2] = (uint32_t)A.t;
-      A.t >>= 32;
-    }
+    A.T[w >> 2] = crt_mad_wide(z, 1u << (8 * (w & 3)), A.T[w >> 2]);
   } else if (w == nbytes) {
     A.S += bias ? z - 0x4B000000u : z;
   } else if (w == nbytes + 1) {
@@ -610,18 +648,25 @@ QB_HD void crt_fold_column(CrtFoldAcc<NW>& A, int w, uint32_t z, bool bias = fal
 
 template <int NW>
 QB_HD q128 crt_fold_finish(CrtFoldAcc<NW>& A, const uint32_t* negM, int e, bool bias = false) {
-  // byte 4 NW - 2 ended the last word (three columns of it)
-  if (bias) A.t -= 0x4B000000ull * 0x00010101ull;
-  A.X[NW - 1] = (uint32_t)A.t;
   const uint32_t Q = (A.S + (1u << 23)) >> 24;  // below 2^8
+  // T_w + Q negM_w for every word at once (T_w < 2^49 once its offsets are
+  // off, Q negM_w < 2^40), then the carries
+  uint64_t V[NW];
+#pragma unroll
+  for (int w = 0; w < NW; ++w) {
+    // the last word holds three columns (bytes 4 NW - 4 .. 4 NW - 2)
+    const uint64_t off = bias ? 0x4B000000ull * (w == NW - 1 ? 0x00010101ull : 0x01010101ull) : 0ull;
+    V[w] = crt_mad_wide(Q, negM[w], A.T[w] - off);
+  }
+  uint32_t X[NW];
   uint64_t c = 0;
 #pragma unroll
   for (int w = 0; w < NW; ++w) {
-    c = crt_mad_wide(Q, negM[w], c + A.X[w]);
-    A.X[w] = (uint32_t)c;
+    c += V[w];
+    X[w] = (uint32_t)c;
     c >>= 32;
   }
-  return crt_round_x<NW>(A.X, e);
+  return crt_round_x<NW>(X, e);
 }
 
 // All columns at once (host form): Z[0 .. nbytes + 1].

@@ -36,7 +36,9 @@ def crt(qlib):
     api.set_ozaki_digit_bits(0)
 
 
-def run_case(O, sq, rng, layout, transa, transb, m, n, k, s, gen, al_d, be_d, b=9):
+def run_case(O, sq, rng, layout, transa, transb, m, n, k, s, gen, al_d, be_d, b=9, torch=None):
+    """One call (host pointers, or device pointers when torch is given)
+    against the emulation of the same algorithm."""
     col = layout == "C"
     ta, tb = transa == "T", transb == "T"
     ar, ac = (k, m) if ta else (m, k)
@@ -50,8 +52,14 @@ def run_case(O, sq, rng, layout, transa, transb, m, n, k, s, gen, al_d, be_d, b=
     alpha, beta = Q.scalar(al_d), Q.scalar(be_d)
     api.set_ozaki_slices(s)
     api.set_ozaki_digit_bits(b)
-    got = C.copy()
-    api.gemm(layout, transa, transb, m, n, k, alpha, A, lda, B, ldb, beta, got, ldc)
+    if torch is None:
+        got = C.copy()
+        api.gemm(layout, transa, transb, m, n, k, alpha, A, lda, B, ldb, beta, got, ldc)
+    else:
+        dA, dB, dC = to_dev(torch, A), to_dev(torch, B), to_dev(torch, C)
+        api.gemm_dev(layout, transa, transb, m, n, k, alpha, dA, lda, dB, ldb, beta, dC, ldc)
+        torch.cuda.synchronize()
+        got = to_host(dC)
     (sai, sal), (sbl, sbj), (sci, scj) = strides(layout, ta, tb, lda, ldb, ldc)
     sums = E.crt_gemm_sum(sq, m, n, k, A, sai, sal, B, sbl, sbj, b * s - 1)
     rows, cols = np.meshgrid(np.arange(m), np.arange(n), indexing="ij")
@@ -102,6 +110,20 @@ def test_crt_mixed_magnitudes(crt, O, sq):
     for b, s in ((9, 16), (8, 18), (7, 20)):
         got, idx, exp = run_case(O, sq, rng, "R", "N", "N", 67, 301, 45, s, gen, 1.0, 0.0, b)
         assert Q.same_bits(got[idx], exp).all(), b
+
+
+@pytest.mark.parametrize("layout,transa,transb,m,n,k", [("R", "N", "N", 70, 90, 300), ("R", "T", "N", 65, 33, 129),
+                                                     ("C", "N", "T", 129, 70, 65), ("C", "T", "T", 33, 290, 129),
+                                                     ("R", "N", "T", 300, 257, 1000)])
+def test_crt_device_pointer_bit_exact(crt, O, sq, torch_cuda, layout, transa, transb, m, n, k):
+    """Device-pointer calls on one stream: op(A)'s scales come from the side
+    warp of op(B)'s residue split where op(A)'s rows are contiguous (R/N, C/T,
+    R/N/T), from their own launch otherwise; bit-exact against the emulation
+    either way."""
+    rng = G.rng_for(431 + m)
+    got, idx, exp = run_case(O, sq, rng, layout, transa, transb, m, n, k, 15, G.spread_uniform, 1.5, -0.75,
+                             torch=torch_cuda)
+    assert Q.same_bits(got[idx], exp).all(), int((~Q.same_bits(got[idx], exp)).sum())
 
 
 @pytest.mark.parametrize("size", [512, 4096])
@@ -165,7 +187,10 @@ def test_host_pointer_row_bands_match_device(crt, torch_cuda, scheme, shape, pin
     assert Q.same_bits(got, ref).all(), int((~Q.same_bits(got, ref)).sum())
 
 
-def test_crt_special_values(crt, O):
+@pytest.mark.parametrize("device", [False, True])
+def test_crt_special_values(crt, O, device, request):
+    """Host pointers, and device pointers on one stream (there op(A)'s row
+    scales and flags come from the side warp of op(B)'s split)."""
     rng = G.rng_for(422)
     m, n, k = 9, 11, 13
     A, B = G.uniform_full(rng, m * k), G.uniform_full(rng, k * n)
@@ -173,8 +198,15 @@ def test_crt_special_values(crt, O):
     A[5 * k + 1] = [0, 0x7FFF000000000000]   # +inf in row 5
     B[4 * n + 7] = [0, 0xFFFF000000000000]   # -inf in column 7
     C = Q.from_double(np.zeros(m * n))
-    got = C.copy()
-    api.gemm("R", "N", "N", m, n, k, Q.scalar(1.0), A, k, B, n, Q.scalar(0.0), got, n)
+    if device:
+        torch = request.getfixturevalue("torch_cuda")
+        dA, dB, dC = to_dev(torch, A), to_dev(torch, B), to_dev(torch, C)
+        api.gemm_dev("R", "N", "N", m, n, k, Q.scalar(1.0), dA, k, dB, n, Q.scalar(0.0), dC, n)
+        torch.cuda.synchronize()
+        got = to_host(dC)
+    else:
+        got = C.copy()
+        api.gemm("R", "N", "N", m, n, k, Q.scalar(1.0), A, k, B, n, Q.scalar(0.0), got, n)
     rows, cols = np.meshgrid(np.arange(m), np.arange(n), indexing="ij")
     R, _, _ = O.exact_gemm(k, A, k, 1, B, n, 1, rows.ravel(), cols.ravel())
     special = np.zeros((m, n), bool)
