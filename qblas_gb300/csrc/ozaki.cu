@@ -984,22 +984,21 @@ constexpr size_t kFoldSmem = 128 + kFoldBufs * kFoldBufBytes + kCrtFoldK * kCrtF
 
 template <int NW, bool kGrouped>
 __global__ void __launch_bounds__(kFoldThreads, kFoldCtasPerSm)
-    ozaki_crt_fold_tc_kernel(const __grid_constant__ CUtensorMap tmY, const __grid_constant__ OzakiFoldParams P,
-                             const __grid_constant__ CrtFoldTable tab) {
+    ozaki_crt_fold_tc_kernel(const __grid_constant__ OzakiFoldParams P, const __grid_constant__ CrtFoldTable tab) {
   constexpr int N = crt_fold_n(NW);
   extern __shared__ __align__(128) uint8_t fold_smem[];
   uint8_t* sbase = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(fold_smem) + 127) & ~(uintptr_t)127);
-  uint8_t* ybuf = sbase;                                  // [3] A operands (TMA)
+  uint8_t* ybuf = sbase;                                  // [3] A operands
   uint8_t* tbase = ybuf + kFoldBufs * kFoldBufBytes;      // the B table
-  uint64_t* bar = reinterpret_cast<uint64_t*>(tbase + kCrtFoldK * kCrtFoldMaxN * 2);  // mma, full[3]
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar + 1 + kFoldBufs);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(tbase + kCrtFoldK * kCrtFoldMaxN * 2);  // MMA completion
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar + 1);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nmod = tab.nmod, nboxes = (nmod + 15) / 16;
   for (int i = threadIdx.x; i < N * kCrtFoldK / 8; i += kFoldThreads)
     reinterpret_cast<uint4*>(tbase)[i] = reinterpret_cast<const uint4*>(tab.b)[i];
   fence_proxy_async_smem();
   if (threadIdx.x == 0) {
-    for (int b = 0; b < 1 + kFoldBufs; ++b) mbar_init(smem_u32(bar + b), 1);
+    mbar_init(smem_u32(bar), 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 0) {
@@ -1018,7 +1017,6 @@ __global__ void __launch_bounds__(kFoldThreads, kFoldCtasPerSm)
   const uint32_t sb = smem_u32(tbase), lbo = (uint32_t)N * 16u, sy = smem_u32(ybuf);
   const bool failed = (P.err[0] | P.err[1] | P.err[2]) != 0;
   if (failed && P.report && blockIdx.x == 0 && threadIdx.x == 0) *reinterpret_cast<volatile int*>(P.report) = 1;
-  auto full_bar = [&](uint32_t u) { return smem_u32(bar + 1 + u % kFoldBufs); };
 
   // tiles t = blockIdx.x, + gridDim.x, ...: (row tile, column tile), by counting
   const int tiles_c = (int)((P.n + 31) / 32), tiles_r = (int)((P.m + 3) / 4);
@@ -1034,21 +1032,33 @@ __global__ void __launch_bounds__(kFoldThreads, kFoldCtasPerSm)
   int tr = (int)blockIdx.x / tiles_c, tc = (int)blockIdx.x % tiles_c;  // the tile whose sums are read next
   int pr = tr, pc = tc;                                                 // the next tile to fetch
   uint32_t issued = 0, used = 0;  // tiles fetched / multiplied (buffer = count % 3)
-  uint32_t landed = 0;             // thread 0: tiles whose copy it saw complete
-  auto fetch = [&]() {             // thread 0: the next tile's y into its buffer
-    const uint32_t fb = full_bar(issued), dst = sy + (issued % kFoldBufs) * kFoldBufBytes;
-    mbar_expect_tx(fb, (uint32_t)(nboxes * kFoldBoxBytes));
-    for (int x = 0; x < nboxes; ++x) tma_load_4d(dst + x * kFoldBoxBytes, &tmY, fb, 0, 16 * x, 4 * pc, 4 * pr);
-    ++issued;
-    advance(pr, pc);
+  // every thread: its 16-byte pieces of the next tile (a box per 16 moduli,
+  // [row][column group][modulus][8 columns] as above, 256 pieces per box:
+  // 4 consecutive lanes read a row's 64 contiguous bytes of one plane) into
+  // the tile's buffer, moduli beyond nmod as zeros; one commit group per
+  // call, empty past the last tile
+  const int64_t plane = P.m_pad * P.n_pad;
+  auto fetch = [&]() {
+    if (pr < tiles_r) {
+      const uint32_t dst = sy + (issued % kFoldBufs) * kFoldBufBytes;
+      const int64_t i0 = (int64_t)pr * 4, j0 = (int64_t)pc * 32;
+      for (int p = threadIdx.x; p < nboxes * 256; p += kFoldThreads) {
+        const int g = p & 3, m = (p >> 2) & 15, r = (p >> 6) & 3, x = p >> 8;
+        const int q = 16 * x + m;
+        const uint32_t so = (uint32_t)(x * kFoldBoxBytes + r * 1024 + g * 256 + m * 16);
+        const uint16_t* src = P.Y + (q < nmod ? q * plane + (i0 + r) * P.n_pad + j0 + 8 * g : 0);
+        cp_async16_zfill(dst + so, src, q < nmod ? 16u : 0u);
+      }
+      ++issued;
+      advance(pr, pc);
+    }
+    cp_async_commit();
   };
   bool outstanding = false;  // thread 0: an MMA group issued and not yet seen complete
-  // thread 0: tile `used` has landed; its MMAs (one per box fetched: moduli
-  // beyond nmod within a box are zero; boxes not fetched hold another tile's
-  // values and are not read) into the accumulator
-  auto multiply = [&]() -> bool {
-    if (!mbar_wait(full_bar(used), (used / kFoldBufs) & 1u)) return false;
-    ++landed;
+  // thread 0: tile `used`'s pieces are in and visible to the tensor cores;
+  // its MMAs (one per box: moduli beyond nmod within a box are zero) into
+  // the accumulator
+  auto multiply = [&]() {
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t a0 = sy + (used % kFoldBufs) * kFoldBufBytes;
     for (int kt = 0; kt < nboxes; ++kt)
@@ -1057,27 +1067,31 @@ __global__ void __launch_bounds__(kFoldThreads, kFoldCtasPerSm)
     mma_commit(smem_u32(bar));
     outstanding = true;
     ++used;
-    return true;
   };
   bool ok = true;
-  if (threadIdx.x == 0 && tr < tiles_r) {
-    for (int f = 0; f < kFoldBufs && pr < tiles_r; ++f) fetch();
-    ok = multiply();
-  }
-  // a tile's outputs (one per thread): where it goes, its exponent, flags,
+  // the first three tiles' pieces (three groups); the first tile's MMAs once
+  // its group is in (the copies are generic-proxy writes: each thread fences
+  // them to the async proxy before the barrier)
+  for (int f = 0; f < kFoldBufs; ++f) fetch();
+  cp_async_wait<kFoldBufs - 1>();
+  fence_proxy_async_smem();
+  __syncthreads();
+  if (threadIdx.x == 0 && tr < tiles_r) multiply();
+  // a tile's outputs (one per thread): where it goes, its scales and flags,
   // old C value (and, grouped, its problem's alpha and beta), loaded a tile
-  // ahead of its rounding
+  // ahead of its rounding and combined only there, so that the loads are in
+  // flight for a whole tile
   struct OutInfo {
     q128* cp;
     q128 cold;
     q128 al, be;
-    int e;
-    bool mine, special;
+    int S, F;
+    uint32_t fa, fb;
+    bool mine;
   };
   auto out_info = [&](int r_t, int c_t) {
     OutInfo o;
     const int64_t i = (int64_t)r_t * 4 + warp, j = (int64_t)c_t * 32 + lane;
-    uint32_t fl;
     if constexpr (kGrouped) {
       // m = 128 x tiles and n = 256: every (i, j) is inside the tile list
       const OzakiGroupTile gt = P.gtiles[i >> 7];
@@ -1086,20 +1100,23 @@ __global__ void __launch_bounds__(kFoldThreads, kFoldCtasPerSm)
       const int64_t ai = (int64_t)gt.a_tile * 128 + (i & 127), bj = (int64_t)gt.b_tile * 256 + j;
       o.mine = li < pr_.m && lj < pr_.n;
       o.cp = pr_.C + (o.mine ? li * pr_.sci + lj * pr_.scj : 0);
-      fl = P.fa[ai] | P.fb[bj];
-      o.e = P.S[ai] + P.F[bj] - 2 * P.T;
+      o.fa = P.fa[ai];
+      o.fb = P.fb[bj];
+      o.S = P.S[ai];
+      o.F = P.F[bj];
       o.al = pr_.alpha;
       o.be = pr_.beta;
     } else {
       o.mine = i < P.m && j < P.n;
       const int64_t ii = o.mine ? i : 0, jj = o.mine ? j : 0;
       o.cp = P.Cout + ii * P.sci + jj * P.scj;
-      fl = P.fa[ii] | P.fb[jj];
-      o.e = P.S[ii] + P.F[jj] - 2 * P.T;
+      o.fa = P.fa[ii];
+      o.fb = P.fb[jj];
+      o.S = P.S[ii];
+      o.F = P.F[jj];
       o.al = P.alpha;
       o.be = P.beta;
     }
-    o.special = fl != 0;  // NaN / inf rows and columns: ozaki_special_kernel
     o.cold = ld_stream(o.cp);
     return o;
   };
@@ -1140,6 +1157,9 @@ __global__ void __launch_bounds__(kFoldThreads, kFoldCtasPerSm)
     } else {
       ok = false;
     }
+    // the next tile's pieces (the group before the newest) are in
+    cp_async_wait<1>();
+    fence_proxy_async_smem();
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     // the accumulator is read and this tile's y buffer is free: the next
     // tile's MMAs run while this tile is rounded, and the tile three ahead is
@@ -1148,12 +1168,11 @@ __global__ void __launch_bounds__(kFoldThreads, kFoldCtasPerSm)
       ok = false;
       break;
     }
-    if (threadIdx.x == 0) {
-      if (nr < tiles_r && !multiply()) ok = false;
-      if (ok && pr < tiles_r) fetch();
-    }
-    if (cur.mine && !cur.special) {
-      const q128 sum = failed ? q_nan() : crt_fold_finish(acc, tab.negM, cur.e, true);
+    if (threadIdx.x == 0 && nr < tiles_r) multiply();
+    fetch();
+    // NaN / inf rows and columns (a flag set) are ozaki_special_kernel's
+    if (cur.mine && (cur.fa | cur.fb) == 0u) {
+      const q128 sum = failed ? q_nan() : crt_fold_finish(acc, tab.negM, cur.S + cur.F - 2 * P.T, true);
       if constexpr (kGrouped)
         *cur.cp = q_epilogue(cur.al, sum, cur.be, cur.cold);
       else
@@ -1172,8 +1191,8 @@ __global__ void __launch_bounds__(kFoldThreads, kFoldCtasPerSm)
       if (P.report) *reinterpret_cast<volatile int*>(P.report) = 1;
     }
     if (outstanding) mbar_wait(smem_u32(bar), mma_phase & 1u);
-    for (uint32_t u = landed; u < issued; ++u) mbar_wait(full_bar(u), (u / kFoldBufs) & 1u);
   }
+  cp_async_wait<0>();
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -1468,24 +1487,9 @@ static cudaError_t launch_crt_fold(const CrtFoldTable& ft, cudaStream_t st, cons
   const int64_t tiles = ((F.m + 3) / 4) * ((F.n + 31) / 32);
   if (tiles <= 0) return cudaSuccess;
   if (tiles > INT32_MAX || ft.N != crt_fold_n(ft.nw)) return cudaErrorInvalidValue;
-  // y planes as a 4-D tensor of 16-bit values: (8 columns, moduli, column
-  // groups of 8, rows); a box of 8 x 16 x 4 x 4 lands as [row][column
-  // group][modulus][8 columns], the M-major operand of the kernel (the
-  // moduli beyond nmod read as zero)
-  if (F.n_pad % 32 || y_rows % 4) return cudaErrorInvalidValue;
-  CUtensorMap map;
-  {
-    EncodeTiledFn fn = encode_fn();
-    if (!fn) return cudaErrorNotSupported;
-    cuuint64_t dims[4] = {8, (cuuint64_t)ft.nmod, (cuuint64_t)F.n_pad / 8, (cuuint64_t)y_rows};
-    cuuint64_t strides[3] = {(cuuint64_t)F.m_pad * F.n_pad * 2, 16, (cuuint64_t)F.n_pad * 2};
-    cuuint32_t box[4] = {8, 16, 4, 4};
-    cuuint32_t estr[4] = {1, 1, 1, 1};
-    if (fn(&map, CU_TENSOR_MAP_DATA_TYPE_UINT16, 4, const_cast<uint16_t*>(F.Y), dims, strides, box, estr,
-           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
-      return cudaErrorInvalidValue;
-  }
+  // the kernel reads each tile's y values as 16-byte pieces (8 columns of a
+  // row of a plane): 16-byte aligned rows and planes, whole row tiles
+  if (F.n_pad % 32 || y_rows % 4 || (reinterpret_cast<uintptr_t>(F.Y) & 15)) return cudaErrorInvalidValue;
   static std::atomic<bool> attr_set[64];
   int dev = 0;
   cudaGetDevice(&dev);
@@ -1503,19 +1507,19 @@ static cudaError_t launch_crt_fold(const CrtFoldTable& ft, cudaStream_t st, cons
   const bool grouped = F.gtiles != nullptr;
   if (ft.nw <= 8) {
     if (grouped)
-      ozaki_crt_fold_tc_kernel<8, true><<<grid, kFoldThreads, kFoldSmem, st>>>(map, F, ft);
+      ozaki_crt_fold_tc_kernel<8, true><<<grid, kFoldThreads, kFoldSmem, st>>>(F, ft);
     else
-      ozaki_crt_fold_tc_kernel<8, false><<<grid, kFoldThreads, kFoldSmem, st>>>(map, F, ft);
+      ozaki_crt_fold_tc_kernel<8, false><<<grid, kFoldThreads, kFoldSmem, st>>>(F, ft);
   } else if (ft.nw <= 10) {
     if (grouped)
-      ozaki_crt_fold_tc_kernel<10, true><<<grid, kFoldThreads, kFoldSmem, st>>>(map, F, ft);
+      ozaki_crt_fold_tc_kernel<10, true><<<grid, kFoldThreads, kFoldSmem, st>>>(F, ft);
     else
-      ozaki_crt_fold_tc_kernel<10, false><<<grid, kFoldThreads, kFoldSmem, st>>>(map, F, ft);
+      ozaki_crt_fold_tc_kernel<10, false><<<grid, kFoldThreads, kFoldSmem, st>>>(F, ft);
   } else {
     if (grouped)
-      ozaki_crt_fold_tc_kernel<12, true><<<grid, kFoldThreads, kFoldSmem, st>>>(map, F, ft);
+      ozaki_crt_fold_tc_kernel<12, true><<<grid, kFoldThreads, kFoldSmem, st>>>(F, ft);
     else
-      ozaki_crt_fold_tc_kernel<12, false><<<grid, kFoldThreads, kFoldSmem, st>>>(map, F, ft);
+      ozaki_crt_fold_tc_kernel<12, false><<<grid, kFoldThreads, kFoldSmem, st>>>(F, ft);
   }
   return cudaGetLastError();
 }

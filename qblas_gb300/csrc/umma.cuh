@@ -38,6 +38,20 @@ __device__ __forceinline__ uint64_t f32x2_add(uint64_t a, uint64_t b) {
   return d;
 }
 
+// 16-byte asynchronous copy global -> shared (L2 only); src_bytes 0 writes
+// zeros without reading.  The copies of a thread are grouped by commit and
+// waited for by group (at most N newer groups left in flight).
+__device__ __forceinline__ void cp_async16_zfill(uint32_t dst, const void* src, uint32_t src_bytes) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(src_bytes) : "memory");
+}
+
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
 __device__ __forceinline__ unsigned long long global_timer() {
   unsigned long long t;
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
