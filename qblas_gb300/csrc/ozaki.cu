@@ -950,14 +950,15 @@ __global__ void __launch_bounds__(256)
 // as fp16 values (one k pass, or the passes summed by
 // ozaki_crt_pass_sum_kernel).  Persistent CTAs of 4 warps walk tiles of
 // 4 rows x 32 columns of C: warp w takes row 4t + w, lane l column l (one
-// accumulator lane per output, M index 32w + l).  A tile's y values arrive by
-// TMA straight into the MMA's A operand: the planes are read as a 4-D tensor
-// (8 columns, moduli, column groups of 8, rows), so that a box of
-// 8 x 16 x 4 x 4 lands as [row][column group][modulus][8 columns] — an
-// M-major operand without swizzle (8 outputs x 8 moduli per core matrix, the
-// next 8 outputs 256 bytes on, the next 8 moduli 128 bytes on); moduli
-// beyond nmod are zero-filled.  Three buffers, fetched up to three tiles
-// ahead.  One thread issues one MMA per 16 moduli (M = 128, K = 16,
+// accumulator lane per output, M index 32w + l).  A tile's y values are
+// copied (16-byte cp.async by every thread, 8 columns of one row of one
+// plane each) straight into the MMA's A operand, per 16 moduli a block of
+// [row][column group][modulus][8 columns] — an M-major operand without
+// swizzle (8 outputs x 8 moduli per core matrix, the next 8 outputs 256
+// bytes on, the next 8 moduli 128 bytes on); moduli beyond nmod are written
+// as zeros.  Three buffers, fetched up to three tiles ahead; each thread
+// fences its copies to the async proxy before the barrier after which the
+// tile's MMAs are issued.  One thread issues one MMA per 16 moduli (M = 128, K = 16,
 // N = crt_fold_n(NW)) of a tile against the byte table of M / p_q (K-major)
 // into the CTA's accumulator.  Every thread reads its column sums (exact
 // integers below 2^23, made integers by adding 2^23) into word sums
@@ -965,15 +966,15 @@ __global__ void __launch_bounds__(256)
 // same accumulator and, while they run, each thread rounds X = Y - Q M once
 // at 2^(S_i + F_j - 2T) and applies the reference epilogue.  One 64-column
 // accumulator per CTA, five CTAs per SM (registers allow no more).  Every
-// wait is bounded (1 s); on a
-// timeout the CTA stops, waits (bounded) for its copies and MMAs in flight,
-// records it in err[0] and frees its tensor memory (its remaining outputs
-// stay unwritten, and the call reports the timeout).
+// wait is bounded (1 s); on a timeout the CTA stops, waits for its copies
+// and (bounded) for its MMAs in flight, records it in err[0] and frees its
+// tensor memory (its remaining outputs stay unwritten, and the call reports
+// the timeout).
 constexpr int kFoldThreads = 128;
 constexpr int kFoldTmemCols = 64;  // one accumulator (N <= 64 columns)
 constexpr int kFoldCtasPerSm = 5;
 constexpr int kFoldBufs = 3;
-constexpr int kFoldBoxBytes = 8 * 16 * 4 * 4 * 2;                  // one TMA box: 16 moduli of a tile (4 KiB)
+constexpr int kFoldBoxBytes = 8 * 16 * 4 * 4 * 2;                  // 16 moduli of a tile (4 KiB)
 constexpr int kFoldBufBytes = kFoldBoxBytes * (kCrtMaxMods / 16);  // 12 KiB: every modulus of a tile
 // M-major operand without swizzle: the descriptor's leading byte offset is
 // the step between core matrices along K, its stride byte offset the step

@@ -114,12 +114,12 @@ def test_crt_mixed_magnitudes(crt, O, sq):
 
 @pytest.mark.parametrize("layout,transa,transb,m,n,k", [("R", "N", "N", 70, 90, 300), ("R", "T", "N", 65, 33, 129),
                                                      ("C", "N", "T", 129, 70, 65), ("C", "T", "T", 33, 290, 129),
-                                                     ("R", "N", "T", 300, 257, 1000)])
+                                                     ("R", "N", "T", 300, 257, 1000), ("R", "N", "N", 600, 130, 200)])
 def test_crt_device_pointer_bit_exact(crt, O, sq, torch_cuda, layout, transa, transb, m, n, k):
     """Device-pointer calls on one stream: op(A)'s scales come from the side
-    warp of op(B)'s residue split where op(A)'s rows are contiguous (R/N, C/T,
-    R/N/T), from their own launch otherwise; bit-exact against the emulation
-    either way."""
+    warp of op(B)'s residue split where op(A)'s rows are contiguous and
+    m <= 2n (R/N, C/T, R/N/T), from their own launch otherwise (transposed
+    layouts, and 600 > 2 * 130); bit-exact against the emulation either way."""
     rng = G.rng_for(431 + m)
     got, idx, exp = run_case(O, sq, rng, layout, transa, transb, m, n, k, 15, G.spread_uniform, 1.5, -0.75,
                              torch=torch_cuda)
