@@ -86,6 +86,8 @@ namespace qb {
 __global__ void ozaki_scale_kernel(int64_t rows, int64_t cols, const q128* __restrict__ p,
                                    int64_t sr, int64_t sc, int* __restrict__ S,
                                    uint32_t* __restrict__ flags, int* __restrict__ any) {
+  pdl_wait();
+  pdl_trigger();
   const int64_t nchunk = (cols + 63) / 64;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < rows * nchunk; w += stride) {
@@ -120,6 +122,8 @@ __global__ void ozaki_scale_kernel(int64_t rows, int64_t cols, const q128* __res
 __global__ void __launch_bounds__(256)
     ozaki_scale_rows_kernel(int64_t rows, int64_t cols, const q128* __restrict__ p, int64_t sr,
                             int* __restrict__ S, uint32_t* __restrict__ flags, int* __restrict__ any) {
+  pdl_wait();
+  pdl_trigger();
   const int lane = threadIdx.x & 31;
   const int64_t nchunk = (cols + 255) / 256;
   const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x / 32);
@@ -152,19 +156,43 @@ __global__ void __launch_bounds__(256)
   }
 }
 
-// Scales and flags of a view (rows x cols), on stream st.
-static void launch_scale(int64_t rows, int64_t cols, const q128* p, int64_t sr, int64_t sc, int* S,
-                         uint32_t* flags, int* any, int sms, cudaStream_t st) {
-  if (rows <= 0) return;
+// Launches kern on st; with pdl, as a programmatic dependent of the kernel
+// before it in the stream (its launch may start while that kernel runs;
+// the kernel's pdl_wait orders its memory accesses after it).
+template <typename... KArgs, typename... Args>
+static cudaError_t launch_maybe_pdl(bool pdl, void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                                    cudaStream_t st, Args... args) {
+  if (!pdl) {
+    kern<<<grid, block, smem, st>>>(args...);
+    return cudaGetLastError();
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kern, args...);
+}
+
+// Scales and flags of a view (rows x cols), on stream st (pdl: as a
+// programmatic dependent of the kernel before it).
+static cudaError_t launch_scale(int64_t rows, int64_t cols, const q128* p, int64_t sr, int64_t sc, int* S,
+                                uint32_t* flags, int* any, int sms, cudaStream_t st, bool pdl = false) {
+  if (rows <= 0) return cudaSuccess;
   if (sc == 1) {
     const int64_t warps = rows * ((cols + 255) / 256);
     const unsigned b = (unsigned)std::max<int64_t>(1, std::min<int64_t>((warps + 7) / 8, (int64_t)sms * 8));
-    ozaki_scale_rows_kernel<<<b, 256, 0, st>>>(rows, cols, p, sr, S, flags, any);
-  } else {
-    const int64_t w = rows * ((cols + 63) / 64);
-    const unsigned b = (unsigned)std::max<int64_t>(1, std::min<int64_t>((w + 255) / 256, (int64_t)sms * 8));
-    ozaki_scale_kernel<<<b, 256, 0, st>>>(rows, cols, p, sr, sc, S, flags, any);
+    return launch_maybe_pdl(pdl, ozaki_scale_rows_kernel, dim3(b), dim3(256), 0, st, rows, cols, p, sr, S, flags,
+                            any);
   }
+  const int64_t w = rows * ((cols + 63) / 64);
+  const unsigned b = (unsigned)std::max<int64_t>(1, std::min<int64_t>((w + 255) / 256, (int64_t)sms * 8));
+  return launch_maybe_pdl(pdl, ozaki_scale_kernel, dim3(b), dim3(256), 0, st, rows, cols, p, sr, sc, S, flags, any);
 }
 
 // One-stream form of the two fills and the error-word resets: S, fa for m
@@ -355,6 +383,8 @@ __global__ void __launch_bounds__(kSplitSideThreads)
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmem_slot;
+  pdl_wait();
+  pdl_trigger();
   const uint32_t tlane = tmem + ((uint32_t)(warp * 32) << 16);
   const uint32_t idesc = (1u << 4) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
   const uint32_t sb = smem_u32(sbase), lbo = (uint32_t)N * 16u;
@@ -655,6 +685,8 @@ __global__ void __launch_bounds__(kMmaThreads, 1)
   const uint32_t tmem = *tmem_slot;
   // paired: the peer's barriers are initialised before any copy or commit reaches them
   if (P.pair) cluster_sync_all();
+  pdl_wait();
+  pdl_trigger();
 
   const UnitDeal deal = unit_deal(P);
   const int nun = cta_unit_count(P, deal);
@@ -1012,6 +1044,8 @@ __global__ void __launch_bounds__(kFoldThreads, kFoldCtasPerSm)
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmem_slot;
+  pdl_wait();
+  pdl_trigger();
   const uint32_t tlane = tmem + ((uint32_t)(warp * 32) << 16);
   // kind::f16, fp32 D, fp16 A (M-major: bit 15) and B (K-major), N, M = 128
   constexpr uint32_t idesc = (1u << 4) | (1u << 15) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
@@ -1209,6 +1243,7 @@ __global__ void __launch_bounds__(kFoldThreads, kFoldCtasPerSm)
 // there is one at all; without, the launch returns at once.  Grid-stride
 // over the outputs; threads of other outputs skip them.
 __global__ void __launch_bounds__(256) ozaki_special_kernel(OzakiFoldParams P, const int* __restrict__ any) {
+  pdl_wait();
   if ((any[0] | any[1]) == 0) return;
   const int64_t total = P.m * P.n;
   for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < total; x += (int64_t)gridDim.x * blockDim.x) {
@@ -1448,7 +1483,7 @@ struct SplitSideScales {
 static cudaError_t launch_crt_split(const CrtSplitTable& stab, cudaStream_t st, int64_t rows, int64_t cols,
                                     int64_t rows_pad, int64_t cols_pad, int64_t plane, const q128* p, int64_t sr,
                                     int64_t sc, const int* S, uint16_t* D, int* err,
-                                    const SplitSideScales* side = nullptr) {
+                                    const SplitSideScales* side = nullptr, bool pdl = false) {
   CrtSplitParams P;
   P.rows = rows;
   P.cols = cols;
@@ -1475,16 +1510,14 @@ static cudaError_t launch_crt_split(const CrtSplitTable& stab, cudaStream_t st, 
   const unsigned grid = (unsigned)std::min<int64_t>(ntiles, kSplitCtasPerSm * (int64_t)device_sm_count());
   const int threads = with_side ? kSplitSideThreads : kSplitThreads;
   if (stab.NB == 18)
-    ozaki_crt_split_tc_kernel<18><<<grid, threads, kSplitSmem, st>>>(P, stab);
-  else
-    ozaki_crt_split_tc_kernel<24><<<grid, threads, kSplitSmem, st>>>(P, stab);
-  return cudaGetLastError();
+    return launch_maybe_pdl(pdl, ozaki_crt_split_tc_kernel<18>, dim3(grid), dim3(threads), kSplitSmem, st, P, stab);
+  return launch_maybe_pdl(pdl, ozaki_crt_split_tc_kernel<24>, dim3(grid), dim3(threads), kSplitSmem, st, P, stab);
 }
 
 // The reconstruction of rows [0, F.m) of F (its Y already offset to the
 // band's first row; y_rows rows of each plane remain from there).
 static cudaError_t launch_crt_fold(const CrtFoldTable& ft, cudaStream_t st, const OzakiFoldParams& F,
-                                   int64_t y_rows) {
+                                   int64_t y_rows, bool pdl = false) {
   const int64_t tiles = ((F.m + 3) / 4) * ((F.n + 31) / 32);
   if (tiles <= 0) return cudaSuccess;
   if (tiles > INT32_MAX || ft.N != crt_fold_n(ft.nw)) return cudaErrorInvalidValue;
@@ -1506,23 +1539,15 @@ static cudaError_t launch_crt_fold(const CrtFoldTable& ft, cudaStream_t st, cons
   }
   const unsigned grid = (unsigned)std::min<int64_t>(tiles, kFoldCtasPerSm * (int64_t)device_sm_count());
   const bool grouped = F.gtiles != nullptr;
-  if (ft.nw <= 8) {
-    if (grouped)
-      ozaki_crt_fold_tc_kernel<8, true><<<grid, kFoldThreads, kFoldSmem, st>>>(F, ft);
-    else
-      ozaki_crt_fold_tc_kernel<8, false><<<grid, kFoldThreads, kFoldSmem, st>>>(F, ft);
-  } else if (ft.nw <= 10) {
-    if (grouped)
-      ozaki_crt_fold_tc_kernel<10, true><<<grid, kFoldThreads, kFoldSmem, st>>>(F, ft);
-    else
-      ozaki_crt_fold_tc_kernel<10, false><<<grid, kFoldThreads, kFoldSmem, st>>>(F, ft);
-  } else {
-    if (grouped)
-      ozaki_crt_fold_tc_kernel<12, true><<<grid, kFoldThreads, kFoldSmem, st>>>(F, ft);
-    else
-      ozaki_crt_fold_tc_kernel<12, false><<<grid, kFoldThreads, kFoldSmem, st>>>(F, ft);
-  }
-  return cudaGetLastError();
+  const dim3 g(grid), blk(kFoldThreads);
+  if (ft.nw <= 8)
+    return grouped ? launch_maybe_pdl(pdl, ozaki_crt_fold_tc_kernel<8, true>, g, blk, kFoldSmem, st, F, ft)
+                   : launch_maybe_pdl(pdl, ozaki_crt_fold_tc_kernel<8, false>, g, blk, kFoldSmem, st, F, ft);
+  if (ft.nw <= 10)
+    return grouped ? launch_maybe_pdl(pdl, ozaki_crt_fold_tc_kernel<10, true>, g, blk, kFoldSmem, st, F, ft)
+                   : launch_maybe_pdl(pdl, ozaki_crt_fold_tc_kernel<10, false>, g, blk, kFoldSmem, st, F, ft);
+  return grouped ? launch_maybe_pdl(pdl, ozaki_crt_fold_tc_kernel<12, true>, g, blk, kFoldSmem, st, F, ft)
+                 : launch_maybe_pdl(pdl, ozaki_crt_fold_tc_kernel<12, false>, g, blk, kFoldSmem, st, F, ft);
 }
 
 // Test hook of quadblas_debug_stall_next_call: set, the next Ozaki qgemm's
@@ -1627,13 +1652,17 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scr
   // a warp streams whole rows of op(A) at about twice the rate a split CTA
   // consumes op(B), so the side job ends within the split while m <= 2 n
   const bool a_side = crt && !ov && g.sal == 1 && g.m <= 2 * g.n;
+  // on one stream the residue scheme's kernels after the first are launched
+  // as programmatic dependents (each waits for the one before it in its
+  // pdl_wait; their launches overlap the tail of the kernel before)
+  const bool pdl = crt && !ov;
   {
-    launch_scale(g.n, g.k, g.B, g.sbj, g.sbl, F, fb, err + 4, sms, sb);
+    if ((e = launch_scale(g.n, g.k, g.B, g.sbj, g.sbl, F, fb, err + 4, sms, sb, pdl)) != cudaSuccess) return e;
     dim3 gb((unsigned)(L.k_pad / 64), (unsigned)(L.n_pad / 8));
     const SplitSideScales side = {g.A, g.m, g.k, g.sai, S, fa, err + 5};
     if (crt)
       e = launch_crt_split(stab, sb, g.n, g.k, L.n_pad, L.k_pad, plane_b, g.B, g.sbj, g.sbl, F, DB, err + 1,
-                           a_side ? &side : nullptr);
+                           a_side ? &side : nullptr, pdl);
     else
       launch_split(L.b, gb, blk, sb, g.n, g.k, L.n_pad, L.k_pad, plane_b, g.B, g.sbj, g.sbl, F, L.s, DB);
     if (e != cudaSuccess || (e = cudaGetLastError()) != cudaSuccess) return e;
@@ -1651,13 +1680,16 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scr
     if (ov && r0 == 0 &&
         ((ee = cudaMemsetAsync(err + 2, 0, 4, sa)) != cudaSuccess || (ee = cudaMemsetAsync(err + 5, 0, 4, sa)) != cudaSuccess))
       return ee;
-    if (!a_side) launch_scale(rows, g.k, g.A + r0 * g.sai, g.sai, g.sal, S + r0, fa + r0, err + 5, sms, sa);
+    if (!a_side &&
+        (ee = launch_scale(rows, g.k, g.A + r0 * g.sai, g.sai, g.sal, S + r0, fa + r0, err + 5, sms, sa, pdl)) !=
+            cudaSuccess)
+      return ee;
     dim3 ga((unsigned)(L.k_pad / 64), (unsigned)((r1 - r0) / 8));
     const q128* Ab = g.A + r0 * g.sai;
     ee = cudaSuccess;
     if (crt)
       ee = launch_crt_split(stab, sa, rows, g.k, r1 - r0, L.k_pad, plane_a, Ab, g.sai, g.sal, S + r0,
-                            DA + r0 * L.k_pad, err + 2);
+                            DA + r0 * L.k_pad, err + 2, nullptr, pdl);
     else
       launch_split(L.b, ga, blk, sa, rows, g.k, r1 - r0, L.k_pad, plane_a, Ab, g.sai, g.sal, S + r0, L.s,
                    DA + r0 * L.k_pad);
@@ -1752,13 +1784,15 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scr
                                                        L.m_pad * L.n_pad, tab.n, L.npass, tab);
         if ((ee = cudaGetLastError()) != cudaSuccess) return ee;
       }
-      if ((ee = launch_crt_fold(ftab, st, Fb, L.m_pad - i0)) != cudaSuccess) return ee;
+      if ((ee = launch_crt_fold(ftab, st, Fb, L.m_pad - i0, pdl && L.npass == 1)) != cudaSuccess) return ee;
     } else {
       launch_fold(L.b, st, Fb);
     }
     if ((ee = cudaGetLastError()) != cudaSuccess) return ee;
     const unsigned sgrid = (unsigned)std::max<int64_t>(1, std::min<int64_t>((Fb.m * g.n + 255) / 256, (int64_t)sms * 2));
-    ozaki_special_kernel<<<sgrid, 256, 0, st>>>(Fb, err + 4);
+    if ((ee = launch_maybe_pdl(pdl, ozaki_special_kernel, dim3(sgrid), dim3(256), 0, st, Fb,
+                               (const int*)(err + 4))) != cudaSuccess)
+      return ee;
     if ((ee = cudaGetLastError()) != cudaSuccess) return ee;
     if (fold_banded && ov->band_done(ov->band_ctx, i0, i1) != 0) return cudaErrorUnknown;
     return cudaSuccess;
@@ -1811,16 +1845,20 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scr
         cfg.blockDim = dim3(kMmaThreads);
         cfg.dynamicSmemBytes = kMmaSmem;
         cfg.stream = st;
-        cudaLaunchAttribute at[1];
+        cudaLaunchAttribute at[2];
         at[0].id = cudaLaunchAttributeClusterDimension;
         at[0].val.clusterDim.x = 2;
         at[0].val.clusterDim.y = 1;
         at[0].val.clusterDim.z = 1;
+        at[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        at[1].val.programmaticStreamSerializationAllowed = 1;
         cfg.attrs = at;
-        cfg.numAttrs = 1;
+        cfg.numAttrs = pdl ? 2 : 1;
         if ((e = cudaLaunchKernelEx(&cfg, ozaki_mma_kernel, tmA, tmB, tmBh, P)) != cudaSuccess) return e;
       } else {
-        ozaki_mma_kernel<<<(unsigned)std::min(units, sms), kMmaThreads, kMmaSmem, st>>>(tmA, tmB, tmBh, P);
+        if ((e = launch_maybe_pdl(pdl, ozaki_mma_kernel, dim3((unsigned)std::min(units, sms)), dim3(kMmaThreads),
+                                  kMmaSmem, st, tmA, tmB, tmBh, P)) != cudaSuccess)
+          return e;
       }
       if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }

@@ -38,6 +38,16 @@ __device__ __forceinline__ uint64_t f32x2_add(uint64_t a, uint64_t b) {
   return d;
 }
 
+// Programmatic dependent launch.  pdl_wait: every grid this one was
+// launched to depend on has completed and its writes are visible (a no-op
+// for a grid launched without the dependency); call it before the first
+// global memory access.  pdl_trigger: the next grid in the stream may start
+// launching (its CTAs wait in their own pdl_wait); call it after this CTA's
+// tensor memory is allocated, so that a later grid never holds tensor
+// memory this one still needs.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 // 16-byte asynchronous copy global -> shared (L2 only); src_bytes 0 writes
 // zeros without reading.  The copies of a thread are grouped by commit and
 // waited for by group (at most N newer groups left in flight).
