@@ -247,7 +247,10 @@ int quadblas_get_ozaki_scheme(void);
  * enabled, each call records CUDA events on its stream; read returns the
  * summed times in ms since the last read — out4[0] scaling and digit split,
  * out4[1] digit products on the tensor cores, out4[2] fold and epilogue —
- * and out4[3] the tensor flops of those calls (2*m*n*k*pairs). */
+ * and out4[3] the tensor flops of those calls (2*m*n*k*pairs).  on = 1
+ * records every phase; on = 2 only the two events around the tensor-core
+ * products (out4[0] and out4[2] stay 0), so that the kernels before and
+ * after them, and consecutive calls, still overlap their launches. */
 int quadblas_profile_enable(int on);
 int quadblas_profile_read(double *out4, int *calls);
 /* Frees the staging buffers that host-pointer calls keep on the current

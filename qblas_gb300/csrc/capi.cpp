@@ -975,7 +975,7 @@ QBLAS_EXPORT int quadblas_set_ozaki_scheme(int scheme) {
 }
 QBLAS_EXPORT int quadblas_get_ozaki_scheme(void) { return g_ozaki_scheme.load(); }
 QBLAS_EXPORT int quadblas_profile_enable(int on) {
-  qb::ozaki_profile_enable(on != 0);
+  qb::ozaki_profile_enable(on == 2 ? 2 : (on != 0 ? 1 : 0));
   return qb::kOk;
 }
 QBLAS_EXPORT int quadblas_profile_read(double* out4, int* calls) {

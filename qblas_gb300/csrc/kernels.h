@@ -170,7 +170,7 @@ bool batch_gemm_routed(int64_t m, int64_t n, int64_t k);
 void ozaki_debug_stall_next();
 void ozgemv_debug_stall_next();
 // Phase timing of Ozaki calls with CUDA events (off by default).
-void ozaki_profile_enable(bool on);
+void ozaki_profile_enable(int mode);  // 0 off, 1 every phase, 2 the products only
 int ozaki_profile_read(double* out4, int* calls);
 
 // Multiprocessor count of the current device (cached).

@@ -199,6 +199,8 @@ static cudaError_t launch_scale(int64_t rows, int64_t cols, const q128* p, int64
 // rows, F, fb for n, and err[0], [1], [2], [4], [5] zeroed.
 __global__ void ozaki_init_kernel(int64_t m, int* __restrict__ S, uint32_t* __restrict__ fa, int64_t n,
                                   int* __restrict__ F, uint32_t* __restrict__ fb, int* __restrict__ err) {
+  pdl_wait();
+  pdl_trigger();
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < m) {
     S[i] = kOzakiScaleEmpty;
@@ -1244,6 +1246,7 @@ __global__ void __launch_bounds__(kFoldThreads, kFoldCtasPerSm)
 // over the outputs; threads of other outputs skip them.
 __global__ void __launch_bounds__(256) ozaki_special_kernel(OzakiFoldParams P, const int* __restrict__ any) {
   pdl_wait();
+  pdl_trigger();
   if ((any[0] | any[1]) == 0) return;
   const int64_t total = P.m * P.n;
   for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < total; x += (int64_t)gridDim.x * blockDim.x) {
@@ -1383,22 +1386,23 @@ namespace {
 struct PhaseEvents {
   cudaEvent_t ev[4];  // start, after split, after digit products, after fold
   int64_t mma_flop_units;  // 2*m*n*k*pairs / 2^20, for the tensor roofline
+  bool full;               // all four recorded (else only the products' two)
 };
 std::mutex g_prof_mu;
-bool g_prof_on = false;
+int g_prof_mode = 0;  // 0 off, 1 every phase, 2 the tensor-core products only
 std::vector<PhaseEvents> g_prof_pending;
 double g_prof_sum[3] = {0, 0, 0};
 double g_prof_flop = 0;
 int g_prof_calls = 0;
 
 void prof_record(PhaseEvents* pe, int i, cudaStream_t st) {
-  if (pe) cudaEventRecord(pe->ev[i], st);
+  if (pe && (pe->full || i == 1 || i == 2)) cudaEventRecord(pe->ev[i], st);
 }
 }  // namespace
 
-void ozaki_profile_enable(bool on) {
+void ozaki_profile_enable(int mode) {
   std::lock_guard<std::mutex> l(g_prof_mu);
-  g_prof_on = on;
+  g_prof_mode = mode;
 }
 
 // Sums of the phase times (ms) of the calls recorded since the last read:
@@ -1407,11 +1411,11 @@ void ozaki_profile_enable(bool on) {
 int ozaki_profile_read(double* out, int* calls) {
   std::lock_guard<std::mutex> l(g_prof_mu);
   for (PhaseEvents& pe : g_prof_pending) {
-    cudaEventSynchronize(pe.ev[3]);
+    cudaEventSynchronize(pe.ev[pe.full ? 3 : 2]);
     float a = 0, b = 0, c = 0;
-    cudaEventElapsedTime(&a, pe.ev[0], pe.ev[1]);
+    if (pe.full) cudaEventElapsedTime(&a, pe.ev[0], pe.ev[1]);
     cudaEventElapsedTime(&b, pe.ev[1], pe.ev[2]);
-    cudaEventElapsedTime(&c, pe.ev[2], pe.ev[3]);
+    if (pe.full) cudaEventElapsedTime(&c, pe.ev[2], pe.ev[3]);
     g_prof_sum[0] += a;
     g_prof_sum[1] += b;
     g_prof_sum[2] += c;
@@ -1615,10 +1619,11 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scr
   PhaseEvents* pe = nullptr;
   {
     std::lock_guard<std::mutex> l(g_prof_mu);
-    if (g_prof_on) {
+    if (g_prof_mode) {
       bool okev = true;
       for (int i = 0; i < 4; ++i) okev = okev && cudaEventCreate(&pev.ev[i]) == cudaSuccess;
       if (okev) pe = &pev;
+      pev.full = g_prof_mode == 1;
       int64_t pairs = crt ? (int64_t)tab.n : (int64_t)L.s * (L.s + 1) / 2;
       pev.mma_flop_units = (int64_t)((2.0 * g.m * g.n * g.k * pairs) / 1048576.0);
     }
@@ -1636,8 +1641,12 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scr
   // On one stream one kernel sets the scales' starting values and resets
   // them; with a caller's streams each is reset on the stream of its writer.
   if (!ov) {
+    // a programmatic dependent of whatever kernel came before in the stream:
+    // it waits for it before its first write
     const int64_t mn = std::max<int64_t>(g.m, g.n);
-    ozaki_init_kernel<<<(unsigned)((mn + 255) / 256), 256, 0, st>>>(g.m, S, fa, g.n, F, fb, err);
+    if ((e = launch_maybe_pdl(crt, ozaki_init_kernel, dim3((unsigned)((mn + 255) / 256)), dim3(256), 0, st, g.m, S,
+                              fa, g.n, F, fb, err)) != cudaSuccess)
+      return e;
   } else {
     ozaki_fill_kernel<<<(unsigned)((g.m + 255) / 256), 256, 0, sa>>>(g.m, S, fa);
     ozaki_fill_kernel<<<(unsigned)((g.n + 255) / 256), 256, 0, sb>>>(g.n, F, fb);

@@ -232,3 +232,34 @@ def test_crt_default_scheme_and_c_interface(qlib, O, sq):
         api.set_method(0)
     sums = E.crt_gemm_sum(sq, m, n, k, A, k, 1, B, n, 1, 16 * 9 - 1)
     assert Q.same_bits(got, epilogue(O, Q.scalar(2.0), sums, Q.scalar(0.5), C)).all()
+
+
+@pytest.mark.parametrize("mode", [1, 2])
+def test_profile_modes(crt, torch_cuda, mode):
+    """quadblas_profile_enable: mode 1 times every phase of a device-pointer
+    call, mode 2 only the tensor-core products (the other phases read 0)."""
+    import ctypes
+    from qblas_gb300._lib import load
+    torch = torch_cuda
+    lib = load()
+    m = n = k = 256
+    rng = G.rng_for(77)
+    A, B = G.spread_uniform(rng, m * k), G.spread_uniform(rng, k * n)
+    dA, dB, dC = to_dev(torch, A), to_dev(torch, B), to_dev(torch, Q.from_double(np.zeros(m * n)))
+    out, calls = (ctypes.c_double * 4)(), ctypes.c_int(0)
+    lib.quadblas_profile_read(out, ctypes.byref(calls))  # drop anything recorded before
+    lib.quadblas_profile_enable(mode)
+    try:
+        for _ in range(3):
+            api.gemm_dev("R", "N", "N", m, n, k, Q.scalar(1.0), dA, k, dB, n, Q.scalar(0.0), dC, n)
+        torch.cuda.synchronize()
+    finally:
+        lib.quadblas_profile_enable(0)
+    assert lib.quadblas_profile_read(out, ctypes.byref(calls)) == 0
+    assert calls.value == 3
+    products = out[3] / (3 * 2.0 * m * n * k)  # residue products per call (one per modulus)
+    assert out[1] > 0 and 20 <= round(products) <= 48 and abs(products - round(products)) < 1e-3
+    if mode == 1:
+        assert out[0] > 0 and out[2] > 0
+    else:
+        assert out[0] == 0 and out[2] == 0
