@@ -263,3 +263,30 @@ def test_profile_modes(crt, torch_cuda, mode):
         assert out[0] > 0 and out[2] > 0
     else:
         assert out[0] == 0 and out[2] == 0
+
+
+@pytest.mark.parametrize("k", [4096, 7600])
+@pytest.mark.parametrize("sign", [1, -1])
+def test_crt_largest_sums(crt, torch_cuda, k, sign):
+    """Every operand 1 - 2^-113 and every product of one sign, T = 134: the
+    largest sum the truncated operands allow, at 0.265 M (k = 4096) and
+    0.4917 M (k = 7600, 32 moduli still) against the 32/65 M the
+    reconstruction's quotient estimate is proved for; every output is the
+    correctly rounded k (1 - 2^-113)^2."""
+    from fractions import Fraction
+    from test_oracle import fraction_to_q
+    torch = torch_cuda
+    m, n = 130, 70
+    top = np.array([0xFFFFFFFFFFFFFFFF, 0x3FFEFFFFFFFFFFFF], dtype=np.uint64)
+    A = np.tile(top, (m * k, 1))
+    B = np.tile(top, (k * n, 1))
+    if sign < 0:
+        B[:, 1] |= np.uint64(1 << 63)
+    dA, dB, dC = to_dev(torch, A), to_dev(torch, B), to_dev(torch, Q.from_double(np.zeros(m * n)))
+    api.set_ozaki_slices(15)
+    api.set_ozaki_digit_bits(9)
+    api.gemm_dev("R", "N", "N", m, n, k, Q.scalar(1.0), dA, k, dB, n, Q.scalar(0.0), dC, n)
+    torch.cuda.synchronize()
+    got = to_host(dC)
+    want = fraction_to_q(sign * k * (1 - Fraction(1, 1 << 113)) ** 2)
+    assert (got[:, 0] == np.uint64(want[0])).all() and (got[:, 1] == np.uint64(want[1])).all()

@@ -408,3 +408,24 @@ def test_reconstruct_rounding_edges(sq):
     sq.sq_crt_reconstruct(ctypes.c_int64(len(keep)), P(C), P(e), ctypes.c_int(T), ctypes.c_int64(k), P(out))
     for i, (x, ee) in enumerate(keep):
         assert (int(out[i, 0]), int(out[i, 1])) == fraction_to_q(Fraction(x) * Fraction(2) ** ee), (i, x, ee)
+
+
+@pytest.mark.parametrize("k", [4096, 7600])
+@pytest.mark.parametrize("sign", [1, -1])
+def test_crt_gemm_largest_sums(sq, k, sign):
+    """Every operand 1 - 2^-113 (significand all ones) and every product of
+    one sign: X = k (2^134 - 2^21)^2, the largest sum T = 134 bits allow.
+    For k = 7600 the 32 moduli still cover it and |X| = 0.4917 M, next to the
+    32/65 M the quotient estimate is proved for (k = 4096: 0.265 M)."""
+    import ozaki_emul as E
+    T, m, n = 134, 2, 3
+    n_mod, _, _, _, _ = table(sq, T, k)
+    assert n_mod == 32
+    top = np.array([0xFFFFFFFFFFFFFFFF, 0x3FFEFFFFFFFFFFFF], dtype=np.uint64)  # 1 - 2^-113
+    A = np.tile(top, (m * k, 1))
+    B = np.tile(top, (k * n, 1))
+    if sign < 0:
+        B[:, 1] |= np.uint64(1 << 63)
+    got = E.crt_gemm_sum(sq, m, n, k, A, k, 1, B, n, 1, T)
+    want = fraction_to_q(sign * k * (1 - Fraction(1, 1 << 113)) ** 2)
+    assert all((int(g[0]), int(g[1])) == want for g in got)
