@@ -120,7 +120,7 @@ inline uint32_t crt_inverse(uint32_t a, uint32_t p) {  // a^-1 mod p, gcd(a, p) 
 // The moduli product M must exceed (65/32) k 2^(2T) for operands of T bits
 // and inner dimension k.  Then |X| < k 2^(2T) < (32/65) M, and Q is the
 // integer nearest to Y / M = Q + X / M.  Its estimate S 2^-24, S = sum_q y_q
-// P24_q with |P24_q - 2^24 / p_q| <= 1/2 and y_q < 512, is off by at most
+// P24_q with |P24_q - 2^24 / p_q| <= 1/2 and y_q <= 512, is off by at most
 // n 2^-16 <= 48 2^-16 < 7.4e-4 from Y / M; |X / M| + 7.4e-4 < 32/65 + 7.4e-4
 // < 1/2, so rounding S 2^-24 gives Q.
 //
