@@ -322,11 +322,16 @@ __global__ void __launch_bounds__(kOgThreads, 1)
     const uint32_t off0 = og_elem_offset<kLayout>(r, 2 * grp), off1 = og_elem_offset<kLayout>(r, 2 * grp + 1);
     const uint32_t tlane = tmem + ((uint32_t)(qd * 32) << 16) + kOgAccCols + 2 * grp;
     uint32_t q = 0, it = 0;
+    // a chunk's k-steps q .. q + 3 (q a multiple of 4) fill slots s0 .. s0 + 3,
+    // s0 = q % kOgSlots, with parity fp = (q / kOgSlots) & 1: kept by counting
+    static_assert(kOgSlots % kOgKSteps == 0, "a chunk's k-steps never wrap the slot ring");
+    int s0 = 0;
+    uint32_t fp = 0;
     for (int64_t w = w0; w < w1 && ok; ++w, ++it) {
       // all k-steps of the chunk are needed for its row exponents
       bool got = true;
 #pragma unroll
-      for (int ks = 0; ks < kOgKSteps; ++ks) got = got && mbar_wait_ns(full_bar(slot_of(q + ks)), fill_parity(q + ks), P.wait_ns);
+      for (int ks = 0; ks < kOgKSteps; ++ks) got = got && mbar_wait_ns(full_bar(s0 + ks), fp, P.wait_ns);
       if (!got) {
         ok = false;
         break;
@@ -339,7 +344,7 @@ __global__ void __launch_bounds__(kOgThreads, 1)
       uint32_t mx = 0;
 #pragma unroll
       for (int ks = 0; ks < kOgKSteps; ++ks) {
-        const uint32_t slot = base + slot_of(q + ks) * kOgSlotBytes;
+        const uint32_t slot = base + (s0 + ks) * kOgSlotBytes;
         mx = max(mx, max(ld_shared_u32(slot + off0 + 12) << 1, ld_shared_u32(slot + off1 + 12) << 1));
       }
       uint32_t* em = emax + (it & 1) * 4 * kOgRows;
@@ -356,10 +361,10 @@ __global__ void __launch_bounds__(kOgThreads, 1)
       const uint32_t sp = bmax == 0x7FFFu ? 1u : 0u;
 #pragma unroll 1
       for (int ks = 0; ks < kOgKSteps; ++ks, ++q) {
-        const uint32_t slot = base + slot_of(q) * kOgSlotBytes;
+        const uint32_t slot = base + (s0 + ks) * kOgSlotBytes;
         const uint4 v0 = ld_shared_v4(slot + off0), v1 = ld_shared_v4(slot + off1);
         __syncwarp();
-        if (lane == 0) mbar_arrive(empty_bar(slot_of(q)));  // this k-step's elements are in registers
+        if (lane == 0) mbar_arrive(empty_bar(s0 + ks));  // this k-step's elements are in registers
         uint32_t W[2][5], sg[2], bs[2];
         const int sh0 = og_shift(E, v0.w), sh1 = og_shift(E, v1.w);
         // the four-word level of the shift only when a lane of the warp needs it
@@ -388,6 +393,11 @@ __global__ void __launch_bounds__(kOgThreads, 1)
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
         __syncwarp();
         if (lane == 0) mbar_arrive(ready_bar(st));
+      }
+      s0 += kOgKSteps;
+      if (s0 == kOgSlots) {
+        s0 = 0;
+        fp ^= 1u;
       }
     }
     if (!ok && lane == 0) atomicExch(P.err, 1);
