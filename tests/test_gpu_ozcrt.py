@@ -36,9 +36,10 @@ def crt(qlib):
     api.set_ozaki_digit_bits(0)
 
 
-def run_case(O, sq, rng, layout, transa, transb, m, n, k, s, gen, al_d, be_d, b=9, torch=None):
+def run_case(O, sq, rng, layout, transa, transb, m, n, k, s, gen, al_d, be_d, b=9, torch=None, c_specials=False):
     """One call (host pointers, or device pointers when torch is given)
-    against the emulation of the same algorithm."""
+    against the emulation of the same algorithm; c_specials plants NaN,
+    +-inf and +-0 in C (what beta * C makes of them is the epilogue's)."""
     col = layout == "C"
     ta, tb = transa == "T", transb == "T"
     ar, ac = (k, m) if ta else (m, k)
@@ -49,6 +50,11 @@ def run_case(O, sq, rng, layout, transa, transb, m, n, k, s, gen, al_d, be_d, b=
     A = gen(rng, (ac if col else ar) * lda)
     B = gen(rng, (bc if col else br) * ldb)
     C = G.uniform_full(rng, (n if col else m) * ldc)
+    if c_specials:
+        specials = [[0, 0x7FFF800000000000], [0, 0x7FFF000000000000], [0, 0xFFFF000000000000],
+                    [0, 0x8000000000000000], [0, 0]]
+        for t, pos in enumerate(rng.choice(len(C), size=5 * 7, replace=False)):
+            C[pos] = specials[t % 5]
     alpha, beta = Q.scalar(al_d), Q.scalar(be_d)
     api.set_ozaki_slices(s)
     api.set_ozaki_digit_bits(b)
@@ -123,6 +129,20 @@ def test_crt_device_pointer_bit_exact(crt, O, sq, torch_cuda, layout, transa, tr
     rng = G.rng_for(431 + m)
     got, idx, exp = run_case(O, sq, rng, layout, transa, transb, m, n, k, 15, G.spread_uniform, 1.5, -0.75,
                              torch=torch_cuda)
+    assert Q.same_bits(got[idx], exp).all(), int((~Q.same_bits(got[idx], exp)).sum())
+
+
+@pytest.mark.parametrize("device", [False, True])
+@pytest.mark.parametrize("al_d,be_d", [(1.0, 0.0), (1.0, -0.0), (2.0, 0.0), (-1.0, -0.0)])
+def test_crt_beta_zero_with_special_c(crt, O, sq, request, device, al_d, be_d):
+    """beta = +-0 with NaN, +-inf and +-0 already in C: every output is
+    fma(alpha, sum, beta * C) as the reference epilogue forms it (NaN where
+    C held NaN or inf, the sign of a zero sum from beta * C), with the
+    epilogue's fast path for alpha = 1 and the product path otherwise."""
+    torch = request.getfixturevalue("torch_cuda") if device else None
+    rng = G.rng_for(451)
+    got, idx, exp = run_case(O, sq, rng, "R", "N", "N", 37, 45, 70, 15, G.spread_uniform, al_d, be_d,
+                             torch=torch, c_specials=True)
     assert Q.same_bits(got[idx], exp).all(), int((~Q.same_bits(got[idx], exp)).sum())
 
 
