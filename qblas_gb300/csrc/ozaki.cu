@@ -1657,10 +1657,14 @@ cudaError_t launch_gemm_ozaki(const GemmArgs& g, int digits, int bits, void* scr
   const dim3 blk(32, 8);
   const int64_t plane_a = L.m_pad * L.k_pad, plane_b = L.n_pad * L.k_pad;
   // on one stream with op(A)'s rows contiguous, op(A)'s scales are taken by
-  // a fifth warp of op(B)'s residue split instead of a launch of their own:
-  // a warp streams whole rows of op(A) at about twice the rate a split CTA
-  // consumes op(B), so the side job ends within the split while m <= 2 n
-  const bool a_side = crt && !ov && g.sal == 1 && g.m <= 2 * g.n;
+  // a fifth warp of op(B)'s residue split instead of a launch of their own,
+  // when that ends within the split: min(m, G) side warps (G CTAs in the
+  // split's grid) each stream whole rows of op(A), 16 k bytes a row, at about
+  // 3.4 GB/s, while the split moves about 80 n k bytes at about 5 TB/s, so
+  // the side job fits when 300 m <= n min(m, G) (for m >= G: m <= about 2 n)
+  const int64_t split_grid_b =
+      std::min<int64_t>((L.n_pad / 4) * (L.k_pad / 64), (int64_t)kSplitCtasPerSm * sms);
+  const bool a_side = crt && !ov && g.sal == 1 && 300 * g.m <= g.n * std::min<int64_t>(g.m, split_grid_b);
   // on one stream the residue scheme's kernels after the first are launched
   // as programmatic dependents (each waits for the one before it in its
   // pdl_wait; their launches overlap the tail of the kernel before)

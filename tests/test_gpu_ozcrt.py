@@ -120,12 +120,15 @@ def test_crt_mixed_magnitudes(crt, O, sq):
 
 @pytest.mark.parametrize("layout,transa,transb,m,n,k", [("R", "N", "N", 70, 90, 300), ("R", "T", "N", 65, 33, 129),
                                                      ("C", "N", "T", 129, 70, 65), ("C", "T", "T", 33, 290, 129),
-                                                     ("R", "N", "T", 300, 257, 1000), ("R", "N", "N", 600, 130, 200)])
+                                                     ("R", "N", "T", 300, 257, 1000), ("R", "N", "N", 600, 130, 200),
+                                                     ("R", "N", "N", 320, 400, 150), ("C", "T", "T", 300, 400, 90)])
 def test_crt_device_pointer_bit_exact(crt, O, sq, torch_cuda, layout, transa, transb, m, n, k):
     """Device-pointer calls on one stream: op(A)'s scales come from the side
-    warp of op(B)'s residue split where op(A)'s rows are contiguous and
-    m <= 2n (R/N, C/T, R/N/T), from their own launch otherwise (transposed
-    layouts, and 600 > 2 * 130); bit-exact against the emulation either way."""
+    warp of op(B)'s residue split where op(A)'s rows are contiguous and the
+    side job ends within the split (300 m <= n min(m, split grid): the
+    320 x 400 x 150 and 300 x 400 x 90 cases, and 300 x 257 x 1000), from
+    their own launch otherwise (transposed layouts, small n, 600 > 2 * 130);
+    bit-exact against the emulation either way."""
     rng = G.rng_for(431 + m)
     got, idx, exp = run_case(O, sq, rng, layout, transa, transb, m, n, k, 15, G.spread_uniform, 1.5, -0.75,
                              torch=torch_cuda)
@@ -207,12 +210,11 @@ def test_host_pointer_row_bands_match_device(crt, torch_cuda, scheme, shape, pin
     assert Q.same_bits(got, ref).all(), int((~Q.same_bits(got, ref)).sum())
 
 
-@pytest.mark.parametrize("device", [False, True])
-def test_crt_special_values(crt, O, device, request):
-    """Host pointers, and device pointers on one stream (there op(A)'s row
-    scales and flags come from the side warp of op(B)'s split)."""
+@pytest.mark.parametrize("device,m,n,k", [(False, 9, 11, 13), (True, 9, 11, 13), (True, 310, 320, 300)])
+def test_crt_special_values(crt, O, device, m, n, k, request):
+    """Host pointers, and device pointers on one stream (at 310 x 320 x 300
+    op(A)'s row scales and flags come from the side warp of op(B)'s split)."""
     rng = G.rng_for(422)
-    m, n, k = 9, 11, 13
     A, B = G.uniform_full(rng, m * k), G.uniform_full(rng, k * n)
     A[2 * k + 3] = [0, 0x7FFF800000000000]   # NaN in row 2
     A[5 * k + 1] = [0, 0x7FFF000000000000]   # +inf in row 5
@@ -227,13 +229,13 @@ def test_crt_special_values(crt, O, device, request):
     else:
         got = C.copy()
         api.gemm("R", "N", "N", m, n, k, Q.scalar(1.0), A, k, B, n, Q.scalar(0.0), got, n)
-    rows, cols = np.meshgrid(np.arange(m), np.arange(n), indexing="ij")
-    R, _, _ = O.exact_gemm(k, A, k, 1, B, n, 1, rows.ravel(), cols.ravel())
     special = np.zeros((m, n), bool)
     special[[2, 5], :] = True
     special[:, 7] = True
     sp = special.ravel()
-    assert Q.same_bits(got[sp], R[sp]).all()
+    rows, cols = np.nonzero(special)
+    R, _, _ = O.exact_gemm(k, A, k, 1, B, n, 1, rows, cols)
+    assert Q.same_bits(got[sp], R).all()
     assert Q.is_nan(got[~sp]).sum() == 0
 
 
